@@ -1,0 +1,406 @@
+#!/usr/bin/env python3
+"""Benchmark of the plain explicit heat sweep (the ScaFES update phase).
+
+Workload (the large heat configuration): 3D heat equation u_t = Laplace(u)
+on the unit cube, 512^3 nodes, FP64, 7-point stencil, homogeneous Dirichlet
+border, u0 = sin(pi x) sin(pi y) sin(pi z) plus seeded (seed 2) uniform
+noise in [-1e-3, 1e-3] at inner nodes, tau = 0.9 h^2/6.  One bench step is
+one solve: 1000 explicit Euler time steps (1000 sweep launches).  Synthetic
+data; every field (1 GiB) is larger than L2, so no L2 flush is needed.
+
+  value  : GLUP/s (nodes x time steps / s, all nodes counted) with the field
+           resident in HBM, CUDA events on the launching stream
+  e2e    : same metric through the C ABI with host buffers: upload (pinned
+           host -> device), 1000 steps, download (device -> pinned host)
+  roofline / cpu_baseline / clocks / variants: see the keys' comments.
+
+``--impl reference`` times the reference's CPU path (the C restatement of
+the reference's update in oracle/, all host threads) on a bounded sample of
+the same workload and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "GLUP/s and % HBM roofline, plain vs batched vs adjoint on 1 GB300, at stated error"
+UNIT = "GLUP/s"
+B_PER_LUP = {"f64": 16, "f32x2": 16, "f32": 8}   # algorithmic bytes per node update
+FP64_OPS_PER_LUP = 7                               # DMUL + 3 DADD + 3 DFMA
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--time-steps", type=int, default=1000)
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---- process group (replicas only: no data-path collective) ---------------
+
+class Dist:
+    def __init__(self, backend: str):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        dev = "cuda" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---- inputs -----------------------------------------------------------------
+
+def workload(n: int):
+    h = 1.0 / (n - 1)
+    tau = 0.9 * h * h / 6.0
+    return h, tau
+
+
+def make_u0(n: int, out: np.ndarray, seed: int = 2) -> np.ndarray:
+    """Sine mode + seeded noise at inner nodes, border 0, written into out
+    (shape (n, n, n), x fastest)."""
+    h, _ = workload(n)
+    s = np.sin(np.pi * h * np.arange(n))
+    rng = np.random.default_rng(seed)
+    inner = np.zeros(n, dtype=bool)
+    inner[1:-1] = True
+    for k in range(n):
+        plane = s[k] * (s[:, None] * s[None, :])
+        plane = plane + rng.uniform(-1e-3, 1e-3, (n, n))
+        if inner[k]:
+            plane[0, :] = plane[-1, :] = 0.0
+            plane[:, 0] = plane[:, -1] = 0.0
+        else:
+            plane[:] = 0.0
+        out[k] = plane
+    return out
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def pipe_peaks():
+    """FP64 and FP32 FMA issue rates of this GPU (G op/s), measured live by
+    scafes_probe_pipe_rates (CUDA events)."""
+    import ctypes as C
+
+    import masterthesis_gb300 as M
+    f64, f32 = C.c_double(), C.c_double()
+    if M.lib().scafes_probe_pipe_rates(C.byref(f64), C.byref(f32)) != 0:
+        return None, None
+    return f64.value, f32.value
+
+
+def ncu_traffic(kernel_key: str):
+    """Per-launch DRAM bytes (read + write) of one ncu capture, from the
+    committed profile summary of that kernel."""
+    for p in sorted((ROOT / "profiles").glob("*.md")):
+        txt = p.read_text()
+        m = re.search(rf"traffic_bytes_per_launch\[{re.escape(kernel_key)}\]:\s*([0-9.eE+]+)", txt)
+        if m:
+            return float(m.group(1))
+    return None
+
+
+# ---- GPU clock sampling during the timed region -----------------------------
+
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = [r for r in csv.reader(io.StringIO(out)) if len(r) >= 9]
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        load = [v for v in sm if v > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ---- CPU baseline (the oracle port of the reference's update) ---------------
+
+def cpu_sample_glups(n: int, target_s: float, max_sweeps: int = 50):
+    """Times the reference's update (C restatement, all host threads) on the
+    512^3 workload for a bounded number of sweeps (~target_s seconds)."""
+    import oracle as O
+    _, tau = workload(n)
+    g = O.make_grid((n, n, n), tau=tau)
+    u0 = np.empty((n, n, n))
+    make_u0(n, u0)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    O.heat_dirichlet(g, u0, 1, nthreads=threads)
+    one = time.perf_counter() - t0
+    sweeps = int(max(1, min(max_sweeps, target_s / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    O.heat_dirichlet(g, u0, sweeps, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return n ** 3 * sweeps / dt / 1e9, threads, sweeps, dt
+
+
+# ---- GPU arm ----------------------------------------------------------------
+
+def run_ours(args, dist: Dist):
+    import torch
+
+    import masterthesis_gb300 as M
+    from masterthesis_gb300 import build as B
+
+    B.build_library()
+    torch.cuda.set_device(dist.local_rank)
+    n, T = args.n, args.time_steps
+    _, tau = workload(n)
+    nn = n ** 3
+    host_u0 = torch.empty((n, n, n), dtype=torch.float64, pin_memory=True)
+    host_out = torch.empty((n, n, n), dtype=torch.float64, pin_memory=True)
+    u0 = host_u0.numpy()
+    make_u0(n, u0)
+    out = host_out.numpy()
+    stream = torch.cuda.Stream()
+
+    def device_timed(prec: str, steps: int, warmup: int, clocks: Clocks | None):
+        cfg = M.make_cfg((n, n, n), tau=tau, precision=prec, heat=(1.0, 1.0, 0.0),
+                         stream=stream.cuda_stream)
+        with M.Plain(cfg) as p:
+            p.upload(M.FIELD_U, u0)
+            for _ in range(warmup):
+                p.step(T)
+            stream.synchronize()
+            dist.barrier()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            if clocks:
+                clocks.start()
+            e0.record(stream)
+            launches = 0
+            for _ in range(steps):
+                p.step(T)
+                launches += p.last_step_launches()
+            e1.record(stream)
+            e1.synchronize()
+            clk = clocks.stop() if clocks else None
+            torch.cuda.synchronize()
+            dist.barrier()
+            dt = dist.max(e0.elapsed_time(e1) / 1e3)
+        return dt, launches, clk
+
+    # Headline: FP64 storage and arithmetic.
+    dt, launches, clk = device_timed("f64", args.steps, args.warmup, Clocks(dist.local_rank))
+    value = dist.world * nn * T * args.steps / dt / 1e9
+    launch_s = dt / (args.steps * T)
+    hbm_peak, peak_src = measured_peaks()
+    achieved_gbs = B_PER_LUP["f64"] * nn / launch_s / 1e9
+    traffic = ncu_traffic("star7_sweep<PolF64>")
+    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved_gbs / hbm_peak, "traffic": traffic,
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "kernel": "star7_sweep<PolF64>", "bytes_per_launch_alg": B_PER_LUP["f64"] * nn,
+                "launch_ms": launch_s * 1e3}
+    fp64_peak, fp32_peak = pipe_peaks()
+    if fp64_peak:
+        ach = FP64_OPS_PER_LUP * nn / launch_s / 1e9
+        roofline["fp64_pipe"] = {"achieved_gops": ach, "peak_gops": fp64_peak, "frac": ach / fp64_peak,
+                                 "ops_per_lup": FP64_OPS_PER_LUP, "fp32_fma_gops": fp32_peak,
+                                 "peak_source": "measured live (scafes_probe_pipe_rates)",
+                                 "note": "the FP64 issue rate, not HBM, binds this kernel on GB300"}
+
+    # e2e through the C ABI with host buffers.
+    cfg = M.make_cfg((n, n, n), tau=tau, precision="f64", heat=(1.0, 1.0, 0.0), stream=stream.cuda_stream)
+    e2e_times = []
+    with M.Plain(cfg) as p:
+        for it in range(1 + args.steps):
+            dist.barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            p.upload(M.FIELD_U, u0)
+            p.step(T)
+            p.download(M.FIELD_U, out)
+            t1 = time.perf_counter()
+            if it > 0:
+                e2e_times.append(t1 - t0)
+    e2e_dt = dist.max(sum(e2e_times))
+    e2e = {"value": dist.world * nn * T * len(e2e_times) / e2e_dt / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": nn * 8, "d2h_bytes_per_step": nn * 8,
+           "ms_per_step": e2e_dt / len(e2e_times) * 1e3,
+           "path": "scafes_gpu_upload + scafes_gpu_step(1000) + scafes_gpu_download, pinned host buffers"}
+
+    variants = {}
+    if not args.no_variants:
+        finals = {}
+        for prec in ("f32x2", "f32"):
+            vdt, vl, _ = device_timed(prec, max(1, args.steps // 2), 1, None)
+            lps = vdt / (max(1, args.steps // 2) * T)
+            variants[prec] = {"value": dist.world * nn * T * max(1, args.steps // 2) / vdt / 1e9,
+                              "unit": UNIT, "hbm_frac": B_PER_LUP[prec] * nn / lps / 1e9 / hbm_peak,
+                              "bytes_per_lup": B_PER_LUP[prec], "launch_ms": lps * 1e3}
+        # Stated error: each variant against FP64 on the same inputs, one solve.
+        for prec in ("f64", "f32x2", "f32"):
+            cfg = M.make_cfg((n, n, n), tau=tau, precision=prec, heat=(1.0, 1.0, 0.0),
+                             stream=stream.cuda_stream)
+            with M.Plain(cfg) as p:
+                p.upload(M.FIELD_U, u0)
+                p.step(T)
+                finals[prec] = p.download()
+        ref = finals["f64"]
+        scale = float(np.max(np.abs(ref)))
+        for prec in ("f32x2", "f32"):
+            variants[prec]["rel_err_vs_f64"] = float(np.max(np.abs(finals[prec] - ref))) / scale
+
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"heat3d {n}^3 FP64 plain sweep, sine+noise(seed 2), Dirichlet 0, "
+                               f"tau=0.9h^2/6, {T} explicit Euler steps per bench step",
+                   "nodes": [n, n, n], "time_steps_per_step": T, "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs larger than L2 (1 GiB per field), no flush"},
+        "e2e": e2e, "roofline": roofline, "gpu_launches": launches,
+        "error": {"f64_vs_oracle": "<=1e-12 rel max-norm (tests, 64^3 x 200 and golden cases)",
+                  "note": "f64 is the reference's arithmetic with FMA contraction"},
+    }
+    if variants:
+        res["variants"] = variants
+    if clk:
+        res["clocks"] = clk
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        v, cores, sweeps, cdt = cpu_sample_glups(n, target_s=10.0)
+        res["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"{sweeps} sweeps of the {n}^3 workload ({cdt:.1f} s), "
+                                         f"C restatement of the reference update (oracle/), OpenMP"}
+    return res
+
+
+def run_reference(args, dist: Dist):
+    """The reference's CPU update (oracle port; the reference's own driver
+    is not built on this machine), all host threads, bounded sample."""
+    if dist.rank != 0:
+        return None
+    import oracle as O
+    O.build()
+    n = args.n
+    _, tau = workload(n)
+    g = O.make_grid((n, n, n), tau=tau)
+    u = np.empty((n, n, n))
+    make_u0(n, u)
+    threads = os.cpu_count() or 1
+    sweeps = 2
+    for _ in range(args.warmup):
+        O.heat_dirichlet(g, u, 1, nthreads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        O.heat_dirichlet(g, u, sweeps, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    dt = sum(times)
+    value = n ** 3 * sweeps * args.steps / dt / 1e9
+    sample = (f"{sweeps} sweeps of the {n}^3 workload per step (the solve has {args.time_steps}); "
+              f"C restatement of the reference update (oracle/), OpenMP {threads} threads")
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": f"heat3d {n}^3 FP64 plain sweep, sine+noise(seed 2), Dirichlet 0, "
+                               f"tau=0.9h^2/6, {args.time_steps} explicit Euler steps per bench step",
+                   "nodes": [n, n, n], "time_steps_per_step": args.time_steps, "parallelism": "cpu"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        dist = Dist("gloo")
+        res = run_reference(args, dist)
+    else:
+        dist = Dist("nccl")
+        res = run_ours(args, dist)
+    if res is not None and dist.rank == 0:
+        print(json.dumps(res), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,173 @@
+/*
+ * scafes_gb300.h -- C ABI of the GB300-native explicit-stencil engine.
+ *
+ * This library replaces the per-node update sweep of ScaFES
+ * (src/ScaFES_Problem.hpp:5399-5476, evalTypeTwoAt), the known-field
+ * evaluation feeding it (:3434-3485), the pointer swap (:3273-3316) and the
+ * MPI ghost exchange (src/ScaFES_DataField.hpp:1912-1934) with hand-written
+ * sm_103a kernels on one GPU.  Its only counterpart in the reference is the
+ * never-called CUDA stub src/ScaFES_ProblemCuda.hpp:84-105
+ * (updateGlobalInnerUsingCudaVect) / src/ScaFES_ProblemCuda.cu:23-37; the
+ * functions below are what a ScaFES::Problem would bind in its place.
+ *
+ * Conventions
+ *  - Host arrays hold the nodes of the global grid in Fortran order
+ *    (x fastest): idx = i + nx*(j + ny*k), the order of
+ *    Grid::idxNodeTuple2ScalarStyleFortran (src/ScaFES_Grid.hpp:956-968),
+ *    without the ghost layer and the trailing time slot of a DataField.
+ *  - Every call returns SCAFES_OK (0) or a negative status; nothing exits,
+ *    aborts or throws across the ABI (the reference's stub calls exit(-1),
+ *    src/ScaFES_ProblemCuda.hpp:45-55).  The message of the last failure is
+ *    available from the *_last_error functions.
+ *  - Calls on one handle are single-threaded and ordered on the handle's
+ *    stream.  Uploads and downloads synchronise that stream.
+ *  - The handle owns its device memory.
+ */
+#ifndef SCAFES_GB300_H
+#define SCAFES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SCAFES_OK 0
+#define SCAFES_ERR_ARG (-1)         /* invalid argument or size            */
+#define SCAFES_ERR_CUDA (-2)        /* a CUDA runtime call failed          */
+#define SCAFES_ERR_STATE (-3)       /* call out of order (e.g. no upload)  */
+#define SCAFES_ERR_UNSUPPORTED (-4) /* configuration no kernel covers      */
+#define SCAFES_ERR_NOMEM (-5)       /* device or host allocation failed    */
+#define SCAFES_ERR_TIMEOUT (-6)     /* a bounded device wait ran out       */
+
+/* ---- arithmetic / storage of the unknown field ------------------------- */
+enum scafes_precision {
+    /* FP64 storage, FP64 arithmetic (the reference's CT = double). */
+    SCAFES_PREC_F64 = 0,
+    /* Compensated FP32: each value is an unevaluated pair hi + lo of FP32
+     * numbers (8 bytes per node), updated with error-free transformations
+     * (Knuth TwoSum, FMA-based TwoProd).  About 48 significant bits. */
+    SCAFES_PREC_F32X2 = 1,
+    /* Plain FP32 storage and arithmetic. */
+    SCAFES_PREC_F32 = 2,
+    /* FP64 storage, arithmetic emulated with FP32 pairs: values are split
+     * into hi + lo on load and rounded back to FP64 on store. */
+    SCAFES_PREC_F64E = 3
+};
+
+/* ---- field slots of a plain problem ------------------------------------ */
+enum scafes_field {
+    SCAFES_FIELD_U = 0,   /* the unknown data field (iterate)            */
+    SCAFES_FIELD_F_A = 1, /* source F(t) = F_A + time(t) * F_B            */
+    SCAFES_FIELD_F_B = 2,
+    SCAFES_FIELD_G_A = 3, /* border value G(t) = G_A + time(t) * G_B      */
+    SCAFES_FIELD_G_B = 4,
+    SCAFES_FIELD_E_A = 5, /* exact solution E(t) = E_A + time(t) * E_B,   */
+    SCAFES_FIELD_E_B = 6, /* only read by scafes_gpu_err_linf            */
+    SCAFES_FIELD_COUNT = 7
+};
+
+/* ---- border (updateBorder) kinds --------------------------------------- */
+enum scafes_border {
+    /* u_new = G(time(t+1)) on every global-border node: the Dirichlet
+     * updateBorder of tests/system/HeatEqnFDM/Dirichlet/Dirichlet.hpp:125-131
+     * and tests/system/PennesBioheatEqnFDM/Dirichlet/Dirichlet.hpp:125-131. */
+    SCAFES_BORDER_DIRICHLET = 0,
+    /* u_new = u_old + u_old(opposite neighbour) - s * 2^(t) at a face node,
+     * the border update of tests/system/HeatEqnFdmStencilWidthOne/
+     * HeatEqnFdmStencilWidthOne.hpp:136-163 (s = +1 at min faces, -1 at max
+     * faces, last face in direction order wins). */
+    SCAFES_BORDER_MIRROR_POW2 = 1
+};
+
+/* Configuration of one plain (single-instance) problem.
+ *
+ * The inner update is the 7-point linear "star" form every constant-
+ * coefficient ScaFES heat-type callback reduces to:
+ *   u_new = c0*u + sum_p cp[p]*(u_{p-} + u_{p+}) + cf*F(time(t-1))
+ * e.g. HeatEqnFDM (tests/system/HeatEqnFDM/HeatEqnFDM.hpp:205-218):
+ *   cp[p] = tau*a/h_p^2, c0 = 1 - 2*sum_p cp[p], cf = tau/(rho*c);
+ * Pennes (tests/system/PennesBioheatEqnFDM/PennesBioheatEqnFDM.hpp:153-168)
+ * additionally subtracts tau*(rho_b*c_b/(rho*c))*W from c0.
+ * scafes_star7_heat_coeffs() fills them from the physical parameters. */
+typedef struct scafes_cfg {
+    int dim;                 /* must be 3 */
+    int n_nodes[3];          /* nodes per axis, each >= 3 */
+    double coord_first[3];   /* coordinates of node 0 and node n-1 */
+    double coord_last[3];
+    double tau;              /* time step size */
+    double t_start;          /* time of iterate 0 */
+    int n_layers_at_border;  /* must be 1 (reference default) */
+    int precision;           /* enum scafes_precision */
+    int border;              /* enum scafes_border */
+    double c0;               /* centre coefficient */
+    double cp[3];            /* pair coefficient per axis */
+    double cf;               /* source coefficient (0 disables F) */
+    void* stream;            /* cudaStream_t to run on, or NULL for an own one */
+} scafes_cfg;
+
+typedef struct scafes_handle scafes_handle;
+
+/* Fills c0, cp[3], cf of *cfg for the heat / Pennes inner update from the
+ * grid of *cfg (h_p = (last-first)/(n-1), src/ScaFES_Grid.hpp:551-553):
+ * coeff_a = lambda/(rho*c), rho_c = rho*c, perf = rho_b*c_b*W/(rho*c)
+ * (0 for plain heat). */
+int scafes_star7_heat_coeffs(scafes_cfg* cfg, double coeff_a, double rho_c,
+                             double perf);
+
+/* Allocates device memory for the problem of *cfg.  Replaces the field
+ * allocation of the Problem constructor (src/ScaFES_Problem.hpp:1604-1674). */
+int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out);
+
+/* Copies a host field (n = nx*ny*nz doubles) into slot `field` and, for the
+ * unknown field, resets the step counter to 0 (the initial iterate; replaces
+ * evalInitPbPhase, src/ScaFES_Problem.hpp:2755-2826, whose values come from
+ * the host).  Known-field slots not uploaded read as 0. */
+int scafes_gpu_upload(scafes_handle* h, int field, const double* host,
+                      size_t n);
+
+/* Advances the unknown field by n_steps time steps (one step = the update
+ * phase of one iteration of iterateOverTime, src/ScaFES_Problem.hpp:
+ * 2596-2603, including the border pass and the old/new swap).  Asynchronous
+ * on the handle's stream. */
+int scafes_gpu_step(scafes_handle* h, int n_steps);
+
+/* Copies the current iterate (or another slot) back to the host; n as for
+ * upload.  Synchronises the handle's stream. */
+int scafes_gpu_download(scafes_handle* h, int field, double* host, size_t n);
+
+/* Number of steps taken since the last upload of the unknown field. */
+int scafes_gpu_timestep(const scafes_handle* h, int* t);
+
+/* Max-norm error of the current iterate against the exact-solution slots on
+ * the device (DataField::compErrLinf, src/ScaFES_DataField.hpp:1440-1530):
+ * *err = max|u - E(time(t))|, *max_ref = max|E(time(t))| over all nodes.
+ * Uses a per-handle device scratch buffer for the partial maxima.
+ * Synchronises the handle's stream. */
+int scafes_gpu_err_linf(scafes_handle* h, double* err, double* max_ref);
+
+/* Time of the last kernel sweep sequence, in ms, measured with CUDA events
+ * on the handle's stream by the last scafes_gpu_step call. */
+int scafes_gpu_last_step_ms(const scafes_handle* h, float* ms);
+
+/* Number of kernel launches issued by the last scafes_gpu_step call. */
+int scafes_gpu_last_step_launches(const scafes_handle* h, int* launches);
+
+const char* scafes_gpu_last_error(const scafes_handle* h);
+void scafes_gpu_destroy(scafes_handle* h);
+
+/* Message of the most recent failure of any call made on this thread
+ * (covers failures before a handle exists). */
+const char* scafes_last_error(void);
+
+/* No counterpart in the reference: measures the FP64 and FP32 FMA issue
+ * rates of the current GPU (G op/s) with CUDA events, the compute ceilings
+ * the benchmark reports beside the HBM roofline. */
+int scafes_probe_pipe_rates(double* fp64_gops, double* fp32_gops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,177 @@
+"""GB300-native explicit-stencil engine for ScaFES problems.
+
+This package holds the CUDA kernels and the C ABI (``csrc/``, built into
+``libscafes_gb300.so``; declarations in ``include/scafes_gb300.h``) and a thin
+ctypes binding used by the tests and the benchmark.  The C++ drop-in for
+``ScaFES::Problem`` lives in ``masterthesis_gb300/scafes/``.
+
+There is no CPU fallback: every call goes to the native library, and loading
+fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libscafes_gb300.so"
+
+# enum scafes_precision
+PREC_F64, PREC_F32X2, PREC_F32, PREC_F64E = 0, 1, 2, 3
+PRECISIONS = {"f64": PREC_F64, "f32x2": PREC_F32X2, "f32": PREC_F32, "f64e": PREC_F64E}
+# enum scafes_field
+FIELD_U, FIELD_F_A, FIELD_F_B, FIELD_G_A, FIELD_G_B, FIELD_E_A, FIELD_E_B = range(7)
+# enum scafes_border
+BORDER_DIRICHLET, BORDER_MIRROR_POW2 = 0, 1
+
+STATUS = {0: "SCAFES_OK", -1: "SCAFES_ERR_ARG", -2: "SCAFES_ERR_CUDA", -3: "SCAFES_ERR_STATE",
+          -4: "SCAFES_ERR_UNSUPPORTED", -5: "SCAFES_ERR_NOMEM", -6: "SCAFES_ERR_TIMEOUT"}
+
+
+class ScafesError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Cfg(C.Structure):
+    """Mirror of ``struct scafes_cfg``."""
+    _fields_ = [("dim", C.c_int), ("n_nodes", C.c_int * 3), ("coord_first", C.c_double * 3),
+                ("coord_last", C.c_double * 3), ("tau", C.c_double), ("t_start", C.c_double),
+                ("n_layers_at_border", C.c_int), ("precision", C.c_int), ("border", C.c_int),
+                ("c0", C.c_double), ("cp", C.c_double * 3), ("cf", C.c_double),
+                ("stream", C.c_void_p)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The loaded native library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with masterthesis_gb300.build.build_library() "
+                "(there is no CPU fallback)")
+        L = C.CDLL(str(LIB_PATH))
+        vp, dp = C.c_void_p, C.POINTER(C.c_double)
+        L.scafes_star7_heat_coeffs.argtypes = [C.POINTER(Cfg), C.c_double, C.c_double, C.c_double]
+        L.scafes_gpu_create.argtypes = [C.POINTER(Cfg), C.POINTER(vp)]
+        L.scafes_gpu_upload.argtypes = [vp, C.c_int, dp, C.c_size_t]
+        L.scafes_gpu_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
+        L.scafes_gpu_step.argtypes = [vp, C.c_int]
+        L.scafes_gpu_timestep.argtypes = [vp, C.POINTER(C.c_int)]
+        L.scafes_gpu_err_linf.argtypes = [vp, dp, dp]
+        L.scafes_gpu_last_step_ms.argtypes = [vp, C.POINTER(C.c_float)]
+        L.scafes_gpu_last_step_launches.argtypes = [vp, C.POINTER(C.c_int)]
+        L.scafes_gpu_last_error.argtypes = [vp]
+        L.scafes_gpu_last_error.restype = C.c_char_p
+        L.scafes_last_error.restype = C.c_char_p
+        L.scafes_gpu_destroy.argtypes = [vp]
+        L.scafes_gpu_destroy.restype = None
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, h=None):
+    if rc != 0:
+        L = lib()
+        msg = (L.scafes_gpu_last_error(h) if h else L.scafes_last_error()) or b""
+        raise ScafesError(rc, msg.decode())
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def make_cfg(n, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), tau=0.0, t_start=0.0,
+             precision="f64", border=BORDER_DIRICHLET, c0=None, cp=None, cf=0.0,
+             heat=None, stream=None) -> Cfg:
+    """Builds a scafes_cfg.  ``heat=(coeff_a, rho_c, perf)`` fills the heat /
+    Pennes coefficients via scafes_star7_heat_coeffs; otherwise give c0/cp/cf."""
+    c = Cfg()
+    c.dim = 3
+    c.n_nodes[:] = list(n)
+    c.coord_first[:] = list(first)
+    c.coord_last[:] = list(last)
+    c.tau, c.t_start = tau, t_start
+    c.n_layers_at_border = 1
+    c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    c.border = border
+    c.stream = stream
+    if heat is not None:
+        _check(lib().scafes_star7_heat_coeffs(C.byref(c), *heat))
+    else:
+        c.c0 = c0
+        c.cp[:] = list(cp)
+        c.cf = cf
+    return c
+
+
+class Plain:
+    """One single-instance problem on the GPU (owns a scafes_handle)."""
+
+    def __init__(self, cfg: Cfg):
+        self.cfg = cfg
+        self.n = tuple(cfg.n_nodes)
+        h = C.c_void_p()
+        _check(lib().scafes_gpu_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    @property
+    def shape(self):
+        return (self.n[2], self.n[1], self.n[0])
+
+    def upload(self, field: int, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        if a.size != int(np.prod(self.n)):
+            raise ValueError(f"field has {a.size} values, grid has {int(np.prod(self.n))}")
+        _check(lib().scafes_gpu_upload(self.h, field, _dp(a), a.size), self.h)
+
+    def download(self, field: int = FIELD_U, out: np.ndarray | None = None) -> np.ndarray:
+        a = np.empty(self.shape, dtype=np.float64) if out is None else out
+        _check(lib().scafes_gpu_download(self.h, field, _dp(a), a.size), self.h)
+        return a
+
+    def step(self, n_steps: int):
+        _check(lib().scafes_gpu_step(self.h, n_steps), self.h)
+
+    def timestep(self) -> int:
+        t = C.c_int()
+        _check(lib().scafes_gpu_timestep(self.h, C.byref(t)), self.h)
+        return t.value
+
+    def err_linf(self):
+        e, m = C.c_double(), C.c_double()
+        _check(lib().scafes_gpu_err_linf(self.h, C.byref(e), C.byref(m)), self.h)
+        return e.value, m.value
+
+    def last_step_ms(self) -> float:
+        v = C.c_float()
+        _check(lib().scafes_gpu_last_step_ms(self.h, C.byref(v)), self.h)
+        return v.value
+
+    def last_step_launches(self) -> int:
+        v = C.c_int()
+        _check(lib().scafes_gpu_last_step_launches(self.h, C.byref(v)), self.h)
+        return v.value
+
+    def close(self):
+        if self.h:
+            lib().scafes_gpu_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,445 @@
+// C ABI of the plain (single-instance) problem: handle life cycle, field
+// transfer, the time-step loop and the L-infinity error check.
+//
+// The handle plays the role of the field lumps the ScaFES Problem
+// constructor allocates (src/ScaFES_Problem.hpp:1604-1674): two ping-pong
+// buffers of the unknown field (the old/new pair swapped by
+// swapPointersOfUnknownDfs, :3273-3316) plus the known fields.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "star7.cuh"
+#include "../../include/scafes_gb300.h"
+
+using namespace scafes;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(std::string* where, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    if (where) *where = buf;
+    return code;
+}
+
+// Bytes of host staging used for precision conversions (per slab).
+constexpr size_t kStageBytes = 64ull << 20;
+
+}  // namespace
+
+struct scafes_handle {
+    scafes_cfg cfg;
+    Layout L;
+    size_t esz = 0;
+    void* u[2] = {nullptr, nullptr};
+    int cur = 0;
+    void* fld[SCAFES_FIELD_COUNT] = {};   // known slots (U slot unused here)
+    bool has[SCAFES_FIELD_COUNT] = {};
+    double* stage = nullptr;              // device staging for conversions
+    size_t stage_elems = 0;
+    double* red = nullptr;                // err_linf partial maxima (scratch)
+    int red_blocks = 0;
+    double* red_host = nullptr;           // pinned result of err_linf
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed = false;
+    int launches = 0;
+    int t = 0;
+    bool uploaded = false;
+    std::string err;
+};
+
+#define CUDA_TRY(h, call)                                                           \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess)                                                      \
+            return fail((h) ? &(h)->err : nullptr, SCAFES_ERR_CUDA, "%s: %s (%s:%d)", \
+                        #call, cudaGetErrorString(e_), __FILE__, __LINE__);         \
+    } while (0)
+
+extern "C" const char* scafes_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" const char* scafes_gpu_last_error(const scafes_handle* h) {
+    return h ? h->err.c_str() : g_last_error.c_str();
+}
+
+extern "C" int scafes_star7_heat_coeffs(scafes_cfg* cfg, double coeff_a,
+                                        double rho_c, double perf) {
+    if (!cfg || cfg->dim != 3 || rho_c == 0.0)
+        return fail(nullptr, SCAFES_ERR_ARG, "scafes_star7_heat_coeffs: bad arguments");
+    double sum = 0.0;
+    for (int p = 0; p < 3; ++p) {
+        if (cfg->n_nodes[p] < 2)
+            return fail(nullptr, SCAFES_ERR_ARG, "scafes_star7_heat_coeffs: n_nodes[%d] < 2", p);
+        const double h = (cfg->coord_last[p] - cfg->coord_first[p]) / (cfg->n_nodes[p] - 1);
+        cfg->cp[p] = cfg->tau * coeff_a / (h * h);
+        sum += cfg->cp[p];
+    }
+    cfg->c0 = 1.0 - 2.0 * sum - cfg->tau * perf;
+    cfg->cf = cfg->tau * (1.0 / rho_c);
+    return SCAFES_OK;
+}
+
+static int validate(const scafes_cfg* c) {
+    if (!c) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_create: cfg is NULL");
+    if (c->dim != 3)
+        return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: dim=%d (only 3 is supported)", c->dim);
+    for (int p = 0; p < 3; ++p)
+        if (c->n_nodes[p] < 3 || c->n_nodes[p] > (1 << 20))
+            return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_create: n_nodes[%d]=%d out of range [3, 2^20]",
+                        p, c->n_nodes[p]);
+    if (c->n_layers_at_border != 1)
+        return fail(nullptr, SCAFES_ERR_UNSUPPORTED,
+                    "scafes_gpu_create: n_layers_at_border=%d (only 1 is supported)", c->n_layers_at_border);
+    if (c->precision != SCAFES_PREC_F64 && c->precision != SCAFES_PREC_F32X2 &&
+        c->precision != SCAFES_PREC_F32)
+        return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: precision %d not supported", c->precision);
+    if (c->border != SCAFES_BORDER_DIRICHLET && c->border != SCAFES_BORDER_MIRROR_POW2)
+        return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: border kind %d not supported", c->border);
+    return SCAFES_OK;
+}
+
+extern "C" void scafes_gpu_destroy(scafes_handle* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (int i = 0; i < 2; ++i) cudaFree(h->u[i]);
+    for (int i = 0; i < SCAFES_FIELD_COUNT; ++i) cudaFree(h->fld[i]);
+    cudaFree(h->stage);
+    cudaFree(h->red);
+    if (h->red_host) cudaFreeHost(h->red_host);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+extern "C" int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out) {
+    if (!out) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_create: out is NULL");
+    *out = nullptr;
+    int rc = validate(cfg);
+    if (rc != SCAFES_OK) return rc;
+    scafes_handle* h = new (std::nothrow) scafes_handle();
+    if (!h) return fail(nullptr, SCAFES_ERR_NOMEM, "scafes_gpu_create: out of host memory");
+    h->cfg = *cfg;
+    h->L = make_layout(cfg->n_nodes[0], cfg->n_nodes[1], cfg->n_nodes[2]);
+    h->esz = element_size(cfg->precision);
+    const size_t bytes = (size_t)h->L.size() * h->esz;
+    auto bail = [&](int code, const char* what, cudaError_t e) {
+        int r = fail(nullptr, code, "scafes_gpu_create: %s: %s", what, cudaGetErrorString(e));
+        scafes_gpu_destroy(h);
+        return r;
+    };
+    cudaError_t e;
+    if (cfg->stream) {
+        h->stream = (cudaStream_t)cfg->stream;
+    } else {
+        if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess)
+            return bail(SCAFES_ERR_CUDA, "cudaStreamCreate", e);
+        h->own_stream = true;
+    }
+    for (int i = 0; i < 2; ++i) {
+        if ((e = cudaMalloc(&h->u[i], bytes)) != cudaSuccess)
+            return bail(SCAFES_ERR_NOMEM, "cudaMalloc(u)", e);
+        if ((e = cudaMemsetAsync(h->u[i], 0, bytes, h->stream)) != cudaSuccess)
+            return bail(SCAFES_ERR_CUDA, "cudaMemset(u)", e);
+    }
+    if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) return bail(SCAFES_ERR_CUDA, "cudaEventCreate", e);
+    if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(SCAFES_ERR_CUDA, "cudaEventCreate", e);
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    h->red_blocks = sms * 4;
+    if ((e = cudaMalloc(&h->red, sizeof(double) * 2 * (h->red_blocks + 1))) != cudaSuccess)
+        return bail(SCAFES_ERR_NOMEM, "cudaMalloc(scratch)", e);
+    if ((e = cudaMallocHost(&h->red_host, sizeof(double) * 2)) != cudaSuccess)
+        return bail(SCAFES_ERR_NOMEM, "cudaMallocHost", e);
+    if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) return bail(SCAFES_ERR_CUDA, "sync", e);
+    *out = h;
+    return SCAFES_OK;
+}
+
+static bool slot_is_double(int field) {
+    return field == SCAFES_FIELD_G_A || field == SCAFES_FIELD_G_B ||
+           field == SCAFES_FIELD_E_A || field == SCAFES_FIELD_E_B;
+}
+
+static int ensure_stage(scafes_handle* h) {
+    if (h->stage) return SCAFES_OK;
+    const size_t plane_elems = (size_t)h->L.nx * h->L.ny;
+    size_t planes = kStageBytes / (plane_elems * sizeof(double));
+    if (planes < 1) planes = 1;
+    if (planes > (size_t)h->L.nz) planes = h->L.nz;
+    h->stage_elems = planes * plane_elems;
+    CUDA_TRY(h, cudaMalloc(&h->stage, h->stage_elems * sizeof(double)));
+    return SCAFES_OK;
+}
+
+// host dense -> device field of element type `prec` (or double when prec < 0)
+static int h2d(scafes_handle* h, void* dst, int prec, const double* host) {
+    const Layout& L = h->L;
+    if (prec == SCAFES_PREC_F64) {
+        CUDA_TRY(h, cudaMemcpy2DAsync(dst, (size_t)L.pitch * sizeof(double), host,
+                                      (size_t)L.nx * sizeof(double), (size_t)L.nx * sizeof(double),
+                                      (size_t)L.ny * L.nz, cudaMemcpyHostToDevice, h->stream));
+        return SCAFES_OK;
+    }
+    int rc = ensure_stage(h);
+    if (rc) return rc;
+    const size_t plane_elems = (size_t)L.nx * L.ny;
+    const int planes = (int)(h->stage_elems / plane_elems);
+    const size_t esz = element_size(prec);
+    for (int z0 = 0; z0 < L.nz; z0 += planes) {
+        const int nzs = (z0 + planes <= L.nz) ? planes : L.nz - z0;
+        CUDA_TRY(h, cudaMemcpyAsync(h->stage, host + (size_t)z0 * plane_elems,
+                                    (size_t)nzs * plane_elems * sizeof(double),
+                                    cudaMemcpyHostToDevice, h->stream));
+        Layout S = L;
+        S.nz = nzs;
+        char* d = (char*)dst + (size_t)z0 * L.plane * esz;
+        CUDA_TRY(h, convert_to_device(prec, h->stage, d, S, h->stream));
+    }
+    return SCAFES_OK;
+}
+
+static int d2h(scafes_handle* h, const void* src, int prec, double* host) {
+    const Layout& L = h->L;
+    if (prec == SCAFES_PREC_F64) {
+        CUDA_TRY(h, cudaMemcpy2DAsync(host, (size_t)L.nx * sizeof(double), src,
+                                      (size_t)L.pitch * sizeof(double), (size_t)L.nx * sizeof(double),
+                                      (size_t)L.ny * L.nz, cudaMemcpyDeviceToHost, h->stream));
+        return SCAFES_OK;
+    }
+    int rc = ensure_stage(h);
+    if (rc) return rc;
+    const size_t plane_elems = (size_t)L.nx * L.ny;
+    const int planes = (int)(h->stage_elems / plane_elems);
+    const size_t esz = element_size(prec);
+    for (int z0 = 0; z0 < L.nz; z0 += planes) {
+        const int nzs = (z0 + planes <= L.nz) ? planes : L.nz - z0;
+        Layout S = L;
+        S.nz = nzs;
+        const char* s = (const char*)src + (size_t)z0 * L.plane * esz;
+        CUDA_TRY(h, convert_from_device(prec, s, h->stage, S, h->stream));
+        CUDA_TRY(h, cudaMemcpyAsync(host + (size_t)z0 * plane_elems, h->stage,
+                                    (size_t)nzs * plane_elems * sizeof(double),
+                                    cudaMemcpyDeviceToHost, h->stream));
+    }
+    return SCAFES_OK;
+}
+
+static size_t n_nodes(const scafes_handle* h) {
+    return (size_t)h->L.nx * h->L.ny * h->L.nz;
+}
+
+extern "C" int scafes_gpu_upload(scafes_handle* h, int field, const double* host, size_t n) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_upload: handle is NULL");
+    if (field < 0 || field >= SCAFES_FIELD_COUNT)
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_upload: field %d out of range", field);
+    if (!host || n != n_nodes(h))
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_upload: expected %zu values, got %zu%s",
+                    n_nodes(h), n, host ? "" : " (NULL pointer)");
+    int rc;
+    if (field == SCAFES_FIELD_U) {
+        rc = h2d(h, h->u[0], h->cfg.precision, host);
+        if (rc) return rc;
+        h->cur = 0;
+        h->t = 0;
+        h->uploaded = true;
+    } else {
+        const bool dbl = slot_is_double(field);
+        const size_t esz = dbl ? sizeof(double) : h->esz;
+        if (!h->fld[field]) {
+            CUDA_TRY(h, cudaMalloc(&h->fld[field], (size_t)h->L.size() * esz));
+            CUDA_TRY(h, cudaMemsetAsync(h->fld[field], 0, (size_t)h->L.size() * esz, h->stream));
+        }
+        rc = h2d(h, h->fld[field], dbl ? SCAFES_PREC_F64 : h->cfg.precision, host);
+        if (rc) return rc;
+        h->has[field] = true;
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_download(scafes_handle* h, int field, double* host, size_t n) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_download: handle is NULL");
+    if (field < 0 || field >= SCAFES_FIELD_COUNT)
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_download: field %d out of range", field);
+    if (!host || n != n_nodes(h))
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_download: expected %zu values, got %zu",
+                    n_nodes(h), n);
+    int rc;
+    if (field == SCAFES_FIELD_U) {
+        if (!h->uploaded)
+            return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_download: the unknown field was never uploaded");
+        rc = d2h(h, h->u[h->cur], h->cfg.precision, host);
+    } else {
+        if (!h->has[field])
+            return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_download: slot %d was never uploaded", field);
+        rc = d2h(h, h->fld[field], slot_is_double(field) ? SCAFES_PREC_F64 : h->cfg.precision, host);
+    }
+    if (rc) return rc;
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_step(scafes_handle* h, int n_steps) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_step: handle is NULL");
+    if (n_steps < 0) return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_step: n_steps=%d < 0", n_steps);
+    if (!h->uploaded)
+        return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_step: upload the unknown field first");
+    Star7Launch a;
+    a.precision = h->cfg.precision;
+    a.border = h->cfg.border;
+    a.L = h->L;
+    a.fa = h->has[SCAFES_FIELD_F_A] ? h->fld[SCAFES_FIELD_F_A] : nullptr;
+    a.fb = h->has[SCAFES_FIELD_F_B] ? h->fld[SCAFES_FIELD_F_B] : nullptr;
+    a.ga = h->has[SCAFES_FIELD_G_A] ? (const double*)h->fld[SCAFES_FIELD_G_A] : nullptr;
+    a.gb = h->has[SCAFES_FIELD_G_B] ? (const double*)h->fld[SCAFES_FIELD_G_B] : nullptr;
+    a.c = make_star7_coeffs(h->cfg.c0, h->cfg.cp, h->cfg.cf);
+    if (!h->has[SCAFES_FIELD_F_A] && h->has[SCAFES_FIELD_F_B])
+        return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                    "scafes_gpu_step: upload F_A (possibly zeros) when F_B is used");
+    CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
+    for (int s = 0; s < n_steps; ++s) {
+        a.uo = h->u[h->cur];
+        a.un = h->u[h->cur ^ 1];
+        a.time_old = h->cfg.t_start + h->t * h->cfg.tau;          // time(t)
+        a.time_new = h->cfg.t_start + (h->t + 1) * h->cfg.tau;    // time(t+1)
+        a.mirror_corr = ldexp(1.0, h->t);                          // 2^(t_new - 1)
+        cudaError_t e = launch_star7(a, h->stream);
+        if (e != cudaSuccess)
+            return fail(&h->err, SCAFES_ERR_CUDA, "scafes_gpu_step: launch failed: %s", cudaGetErrorString(e));
+        h->cur ^= 1;
+        h->t += 1;
+    }
+    CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
+    h->timed = true;
+    h->launches = n_steps;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_timestep(const scafes_handle* h, int* t) {
+    if (!h || !t) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_timestep: NULL argument");
+    *t = h->t;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_last_step_ms(const scafes_handle* h, float* ms) {
+    if (!h || !ms) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_last_step_ms: NULL argument");
+    if (!h->timed) return fail(nullptr, SCAFES_ERR_STATE, "scafes_gpu_last_step_ms: no step yet");
+    cudaError_t e = cudaEventSynchronize(h->ev1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, h->ev0, h->ev1);
+    if (e != cudaSuccess)
+        return fail(nullptr, SCAFES_ERR_CUDA, "scafes_gpu_last_step_ms: %s", cudaGetErrorString(e));
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_last_step_launches(const scafes_handle* h, int* launches) {
+    if (!h || !launches) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_last_step_launches: NULL argument");
+    *launches = h->launches;
+    return SCAFES_OK;
+}
+
+// ---- L-infinity error (DataField::compErrLinf) -------------------------------
+
+template <class T>
+__device__ __forceinline__ double load_as_double(const T* p, long long o);
+template <>
+__device__ __forceinline__ double load_as_double<double>(const double* p, long long o) { return p[o]; }
+template <>
+__device__ __forceinline__ double load_as_double<float>(const float* p, long long o) { return (double)p[o]; }
+template <>
+__device__ __forceinline__ double load_as_double<float2>(const float2* p, long long o) {
+    float2 v = p[o];
+    return join_pair(v.x, v.y);
+}
+
+__device__ __forceinline__ double nan_to_inf(double d) { return (d != d) ? __longlong_as_double(0x7ff0000000000000LL) : d; }
+
+// Pass 1: per-CTA maxima of |u - E| and |E| into part[2*blockIdx.x + {0,1}].
+template <class T>
+__global__ void k_err_partial(const T* __restrict__ u, const double* __restrict__ ea,
+                              const double* __restrict__ eb, double time, Layout L,
+                              double* __restrict__ part) {
+    __shared__ double s_err[8], s_ref[8];
+    double me = 0.0, mr = 0.0;
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < n;
+         m += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(m % L.nx);
+        const long long r = m / L.nx;
+        const long long o = L.idx(i, (int)(r % L.ny), (int)(r / L.ny));
+        double e = ea ? ea[o] : 0.0;
+        if (eb) e += time * eb[o];
+        const double d = nan_to_inf(fabs(load_as_double<T>(u, o) - e));
+        me = fmax(me, d);
+        mr = fmax(mr, fabs(e));
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        me = fmax(me, __shfl_down_sync(0xffffffffu, me, s));
+        mr = fmax(mr, __shfl_down_sync(0xffffffffu, mr, s));
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { s_err[w] = me; s_ref[w] = mr; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { me = fmax(me, s_err[k]); mr = fmax(mr, s_ref[k]); }
+        part[2 * blockIdx.x] = me;
+        part[2 * blockIdx.x + 1] = mr;
+    }
+}
+
+// Pass 2: one CTA folds the partial maxima into out[0..1].
+__global__ void k_err_final(const double* __restrict__ part, int nparts, double* __restrict__ out) {
+    double me = 0.0, mr = 0.0;
+    for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+        me = fmax(me, part[2 * k]);
+        mr = fmax(mr, part[2 * k + 1]);
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        me = fmax(me, __shfl_down_sync(0xffffffffu, me, s));
+        mr = fmax(mr, __shfl_down_sync(0xffffffffu, mr, s));
+    }
+    __shared__ double s_err[32], s_ref[32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { s_err[w] = me; s_ref[w] = mr; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) { me = fmax(me, s_err[k]); mr = fmax(mr, s_ref[k]); }
+        out[0] = me;
+        out[1] = mr;
+    }
+}
+
+extern "C" int scafes_gpu_err_linf(scafes_handle* h, double* err, double* max_ref) {
+    if (!h || !err || !max_ref) return fail(h ? &h->err : nullptr, SCAFES_ERR_ARG, "scafes_gpu_err_linf: NULL argument");
+    if (!h->uploaded) return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_err_linf: upload the unknown field first");
+    const double* ea = h->has[SCAFES_FIELD_E_A] ? (const double*)h->fld[SCAFES_FIELD_E_A] : nullptr;
+    const double* eb = h->has[SCAFES_FIELD_E_B] ? (const double*)h->fld[SCAFES_FIELD_E_B] : nullptr;
+    const double time = h->cfg.t_start + h->t * h->cfg.tau;
+    double* part = h->red;
+    double* out = h->red + 2 * h->red_blocks;
+    const void* u = h->u[h->cur];
+    switch (h->cfg.precision) {
+        case SCAFES_PREC_F64: k_err_partial<double><<<h->red_blocks, 256, 0, h->stream>>>((const double*)u, ea, eb, time, h->L, part); break;
+        case SCAFES_PREC_F32: k_err_partial<float><<<h->red_blocks, 256, 0, h->stream>>>((const float*)u, ea, eb, time, h->L, part); break;
+        default: k_err_partial<float2><<<h->red_blocks, 256, 0, h->stream>>>((const float2*)u, ea, eb, time, h->L, part); break;
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    k_err_final<<<1, 1024, 0, h->stream>>>(part, h->red_blocks, out);
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaMemcpyAsync(h->red_host, out, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    *err = h->red_host[0];
+    *max_ref = h->red_host[1];
+    return SCAFES_OK;
+}

@@ -1,0 +1,70 @@
+// Issue-rate probes for the roofline of the sweep kernels: the FP64 FMA rate
+// and the FP32 FMA rate of the current GPU, measured with CUDA events.
+// On GB300 the FP64 rate, not HBM, bounds an FP64 7-point sweep, so the
+// benchmark reports that bound beside the HBM one.
+#include <cuda_runtime.h>
+
+#include "../../include/scafes_gb300.h"
+
+namespace {
+
+constexpr int kIters = 2048;
+
+__global__ void k_dfma_rate(double* out, double a, double b) {
+    double x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+#pragma unroll 4
+    for (int i = 0; i < kIters; ++i) {
+        x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+__global__ void k_ffma_rate(float* out, float a, float b) {
+    float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    float x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+#pragma unroll 4
+    for (int i = 0; i < 4 * kIters; ++i) {
+        x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+        x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+}  // namespace
+
+// No counterpart in the reference: a measurement utility for the roofline.
+extern "C" int scafes_probe_pipe_rates(double* fp64_gops, double* fp32_gops) {
+    if (!fp64_gops || !fp32_gops) return SCAFES_ERR_ARG;
+    int dev = 0, sms = 1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return SCAFES_ERR_CUDA;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, threads = 256;
+    double* buf = nullptr;
+    if (cudaMalloc(&buf, sizeof(double) * blocks * threads) != cudaSuccess) return SCAFES_ERR_NOMEM;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float ms = 0.f;
+    const double lanes = (double)blocks * threads * 8;
+    k_dfma_rate<<<blocks, threads>>>(buf, 1.0000001, 1e-9);  // warm-up
+    cudaEventRecord(e0);
+    for (int r = 0; r < 3; ++r) k_dfma_rate<<<blocks, threads>>>(buf, 1.0000001, 1e-9);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    *fp64_gops = lanes * kIters * 3 / (ms * 1e-3) / 1e9;
+    k_ffma_rate<<<blocks, threads>>>((float*)buf, 1.0000001f, 1e-9f);
+    cudaEventRecord(e0);
+    for (int r = 0; r < 3; ++r) k_ffma_rate<<<blocks, threads>>>((float*)buf, 1.0000001f, 1e-9f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    *fp32_gops = lanes * 4 * kIters * 3 / (ms * 1e-3) / 1e9;
+    cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    return err == cudaSuccess ? SCAFES_OK : SCAFES_ERR_CUDA;
+}

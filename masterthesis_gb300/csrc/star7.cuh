@@ -1,0 +1,48 @@
+// Internal interface between the C ABI (capi.cu) and the plain 7-point sweep
+// kernels (sweep_star7.cu).
+#pragma once
+
+#include "scafes_common.cuh"
+
+namespace scafes {
+
+// Coefficients of u_new = c0*u + sum_p cp*(u_{p-}+u_{p+}) + cf*F, in double
+// and split into FP32 hi/lo pairs for the compensated path.
+struct Star7Coeffs {
+    double c0, cx, cy, cz, cf;
+    float c0h, c0l, cxh, cxl, cyh, cyl, czh, czl, cfh, cfl;
+};
+
+Star7Coeffs make_star7_coeffs(double c0, const double cp[3], double cf);
+
+struct Star7Launch {
+    int precision;        // enum scafes_precision
+    int border;           // enum scafes_border
+    Layout L;
+    const void* uo;       // old iterate (element type per precision)
+    void* un;             // new iterate
+    const void* fa;       // source F_A (element type per precision) or null
+    const void* fb;       // source F_B or null
+    const double* ga;     // border value G_A (double) or null
+    const double* gb;     // border value G_B (double) or null
+    Star7Coeffs c;
+    double time_old;      // time(t)   : F is read at the old time
+    double time_new;      // time(t+1) : G is read at the new time
+    double mirror_corr;   // 2^t for SCAFES_BORDER_MIRROR_POW2
+};
+
+// Enqueues one sweep (one time step) on `stream`.  Returns cudaSuccess or the
+// launch error.
+cudaError_t launch_star7(const Star7Launch& a, cudaStream_t stream);
+
+// Conversions between host-layout doubles (dense, x fastest) staged on the
+// device and the padded device layout of each precision.
+cudaError_t convert_to_device(int precision, const double* dense, void* field,
+                              const Layout& L, cudaStream_t stream);
+cudaError_t convert_from_device(int precision, const void* field,
+                                double* dense, const Layout& L,
+                                cudaStream_t stream);
+
+size_t element_size(int precision);
+
+}  // namespace scafes

@@ -1,0 +1,201 @@
+"""CPU oracle for the ScaFES explicit update path -- TEST INFRASTRUCTURE ONLY.
+
+Python access (ctypes) to ``liboracle_scafes.so``, the plain-C restatement of
+the reference's update sweeps in ``scafes_oracle.c``, plus helpers that run the
+reference-driver programs of ``oracle/_ref`` (built from the untouched
+reference headers by ``make -C oracle ref``).  Only ``tests/``, the smoke
+check and the CPU-baseline leg of ``bench.py`` import this package, as the
+checker.  The product library never uses it.
+
+Field arrays are float64 numpy arrays of shape (nz, ny, nx) in C order, which
+is the reference's Fortran node order (x fastest) in memory.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "liboracle_scafes.so"
+REF_DIR = HERE / "_ref"
+
+
+def build(force: bool = False) -> Path:
+    """Compile liboracle_scafes.so (gcc + OpenMP)."""
+    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < (HERE / "scafes_oracle.c").stat().st_mtime:
+        subprocess.run(["make", "-C", str(HERE), "liboracle_scafes.so"], check=True,
+                       capture_output=True)
+    return LIB_PATH
+
+
+def build_ref(reference: str = "/root/reference") -> bool:
+    """Compile the reference-driver programs into oracle/_ref (only where the
+    reference checkout exists)."""
+    if not Path(reference, "src", "ScaFES_Problem.hpp").exists():
+        return False
+    subprocess.run(["make", "-C", str(HERE), "-j8", "ref", f"REF={reference}"], check=True,
+                   capture_output=True)
+    return True
+
+
+class Grid(C.Structure):
+    _fields_ = [("dim", C.c_int), ("n", C.c_int * 3), ("first", C.c_double * 3),
+                ("last", C.c_double * 3), ("h", C.c_double * 3), ("tau", C.c_double),
+                ("t_start", C.c_double), ("n_layers", C.c_int)]
+
+
+class Known(C.Structure):
+    _fields_ = [("base", C.POINTER(C.c_double)), ("form", C.c_int), ("a", C.c_double),
+                ("b", C.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB_PATH))
+        dp = C.POINTER(C.c_double)
+        L.orc_grid_init.argtypes = [C.POINTER(Grid), C.c_int, C.POINTER(C.c_int), dp, dp,
+                                    C.c_double, C.c_double, C.c_int]
+        L.orc_heat_dirichlet.argtypes = [C.POINTER(Grid), C.c_double, C.c_double, C.c_double,
+                                         C.c_double, C.c_int, dp, Known, Known, C.c_int]
+        L.orc_pennes_mri.argtypes = [C.POINTER(Grid)] + [C.c_double] * 7 + [dp, dp, C.c_int, dp, C.c_int]
+        L.orc_stencil_width_one.argtypes = [C.POINTER(Grid), C.c_int, dp, C.c_int]
+        L.orc_stencil_width_var.argtypes = [C.POINTER(Grid), C.c_int, C.c_int, dp, C.c_int]
+        L.orc_kheat_forward.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.c_int]
+        L.orc_kheat_adjoint.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, dp, dp, dp, C.c_int]
+        for f in ("orc_heat_dirichlet", "orc_pennes_mri", "orc_stencil_width_one",
+                  "orc_stencil_width_var", "orc_kheat_forward", "orc_kheat_adjoint"):
+            getattr(L, f).restype = C.c_int
+        L.orc_time.restype = C.c_double
+        L.orc_time.argtypes = [C.POINTER(Grid), C.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError(f"oracle {what} failed with status {rc}")
+
+
+def make_grid(n, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), tau=0.0, t_start=0.0,
+              n_layers=1, dim=3) -> Grid:
+    g = Grid()
+    nn = (C.c_int * 3)(*n)
+    f = (C.c_double * 3)(*first)
+    l_ = (C.c_double * 3)(*last)
+    lib().orc_grid_init(C.byref(g), dim, nn, f, l_, tau, t_start, n_layers)
+    return g
+
+
+def coords(g: Grid):
+    """Coordinates x_p = first_p + h_p * i_p (src/ScaFES_Grid.hpp:721-733),
+    broadcastable to (nz, ny, nx)."""
+    nx, ny, nz = g.n[0], g.n[1], g.n[2]
+    x = g.first[0] + g.h[0] * np.arange(nx, dtype=np.float64)
+    y = g.first[1] + g.h[1] * np.arange(ny, dtype=np.float64)
+    z = g.first[2] + g.h[2] * np.arange(nz, dtype=np.float64)
+    return x[None, None, :], y[None, :, None], z[:, None, None]
+
+
+def border_mask(g: Grid) -> np.ndarray:
+    """Global-border nodes (src/ScaFES_Problem.hpp:3952-3971)."""
+    nx, ny, nz = g.n[0], g.n[1], g.n[2]
+    L = g.n_layers
+    m = np.zeros((nz, ny, nx), dtype=bool)
+    m[:L, :, :] = m[-L:, :, :] = True
+    m[:, :L, :] = m[:, -L:, :] = True
+    m[:, :, :L] = m[:, :, -L:] = True
+    return m
+
+
+def heat_dirichlet(g: Grid, u0, nsteps, coeff_a=1.0, rho_c=1.0, perf_q1=0.0, perf_w=0.0,
+                   f_base=None, f_form=0, f_a=1.0, f_b=0.0,
+                   g_base=None, g_form=0, g_a=1.0, g_b=0.0, nthreads=0):
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    fk = Known(_p(f_base), f_form, f_a, f_b)
+    gk = Known(_p(g_base), g_form, g_a, g_b)
+    _check(lib().orc_heat_dirichlet(C.byref(g), coeff_a, rho_c, perf_q1, perf_w, nsteps,
+                                    _p(u), fk, gk, nthreads), "heat_dirichlet")
+    return u
+
+
+def pennes_mri(g: Grid, u0, nsteps, rho, c, k, rho_b, c_b, omega, t_blood, q, g_bdry, nthreads=0):
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    gb = np.ascontiguousarray(g_bdry, dtype=np.float64)
+    _check(lib().orc_pennes_mri(C.byref(g), rho, c, k, rho_b, c_b, omega, t_blood, _p(q), _p(gb),
+                                nsteps, _p(u), nthreads), "pennes_mri")
+    return u
+
+
+def stencil_width_one(g: Grid, u0, nsteps, nthreads=0):
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    _check(lib().orc_stencil_width_one(C.byref(g), nsteps, _p(u), nthreads), "stencil_width_one")
+    return u
+
+
+def stencil_width_var(g: Grid, u0, bw, nsteps, nthreads=0):
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    _check(lib().orc_stencil_width_var(C.byref(g), bw, nsteps, _p(u), nthreads), "stencil_width_var")
+    return u
+
+
+def kheat_forward(g: Grid, k, u0, nsteps, keep_traj=False, nthreads=0):
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    traj = np.empty((nsteps + 1,) + u.shape, dtype=np.float64) if keep_traj else None
+    _check(lib().orc_kheat_forward(C.byref(g), _p(k), nsteps, _p(u), _p(traj), nthreads), "kheat_forward")
+    return (u, traj) if keep_traj else u
+
+
+def kheat_adjoint(g: Grid, k, traj, target, nthreads=0):
+    nsteps = traj.shape[0] - 1
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    target = np.ascontiguousarray(target, dtype=np.float64)
+    gk = np.empty_like(k)
+    gu = np.empty_like(k)
+    j = C.c_double(0.0)
+    _check(lib().orc_kheat_adjoint(C.byref(g), _p(k), nsteps, _p(traj), _p(target), _p(gk), _p(gu),
+                                   C.byref(j), nthreads), "kheat_adjoint")
+    return j.value, gk, gu
+
+
+# ---- reference-driver programs (oracle/_ref) ---------------------------------
+
+def ref_available(name: str) -> bool:
+    return (REF_DIR / name).exists() and os.access(REF_DIR / name, os.X_OK)
+
+
+def run_ref(name: str, n, nsteps, workdir, t_start=0.0, t_end=1.0, tau=0.0,
+            first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), inputs=None, extra=(), nfields=1,
+            threads=1) -> np.ndarray:
+    """Runs oracle/_ref/<name> and returns its final field(s), shape
+    (nfields, nz, ny, nx) (or (nz, ny, nx) for one field)."""
+    workdir = Path(workdir)
+    out = workdir / f"{name}.out.bin"
+    args = [str(REF_DIR / name), *map(str, n), str(nsteps), repr(float(t_start)), repr(float(t_end)),
+            repr(float(tau)), *map(lambda v: repr(float(v)), first), *map(lambda v: repr(float(v)), last),
+            str(out)]
+    if inputs is not None:
+        inp = workdir / f"{name}.in.bin"
+        np.ascontiguousarray(inputs, dtype=np.float64).tofile(inp)
+        args.append(str(inp))
+    args += [repr(float(v)) for v in extra]
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    subprocess.run(args, check=True, capture_output=True, env=env)
+    nz, ny, nx = n[2], n[1], n[0]
+    v = np.fromfile(out, dtype=np.float64)
+    v = v.reshape((nfields, nz, ny, nx))
+    return v[0] if nfields == 1 else v

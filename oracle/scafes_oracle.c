@@ -1,0 +1,419 @@
+/*
+ * CPU oracle for the ScaFES explicit update path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference's per-node update sweeps, written
+ * operation for operation in the order the reference's callbacks evaluate
+ * them, so that the result is bit-identical to the reference built with the
+ * same compiler flags (-ffp-contract=off).  Only tests/, the smoke check and
+ * the CPU-baseline leg of bench.py use it, as the checker; the product
+ * library never links it.
+ *
+ * Step semantics (src/ScaFES_Problem.hpp:2582-2638, 5078-5082, 5419-5466):
+ *   - t = 0 is the initial iterate (given by the caller);
+ *   - for t = 1..nsteps every node of the new iterate starts as a copy of
+ *     the old one, global-inner nodes run updateInner, global-border nodes
+ *     (within nLayersAtBorder of a face, :3952-3971) run updateBorder;
+ *   - knownDf(i, n) is the known field at time(t), knownDfOld(i, n) the one
+ *     at time(t-1), time(t) = t_start + t*tau (:2483-2486, :2519-2541);
+ *   - old/new are swapped after each step (:3273-3316).
+ */
+#include "scafes_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define IDX(i, j, k, nx, ny) ((size_t)(i) + (size_t)(nx) * ((size_t)(j) + (size_t)(ny) * (size_t)(k)))
+
+static void set_threads(int nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+}
+
+/* src/ScaFES_Grid.hpp:551-553: h_p = (last_p - first_p)/(n_p - 1). */
+void orc_grid_init(orc_grid* g, int dim, const int* n, const double* first,
+                   const double* last, double tau, double t_start,
+                   int n_layers)
+{
+    memset(g, 0, sizeof(*g));
+    g->dim = dim;
+    for (int p = 0; p < 3; ++p) {
+        g->n[p] = (p < dim) ? n[p] : 1;
+        g->first[p] = (p < dim) ? first[p] : 0.0;
+        g->last[p] = (p < dim) ? last[p] : 0.0;
+        g->h[p] = (p < dim && g->n[p] > 1)
+                      ? (g->last[p] - g->first[p]) / (g->n[p] - 1)
+                      : 0.0;
+    }
+    g->tau = tau;
+    g->t_start = t_start;
+    g->n_layers = n_layers;
+}
+
+/* src/ScaFES_Problem.hpp:2483-2486. */
+double orc_time(const orc_grid* g, int timestep)
+{
+    return g->t_start + timestep * g->tau;
+}
+
+/* src/ScaFES_Problem.hpp:3952-3971 (global border: within nLayers of a face). */
+int orc_is_border(const orc_grid* g, int i, int j, int k)
+{
+    const int idx[3] = {i, j, k};
+    for (int p = 0; p < g->dim; ++p) {
+        if (idx[p] < g->n_layers || idx[p] > g->n[p] - 1 - g->n_layers)
+            return 1;
+    }
+    return 0;
+}
+
+/* src/ScaFES_Grid.hpp:721-733. */
+void orc_coords(const orc_grid* g, int i, int j, int k, double* x)
+{
+    const int idx[3] = {i, j, k};
+    for (int p = 0; p < 3; ++p) x[p] = g->first[p] + g->h[p] * idx[p];
+}
+
+static double known_at(orc_known kf, size_t m, double time)
+{
+    if (!kf.base) return 0.0;
+    if (kf.form == 1) {
+        double v = kf.base[m];
+        v *= kf.a;
+        double tmp = kf.base[m];
+        tmp *= (1.0 + time);
+        v += kf.b * tmp;
+        return v;
+    }
+    return kf.base[m] * (kf.a + kf.b * time);
+}
+
+static size_t n_total(const orc_grid* g)
+{
+    return (size_t)g->n[0] * g->n[1] * g->n[2];
+}
+
+int orc_heat_dirichlet(const orc_grid* g, double coeff_a, double rho_c,
+                       double perf_q1, double perf_w, int nsteps, double* u,
+                       orc_known f_src, orc_known g_bdry, int nthreads)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const size_t nn = n_total(g);
+    double* w = (double*)malloc(nn * sizeof(double));
+    if (!w) return -1;
+    const int use_perf = (perf_q1 != 0.0 || perf_w != 0.0);
+    const long sx = 1, sy = nx, sz = (long)nx * ny;
+    const long stride[3] = {sx, sy, sz};
+    set_threads(nthreads);
+    double* uo = u;
+    double* un = w;
+    for (int t = 1; t <= nsteps; ++t) {
+        const double t_new = orc_time(g, t);
+        const double t_old = orc_time(g, t - 1);
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nz; ++k) {
+            for (int j = 0; j < ny; ++j) {
+                for (int i = 0; i < nx; ++i) {
+                    const size_t m = IDX(i, j, k, nx, ny);
+                    if (orc_is_border(g, i, j, k)) {
+                        /* Dirichlet.hpp:125-131: vNew = knownDf(1) (time t). */
+                        un[m] = known_at(g_bdry, m, t_new);
+                        continue;
+                    }
+                    /* HeatEqnFDM.hpp:207-217 / PennesBioheatEqnFDM.hpp:155-167 */
+                    double v = uo[m];
+                    for (int p = 0; p < g->dim; ++p) {
+                        const double s = uo[m - stride[p]] + uo[m + stride[p]] - 2.0 * uo[m];
+                        v += g->tau * coeff_a * s / (g->h[p] * g->h[p]);
+                    }
+                    if (use_perf) v -= g->tau * perf_q1 * perf_w * uo[m];
+                    v += g->tau * (1.0 / rho_c) * known_at(f_src, m, t_old);
+                    un[m] = v;
+                }
+            }
+        }
+        double* tmp = uo; uo = un; un = tmp;
+    }
+    if (uo != u) memcpy(u, uo, nn * sizeof(double));
+    free(w);
+    return 0;
+}
+
+int orc_pennes_mri(const orc_grid* g, double rho, double c, double k,
+                   double rho_b, double c_b, double omega, double t_blood,
+                   const double* q, const double* g_bdry, int nsteps,
+                   double* u, int nthreads)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const size_t nn = n_total(g);
+    double* w = (double*)malloc(nn * sizeof(double));
+    if (!w) return -1;
+    const long stride[3] = {1, nx, (long)nx * ny};
+    set_threads(nthreads);
+    double* uo = u;
+    double* un = w;
+    for (int t = 1; t <= nsteps; ++t) {
+#pragma omp parallel for schedule(static)
+        for (int kk = 0; kk < nz; ++kk) {
+            for (int j = 0; j < ny; ++j) {
+                for (int i = 0; i < nx; ++i) {
+                    const size_t m = IDX(i, j, kk, nx, ny);
+                    if (orc_is_border(g, i, j, kk)) {
+                        un[m] = g_bdry ? g_bdry[m] : 0.0;
+                        continue;
+                    }
+                    /* MRIDataPBHEqnFDM.hpp:156-168 */
+                    double v = uo[m];
+                    for (int p = 0; p < g->dim; ++p) {
+                        v += g->tau * (k / (rho * c))
+                             * (uo[m - stride[p]] + uo[m + stride[p]] - 2.0 * uo[m])
+                             / (g->h[p] * g->h[p]);
+                    }
+                    v += g->tau * ((rho_b * c_b) / (rho * c)) * omega * (t_blood - uo[m]);
+                    v += g->tau * (1.0 / (rho * c)) * (q ? q[m] : 0.0);
+                    un[m] = v;
+                }
+            }
+        }
+        double* tmp = uo; uo = un; un = tmp;
+    }
+    if (uo != u) memcpy(u, uo, nn * sizeof(double));
+    free(w);
+    return 0;
+}
+
+int orc_stencil_width_one(const orc_grid* g, int nsteps, double* u,
+                          int nthreads)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const size_t nn = n_total(g);
+    double* w = (double*)malloc(nn * sizeof(double));
+    if (!w) return -1;
+    const long stride[3] = {1, nx, (long)nx * ny};
+    const int ndir = 2 * g->dim;
+    set_threads(nthreads);
+    double* uo = u;
+    double* un = w;
+    for (int t = 1; t <= nsteps; ++t) {
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nz; ++k) {
+            for (int j = 0; j < ny; ++j) {
+                for (int i = 0; i < nx; ++i) {
+                    const int idx[3] = {i, j, k};
+                    const size_t m = IDX(i, j, k, nx, ny);
+                    double v = uo[m]; /* copy-before-update */
+                    if (!orc_is_border(g, i, j, k)) {
+                        /* HeatEqnFdmStencilWidthOne.hpp:124-131 */
+                        for (int pp = 0; pp < ndir; ++pp) {
+                            const long off = (pp % 2 == 0) ? -stride[pp / 2] : stride[pp / 2];
+                            v += uo[m + off];
+                        }
+                        v *= (2.0 / (2 * g->dim + 1));
+                    } else {
+                        /* HeatEqnFdmStencilWidthOne.hpp:140-162: at a face in
+                         * direction pp, mirror from the opposite neighbour. */
+                        const double correction = pow(2.0, t - 1);
+                        for (int pp = 0; pp < ndir; ++pp) {
+                            const int p = pp / 2;
+                            const int at_edge = (pp % 2 == 0) ? (idx[p] == 0) : (idx[p] == g->n[p] - 1);
+                            if (at_edge) {
+                                const long off = (pp % 2 == 0) ? stride[p] : -stride[p];
+                                const double sgn = pow(-1.0, pp);
+                                v = uo[m] + uo[m + off] - sgn * correction;
+                            }
+                        }
+                    }
+                    un[m] = v;
+                }
+            }
+        }
+        double* tmp = uo; uo = un; un = tmp;
+    }
+    if (uo != u) memcpy(u, uo, nn * sizeof(double));
+    free(w);
+    return 0;
+}
+
+int orc_stencil_width_var(const orc_grid* g, int bw, int nsteps, double* u,
+                          int nthreads)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const size_t nn = n_total(g);
+    double* w = (double*)malloc(nn * sizeof(double));
+    if (!w) return -1;
+    const long stride[3] = {1, nx, (long)nx * ny};
+    set_threads(nthreads);
+    double* uo = u;
+    double* un = w;
+    for (int t = 1; t <= nsteps; ++t) {
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nz; ++k) {
+            for (int j = 0; j < ny; ++j) {
+                for (int i = 0; i < nx; ++i) {
+                    const int idx[3] = {i, j, k};
+                    const size_t m = IDX(i, j, k, nx, ny);
+                    /* HeatEqnFdmStencilWidthVar.hpp:127-163 (inner and border) */
+                    double sum = 0.0;
+                    int cc = 0;
+                    int nadd = 1;
+                    for (int p = 0; p < g->dim; ++p) {
+                        const int d_start = idx[p];
+                        const int d_end = g->n[p] - 1 - idx[p];
+                        const int min_s = d_start < bw ? d_start : bw;
+                        for (int rr = 1; rr <= min_s; ++rr) {
+                            sum += uo[m - rr * stride[p]];
+                            cc -= rr;
+                        }
+                        const int min_e = d_end < bw ? d_end : bw;
+                        for (int rr = 1; rr <= min_e; ++rr) {
+                            sum += uo[m + rr * stride[p]];
+                            cc += rr;
+                        }
+                        nadd += min_s + min_e;
+                    }
+                    un[m] = 2.0 + (sum + uo[m] - cc) / nadd;
+                }
+            }
+        }
+        double* tmp = uo; uo = un; un = tmp;
+    }
+    if (uo != u) memcpy(u, uo, nn * sizeof(double));
+    free(w);
+    return 0;
+}
+
+void orc_err_linf(const double* u, const double* exact, size_t n,
+                  double* err, double* max_exact)
+{
+    double e = 0.0, mx = 0.0;
+    for (size_t i = 0; i < n; ++i) {
+        const double d = fabs(u[i] - exact[i]);
+        if (d > e || d != d) e = (d != d) ? INFINITY : d;
+        const double a = fabs(exact[i]);
+        if (a > mx) mx = a;
+    }
+    *err = e;
+    *max_exact = mx;
+}
+
+/* ---- Flux-form variable-conductivity heat and its adjoint. ------------- */
+
+static void kheat_step(const orc_grid* g, const double* k, const double* uo,
+                       double* un)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const long stride[3] = {1, nx, (long)nx * ny};
+#pragma omp parallel for schedule(static)
+    for (int kk = 0; kk < nz; ++kk) {
+        for (int j = 0; j < ny; ++j) {
+            for (int i = 0; i < nx; ++i) {
+                const size_t m = IDX(i, j, kk, nx, ny);
+                if (orc_is_border(g, i, j, kk)) { un[m] = uo[m]; continue; }
+                double v = uo[m];
+                for (int p = 0; p < g->dim; ++p) {
+                    const double c = g->tau / (g->h[p] * g->h[p]);
+                    const double kp = 0.5 * (k[m] + k[m + stride[p]]);
+                    const double km = 0.5 * (k[m] + k[m - stride[p]]);
+                    v += c * (kp * (uo[m + stride[p]] - uo[m]) - km * (uo[m] - uo[m - stride[p]]));
+                }
+                un[m] = v;
+            }
+        }
+    }
+}
+
+int orc_kheat_forward(const orc_grid* g, const double* k, int nsteps,
+                      double* u, double* traj, int nthreads)
+{
+    const size_t nn = n_total(g);
+    double* w = (double*)malloc(nn * sizeof(double));
+    if (!w) return -1;
+    set_threads(nthreads);
+    if (traj) memcpy(traj, u, nn * sizeof(double));
+    double* uo = u;
+    double* un = w;
+    for (int t = 1; t <= nsteps; ++t) {
+        kheat_step(g, k, uo, un);
+        if (traj) memcpy(traj + (size_t)t * nn, un, nn * sizeof(double));
+        double* tmp = uo; uo = un; un = tmp;
+    }
+    if (uo != u) memcpy(u, uo, nn * sizeof(double));
+    free(w);
+    return 0;
+}
+
+int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
+                      const double* traj, const double* target,
+                      double* grad_k, double* grad_u0, double* j_out,
+                      int nthreads)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const size_t nn = n_total(g);
+    const long stride[3] = {1, nx, (long)nx * ny};
+    double* lam = (double*)malloc(nn * sizeof(double));
+    double* lam2 = (double*)malloc(nn * sizeof(double));
+    double* lt = (double*)malloc(nn * sizeof(double)); /* lambda masked to inner */
+    if (!lam || !lam2 || !lt) { free(lam); free(lam2); free(lt); return -1; }
+    set_threads(nthreads);
+    const double* uT = traj + (size_t)nsteps * nn;
+    double jsum = 0.0;
+    for (size_t m = 0; m < nn; ++m) {
+        lam[m] = uT[m] - target[m];
+        jsum += 0.5 * lam[m] * lam[m];
+        grad_k[m] = 0.0;
+    }
+    for (int t = nsteps - 1; t >= 0; --t) {
+        const double* un = traj + (size_t)t * nn; /* state the step t -> t+1 read */
+#pragma omp parallel for schedule(static)
+        for (int kk = 0; kk < nz; ++kk)
+            for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) {
+                    const size_t m = IDX(i, j, kk, nx, ny);
+                    lt[m] = orc_is_border(g, i, j, kk) ? 0.0 : lam[m];
+                }
+#pragma omp parallel for schedule(static)
+        for (int kk = 0; kk < nz; ++kk) {
+            for (int j = 0; j < ny; ++j) {
+                for (int i = 0; i < nx; ++i) {
+                    const int idx[3] = {i, j, kk};
+                    const size_t m = IDX(i, j, kk, nx, ny);
+                    const int border = orc_is_border(g, i, j, kk);
+                    /* lambda_t = M^T lambda_{t+1} */
+                    double v = lam[m];
+                    double gk = 0.0;
+                    for (int p = 0; p < g->dim; ++p) {
+                        const double c = g->tau / (g->h[p] * g->h[p]);
+                        const int has_m = idx[p] > 0;
+                        const int has_p = idx[p] < g->n[p] - 1;
+                        const double lm = has_m ? lt[m - stride[p]] : 0.0;
+                        const double lp = has_p ? lt[m + stride[p]] : 0.0;
+                        const double kpv = has_p ? 0.5 * (k[m] + k[m + stride[p]]) : 0.0;
+                        const double kmv = has_m ? 0.5 * (k[m] + k[m - stride[p]]) : 0.0;
+                        const double dup = has_p ? un[m + stride[p]] - un[m] : 0.0;
+                        const double dum = has_m ? un[m - stride[p]] - un[m] : 0.0;
+                        if (border) {
+                            v += c * (kmv * lm + kpv * lp);
+                        } else {
+                            v += c * (kpv * (lp - lt[m]) + kmv * (lm - lt[m]));
+                        }
+                        gk += 0.5 * c * (dup * (lt[m] - lp) + dum * (lt[m] - lm));
+                    }
+                    lam2[m] = v;
+                    grad_k[m] += gk;
+                }
+            }
+        }
+        double* tmp = lam; lam = lam2; lam2 = tmp;
+    }
+    memcpy(grad_u0, lam, nn * sizeof(double));
+    *j_out = jsum;
+    free(lam); free(lam2); free(lt);
+    return 0;
+}

@@ -1,0 +1,110 @@
+/*
+ * CPU oracle for the ScaFES explicit update path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This header declares a plain-C restatement of the reference's per-node
+ * update sweeps.  It exists so that tests, the smoke check and the CPU
+ * baseline leg of the benchmark can check the CUDA path against the
+ * reference arithmetic.  Nothing in the product library links or calls it.
+ *
+ * Layout of every field array: the nodes of the global grid in Fortran order
+ * (x fastest), idx = i + nx*(j + ny*k), without ghost layers and without the
+ * trailing "time" slot the reference appends
+ * (src/ScaFES_DataField.hpp:948-953).
+ *
+ * Parity: pinned bit-for-bit against the reference itself, compiled from the
+ * untouched reference headers by oracle/Makefile into oracle/_ref/, on the
+ * system-test problems (tests/golden/ holds the vectors and the script).
+ */
+#ifndef SCAFES_ORACLE_H
+#define SCAFES_ORACLE_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Discrete domain + time axis (src/ScaFES_Grid.hpp:538-556,
+ * src/ScaFES_Parameters.hpp tau/timeIntervalStart). */
+typedef struct orc_grid {
+    int dim;            /* 1..3; unused axes have n = 1 */
+    int n[3];           /* nodes per axis */
+    double first[3];    /* coordinate of node 0 */
+    double last[3];     /* coordinate of node n-1 */
+    double h[3];        /* (last-first)/(n-1), filled by orc_grid_init */
+    double tau;         /* time step size */
+    double t_start;     /* timeIntervalStart */
+    int n_layers;       /* nLayersAtBorder (reference default 1) */
+} orc_grid;
+
+void orc_grid_init(orc_grid* g, int dim, const int* n, const double* first,
+                   const double* last, double tau, double t_start,
+                   int n_layers);
+double orc_time(const orc_grid* g, int timestep);
+int orc_is_border(const orc_grid* g, int i, int j, int k);
+void orc_coords(const orc_grid* g, int i, int j, int k, double* x);
+
+/* A known field evaluated at time(t); base may be NULL (=> 0).
+ *   form 0: base * (a + b*time)          (HeatEqnFDM TimeLinSpaceLin g, f)
+ *   form 1: base*a + b*(base*(1 + time)) (PennesBioheatEqnFDM/Dirichlet/
+ *           TimeLinSpaceLin/TimeLinSpaceLin.hpp:82-91 f, with
+ *           a = RHO*C and b = RHO_BLOOD*C_BLOOD*W) */
+typedef struct orc_known {
+    const double* base;
+    int form;
+    double a, b;
+} orc_known;
+
+/* Heat / Pennes (constant coefficients) with Dirichlet border.
+ * Inner nodes: tests/system/HeatEqnFDM/HeatEqnFDM.hpp:205-218 (perf_q1 == 0)
+ *   or tests/system/PennesBioheatEqnFDM/PennesBioheatEqnFDM.hpp:153-168.
+ * Border nodes: u = knownDf(1) at time(t)  (Dirichlet/Dirichlet.hpp:125-131).
+ * u holds the t = 0 iterate on entry and the t = nsteps iterate on exit.
+ * Returns 0 or a negative status. */
+int orc_heat_dirichlet(const orc_grid* g, double coeff_a, double rho_c,
+                       double perf_q1, double perf_w, int nsteps, double* u,
+                       orc_known f_src, orc_known g_bdry, int nthreads);
+
+/* Variable-coefficient Pennes bioheat (examples/MRIDataPBHEqnFDM/
+ * MRIDataPBHEqnFDM.hpp:143-169) with scalar rho, c, k, rho_b, c_b, omega,
+ * T_b and a stored heat-source field q; Dirichlet border value g_bdry. */
+int orc_pennes_mri(const orc_grid* g, double rho, double c, double k,
+                   double rho_b, double c_b, double omega, double t_blood,
+                   const double* q, const double* g_bdry, int nsteps,
+                   double* u, int nthreads);
+
+/* HeatEqnFdmStencilWidthOne (tests/system/HeatEqnFdmStencilWidthOne/
+ * HeatEqnFdmStencilWidthOne.hpp:120-163). */
+int orc_stencil_width_one(const orc_grid* g, int nsteps, double* u,
+                          int nthreads);
+
+/* HeatEqnFdmStencilWidthVar (tests/system/HeatEqnFdmStencilWidthVar/
+ * HeatEqnFdmStencilWidthVar.hpp:120-165) for one field of width bw. */
+int orc_stencil_width_var(const orc_grid* g, int bw, int nsteps, double* u,
+                          int nthreads);
+
+/* L-infinity norm of (u - exact) over all nodes, and max |exact|
+ * (src/ScaFES_DataField.hpp:1440-1530 computes the former). */
+void orc_err_linf(const double* u, const double* exact, size_t n,
+                  double* err, double* max_exact);
+
+/* Flux-form heat with conductivity field k (adjoint workload).
+ *   u'_i = u_i + sum_p (tau/h_p^2) [ kp (u_{i+p} - u_i) - km (u_i - u_{i-p}) ]
+ *   kp = 0.5 (k_i + k_{i+p}),  km = 0.5 (k_i + k_{i-p});  border nodes fixed.
+ * orc_kheat_forward advances u by nsteps; if traj != NULL it receives the
+ * nsteps+1 iterates (t = 0..nsteps) back to back. */
+int orc_kheat_forward(const orc_grid* g, const double* k, int nsteps,
+                      double* u, double* traj, int nthreads);
+
+/* Adjoint of orc_kheat_forward for J = 0.5 ||u_T - target||^2.
+ * traj holds the nsteps+1 forward iterates. Outputs dJ/dk and dJ/du0 and
+ * returns J in *j_out. */
+int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
+                      const double* traj, const double* target,
+                      double* grad_k, double* grad_u0, double* j_out,
+                      int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

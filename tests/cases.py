@@ -1,0 +1,99 @@
+"""Inputs of the golden cases for the CUDA path (test infrastructure).
+
+Each builder returns the scafes_cfg arguments and the host arrays to upload
+for one golden case of tests/golden/, with the known fields written in the
+affine-in-time form the C ABI takes (K(t) = K_A + time(t) * K_B).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+import masterthesis_gb300 as M
+import oracle as O
+from conftest import load_golden
+
+
+def unit_grid(n, last=(1.0, 1.0, 1.0), tau=0.0):
+    return O.make_grid(n, last=last, tau=tau)
+
+
+def lin_s(g):
+    """1 + x + y + z in the reference's evaluation order
+    (tests/system/HeatEqnFDM/Dirichlet/TimeLinSpaceLin/TimeLinSpaceLin.hpp:82-85)."""
+    x, y, z = O.coords(g)
+    return np.broadcast_to(((1.0 + x) + y) + z, (g.n[2], g.n[1], g.n[0])).copy()
+
+
+def heat_noise(name, precision):
+    d = load_golden(name)
+    n = tuple(int(v) for v in d["n"])
+    tau = float(d["tau"])
+    cfg = M.make_cfg(n, tau=tau, precision=precision, heat=(1.0, 1.0, 0.0))
+    return d, cfg, {M.FIELD_U: d["u0"]}
+
+
+def heat_timelin(precision):
+    d = load_golden("heat_timelin")
+    n = tuple(int(v) for v in d["n"])
+    T = int(d["nsteps"])
+    tau = float(d["t_end"]) / T
+    g = unit_grid(n, tau=tau)
+    S = lin_s(g)
+    cfg = M.make_cfg(n, tau=tau, precision=precision, heat=(1.0, 1.0, 0.0))
+    fields = {M.FIELD_U: S, M.FIELD_F_A: S, M.FIELD_G_A: S, M.FIELD_G_B: S,
+              M.FIELD_E_A: S, M.FIELD_E_B: S}
+    return d, cfg, fields
+
+
+def pennes_timelin(precision):
+    """Pennes system test: perfusion rho_b c_b W/(rho c) = 1 and
+    f(t) = S + S (1 + t) (PennesBioheatEqnFDM/Dirichlet/TimeLinSpaceLin)."""
+    d = load_golden("pennes_timelin")
+    n = tuple(int(v) for v in d["n"])
+    T = int(d["nsteps"])
+    tau = float(d["t_end"]) / T
+    g = unit_grid(n, tau=tau)
+    S = lin_s(g)
+    cfg = M.make_cfg(n, tau=tau, precision=precision, heat=(1.0, 1.0, 1.0))
+    fields = {M.FIELD_U: S, M.FIELD_F_A: 2.0 * S, M.FIELD_F_B: S, M.FIELD_G_A: S, M.FIELD_G_B: S,
+              M.FIELD_E_A: S, M.FIELD_E_B: S}
+    return d, cfg, fields
+
+
+def stencil_width_one(precision):
+    d = load_golden("stencil_width_one")
+    n = tuple(int(v) for v in d["n"])
+    k, j, i = np.meshgrid(np.arange(n[2]), np.arange(n[1]), np.arange(n[0]), indexing="ij")
+    c = 2.0 / 7.0
+    cfg = M.make_cfg(n, last=tuple(float(v) for v in d["last"]), tau=1.0 / int(d["nsteps"]),
+                     precision=precision, border=M.BORDER_MIRROR_POW2, c0=c, cp=(c, c, c), cf=0.0)
+    return d, cfg, {M.FIELD_U: (i + j + k).astype(np.float64)}
+
+
+def pennes_mri(precision):
+    """MRI-form Pennes with scalar coefficients as a 7-point star:
+    c_p = tau k/(rho c)/h_p^2, c0 = 1 - 2 sum c_p - tau (rho_b c_b/(rho c)) omega,
+    cf = tau/(rho c), F = q + rho_b c_b omega T_b."""
+    d = load_golden("pennes_mri")
+    n = tuple(int(v) for v in d["n"])
+    tau = float(d["tau"])
+    rho, c, k, rho_b, c_b, omega, t_b = (float(v) for v in d["params"])
+    cfg = M.make_cfg(n, tau=tau, precision=precision, heat=(k / (rho * c), rho * c,
+                                                           (rho_b * c_b) / (rho * c) * omega))
+    fields = {M.FIELD_U: d["u0"], M.FIELD_F_A: d["q"] + rho_b * c_b * omega * t_b,
+              M.FIELD_G_A: d["g"]}
+    return d, cfg, fields
+
+
+def run(cfg, fields, nsteps):
+    with M.Plain(cfg) as p:
+        for f, a in fields.items():
+            if f != M.FIELD_U:
+                p.upload(f, a)
+        p.upload(M.FIELD_U, fields[M.FIELD_U])
+        p.step(nsteps)
+        return p.download()
+
+
+def rel_err(a, ref):
+    return float(np.max(np.abs(a - ref)) / max(np.max(np.abs(ref)), 1e-300))

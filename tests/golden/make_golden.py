@@ -1,0 +1,101 @@
+"""Generates the golden vectors in tests/golden/ by running the reference.
+
+Each case runs one of the reference-driver programs in oracle/_ref/ -- the
+reference's own Problem::iterateOverTime() and, where the reference has one,
+its own system-test problem class, compiled from the untouched reference
+headers by ``make -C oracle ref`` -- and stores its inputs and final iterate.
+
+Run from the repository root (needs the reference checkout for the build):
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+The .npz files are committed; the GPU machine never runs this script.
+"""
+from __future__ import annotations
+
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+import oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def ijk(n):
+    k, j, i = np.meshgrid(np.arange(n[2]), np.arange(n[1]), np.arange(n[0]), indexing="ij")
+    return i, j, k
+
+
+def sine_noise(n, seed, amp=1e-3):
+    """sin(pi x) sin(pi y) sin(pi z) on the unit cube plus seeded uniform
+    noise in [-amp, amp] at inner nodes; border nodes 0."""
+    g = O.make_grid(n)
+    x, y, z = O.coords(g)
+    u0 = np.broadcast_to(np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z),
+                         (n[2], n[1], n[0])).copy()
+    border = O.border_mask(g)
+    if amp:
+        u0 += np.random.default_rng(seed).uniform(-amp, amp, u0.shape) * (~border)
+    u0[border] = 0.0
+    return u0
+
+
+def main():
+    tmp = tempfile.mkdtemp()
+    cases = {}
+
+    # tests/system/HeatEqnFdmStencilWidthOne/TESTMATRIX_RUN_3D.sh.in: 32^3, 20 steps,
+    # coordinates 0..1000.
+    n, T = (32, 32, 32), 20
+    r = O.run_ref("ref_stencil_width_one", n, T, tmp, last=(1000.0, 1000.0, 1000.0))
+    cases["stencil_width_one"] = dict(n=n, nsteps=T, last=(1000.0,) * 3, t_end=1.0, final=r)
+
+    # tests/system/HeatEqnFDM/Dirichlet/TimeLinSpaceLin/RUN_3D.sh.in: 8^3, 300 steps, t in [0,1].
+    n, T = (8, 8, 8), 300
+    r = O.run_ref("ref_heat_timelin", n, T, tmp)
+    cases["heat_timelin"] = dict(n=n, nsteps=T, t_end=1.0, final=r)
+
+    # tests/system/PennesBioheatEqnFDM/Dirichlet/TimeLinSpaceLin/RUN_3D.sh.in: 8^3, 300 steps.
+    r = O.run_ref("ref_pennes_timelin", n, T, tmp)
+    cases["pennes_timelin"] = dict(n=n, nsteps=T, t_end=1.0, final=r)
+
+    # tests/system/HeatEqnFdmStencilWidthVar/TESTMATRIX_RUN_3D.sh.in: 32^3, 20 steps.
+    n, T = (32, 32, 32), 20
+    r = O.run_ref("ref_stencil_width_var", n, T, tmp, nfields=3)
+    cases["stencil_width_var"] = dict(n=n, nsteps=T, t_end=1.0, final=r)
+
+    # Heat, sine mode + seeded noise, Dirichlet 0, tau = 0.9 of the stability limit.
+    for name, n, T, seed in (("heat_noise_16", (16, 16, 16), 50, 2), ("heat_noise_odd", (17, 9, 5), 30, 3)):
+        h2 = sum(1.0 / ((1.0 / (m - 1)) ** 2) for m in n)
+        tau = 0.9 / (2.0 * h2)
+        u0 = sine_noise(n, seed)
+        r = O.run_ref("ref_heat_dirichlet", n, T, tmp, tau=tau, t_end=tau * T, inputs=u0)
+        cases[name] = dict(n=n, nsteps=T, tau=tau, t_end=tau * T, u0=u0, final=r)
+
+    # Variable-coefficient Pennes (MRI form), Dirichlet 37, seeded data.
+    n, T = (12, 10, 9), 100
+    rng = np.random.default_rng(8)
+    shape = (n[2], n[1], n[0])
+    u0 = 37.0 + rng.uniform(-1.0, 1.0, shape)
+    q = rng.uniform(0.0, 10.0, shape)
+    gb = np.full(shape, 37.0)
+    params = np.array([1.0, 1.0, 0.5, 1.0, 1.0, 2e-3, 37.0])  # rho c k rho_b c_b omega T_b
+    tau = 1e-4
+    r = O.run_ref("ref_pennes_mri", n, T, tmp, tau=tau, t_end=tau * T,
+                  inputs=np.concatenate([u0.ravel(), q.ravel(), gb.ravel()]), extra=params)
+    cases["pennes_mri"] = dict(n=n, nsteps=T, tau=tau, t_end=tau * T, u0=u0, q=q, g=gb,
+                               params=params, final=r)
+
+    for name, c in cases.items():
+        arrays = {k: np.asarray(v) for k, v in c.items()}
+        np.savez_compressed(OUT / f"{name}.npz", **arrays)
+        print(f"{name}: {OUT / (name + '.npz')}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,82 @@
+"""Host-side checks of the C ABI that need no GPU: the library loads, it
+exports every function include/*.h declares, and invalid configurations are
+rejected with a status code (argument checking happens before any CUDA call).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    names = []
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(scafes_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    for expected in ("scafes_gpu_create", "scafes_gpu_upload", "scafes_gpu_step",
+                     "scafes_gpu_download", "scafes_gpu_destroy", "scafes_gpu_last_error"):
+        assert expected in names
+
+
+def test_library_exports_every_declared_symbol(native):
+    L = native.lib()
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def _create(M, **kw):
+    cfg = M.make_cfg((8, 8, 8), tau=1e-3, precision="f64", c0=0.4, cp=(0.1, 0.1, 0.1))
+    for k, v in kw.items():
+        if k == "n_nodes":
+            cfg.n_nodes[:] = v
+        else:
+            setattr(cfg, k, v)
+    h = C.c_void_p()
+    rc = M.lib().scafes_gpu_create(C.byref(cfg), C.byref(h))
+    return rc, h
+
+
+@pytest.mark.parametrize("kw,code", [
+    (dict(dim=2), -4),
+    (dict(n_nodes=(2, 8, 8)), -1),
+    (dict(n_nodes=(8, 8, 0)), -1),
+    (dict(n_layers_at_border=2), -4),
+    (dict(precision=17), -4),
+    (dict(border=9), -4),
+])
+def test_invalid_config_rejected(native, kw, code):
+    rc, h = _create(native, **kw)
+    assert rc == code
+    assert not h.value
+    assert native.lib().scafes_last_error()  # a message is recorded
+
+
+def test_null_arguments(native):
+    L = native.lib()
+    h = C.c_void_p()
+    assert L.scafes_gpu_create(None, C.byref(h)) == -1
+    assert L.scafes_gpu_step(None, 1) == -1
+    assert L.scafes_gpu_upload(None, 0, None, 0) == -1
+    assert L.scafes_gpu_download(None, 0, None, 0) == -1
+    L.scafes_gpu_destroy(None)  # no-op
+
+
+def test_heat_coeffs_helper(native):
+    M = native
+    n, tau = (11, 21, 31), 1e-5
+    cfg = M.make_cfg(n, last=(1.0, 2.0, 3.0), tau=tau, heat=(0.7, 2.0, 0.25))
+    h = [(l - 0.0) / (m - 1) for l, m in zip((1.0, 2.0, 3.0), n)]
+    cp = [tau * 0.7 / (hh * hh) for hh in h]
+    assert list(cfg.cp) == pytest.approx(cp, rel=1e-15)
+    assert cfg.c0 == pytest.approx(1.0 - 2.0 * sum(cp) - tau * 0.25, rel=1e-15)
+    assert cfg.cf == pytest.approx(tau / 2.0, rel=1e-15)

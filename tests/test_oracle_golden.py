@@ -1,0 +1,125 @@
+"""The CPU oracle against the golden vectors made by the reference itself.
+
+The golden vectors (tests/golden/, made by make_golden.py) are the final
+iterates of the reference's own Problem::iterateOverTime() on its system-test
+problems.  The C restatement must reproduce them bit for bit.  Where the
+reference-driver programs are built (oracle/_ref, this container only), a
+fresh reference run at another size is compared too.
+"""
+from __future__ import annotations
+
+import tempfile
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import load_golden
+
+
+def test_stencil_width_one_bit_exact():
+    d = load_golden("stencil_width_one")
+    n, T = tuple(d["n"]), int(d["nsteps"])
+    g = O.make_grid(n, last=tuple(d["last"]), tau=1.0 / T)
+    k, j, i = np.meshgrid(*(np.arange(v) for v in n[::-1]), indexing="ij")
+    u = O.stencil_width_one(g, (i + j + k).astype(np.float64), T)
+    assert np.array_equal(u, d["final"])
+    # HeatEqnFdmStencilWidthOne.hpp:39-40: f^n = 2^n (i+j+k) exactly.
+    assert np.array_equal(u, 2.0 ** T * (i + j + k))
+
+
+def test_stencil_width_var_bit_exact():
+    d = load_golden("stencil_width_var")
+    n, T = tuple(d["n"]), int(d["nsteps"])
+    g = O.make_grid(n, tau=1.0 / T)
+    k, j, i = np.meshgrid(*(np.arange(v) for v in n[::-1]), indexing="ij")
+    u0 = (i + j + k).astype(np.float64)
+    for bw in range(3):
+        u = O.stencil_width_var(g, u0, bw, T)
+        assert np.array_equal(u, d["final"][bw])
+        assert np.array_equal(u, u0 + 2.0 * T)  # exact solution i+j+k+2n
+
+
+@pytest.mark.parametrize("name,pennes", [("heat_timelin", False), ("pennes_timelin", True)])
+def test_timelin_bit_exact(name, pennes):
+    d = load_golden(name)
+    n, T = tuple(d["n"]), int(d["nsteps"])
+    g = O.make_grid(n, tau=float(d["t_end"]) / T)
+    x, y, z = O.coords(g)
+    S = np.broadcast_to(((1.0 + x) + y) + z, (n[2], n[1], n[0])).copy()
+    if pennes:
+        u = O.heat_dirichlet(g, S * 1.0, T, perf_q1=1.0, perf_w=1.0, f_base=S, f_form=1,
+                             f_a=1.0, f_b=1.0, g_base=S, g_a=1.0, g_b=1.0)
+    else:
+        u = O.heat_dirichlet(g, S * 1.0, T, f_base=S, g_base=S, g_a=1.0, g_b=1.0)
+    assert np.array_equal(u, d["final"])
+    exact = S * (1.0 + O.lib().orc_time(g, T))
+    assert np.max(np.abs(u - exact)) / np.max(np.abs(exact)) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["heat_noise_16", "heat_noise_odd"])
+def test_heat_noise_bit_exact(name):
+    d = load_golden(name)
+    n, T = tuple(d["n"]), int(d["nsteps"])
+    g = O.make_grid(n, tau=float(d["tau"]))
+    assert np.array_equal(O.heat_dirichlet(g, d["u0"], T), d["final"])
+
+
+def test_pennes_mri_bit_exact():
+    d = load_golden("pennes_mri")
+    n, T = tuple(d["n"]), int(d["nsteps"])
+    g = O.make_grid(n, tau=float(d["tau"]))
+    u = O.pennes_mri(g, d["u0"], T, *d["params"], d["q"], d["g"])
+    assert np.array_equal(u, d["final"])
+
+
+def test_oracle_threads_deterministic():
+    d = load_golden("heat_noise_16")
+    g = O.make_grid(tuple(d["n"]), tau=float(d["tau"]))
+    a = O.heat_dirichlet(g, d["u0"], 20, nthreads=1)
+    b = O.heat_dirichlet(g, d["u0"], 20, nthreads=4)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.skipif(not O.ref_available("ref_heat_dirichlet"),
+                    reason="reference-driver programs not built here (oracle/_ref)")
+def test_fresh_reference_run_other_size():
+    n, T = (11, 13, 7), 25
+    h2 = sum((m - 1) ** 2 for m in n)
+    tau = 0.9 / (2.0 * h2)
+    g = O.make_grid(n, tau=tau)
+    rng = np.random.default_rng(11)
+    u0 = rng.uniform(-1, 1, (n[2], n[1], n[0]))
+    u0[O.border_mask(g)] = 0.0
+    with tempfile.TemporaryDirectory() as tmp:
+        r = O.run_ref("ref_heat_dirichlet", n, T, tmp, tau=tau, t_end=tau * T, inputs=u0)
+    assert np.array_equal(O.heat_dirichlet(g, u0, T), r)
+
+
+def test_kheat_adjoint_matches_finite_differences():
+    """The oracle's own adjoint (no reference counterpart: the reference
+    only has ADOL-C forward mode) against central differences."""
+    n, T = (9, 8, 7), 12
+    h2 = sum((m - 1) ** 2 for m in n)
+    g = O.make_grid(n, tau=0.2 / (2.0 * h2))
+    rng = np.random.default_rng(5)
+    shape = (n[2], n[1], n[0])
+    k = np.exp(0.3 * rng.standard_normal(shape))
+    u0 = rng.uniform(-1, 1, shape)
+    target = rng.uniform(-1, 1, shape)
+    _, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
+    J, gk, gu = O.kheat_adjoint(g, k, traj, target)
+
+    def J_of(kk, uu):
+        uT = O.kheat_forward(g, kk, uu, T)
+        return 0.5 * float(np.sum((uT - target) ** 2))
+
+    assert abs(J - J_of(k, u0)) <= 1e-12 * abs(J)
+    for seed in range(3):
+        dk = np.random.default_rng(100 + seed).standard_normal(shape)
+        du = np.random.default_rng(200 + seed).standard_normal(shape)
+        eps = 1e-6
+        fd_k = (J_of(k + eps * dk, u0) - J_of(k - eps * dk, u0)) / (2 * eps)
+        fd_u = (J_of(k, u0 + eps * du) - J_of(k, u0 - eps * du)) / (2 * eps)
+        assert abs(fd_k - np.sum(gk * dk)) <= 1e-6 * max(abs(fd_k), 1e-12)
+        assert abs(fd_u - np.sum(gu * du)) <= 1e-6 * max(abs(fd_u), 1e-12)

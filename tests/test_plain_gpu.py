@@ -1,0 +1,169 @@
+"""Parity of the plain sweep (C ABI, CUDA) with the reference.
+
+Small cases compare against the golden vectors the reference produced
+(tests/golden/) and against the CPU oracle run live; the full-size cases
+check size-independent properties.
+
+Tolerances (relative max-norm, max|a-b| / max|b|):
+  f64   : 1e-12  (the reference's FP64 arithmetic up to FMA contraction and
+                  precomputed coefficients)
+  f32x2 : 1e-12  (compensated FP32 pairs, ~48 significant bits)
+  f32   : 2e-5   (plain FP32; reported, not an FP64-accuracy claim)
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import cases
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"f64": 1e-12, "f32x2": 1e-12, "f32": 2e-5}
+PRECS = ["f64", "f32x2", "f32"]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("name", ["heat_noise_16", "heat_noise_odd"])
+def test_heat_noise_golden(gpu, name, prec):
+    d, cfg, fields = cases.heat_noise(name, prec)
+    u = cases.run(cfg, fields, int(d["nsteps"]))
+    assert cases.rel_err(u, d["final"]) <= TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_heat_timelin_golden(gpu, prec):
+    d, cfg, fields = cases.heat_timelin(prec)
+    M = gpu
+    T = int(d["nsteps"])
+    with M.Plain(cfg) as p:
+        for f, a in fields.items():
+            p.upload(f, a)
+        p.step(T)
+        u = p.download()
+        err, mx = p.err_linf()
+    assert cases.rel_err(u, d["final"]) <= TOL[prec]
+    # compErrLinf against the exact solution (1+t)(1+sum x): round-off only.
+    assert err / mx <= 10 * TOL[prec]
+    assert mx == pytest.approx(float(np.max(np.abs(d["final"]))), rel=1e-12)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_pennes_timelin_golden(gpu, prec):
+    d, cfg, fields = cases.pennes_timelin(prec)
+    u = cases.run(cfg, fields, int(d["nsteps"]))
+    assert cases.rel_err(u, d["final"]) <= TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_stencil_width_one_golden(gpu, prec):
+    d, cfg, fields = cases.stencil_width_one(prec)
+    u = cases.run(cfg, fields, int(d["nsteps"]))
+    assert cases.rel_err(u, d["final"]) <= TOL[prec]
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_pennes_mri_golden(gpu, prec):
+    d, cfg, fields = cases.pennes_mri(prec)
+    u = cases.run(cfg, fields, int(d["nsteps"]))
+    assert cases.rel_err(u, d["final"]) <= TOL[prec]
+
+
+@pytest.mark.parametrize("n", [(3, 3, 3), (4, 3, 5), (33, 7, 65), (5, 40, 9), (64, 17, 3), (31, 33, 35)])
+def test_ragged_shapes_vs_oracle(gpu, n):
+    M = gpu
+    rng = np.random.default_rng(sum(n))
+    shape = (n[2], n[1], n[0])
+    h2 = sum((m - 1) ** 2 for m in n)
+    tau = 0.9 / (2.0 * h2)
+    g = O.make_grid(n, tau=tau)
+    u0 = rng.uniform(-1.0, 1.0, shape)
+    gA = rng.uniform(-1.0, 1.0, shape)
+    fA = rng.uniform(-1.0, 1.0, shape)
+    T = 17
+    ref = O.heat_dirichlet(g, u0, T, coeff_a=1.0, rho_c=2.0, f_base=fA, g_base=gA)
+    for prec in PRECS:
+        cfg = M.make_cfg(n, tau=tau, precision=prec, heat=(1.0, 2.0, 0.0))
+        u = cases.run(cfg, {M.FIELD_F_A: fA, M.FIELD_G_A: gA, M.FIELD_U: u0}, T)
+        assert cases.rel_err(u, ref) <= TOL[prec], prec
+
+
+def test_config1_heat_64_full_size_vs_oracle(gpu):
+    """64^3, 200 steps, u0 = sin sin sin, tau = 0.9 h^2/6: against the oracle
+    and against the analytic decay exp(-3 pi^2 t) u0 (discretisation error)."""
+    M = gpu
+    n, T = (64, 64, 64), 200
+    h = 1.0 / 63
+    tau = 0.9 * h * h / 6.0
+    g = O.make_grid(n, tau=tau)
+    x, y, z = O.coords(g)
+    u0 = np.broadcast_to(np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z), (64, 64, 64)).copy()
+    u0[O.border_mask(g)] = 0.0
+    ref = O.heat_dirichlet(g, u0, T)
+    exact = np.exp(-3.0 * np.pi ** 2 * tau * T) * u0
+    for prec in ("f64", "f32x2"):
+        cfg = M.make_cfg(n, tau=tau, precision=prec, heat=(1.0, 1.0, 0.0))
+        u = cases.run(cfg, {M.FIELD_U: u0}, T)
+        assert cases.rel_err(u, ref) <= 1e-12, prec
+        assert cases.rel_err(u, exact) <= 2e-4, prec
+
+
+def test_step_counter_and_restart(gpu):
+    M = gpu
+    d, cfg, fields = cases.heat_noise("heat_noise_16", "f64")
+    with M.Plain(cfg) as p:
+        p.upload(M.FIELD_U, fields[M.FIELD_U])
+        p.step(20)
+        p.step(30)
+        assert p.timestep() == 50
+        a = p.download()
+        p.upload(M.FIELD_U, fields[M.FIELD_U])
+        assert p.timestep() == 0
+        p.step(50)
+        b = p.download()
+    assert np.array_equal(a, b)
+    assert np.array_equal(a, d["final"]) or cases.rel_err(a, d["final"]) <= 1e-12
+
+
+def test_state_errors(gpu):
+    M = gpu
+    cfg = M.make_cfg((8, 8, 8), tau=1e-3, heat=(1.0, 1.0, 0.0))
+    with M.Plain(cfg) as p:
+        with pytest.raises(M.ScafesError) as e:
+            p.step(1)
+        assert e.value.code == -3
+        with pytest.raises(M.ScafesError) as e:
+            p.download()
+        assert e.value.code == -3
+        with pytest.raises(ValueError):
+            p.upload(M.FIELD_U, np.zeros(10))
+        import ctypes as C
+        bad = np.zeros(10)
+        rc = M.lib().scafes_gpu_upload(p.h, M.FIELD_U, bad.ctypes.data_as(C.POINTER(C.c_double)), 10)
+        assert rc == -1
+        rc = M.lib().scafes_gpu_upload(p.h, 99, bad.ctypes.data_as(C.POINTER(C.c_double)), 512)
+        assert rc == -1
+
+
+def test_config2_heat_512_f32x2_matches_f64(gpu):
+    """Full size of the large heat workload (512^3, sine + seeded noise,
+    1000 steps): the compensated FP32-pair path against the FP64 path on the
+    same inputs, within the FP64 bar; both against the analytic decay of the
+    sine mode within discretisation + noise error."""
+    M = gpu
+    n, T = (512, 512, 512), 1000
+    h = 1.0 / 511
+    tau = 0.9 * h * h / 6.0
+    g = O.make_grid(n, tau=tau)
+    x, y, z = O.coords(g)
+    u0 = np.broadcast_to(np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z), (512, 512, 512)).copy()
+    border = O.border_mask(g)
+    u0 += np.random.default_rng(2).uniform(-1e-3, 1e-3, u0.shape) * (~border)
+    u0[border] = 0.0
+    out = {}
+    for prec in ("f64", "f32x2"):
+        cfg = M.make_cfg(n, tau=tau, precision=prec, heat=(1.0, 1.0, 0.0))
+        out[prec] = cases.run(cfg, {M.FIELD_U: u0}, T)
+    assert cases.rel_err(out["f32x2"], out["f64"]) <= 1e-12
+    assert np.all(np.abs(out["f64"]) <= np.max(np.abs(u0)) * (1 + 1e-12))  # maximum principle
