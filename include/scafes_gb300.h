@@ -102,6 +102,8 @@ typedef struct scafes_cfg {
     int n_layers_at_border;  /* must be 1 (reference default) */
     int precision;           /* enum scafes_precision */
     int border;              /* enum scafes_border */
+    int tile;                /* sweep tile variant 1..4, 0 = default
+                                (see scafes_gpu_autotune) */
     double c0;               /* centre coefficient */
     double cp[3];            /* pair coefficient per axis */
     double cf;               /* source coefficient (0 disables F) */
@@ -137,6 +139,16 @@ int scafes_gpu_step(scafes_handle* h, int n_steps);
 /* Copies the current iterate (or another slot) back to the host; n as for
  * upload.  Synchronises the handle's stream. */
 int scafes_gpu_download(scafes_handle* h, int field, double* host, size_t n);
+
+/* No counterpart in the reference (its node loop has no tunables): times
+ * n_steps sweeps with each tile variant of the sweep kernel (32 x BY CTA
+ * tile, R rows per thread) on the uploaded problem, keeps the fastest for
+ * later scafes_gpu_step calls and returns it (1-based) in *chosen and the
+ * per-variant ms per step in ms_per_tile[4] (may be NULL).  The iterate and
+ * the step counter are restored afterwards.  Allocates one temporary copy
+ * of the iterate. */
+int scafes_gpu_autotune(scafes_handle* h, int n_steps, int* chosen,
+                        float* ms_per_tile);
 
 /* Number of steps taken since the last upload of the unknown field. */
 int scafes_gpu_timestep(const scafes_handle* h, int* t);

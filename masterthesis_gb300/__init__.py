@@ -41,7 +41,7 @@ class Cfg(C.Structure):
     _fields_ = [("dim", C.c_int), ("n_nodes", C.c_int * 3), ("coord_first", C.c_double * 3),
                 ("coord_last", C.c_double * 3), ("tau", C.c_double), ("t_start", C.c_double),
                 ("n_layers_at_border", C.c_int), ("precision", C.c_int), ("border", C.c_int),
-                ("c0", C.c_double), ("cp", C.c_double * 3), ("cf", C.c_double),
+                ("tile", C.c_int), ("c0", C.c_double), ("cp", C.c_double * 3), ("cf", C.c_double),
                 ("stream", C.c_void_p)]
 
 
@@ -63,6 +63,7 @@ def lib() -> C.CDLL:
         L.scafes_gpu_upload.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_step.argtypes = [vp, C.c_int]
+        L.scafes_gpu_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
         L.scafes_gpu_timestep.argtypes = [vp, C.POINTER(C.c_int)]
         L.scafes_gpu_err_linf.argtypes = [vp, dp, dp]
         L.scafes_gpu_last_step_ms.argtypes = [vp, C.POINTER(C.c_float)]
@@ -89,7 +90,7 @@ def _dp(a: np.ndarray):
 
 def make_cfg(n, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), tau=0.0, t_start=0.0,
              precision="f64", border=BORDER_DIRICHLET, c0=None, cp=None, cf=0.0,
-             heat=None, stream=None) -> Cfg:
+             heat=None, stream=None, tile=0) -> Cfg:
     """Builds a scafes_cfg.  ``heat=(coeff_a, rho_c, perf)`` fills the heat /
     Pennes coefficients via scafes_star7_heat_coeffs; otherwise give c0/cp/cf."""
     c = Cfg()
@@ -101,6 +102,7 @@ def make_cfg(n, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), tau=0.0, t_start=0.
     c.n_layers_at_border = 1
     c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     c.border = border
+    c.tile = tile
     c.stream = stream
     if heat is not None:
         _check(lib().scafes_star7_heat_coeffs(C.byref(c), *heat))
@@ -138,6 +140,14 @@ class Plain:
 
     def step(self, n_steps: int):
         _check(lib().scafes_gpu_step(self.h, n_steps), self.h)
+
+    def autotune(self, n_steps: int = 20):
+        """Picks the fastest sweep tile variant on this problem; returns
+        (chosen 1-based variant, ms per step of each variant)."""
+        chosen = C.c_int()
+        ms = (C.c_float * 4)()
+        _check(lib().scafes_gpu_autotune(self.h, n_steps, C.byref(chosen), ms), self.h)
+        return chosen.value, list(ms)
 
     def timestep(self) -> int:
         t = C.c_int()

@@ -11,6 +11,7 @@
 #include <string>
 
 #include "star7.cuh"
+#include "tma.cuh"
 #include "../../include/scafes_gb300.h"
 
 using namespace scafes;
@@ -40,6 +41,10 @@ struct scafes_handle {
     Layout L;
     size_t esz = 0;
     void* u[2] = {nullptr, nullptr};
+    CUtensorMap tm[2][STAR7_NUM_TILES];   // TMA descriptors of u[0], u[1] per tile
+    bool tm_ok[2][STAR7_NUM_TILES] = {};
+    int tile = 0;                         // tile variant of the sweep
+    int* status = nullptr;                // device status word of the kernels
     int cur = 0;
     void* fld[SCAFES_FIELD_COUNT] = {};   // known slots (U slot unused here)
     bool has[SCAFES_FIELD_COUNT] = {};
@@ -105,6 +110,9 @@ static int validate(const scafes_cfg* c) {
         return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: precision %d not supported", c->precision);
     if (c->border != SCAFES_BORDER_DIRICHLET && c->border != SCAFES_BORDER_MIRROR_POW2)
         return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: border kind %d not supported", c->border);
+    if (c->tile < 0 || c->tile > STAR7_NUM_TILES)
+        return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_create: tile=%d out of range [0, %d]", c->tile,
+                    STAR7_NUM_TILES);
     return SCAFES_OK;
 }
 
@@ -112,6 +120,7 @@ extern "C" void scafes_gpu_destroy(scafes_handle* h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (int i = 0; i < 2; ++i) cudaFree(h->u[i]);
+    cudaFree(h->status);
     for (int i = 0; i < SCAFES_FIELD_COUNT; ++i) cudaFree(h->fld[i]);
     cudaFree(h->stage);
     cudaFree(h->red);
@@ -152,6 +161,11 @@ extern "C" int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out) {
         if ((e = cudaMemsetAsync(h->u[i], 0, bytes, h->stream)) != cudaSuccess)
             return bail(SCAFES_ERR_CUDA, "cudaMemset(u)", e);
     }
+    h->tile = cfg->tile > 0 ? cfg->tile - 1 : star7_default_tile(h->L);
+    if ((e = cudaMalloc(&h->status, sizeof(int))) != cudaSuccess)
+        return bail(SCAFES_ERR_NOMEM, "cudaMalloc(status)", e);
+    if ((e = cudaMemsetAsync(h->status, 0, sizeof(int), h->stream)) != cudaSuccess)
+        return bail(SCAFES_ERR_CUDA, "cudaMemset(status)", e);
     if ((e = cudaEventCreate(&h->ev0)) != cudaSuccess) return bail(SCAFES_ERR_CUDA, "cudaEventCreate", e);
     if ((e = cudaEventCreate(&h->ev1)) != cudaSuccess) return bail(SCAFES_ERR_CUDA, "cudaEventCreate", e);
     int dev = 0, sms = 1;
@@ -240,6 +254,20 @@ static size_t n_nodes(const scafes_handle* h) {
     return (size_t)h->L.nx * h->L.ny * h->L.nz;
 }
 
+// Reads (and clears) the kernels' status word after the stream drained: a
+// bounded device wait that ran out is reported here instead of a hang.
+static int check_status(scafes_handle* h) {
+    int st = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (st != 0) {
+        cudaMemsetAsync(h->status, 0, sizeof(int), h->stream);
+        return fail(&h->err, SCAFES_ERR_TIMEOUT,
+                    "a sweep kernel gave up waiting for its TMA loads (status %d); results are invalid", st);
+    }
+    return SCAFES_OK;
+}
+
 extern "C" int scafes_gpu_upload(scafes_handle* h, int field, const double* host, size_t n) {
     if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_upload: handle is NULL");
     if (field < 0 || field >= SCAFES_FIELD_COUNT)
@@ -280,6 +308,8 @@ extern "C" int scafes_gpu_download(scafes_handle* h, int field, double* host, si
     if (field == SCAFES_FIELD_U) {
         if (!h->uploaded)
             return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_download: the unknown field was never uploaded");
+        rc = check_status(h);
+        if (rc) return rc;
         rc = d2h(h, h->u[h->cur], h->cfg.precision, host);
     } else {
         if (!h->has[field])
@@ -291,14 +321,28 @@ extern "C" int scafes_gpu_download(scafes_handle* h, int field, double* host, si
     return SCAFES_OK;
 }
 
-extern "C" int scafes_gpu_step(scafes_handle* h, int n_steps) {
-    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_step: handle is NULL");
-    if (n_steps < 0) return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_step: n_steps=%d < 0", n_steps);
-    if (!h->uploaded)
-        return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_step: upload the unknown field first");
+// TMA descriptor of buffer `buf` for tile variant `tile` (encoded on first use).
+static const CUtensorMap* tensor_map(scafes_handle* h, int buf, int tile) {
+    if (!h->tm_ok[buf][tile]) {
+        CUresult r = make_tensor_map_3d(&h->tm[buf][tile], h->u[buf], (int)h->esz, h->L.nx, h->L.ny, h->L.nz,
+                                        (size_t)h->L.pitch * h->esz, (size_t)h->L.plane * h->esz,
+                                        star7_box_width(h->cfg.precision), star7_box_height(tile));
+        if (r != CUDA_SUCCESS) {
+            fail(&h->err, SCAFES_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+            return nullptr;
+        }
+        h->tm_ok[buf][tile] = true;
+    }
+    return &h->tm[buf][tile];
+}
+
+static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
     Star7Launch a;
     a.precision = h->cfg.precision;
     a.border = h->cfg.border;
+    a.tile = tile;
+    for (int b = 0; b < 2; ++b)
+        if (!tensor_map(h, b, tile)) return SCAFES_ERR_CUDA;
     a.L = h->L;
     a.fa = h->has[SCAFES_FIELD_F_A] ? h->fld[SCAFES_FIELD_F_A] : nullptr;
     a.fb = h->has[SCAFES_FIELD_F_B] ? h->fld[SCAFES_FIELD_F_B] : nullptr;
@@ -308,8 +352,10 @@ extern "C" int scafes_gpu_step(scafes_handle* h, int n_steps) {
     if (!h->has[SCAFES_FIELD_F_A] && h->has[SCAFES_FIELD_F_B])
         return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
                     "scafes_gpu_step: upload F_A (possibly zeros) when F_B is used");
-    CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
+    if (timed) CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
+    a.status = h->status;
     for (int s = 0; s < n_steps; ++s) {
+        a.tm_uo = &h->tm[h->cur][tile];
         a.uo = h->u[h->cur];
         a.un = h->u[h->cur ^ 1];
         a.time_old = h->cfg.t_start + h->t * h->cfg.tau;          // time(t)
@@ -321,9 +367,63 @@ extern "C" int scafes_gpu_step(scafes_handle* h, int n_steps) {
         h->cur ^= 1;
         h->t += 1;
     }
-    CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
-    h->timed = true;
-    h->launches = n_steps;
+    if (timed) {
+        CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
+        h->timed = true;
+        h->launches = n_steps;
+    }
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_step(scafes_handle* h, int n_steps) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_step: handle is NULL");
+    if (n_steps < 0) return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_step: n_steps=%d < 0", n_steps);
+    if (!h->uploaded)
+        return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_step: upload the unknown field first");
+    return step_impl(h, n_steps, h->tile, true);
+}
+
+extern "C" int scafes_gpu_autotune(scafes_handle* h, int n_steps, int* chosen, float* ms_per_tile) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_autotune: handle is NULL");
+    if (n_steps < 1) return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_autotune: n_steps=%d < 1", n_steps);
+    if (!h->uploaded)
+        return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_autotune: upload the unknown field first");
+    // Trial steps run on a copy: the iterate and the step counter are
+    // restored afterwards.
+    const size_t bytes = (size_t)h->L.size() * h->esz;
+    void* save = nullptr;
+    CUDA_TRY(h, cudaMalloc(&save, bytes));
+    const int t_save = h->t, cur_save = h->cur;
+    cudaError_t e = cudaMemcpyAsync(save, h->u[h->cur], bytes, cudaMemcpyDeviceToDevice, h->stream);
+    int best = h->tile, rc = SCAFES_OK;
+    float best_ms = 0.f;
+    for (int tile = 0; tile < STAR7_NUM_TILES && e == cudaSuccess && rc == SCAFES_OK; ++tile) {
+        rc = step_impl(h, 1, tile, false);  // warm-up (and first-use setup)
+        if (rc == SCAFES_OK) rc = step_impl(h, n_steps, tile, true);
+        float ms = 0.f;
+        if (rc == SCAFES_OK) {
+            e = cudaEventSynchronize(h->ev1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+        }
+        if (ms_per_tile) ms_per_tile[tile] = ms / n_steps;
+        if (rc == SCAFES_OK && e == cudaSuccess && (tile == 0 || ms < best_ms)) {
+            best_ms = ms;
+            best = tile;
+        }
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h->u[cur_save], save, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(save);
+    h->t = t_save;
+    h->cur = cur_save;
+    h->timed = false;
+    if (rc != SCAFES_OK) return rc;
+    if (e != cudaSuccess)
+        return fail(&h->err, SCAFES_ERR_CUDA, "scafes_gpu_autotune: %s", cudaGetErrorString(e));
+    rc = check_status(h);
+    if (rc) return rc;
+    h->tile = best;
+    if (chosen) *chosen = best + 1;
     return SCAFES_OK;
 }
 
@@ -441,5 +541,5 @@ extern "C" int scafes_gpu_err_linf(scafes_handle* h, double* err, double* max_re
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     *err = h->red_host[0];
     *max_ref = h->red_host[1];
-    return SCAFES_OK;
+    return check_status(h);
 }

@@ -2,23 +2,41 @@
 // kernels (sweep_star7.cu).
 #pragma once
 
+#include <cuda.h>
+
 #include "scafes_common.cuh"
 
 namespace scafes {
 
+// Number of CTA tile variants of the plain sweep (32 x BY columns, R rows
+// per thread): {8,1}, {16,2}, {32,4}, {16,4}.
+constexpr int STAR7_NUM_TILES = 4;
+
 // Coefficients of u_new = c0*u + sum_p cp*(u_{p-}+u_{p+}) + cf*F, in double
-// and split into FP32 hi/lo pairs for the compensated path.
+// and split into FP32 triples (hi + lo + lo2, ~72 bits) for the
+// compensated path.
 struct Star7Coeffs {
     double c0, cx, cy, cz, cf;
-    float c0h, c0l, cxh, cxl, cyh, cyl, czh, czl, cfh, cfl;
+    float c0h, c0l, c0ll, cxh, cxl, cxll, cyh, cyl, cyll, czh, czl, czll, cfh, cfl, cfll;
 };
 
 Star7Coeffs make_star7_coeffs(double c0, const double cp[3], double cf);
 
+// Width (elements) of the TMA box of the sweep for a precision: the 32-wide
+// tile plus a halo padded to 16 bytes on each side.
+int star7_box_width(int precision);
+// Height (rows) of the TMA box of tile variant `tile`.
+int star7_box_height(int tile);
+// Tile variant used when none is chosen: {32,4} on large grids, {8,1} else.
+int star7_default_tile(const Layout& L);
+
 struct Star7Launch {
     int precision;        // enum scafes_precision
     int border;           // enum scafes_border
+    int tile;             // tile variant 0 .. STAR7_NUM_TILES-1
     Layout L;
+    const CUtensorMap* tm_uo;  // TMA descriptor of the old iterate
+    int* status;          // device status word (0 = ok)
     const void* uo;       // old iterate (element type per precision)
     void* un;             // new iterate
     const void* fa;       // source F_A (element type per precision) or null

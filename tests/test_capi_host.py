@@ -53,6 +53,8 @@ def _create(M, **kw):
     (dict(n_layers_at_border=2), -4),
     (dict(precision=17), -4),
     (dict(border=9), -4),
+    (dict(tile=5), -1),
+    (dict(tile=-1), -1),
 ])
 def test_invalid_config_rejected(native, kw, code):
     rc, h = _create(native, **kw)

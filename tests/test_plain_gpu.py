@@ -89,6 +89,37 @@ def test_ragged_shapes_vs_oracle(gpu, n):
         assert cases.rel_err(u, ref) <= TOL[prec], prec
 
 
+@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+@pytest.mark.parametrize("prec", PRECS)
+def test_every_tile_variant(gpu, tile, prec):
+    """Each CTA tile variant (32xBY, R rows per thread) on ragged shapes,
+    including rows that end inside a thread's row block."""
+    M = gpu
+    for name in ("heat_noise_odd", "heat_noise_16"):
+        d, cfg, fields = cases.heat_noise(name, prec)
+        cfg.tile = tile
+        u = cases.run(cfg, fields, int(d["nsteps"]))
+        assert cases.rel_err(u, d["final"]) <= TOL[prec], name
+    d, cfg, fields = cases.stencil_width_one(prec)
+    cfg.tile = tile
+    u = cases.run(cfg, fields, int(d["nsteps"]))
+    assert cases.rel_err(u, d["final"]) <= TOL[prec]
+
+
+def test_autotune_restores_state(gpu):
+    M = gpu
+    d, cfg, fields = cases.heat_noise("heat_noise_16", "f64")
+    with M.Plain(cfg) as p:
+        p.upload(M.FIELD_U, fields[M.FIELD_U])
+        p.step(10)
+        chosen, ms = p.autotune(5)
+        assert 1 <= chosen <= 4 and all(m > 0 for m in ms)
+        assert p.timestep() == 10
+        p.step(int(d["nsteps"]) - 10)
+        u = p.download()
+    assert cases.rel_err(u, d["final"]) <= 1e-12
+
+
 def test_config1_heat_64_full_size_vs_oracle(gpu):
     """64^3, 200 steps, u0 = sin sin sin, tau = 0.9 h^2/6: against the oracle
     and against the analytic decay exp(-3 pi^2 t) u0 (discretisation error)."""
