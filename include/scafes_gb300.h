@@ -174,6 +174,28 @@ void scafes_gpu_destroy(scafes_handle* h);
  * (covers failures before a handle exists). */
 const char* scafes_last_error(void);
 
+/* No counterpart in the reference.  The same max-norm check as
+ * scafes_gpu_err_linf, for callers that must not allocate device memory at
+ * the point of the call -- a time loop being recorded into a CUDA graph, a
+ * serving loop that forbids cudaMalloc after start-up (it can synchronise
+ * the device and fail under memory pressure), or a host whose device memory
+ * all comes from its own pool.  It allocates nothing: u and exact are
+ * caller-owned device arrays of n doubles, out is a caller-owned device
+ * array of 2 doubles that receives max|u - exact| and max|exact|, and the
+ * partial maxima live in a fixed 256 KiB array in the library's device
+ * image, which every GPU that loads the library holds until the process
+ * exits.  n may be at most SCAFES_ERR_LINF_NOALLOC_MAX_N; larger n is
+ * rejected with SCAFES_ERR_ARG and a message in scafes_last_error().  The
+ * call is asynchronous on `stream` (NULL = legacy default stream).  The
+ * first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, which may load the module), so make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU (e.g. on two streams without ordering) race on it and
+ * give wrong results. */
+#define SCAFES_ERR_LINF_NOALLOC_MAX_N (16384LL * 32768LL)
+int scafes_err_linf_noalloc(const double* u, const double* exact, long long n,
+                            double* out, void* stream);
+
 /* No counterpart in the reference: measures the FP64 and FP32 FMA issue
  * rates of the current GPU (G op/s) with CUDA events, the compute ceilings
  * the benchmark reports beside the HBM roofline. */

@@ -71,6 +71,12 @@ struct scafes_handle {
                         #call, cudaGetErrorString(e_), __FILE__, __LINE__);         \
     } while (0)
 
+namespace scafes {
+// Lets other translation units of the library record a message for
+// scafes_last_error().
+void set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+}  // namespace scafes
+
 extern "C" const char* scafes_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" const char* scafes_gpu_last_error(const scafes_handle* h) {
