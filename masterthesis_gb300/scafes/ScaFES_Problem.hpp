@@ -1,0 +1,551 @@
+// ScaFES::Problem -- drop-in CRTP base whose time loop runs on the GPU.
+//
+// Same constructor, callback names and signatures and accessors as the
+// reference's Problem<OWNPRBLM, CT, DIM> (src/ScaFES_Problem.hpp:313-324,
+// 433-449, 2418-2553), so a user problem class derived from it compiles
+// unchanged.  iterateOverTime() (reference :2559-2715) does:
+//
+//  1. evaluate the user's evalInner/evalBorder at time steps 0, 1, 2 on the
+//     host and store every known field affine in time, K = K_A + time*K_B
+//     (checked at step 2); this replaces the per-step evalKnownDfs
+//     (:3434-3485);
+//  2. run initInner/initBorder on the host for the initial iterate
+//     (evalInitPbPhase, :2755-2826);
+//  3. extract the update: updateInner<gpu::Sym> at probe nodes and
+//     updateBorder<gpu::Sym> at every global-border node, at two time
+//     steps, give linear forms that must match one of the device kernels --
+//     the 7-point star with a source, and the Dirichlet or StencilWidthOne
+//     mirror border -- otherwise the constructor-time contract is broken and
+//     iterateOverTime throws (there is no CPU fallback);
+//  4. upload, run all nTimesteps sweeps on the device through the C ABI
+//     (include/scafes_gb300.h), download the final iterate into the
+//     unknown data fields, and compute the max-norm error against the exact
+//     solution at the final step for fields with computeError set
+//     (DataField::compErrLinf, src/ScaFES_DataField.hpp:1440-1530).
+//
+// After the run the latest iterate is in mVectUnknownDfsDomOld, as after the
+// reference's final pointer swap (:2634-2635).
+#ifndef SCAFES_GB300_PROBLEM_HPP
+#define SCAFES_GB300_PROBLEM_HPP
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ScaFES_DataField.hpp"
+#include "ScaFES_Grid.hpp"
+#include "ScaFES_Ntuple.hpp"
+#include "ScaFES_Parameters.hpp"
+#include "ScaFES_Sym.hpp"
+#include "scafes_gb300.h"
+
+namespace ScaFES {
+
+template <class OWNPRBLM, typename CT = double, std::size_t DIM = 3>
+class Problem {
+public:
+    typedef CT value_type;
+    template <typename TT>
+    using ScaFES_VectDf = std::vector<ScaFES::DataField<TT, DIM>>;
+    typedef ScaFES::Ntuple<int, DIM> ScaFES_IntNtuple;
+
+    Problem(const ScaFES::Parameters& params, const ScaFES::GridGlobal<DIM>& gg, const bool& useLeapfrog,
+            const std::vector<std::string>& nameDatafield, const std::vector<int>& stencilWidth,
+            const std::vector<bool>& isKnownDf, const std::vector<int>& nLayers = std::vector<int>(),
+            const std::vector<CT>& defaultValue = std::vector<CT>(),
+            const std::vector<ScaFES::WriteHowOften>& writeToFile = std::vector<ScaFES::WriteHowOften>(),
+            const std::vector<bool>& computeError = std::vector<bool>(),
+            const std::vector<CT>& geomparamsInit = std::vector<CT>(),
+            const std::vector<bool>& checkConvergence = std::vector<bool>())
+        : mParams(params), mGG(gg), mUseLeapfrog(useLeapfrog), mNames(nameDatafield),
+          mStencilWidth(stencilWidth), mIsKnown(isKnownDf), mComputeError(computeError),
+          mVectParamsCurr(geomparamsInit) {
+        (void)nLayers; (void)defaultValue; (void)writeToFile; (void)checkConvergence;
+        // Argument checks of the reference constructor (:1400-1423).
+        const std::size_t nf = nameDatafield.size();
+        if (nf == 0 || stencilWidth.size() != nf || isKnownDf.size() != nf)
+            throw std::runtime_error("ScaFES::Problem: field name, stencil width and isKnownDf vectors differ in size");
+        if (!computeError.empty() && computeError.size() != nf)
+            throw std::runtime_error("ScaFES::Problem: computeError must have one entry per field");
+        if (DIM != 3) throw std::runtime_error("ScaFES::Problem: the GPU engine runs DIM = 3 problems");
+        mComputeError.resize(nf, false);
+        mN = gg.discreteDomain().nNodesTotal();
+        for (std::size_t f = 0; f < nf; ++f) {
+            if (!isKnownDf[f]) mUnknownIdx.push_back((int)f);
+        }
+        if (mUnknownIdx.empty()) throw std::runtime_error("ScaFES::Problem: no unknown data field");
+        const std::size_t nu = mUnknownIdx.size();
+        mKnownNewStore.assign(nf * mN, CT());
+        mKnownOldStore.assign(nf * mN, CT());
+        mUnknownNewStore.assign(nu * mN, CT());
+        mUnknownOldStore.assign(nu * mN, CT());
+        for (std::size_t f = 0; f < nf; ++f) {
+            mVectKnownDfsDomNew.emplace_back(nameDatafield[f], &mGG, mKnownNewStore.data() + f * mN, stencilWidth[f]);
+            mVectKnownDfsDomOld.emplace_back(nameDatafield[f], &mGG, mKnownOldStore.data() + f * mN, stencilWidth[f]);
+        }
+        for (std::size_t u = 0; u < nu; ++u) {
+            const int f = mUnknownIdx[u];
+            mVectUnknownDfsDomNew.emplace_back(nameDatafield[f], &mGG, mUnknownNewStore.data() + u * mN, stencilWidth[f]);
+            mVectUnknownDfsDomOld.emplace_back(nameDatafield[f], &mGG, mUnknownOldStore.data() + u * mN, stencilWidth[f]);
+        }
+    }
+
+    Problem(const Problem&) = delete;
+    Problem& operator=(const Problem&) = delete;
+    virtual ~Problem() {
+        if (mHandle) scafes_gpu_destroy(mHandle);
+    }
+
+    // ---- accessors of the reference interface (:2418-2553) -----------------
+    const ScaFES::Parameters& params() const { return mParams; }
+    const double& gridsize(const int& idx) const { return mGG.discreteDomain().gridsize(idx); }
+    const double& tau() const { return mParams.tau(); }
+    const int& nTimesteps() const { return mParams.nTimesteps(); }
+    const ScaFES::GridGlobal<DIM>& globalGrid() const { return mGG; }
+    const ScaFES_IntNtuple& nNodes() const { return mGG.discreteDomain().nNodes(); }
+    const int& nNodes(const int& dim) const { return mGG.discreteDomain().nNodes(dim); }
+    ScaFES::Ntuple<double, DIM> coordinates(const ScaFES_IntNtuple& n) const {
+        return mGG.discreteDomain().coordinates(n);
+    }
+    double time(const int& timestep) const { return mParams.timeIntervalStart() + timestep * mParams.tau(); }
+    ScaFES_IntNtuple connect(const ScaFES_IntNtuple& n, const int& dir) { return mGG.discreteDomain().neigh(n, dir); }
+    const std::vector<CT>& vectParamsCurr() const { return mVectParamsCurr; }
+    gpu::Known knownDf(const int& idx, const ScaFES_IntNtuple& n) const { return knownDfNew(idx, n); }
+    gpu::Known knownDfNew(const int& idx, const ScaFES_IntNtuple& n) const {
+        return gpu::Known((double)mVectKnownDfsDomNew[idx](n), gpu::Sym::known(idx, 0));
+    }
+    gpu::Known knownDfOld(const int& idx, const ScaFES_IntNtuple& n) const {
+        return gpu::Known((double)mVectKnownDfsDomOld[idx](n), gpu::Sym::known(idx, 1));
+    }
+    const ScaFES_VectDf<CT>& vectSol() const { return mVectKnownDfsDomNew; }
+
+    // ---- results of the last iterateOverTime -------------------------------
+    double errLinf(int field) const {
+        auto it = mErrLinf.find(field);
+        return it == mErrLinf.end() ? -1.0 : it->second;
+    }
+    double gpuMilliseconds() const { return mGpuMs; }
+    const std::string& gpuKernelSummary() const { return mSummary; }
+
+    void iterateOverTime();
+
+    // Runs the host part of iterateOverTime (known fields, initial iterate,
+    // stencil extraction) without touching the GPU and returns the device
+    // form the update maps to; throws if it maps to none.
+    const std::string& deviceForm() {
+        prepareDevice();
+        return mSummary;
+    }
+
+protected:
+    ScaFES::Parameters mParams;
+    const ScaFES::GridGlobal<DIM>& mGG;
+    bool mUseLeapfrog;
+    std::vector<std::string> mNames;
+    std::vector<int> mStencilWidth;
+    std::vector<bool> mIsKnown;
+    std::vector<bool> mComputeError;
+    std::vector<CT> mVectParamsCurr;
+    std::vector<int> mUnknownIdx;
+    long long mN = 0;
+    std::vector<CT> mKnownNewStore, mKnownOldStore, mUnknownNewStore, mUnknownOldStore;
+    ScaFES_VectDf<CT> mVectKnownDfsDomNew, mVectKnownDfsDomOld;
+    ScaFES_VectDf<CT> mVectUnknownDfsDomNew, mVectUnknownDfsDomOld;
+    std::map<std::string, double> mWallClockTimes;
+
+private:
+    struct Affine { std::vector<double> a, b; bool zero = true, timed = false; };
+    struct Form {
+        double c0 = 0, cp[3] = {0, 0, 0}, cst = 0;
+        std::map<std::pair<int, int>, double> known;  // (field, when) -> coefficient
+    };
+
+    bool isBorder(const ScaFES_IntNtuple& n) const {
+        const Grid<DIM>& g = mGG.discreteDomain();
+        const int L = mParams.nLayersAtBorder();
+        for (std::size_t p = 0; p < DIM; ++p)
+            if (n[p] < g.idxNodeFirst(p) + L || n[p] > g.idxNodeLast(p) - L) return true;
+        return false;
+    }
+
+    // Known fields of time step t into the "new" set (evalGlobInner/Border).
+    void evalKnownAt(int t) {
+        const Grid<DIM>& g = mGG.discreteDomain();
+        OWNPRBLM* self = static_cast<OWNPRBLM*>(this);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (long long m = 0; m < mN; ++m) {
+            const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
+            if (isBorder(n)) self->evalBorder(mVectKnownDfsDomNew, n, t);
+            else self->evalInner(mVectKnownDfsDomNew, n, t);
+        }
+    }
+
+    // Records one update callback at node n for time step t.
+    template <bool BORDER>
+    std::vector<gpu::Sym> record(const ScaFES_IntNtuple& n, int t, std::string& err) {
+        gpu::Recorder<DIM> rec;
+        rec.centre = n;
+        rec.grid = &mGG.discreteDomain();
+        const std::size_t nu = mUnknownIdx.size();
+        rec.out.resize(nu);
+        ScaFES_VectDf<gpu::Sym> vNew, vOld;
+        for (std::size_t u = 0; u < nu; ++u) {
+            const int f = mUnknownIdx[u];
+            vNew.emplace_back(mNames[f], &mGG, &rec, (int)u, true, mStencilWidth[f]);
+            vOld.emplace_back(mNames[f], &mGG, &rec, (int)u, false, mStencilWidth[f]);
+            // Copy-before-update: a node the callback leaves alone keeps its
+            // old value (src/ScaFES_Problem.hpp:5078-5082).
+            rec.out[u] = gpu::Sym::unknown((int)u, 0, 0, 0);
+        }
+        OWNPRBLM* self = static_cast<OWNPRBLM*>(this);
+        gpu::comparison_on_unknown() = false;
+        if (BORDER) self->template updateBorder<gpu::Sym>(vNew, vOld, n, t);
+        else self->template updateInner<gpu::Sym>(vNew, vOld, n, t);
+        err = rec.error;
+        if (err.empty() && gpu::comparison_on_unknown())
+            err = "update callback branches on the value of an unknown (not a linear stencil)";
+        return rec.out;
+    }
+
+    static std::string describe(const gpu::Sym& s) {
+        std::ostringstream os;
+        os.precision(17);
+        os << s.constant();
+        for (const auto& kv : s.terms()) {
+            const auto& k = kv.first;
+            if (k.kind == 0) os << " + " << kv.second << "*U" << k.a << "(" << k.b << "," << k.c << "," << k.d << ")";
+            else os << " + " << kv.second << "*K" << k.a << (k.b ? "(old)" : "(new)");
+        }
+        if (s.bad()) os << " [non-linear]";
+        return os.str();
+    }
+
+    static bool same(const gpu::Sym& a, const gpu::Sym& b) {
+        if (a.bad() || b.bad()) return false;
+        if (a.constant() != b.constant() || a.terms().size() != b.terms().size()) return false;
+        for (const auto& kv : a.terms()) {
+            bool found = false;
+            for (const auto& kw : b.terms())
+                if (kw.first == kv.first) { found = kw.second == kv.second; break; }
+            if (!found) return false;
+        }
+        return true;
+    }
+
+    // The inner form -> 7-point star coefficients + source terms.
+    Form starForm(const gpu::Sym& s) const {
+        if (s.bad()) throw std::runtime_error("ScaFES::Problem: updateInner is not linear in the unknowns: " + describe(s));
+        Form F;
+        F.cst = s.constant();
+        double cm[3] = {0, 0, 0}, cpp[3] = {0, 0, 0};
+        for (const auto& kv : s.terms()) {
+            const auto& k = kv.first;
+            if (k.kind == 1) { F.known[{k.a, k.b}] += kv.second; continue; }
+            if (k.a != 0) throw std::runtime_error("ScaFES::Problem: updateInner couples several unknown fields");
+            const int nz = (k.b != 0) + (k.c != 0) + (k.d != 0);
+            const int mag = std::abs(k.b) + std::abs(k.c) + std::abs(k.d);
+            if (nz == 0) { F.c0 += kv.second; continue; }
+            if (nz != 1 || mag != 1)
+                throw std::runtime_error("ScaFES::Problem: updateInner reaches beyond the 7-point star: " + describe(s));
+            const int p = k.b ? 0 : (k.c ? 1 : 2);
+            const int sgn = k.b + k.c + k.d;
+            (sgn < 0 ? cm : cpp)[p] += kv.second;
+        }
+        for (int p = 0; p < 3; ++p) {
+            if (cm[p] != cpp[p])
+                throw std::runtime_error("ScaFES::Problem: updateInner is not symmetric along an axis: " + describe(s));
+            F.cp[p] = cm[p];
+        }
+        return F;
+    }
+
+    void fitAffine(std::vector<Affine>& aff, std::vector<CT>& k0, std::vector<CT>& k1) {
+        const std::size_t nf = mNames.size();
+        const double t0 = time(0), tau = mParams.tau();
+        aff.assign(nf, Affine());
+        for (std::size_t f = 0; f < nf; ++f) {
+            Affine& A = aff[f];
+            A.a.resize(mN);
+            A.b.resize(mN);
+            for (long long m = 0; m < mN; ++m) {
+                const double v0 = (double)k0[f * mN + m], v1 = (double)k1[f * mN + m];
+                const double b = tau != 0.0 ? (v1 - v0) / tau : 0.0;
+                A.b[m] = b;
+                A.a[m] = v0 - t0 * b;
+                if (v0 != 0.0 || v1 != 0.0) A.zero = false;
+                if (b != 0.0) A.timed = true;
+            }
+        }
+    }
+
+    int precisionCode() const {
+        const std::string& p = mParams.gpuPrecision();
+        if (p == "f64") return SCAFES_PREC_F64;
+        if (p == "f32x2") return SCAFES_PREC_F32X2;
+        if (p == "f32") return SCAFES_PREC_F32;
+        throw std::runtime_error("ScaFES::Problem: unknown --gpuPrecision " + p);
+    }
+
+    void check(int rc) const {
+        if (rc != SCAFES_OK)
+            throw std::runtime_error(std::string("ScaFES::Problem (GPU): ") +
+                                     (mHandle ? scafes_gpu_last_error(mHandle) : scafes_last_error()));
+    }
+
+    void prepareDevice();
+
+    // What prepareDevice hands to the device run.
+    bool mPrepared = false;
+    scafes_cfg mCfg = {};
+    std::vector<double> mFa, mFb, mGa, mGb;
+    scafes_handle* mHandle = nullptr;
+    std::map<int, double> mErrLinf;
+    double mGpuMs = 0.0;
+    std::string mSummary;
+};
+
+template <class OWNPRBLM, typename CT, std::size_t DIM>
+void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
+    using clock = std::chrono::steady_clock;
+    if (mPrepared) return;
+    if (mUseLeapfrog)
+        throw std::runtime_error("ScaFES::Problem: leapfrog problems are not mapped to a device kernel yet");
+    if (mUnknownIdx.size() != 1)
+        throw std::runtime_error("ScaFES::Problem: the device path takes exactly one unknown data field");
+    const std::size_t nf = mNames.size();
+    const Grid<DIM>& g = mGG.discreteDomain();
+
+    // 1. Known fields at steps 0, 1, 2 -> affine in time.
+    auto t_eval = clock::now();
+    evalKnownAt(0);
+    std::vector<CT> k0 = mKnownNewStore;
+    evalKnownAt(1);
+    std::vector<CT> k1 = mKnownNewStore;
+    std::vector<Affine> aff;
+    fitAffine(aff, k0, k1);
+    evalKnownAt(2);
+    const double t2 = time(2);
+    for (std::size_t f = 0; f < nf; ++f) {
+        if (!mIsKnown[f]) continue;
+        for (long long m = 0; m < mN; ++m) {
+            const double pred = aff[f].a[m] + t2 * aff[f].b[m];
+            const double v = (double)mKnownNewStore[f * mN + m];
+            if (std::fabs(pred - v) > 1e-12 * std::max(1.0, std::fabs(v))) {
+                aff[f].timed = true;
+                aff[f].zero = false;
+                aff[f].a.clear();  // marks "not affine in time"
+                break;
+            }
+        }
+    }
+    mWallClockTimes["evalKnownDf"] += std::chrono::duration<double>(clock::now() - t_eval).count();
+
+    // 2. Initial iterate (time step 0) on the host.
+    auto t_init = clock::now();
+    std::copy(k0.begin(), k0.end(), mKnownNewStore.begin());
+    mKnownOldStore = k0;
+    {
+        OWNPRBLM* self = static_cast<OWNPRBLM*>(this);
+        for (auto& df : mVectUnknownDfsDomNew) df.time() = (CT)time(0);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (long long m = 0; m < mN; ++m) {
+            const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
+            if (isBorder(n)) self->template initBorder<CT>(mVectUnknownDfsDomNew, mVectParamsCurr, n, 0);
+            else self->template initInner<CT>(mVectUnknownDfsDomNew, mVectParamsCurr, n, 0);
+        }
+    }
+    mWallClockTimes["init"] += std::chrono::duration<double>(clock::now() - t_init).count();
+
+    // 3. Extract the update (known values of step 1 as "new", step 0 as "old").
+    auto t_rec = clock::now();
+    std::copy(k1.begin(), k1.end(), mKnownNewStore.begin());
+    std::string err;
+    std::vector<ScaFES_IntNtuple> probes;
+    {
+        ScaFES_IntNtuple lo(1), hi, mid;
+        for (std::size_t p = 0; p < DIM; ++p) { hi[p] = g.nNodes(p) - 2; mid[p] = g.nNodes(p) / 2; }
+        probes.push_back(mid);
+        probes.push_back(lo);
+        probes.push_back(hi);
+        unsigned s = 12345u;
+        for (int k = 0; k < 5; ++k) {
+            ScaFES_IntNtuple r;
+            for (std::size_t p = 0; p < DIM; ++p) {
+                s = s * 1103515245u + 12345u;
+                r[p] = 1 + (int)((s >> 8) % (unsigned)(g.nNodes(p) - 2));
+            }
+            probes.push_back(r);
+        }
+    }
+    gpu::Sym inner;
+    bool first = true;
+    for (int t = 1; t <= 2; ++t) {
+        for (const auto& n : probes) {
+            if (isBorder(n)) continue;
+            gpu::Sym s = record<false>(n, t, err)[0];
+            if (!err.empty()) throw std::runtime_error("ScaFES::Problem: " + err);
+            if (first) { inner = s; first = false; }
+            else if (!same(s, inner))
+                throw std::runtime_error("ScaFES::Problem: updateInner differs between nodes or time steps "
+                                         "(variable coefficients are not mapped to a device kernel): " +
+                                         describe(inner) + " vs " + describe(s));
+        }
+    }
+    if (first) throw std::runtime_error("ScaFES::Problem: the grid has no inner nodes");
+    Form F = starForm(inner);
+
+    // Border: every global-border node, at steps 1 and 2.
+    int border = -1, gfield = -1, gwhen = 0;
+    for (long long m = 0; m < mN; ++m) {
+        const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
+        if (!isBorder(n)) continue;
+        gpu::Sym s1 = record<true>(n, 1, err)[0];
+        if (!err.empty()) throw std::runtime_error("ScaFES::Problem: " + err);
+        gpu::Sym s2 = record<true>(n, 2, err)[0];
+        if (!err.empty()) throw std::runtime_error("ScaFES::Problem: " + err);
+        if (s1.bad()) throw std::runtime_error("ScaFES::Problem: updateBorder is not linear: " + describe(s1));
+        // Dirichlet: u_new = K_j.
+        const auto& tt = s1.terms();
+        if (tt.size() == 1 && tt[0].first.kind == 1 && tt[0].second == 1.0 && s1.constant() == 0.0 && same(s1, s2)) {
+            if (border == -1) { border = SCAFES_BORDER_DIRICHLET; gfield = tt[0].first.a; gwhen = tt[0].first.b; }
+            if (border == SCAFES_BORDER_DIRICHLET && gfield == tt[0].first.a && gwhen == tt[0].first.b) continue;
+        }
+        // StencilWidthOne mirror: u_new = u + u(opposite) + s*2^(t-1).
+        bool mirror = tt.size() == 2 && s1.constant() != 0.0 && s2.constant() == 2.0 * s1.constant() &&
+                      std::fabs(s1.constant()) == 1.0;
+        if (mirror) {
+            for (const auto& kv : tt)
+                if (kv.first.kind != 0 || kv.second != 1.0) mirror = false;
+        }
+        if (mirror) {
+            if (border == -1) border = SCAFES_BORDER_MIRROR_POW2;
+            if (border == SCAFES_BORDER_MIRROR_POW2) continue;
+        }
+        throw std::runtime_error("ScaFES::Problem: updateBorder at node has no device form: " + describe(s1));
+    }
+    if (border == -1) border = SCAFES_BORDER_DIRICHLET;
+    mWallClockTimes["record"] += std::chrono::duration<double>(clock::now() - t_rec).count();
+
+    // 4. Device run.
+    scafes_cfg cfg = {};
+    cfg.dim = 3;
+    for (int p = 0; p < 3; ++p) {
+        cfg.n_nodes[p] = g.nNodes(p);
+        cfg.coord_first[p] = g.coordNodeFirst()[p];
+        cfg.coord_last[p] = g.coordNodeLast()[p];
+    }
+    cfg.tau = mParams.tau();
+    cfg.t_start = mParams.timeIntervalStart();
+    cfg.n_layers_at_border = mParams.nLayersAtBorder();
+    cfg.precision = precisionCode();
+    cfg.border = border;
+    cfg.tile = mParams.gpuTile();
+    cfg.c0 = F.c0;
+    for (int p = 0; p < 3; ++p) cfg.cp[p] = F.cp[p];
+    // Source: F(t_old) = cst + sum_j b_j K_j(t_old or t_new).
+    std::vector<double> fa((std::size_t)mN, F.cst), fb;
+    bool has_f = F.cst != 0.0, has_fb = false;
+    for (const auto& kv : F.known) {
+        const int j = kv.first.first;
+        const bool is_new = kv.first.second == 0;
+        const double bj = kv.second;
+        const Affine& A = aff[j];
+        if (A.zero) continue;
+        if (A.a.empty())
+            throw std::runtime_error("ScaFES::Problem: known field " + mNames[j] +
+                                     " is not affine in time; the device path takes affine known fields");
+        has_f = true;
+        if (A.timed && fb.empty()) fb.assign((std::size_t)mN, 0.0);
+        for (long long m = 0; m < mN; ++m) {
+            fa[m] += bj * (A.a[m] + (is_new ? mParams.tau() * A.b[m] : 0.0));
+            if (A.timed) fb[m] += bj * A.b[m];
+        }
+        has_fb = has_fb || A.timed;
+    }
+    cfg.cf = has_f ? 1.0 : 0.0;
+    if (has_f) mFa.swap(fa);
+    if (has_fb) mFb.swap(fb);
+    if (border == SCAFES_BORDER_DIRICHLET && gfield >= 0 && !aff[gfield].zero) {
+        const Affine& A = aff[gfield];
+        if (A.a.empty())
+            throw std::runtime_error("ScaFES::Problem: border field " + mNames[gfield] + " is not affine in time");
+        mGa = A.a;
+        if (gwhen == 1)
+            for (long long m = 0; m < mN; ++m) mGa[m] -= mParams.tau() * A.b[m];
+        if (A.timed) mGb = A.b;
+    }
+    mCfg = cfg;
+    std::ostringstream os;
+    os << "star7 c0=" << cfg.c0 << " cp=(" << cfg.cp[0] << "," << cfg.cp[1] << "," << cfg.cp[2] << ")"
+       << " source=" << (has_f ? (has_fb ? "affine" : "static") : "none")
+       << " border=" << (border == SCAFES_BORDER_DIRICHLET ? "dirichlet" : "mirror");
+    mSummary = os.str();
+    mPrepared = true;
+}
+
+template <class OWNPRBLM, typename CT, std::size_t DIM>
+void Problem<OWNPRBLM, CT, DIM>::iterateOverTime() {
+    using clock = std::chrono::steady_clock;
+    auto t_all = clock::now();
+    prepareDevice();
+    const int T = mParams.nTimesteps();
+    scafes_cfg cfg = mCfg;
+    if (mHandle) { scafes_gpu_destroy(mHandle); mHandle = nullptr; }
+    check(scafes_gpu_create(&cfg, &mHandle));
+    if (!mFa.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_F_A, mFa.data(), mFa.size()));
+    if (!mFb.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_F_B, mFb.data(), mFb.size()));
+    if (!mGa.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_G_A, mGa.data(), mGa.size()));
+    if (!mGb.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_G_B, mGb.data(), mGb.size()));
+    std::vector<double> u0(mUnknownNewStore.begin(), mUnknownNewStore.end());
+    check(scafes_gpu_upload(mHandle, SCAFES_FIELD_U, u0.data(), u0.size()));
+    int tile = cfg.tile;
+    if (mParams.gpuAutotune()) check(scafes_gpu_autotune(mHandle, 5, &tile, nullptr));
+    auto t_upd = clock::now();
+    check(scafes_gpu_step(mHandle, T));
+    std::vector<double> uT((std::size_t)mN);
+    check(scafes_gpu_download(mHandle, SCAFES_FIELD_U, uT.data(), uT.size()));
+    mWallClockTimes["update"] += std::chrono::duration<double>(clock::now() - t_upd).count();
+    float ms = 0.f;
+    if (T > 0) check(scafes_gpu_last_step_ms(mHandle, &ms));
+    mGpuMs = ms;
+    for (long long m = 0; m < mN; ++m) {
+        mUnknownOldStore[m] = (CT)uT[m];
+        mUnknownNewStore[m] = (CT)uT[m];
+    }
+    for (auto& df : mVectUnknownDfsDomOld) df.time() = (CT)time(T);
+    for (auto& df : mVectUnknownDfsDomNew) df.time() = (CT)time(T);
+
+    // Max-norm error against the exact solution at the final step.
+    const int uf = mUnknownIdx[0];
+    if (mComputeError[uf]) {
+        auto t_err = clock::now();
+        evalKnownAt(T);
+        double e = 0.0;
+        for (long long m = 0; m < mN; ++m)
+            e = std::max(e, std::fabs((double)mUnknownOldStore[m] - (double)mKnownNewStore[uf * mN + m]));
+        mErrLinf[uf] = e;
+        mWallClockTimes["compErr"] += std::chrono::duration<double>(clock::now() - t_err).count();
+        std::cout << "ScaFES-GB300: Local Linf error (" << mNames[uf] << ", t=" << time(T) << ") = " << e << std::endl;
+    }
+    mWallClockTimes["iterate"] += std::chrono::duration<double>(clock::now() - t_all).count();
+    if (mParams.outputLevel() > 0) {
+        std::cout << "ScaFES-GB300: " << mSummary << "\n";
+        for (const auto& kv : mWallClockTimes)
+            std::cout << "ScaFES-GB300:   t(" << kv.first << ") = " << kv.second << " s\n";
+        std::cout << "ScaFES-GB300:   device sweeps: " << T << " steps in " << mGpuMs << " ms" << std::endl;
+    }
+}
+
+}  // namespace ScaFES
+#endif

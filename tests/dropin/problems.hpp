@@ -1,0 +1,206 @@
+// Problem classes written against the ScaFES callback interface (test
+// infrastructure for the drop-in Problem).  Each derives directly from
+// ScaFES::Problem and restates one of the reference's system-test problems:
+//   HeatLin    -- heat equation, Dirichlet border, exact solution
+//                 (1+t)(1+x+y+z)  (tests/system/HeatEqnFDM/Dirichlet/TimeLinSpaceLin)
+//   PennesLin  -- Pennes bioheat with perfusion, same exact solution
+//                 (tests/system/PennesBioheatEqnFDM/Dirichlet/TimeLinSpaceLin)
+//   MirrorPow2 -- the 2/7 averaging stencil with the mirrored border,
+//                 exact solution 2^n (i+j+k) (tests/system/HeatEqnFdmStencilWidthOne)
+//   HeatSine   -- heat equation, Dirichlet 0, u0 = sin(pi x) sin(pi y) sin(pi z)
+#pragma once
+
+#include <cmath>
+#include <vector>
+
+#include "ScaFES.hpp"
+
+template <typename CT, std::size_t DIM>
+class HeatLin : public ScaFES::Problem<HeatLin<CT, DIM>, CT, DIM> {
+    using Base = ScaFES::Problem<HeatLin<CT, DIM>, CT, DIM>;
+public:
+    using Base::Base;
+    const double RHO = 1.0, C = 1.0, LAMBDA = 1.0;
+    static double lin(const ScaFES::Ntuple<double, DIM>& x) {
+        double s = 1.0;
+        for (std::size_t p = 0; p < DIM; ++p) s += x[p];
+        return s;
+    }
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        const double s = lin(this->coordinates(n));
+        v[0](n) = s * (RHO * C);          // heat source f
+        v[1](n) = 0.0;                    // border value g (unused inside)
+        v[2](n) = s * (1.0 + this->time(t));  // exact solution
+    }
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        const double s = lin(this->coordinates(n));
+        v[0](n) = 0.0;
+        v[1](n) = s * (1.0 + this->time(t));
+        v[2](n) = v[1](n);
+    }
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        v[0](n) = lin(this->coordinates(n)) * (1.0 + this->time(t));
+    }
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>& o, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        initInner<TT>(v, o, n, t);
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        vNew[0](n) = vOld[0](n);
+        for (std::size_t p = 0; p < DIM; ++p)
+            vNew[0](n) += this->tau() * (LAMBDA / (RHO * C)) *
+                          (vOld[0](this->connect(n, 2 * p)) + vOld[0](this->connect(n, 2 * p + 1)) - 2.0 * vOld[0](n)) /
+                          (this->gridsize(p) * this->gridsize(p));
+        vNew[0](n) += this->tau() * (1.0 / (RHO * C)) * this->knownDfOld(0, n);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>&,
+                      const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        vNew[0](n) = this->knownDf(1, n);
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};
+
+template <typename CT, std::size_t DIM>
+class PennesLin : public ScaFES::Problem<PennesLin<CT, DIM>, CT, DIM> {
+    using Base = ScaFES::Problem<PennesLin<CT, DIM>, CT, DIM>;
+public:
+    using Base::Base;
+    const double RHO = 1.0, C = 1.0, LAMBDA = 1.0, RHO_B = 1.0, C_B = 1.0, W = 1.0;
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        const double s = HeatLin<CT, DIM>::lin(this->coordinates(n));
+        v[0](n) = s * (RHO * C) + RHO_B * C_B * W * (s * (1.0 + this->time(t)));
+        v[1](n) = 0.0;
+        v[2](n) = s * (1.0 + this->time(t));
+    }
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        const double s = HeatLin<CT, DIM>::lin(this->coordinates(n));
+        v[0](n) = 0.0;
+        v[1](n) = s * (1.0 + this->time(t));
+        v[2](n) = v[1](n);
+    }
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        v[0](n) = HeatLin<CT, DIM>::lin(this->coordinates(n)) * (1.0 + this->time(t));
+    }
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>& o, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        initInner<TT>(v, o, n, t);
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        vNew[0](n) = vOld[0](n);
+        for (std::size_t p = 0; p < DIM; ++p)
+            vNew[0](n) += this->tau() * (LAMBDA / (RHO * C)) *
+                          (vOld[0](this->connect(n, 2 * p)) + vOld[0](this->connect(n, 2 * p + 1)) - 2.0 * vOld[0](n)) /
+                          (this->gridsize(p) * this->gridsize(p));
+        vNew[0](n) -= this->tau() * ((RHO_B * C_B) / (RHO * C)) * W * vOld[0](n);
+        vNew[0](n) += this->tau() * (1.0 / (RHO * C)) * this->knownDfOld(0, n);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>&,
+                      const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        vNew[0](n) = this->knownDf(1, n);
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};
+
+template <typename CT, std::size_t DIM>
+class MirrorPow2 : public ScaFES::Problem<MirrorPow2<CT, DIM>, CT, DIM> {
+    using Base = ScaFES::Problem<MirrorPow2<CT, DIM>, CT, DIM>;
+public:
+    using Base::Base;
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        double s = 0.0;
+        for (std::size_t p = 0; p < DIM; ++p) s += n[p];
+        v[0](n) = s * std::pow(2.0, t);
+    }
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) { evalInner(v, n, t); }
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        v[0](n) = 0.0;
+        for (std::size_t p = 0; p < DIM; ++p) v[0](n) += n[p];
+    }
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>& o, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        initInner<TT>(v, o, n, t);
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        vNew[0](n) = vOld[0](n);
+        for (std::size_t d = 0; d < 2 * DIM; ++d) vNew[0](n) += vOld[0](this->connect(n, d));
+        vNew[0](n) *= 2.0 / (2 * DIM + 1);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                      const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        TT corr = std::pow(2.0, t - 1);
+        for (std::size_t d = 0; d < 2 * DIM; ++d) {
+            if (ScaFES::Ntuple<int, DIM>(-(int)(d + 1)) == this->connect(n, d)) {
+                const int opp = (d % 2 == 0) ? (int)d + 1 : (int)d - 1;
+                const double sgn = (d % 2 == 0) ? 1.0 : -1.0;
+                vNew[0](n) = vOld[0](n) + vOld[0](this->connect(n, opp)) - sgn * corr;
+            }
+        }
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};
+
+template <typename CT, std::size_t DIM>
+class HeatSine : public ScaFES::Problem<HeatSine<CT, DIM>, CT, DIM> {
+    using Base = ScaFES::Problem<HeatSine<CT, DIM>, CT, DIM>;
+public:
+    using Base::Base;
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        v[0](n) = 0.0;
+        v[1](n) = 0.0;
+    }
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) { evalInner(v, n, t); }
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        const ScaFES::Ntuple<double, DIM> x = this->coordinates(n);
+        double s = 1.0;
+        for (std::size_t p = 0; p < DIM; ++p) s *= std::sin(M_PI * x[p]);
+        v[0](n) = s;
+    }
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        v[0](n) = 0.0;
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        vNew[0](n) = vOld[0](n);
+        for (std::size_t p = 0; p < DIM; ++p)
+            vNew[0](n) += this->tau() * (vOld[0](this->connect(n, 2 * p)) + vOld[0](this->connect(n, 2 * p + 1)) - 2.0 * vOld[0](n)) /
+                          (this->gridsize(p) * this->gridsize(p));
+        vNew[0](n) += this->tau() * this->knownDfOld(0, n);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>&,
+                      const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        vNew[0](n) = this->knownDf(1, n);
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};

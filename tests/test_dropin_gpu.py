@@ -1,0 +1,60 @@
+"""The C++ drop-in ScaFES::Problem on the GPU: problem classes written
+against the ScaFES callback interface run iterateOverTime() through the C
+ABI and reproduce the reference's golden vectors (relative max-norm 1e-12)."""
+from __future__ import annotations
+
+import subprocess
+
+import numpy as np
+import pytest
+
+import cases
+import oracle as O
+from conftest import load_golden
+from dropin.build import HERE, compile_cpp
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def run_problem(gpu, tmp_path_factory):
+    return compile_cpp(HERE / "run_problem.cpp", tmp_path_factory.mktemp("dropin_gpu") / "run_problem")
+
+
+def run(exe, name, out, n, *opts):
+    res = subprocess.run([str(exe), name, str(out), *opts], capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stdout + res.stderr
+    return np.fromfile(out, dtype=np.float64).reshape(n[2], n[1], n[0]), res.stdout
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+@pytest.mark.parametrize("name,golden", [("heat_lin", "heat_timelin"), ("pennes_lin", "pennes_timelin")])
+def test_dropin_timelin_matches_reference(run_problem, tmp_path, name, golden, prec):
+    d = load_golden(golden)
+    n = tuple(int(v) for v in d["n"])
+    u, out = run(run_problem, name, tmp_path / "u.bin", n, f"--nNodes={n[0]}x{n[1]}x{n[2]}",
+                 f"--nTimesteps={int(d['nsteps'])}", f"--endtime={float(d['t_end'])!r}", f"--gpuPrecision={prec}")
+    assert cases.rel_err(u, d["final"]) <= 1e-12
+    assert "Local Linf error" in out
+
+
+def test_dropin_stencil_width_one_matches_reference(run_problem, tmp_path):
+    d = load_golden("stencil_width_one")
+    n = tuple(int(v) for v in d["n"])
+    u, _ = run(run_problem, "mirror_pow2", tmp_path / "u.bin", n, "--nNodes=32x32x32", "--nTimesteps=20",
+               "--coordNodeLast=1000x1000x1000", "--gpuAutotune=1")
+    assert cases.rel_err(u, d["final"]) <= 1e-12
+
+
+def test_dropin_heat_sine_config1_vs_oracle(run_problem, tmp_path):
+    n, T = (64, 64, 64), 200
+    h = 1.0 / 63
+    tau = 0.9 * h * h / 6.0
+    u, _ = run(run_problem, "heat_sine", tmp_path / "u.bin", n, "--nNodes=64x64x64", f"--nTimesteps={T}",
+               f"--tau={tau!r}")
+    g = O.make_grid(n, tau=tau)
+    x, y, z = O.coords(g)
+    u0 = np.broadcast_to(np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z), (64, 64, 64)).copy()
+    u0[O.border_mask(g)] = 0.0
+    ref = O.heat_dirichlet(g, u0, T)
+    assert cases.rel_err(u, ref) <= 1e-12
