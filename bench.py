@@ -53,6 +53,9 @@ def parse_args():
     ap.add_argument("--time-steps", type=int, default=1000)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=256)
+    ap.add_argument("--batch-time-steps", type=int, default=500)
     return ap.parse_args()
 
 
@@ -219,6 +222,47 @@ def cpu_sample_glups(n: int, target_s: float, max_sweeps: int = 50):
     return n ** 3 * sweeps / dt / 1e9, threads, sweeps, dt
 
 
+# ---- batched ensemble ---------------------------------------------------------
+
+def run_batched(M, args, dist: Dist, hbm_peak: float):
+    """Pennes ensemble (256 instances, sizes {32..160}^3 drawn by seed 8,
+    500 steps, FP64): all instances in one persistent launch per step with
+    the loop replayed from a CUDA graph, against one plain launch per
+    instance per step.  24 algorithmic bytes per node update (T read and
+    write, source read)."""
+    from masterthesis_gb300 import workloads as W
+    specs = W.pennes_ensemble(n_inst=args.batch_instances, seed=8)
+    T = args.batch_time_steps
+    out = {"workload": f"Pennes ensemble: {len(specs)} instances, sizes {{32,48,...,160}}^3 (seed 8), "
+                       f"FP64, {T} steps, Dirichlet 37, Gaussian source"}
+    for prec in ("f64", "f32x2"):
+        b = M.Batch([W.pennes_batch_instance(s) for s in specs], precision=prec)
+        try:
+            for i, s in enumerate(specs):
+                b.upload(i, M.FIELD_F_A, W.pennes_source(s))
+                b.upload(i, M.FIELD_U, np.full((s["n"][2], s["n"][1], s["n"][0]), W.T_ARTERIAL))
+            tile, ctas = b.autotune(5)
+            nodes = b.info()["nodes"]
+            b.step(T)                  # warm-up: captures the graph
+            dist.barrier()
+            b.step(T)
+            ms_b = dist.max(b.last_ms())
+            launches_b = b.info()["launches"]
+            b.step_looped(T)
+            ms_l = dist.max(b.last_ms())
+            launches_l = b.info()["launches"]
+        finally:
+            b.close()
+        lup = nodes * T
+        g_b = dist.world * lup / (ms_b * 1e-3) / 1e9
+        g_l = dist.world * lup / (ms_l * 1e-3) / 1e9
+        out[prec] = {"value": g_b, "unit": UNIT, "looped_value": g_l, "speedup_vs_looped": ms_l / ms_b,
+                     "hbm_frac": 24 * lup / (ms_b * 1e-3) / 1e9 / hbm_peak, "ms": ms_b, "looped_ms": ms_l,
+                     "nodes": nodes, "tile": tile, "ctas_per_sm": ctas, "launches": launches_b,
+                     "looped_launches": launches_l}
+    return out
+
+
 # ---- GPU arm ----------------------------------------------------------------
 
 def run_ours(args, dist: Dist):
@@ -330,6 +374,8 @@ def run_ours(args, dist: Dist):
         for prec in ("f32x2", "f32"):
             variants[prec]["rel_err_vs_f64"] = float(np.max(np.abs(finals[prec] - ref))) / scale
 
+    batched = None if args.no_batched else run_batched(M, args, dist, hbm_peak)
+
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
@@ -345,6 +391,8 @@ def run_ours(args, dist: Dist):
     }
     if variants:
         res["variants"] = variants
+    if batched:
+        res["batched"] = batched
     if clk:
         res["clocks"] = clk
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:

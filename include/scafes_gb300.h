@@ -174,6 +174,76 @@ void scafes_gpu_destroy(scafes_handle* h);
  * (covers failures before a handle exists). */
 const char* scafes_last_error(void);
 
+/* ---- batched ensembles --------------------------------------------------
+ *
+ * No counterpart in the reference, which solves one problem per process
+ * (its MCMC drivers, examples/MRIDataPBHEqnFDM/startMCMCFit.py, launch
+ * runs one after the other).  An ensemble holds many independent
+ * instances of the constant-coefficient 7-point update with a static
+ * source field and a constant Dirichlet border -- the Pennes bioheat update
+ * of examples/MRIDataPBHEqnFDM/MRIDataPBHEqnFDM.hpp:143-169 with scalar
+ * coefficients -- each with its own grid, time step and coefficients:
+ *   u_new = c0*u + sum_p cp[p]*(u_{p-}+u_{p+}) + cf*F   (inner nodes)
+ *   u_new = g_value                                     (border nodes)
+ * All instances advance together; one step of the whole ensemble is one
+ * launch of a persistent kernel that pulls (instance, tile, z-chunk) work
+ * items from a device queue, and the time loop is replayed from a CUDA
+ * graph. */
+typedef struct scafes_batch_instance {
+    int n_nodes[3];          /* nodes per axis, each in [3, 32767] */
+    double coord_first[3];
+    double coord_last[3];
+    double tau;              /* time step of this instance */
+    double c0, cp[3], cf;    /* star coefficients (scafes_batch_star7_coeffs) */
+    double g_value;          /* Dirichlet value on the global border */
+} scafes_batch_instance;
+
+typedef struct scafes_batch scafes_batch;
+
+/* Fills c0, cp, cf of one instance like scafes_star7_heat_coeffs:
+ * cp = tau*coeff_a/h_p^2, c0 = 1 - 2*sum cp - tau*perf, cf = tau/rho_c. */
+int scafes_batch_star7_coeffs(scafes_batch_instance* inst, double coeff_a,
+                              double rho_c, double perf);
+
+/* Allocates all instances (two iterates + the source field each, padded
+ * layout, one device pool) and their TMA descriptors and work lists. */
+int scafes_batch_create(const scafes_batch_instance* inst, int n_inst,
+                        int precision, void* stream, scafes_batch** out);
+
+/* Host <-> device copy of one instance's field: SCAFES_FIELD_U (the
+ * iterate; uploading it resets the step counter) or SCAFES_FIELD_F_A (the
+ * source F).  n = nodes of that instance.  Synchronises the stream. */
+int scafes_batch_upload(scafes_batch* b, int inst, int field,
+                        const double* host, size_t n);
+int scafes_batch_download(scafes_batch* b, int inst, int field,
+                          double* host, size_t n);
+
+/* Advances every instance by n_steps: one persistent launch per step, the
+ * whole loop recorded once per (n_steps, schedule) into a CUDA graph and
+ * replayed.  Asynchronous on the batch's stream. */
+int scafes_batch_step(scafes_batch* b, int n_steps);
+
+/* Advances every instance by n_steps with one plain sweep launch per
+ * instance per step (the schedule of running the instances one by one);
+ * for comparison with scafes_batch_step. */
+int scafes_batch_step_looped(scafes_batch* b, int n_steps);
+
+/* Times every tile variant x {occupancy, 1, 2, 4} CTAs per SM for n_steps
+ * batched steps, keeps the fastest (iterates restored afterwards). */
+int scafes_batch_autotune(scafes_batch* b, int n_steps, int* tile,
+                          int* ctas_per_sm);
+/* Sets the schedule directly: tile 1..4, ctas_per_sm 0 (= occupancy) .. 16. */
+int scafes_batch_set_schedule(scafes_batch* b, int tile, int ctas_per_sm);
+
+/* ms of the last scafes_batch_step / _step_looped call (CUDA events). */
+int scafes_batch_last_ms(const scafes_batch* b, float* ms);
+/* Work items per step, kernel launches of the last step call, schedule and
+ * total nodes of the ensemble. */
+int scafes_batch_info(const scafes_batch* b, int* n_items, int* launches,
+                      int* tile, int* ctas_per_sm, long long* n_nodes);
+const char* scafes_batch_last_error(const scafes_batch* b);
+void scafes_batch_destroy(scafes_batch* b);
+
 /* No counterpart in the reference.  The same max-norm check as
  * scafes_gpu_err_linf, for callers that must not allocate device memory at
  * the point of the call -- a time loop being recorded into a CUDA graph, a

@@ -45,6 +45,13 @@ class Cfg(C.Structure):
                 ("stream", C.c_void_p)]
 
 
+class BatchInstance(C.Structure):
+    """Mirror of ``struct scafes_batch_instance``."""
+    _fields_ = [("n_nodes", C.c_int * 3), ("coord_first", C.c_double * 3),
+                ("coord_last", C.c_double * 3), ("tau", C.c_double), ("c0", C.c_double),
+                ("cp", C.c_double * 3), ("cf", C.c_double), ("g_value", C.c_double)]
+
+
 _lib = None
 
 
@@ -73,6 +80,22 @@ def lib() -> C.CDLL:
         L.scafes_last_error.restype = C.c_char_p
         L.scafes_gpu_destroy.argtypes = [vp]
         L.scafes_gpu_destroy.restype = None
+        bi = C.POINTER(BatchInstance)
+        L.scafes_batch_star7_coeffs.argtypes = [bi, C.c_double, C.c_double, C.c_double]
+        L.scafes_batch_create.argtypes = [bi, C.c_int, C.c_int, vp, C.POINTER(vp)]
+        L.scafes_batch_upload.argtypes = [vp, C.c_int, C.c_int, dp, C.c_size_t]
+        L.scafes_batch_download.argtypes = [vp, C.c_int, C.c_int, dp, C.c_size_t]
+        L.scafes_batch_step.argtypes = [vp, C.c_int]
+        L.scafes_batch_step_looped.argtypes = [vp, C.c_int]
+        L.scafes_batch_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.scafes_batch_set_schedule.argtypes = [vp, C.c_int, C.c_int]
+        L.scafes_batch_last_ms.argtypes = [vp, C.POINTER(C.c_float)]
+        L.scafes_batch_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
+        L.scafes_batch_last_error.argtypes = [vp]
+        L.scafes_batch_last_error.restype = C.c_char_p
+        L.scafes_batch_destroy.argtypes = [vp]
+        L.scafes_batch_destroy.restype = None
         _lib = L
     return _lib
 
@@ -172,6 +195,92 @@ class Plain:
     def close(self):
         if self.h:
             lib().scafes_gpu_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _bcheck(rc: int, b=None):
+    if rc != 0:
+        L = lib()
+        msg = (L.scafes_batch_last_error(b) if b else L.scafes_last_error()) or b""
+        raise ScafesError(rc, msg.decode())
+
+
+def batch_instance(n, tau, coeff_a, rho_c=1.0, perf=0.0, g_value=0.0,
+                   first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0)) -> BatchInstance:
+    """One ensemble instance with star coefficients from the heat/Pennes
+    parameters (scafes_batch_star7_coeffs)."""
+    bi = BatchInstance()
+    bi.n_nodes[:] = list(n)
+    bi.coord_first[:] = list(first)
+    bi.coord_last[:] = list(last)
+    bi.tau = tau
+    bi.g_value = g_value
+    _bcheck(lib().scafes_batch_star7_coeffs(C.byref(bi), coeff_a, rho_c, perf))
+    return bi
+
+
+class Batch:
+    """An ensemble of independent instances advanced together (owns a
+    scafes_batch)."""
+
+    def __init__(self, instances, precision="f64", stream=None):
+        arr = (BatchInstance * len(instances))(*instances)
+        self.shapes = [(bi.n_nodes[2], bi.n_nodes[1], bi.n_nodes[0]) for bi in instances]
+        h = C.c_void_p()
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        _bcheck(lib().scafes_batch_create(arr, len(instances), prec, stream, C.byref(h)))
+        self.h = h
+
+    def upload(self, inst: int, field: int, arr: np.ndarray):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        _bcheck(lib().scafes_batch_upload(self.h, inst, field, _dp(a), a.size), self.h)
+
+    def download(self, inst: int, field: int = FIELD_U) -> np.ndarray:
+        a = np.empty(self.shapes[inst], dtype=np.float64)
+        _bcheck(lib().scafes_batch_download(self.h, inst, field, _dp(a), a.size), self.h)
+        return a
+
+    def step(self, n_steps: int):
+        _bcheck(lib().scafes_batch_step(self.h, n_steps), self.h)
+
+    def step_looped(self, n_steps: int):
+        _bcheck(lib().scafes_batch_step_looped(self.h, n_steps), self.h)
+
+    def autotune(self, n_steps: int = 5):
+        t, c = C.c_int(), C.c_int()
+        _bcheck(lib().scafes_batch_autotune(self.h, n_steps, C.byref(t), C.byref(c)), self.h)
+        return t.value, c.value
+
+    def set_schedule(self, tile: int, ctas_per_sm: int = 0):
+        _bcheck(lib().scafes_batch_set_schedule(self.h, tile, ctas_per_sm), self.h)
+
+    def last_ms(self) -> float:
+        v = C.c_float()
+        _bcheck(lib().scafes_batch_last_ms(self.h, C.byref(v)), self.h)
+        return v.value
+
+    def info(self) -> dict:
+        it, la, ti, ct, nn = C.c_int(), C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+        _bcheck(lib().scafes_batch_info(self.h, C.byref(it), C.byref(la), C.byref(ti), C.byref(ct),
+                                        C.byref(nn)), self.h)
+        return {"items": it.value, "launches": la.value, "tile": ti.value, "ctas_per_sm": ct.value,
+                "nodes": nn.value}
+
+    def close(self):
+        if self.h:
+            lib().scafes_batch_destroy(self.h)
             self.h = None
 
     def __enter__(self):

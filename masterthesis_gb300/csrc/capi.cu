@@ -354,6 +354,7 @@ static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
     a.fb = h->has[SCAFES_FIELD_F_B] ? h->fld[SCAFES_FIELD_F_B] : nullptr;
     a.ga = h->has[SCAFES_FIELD_G_A] ? (const double*)h->fld[SCAFES_FIELD_G_A] : nullptr;
     a.gb = h->has[SCAFES_FIELD_G_B] ? (const double*)h->fld[SCAFES_FIELD_G_B] : nullptr;
+    a.gconst = 0.0;
     a.c = make_star7_coeffs(h->cfg.c0, h->cfg.cp, h->cfg.cf);
     if (!h->has[SCAFES_FIELD_F_A] && h->has[SCAFES_FIELD_F_B])
         return fail(&h->err, SCAFES_ERR_UNSUPPORTED,

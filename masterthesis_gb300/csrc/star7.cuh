@@ -43,6 +43,7 @@ struct Star7Launch {
     const void* fb;       // source F_B or null
     const double* ga;     // border value G_A (double) or null
     const double* gb;     // border value G_B (double) or null
+    double gconst;        // border value when ga is null
     Star7Coeffs c;
     double time_old;      // time(t)   : F is read at the old time
     double time_new;      // time(t+1) : G is read at the new time

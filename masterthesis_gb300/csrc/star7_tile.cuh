@@ -1,0 +1,191 @@
+// One CTA tile of the 7-point sweep: a 32 x BY column tile marched through
+// the z-planes [z0, z1), fed by a ring of TMA-loaded shared-memory stages.
+// Shared by the plain sweep (one tile per CTA) and the batched ensemble
+// (a persistent CTA works through many tiles of many instances).
+//
+// Mapping: one elected thread streams the tile's planes (with a one-node
+// halo in x and y, x padded to 16 bytes) into an NSTAGE-deep ring of
+// stages with 3D TMA loads, each stage completing on its own mbarrier.
+// Each thread owns R consecutive rows of one column and keeps u(z-1),
+// u(z), u(z+1) of them in registers (the z-marching queue); y-neighbours
+// inside its rows come from registers, x-neighbours and the two outer
+// y-neighbours from the staged plane.  Out-of-domain halo cells are
+// zero-filled by the TMA unit.  Stores are row-contiguous per warp.
+#pragma once
+
+#include "star7_policies.cuh"
+#include "tma.cuh"
+#include "../../include/scafes_gb300.h"
+
+namespace scafes {
+
+constexpr int BX = 32;
+constexpr int NSTAGE = 8;  // power of two: stage/phase indices are shifts
+
+template <class T, int BY>
+struct Tile {
+    static constexpr int ESZ = (int)sizeof(T);
+    static constexpr int LP = 16 / ESZ;          // left halo padded to 16 bytes
+    static constexpr int W = BX + 2 * LP;        // box width (elements)
+    static constexpr int H = BY + 2;             // box height (rows)
+    static constexpr uint32_t TX_BYTES = W * H * ESZ;
+    static constexpr int STRIDE = ((W * H * ESZ + 127) / 128) * 128 / ESZ;  // elements per stage
+    static constexpr size_t SMEM = (size_t)NSTAGE * STRIDE * ESZ + NSTAGE * sizeof(uint64_t);
+};
+
+// Tile variants {BY, R}: CTA tile 32 x BY, R rows per thread.
+struct TileShape { int by, r; };
+constexpr TileShape kTiles[STAR7_NUM_TILES] = {{8, 1}, {16, 2}, {32, 4}, {16, 4}};
+
+// Everything one tile needs besides its position.
+template <class T>
+struct TileJob {
+    const CUtensorMap* tm;   // TMA descriptor of the old iterate
+    T* un;                   // new iterate
+    const T* fa;             // source F_A or null
+    const T* fb;             // source F_B or null
+    const double* ga;        // border value G_A or null (then gconst)
+    const double* gb;        // border value G_B or null
+    double gconst;           // border value when ga is null
+    Layout L;
+    double time_old, time_new, corr;
+};
+
+// Initialises the ring's mbarriers (thread 0) -- once per CTA.
+template <class T, int BY>
+__device__ __forceinline__ void ring_init(uint64_t* bar) {
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+}
+
+// Processes planes [z0, z1) of the tile at (x0, y0).  `base` counts the
+// planes this CTA has streamed through the ring so far (it fixes the stage
+// and phase of every plane); it is advanced by the planes this tile used.
+// Returns false (and records SCAFES_ERR_TIMEOUT) when a stage never
+// arrived; the caller must then stop.
+template <class P, bool HAS_F, int BORDER, int BY, int R>
+__device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, const Star7Coeffs& c,
+                                           int x0, int y0, int z0, int z1,
+                                           typename P::T* st, uint64_t* bar, uint32_t& base,
+                                           int* status) {
+    using T = typename P::T;
+    using G = Tile<T, BY>;
+    const Layout& L = J.L;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * BX + tx;
+    const int x = x0 + tx;
+    const int yb = y0 + ty * R;  // first row of this thread
+    const int rb = ty * R + 1;   // its row inside a stage
+    const int np = z1 - z0 + 2;  // planes z0-1 .. z1 (index p <-> z = z0 - 1 + p)
+    const uint32_t b0 = base;
+
+    if (tid == 0) {
+        const int pre = np < NSTAGE ? np : NSTAGE;
+        fence_proxy_async_smem();
+        for (int p = 0; p < pre; ++p) {
+            const uint32_t s = (b0 + p) & (NSTAGE - 1);
+            mbar_arrive_expect_tx(&bar[s], G::TX_BYTES);
+            tma_load_3d(st + s * G::STRIDE, J.tm, x0 - G::LP, y0 - 1, z0 - 1 + p, &bar[s]);
+        }
+    }
+
+    const bool xin = x < L.nx;
+    const bool xb = (x == 0 || x == L.nx - 1);
+    const bool has_fb = (J.fb != nullptr);
+    const bool has_gb = (J.gb != nullptr);
+    const int cc = G::LP + tx;  // this thread's column inside a stage row
+    auto slot = [&](int p) { return (b0 + (uint32_t)p) & (NSTAGE - 1); };
+    auto phase = [&](int p) { return ((b0 + (uint32_t)p) / NSTAGE) & 1; };
+
+    bool ok = bounded_wait(&bar[slot(0)], phase(0));
+    ok = bounded_wait(&bar[slot(1)], phase(1)) && ok;
+    T below[R], cur[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        below[k] = st[slot(0) * G::STRIDE + (rb + k) * G::W + cc];
+        cur[k] = st[slot(1) * G::STRIDE + (rb + k) * G::W + cc];
+    }
+    int p = 1;
+    for (int z = z0; z < z1; ++z, ++p) {
+        const uint32_t sa = slot(p + 1);
+        ok = bounded_wait(&bar[sa], phase(p + 1)) && ok;
+        const T* pl = st + slot(p) * G::STRIDE + cc;
+        const T* pa = st + sa * G::STRIDE + cc;
+        T above[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) above[k] = pa[(rb + k) * G::W];
+        if (xin && ok) {
+            const bool zb = (z == 0 || z == L.nz - 1);
+            const long long zoff = (long long)z * L.plane + x;
+            const T ym = pl[(rb - 1) * G::W];
+            const T yp = pl[(rb + R) * G::W];
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const int y = yb + k;
+                if (y < L.ny) {
+                    const long long off = zoff + (long long)y * L.pitch;
+                    const T s = (k == 0) ? ym : cur[k - 1];
+                    const T n = (k == R - 1) ? yp : cur[k + 1];
+                    const T w = pl[(rb + k) * G::W - 1];
+                    const T e = pl[(rb + k) * G::W + 1];
+                    const bool border = xb || zb || y == 0 || y == L.ny - 1;
+                    T v;
+                    if (!border) {
+                        T f = P::zero();
+                        if (HAS_F) f = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
+                        v = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
+                    } else if (BORDER == SCAFES_BORDER_DIRICHLET) {
+                        double g = J.ga ? J.ga[off] : J.gconst;
+                        if (has_gb) g += J.time_new * J.gb[off];
+                        v = P::from_double(g);
+                    } else {
+                        // Mirror border: the last face (in direction order
+                        // x-, x+, y-, y+, z-, z+) the node lies on decides.
+                        T opp;
+                        double cs;
+                        if (z == L.nz - 1)      { opp = below[k]; cs = -J.corr; }
+                        else if (z == 0)        { opp = above[k]; cs = J.corr; }
+                        else if (y == L.ny - 1) { opp = s; cs = -J.corr; }
+                        else if (y == 0)        { opp = n; cs = J.corr; }
+                        else if (x == L.nx - 1) { opp = w; cs = -J.corr; }
+                        else                    { opp = e; cs = J.corr; }
+                        v = P::mirror(cur[k], opp, cs);
+                    }
+                    J.un[off] = v;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            below[k] = cur[k];
+            cur[k] = above[k];
+        }
+        // Everyone is done with plane p-1: its stage takes plane p-1+NSTAGE.
+        if (!__syncthreads_and(ok)) break;
+        if (tid == 0) {
+            const int pn = p - 1 + NSTAGE;
+            if (pn < np) {
+                const uint32_t s = slot(pn);
+                fence_proxy_async_smem();
+                mbar_arrive_expect_tx(&bar[s], G::TX_BYTES);
+                tma_load_3d(st + s * G::STRIDE, J.tm, x0 - G::LP, y0 - 1, z0 - 1 + pn, &bar[s]);
+            }
+        }
+    }
+    if (!__syncthreads_and(ok)) {
+        if (tid == 0) {
+            // A stage never completed: report, drain what was issued, stop.
+            atomicExch(status, SCAFES_ERR_TIMEOUT);
+            for (int q = (p > 0 ? p - 1 : 0); q < np && q < p - 1 + NSTAGE; ++q)
+                bounded_wait(&bar[slot(q)], phase(q), kWaitLimitNs / 8);
+        }
+        return false;
+    }
+    base = b0 + (uint32_t)np;
+    return true;
+}
+
+}  // namespace scafes

@@ -6,47 +6,16 @@
 //  tests/system/PennesBioheatEqnFDM/PennesBioheatEqnFDM.hpp:153-168) and
 // their Dirichlet border (.../Dirichlet/Dirichlet.hpp:125-131), and the copy
 // old->new that precedes it (:5078-5082): every node is written each step.
-//
-// Mapping: a CTA owns a 32 x BY column tile and marches it through a chunk
-// of z-planes.  One elected thread streams the tile's planes (with a one-
-// node halo in x and y) from HBM into an NSTAGE-deep ring of shared-memory
-// stages with 3D TMA loads, each stage completing on its own mbarrier, so
-// that several planes per CTA are in flight.  Each thread owns R consecutive
-// rows of one column: it keeps u(z-1), u(z), u(z+1) of those rows in
-// registers (the z-marching queue), takes the y-neighbours inside its rows
-// from registers and the x-neighbours (and the two outer y-neighbours) from
-// the staged plane.  Blocking R rows per thread amortises the per-plane
-// wait, barrier and index work over R node updates.  Out-of-domain halo
-// cells are zero-filled by the TMA unit.  Stores are row-contiguous per warp.
-#include "star7_policies.cuh"
-#include "tma.cuh"
-#include "../../include/scafes_gb300.h"
+// Each CTA runs one tile (star7_tile.cuh) over a chunk of z-planes.
+#include "star7_tile.cuh"
 
 namespace scafes {
-
-constexpr int BX = 32;
-constexpr int NSTAGE = 8;  // power of two: stage/phase indices are shifts
-
-template <class T, int BY>
-struct Tile {
-    static constexpr int ESZ = (int)sizeof(T);
-    static constexpr int LP = 16 / ESZ;          // left halo padded to 16 bytes
-    static constexpr int W = BX + 2 * LP;        // box width (elements)
-    static constexpr int H = BY + 2;             // box height (rows)
-    static constexpr uint32_t TX_BYTES = W * H * ESZ;
-    static constexpr int STRIDE = ((W * H * ESZ + 127) / 128) * 128 / ESZ;  // elements per stage
-    static constexpr size_t SMEM = (size_t)NSTAGE * STRIDE * ESZ + NSTAGE * sizeof(uint64_t);
-};
-
-// Tile variants {BY, R}: CTA tile 32 x BY, R rows per thread.
-struct TileShape { int by, r; };
-constexpr TileShape kTiles[STAR7_NUM_TILES] = {{8, 1}, {16, 2}, {32, 4}, {16, 4}};
 
 template <class P, bool HAS_F, int BORDER, int BY, int R>
 __global__ void __launch_bounds__(BX * (BY / R))
 star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un,
           const typename P::T* __restrict__ fa, const typename P::T* __restrict__ fb,
-          const double* __restrict__ ga, const double* __restrict__ gb,
+          const double* __restrict__ ga, const double* __restrict__ gb, double gconst,
           Layout L, Star7Coeffs c, double time_old, double time_new,
           double corr, int zchunk, int* __restrict__ status)
 {
@@ -55,117 +24,12 @@ star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* st = reinterpret_cast<T*>(smem_raw);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NSTAGE * G::STRIDE * G::ESZ);
-
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int tid = ty * BX + tx;
-    const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
-    const int x = x0 + tx;
-    const int yb = y0 + ty * R;  // first row of this thread
-    const int rb = ty * R + 1;   // its row inside a stage
+    ring_init<T, BY>(bar);
+    TileJob<T> J{&tm, un, fa, fb, ga, gb, gconst, L, time_old, time_new, corr};
     const int z0 = blockIdx.z * zchunk;
     const int z1 = min(z0 + zchunk, L.nz);
-    const int np = z1 - z0 + 2;  // planes z0-1 .. z1 (index p <-> z = z0 - 1 + p)
-
-    if (tid == 0) {
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    if (tid == 0) {
-        const int pre = np < NSTAGE ? np : NSTAGE;
-        for (int p = 0; p < pre; ++p) {
-            mbar_arrive_expect_tx(&bar[p], G::TX_BYTES);
-            tma_load_3d(st + p * G::STRIDE, &tm, x0 - G::LP, y0 - 1, z0 - 1 + p, &bar[p]);
-        }
-    }
-
-    const bool xin = x < L.nx;
-    const bool xb = (x == 0 || x == L.nx - 1);
-    const bool has_fb = (fb != nullptr);
-    const bool has_gb = (gb != nullptr);
-    const int cc = G::LP + tx;  // this thread's column inside a stage row
-
-    bool ok = bounded_wait(&bar[0], 0);
-    ok = bounded_wait(&bar[1], 0) && ok;
-    T below[R], cur[R];
-#pragma unroll
-    for (int k = 0; k < R; ++k) {
-        below[k] = st[0 * G::STRIDE + (rb + k) * G::W + cc];
-        cur[k] = st[1 * G::STRIDE + (rb + k) * G::W + cc];
-    }
-    int p = 1;
-    for (int z = z0; z < z1; ++z, ++p) {
-        const int sa = (p + 1) & (NSTAGE - 1);
-        ok = bounded_wait(&bar[sa], ((p + 1) / NSTAGE) & 1) && ok;
-        const T* pl = st + (p & (NSTAGE - 1)) * G::STRIDE + cc;
-        const T* pa = st + sa * G::STRIDE + cc;
-        T above[R];
-#pragma unroll
-        for (int k = 0; k < R; ++k) above[k] = pa[(rb + k) * G::W];
-        if (xin && ok) {
-            const bool zb = (z == 0 || z == L.nz - 1);
-            const long long zoff = (long long)z * L.plane + x;
-            const T ym = pl[(rb - 1) * G::W];
-            const T yp = pl[(rb + R) * G::W];
-#pragma unroll
-            for (int k = 0; k < R; ++k) {
-                const int y = yb + k;
-                if (y < L.ny) {
-                    const long long off = zoff + (long long)y * L.pitch;
-                    const T s = (k == 0) ? ym : cur[k - 1];
-                    const T n = (k == R - 1) ? yp : cur[k + 1];
-                    const T w = pl[(rb + k) * G::W - 1];
-                    const T e = pl[(rb + k) * G::W + 1];
-                    const bool border = xb || zb || y == 0 || y == L.ny - 1;
-                    T v;
-                    if (!border) {
-                        T f = P::zero();
-                        if (HAS_F) f = P::src(fa[off], has_fb ? fb[off] : P::zero(), time_old, has_fb);
-                        v = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
-                    } else if (BORDER == SCAFES_BORDER_DIRICHLET) {
-                        double g = ga ? ga[off] : 0.0;
-                        if (has_gb) g += time_new * gb[off];
-                        v = P::from_double(g);
-                    } else {
-                        // Mirror border: the last face (in direction order
-                        // x-, x+, y-, y+, z-, z+) the node lies on decides.
-                        T opp;
-                        double cs;
-                        if (z == L.nz - 1)      { opp = below[k]; cs = -corr; }
-                        else if (z == 0)        { opp = above[k]; cs = corr; }
-                        else if (y == L.ny - 1) { opp = s; cs = -corr; }
-                        else if (y == 0)        { opp = n; cs = corr; }
-                        else if (x == L.nx - 1) { opp = w; cs = -corr; }
-                        else                    { opp = e; cs = corr; }
-                        v = P::mirror(cur[k], opp, cs);
-                    }
-                    un[off] = v;
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-            below[k] = cur[k];
-            cur[k] = above[k];
-        }
-        // Everyone is done with plane p-1: its stage takes plane p-1+NSTAGE.
-        if (!__syncthreads_and(ok)) break;
-        if (tid == 0) {
-            const int pn = p - 1 + NSTAGE;
-            if (pn < np) {
-                const int s = pn & (NSTAGE - 1);
-                fence_proxy_async_smem();
-                mbar_arrive_expect_tx(&bar[s], G::TX_BYTES);
-                tma_load_3d(st + s * G::STRIDE, &tm, x0 - G::LP, y0 - 1, z0 - 1 + pn, &bar[s]);
-            }
-        }
-    }
-    if (!__syncthreads_and(ok) && tid == 0) {
-        // A stage never completed: report, drain what was issued, return.
-        atomicExch(status, SCAFES_ERR_TIMEOUT);
-        for (int q = (p > 0 ? p - 1 : 0); q < np && q < p - 1 + NSTAGE; ++q)
-            bounded_wait(&bar[q & (NSTAGE - 1)], (q / NSTAGE) & 1, kWaitLimitNs / 8);
-    }
+    uint32_t base = 0;
+    star7_tile<P, HAS_F, BORDER, BY, R>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
 }
 
 // ---- host side ---------------------------------------------------------------
@@ -236,7 +100,7 @@ static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
     const int zchunk = choose_zchunk(L, BY);
     dim3 block(BX, BY / R, 1);
     dim3 grid((L.nx + BX - 1) / BX, (L.ny + BY - 1) / BY, (L.nz + zchunk - 1) / zchunk);
-    kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, (T*)a.un, (const T*)a.fa, (const T*)a.fb, a.ga, a.gb, L,
+    kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, (T*)a.un, (const T*)a.fa, (const T*)a.fb, a.ga, a.gb, a.gconst, L,
                                            a.c, a.time_old, a.time_new, a.mirror_corr, zchunk, a.status);
     return cudaGetLastError();
 }

@@ -1,0 +1,85 @@
+"""Seeded synthetic inputs of the benchmark workloads.
+
+The reference measures wall time on synthetic problems only; these
+generators reproduce the shapes, sizes and value distributions of the
+workloads the engine is measured on:
+
+* ``heat_sine_noise``: sin(pi x) sin(pi y) sin(pi z) on the unit cube plus
+  seeded uniform noise at inner nodes, border 0 (the plain heat workloads);
+* ``pennes_ensemble``: independent Pennes bioheat instances with seeded
+  grid sizes, conductivity, perfusion and a Gaussian heat source each
+  (the batched ensemble workload).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def heat_tau(n, alpha: float = 1.0, safety: float = 0.9) -> float:
+    """``safety`` times the explicit-Euler stability limit
+    1 / (2 alpha sum_p 1/h_p^2) on the unit cube."""
+    return safety / (2.0 * alpha * sum((m - 1) ** 2 for m in n))
+
+
+def heat_sine_noise(n, seed: int = 2, amp: float = 1e-3, out: np.ndarray | None = None) -> np.ndarray:
+    """Initial iterate of the plain heat workloads, shape (nz, ny, nx),
+    built plane by plane (so 512^3 needs no temporaries of full size)."""
+    nx, ny, nz = n
+    sx = np.sin(np.pi * np.arange(nx) / (nx - 1))
+    sy = np.sin(np.pi * np.arange(ny) / (ny - 1))
+    sz = np.sin(np.pi * np.arange(nz) / (nz - 1))
+    u = np.empty((nz, ny, nx)) if out is None else out
+    rng = np.random.default_rng(seed)
+    for k in range(nz):
+        plane = sz[k] * (sy[:, None] * sx[None, :])
+        if amp:
+            plane = plane + rng.uniform(-amp, amp, (ny, nx))
+        if k == 0 or k == nz - 1:
+            plane[:] = 0.0
+        else:
+            plane[0, :] = plane[-1, :] = 0.0
+            plane[:, 0] = plane[:, -1] = 0.0
+        u[k] = plane
+    return u
+
+
+T_ARTERIAL = 37.0
+
+
+def pennes_ensemble(n_inst: int = 256, seed: int = 8, sizes=tuple(range(32, 161, 16)),
+                    safety: float = 0.9):
+    """Pennes bioheat ensemble (rho c = rho_b c_b = 1, arterial and initial
+    temperature 37, Dirichlet 37).  Per instance: grid size per axis drawn
+    from ``sizes``, k ~ U[0.4, 0.6], w_b ~ U[0.5, 5]e-3, and a Gaussian heat
+    source Q = A exp(-|x - c|^2 / (2 s^2)) with c ~ U[0.3, 0.7]^3,
+    s ~ U[0.05, 0.15], A ~ U[1, 10].  The time step is ``safety`` times the
+    stability limit of that instance.  Returns a list of dicts with keys
+    n (nx, ny, nz), k, w_b, tau, q (array (nz, ny, nx))."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n_inst):
+        n = tuple(int(v) for v in rng.choice(np.asarray(sizes), size=3))
+        k = float(rng.uniform(0.4, 0.6))
+        w_b = float(rng.uniform(0.5, 5.0) * 1e-3)
+        c = rng.uniform(0.3, 0.7, 3)
+        s = float(rng.uniform(0.05, 0.15))
+        amp = float(rng.uniform(1.0, 10.0))
+        x = np.arange(n[0]) / (n[0] - 1)
+        y = np.arange(n[1]) / (n[1] - 1)
+        z = np.arange(n[2]) / (n[2] - 1)
+        r2 = ((x[None, None, :] - c[0]) ** 2 + (y[None, :, None] - c[1]) ** 2 + (z[:, None, None] - c[2]) ** 2)
+        q = amp * np.exp(-r2 / (2.0 * s * s))
+        tau = safety / (2.0 * k * sum((m - 1) ** 2 for m in n) + w_b)
+        out.append({"n": n, "k": k, "w_b": w_b, "tau": tau, "q": q})
+    return out
+
+
+def pennes_batch_instance(spec: dict):
+    """The C ABI instance of one ensemble member (source F = w_b T_a + Q)."""
+    from masterthesis_gb300 import batch_instance
+    return batch_instance(spec["n"], spec["tau"], coeff_a=spec["k"], rho_c=1.0, perf=spec["w_b"],
+                          g_value=T_ARTERIAL)
+
+
+def pennes_source(spec: dict) -> np.ndarray:
+    return spec["w_b"] * T_ARTERIAL + spec["q"]

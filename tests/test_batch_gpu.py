@@ -1,0 +1,90 @@
+"""Batched Pennes ensemble (C ABI, CUDA): every instance against the CPU
+oracle of the MRI-form Pennes update (examples/MRIDataPBHEqnFDM/
+MRIDataPBHEqnFDM.hpp:143-169, pinned to the reference by the golden
+vectors), the persistent work-queue path against the per-instance looped
+path, and the autotuner.  Tolerance: relative max-norm 1e-12 (f64, f32x2)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import cases
+import oracle as O
+from masterthesis_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def small_ensemble(n_inst=7, seed=3):
+    return W.pennes_ensemble(n_inst=n_inst, seed=seed, sizes=(3, 4, 7, 9, 17, 33, 40))
+
+
+def oracle_run(spec, T):
+    n = spec["n"]
+    g = O.make_grid(n, tau=spec["tau"])
+    shape = (n[2], n[1], n[0])
+    u0 = np.full(shape, W.T_ARTERIAL)
+    gb = np.full(shape, W.T_ARTERIAL)
+    return O.pennes_mri(g, u0, T, 1.0, 1.0, spec["k"], 1.0, 1.0, spec["w_b"], W.T_ARTERIAL, spec["q"], gb)
+
+
+def make_batch(M, specs, prec):
+    b = M.Batch([W.pennes_batch_instance(s) for s in specs], precision=prec)
+    for i, s in enumerate(specs):
+        shape = (s["n"][2], s["n"][1], s["n"][0])
+        b.upload(i, M.FIELD_F_A, W.pennes_source(s))
+        b.upload(i, M.FIELD_U, np.full(shape, W.T_ARTERIAL))
+    return b
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+def test_batch_matches_oracle_per_instance(gpu, prec):
+    M = gpu
+    specs = small_ensemble()
+    T = 25
+    with make_batch(M, specs, prec) as b:
+        b.step(T)
+        for i, s in enumerate(specs):
+            assert cases.rel_err(b.download(i), oracle_run(s, T)) <= 1e-12, (i, s["n"])
+
+
+def test_batch_equals_looped_and_all_schedules(gpu):
+    M = gpu
+    specs = small_ensemble(n_inst=9, seed=4)
+    T = 13
+    with make_batch(M, specs, "f64") as ref:
+        ref.step_looped(T)
+        want = [ref.download(i) for i in range(len(specs))]
+    for tile in (1, 2, 3, 4):
+        for ctas in (0, 1, 3):
+            with make_batch(M, specs, "f64") as b:
+                b.set_schedule(tile, ctas)
+                b.step(T)
+                for i in range(len(specs)):
+                    assert np.array_equal(b.download(i), want[i]), (tile, ctas, i)
+
+
+def test_batch_graph_replay_and_autotune(gpu):
+    M = gpu
+    specs = small_ensemble(n_inst=5, seed=5)
+    with make_batch(M, specs, "f64") as b:
+        tile, ctas = b.autotune(3)
+        assert 1 <= tile <= 4 and ctas in (0, 1, 2, 4)
+        b.step(10)   # captures the graph for 10 steps
+        b.step(10)   # replays it (other buffer parity: second graph)
+        b.step(10)   # replays the first graph
+        got = [b.download(i) for i in range(len(specs))]
+    for i, s in enumerate(specs):
+        assert cases.rel_err(got[i], oracle_run(s, 30)) <= 1e-12
+
+
+def test_batch_errors(gpu):
+    M = gpu
+    specs = small_ensemble(n_inst=2)
+    with make_batch(M, specs, "f64") as b:
+        with pytest.raises(M.ScafesError):
+            b.upload(5, M.FIELD_U, np.zeros(8))
+        with pytest.raises(M.ScafesError):
+            b.upload(0, M.FIELD_U, np.zeros(3))
+        with pytest.raises(M.ScafesError):
+            b.set_schedule(9, 0)
