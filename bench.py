@@ -56,6 +56,10 @@ def parse_args():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-instances", type=int, default=256)
     ap.add_argument("--batch-time-steps", type=int, default=500)
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adj-n", type=int, default=256)
+    ap.add_argument("--adj-time-steps", type=int, default=2000)
+    ap.add_argument("--adj-fd-directions", type=int, default=4)
     return ap.parse_args()
 
 
@@ -263,6 +267,77 @@ def run_batched(M, args, dist: Dist, hbm_peak: float):
     return out
 
 
+# ---- adjoint --------------------------------------------------------------------
+
+def smooth_gauss(n, seed):
+    """Seeded standard-normal field smoothed by 3 Jacobi passes (x fastest)."""
+    g = np.random.default_rng(seed).standard_normal((n[2], n[1], n[0]))
+    for _ in range(3):
+        g[1:-1, 1:-1, 1:-1] = (g[2:, 1:-1, 1:-1] + g[:-2, 1:-1, 1:-1] + g[1:-1, 2:, 1:-1] + g[1:-1, :-2, 1:-1]
+                               + g[1:-1, 1:-1, 2:] + g[1:-1, 1:-1, :-2]) / 6.0
+    return g
+
+
+def run_adjoint(M, args, dist: Dist):
+    """Adjoint workload: flux-form heat with k = exp(0.3 g), g a seeded
+    (seed 5) smoothed Gaussian field, 256^3, FP64, 2000 steps, u0 = sine
+    mode, target = the forward solve with a second conductivity (seed 6).
+    Reports the forward and gradient times, their ratio for 45 snapshots and
+    (when it fits in device memory) for every state stored, and central
+    finite differences of J on seeded directions."""
+    import torch
+    from masterthesis_gb300 import workloads as W
+    n = (args.adj_n,) * 3
+    T = args.adj_time_steps
+    k = np.exp(0.3 * smooth_gauss(n, 5))
+    k2 = np.exp(0.3 * smooth_gauss(n, 6))
+    tau = 0.9 / (2.0 * max(k.max(), k2.max()) * sum((m - 1) ** 2 for m in n))
+    u0 = W.heat_sine_noise(n, amp=0.0)
+    out = {"workload": f"adjoint heat, k=exp(0.3 g) (seed 5), {n[0]}^3 FP64, {T} steps, "
+                       f"J=0.5||u_T-u_target||^2, u_target from k seed 6"}
+    free, _ = torch.cuda.mem_get_info()
+    field = int(np.prod(n)) * 8
+    runs = [("snapshots_45", 45)]
+    if (T + 1) * field + 40 * field < free:
+        runs.append(("store_all", T + 1))
+    with M.Adjoint(n, tau, 2) as a:
+        a.set_conductivity(k2)
+        target = a.forward(u0, T)
+        a.set_conductivity(k)
+        a.forward(u0, 2)  # warm-up
+        a.forward(u0, T)
+        fwd_ms = a.stats()["forward_ms"]
+    out["forward_ms"] = fwd_ms
+    out["forward_glups"] = float(np.prod(n)) * T / (fwd_ms * 1e-3) / 1e9
+    grads = None
+    for name, s in runs:
+        with M.Adjoint(n, tau, s) as a:
+            a.set_conductivity(k)
+            J, gk, gu = a.gradient(u0, target, T)
+            st = a.stats()
+        out[name] = {"gradient_ms": st["gradient_ms"], "cost_ratio": st["gradient_ms"] / fwd_ms,
+                     "forward_steps": st["forward_steps"], "adjoint_steps": st["adjoint_steps"],
+                     "snapshot_bytes": s * field, "J": J}
+        grads = (J, gk, gu)
+    # Central differences of J on seeded directions (k relative, u0 absolute).
+    J, gk, gu = grads
+    errs = []
+    with M.Adjoint(n, tau, 2) as a:
+        def J_of(kk, uu):
+            a.set_conductivity(kk)
+            uT = a.forward(uu, T)
+            return 0.5 * float(np.sum((uT - target) ** 2))
+        for seed in range(args.adj_fd_directions):
+            rng = np.random.default_rng(7000 + seed)
+            dk = rng.standard_normal(k.shape) * k
+            eps = 1e-6
+            fd = (J_of(k + eps * dk, u0) - J_of(k - eps * dk, u0)) / (2 * eps)
+            errs.append(abs(fd - float(np.sum(gk * dk))) / abs(fd))
+    out["fd_directions"] = len(errs)
+    out["fd_max_rel_err"] = max(errs) if errs else None
+    return out
+
+
 # ---- GPU arm ----------------------------------------------------------------
 
 def run_ours(args, dist: Dist):
@@ -375,6 +450,7 @@ def run_ours(args, dist: Dist):
             variants[prec]["rel_err_vs_f64"] = float(np.max(np.abs(finals[prec] - ref))) / scale
 
     batched = None if args.no_batched else run_batched(M, args, dist, hbm_peak)
+    adjoint = None if args.no_adjoint else run_adjoint(M, args, dist)
 
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
@@ -393,6 +469,8 @@ def run_ours(args, dist: Dist):
         res["variants"] = variants
     if batched:
         res["batched"] = batched
+    if adjoint:
+        res["adjoint"] = adjoint
     if clk:
         res["clocks"] = clk
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:

@@ -244,6 +244,84 @@ int scafes_batch_info(const scafes_batch* b, int* n_items, int* launches,
 const char* scafes_batch_last_error(const scafes_batch* b);
 void scafes_batch_destroy(scafes_batch* b);
 
+/* ---- multi-field leapfrog workloads -------------------------------------
+ *
+ * Problems with several unknown fields and a second ("leapfrog") update
+ * phase (src/ScaFES_Problem.hpp:2604-2619, :2875-2918):
+ *  SCAFES_MF_LAME  Lame-Navier elastic wave, 3 displacement components,
+ *     u^{n+1} = 2u^n - u^{n-1} + tau^2/rho [ (lambda+2mu) d_cc u_c
+ *               + mu sum_{p!=c} d_pp u_c + (lambda+mu) sum_{q!=c} d_cq u_q ],
+ *     central differences incl. the 4-point mixed difference, border 0
+ *     (examples/LameNavierEqnFDM/LameNavierEqnFDM.hpp:269-378 is the
+ *     reference's form; it cannot advance, :23-25).  p = {lambda, mu, rho}.
+ *     Fields 0..2: u^n (x, y, z), 3..5: u^{n-1}.  FP64.
+ *  SCAFES_MF_YEE   Yee FDTD in a PEC box (eps = mu = 1), H half step then
+ *     E step (examples/EMFDTD/EMFDTD.hpp:295-385 without CPML), soft
+ *     current source Ez[src] -= tau*amp*exp(-((t-t0)/w)^2) sin(2 pi f t).
+ *     p = {amp, t0, w, f}.  Fields 0..5: Ex, Ey, Ez, Hx, Hy, Hz.  FP64/FP32. */
+enum scafes_mf_kind { SCAFES_MF_LAME = 0, SCAFES_MF_YEE = 1 };
+
+typedef struct scafes_mf_cfg {
+    int kind;                /* enum scafes_mf_kind */
+    int n_nodes[3];
+    double coord_first[3];
+    double coord_last[3];
+    double tau;
+    double t_start;
+    int precision;           /* SCAFES_PREC_F64 (both) or SCAFES_PREC_F32 (Yee) */
+    double p[8];             /* problem parameters, see above */
+    int src[3];              /* Yee source node */
+    void* stream;
+} scafes_mf_cfg;
+
+typedef struct scafes_mf scafes_mf;
+int scafes_mf_create(const scafes_mf_cfg* cfg, scafes_mf** out);
+int scafes_mf_upload(scafes_mf* h, int field, const double* host, size_t n);
+int scafes_mf_download(scafes_mf* h, int field, double* host, size_t n);
+int scafes_mf_step(scafes_mf* h, int n_steps);
+int scafes_mf_last_ms(const scafes_mf* h, float* ms);
+const char* scafes_mf_last_error(const scafes_mf* h);
+void scafes_mf_destroy(scafes_mf* h);
+
+/* ---- adjoint (gradients) -------------------------------------------------
+ *
+ * Replaces the reference's ADOL-C gradient path (src/ScaFES_Problem.hpp:
+ * 5843-5967 traceTypeTwo, :6633-6747 evalFovForwardTypeTwo with
+ * ::fov_forward at :6714), which tapes the update and evaluates the tape
+ * in forward mode, one direction per parameter.  Here the reverse-time
+ * sweep is hand-written for the flux-form variable-conductivity heat
+ * update
+ *   u'_i = u_i + sum_p tau/h_p^2 [ kp (u_{i+p} - u_i) - km (u_i - u_{i-p}) ],
+ *   kp = (k_i + k_{i+p})/2, km = (k_i + k_{i-p})/2, border nodes fixed,
+ * for J = 1/2 ||u_T - target||^2, giving dJ/dk and dJ/du0 in one reverse
+ * sweep.  Forward states are recomputed from snapshots held in device
+ * memory on the optimal binomial (revolve) schedule; with n_snapshots >=
+ * n_steps every state is stored and nothing is recomputed. */
+typedef struct scafes_adj scafes_adj;
+
+/* n_snapshots >= 2 forward states (one field each) are kept on the device. */
+int scafes_adj_create(const int n_nodes[3], const double coord_first[3],
+                      const double coord_last[3], double tau, int n_snapshots,
+                      void* stream, scafes_adj** out);
+/* Conductivity k at the nodes (dense host array, x fastest). */
+int scafes_adj_set_conductivity(scafes_adj* a, const double* k, size_t n);
+/* Plain forward solve u0 -> u_T (n_steps steps); times itself. */
+int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps,
+                       double* uT, size_t n);
+/* J and its gradients for the forward solve from u0 over n_steps steps. */
+int scafes_adj_gradient(scafes_adj* a, const double* u0, const double* target,
+                        int n_steps, double* J, double* grad_k,
+                        double* grad_u0, size_t n);
+/* ms of the last forward solve and gradient, forward steps the last call
+ * ran (including recomputation), adjoint steps, snapshots. */
+int scafes_adj_stats(const scafes_adj* a, float* forward_ms, float* gradient_ms,
+                     long long* forward_steps, long long* adjoint_steps,
+                     int* snapshots);
+/* Forward steps the binomial schedule needs for n_steps with n_snapshots. */
+long long scafes_adj_schedule_cost(int n_steps, int n_snapshots);
+const char* scafes_adj_last_error(const scafes_adj* a);
+void scafes_adj_destroy(scafes_adj* a);
+
 /* No counterpart in the reference.  The same max-norm check as
  * scafes_gpu_err_linf, for callers that must not allocate device memory at
  * the point of the call -- a time loop being recorded into a CUDA graph, a

@@ -294,3 +294,173 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Adjoint:
+    """Gradient of J = 1/2 ||u_T - target||^2 for the flux-form
+    variable-conductivity heat update (owns a scafes_adj)."""
+
+    def __init__(self, n, tau, n_snapshots, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), stream=None):
+        L = lib()
+        if not getattr(L, "_adj_set", False):
+            vp, dp = C.c_void_p, C.POINTER(C.c_double)
+            i3, d3 = C.c_int * 3, C.c_double * 3
+            L.scafes_adj_create.argtypes = [i3, d3, d3, C.c_double, C.c_int, vp, C.POINTER(vp)]
+            L.scafes_adj_set_conductivity.argtypes = [vp, dp, C.c_size_t]
+            L.scafes_adj_forward.argtypes = [vp, dp, C.c_int, dp, C.c_size_t]
+            L.scafes_adj_gradient.argtypes = [vp, dp, dp, C.c_int, dp, dp, dp, C.c_size_t]
+            L.scafes_adj_stats.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                           C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]
+            L.scafes_adj_schedule_cost.argtypes = [C.c_int, C.c_int]
+            L.scafes_adj_schedule_cost.restype = C.c_longlong
+            L.scafes_adj_last_error.argtypes = [vp]
+            L.scafes_adj_last_error.restype = C.c_char_p
+            L.scafes_adj_destroy.argtypes = [vp]
+            L.scafes_adj_destroy.restype = None
+            L._adj_set = True
+        self.n = tuple(n)
+        self.shape = (n[2], n[1], n[0])
+        h = C.c_void_p()
+        rc = L.scafes_adj_create((C.c_int * 3)(*n), (C.c_double * 3)(*first), (C.c_double * 3)(*last),
+                                 tau, n_snapshots, stream, C.byref(h))
+        if rc != 0:
+            raise ScafesError(rc, (L.scafes_last_error() or b"").decode())
+        self.h = h
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise ScafesError(rc, (lib().scafes_adj_last_error(self.h) or b"").decode())
+
+    def set_conductivity(self, k):
+        a = np.ascontiguousarray(k, dtype=np.float64)
+        self._chk(lib().scafes_adj_set_conductivity(self.h, _dp(a), a.size))
+
+    def forward(self, u0, n_steps):
+        a = np.ascontiguousarray(u0, dtype=np.float64)
+        out = np.empty(self.shape)
+        self._chk(lib().scafes_adj_forward(self.h, _dp(a), n_steps, _dp(out), out.size))
+        return out
+
+    def gradient(self, u0, target, n_steps):
+        a = np.ascontiguousarray(u0, dtype=np.float64)
+        t = np.ascontiguousarray(target, dtype=np.float64)
+        gk, gu = np.empty(self.shape), np.empty(self.shape)
+        J = C.c_double()
+        self._chk(lib().scafes_adj_gradient(self.h, _dp(a), _dp(t), n_steps, C.byref(J), _dp(gk), _dp(gu), gk.size))
+        return J.value, gk, gu
+
+    def stats(self) -> dict:
+        f, g = C.c_float(), C.c_float()
+        fs, as_, s = C.c_longlong(), C.c_longlong(), C.c_int()
+        self._chk(lib().scafes_adj_stats(self.h, C.byref(f), C.byref(g), C.byref(fs), C.byref(as_), C.byref(s)))
+        return {"forward_ms": f.value, "gradient_ms": g.value, "forward_steps": fs.value,
+                "adjoint_steps": as_.value, "snapshots": s.value}
+
+    @staticmethod
+    def schedule_cost(n_steps: int, n_snapshots: int) -> int:
+        L = lib()
+        L.scafes_adj_schedule_cost.argtypes = [C.c_int, C.c_int]
+        L.scafes_adj_schedule_cost.restype = C.c_longlong
+        return L.scafes_adj_schedule_cost(n_steps, n_snapshots)
+
+    def close(self):
+        if self.h:
+            lib().scafes_adj_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+MF_LAME, MF_YEE = 0, 1
+
+
+class MfCfg(C.Structure):
+    """Mirror of ``struct scafes_mf_cfg``."""
+    _fields_ = [("kind", C.c_int), ("n_nodes", C.c_int * 3), ("coord_first", C.c_double * 3),
+                ("coord_last", C.c_double * 3), ("tau", C.c_double), ("t_start", C.c_double),
+                ("precision", C.c_int), ("p", C.c_double * 8), ("src", C.c_int * 3), ("stream", C.c_void_p)]
+
+
+class MultiField:
+    """A multi-field leapfrog workload (Lame-Navier or Yee) on the GPU."""
+
+    def __init__(self, kind, n, tau, params, precision="f64", src=(0, 0, 0), first=(0.0, 0.0, 0.0),
+                 last=(1.0, 1.0, 1.0), t_start=0.0, stream=None):
+        L = lib()
+        if not getattr(L, "_mf_set", False):
+            vp, dp = C.c_void_p, C.POINTER(C.c_double)
+            L.scafes_mf_create.argtypes = [C.POINTER(MfCfg), C.POINTER(vp)]
+            L.scafes_mf_upload.argtypes = [vp, C.c_int, dp, C.c_size_t]
+            L.scafes_mf_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
+            L.scafes_mf_step.argtypes = [vp, C.c_int]
+            L.scafes_mf_last_ms.argtypes = [vp, C.POINTER(C.c_float)]
+            L.scafes_mf_last_error.argtypes = [vp]
+            L.scafes_mf_last_error.restype = C.c_char_p
+            L.scafes_mf_destroy.argtypes = [vp]
+            L.scafes_mf_destroy.restype = None
+            L._mf_set = True
+        c = MfCfg()
+        c.kind = kind
+        c.n_nodes[:] = list(n)
+        c.coord_first[:] = list(first)
+        c.coord_last[:] = list(last)
+        c.tau, c.t_start = tau, t_start
+        c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        p = list(params) + [0.0] * (8 - len(params))
+        c.p[:] = p
+        c.src[:] = list(src)
+        c.stream = stream
+        self.shape = (n[2], n[1], n[0])
+        h = C.c_void_p()
+        rc = L.scafes_mf_create(C.byref(c), C.byref(h))
+        if rc != 0:
+            raise ScafesError(rc, (L.scafes_last_error() or b"").decode())
+        self.h = h
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise ScafesError(rc, (lib().scafes_mf_last_error(self.h) or b"").decode())
+
+    def upload(self, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self._chk(lib().scafes_mf_upload(self.h, field, _dp(a), a.size))
+
+    def download(self, field):
+        a = np.empty(self.shape)
+        self._chk(lib().scafes_mf_download(self.h, field, _dp(a), a.size))
+        return a
+
+    def step(self, n_steps):
+        self._chk(lib().scafes_mf_step(self.h, n_steps))
+
+    def last_ms(self):
+        v = C.c_float()
+        self._chk(lib().scafes_mf_last_ms(self.h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.h:
+            lib().scafes_mf_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,523 @@
+// Hand-written adjoint of the flux-form variable-conductivity heat update,
+// with binomial checkpointing.
+//
+// Forward update (inner nodes; border nodes keep their value):
+//   u'_i = u_i + sum_p [ K_p[i] (u_{i+p} - u_i) - K_p[i-p] (u_i - u_{i-p}) ]
+//   K_p[i] = (tau/h_p^2) * (k_i + k_{i+p}) / 2     (conductivity of face i|i+p)
+// Objective J = 1/2 ||u_T - target||^2.  Gradients dJ/dk and dJ/du0.
+//
+// The reference obtains gradients by taping the update with ADOL-C and
+// evaluating the tape in forward mode with one direction per parameter
+// (src/ScaFES_Problem.hpp:5843-5967 traceTypeTwo, :6633-6747
+// evalFovForwardTypeTwo, ::fov_forward at :6714).  Here the reverse-time
+// (adjoint) sweep is hand-written: the update is linear in u and its
+// matrix is symmetric on the inner nodes, so the adjoint step has the same
+// stencil as the forward step applied to lambda (zero on border nodes),
+// plus the accumulation of the face-conductivity gradients
+//   G_p[i] += (u_{i+p} - u_i) (lambda_i - lambda_{i+p})
+// from which dJ/dk_i = sum_p (tau/h_p^2)/2 (G_p[i] + G_p[i-p]).
+// The forward states the adjoint needs are recomputed from snapshots kept
+// in device memory; the split points follow the optimal binomial schedule
+// (Griewank & Walther, "Algorithm 799: revolve", ACM TOMS 26(1), 2000),
+// computed here by dynamic programming over (steps, free snapshots).
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "scafes_common.cuh"
+#include "../../include/scafes_gb300.h"
+
+using namespace scafes;
+
+namespace scafes {
+void set_last_error(const char* msg);
+}
+
+namespace {
+
+constexpr int AX = 32, AY = 8;
+
+// Face conductivities K_p[i] = w_p (k_i + k_{i+p}) / 2, zero where i+p is
+// outside the grid.
+__global__ void k_faces(const double* __restrict__ k, double* __restrict__ kx, double* __restrict__ ky,
+                        double* __restrict__ kz, Layout L, double wx, double wy, double wz) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    for (int z = 0; z < L.nz; ++z) {
+        const long long o = L.idx(x, y, z);
+        const double kc = k[o];
+        kx[o] = x + 1 < L.nx ? wx * 0.5 * (kc + k[o + 1]) : 0.0;
+        ky[o] = y + 1 < L.ny ? wy * 0.5 * (kc + k[o + L.pitch]) : 0.0;
+        kz[o] = z + 1 < L.nz ? wz * 0.5 * (kc + k[o + L.plane]) : 0.0;
+    }
+}
+
+// One forward step (inner nodes; border nodes copied).
+__global__ void __launch_bounds__(AX * AY)
+k_forward(const double* __restrict__ u, double* __restrict__ un, const double* __restrict__ kx,
+          const double* __restrict__ ky, const double* __restrict__ kz, Layout L) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+    const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
+    for (int z = zb; z < ze; ++z) {
+        const long long o = L.idx(x, y, z);
+        const double uc = u[o];
+        if (colb || z == 0 || z == L.nz - 1) {
+            un[o] = uc;
+            continue;
+        }
+        double v = uc;
+        v = fma(kx[o], u[o + 1] - uc, v);
+        v = fma(-kx[o - 1], uc - u[o - 1], v);
+        v = fma(ky[o], u[o + L.pitch] - uc, v);
+        v = fma(-ky[o - L.pitch], uc - u[o - L.pitch], v);
+        v = fma(kz[o], u[o + L.plane] - uc, v);
+        v = fma(-kz[o - L.plane], uc - u[o - L.plane], v);
+        un[o] = v;
+    }
+}
+
+// One adjoint step: lambda_t from lambda_{t+1} (lam, zero on border nodes)
+// and the forward state u_t; accumulates the face gradients G and, on
+// border nodes, the border part of dJ/du0 (bnd).
+__global__ void __launch_bounds__(AX * AY)
+k_adjoint(const double* __restrict__ lam, double* __restrict__ lamn, const double* __restrict__ u,
+          const double* __restrict__ kx, const double* __restrict__ ky, const double* __restrict__ kz,
+          double* __restrict__ gx, double* __restrict__ gy, double* __restrict__ gz, double* __restrict__ bnd,
+          Layout L) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+    const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
+    for (int z = zb; z < ze; ++z) {
+        const long long o = L.idx(x, y, z);
+        const bool border = colb || z == 0 || z == L.nz - 1;
+        const double lc = lam[o];  // zero on border nodes
+        const double uc = u[o];
+        // +x face
+        if (x + 1 < L.nx) gx[o] = fma(u[o + 1] - uc, lc - lam[o + 1], gx[o]);
+        if (y + 1 < L.ny) gy[o] = fma(u[o + L.pitch] - uc, lc - lam[o + L.pitch], gy[o]);
+        if (z + 1 < L.nz) gz[o] = fma(u[o + L.plane] - uc, lc - lam[o + L.plane], gz[o]);
+        double s = 0.0;
+        const double lxp = x + 1 < L.nx ? lam[o + 1] : 0.0, lxm = x > 0 ? lam[o - 1] : 0.0;
+        const double lyp = y + 1 < L.ny ? lam[o + L.pitch] : 0.0, lym = y > 0 ? lam[o - L.pitch] : 0.0;
+        const double lzp = z + 1 < L.nz ? lam[o + L.plane] : 0.0, lzm = z > 0 ? lam[o - L.plane] : 0.0;
+        const double kxm = x > 0 ? kx[o - 1] : 0.0, kym = y > 0 ? ky[o - L.pitch] : 0.0;
+        const double kzm = z > 0 ? kz[o - L.plane] : 0.0;
+        if (border) {
+            // Border rows of the update are the identity: lambda on the border
+            // only collects what the inner neighbours pass back.
+            s = fma(kx[o], lxp, s);
+            s = fma(kxm, lxm, s);
+            s = fma(ky[o], lyp, s);
+            s = fma(kym, lym, s);
+            s = fma(kz[o], lzp, s);
+            s = fma(kzm, lzm, s);
+            bnd[o] += s;
+            lamn[o] = 0.0;
+        } else {
+            double v = lc;
+            v = fma(kx[o], lxp - lc, v);
+            v = fma(kxm, lxm - lc, v);
+            v = fma(ky[o], lyp - lc, v);
+            v = fma(kym, lym - lc, v);
+            v = fma(kz[o], lzp - lc, v);
+            v = fma(kzm, lzm - lc, v);
+            lamn[o] = v;
+        }
+    }
+}
+
+// lambda_T = u_T - target: inner part into lam, border part into bnd;
+// per-CTA partial sums of 0.5 (u_T - target)^2 into part.
+__global__ void k_terminal(const double* __restrict__ uT, const double* __restrict__ target,
+                           double* __restrict__ lam, double* __restrict__ bnd, double* __restrict__ part, Layout L) {
+    __shared__ double sh[AX * AY];
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    double acc = 0.0;
+    if (x < L.nx && y < L.ny) {
+        const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+        for (int z = 0; z < L.nz; ++z) {
+            const long long o = L.idx(x, y, z);
+            const double d = uT[o] - target[o];
+            acc += 0.5 * d * d;
+            const bool border = colb || z == 0 || z == L.nz - 1;
+            lam[o] = border ? 0.0 : d;
+            bnd[o] = border ? d : 0.0;
+        }
+    }
+    const int t = threadIdx.y * AX + threadIdx.x;
+    sh[t] = acc;
+    __syncthreads();
+    for (int s = AX * AY / 2; s > 0; s >>= 1) {
+        if (t < s) sh[t] += sh[t + s];
+        __syncthreads();
+    }
+    if (t == 0) part[blockIdx.y * gridDim.x + blockIdx.x] = sh[0];
+}
+
+// dJ/dk_i = sum_p w_p/2 (G_p[i] + G_p[i-p]); dJ/du0 = lambda_0 + border part.
+__global__ void k_finalize(const double* __restrict__ gx, const double* __restrict__ gy,
+                           const double* __restrict__ gz, const double* __restrict__ lam,
+                           const double* __restrict__ bnd, double* __restrict__ dk, double* __restrict__ du0,
+                           Layout L, double wx, double wy, double wz) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    for (int z = 0; z < L.nz; ++z) {
+        const long long o = L.idx(x, y, z);
+        double g = 0.5 * wx * (gx[o] + (x > 0 ? gx[o - 1] : 0.0));
+        g += 0.5 * wy * (gy[o] + (y > 0 ? gy[o - L.pitch] : 0.0));
+        g += 0.5 * wz * (gz[o] + (z > 0 ? gz[o - L.plane] : 0.0));
+        dk[o] = g;
+        du0[o] = lam[o] + bnd[o];
+    }
+}
+
+}  // namespace
+
+struct scafes_adj {
+    Layout L;
+    double tau = 0.0, w[3] = {0, 0, 0};
+    int n_snap = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    double *kx = nullptr, *ky = nullptr, *kz = nullptr;
+    double *u[2] = {nullptr, nullptr}, *lam[2] = {nullptr, nullptr};
+    double *gx = nullptr, *gy = nullptr, *gz = nullptr, *bnd = nullptr;
+    double *snaps = nullptr;   // n_snap fields
+    double *work = nullptr;    // staging of host arrays (dense doubles)
+    double *part = nullptr;    // J partial sums
+    int part_n = 0;
+    bool have_k = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float fwd_ms = 0.f, grad_ms = 0.f;
+    long long fwd_steps = 0, adj_steps = 0;
+    // Binomial schedule tables: cost[n][s] and the optimal first split.
+    int tab_n = 0, tab_s = 0;
+    std::vector<long long> cost;
+    std::vector<int> split;
+    std::string err;
+};
+
+namespace {
+
+int afail(scafes_adj* a, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (a) a->err = buf;
+    scafes::set_last_error(buf);
+    return code;
+}
+
+#define ATRY(a, call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return afail(a, SCAFES_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                         __FILE__, __LINE__);                                                  \
+    } while (0)
+
+dim3 grid2(const Layout& L) { return dim3((L.nx + AX - 1) / AX, (L.ny + AY - 1) / AY, 1); }
+dim3 grid3(const Layout& L) { return dim3((L.nx + AX - 1) / AX, (L.ny + AY - 1) / AY, (L.nz + 15) / 16); }
+size_t field_bytes(const scafes_adj* a) { return (size_t)a->L.size() * sizeof(double); }
+double* snap(scafes_adj* a, int s) { return a->snaps + (size_t)s * a->L.size(); }
+
+int fwd(scafes_adj* a, const double* src, double* dst) {
+    k_forward<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(src, dst, a->kx, a->ky, a->kz, a->L);
+    ATRY(a, cudaGetLastError());
+    ++a->fwd_steps;
+    return SCAFES_OK;
+}
+
+// Optimal binomial schedule: cost(n, s) = fewest forward steps that reverse
+// n steps starting from a stored state with s free snapshots;
+// cost(1, s) = 0, cost(n, 0) = n(n-1)/2,
+// cost(n, s) = min_m  m + cost(n - m, s - 1) + cost(m, s).
+void build_schedule(scafes_adj* a, int n, int s) {
+    if (s >= n - 1) return;  // every state gets a slot: split_of answers 1
+    if (n <= a->tab_n && s <= a->tab_s) return;
+    const int N = n, S = s;
+    a->cost.assign((size_t)(N + 1) * (S + 1), 0);
+    a->split.assign((size_t)(N + 1) * (S + 1), 1);
+    auto C = [&](int nn, int ss) -> long long& { return a->cost[(size_t)nn * (S + 1) + ss]; };
+    auto M = [&](int nn, int ss) -> int& { return a->split[(size_t)nn * (S + 1) + ss]; };
+    for (int nn = 1; nn <= N; ++nn) C(nn, 0) = (long long)nn * (nn - 1) / 2;
+    for (int ss = 1; ss <= S; ++ss) {
+        C(1, ss) = 0;
+        for (int nn = 2; nn <= N; ++nn) {
+            if (ss >= nn - 1) {  // a slot for every state: store them all
+                C(nn, ss) = nn - 1;
+                M(nn, ss) = 1;
+                continue;
+            }
+            long long best = -1;
+            int bm = 1;
+            for (int m = 1; m < nn; ++m) {
+                const long long c = m + C(nn - m, ss - 1) + C(m, ss);
+                if (best < 0 || c < best) { best = c; bm = m; }
+            }
+            C(nn, ss) = best;
+            M(nn, ss) = bm;
+        }
+    }
+    a->tab_n = N;
+    a->tab_s = S;
+}
+
+int split_of(scafes_adj* a, int n, int s) {
+    if (s >= n - 1) return 1;
+    return a->split[(size_t)n * (a->tab_s + 1) + s];
+}
+
+// Free snapshot slots the schedule uses: all states when they fit, else at
+// most kMaxSchedSlots (the dynamic program is O(n^2 s); with 128 slots and a
+// few thousand steps the recomputation is already below one extra sweep).
+constexpr int kMaxSchedSlots = 128;
+int schedule_slots(int n_snap, int n_steps) {
+    const int free = n_snap - 1;
+    if (free >= n_steps - 1) return n_steps - 1;
+    return free < kMaxSchedSlots ? free : kMaxSchedSlots;
+}
+
+struct Rev {
+    scafes_adj* a;
+    const double* target;
+    int T;
+    int cur;  // lambda buffer holding lambda_b
+    bool started;
+    double* Jpart;
+};
+
+int adj_step(Rev& R, const double* u_t) {
+    scafes_adj* a = R.a;
+    k_adjoint<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(a->lam[R.cur], a->lam[R.cur ^ 1], u_t, a->kx, a->ky,
+                                                           a->kz, a->gx, a->gy, a->gz, a->bnd, a->L);
+    ATRY(a, cudaGetLastError());
+    R.cur ^= 1;
+    ++a->adj_steps;
+    return SCAFES_OK;
+}
+
+// Reverses steps [lo, hi): the state u_lo is in snapshot slot `slot`;
+// `free` further slots (slot+1 .. slot+free) may be used.
+int reverse(Rev& R, int lo, int hi, int slot, int free) {
+    scafes_adj* a = R.a;
+    int rc;
+    if (hi - lo == 1) {
+        if (!R.started) {
+            // Bottom of the first descent: u_T from u_{T-1} gives J and lambda_T.
+            if ((rc = fwd(a, snap(a, slot), a->u[0]))) return rc;
+            k_terminal<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->u[0], R.target, a->lam[R.cur], a->bnd,
+                                                                    R.Jpart, a->L);
+            ATRY(a, cudaGetLastError());
+            R.started = true;
+        }
+        return adj_step(R, snap(a, slot));
+    }
+    if (free == 0) {
+        // No slot left: recompute every state from u_lo.
+        for (int t = hi - 1; t >= lo; --t) {
+            const double* src = snap(a, slot);
+            int buf = 0;
+            for (int s = lo; s < t; ++s) {
+                if ((rc = fwd(a, src, a->u[buf]))) return rc;
+                src = a->u[buf];
+                buf ^= 1;
+            }
+            if (t == hi - 1 && !R.started) {
+                if ((rc = fwd(a, src, a->u[buf]))) return rc;
+                k_terminal<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->u[buf], R.target, a->lam[R.cur], a->bnd,
+                                                                        R.Jpart, a->L);
+                ATRY(a, cudaGetLastError());
+                R.started = true;
+            }
+            if ((rc = adj_step(R, src))) return rc;
+        }
+        return SCAFES_OK;
+    }
+    const int m = lo + split_of(a, hi - lo, free);
+    // Advance u_lo -> u_m into slot+1.
+    const double* src = snap(a, slot);
+    int buf = 0;
+    for (int s = lo; s < m - 1; ++s) {
+        if ((rc = fwd(a, src, a->u[buf]))) return rc;
+        src = a->u[buf];
+        buf ^= 1;
+    }
+    if ((rc = fwd(a, src, snap(a, slot + 1)))) return rc;
+    if ((rc = reverse(R, m, hi, slot + 1, free - 1))) return rc;
+    return reverse(R, lo, m, slot, free);
+}
+
+int upload_dense(scafes_adj* a, const double* host, double* dev) {
+    const Layout& L = a->L;
+    ATRY(a, cudaMemcpy2DAsync(dev, (size_t)L.pitch * sizeof(double), host, (size_t)L.nx * sizeof(double),
+                              (size_t)L.nx * sizeof(double), (size_t)L.ny * L.nz, cudaMemcpyHostToDevice, a->stream));
+    return SCAFES_OK;
+}
+
+int download_dense(scafes_adj* a, const double* dev, double* host) {
+    const Layout& L = a->L;
+    ATRY(a, cudaMemcpy2DAsync(host, (size_t)L.nx * sizeof(double), dev, (size_t)L.pitch * sizeof(double),
+                              (size_t)L.nx * sizeof(double), (size_t)L.ny * L.nz, cudaMemcpyDeviceToHost, a->stream));
+    return SCAFES_OK;
+}
+
+}  // namespace
+
+extern "C" const char* scafes_adj_last_error(const scafes_adj* a) { return a ? a->err.c_str() : ""; }
+
+extern "C" void scafes_adj_destroy(scafes_adj* a) {
+    if (!a) return;
+    if (a->stream) cudaStreamSynchronize(a->stream);
+    double* bufs[] = {a->kx, a->ky, a->kz, a->u[0], a->u[1], a->lam[0], a->lam[1], a->gx, a->gy, a->gz,
+                      a->bnd, a->snaps, a->work, a->part};
+    for (double* b : bufs) cudaFree(b);
+    if (a->e0) cudaEventDestroy(a->e0);
+    if (a->e1) cudaEventDestroy(a->e1);
+    if (a->own_stream && a->stream) cudaStreamDestroy(a->stream);
+    delete a;
+}
+
+extern "C" int scafes_adj_create(const int n_nodes[3], const double coord_first[3], const double coord_last[3],
+                                 double tau, int n_snapshots, void* stream, scafes_adj** out) {
+    if (!out || !n_nodes || !coord_first || !coord_last)
+        return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_create: NULL argument");
+    *out = nullptr;
+    for (int p = 0; p < 3; ++p)
+        if (n_nodes[p] < 3 || n_nodes[p] > (1 << 16))
+            return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_create: n_nodes[%d]=%d out of [3, 65536]", p, n_nodes[p]);
+    if (n_snapshots < 2) return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_create: need at least 2 snapshots");
+    if (!(tau > 0.0)) return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_create: tau must be > 0");
+    scafes_adj* a = new (std::nothrow) scafes_adj();
+    if (!a) return afail(nullptr, SCAFES_ERR_NOMEM, "scafes_adj_create: out of host memory");
+    a->L = make_layout(n_nodes[0], n_nodes[1], n_nodes[2]);
+    a->tau = tau;
+    for (int p = 0; p < 3; ++p) {
+        const double h = (coord_last[p] - coord_first[p]) / (n_nodes[p] - 1);
+        a->w[p] = tau / (h * h);
+    }
+    a->n_snap = n_snapshots;
+    const size_t fb = field_bytes(a);
+    cudaError_t e = cudaSuccess;
+    if (stream) a->stream = (cudaStream_t)stream;
+    else { e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking); a->own_stream = true; }
+    double** fields[] = {&a->kx, &a->ky, &a->kz, &a->u[0], &a->u[1], &a->lam[0], &a->lam[1], &a->gx, &a->gy,
+                         &a->gz, &a->bnd, &a->work};
+    for (double** f : fields)
+        if (e == cudaSuccess) e = cudaMalloc(f, fb);
+    if (e == cudaSuccess) e = cudaMalloc(&a->snaps, fb * (size_t)n_snapshots);
+    a->part_n = grid2(a->L).x * grid2(a->L).y;
+    if (e == cudaSuccess) e = cudaMalloc(&a->part, sizeof(double) * a->part_n);
+    if (e == cudaSuccess) e = cudaMemsetAsync(a->snaps, 0, fb * (size_t)n_snapshots, a->stream);
+    for (double** f : fields)
+        if (e == cudaSuccess) e = cudaMemsetAsync(*f, 0, fb, a->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&a->e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&a->e1);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(a->stream);
+    if (e != cudaSuccess) {
+        const int code = e == cudaErrorMemoryAllocation ? SCAFES_ERR_NOMEM : SCAFES_ERR_CUDA;
+        afail(nullptr, code, "scafes_adj_create: %s (%d snapshots of %zu bytes)", cudaGetErrorString(e), n_snapshots, fb);
+        scafes_adj_destroy(a);
+        return code;
+    }
+    *out = a;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_adj_set_conductivity(scafes_adj* a, const double* k, size_t n) {
+    if (!a || !k) return afail(a, SCAFES_ERR_ARG, "scafes_adj_set_conductivity: NULL argument");
+    if (n != (size_t)a->L.nx * a->L.ny * a->L.nz)
+        return afail(a, SCAFES_ERR_ARG, "scafes_adj_set_conductivity: expected %zu values",
+                     (size_t)a->L.nx * a->L.ny * a->L.nz);
+    int rc = upload_dense(a, k, a->work);
+    if (rc) return rc;
+    k_faces<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->work, a->kx, a->ky, a->kz, a->L, a->w[0], a->w[1], a->w[2]);
+    ATRY(a, cudaGetLastError());
+    ATRY(a, cudaStreamSynchronize(a->stream));
+    a->have_k = true;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps, double* uT, size_t n) {
+    if (!a || !u0 || !uT || n_steps < 0) return afail(a, SCAFES_ERR_ARG, "scafes_adj_forward: bad arguments");
+    if (n != (size_t)a->L.nx * a->L.ny * a->L.nz) return afail(a, SCAFES_ERR_ARG, "scafes_adj_forward: wrong size");
+    if (!a->have_k) return afail(a, SCAFES_ERR_STATE, "scafes_adj_forward: set the conductivity first");
+    int rc = upload_dense(a, u0, a->u[0]);
+    if (rc) return rc;
+    a->fwd_steps = 0;
+    ATRY(a, cudaEventRecord(a->e0, a->stream));
+    int cur = 0;
+    for (int s = 0; s < n_steps; ++s) {
+        if ((rc = fwd(a, a->u[cur], a->u[cur ^ 1]))) return rc;
+        cur ^= 1;
+    }
+    ATRY(a, cudaEventRecord(a->e1, a->stream));
+    if ((rc = download_dense(a, a->u[cur], uT))) return rc;
+    ATRY(a, cudaStreamSynchronize(a->stream));
+    ATRY(a, cudaEventElapsedTime(&a->fwd_ms, a->e0, a->e1));
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_adj_gradient(scafes_adj* a, const double* u0, const double* target, int n_steps, double* J,
+                                   double* grad_k, double* grad_u0, size_t n) {
+    if (!a || !u0 || !target || !J || !grad_k || !grad_u0 || n_steps < 1)
+        return afail(a, SCAFES_ERR_ARG, "scafes_adj_gradient: bad arguments");
+    if (n != (size_t)a->L.nx * a->L.ny * a->L.nz) return afail(a, SCAFES_ERR_ARG, "scafes_adj_gradient: wrong size");
+    if (!a->have_k) return afail(a, SCAFES_ERR_STATE, "scafes_adj_gradient: set the conductivity first");
+    const int free = schedule_slots(a->n_snap, n_steps);
+    build_schedule(a, n_steps, free);
+    const size_t fb = field_bytes(a);
+    int rc = upload_dense(a, u0, snap(a, 0));
+    if (rc) return rc;
+    // The target goes to u[1]'s slot only transiently: keep it in `work`.
+    if ((rc = upload_dense(a, target, a->work))) return rc;
+    ATRY(a, cudaMemsetAsync(a->gx, 0, fb, a->stream));
+    ATRY(a, cudaMemsetAsync(a->gy, 0, fb, a->stream));
+    ATRY(a, cudaMemsetAsync(a->gz, 0, fb, a->stream));
+    a->fwd_steps = 0;
+    a->adj_steps = 0;
+    ATRY(a, cudaEventRecord(a->e0, a->stream));
+    Rev R{a, a->work, n_steps, 0, false, a->part};
+    if ((rc = reverse(R, 0, n_steps, 0, free))) return rc;
+    k_finalize<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->gx, a->gy, a->gz, a->lam[R.cur], a->bnd, a->u[0],
+                                                            a->u[1], a->L, a->w[0], a->w[1], a->w[2]);
+    ATRY(a, cudaGetLastError());
+    ATRY(a, cudaEventRecord(a->e1, a->stream));
+    std::vector<double> part(a->part_n);
+    ATRY(a, cudaMemcpyAsync(part.data(), a->part, sizeof(double) * a->part_n, cudaMemcpyDeviceToHost, a->stream));
+    if ((rc = download_dense(a, a->u[0], grad_k))) return rc;
+    if ((rc = download_dense(a, a->u[1], grad_u0))) return rc;
+    ATRY(a, cudaStreamSynchronize(a->stream));
+    ATRY(a, cudaEventElapsedTime(&a->grad_ms, a->e0, a->e1));
+    double s = 0.0;
+    for (double v : part) s += v;
+    *J = s;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_adj_stats(const scafes_adj* a, float* forward_ms, float* gradient_ms, long long* forward_steps,
+                                long long* adjoint_steps, int* snapshots) {
+    if (!a) return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_stats: NULL handle");
+    if (forward_ms) *forward_ms = a->fwd_ms;
+    if (gradient_ms) *gradient_ms = a->grad_ms;
+    if (forward_steps) *forward_steps = a->fwd_steps;
+    if (adjoint_steps) *adjoint_steps = a->adj_steps;
+    if (snapshots) *snapshots = a->n_snap;
+    return SCAFES_OK;
+}
+
+extern "C" long long scafes_adj_schedule_cost(int n_steps, int n_snapshots) {
+    if (n_steps < 1 || n_snapshots < 1) return -1;
+    scafes_adj tmp;
+    const int free = schedule_slots(n_snapshots, n_steps);
+    if (free >= n_steps - 1) return n_steps;  // one sweep, every state stored
+    build_schedule(&tmp, n_steps, free);
+    return tmp.cost[(size_t)n_steps * (free + 1) + free] + 1;  // + the step that gives u_T
+}

@@ -76,9 +76,9 @@ batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ 
         J.fb = nullptr;
         J.ga = nullptr;
         J.gb = nullptr;
-        J.gconst = I.gconst;
+        J.gval = P::from_double(I.gconst);
         J.L = I.L;
-        J.time_old = J.time_new = J.corr = 0.0;
+        J.time_old = J.time_new = J.corr = Split{0.0, 0.f, 0.f};
         if (!star7_tile<P, true, SCAFES_BORDER_DIRICHLET, BY, R>(J, I.c, w.tx * BX, w.ty * BY, w.z0, w.z1, st, bar,
                                                                  base, status))
             break;
@@ -184,6 +184,7 @@ KernelInfo kinfo(int precision, int tile) {
 int grid_size(scafes_batch* b, const KernelInfo& k) {
     int occ = 0;
     cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
+    cudaFuncSetAttribute(k.fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k.fn, k.block.x * k.block.y, k.smem);
     if (occ < 1) occ = 1;
     int per_sm = b->ctas_per_sm > 0 && b->ctas_per_sm < occ ? b->ctas_per_sm : occ;

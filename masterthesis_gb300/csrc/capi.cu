@@ -187,9 +187,10 @@ extern "C" int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out) {
     return SCAFES_OK;
 }
 
+// Exact-solution slots stay double (only the error check reads them);
+// source and border slots use the element type of the unknown field.
 static bool slot_is_double(int field) {
-    return field == SCAFES_FIELD_G_A || field == SCAFES_FIELD_G_B ||
-           field == SCAFES_FIELD_E_A || field == SCAFES_FIELD_E_B;
+    return field == SCAFES_FIELD_E_A || field == SCAFES_FIELD_E_B;
 }
 
 static int ensure_stage(scafes_handle* h) {
@@ -352,8 +353,8 @@ static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
     a.L = h->L;
     a.fa = h->has[SCAFES_FIELD_F_A] ? h->fld[SCAFES_FIELD_F_A] : nullptr;
     a.fb = h->has[SCAFES_FIELD_F_B] ? h->fld[SCAFES_FIELD_F_B] : nullptr;
-    a.ga = h->has[SCAFES_FIELD_G_A] ? (const double*)h->fld[SCAFES_FIELD_G_A] : nullptr;
-    a.gb = h->has[SCAFES_FIELD_G_B] ? (const double*)h->fld[SCAFES_FIELD_G_B] : nullptr;
+    a.ga = h->has[SCAFES_FIELD_G_A] ? h->fld[SCAFES_FIELD_G_A] : nullptr;
+    a.gb = h->has[SCAFES_FIELD_G_B] ? h->fld[SCAFES_FIELD_G_B] : nullptr;
     a.gconst = 0.0;
     a.c = make_star7_coeffs(h->cfg.c0, h->cfg.cp, h->cfg.cf);
     if (!h->has[SCAFES_FIELD_F_A] && h->has[SCAFES_FIELD_F_B])

@@ -1,0 +1,340 @@
+// Multi-field leapfrog workloads: the Lame-Navier elastic wave (3
+// displacement components, mixed second derivatives) and the Yee FDTD
+// scheme for Maxwell's equations (6 staggered fields).
+//
+// In ScaFES these are problems with several unknown data fields and a
+// second update phase (the leapfrog "update2" of src/ScaFES_Problem.hpp:
+// 2604-2619, :2875-2918).  The Yee problem of the reference
+// (examples/EMFDTD/EMFDTD.hpp:295-385: H in updateInner, D/E/I in
+// updateInner2) is not built by the reference (examples/Makefile.am:14) and
+// its Lame-Navier example cannot advance (examples/LameNavierEqnFDM/
+// LameNavierEqnFDM.hpp:23-25: only one old time level is exposed), so the
+// schemes here follow the textbook forms written out in the oracle
+// (orc_lame, orc_yee), which the tests use as the reference.
+//
+// Both are FP64-issue-bound on GB300 (Lame: ~57 FP64 operations per node,
+// Yee: ~24 per cell and step), so the kernels read neighbours straight from
+// global memory through L1 instead of staging tiles: one thread per (x, y)
+// column marches a chunk of 16 z-planes.
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <string>
+
+#include "scafes_common.cuh"
+#include "../../include/scafes_gb300.h"
+
+using namespace scafes;
+
+namespace scafes {
+void set_last_error(const char* msg);
+}
+
+namespace {
+
+constexpr int MX = 32, MY = 8, MZ = 16;
+
+struct LameCoef {
+    double a[3][3];   // a[c][p]: weight of d_pp on component c (includes tau^2/rho/h_p^2)
+    double b[3][3];   // b[c][q]: weight of d_cq u_q (includes tau^2/rho/(4 h_c h_q))
+};
+
+// u_new (written over uprev) = 2u - uprev + sum ... on inner nodes; 0 on border.
+__global__ void __launch_bounds__(MX * MY)
+k_lame(const double* __restrict__ u, double* __restrict__ up, LameCoef K, Layout L, long long comp) {
+    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+    const long long st[3] = {1, L.pitch, L.plane};
+    const int z0 = blockIdx.z * MZ, z1 = min(z0 + MZ, L.nz);
+    for (int z = z0; z < z1; ++z) {
+        const long long m = L.idx(x, y, z);
+        if (colb || z == 0 || z == L.nz - 1) {
+            up[m] = 0.0;
+            up[m + comp] = 0.0;
+            up[m + 2 * comp] = 0.0;
+            continue;
+        }
+        double out[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double* uc = u + c * comp;
+            const double uv = uc[m];
+            double acc = 2.0 * uv - up[m + c * comp];
+#pragma unroll
+            for (int p = 0; p < 3; ++p)
+                acc = fma(K.a[c][p], (uc[m + st[p]] + uc[m - st[p]]) - 2.0 * uv, acc);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (q == c) continue;
+                const double* uq = u + q * comp;
+                const long long sp = st[c], sq = st[q];
+                acc = fma(K.b[c][q], (uq[m + sp + sq] - uq[m + sp - sq]) - (uq[m - sp + sq] - uq[m - sp - sq]), acc);
+            }
+            out[c] = acc;
+        }
+        up[m] = out[0];
+        up[m + comp] = out[1];
+        up[m + 2 * comp] = out[2];
+    }
+}
+
+// Yee H half step (see orc_yee for the staggering).
+template <class T>
+__global__ void __launch_bounds__(MX * MY)
+k_yee_h(const T* __restrict__ ex, const T* __restrict__ ey, const T* __restrict__ ez, T* __restrict__ hx,
+        T* __restrict__ hy, T* __restrict__ hz, Layout L, T ch) {
+    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const int z0 = blockIdx.z * MZ, z1 = min(z0 + MZ, L.nz);
+    for (int z = z0; z < z1; ++z) {
+        const long long m = L.idx(x, y, z);
+        const bool xi = x + 1 < L.nx, yi = y + 1 < L.ny, zi = z + 1 < L.nz;
+        if (yi && zi) hx[m] -= ch * ((ez[m + L.pitch] - ez[m]) - (ey[m + L.plane] - ey[m]));
+        if (xi && zi) hy[m] -= ch * ((ex[m + L.plane] - ex[m]) - (ez[m + 1] - ez[m]));
+        if (xi && yi) hz[m] -= ch * ((ey[m + 1] - ey[m]) - (ex[m + L.pitch] - ex[m]));
+    }
+}
+
+// Yee E step with PEC walls and the soft current source.
+template <class T>
+__global__ void __launch_bounds__(MX * MY)
+k_yee_e(T* __restrict__ ex, T* __restrict__ ey, T* __restrict__ ez, const T* __restrict__ hx,
+        const T* __restrict__ hy, const T* __restrict__ hz, Layout L, T ch, long long src, T src_val) {
+    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const int z0 = blockIdx.z * MZ, z1 = min(z0 + MZ, L.nz);
+    const bool xin = x > 0 && x + 1 < L.nx, yin = y > 0 && y + 1 < L.ny;
+    for (int z = z0; z < z1; ++z) {
+        const long long m = L.idx(x, y, z);
+        const bool zin = z > 0 && z + 1 < L.nz;
+        if (x + 1 < L.nx && yin && zin) ex[m] += ch * ((hz[m] - hz[m - L.pitch]) - (hy[m] - hy[m - L.plane]));
+        if (y + 1 < L.ny && xin && zin) ey[m] += ch * ((hx[m] - hx[m - L.plane]) - (hz[m] - hz[m - 1]));
+        if (z + 1 < L.nz && xin && yin) {
+            T v = ez[m] + ch * ((hy[m] - hy[m - 1]) - (hx[m] - hx[m - L.pitch]));
+            if (m == src) v -= src_val;
+            ez[m] = v;
+        }
+    }
+}
+
+template <class T>
+__global__ void k_dense_to_field(const double* __restrict__ d, T* __restrict__ f, Layout L) {
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % L.nx);
+        const long long r = i / L.nx;
+        f[L.idx(x, (int)(r % L.ny), (int)(r / L.ny))] = (T)d[i];
+    }
+}
+
+template <class T>
+__global__ void k_field_to_dense(const T* __restrict__ f, double* __restrict__ d, Layout L) {
+    const long long n = (long long)L.nx * L.ny * L.nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % L.nx);
+        const long long r = i / L.nx;
+        d[i] = (double)f[L.idx(x, (int)(r % L.ny), (int)(r / L.ny))];
+    }
+}
+
+}  // namespace
+
+struct scafes_mf {
+    scafes_mf_cfg cfg;
+    Layout L;
+    size_t esz = 8;
+    int nfields = 0;
+    void* mem = nullptr;      // all fields, component-major
+    double* stage = nullptr;  // dense doubles for transfers
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int cur = 0;              // Lame: which half of mem holds u^n
+    int t = 0;
+    bool timed = false;
+    std::string err;
+};
+
+namespace {
+
+int mfail(scafes_mf* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf;
+    scafes::set_last_error(buf);
+    return code;
+}
+
+#define MTRY(h, call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return mfail(h, SCAFES_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                         __FILE__, __LINE__);                                                  \
+    } while (0)
+
+dim3 mgrid(const Layout& L) { return dim3((L.nx + MX - 1) / MX, (L.ny + MY - 1) / MY, (L.nz + MZ - 1) / MZ); }
+
+char* field_ptr(scafes_mf* h, int f) { return (char*)h->mem + (size_t)f * h->L.size() * h->esz; }
+
+}  // namespace
+
+extern "C" const char* scafes_mf_last_error(const scafes_mf* h) { return h ? h->err.c_str() : ""; }
+
+extern "C" void scafes_mf_destroy(scafes_mf* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    cudaFree(h->mem);
+    cudaFree(h->stage);
+    if (h->e0) cudaEventDestroy(h->e0);
+    if (h->e1) cudaEventDestroy(h->e1);
+    if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+extern "C" int scafes_mf_create(const scafes_mf_cfg* cfg, scafes_mf** out) {
+    if (!cfg || !out) return mfail(nullptr, SCAFES_ERR_ARG, "scafes_mf_create: NULL argument");
+    *out = nullptr;
+    if (cfg->kind != SCAFES_MF_LAME && cfg->kind != SCAFES_MF_YEE)
+        return mfail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_mf_create: kind %d", cfg->kind);
+    for (int p = 0; p < 3; ++p)
+        if (cfg->n_nodes[p] < 3 || cfg->n_nodes[p] > (1 << 16))
+            return mfail(nullptr, SCAFES_ERR_ARG, "scafes_mf_create: n_nodes[%d]=%d out of [3, 65536]", p, cfg->n_nodes[p]);
+    if (cfg->kind == SCAFES_MF_LAME && cfg->precision != SCAFES_PREC_F64)
+        return mfail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_mf_create: Lame-Navier runs in FP64 only");
+    if (cfg->kind == SCAFES_MF_YEE && cfg->precision != SCAFES_PREC_F64 && cfg->precision != SCAFES_PREC_F32)
+        return mfail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_mf_create: Yee runs in FP64 or FP32");
+    if (cfg->kind == SCAFES_MF_YEE)
+        for (int p = 0; p < 3; ++p)
+            if (cfg->src[p] < 0 || cfg->src[p] >= cfg->n_nodes[p])
+                return mfail(nullptr, SCAFES_ERR_ARG, "scafes_mf_create: source index out of the grid");
+    scafes_mf* h = new (std::nothrow) scafes_mf();
+    if (!h) return mfail(nullptr, SCAFES_ERR_NOMEM, "scafes_mf_create: out of host memory");
+    h->cfg = *cfg;
+    h->L = make_layout(cfg->n_nodes[0], cfg->n_nodes[1], cfg->n_nodes[2]);
+    h->esz = cfg->precision == SCAFES_PREC_F32 ? 4 : 8;
+    h->nfields = 6;  // Lame: u^n (3) + u^{n-1} (3); Yee: Ex..Hz
+    cudaError_t e = cudaSuccess;
+    if (cfg->stream) h->stream = (cudaStream_t)cfg->stream;
+    else { e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking); h->own_stream = true; }
+    const size_t bytes = (size_t)h->nfields * h->L.size() * h->esz;
+    if (e == cudaSuccess) e = cudaMalloc(&h->mem, bytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->mem, 0, bytes, h->stream);
+    if (e == cudaSuccess) e = cudaMalloc(&h->stage, (size_t)h->L.nx * h->L.ny * h->L.nz * sizeof(double));
+    if (e == cudaSuccess) e = cudaEventCreate(&h->e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&h->e1);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        const int code = e == cudaErrorMemoryAllocation ? SCAFES_ERR_NOMEM : SCAFES_ERR_CUDA;
+        mfail(nullptr, code, "scafes_mf_create: %s", cudaGetErrorString(e));
+        scafes_mf_destroy(h);
+        return code;
+    }
+    *out = h;
+    return SCAFES_OK;
+}
+
+// Lame fields 0..2 are u^n, 3..5 u^{n-1}; the halves swap every step.
+static int phys_field(const scafes_mf* h, int field) {
+    if (h->cfg.kind != SCAFES_MF_LAME) return field;
+    const int half = field / 3, comp = field % 3;
+    return ((half ^ h->cur) * 3) + comp;
+}
+
+extern "C" int scafes_mf_upload(scafes_mf* h, int field, const double* host, size_t n) {
+    if (!h || !host) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_upload: NULL argument");
+    if (field < 0 || field >= h->nfields) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_upload: field %d", field);
+    if (n != (size_t)h->L.nx * h->L.ny * h->L.nz) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_upload: wrong size");
+    MTRY(h, cudaMemcpyAsync(h->stage, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    char* f = field_ptr(h, phys_field(h, field));
+    if (h->esz == 8) k_dense_to_field<double><<<256, 256, 0, h->stream>>>(h->stage, (double*)f, h->L);
+    else k_dense_to_field<float><<<256, 256, 0, h->stream>>>(h->stage, (float*)f, h->L);
+    MTRY(h, cudaGetLastError());
+    MTRY(h, cudaStreamSynchronize(h->stream));
+    h->t = 0;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_mf_download(scafes_mf* h, int field, double* host, size_t n) {
+    if (!h || !host) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_download: NULL argument");
+    if (field < 0 || field >= h->nfields) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_download: field %d", field);
+    if (n != (size_t)h->L.nx * h->L.ny * h->L.nz) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_download: wrong size");
+    const char* f = field_ptr(h, phys_field(h, field));
+    if (h->esz == 8) k_field_to_dense<double><<<256, 256, 0, h->stream>>>((const double*)f, h->stage, h->L);
+    else k_field_to_dense<float><<<256, 256, 0, h->stream>>>((const float*)f, h->stage, h->L);
+    MTRY(h, cudaGetLastError());
+    MTRY(h, cudaMemcpyAsync(host, h->stage, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    MTRY(h, cudaStreamSynchronize(h->stream));
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_mf_step(scafes_mf* h, int n_steps) {
+    if (!h) return mfail(nullptr, SCAFES_ERR_ARG, "scafes_mf_step: NULL handle");
+    if (n_steps < 0) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_step: n_steps < 0");
+    const Layout& L = h->L;
+    const scafes_mf_cfg& c = h->cfg;
+    MTRY(h, cudaEventRecord(h->e0, h->stream));
+    if (c.kind == SCAFES_MF_LAME) {
+        const double lam = c.p[0], mu = c.p[1], rho = c.p[2];
+        double hh[3];
+        for (int p = 0; p < 3; ++p) hh[p] = (c.coord_last[p] - c.coord_first[p]) / (c.n_nodes[p] - 1);
+        const double s = c.tau * c.tau / rho;
+        LameCoef K;
+        for (int cc = 0; cc < 3; ++cc)
+            for (int p = 0; p < 3; ++p) {
+                K.a[cc][p] = s * (p == cc ? lam + 2.0 * mu : mu) / (hh[p] * hh[p]);
+                K.b[cc][p] = (p == cc) ? 0.0 : s * (lam + mu) / (4.0 * hh[cc] * hh[p]);
+            }
+        const long long comp = L.size();
+        for (int st = 0; st < n_steps; ++st) {
+            const double* u = (const double*)field_ptr(h, 3 * h->cur);
+            double* up = (double*)field_ptr(h, 3 * (h->cur ^ 1));
+            k_lame<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(u, up, K, L, comp);
+            MTRY(h, cudaGetLastError());
+            h->cur ^= 1;
+            h->t += 1;
+        }
+    } else {
+        const double hgrid = (c.coord_last[0] - c.coord_first[0]) / (c.n_nodes[0] - 1);
+        const double ch = c.tau / hgrid;
+        const long long src = L.idx(c.src[0], c.src[1], c.src[2]);
+        const double amp = c.p[0], t0 = c.p[1], w = c.p[2], freq = c.p[3];
+        for (int st = 0; st < n_steps; ++st) {
+            const double time = c.t_start + (h->t + 1) * c.tau;
+            const double a = (time - t0) / w;
+            const double sv = c.tau * amp * std::exp(-a * a) * std::sin(2.0 * 3.14159265358979323846 * freq * time);
+            if (h->esz == 8) {
+                double* f[6];
+                for (int i = 0; i < 6; ++i) f[i] = (double*)field_ptr(h, i);
+                k_yee_h<double><<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L, ch);
+                k_yee_e<double><<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L, ch,
+                                                                          src, sv);
+            } else {
+                float* f[6];
+                for (int i = 0; i < 6; ++i) f[i] = (float*)field_ptr(h, i);
+                k_yee_h<float><<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L,
+                                                                         (float)ch);
+                k_yee_e<float><<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L,
+                                                                         (float)ch, src, (float)sv);
+            }
+            MTRY(h, cudaGetLastError());
+            h->t += 1;
+        }
+    }
+    MTRY(h, cudaEventRecord(h->e1, h->stream));
+    h->timed = true;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_mf_last_ms(const scafes_mf* h, float* ms) {
+    if (!h || !ms) return mfail(nullptr, SCAFES_ERR_ARG, "scafes_mf_last_ms: NULL argument");
+    if (!h->timed) return mfail(nullptr, SCAFES_ERR_STATE, "scafes_mf_last_ms: nothing ran yet");
+    cudaError_t e = cudaEventSynchronize(h->e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(ms, h->e0, h->e1);
+    if (e != cudaSuccess) return mfail(nullptr, SCAFES_ERR_CUDA, "scafes_mf_last_ms: %s", cudaGetErrorString(e));
+    return SCAFES_OK;
+}

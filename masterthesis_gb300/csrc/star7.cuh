@@ -22,6 +22,30 @@ struct Star7Coeffs {
 
 Star7Coeffs make_star7_coeffs(double c0, const double cp[3], double cf);
 
+// A scalar in double and split into an FP32 pair (hi + lo), prepared on the
+// host so that the FP32 kernels never convert doubles themselves.
+struct Split {
+    double d;
+    float hi, lo;
+};
+
+inline Split make_split(double v) {
+    Split s;
+    s.d = v;
+    f2 p = split_double(v);
+    s.hi = p.hi;
+    s.lo = p.lo;
+    return s;
+}
+
+__host__ __device__ inline Split negated(const Split& s) {
+    Split r;
+    r.d = -s.d;
+    r.hi = -s.hi;
+    r.lo = -s.lo;
+    return r;
+}
+
 // Width (elements) of the TMA box of the sweep for a precision: the 32-wide
 // tile plus a halo padded to 16 bytes on each side.
 int star7_box_width(int precision);
@@ -41,8 +65,8 @@ struct Star7Launch {
     void* un;             // new iterate
     const void* fa;       // source F_A (element type per precision) or null
     const void* fb;       // source F_B or null
-    const double* ga;     // border value G_A (double) or null
-    const double* gb;     // border value G_B (double) or null
+    const void* ga;       // border value G_A (element type per precision) or null
+    const void* gb;       // border value G_B or null
     double gconst;        // border value when ga is null
     Star7Coeffs c;
     double time_old;      // time(t)   : F is read at the old time

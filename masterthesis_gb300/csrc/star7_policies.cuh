@@ -24,11 +24,11 @@ struct PolF64 {
         if (HAS_F) v = fma(c.cf, f, v);
         return v;
     }
-    static __device__ __forceinline__ T mirror(T u, T uo, double corr) {
-        return (u + uo) - corr;
+    static __device__ __forceinline__ T mirror(T u, T uo, const Split& corr) {
+        return (u + uo) - corr.d;
     }
-    static __device__ __forceinline__ T src(T fa, T fb, double time, bool has_b) {
-        return has_b ? fa + time * fb : fa;
+    static __device__ __forceinline__ T src(T fa, T fb, const Split& time, bool has_b) {
+        return has_b ? fa + time.d * fb : fa;
     }
 };
 
@@ -46,11 +46,11 @@ struct PolF32 {
         if (HAS_F) v = fmaf(c.cfh, f, v);
         return v;
     }
-    static __device__ __forceinline__ T mirror(T u, T uo, double corr) {
-        return (u + uo) - (float)corr;
+    static __device__ __forceinline__ T mirror(T u, T uo, const Split& corr) {
+        return (u + uo) - corr.hi;
     }
-    static __device__ __forceinline__ T src(T fa, T fb, double time, bool has_b) {
-        return has_b ? fa + (float)time * fb : fa;
+    static __device__ __forceinline__ T src(T fa, T fb, const Split& time, bool has_b) {
+        return has_b ? fmaf(time.hi, fb, fa) : fa;
     }
 };
 
@@ -121,20 +121,26 @@ struct PolF32x2 {
         f2 out = fast_two_sum(hi, r);
         return make_float2(out.hi, out.lo);
     }
-    static __device__ __forceinline__ T mirror(T u, T uo, double corr) {
+    static __device__ __forceinline__ T mirror(T u, T uo, const Split& corr) {
         // (u + uo) - corr with corr a power of two (exact in FP32).
         f2 s = two_sum(u.x, uo.x);
         float lo = s.lo + (u.y + uo.y);
-        f2 d = two_sum(s.hi, -(float)corr);
+        f2 d = two_sum(s.hi, -corr.hi);
         f2 out = fast_two_sum(d.hi, d.lo + lo);
         return make_float2(out.hi, out.lo);
     }
-    static __device__ __forceinline__ T src(T fa, T fb, double time, bool has_b) {
+    static __device__ __forceinline__ T src(T fa, T fb, const Split& time, bool has_b) {
         if (!has_b) return fa;
-        // fa + time * fb; F_B is rare (time-dependent sources only), so FP64
-        // here costs nothing measurable.  The result is split back.
-        double v = ((double)fa.x + (double)fa.y) + time * ((double)fb.x + (double)fb.y);
-        return from_double(v);
+        // fa + time * fb in pair arithmetic with time split on the host: no
+        // FP64 instruction on this path (a predicated FP64 instruction would
+        // still occupy the GB300's narrow FP64 pipe in every lane).
+        float p = time.hi * fb.x;
+        float e = fmaf(time.hi, fb.x, -p);
+        e = fmaf(time.hi, fb.y, e);
+        e = fmaf(time.lo, fb.x, e);
+        f2 s = two_sum(fa.x, p);
+        f2 out = fast_two_sum(s.hi, s.lo + (fa.y + e));
+        return make_float2(out.hi, out.lo);
     }
 };
 

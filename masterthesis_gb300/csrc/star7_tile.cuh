@@ -44,11 +44,11 @@ struct TileJob {
     T* un;                   // new iterate
     const T* fa;             // source F_A or null
     const T* fb;             // source F_B or null
-    const double* ga;        // border value G_A or null (then gconst)
-    const double* gb;        // border value G_B or null
-    double gconst;           // border value when ga is null
+    const T* ga;             // border value G_A or null (then gval)
+    const T* gb;             // border value G_B or null
+    T gval;                  // border value when ga is null
     Layout L;
-    double time_old, time_new, corr;
+    Split time_old, time_new, corr;  // time(t), time(t+1), mirror correction
 };
 
 // Initialises the ring's mbarriers (thread 0) -- once per CTA.
@@ -138,21 +138,22 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                         if (HAS_F) f = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
                         v = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
                     } else if (BORDER == SCAFES_BORDER_DIRICHLET) {
-                        double g = J.ga ? J.ga[off] : J.gconst;
-                        if (has_gb) g += J.time_new * J.gb[off];
-                        v = P::from_double(g);
+                        // Border values are stored in the element type, so
+                        // this branch does no FP64 work on the FP32 paths.
+                        v = J.ga ? J.ga[off] : J.gval;
+                        if (has_gb) v = P::src(v, J.gb[off], J.time_new, true);
                     } else {
                         // Mirror border: the last face (in direction order
                         // x-, x+, y-, y+, z-, z+) the node lies on decides.
                         T opp;
-                        double cs;
-                        if (z == L.nz - 1)      { opp = below[k]; cs = -J.corr; }
-                        else if (z == 0)        { opp = above[k]; cs = J.corr; }
-                        else if (y == L.ny - 1) { opp = s; cs = -J.corr; }
-                        else if (y == 0)        { opp = n; cs = J.corr; }
-                        else if (x == L.nx - 1) { opp = w; cs = -J.corr; }
-                        else                    { opp = e; cs = J.corr; }
-                        v = P::mirror(cur[k], opp, cs);
+                        bool minus;
+                        if (z == L.nz - 1)      { opp = below[k]; minus = true; }
+                        else if (z == 0)        { opp = above[k]; minus = false; }
+                        else if (y == L.ny - 1) { opp = s; minus = true; }
+                        else if (y == 0)        { opp = n; minus = false; }
+                        else if (x == L.nx - 1) { opp = w; minus = true; }
+                        else                    { opp = e; minus = false; }
+                        v = P::mirror(cur[k], opp, minus ? negated(J.corr) : J.corr);
                     }
                     J.un[off] = v;
                 }

@@ -15,9 +15,9 @@ template <class P, bool HAS_F, int BORDER, int BY, int R>
 __global__ void __launch_bounds__(BX * (BY / R))
 star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un,
           const typename P::T* __restrict__ fa, const typename P::T* __restrict__ fb,
-          const double* __restrict__ ga, const double* __restrict__ gb, double gconst,
-          Layout L, Star7Coeffs c, double time_old, double time_new,
-          double corr, int zchunk, int* __restrict__ status)
+          const typename P::T* __restrict__ ga, const typename P::T* __restrict__ gb, typename P::T gval,
+          Layout L, Star7Coeffs c, Split time_old, Split time_new,
+          Split corr, int zchunk, int* __restrict__ status)
 {
     using T = typename P::T;
     using G = Tile<T, BY>;
@@ -25,7 +25,7 @@ star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
     T* st = reinterpret_cast<T*>(smem_raw);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NSTAGE * G::STRIDE * G::ESZ);
     ring_init<T, BY>(bar);
-    TileJob<T> J{&tm, un, fa, fb, ga, gb, gconst, L, time_old, time_new, corr};
+    TileJob<T> J{&tm, un, fa, fb, ga, gb, gval, L, time_old, time_new, corr};
     const int z0 = blockIdx.z * zchunk;
     const int z1 = min(z0 + zchunk, L.nz);
     uint32_t base = 0;
@@ -86,6 +86,14 @@ static int choose_zchunk(const Layout& L, int by) {
     return zc;
 }
 
+// A double as the element type of a precision (host side).
+static inline void to_elem(double d, double& out) { out = d; }
+static inline void to_elem(double d, float& out) { out = (float)d; }
+static inline void to_elem(double d, float2& out) {
+    f2 p = split_double(d);
+    out = make_float2(p.hi, p.lo);
+}
+
 template <class P, bool HAS_F, int BORDER, int BY, int R>
 static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
     using T = typename P::T;
@@ -95,13 +103,21 @@ static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
+        // The ring lives in shared memory: ask for the largest carveout so
+        // that occupancy is not capped by a small L1/shared split.
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
         attr = true;
     }
+    T gval;
+    to_elem(a.gconst, gval);
     const int zchunk = choose_zchunk(L, BY);
     dim3 block(BX, BY / R, 1);
     dim3 grid((L.nx + BX - 1) / BX, (L.ny + BY - 1) / BY, (L.nz + zchunk - 1) / zchunk);
-    kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, (T*)a.un, (const T*)a.fa, (const T*)a.fb, a.ga, a.gb, a.gconst, L,
-                                           a.c, a.time_old, a.time_new, a.mirror_corr, zchunk, a.status);
+    kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, (T*)a.un, (const T*)a.fa, (const T*)a.fb, (const T*)a.ga,
+                                           (const T*)a.gb, gval, L,
+                                           a.c, make_split(a.time_old), make_split(a.time_new),
+                                           make_split(a.mirror_corr), zchunk, a.status);
     return cudaGetLastError();
 }
 

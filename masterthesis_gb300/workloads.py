@@ -83,3 +83,44 @@ def pennes_batch_instance(spec: dict):
 
 def pennes_source(spec: dict) -> np.ndarray:
     return spec["w_b"] * T_ARTERIAL + spec["q"]
+
+
+def gaussian_bump_displacement(n, seed: int = 3):
+    """Lame-Navier initial displacement: a seeded Gaussian bump per
+    component (centre c ~ U[0.35, 0.65]^3, width s ~ U[0.05, 0.1],
+    amplitude ~ U[-1, 1] per component), zero on the border.  Shape
+    (3, nz, ny, nx)."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.35, 0.65, 3)
+    s = float(rng.uniform(0.05, 0.1))
+    amp = rng.uniform(-1.0, 1.0, 3)
+    x = np.arange(n[0]) / (n[0] - 1)
+    y = np.arange(n[1]) / (n[1] - 1)
+    z = np.arange(n[2]) / (n[2] - 1)
+    r2 = (x[None, None, :] - c[0]) ** 2 + (y[None, :, None] - c[1]) ** 2 + (z[:, None, None] - c[2]) ** 2
+    bump = np.exp(-r2 / (2.0 * s * s))
+    u = np.stack([a * bump for a in amp])
+    u[:, 0, :, :] = u[:, -1, :, :] = 0.0
+    u[:, :, 0, :] = u[:, :, -1, :] = 0.0
+    u[:, :, :, 0] = u[:, :, :, -1] = 0.0
+    return u
+
+
+def lame_tau(n, lam=1.0, mu=0.5, rho=1.0, safety: float = 0.5) -> float:
+    """A stable leapfrog step for the Lame-Navier scheme: ``safety`` times
+    h / (c_p sqrt(3)) with the pressure-wave speed c_p = sqrt((lam+2mu)/rho)."""
+    h = 1.0 / (max(n) - 1)
+    return safety * h / (np.sqrt((lam + 2.0 * mu) / rho) * np.sqrt(3.0))
+
+
+def yee_setup(n, seed: int = 4, courant: float = 0.5):
+    """Yee workload: tau = courant * h / sqrt(3) (eps = mu = 1) and a seeded
+    point dipole (Ez soft source) near the centre; source parameters
+    (amp, t0, w, freq) of a Gaussian-modulated sine a few periods long."""
+    rng = np.random.default_rng(seed)
+    h = 1.0 / (n[0] - 1)
+    tau = courant * h / np.sqrt(3.0)
+    src = tuple(int(v) for v in (np.array(n) // 2 + rng.integers(-2, 3, 3)))
+    freq = 4.0
+    w = 1.0 / freq
+    return tau, src, (1.0, 2.0 * w, w, freq)

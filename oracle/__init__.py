@@ -71,8 +71,11 @@ def lib():
         L.orc_stencil_width_var.argtypes = [C.POINTER(Grid), C.c_int, C.c_int, dp, C.c_int]
         L.orc_kheat_forward.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.c_int]
         L.orc_kheat_adjoint.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, dp, dp, dp, C.c_int]
+        L.orc_lame.argtypes = [C.POINTER(Grid), C.c_double, C.c_double, C.c_double, C.c_int, dp, dp, C.c_int]
+        L.orc_yee.argtypes = [C.POINTER(Grid), C.c_int, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                              C.c_double, C.c_double, C.c_int]
         for f in ("orc_heat_dirichlet", "orc_pennes_mri", "orc_stencil_width_one",
-                  "orc_stencil_width_var", "orc_kheat_forward", "orc_kheat_adjoint"):
+                  "orc_stencil_width_var", "orc_kheat_forward", "orc_kheat_adjoint", "orc_lame", "orc_yee"):
             getattr(L, f).restype = C.c_int
         L.orc_time.restype = C.c_double
         L.orc_time.argtypes = [C.POINTER(Grid), C.c_int]
@@ -170,6 +173,22 @@ def kheat_adjoint(g: Grid, k, traj, target, nthreads=0):
     _check(lib().orc_kheat_adjoint(C.byref(g), _p(k), nsteps, _p(traj), _p(target), _p(gk), _p(gu),
                                    C.byref(j), nthreads), "kheat_adjoint")
     return j.value, gk, gu
+
+
+def lame(g: Grid, u, uprev, nsteps, lam, mu, rho, nthreads=0):
+    """u, uprev: arrays (3, nz, ny, nx); returns (u^nsteps, u^(nsteps-1))."""
+    u = np.ascontiguousarray(u, dtype=np.float64).copy()
+    up = np.ascontiguousarray(uprev, dtype=np.float64).copy()
+    _check(lib().orc_lame(C.byref(g), lam, mu, rho, nsteps, _p(u), _p(up), nthreads), "lame")
+    return u, up
+
+
+def yee(g: Grid, fields, nsteps, src, amp, t0, w, freq, nthreads=0):
+    """fields: array (6, nz, ny, nx) = Ex, Ey, Ez, Hx, Hy, Hz."""
+    f = np.ascontiguousarray(fields, dtype=np.float64).copy()
+    _check(lib().orc_yee(C.byref(g), nsteps, _p(f), int(src[0]), int(src[1]), int(src[2]), amp, t0, w, freq,
+                         nthreads), "yee")
+    return f
 
 
 # ---- reference-driver programs (oracle/_ref) ---------------------------------

@@ -417,3 +417,102 @@ int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
     free(lam); free(lam2); free(lt);
     return 0;
 }
+
+/* ---- Lame-Navier (leapfrog) ------------------------------------------- */
+
+int orc_lame(const orc_grid* g, double lambda, double mu, double rho, int nsteps,
+             double* u, double* uprev, int nthreads)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const size_t nn = n_total(g);
+    const long stride[3] = {1, nx, (long)nx * ny};
+    double* un = (double*)malloc(3 * nn * sizeof(double));
+    if (!un) return -1;
+    set_threads(nthreads);
+    const double c = g->tau * g->tau / rho;
+    for (int t = 1; t <= nsteps; ++t) {
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nz; ++k) {
+            for (int j = 0; j < ny; ++j) {
+                for (int i = 0; i < nx; ++i) {
+                    const size_t m = IDX(i, j, k, nx, ny);
+                    if (orc_is_border(g, i, j, k)) {
+                        for (int cc = 0; cc < 3; ++cc) un[cc * nn + m] = 0.0;
+                        continue;
+                    }
+                    for (int cc = 0; cc < 3; ++cc) {
+                        const double* uc = u + cc * nn;
+                        double L = 0.0;
+                        for (int p = 0; p < 3; ++p) {
+                            const double d2 = (uc[m + stride[p]] - 2.0 * uc[m] + uc[m - stride[p]]) / (g->h[p] * g->h[p]);
+                            L += (p == cc ? lambda + 2.0 * mu : mu) * d2;
+                        }
+                        for (int q = 0; q < 3; ++q) {
+                            if (q == cc) continue;
+                            const double* uq = u + q * nn;
+                            const long sp = stride[cc], sq = stride[q];
+                            const double dm = (uq[m + sp + sq] - uq[m + sp - sq] - uq[m - sp + sq] + uq[m - sp - sq])
+                                              / (4.0 * g->h[cc] * g->h[q]);
+                            L += (lambda + mu) * dm;
+                        }
+                        un[cc * nn + m] = 2.0 * uc[m] - uprev[cc * nn + m] + c * L;
+                    }
+                }
+            }
+        }
+        memcpy(uprev, u, 3 * nn * sizeof(double));
+        memcpy(u, un, 3 * nn * sizeof(double));
+    }
+    free(un);
+    return 0;
+}
+
+/* ---- Yee FDTD ----------------------------------------------------------
+ * Staggering on an n^3 index grid with spacing h (the grid's h[0]):
+ *   Ex(i,j,k) at (i+1/2, j, k)   Hx(i,j,k) at (i, j+1/2, k+1/2)
+ *   Ey(i,j,k) at (i, j+1/2, k)   Hy(i,j,k) at (i+1/2, j, k+1/2)
+ *   Ez(i,j,k) at (i, j, k+1/2)   Hz(i,j,k) at (i+1/2, j+1/2, k)
+ * H update for all cells with the forward neighbours inside; E update for
+ * all edges with the backward neighbours inside; tangential E on the
+ * boundary faces (and components past the last node) held at 0 (PEC). */
+int orc_yee(const orc_grid* g, int nsteps, double* f, int si, int sj, int sk,
+            double amp, double t0, double w, double freq, int nthreads)
+{
+    const int n0 = g->n[0], n1 = g->n[1], n2 = g->n[2];
+    const size_t nn = n_total(g);
+    double *ex = f, *ey = f + nn, *ez = f + 2 * nn, *hx = f + 3 * nn, *hy = f + 4 * nn, *hz = f + 5 * nn;
+    const long sy = n0, sz = (long)n0 * n1;
+    const double ch = g->tau / g->h[0];
+    set_threads(nthreads);
+    for (int t = 1; t <= nsteps; ++t) {
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < n2; ++k)
+            for (int j = 0; j < n1; ++j)
+                for (int i = 0; i < n0; ++i) {
+                    const size_t m = IDX(i, j, k, n0, n1);
+                    if (j + 1 < n1 && k + 1 < n2)
+                        hx[m] -= ch * ((ez[m + sy] - ez[m]) - (ey[m + sz] - ey[m]));
+                    if (i + 1 < n0 && k + 1 < n2)
+                        hy[m] -= ch * ((ex[m + sz] - ex[m]) - (ez[m + 1] - ez[m]));
+                    if (i + 1 < n0 && j + 1 < n1)
+                        hz[m] -= ch * ((ey[m + 1] - ey[m]) - (ex[m + sy] - ex[m]));
+                }
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < n2; ++k)
+            for (int j = 0; j < n1; ++j)
+                for (int i = 0; i < n0; ++i) {
+                    const size_t m = IDX(i, j, k, n0, n1);
+                    if (i + 1 < n0 && j > 0 && j + 1 < n1 && k > 0 && k + 1 < n2)
+                        ex[m] += ch * ((hz[m] - hz[m - sy]) - (hy[m] - hy[m - sz]));
+                    if (j + 1 < n1 && i > 0 && i + 1 < n0 && k > 0 && k + 1 < n2)
+                        ey[m] += ch * ((hx[m] - hx[m - sz]) - (hz[m] - hz[m - 1]));
+                    if (k + 1 < n2 && i > 0 && i + 1 < n0 && j > 0 && j + 1 < n1)
+                        ez[m] += ch * ((hy[m] - hy[m - 1]) - (hx[m] - hx[m - sy]));
+                }
+        const double time = orc_time(g, t);
+        const double a = (time - t0) / w;
+        const double J = amp * exp(-a * a) * sin(2.0 * 3.14159265358979323846 * freq * time);
+        ez[IDX(si, sj, sk, n0, n1)] -= g->tau * J;
+    }
+    return 0;
+}

@@ -104,6 +104,26 @@ int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
                       double* grad_k, double* grad_u0, double* j_out,
                       int nthreads);
 
+/* Lame-Navier elastic wave, leapfrog in time (no reference counterpart that
+ * runs: examples/LameNavierEqnFDM/LameNavierEqnFDM.hpp:23-25 states the
+ * reference cannot advance it).  u and uprev hold 3 components of n nodes
+ * each (component-major); inner nodes:
+ *   u_new_c = 2 u_c - uprev_c + tau^2/rho [ (lambda+2mu) d_cc u_c
+ *             + mu sum_{p!=c} d_pp u_c + (lambda+mu) sum_{q!=c} d_cq u_q ]
+ * with central second differences and the 4-point mixed difference
+ * d_pq f = (f(+p+q) - f(+p-q) - f(-p+q) + f(-p-q)) / (4 h_p h_q);
+ * border nodes are held at 0.  On exit u is step nsteps, uprev step
+ * nsteps-1. */
+int orc_lame(const orc_grid* g, double lambda, double mu, double rho, int nsteps,
+             double* u, double* uprev, int nthreads);
+
+/* Yee FDTD in a PEC box, eps = mu = 1 scaled (see orc_yee in the .c file
+ * for the staggering).  f holds Ex, Ey, Ez, Hx, Hy, Hz (n nodes each).
+ * Each step: H half step, E step, then the soft current source
+ * Ez[src] -= tau * J(time), J(t) = amp * exp(-((t - t0)/w)^2) sin(2 pi freq t). */
+int orc_yee(const orc_grid* g, int nsteps, double* f, int src_i, int src_j, int src_k,
+            double amp, double t0, double w, double freq, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

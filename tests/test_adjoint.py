@@ -1,0 +1,118 @@
+"""Hand-written adjoint with binomial checkpointing.
+
+CPU: the schedule's forward-step count against a brute-force dynamic
+program.  GPU (C ABI): J, dJ/dk and dJ/du0 against the CPU oracle's adjoint
+(itself checked against central differences in test_oracle_golden.py),
+identical results for every snapshot count, and central finite differences
+of J on seeded random directions computed with the GPU forward solve.
+Tolerances: 1e-11 relative max-norm against the oracle (FP64, different
+evaluation order); 1e-6 relative against central differences.
+"""
+from __future__ import annotations
+
+import functools
+
+import numpy as np
+import pytest
+
+import cases
+import oracle as O
+
+
+def brute_cost(n, s):
+    @functools.lru_cache(maxsize=None)
+    def c(nn, ss):
+        if nn == 1:
+            return 0
+        if ss == 0:
+            return nn * (nn - 1) // 2
+        return min(m + c(nn - m, ss - 1) + c(m, ss) for m in range(1, nn))
+    return c(n, min(s, n - 1)) + 1
+
+
+@pytest.mark.parametrize("n,snaps", [(1, 2), (2, 2), (7, 2), (30, 3), (64, 5), (100, 8), (50, 51), (200, 12)])
+def test_schedule_cost_matches_brute_force(native, n, snaps):
+    assert native.Adjoint.schedule_cost(n, snaps) == brute_cost(n, snaps - 1)
+
+
+def test_schedule_cost_store_all_and_monotone(native):
+    A = native.Adjoint
+    assert A.schedule_cost(2000, 2000) == 2000
+    costs = [A.schedule_cost(500, s) for s in (2, 3, 5, 10, 20, 45, 100, 500)]
+    assert all(a >= b for a, b in zip(costs, costs[1:]))
+
+
+def kheat_problem(n, T, seed):
+    rng = np.random.default_rng(seed)
+    shape = (n[2], n[1], n[0])
+    g = rng.standard_normal(shape)
+    for _ in range(3):  # smooth by Jacobi passes
+        g[1:-1, 1:-1, 1:-1] = (g[2:, 1:-1, 1:-1] + g[:-2, 1:-1, 1:-1] + g[1:-1, 2:, 1:-1] + g[1:-1, :-2, 1:-1]
+                               + g[1:-1, 1:-1, 2:] + g[1:-1, 1:-1, :-2]) / 6.0
+    k = np.exp(0.3 * g)
+    tau = 0.9 / (2.0 * k.max() * sum((m - 1) ** 2 for m in n))
+    u0 = rng.uniform(-1.0, 1.0, shape)
+    target = rng.uniform(-1.0, 1.0, shape)
+    return k, tau, u0, target
+
+
+@pytest.mark.gpu
+def test_adjoint_matches_oracle_all_snapshot_counts(gpu):
+    M = gpu
+    n, T = (12, 10, 9), 30
+    k, tau, u0, target = kheat_problem(n, T, 7)
+    g = O.make_grid(n, tau=tau)
+    _, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
+    J_ref, gk_ref, gu_ref = O.kheat_adjoint(g, k, traj, target)
+    first = None
+    for snaps in (2, 3, 7, 31, 64):
+        with M.Adjoint(n, tau, snaps) as a:
+            a.set_conductivity(k)
+            J, gk, gu = a.gradient(u0, target, T)
+            st = a.stats()
+        assert abs(J - J_ref) <= 1e-12 * abs(J_ref)
+        assert cases.rel_err(gk, gk_ref) <= 1e-11, snaps
+        assert cases.rel_err(gu, gu_ref) <= 1e-11, snaps
+        assert st["adjoint_steps"] == T
+        assert st["forward_steps"] == M.Adjoint.schedule_cost(T, snaps)
+        if first is None:
+            first = (gk, gu)
+        else:
+            assert np.array_equal(gk, first[0]) and np.array_equal(gu, first[1]), snaps
+
+
+@pytest.mark.gpu
+def test_adjoint_forward_matches_oracle(gpu):
+    M = gpu
+    n, T = (17, 9, 13), 25
+    k, tau, u0, _ = kheat_problem(n, T, 3)
+    g = O.make_grid(n, tau=tau)
+    with M.Adjoint(n, tau, 2) as a:
+        a.set_conductivity(k)
+        uT = a.forward(u0, T)
+    assert cases.rel_err(uT, O.kheat_forward(g, k, u0, T)) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_adjoint_gradient_vs_central_differences(gpu):
+    M = gpu
+    n, T = (20, 18, 16), 40
+    k, tau, u0, target = kheat_problem(n, T, 11)
+    with M.Adjoint(n, tau, 6) as a:
+        a.set_conductivity(k)
+        J, gk, gu = a.gradient(u0, target, T)
+
+        def J_of(kk, uu):
+            a.set_conductivity(kk)
+            uT = a.forward(uu, T)
+            return 0.5 * float(np.sum((uT - target) ** 2))
+
+        for seed in range(4):
+            rng = np.random.default_rng(1000 + seed)
+            dk = rng.standard_normal(k.shape) * k
+            du = rng.standard_normal(k.shape)
+            eps = 1e-6
+            fd_k = (J_of(k + eps * dk, u0) - J_of(k - eps * dk, u0)) / (2 * eps)
+            fd_u = (J_of(k, u0 + eps * du) - J_of(k, u0 - eps * du)) / (2 * eps)
+            assert abs(fd_k - float(np.sum(gk * dk))) <= 1e-6 * abs(fd_k), seed
+            assert abs(fd_u - float(np.sum(gu * du))) <= 1e-6 * abs(fd_u), seed
