@@ -392,11 +392,11 @@ def run_ours(args, dist: Dist):
     launch_s = dt / (args.steps * T)
     hbm_peak, peak_src = measured_peaks()
     achieved_gbs = B_PER_LUP["f64"] * nn / launch_s / 1e9
-    traffic = ncu_traffic("star7_sweep<PolF64>")
+    traffic = ncu_traffic("star7_tma<PolF64>")
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                "kernel": "star7_sweep<PolF64>", "bytes_per_launch_alg": B_PER_LUP["f64"] * nn,
+                "kernel": "star7_tma<PolF64>", "bytes_per_launch_alg": B_PER_LUP["f64"] * nn,
                 "launch_ms": launch_s * 1e3}
     fp64_peak, fp32_peak = pipe_peaks()
     if fp64_peak:

@@ -69,6 +69,9 @@ batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ 
         if (it >= n_items) break;
         const BatchItem w = items[it];
         const BatchInst& I = inst[w.inst];
+        // Coefficients in registers: read through `I`, every store to the
+        // pool could alias them and force a reload per node.
+        const Star7Coeffs c = I.c;
         TileJob<T> J;
         J.tm = maps + (long long)(2 * w.inst + cur) * map_stride;
         J.un = pool + I.off_u[cur ^ 1];
@@ -79,7 +82,7 @@ batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ 
         J.gval = P::from_double(I.gconst);
         J.L = I.L;
         J.time_old = J.time_new = J.corr = Split{0.0, 0.f, 0.f};
-        if (!star7_tile<P, true, SCAFES_BORDER_DIRICHLET, BY, R>(J, I.c, w.tx * BX, w.ty * BY, w.z0, w.z1, st, bar,
+        if (!star7_tile<P, true, SCAFES_BORDER_DIRICHLET, BY, R>(J, c, w.tx * BX, w.ty * BY, w.z0, w.z1, st, bar,
                                                                  base, status))
             break;
     }

@@ -96,32 +96,53 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
     const bool xb = (x == 0 || x == L.nx - 1);
     const bool has_fb = (J.fb != nullptr);
     const bool has_gb = (J.gb != nullptr);
+    // The whole 32 x BY tile holds inner columns: no per-node border tests.
+    const bool tile_inner = x0 >= 1 && x0 + BX <= L.nx - 1 && y0 >= 1 && y0 + BY <= L.ny - 1;
     const int cc = G::LP + tx;  // this thread's column inside a stage row
     auto slot = [&](int p) { return (b0 + (uint32_t)p) & (NSTAGE - 1); };
     auto phase = [&](int p) { return ((b0 + (uint32_t)p) / NSTAGE) & 1; };
 
     bool ok = bounded_wait(&bar[slot(0)], phase(0));
     ok = bounded_wait(&bar[slot(1)], phase(1)) && ok;
-    T below[R], cur[R];
+    // z-marching queue: three register blocks whose roles (below, current,
+    // above) rotate from plane to plane, so no values are moved.
+    T qa[R], qb[R], qc[R];
 #pragma unroll
     for (int k = 0; k < R; ++k) {
-        below[k] = st[slot(0) * G::STRIDE + (rb + k) * G::W + cc];
-        cur[k] = st[slot(1) * G::STRIDE + (rb + k) * G::W + cc];
+        qa[k] = st[slot(0) * G::STRIDE + (rb + k) * G::W + cc];
+        qb[k] = st[slot(1) * G::STRIDE + (rb + k) * G::W + cc];
     }
-    int p = 1;
-    for (int z = z0; z < z1; ++z, ++p) {
+    int p = 1;  // plane index of the current z (plane p holds z = z0 - 1 + p)
+    int z = z0;
+
+    // One z-plane: `below`, `cur` hold planes p-1, p; `above` receives p+1.
+    // Returns false when a stage did not arrive in any thread of the CTA.
+    auto plane = [&](const T (&below)[R], const T (&cur)[R], T (&above)[R]) -> bool {
         const uint32_t sa = slot(p + 1);
         ok = bounded_wait(&bar[sa], phase(p + 1)) && ok;
         const T* pl = st + slot(p) * G::STRIDE + cc;
         const T* pa = st + sa * G::STRIDE + cc;
-        T above[R];
 #pragma unroll
         for (int k = 0; k < R; ++k) above[k] = pa[(rb + k) * G::W];
-        if (xin && ok) {
-            const bool zb = (z == 0 || z == L.nz - 1);
+        const bool zb = (z == 0 || z == L.nz - 1);
+        const T ym = pl[(rb - 1) * G::W];
+        const T yp = pl[(rb + R) * G::W];
+        if (ok && tile_inner && !zb) {
+            // Inner plane of an inner tile: every node takes the star.
+            const long long o0 = (long long)z * L.plane + (long long)yb * L.pitch + x;
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const long long off = o0 + (long long)k * L.pitch;
+                const T s = (k == 0) ? ym : cur[k - 1];
+                const T n = (k == R - 1) ? yp : cur[k + 1];
+                const T w = pl[(rb + k) * G::W - 1];
+                const T e = pl[(rb + k) * G::W + 1];
+                T f = P::zero();
+                if (HAS_F) f = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
+                J.un[off] = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
+            }
+        } else if (ok && xin) {
             const long long zoff = (long long)z * L.plane + x;
-            const T ym = pl[(rb - 1) * G::W];
-            const T yp = pl[(rb + R) * G::W];
 #pragma unroll
             for (int k = 0; k < R; ++k) {
                 const int y = yb + k;
@@ -159,13 +180,8 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 }
             }
         }
-#pragma unroll
-        for (int k = 0; k < R; ++k) {
-            below[k] = cur[k];
-            cur[k] = above[k];
-        }
         // Everyone is done with plane p-1: its stage takes plane p-1+NSTAGE.
-        if (!__syncthreads_and(ok)) break;
+        if (!__syncthreads_and(ok)) return false;
         if (tid == 0) {
             const int pn = p - 1 + NSTAGE;
             if (pn < np) {
@@ -175,8 +191,18 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 tma_load_3d(st + s * G::STRIDE, J.tm, x0 - G::LP, y0 - 1, z0 - 1 + pn, &bar[s]);
             }
         }
+        ++p;
+        ++z;
+        return true;
+    };
+
+    bool all_ok = true;
+    while (z < z1) {
+        if (!(all_ok = plane(qa, qb, qc)) || z >= z1) break;
+        if (!(all_ok = plane(qb, qc, qa)) || z >= z1) break;
+        if (!(all_ok = plane(qc, qa, qb))) break;
     }
-    if (!__syncthreads_and(ok)) {
+    if (!all_ok) {
         if (tid == 0) {
             // A stage never completed: report, drain what was issued, stop.
             atomicExch(status, SCAFES_ERR_TIMEOUT);
