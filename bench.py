@@ -425,7 +425,7 @@ def run_ours(args, dist: Dist):
     e2e = {"value": dist.world * nn * T * len(e2e_times) / e2e_dt / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": nn * 8, "d2h_bytes_per_step": nn * 8,
            "ms_per_step": e2e_dt / len(e2e_times) * 1e3,
-           "path": "scafes_gpu_upload + scafes_gpu_step(1000) + scafes_gpu_download, pinned host buffers"}
+           "path": f"scafes_gpu_upload + scafes_gpu_step({T}) + scafes_gpu_download, pinned host buffers"}
 
     variants = {}
     if not args.no_variants:

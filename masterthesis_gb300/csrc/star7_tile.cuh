@@ -13,6 +13,8 @@
 // zero-filled by the TMA unit.  Stores are row-contiguous per warp.
 #pragma once
 
+#include <type_traits>
+
 #include "star7_policies.cuh"
 #include "tma.cuh"
 #include "../../include/scafes_gb300.h"
@@ -61,18 +63,24 @@ __device__ __forceinline__ void ring_init(uint64_t* bar) {
     __syncthreads();
 }
 
+// Source term of the update, fixed at compile time so that no predicated
+// arithmetic of an absent term is issued: none, F_A, or F_A + time * F_B.
+enum : int { SRC_NONE = 0, SRC_A = 1, SRC_AB = 2 };
+
 // Processes planes [z0, z1) of the tile at (x0, y0).  `base` counts the
 // planes this CTA has streamed through the ring so far (it fixes the stage
 // and phase of every plane); it is advanced by the planes this tile used.
 // Returns false (and records SCAFES_ERR_TIMEOUT) when a stage never
 // arrived; the caller must then stop.
-template <class P, bool HAS_F, int BORDER, int BY, int R>
+template <class P, int SRC, int BORDER, int BY, int R>
 __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, const Star7Coeffs& c,
                                            int x0, int y0, int z0, int z1,
                                            typename P::T* st, uint64_t* bar, uint32_t& base,
                                            int* status) {
     using T = typename P::T;
     using G = Tile<T, BY>;
+    constexpr bool HAS_F = SRC != SRC_NONE;
+    constexpr bool has_fb = SRC == SRC_AB;
     const Layout& L = J.L;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * BX + tx;
@@ -94,7 +102,6 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
 
     const bool xin = x < L.nx;
     const bool xb = (x == 0 || x == L.nx - 1);
-    const bool has_fb = (J.fb != nullptr);
     const bool has_gb = (J.gb != nullptr);
     // The whole 32 x BY tile holds inner columns: no per-node border tests.
     const bool tile_inner = x0 >= 1 && x0 + BX <= L.nx - 1 && y0 >= 1 && y0 + BY <= L.ny - 1;
@@ -127,20 +134,47 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
         const bool zb = (z == 0 || z == L.nz - 1);
         const T ym = pl[(rb - 1) * G::W];
         const T yp = pl[(rb + R) * G::W];
-        if (ok && tile_inner && !zb) {
-            // Inner plane of an inner tile: every node takes the star.
+        // A plane that is not a z-border plane.  Every node takes the star;
+        // on a tile that touches an x or y face the border nodes then take
+        // the border rule instead (a select, not a branch around the star:
+        // the y test is uniform per warp, the x test hits one or two lanes).
+        auto rows = [&](auto all_inner) {
+            constexpr bool INNER = decltype(all_inner)::value;
             const long long o0 = (long long)z * L.plane + (long long)yb * L.pitch + x;
 #pragma unroll
             for (int k = 0; k < R; ++k) {
                 const long long off = o0 + (long long)k * L.pitch;
+                const int y = yb + k;
+                const bool live = INNER || (xin && y < L.ny);
                 const T s = (k == 0) ? ym : cur[k - 1];
                 const T n = (k == R - 1) ? yp : cur[k + 1];
                 const T w = pl[(rb + k) * G::W - 1];
                 const T e = pl[(rb + k) * G::W + 1];
                 T f = P::zero();
-                if (HAS_F) f = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
-                J.un[off] = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
+                if (HAS_F && live) f = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
+                T v = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
+                if (!INNER && live && (xb || y == 0 || y == L.ny - 1)) {
+                    if (BORDER == SCAFES_BORDER_DIRICHLET) {
+                        v = J.ga ? J.ga[off] : J.gval;
+                        if (has_gb) v = P::src(v, J.gb[off], J.time_new, true);
+                    } else {
+                        // Mirror rule of an x or y face (see the z-border
+                        // path below for the face order).
+                        T opp;
+                        bool minus;
+                        if (y == L.ny - 1)      { opp = s; minus = true; }
+                        else if (y == 0)        { opp = n; minus = false; }
+                        else if (x == L.nx - 1) { opp = w; minus = true; }
+                        else                    { opp = e; minus = false; }
+                        v = P::mirror(cur[k], opp, minus ? negated(J.corr) : J.corr);
+                    }
+                }
+                if (live) J.un[off] = v;
             }
+        };
+        if (ok && !zb) {
+            if (tile_inner) rows(std::true_type{});
+            else rows(std::false_type{});
         } else if (ok && xin) {
             const long long zoff = (long long)z * L.plane + x;
 #pragma unroll

@@ -11,7 +11,7 @@
 
 namespace scafes {
 
-template <class P, bool HAS_F, int BORDER, int BY, int R>
+template <class P, int SRC, int BORDER, int BY, int R>
 __global__ void __launch_bounds__(BX * (BY / R))
 star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un,
           const typename P::T* __restrict__ fa, const typename P::T* __restrict__ fb,
@@ -29,7 +29,7 @@ star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
     const int z0 = blockIdx.z * zchunk;
     const int z1 = min(z0 + zchunk, L.nz);
     uint32_t base = 0;
-    star7_tile<P, HAS_F, BORDER, BY, R>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
+    star7_tile<P, SRC, BORDER, BY, R>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
 }
 
 // ---- host side ---------------------------------------------------------------
@@ -94,12 +94,12 @@ static inline void to_elem(double d, float2& out) {
     out = make_float2(p.hi, p.lo);
 }
 
-template <class P, bool HAS_F, int BORDER, int BY, int R>
+template <class P, int SRC, int BORDER, int BY, int R>
 static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
     using T = typename P::T;
     using G = Tile<T, BY>;
     const Layout& L = a.L;
-    auto kern = star7_tma<P, HAS_F, BORDER, BY, R>;
+    auto kern = star7_tma<P, SRC, BORDER, BY, R>;
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
@@ -121,26 +121,28 @@ static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
-template <class P, bool HAS_F, int BORDER>
+template <class P, int SRC, int BORDER>
 static cudaError_t launch_tile(const Star7Launch& a, cudaStream_t stream) {
     switch (a.tile) {
-        case 0: return launch_typed<P, HAS_F, BORDER, kTiles[0].by, kTiles[0].r>(a, stream);
-        case 1: return launch_typed<P, HAS_F, BORDER, kTiles[1].by, kTiles[1].r>(a, stream);
-        case 2: return launch_typed<P, HAS_F, BORDER, kTiles[2].by, kTiles[2].r>(a, stream);
-        case 3: return launch_typed<P, HAS_F, BORDER, kTiles[3].by, kTiles[3].r>(a, stream);
+        case 0: return launch_typed<P, SRC, BORDER, kTiles[0].by, kTiles[0].r>(a, stream);
+        case 1: return launch_typed<P, SRC, BORDER, kTiles[1].by, kTiles[1].r>(a, stream);
+        case 2: return launch_typed<P, SRC, BORDER, kTiles[2].by, kTiles[2].r>(a, stream);
+        case 3: return launch_typed<P, SRC, BORDER, kTiles[3].by, kTiles[3].r>(a, stream);
         default: return cudaErrorInvalidValue;
     }
 }
 
+template <class P, int BORDER>
+static cudaError_t launch_src(const Star7Launch& a, cudaStream_t stream) {
+    if (a.fa == nullptr || a.c.cf == 0.0) return launch_tile<P, SRC_NONE, BORDER>(a, stream);
+    if (a.fb == nullptr) return launch_tile<P, SRC_A, BORDER>(a, stream);
+    return launch_tile<P, SRC_AB, BORDER>(a, stream);
+}
+
 template <class P>
 static cudaError_t launch_prec(const Star7Launch& a, cudaStream_t stream) {
-    const bool has_f = (a.fa != nullptr) && (a.c.cf != 0.0);
-    if (a.border == SCAFES_BORDER_DIRICHLET) {
-        return has_f ? launch_tile<P, true, SCAFES_BORDER_DIRICHLET>(a, stream)
-                     : launch_tile<P, false, SCAFES_BORDER_DIRICHLET>(a, stream);
-    }
-    return has_f ? launch_tile<P, true, SCAFES_BORDER_MIRROR_POW2>(a, stream)
-                 : launch_tile<P, false, SCAFES_BORDER_MIRROR_POW2>(a, stream);
+    if (a.border == SCAFES_BORDER_DIRICHLET) return launch_src<P, SCAFES_BORDER_DIRICHLET>(a, stream);
+    return launch_src<P, SCAFES_BORDER_MIRROR_POW2>(a, stream);
 }
 
 cudaError_t launch_star7(const Star7Launch& a, cudaStream_t stream) {
