@@ -59,7 +59,7 @@ def parse_args():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--adj-n", type=int, default=256)
     ap.add_argument("--adj-time-steps", type=int, default=2000)
-    ap.add_argument("--adj-fd-directions", type=int, default=4)
+    ap.add_argument("--adj-fd-directions", type=int, default=16)
     return ap.parse_args()
 
 
@@ -280,11 +280,14 @@ def smooth_gauss(n, seed):
 
 def run_adjoint(M, args, dist: Dist):
     """Adjoint workload: flux-form heat with k = exp(0.3 g), g a seeded
-    (seed 5) smoothed Gaussian field, 256^3, FP64, 2000 steps, u0 = sine
-    mode, target = the forward solve with a second conductivity (seed 6).
-    Reports the forward and gradient times, their ratio for 45 snapshots and
-    (when it fits in device memory) for every state stored, and central
-    finite differences of J on seeded directions."""
+    (seed 5) smoothed Gaussian field, 256^3, 2000 steps, u0 = sine mode,
+    target = the forward solve with a second conductivity (seed 6).
+    FP64 sweeps: forward time, gradient time and their ratio for 45
+    snapshots and (when it fits in device memory) for every state stored.
+    Compensated FP32-pair sweeps: the same for 45 snapshots, the gradient's
+    distance to the FP64 gradient, and its ratio to the FP64 forward solve.
+    Both gradients are checked against central differences of J (FP64
+    forward solves) on seeded directions."""
     import torch
     from masterthesis_gb300 import workloads as W
     n = (args.adj_n,) * 3
@@ -293,35 +296,55 @@ def run_adjoint(M, args, dist: Dist):
     k2 = np.exp(0.3 * smooth_gauss(n, 6))
     tau = 0.9 / (2.0 * max(k.max(), k2.max()) * sum((m - 1) ** 2 for m in n))
     u0 = W.heat_sine_noise(n, amp=0.0)
-    out = {"workload": f"adjoint heat, k=exp(0.3 g) (seed 5), {n[0]}^3 FP64, {T} steps, "
+    out = {"workload": f"adjoint heat, k=exp(0.3 g) (seed 5), {n[0]}^3, {T} steps, "
                        f"J=0.5||u_T-u_target||^2, u_target from k seed 6"}
     free, _ = torch.cuda.mem_get_info()
     field = int(np.prod(n)) * 8
-    runs = [("snapshots_45", 45)]
-    if (T + 1) * field + 40 * field < free:
-        runs.append(("store_all", T + 1))
+    lups = float(np.prod(n)) * T
+
+    def forward_ms(prec):
+        with M.Adjoint(n, tau, 2, precision=prec) as a:
+            a.set_conductivity(k)
+            a.forward(u0, 2)  # warm-up
+            a.forward(u0, T)
+            return a.stats()["forward_ms"]
+
+    def gradient(prec, snaps):
+        with M.Adjoint(n, tau, snaps, precision=prec) as a:
+            a.set_conductivity(k)
+            J, gk, gu = a.gradient(u0, target, T)
+            return J, gk, gu, a.stats()
+
     with M.Adjoint(n, tau, 2) as a:
         a.set_conductivity(k2)
         target = a.forward(u0, T)
-        a.set_conductivity(k)
-        a.forward(u0, 2)  # warm-up
-        a.forward(u0, T)
-        fwd_ms = a.stats()["forward_ms"]
-    out["forward_ms"] = fwd_ms
-    out["forward_glups"] = float(np.prod(n)) * T / (fwd_ms * 1e-3) / 1e9
-    grads = None
+    f64_ms = forward_ms("f64")
+    out["f64"] = {"forward_ms": f64_ms, "forward_glups": lups / (f64_ms * 1e-3) / 1e9}
+    runs = [("snapshots_45", 45)]
+    if (T + 1) * field + 40 * field < free:
+        runs.append(("store_all", T + 1))
+    grads = {}
     for name, s in runs:
-        with M.Adjoint(n, tau, s) as a:
-            a.set_conductivity(k)
-            J, gk, gu = a.gradient(u0, target, T)
-            st = a.stats()
-        out[name] = {"gradient_ms": st["gradient_ms"], "cost_ratio": st["gradient_ms"] / fwd_ms,
-                     "forward_steps": st["forward_steps"], "adjoint_steps": st["adjoint_steps"],
-                     "snapshot_bytes": s * field, "J": J}
-        grads = (J, gk, gu)
-    # Central differences of J on seeded directions (k relative, u0 absolute).
-    J, gk, gu = grads
-    errs = []
+        J, gk, gu, st = gradient("f64", s)
+        out["f64"][name] = {"gradient_ms": st["gradient_ms"], "cost_ratio": st["gradient_ms"] / f64_ms,
+                            "forward_steps": st["forward_steps"], "adjoint_steps": st["adjoint_steps"],
+                            "snapshot_bytes": s * field, "J": J}
+        grads["f64"] = (J, gk, gu)
+    x2_ms = forward_ms("f32x2")
+    J, gk, gu, st = gradient("f32x2", 45)
+    grads["f32x2"] = (J, gk, gu)
+    J64, gk64, gu64 = grads["f64"]
+    out["f32x2"] = {"forward_ms": x2_ms, "forward_glups": lups / (x2_ms * 1e-3) / 1e9,
+                    "snapshots_45": {"gradient_ms": st["gradient_ms"],
+                                     "cost_ratio_vs_f64_forward": st["gradient_ms"] / f64_ms,
+                                     "cost_ratio_vs_f32x2_forward": st["gradient_ms"] / x2_ms,
+                                     "forward_steps": st["forward_steps"], "adjoint_steps": st["adjoint_steps"],
+                                     "snapshot_bytes": 45 * field, "J": J},
+                    "rel_diff_vs_f64": {"J": abs(J - J64) / abs(J64),
+                                        "grad_k": float(np.abs(gk - gk64).max() / np.abs(gk64).max()),
+                                        "grad_u0": float(np.abs(gu - gu64).max() / np.abs(gu64).max())}}
+    # Central differences of J on seeded directions (k relative), FP64.
+    errs = {p: [] for p in grads}
     with M.Adjoint(n, tau, 2) as a:
         def J_of(kk, uu):
             a.set_conductivity(kk)
@@ -332,9 +355,11 @@ def run_adjoint(M, args, dist: Dist):
             dk = rng.standard_normal(k.shape) * k
             eps = 1e-6
             fd = (J_of(k + eps * dk, u0) - J_of(k - eps * dk, u0)) / (2 * eps)
-            errs.append(abs(fd - float(np.sum(gk * dk))) / abs(fd))
-    out["fd_directions"] = len(errs)
-    out["fd_max_rel_err"] = max(errs) if errs else None
+            for p, (_, g, _) in grads.items():
+                errs[p].append(abs(fd - float(np.sum(g * dk))) / abs(fd))
+    out["fd_directions"] = args.adj_fd_directions
+    for p, e in errs.items():
+        out[p]["fd_max_rel_err"] = max(e) if e else None
     return out
 
 

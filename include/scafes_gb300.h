@@ -303,6 +303,13 @@ typedef struct scafes_adj scafes_adj;
 int scafes_adj_create(const int n_nodes[3], const double coord_first[3],
                       const double coord_last[3], double tau, int n_snapshots,
                       void* stream, scafes_adj** out);
+/* Arithmetic of the forward and reverse sweeps: SCAFES_PREC_F64 (default;
+ * the flux form above in FP64) or SCAFES_PREC_F32X2 (the same update in
+ * its equivalent diagonal form  u'_i = d_i u_i + sum_f K_f u_nb,
+ * d_i = 1 - sum_f K_f, on compensated FP32 pairs; states, snapshots and
+ * gradient accumulators are pairs, host arrays stay FP64).  Clears the
+ * conductivity: call before scafes_adj_set_conductivity. */
+int scafes_adj_set_precision(scafes_adj* a, int precision);
 /* Conductivity k at the nodes (dense host array, x fastest). */
 int scafes_adj_set_conductivity(scafes_adj* a, const double* k, size_t n);
 /* Plain forward solve u0 -> u_T (n_steps steps); times itself. */

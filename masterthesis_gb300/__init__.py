@@ -300,12 +300,14 @@ class Adjoint:
     """Gradient of J = 1/2 ||u_T - target||^2 for the flux-form
     variable-conductivity heat update (owns a scafes_adj)."""
 
-    def __init__(self, n, tau, n_snapshots, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), stream=None):
+    def __init__(self, n, tau, n_snapshots, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), stream=None,
+                 precision="f64"):
         L = lib()
         if not getattr(L, "_adj_set", False):
             vp, dp = C.c_void_p, C.POINTER(C.c_double)
             i3, d3 = C.c_int * 3, C.c_double * 3
             L.scafes_adj_create.argtypes = [i3, d3, d3, C.c_double, C.c_int, vp, C.POINTER(vp)]
+            L.scafes_adj_set_precision.argtypes = [vp, C.c_int]
             L.scafes_adj_set_conductivity.argtypes = [vp, dp, C.c_size_t]
             L.scafes_adj_forward.argtypes = [vp, dp, C.c_int, dp, C.c_size_t]
             L.scafes_adj_gradient.argtypes = [vp, dp, dp, C.c_int, dp, dp, dp, C.c_size_t]
@@ -326,6 +328,9 @@ class Adjoint:
         if rc != 0:
             raise ScafesError(rc, (L.scafes_last_error() or b"").decode())
         self.h = h
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        if prec != PREC_F64:
+            self._chk(L.scafes_adj_set_precision(self.h, prec))
 
     def _chk(self, rc):
         if rc != 0:

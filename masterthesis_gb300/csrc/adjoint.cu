@@ -176,6 +176,219 @@ __global__ void k_finalize(const double* __restrict__ gx, const double* __restri
     }
 }
 
+// ---- compensated FP32-pair (f32x2) sweeps ----------------------------------
+//
+// The same update in its diagonal form u'_i = d_i u_i + sum_f K_f u_nb with
+// d_i = 1 - sum_f K_f (K and d prepared in FP64, then split into pairs).
+// Products are exact in their hi parts (FMA TwoProd) with the cross terms
+// in FP32; sums are TwoSum-exact in the hi parts; every pair is
+// renormalised once per node (FastTwoSum).  No FP64 instruction is issued
+// in the per-step kernels.
+
+// p = a * b as an unnormalised pair.
+__device__ __forceinline__ f2 pmul(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    return {p, e};
+}
+
+// acc += p (unnormalised).
+__device__ __forceinline__ void pacc(f2& acc, f2 p) {
+    const f2 s = two_sum(acc.hi, p.hi);
+    acc.hi = s.hi;
+    acc.lo += s.lo + p.lo;
+}
+
+// a - b as an unnormalised pair.
+__device__ __forceinline__ f2 psub(float2 a, float2 b) {
+    const f2 s = two_sum(a.x, -b.x);
+    return {s.hi, s.lo + (a.y - b.y)};
+}
+
+__device__ __forceinline__ float2 pnorm(f2 a) {
+    const f2 r = fast_two_sum(a.hi, a.lo);
+    return make_float2(r.hi, r.lo);
+}
+
+__device__ __forceinline__ float2 psplit(double d) {
+    const f2 p = split_double(d);
+    return make_float2(p.hi, p.lo);
+}
+
+__device__ __forceinline__ double pjoin(float2 a) { return (double)a.x + (double)a.y; }
+
+// In-place conversions of a padded field between FP64 and pairs (each
+// element keeps its 8 bytes).
+__global__ void k_to_pair(void* buf, Layout L) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    for (int z = 0; z < L.nz; ++z) {
+        const long long o = L.idx(x, y, z);
+        const double d = reinterpret_cast<const double*>(buf)[o];
+        reinterpret_cast<float2*>(buf)[o] = psplit(d);
+    }
+}
+
+__global__ void k_from_pair(void* buf, Layout L) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    for (int z = 0; z < L.nz; ++z) {
+        const long long o = L.idx(x, y, z);
+        const float2 p = reinterpret_cast<const float2*>(buf)[o];
+        reinterpret_cast<double*>(buf)[o] = pjoin(p);
+    }
+}
+
+// Face conductivities and the diagonal from k (FP64), stored as pairs.
+__global__ void k_prep_x2(const double* __restrict__ k, float2* __restrict__ kx, float2* __restrict__ ky,
+                          float2* __restrict__ kz, float2* __restrict__ dg, Layout L, double wx, double wy,
+                          double wz) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    for (int z = 0; z < L.nz; ++z) {
+        const long long o = L.idx(x, y, z);
+        const double kc = k[o];
+        const double fxp = x + 1 < L.nx ? wx * 0.5 * (kc + k[o + 1]) : 0.0;
+        const double fyp = y + 1 < L.ny ? wy * 0.5 * (kc + k[o + L.pitch]) : 0.0;
+        const double fzp = z + 1 < L.nz ? wz * 0.5 * (kc + k[o + L.plane]) : 0.0;
+        const double fxm = x > 0 ? wx * 0.5 * (k[o - 1] + kc) : 0.0;
+        const double fym = y > 0 ? wy * 0.5 * (k[o - L.pitch] + kc) : 0.0;
+        const double fzm = z > 0 ? wz * 0.5 * (k[o - L.plane] + kc) : 0.0;
+        kx[o] = psplit(fxp);
+        ky[o] = psplit(fyp);
+        kz[o] = psplit(fzp);
+        dg[o] = psplit(1.0 - (((fxp + fxm) + (fyp + fym)) + (fzp + fzm)));
+    }
+}
+
+__global__ void __launch_bounds__(AX * AY)
+k_forward_x2(const float2* __restrict__ u, float2* __restrict__ un, const float2* __restrict__ kx,
+             const float2* __restrict__ ky, const float2* __restrict__ kz, const float2* __restrict__ dg, Layout L) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+    const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
+    for (int z = zb; z < ze; ++z) {
+        const long long o = L.idx(x, y, z);
+        const float2 uc = u[o];
+        if (colb || z == 0 || z == L.nz - 1) {
+            un[o] = uc;
+            continue;
+        }
+        f2 acc = pmul(dg[o], uc);
+        pacc(acc, pmul(kx[o], u[o + 1]));
+        pacc(acc, pmul(kx[o - 1], u[o - 1]));
+        pacc(acc, pmul(ky[o], u[o + L.pitch]));
+        pacc(acc, pmul(ky[o - L.pitch], u[o - L.pitch]));
+        pacc(acc, pmul(kz[o], u[o + L.plane]));
+        pacc(acc, pmul(kz[o - L.plane], u[o - L.plane]));
+        un[o] = pnorm(acc);
+    }
+}
+
+// G += (u_nb - u_c) (l_c - l_nb), renormalised.
+__device__ __forceinline__ float2 gacc(float2 G, float2 unb, float2 uc, float2 lc, float2 lnb) {
+    const f2 du = psub(unb, uc);
+    const f2 dl = psub(lc, lnb);
+    const float p = du.hi * dl.hi;
+    float e = fmaf(du.hi, dl.hi, -p);
+    e = fmaf(du.hi, dl.lo, e);
+    e = fmaf(du.lo, dl.hi, e);
+    f2 acc{G.x, G.y};
+    pacc(acc, {p, e});
+    return pnorm(acc);
+}
+
+__global__ void __launch_bounds__(AX * AY)
+k_adjoint_x2(const float2* __restrict__ lam, float2* __restrict__ lamn, const float2* __restrict__ u,
+             const float2* __restrict__ kx, const float2* __restrict__ ky, const float2* __restrict__ kz,
+             const float2* __restrict__ dg, float2* __restrict__ gx, float2* __restrict__ gy, float2* __restrict__ gz,
+             float2* __restrict__ bnd, Layout L) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+    const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
+    const float2 zero = make_float2(0.f, 0.f);
+    for (int z = zb; z < ze; ++z) {
+        const long long o = L.idx(x, y, z);
+        const bool border = colb || z == 0 || z == L.nz - 1;
+        const float2 lc = lam[o];  // zero on border nodes
+        const float2 uc = u[o];
+        const float2 lxp = x + 1 < L.nx ? lam[o + 1] : zero, lxm = x > 0 ? lam[o - 1] : zero;
+        const float2 lyp = y + 1 < L.ny ? lam[o + L.pitch] : zero, lym = y > 0 ? lam[o - L.pitch] : zero;
+        const float2 lzp = z + 1 < L.nz ? lam[o + L.plane] : zero, lzm = z > 0 ? lam[o - L.plane] : zero;
+        if (x + 1 < L.nx) gx[o] = gacc(gx[o], u[o + 1], uc, lc, lxp);
+        if (y + 1 < L.ny) gy[o] = gacc(gy[o], u[o + L.pitch], uc, lc, lyp);
+        if (z + 1 < L.nz) gz[o] = gacc(gz[o], u[o + L.plane], uc, lc, lzp);
+        const float2 kxp = kx[o], kyp = ky[o], kzp = kz[o];
+        const float2 kxm = x > 0 ? kx[o - 1] : zero, kym = y > 0 ? ky[o - L.pitch] : zero;
+        const float2 kzm = z > 0 ? kz[o - L.plane] : zero;
+        f2 acc = border ? f2{0.f, 0.f} : pmul(dg[o], lc);
+        pacc(acc, pmul(kxp, lxp));
+        pacc(acc, pmul(kxm, lxm));
+        pacc(acc, pmul(kyp, lyp));
+        pacc(acc, pmul(kym, lym));
+        pacc(acc, pmul(kzp, lzp));
+        pacc(acc, pmul(kzm, lzm));
+        if (border) {
+            // Border rows of the update are the identity: lambda on the border
+            // only collects what the inner neighbours pass back.
+            const float2 b = bnd[o];
+            pacc(acc, {b.x, b.y});
+            bnd[o] = pnorm(acc);
+            lamn[o] = zero;
+        } else {
+            lamn[o] = pnorm(acc);
+        }
+    }
+}
+
+// lambda_T = u_T - target (u_T pairs, target FP64): inner part into lam,
+// border part into bnd, per-CTA partial sums of J into part.
+__global__ void k_terminal_x2(const float2* __restrict__ uT, const double* __restrict__ target,
+                              float2* __restrict__ lam, float2* __restrict__ bnd, double* __restrict__ part, Layout L) {
+    __shared__ double sh[AX * AY];
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    double acc = 0.0;
+    if (x < L.nx && y < L.ny) {
+        const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+        for (int z = 0; z < L.nz; ++z) {
+            const long long o = L.idx(x, y, z);
+            const double d = pjoin(uT[o]) - target[o];
+            acc += 0.5 * d * d;
+            const bool border = colb || z == 0 || z == L.nz - 1;
+            lam[o] = border ? make_float2(0.f, 0.f) : psplit(d);
+            bnd[o] = border ? psplit(d) : make_float2(0.f, 0.f);
+        }
+    }
+    const int t = threadIdx.y * AX + threadIdx.x;
+    sh[t] = acc;
+    __syncthreads();
+    for (int s = AX * AY / 2; s > 0; s >>= 1) {
+        if (t < s) sh[t] += sh[t + s];
+        __syncthreads();
+    }
+    if (t == 0) part[blockIdx.y * gridDim.x + blockIdx.x] = sh[0];
+}
+
+__global__ void k_finalize_x2(const float2* __restrict__ gx, const float2* __restrict__ gy,
+                              const float2* __restrict__ gz, const float2* __restrict__ lam,
+                              const float2* __restrict__ bnd, double* __restrict__ dk, double* __restrict__ du0,
+                              Layout L, double wx, double wy, double wz) {
+    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    for (int z = 0; z < L.nz; ++z) {
+        const long long o = L.idx(x, y, z);
+        double g = 0.5 * wx * (pjoin(gx[o]) + (x > 0 ? pjoin(gx[o - 1]) : 0.0));
+        g += 0.5 * wy * (pjoin(gy[o]) + (y > 0 ? pjoin(gy[o - L.pitch]) : 0.0));
+        g += 0.5 * wz * (pjoin(gz[o]) + (z > 0 ? pjoin(gz[o - L.plane]) : 0.0));
+        dk[o] = g;
+        du0[o] = pjoin(lam[o]) + pjoin(bnd[o]);
+    }
+}
+
 }  // namespace
 
 struct scafes_adj {
@@ -184,7 +397,11 @@ struct scafes_adj {
     int n_snap = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    int precision = SCAFES_PREC_F64;
+    // Every field holds 8 bytes per node: FP64 values, or FP32 pairs when
+    // precision is SCAFES_PREC_F32X2.
     double *kx = nullptr, *ky = nullptr, *kz = nullptr;
+    double *dg = nullptr;      // diagonal of the pair form (allocated on demand)
     double *u[2] = {nullptr, nullptr}, *lam[2] = {nullptr, nullptr};
     double *gx = nullptr, *gy = nullptr, *gz = nullptr, *bnd = nullptr;
     double *snaps = nullptr;   // n_snap fields
@@ -228,10 +445,43 @@ dim3 grid3(const Layout& L) { return dim3((L.nx + AX - 1) / AX, (L.ny + AY - 1) 
 size_t field_bytes(const scafes_adj* a) { return (size_t)a->L.size() * sizeof(double); }
 double* snap(scafes_adj* a, int s) { return a->snaps + (size_t)s * a->L.size(); }
 
+bool pairs(const scafes_adj* a) { return a->precision == SCAFES_PREC_F32X2; }
+const float2* P2(const double* p) { return reinterpret_cast<const float2*>(p); }
+float2* P2(double* p) { return reinterpret_cast<float2*>(p); }
+
 int fwd(scafes_adj* a, const double* src, double* dst) {
-    k_forward<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(src, dst, a->kx, a->ky, a->kz, a->L);
+    if (pairs(a))
+        k_forward_x2<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(P2(src), P2(dst), P2(a->kx), P2(a->ky), P2(a->kz),
+                                                                  P2(a->dg), a->L);
+    else
+        k_forward<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(src, dst, a->kx, a->ky, a->kz, a->L);
     ATRY(a, cudaGetLastError());
     ++a->fwd_steps;
+    return SCAFES_OK;
+}
+
+// lambda_T, the border part of dJ/du0 and the partial sums of J from u_T.
+int terminal(scafes_adj* a, const double* uT, const double* target, double* lam, double* Jpart) {
+    if (pairs(a))
+        k_terminal_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(uT), target, P2(lam), P2(a->bnd), Jpart, a->L);
+    else
+        k_terminal<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(uT, target, lam, a->bnd, Jpart, a->L);
+    ATRY(a, cudaGetLastError());
+    return SCAFES_OK;
+}
+
+// Converts a field in place between host-facing FP64 and the sweep's type.
+int to_sweep_type(scafes_adj* a, double* buf) {
+    if (!pairs(a)) return SCAFES_OK;
+    k_to_pair<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(buf, a->L);
+    ATRY(a, cudaGetLastError());
+    return SCAFES_OK;
+}
+
+int from_sweep_type(scafes_adj* a, double* buf) {
+    if (!pairs(a)) return SCAFES_OK;
+    k_from_pair<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(buf, a->L);
+    ATRY(a, cudaGetLastError());
     return SCAFES_OK;
 }
 
@@ -296,8 +546,13 @@ struct Rev {
 
 int adj_step(Rev& R, const double* u_t) {
     scafes_adj* a = R.a;
-    k_adjoint<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(a->lam[R.cur], a->lam[R.cur ^ 1], u_t, a->kx, a->ky,
-                                                           a->kz, a->gx, a->gy, a->gz, a->bnd, a->L);
+    if (pairs(a))
+        k_adjoint_x2<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(
+            P2(a->lam[R.cur]), P2(a->lam[R.cur ^ 1]), P2(u_t), P2(a->kx), P2(a->ky), P2(a->kz), P2(a->dg), P2(a->gx),
+            P2(a->gy), P2(a->gz), P2(a->bnd), a->L);
+    else
+        k_adjoint<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(a->lam[R.cur], a->lam[R.cur ^ 1], u_t, a->kx, a->ky,
+                                                               a->kz, a->gx, a->gy, a->gz, a->bnd, a->L);
     ATRY(a, cudaGetLastError());
     R.cur ^= 1;
     ++a->adj_steps;
@@ -313,9 +568,7 @@ int reverse(Rev& R, int lo, int hi, int slot, int free) {
         if (!R.started) {
             // Bottom of the first descent: u_T from u_{T-1} gives J and lambda_T.
             if ((rc = fwd(a, snap(a, slot), a->u[0]))) return rc;
-            k_terminal<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->u[0], R.target, a->lam[R.cur], a->bnd,
-                                                                    R.Jpart, a->L);
-            ATRY(a, cudaGetLastError());
+            if ((rc = terminal(a, a->u[0], R.target, a->lam[R.cur], R.Jpart))) return rc;
             R.started = true;
         }
         return adj_step(R, snap(a, slot));
@@ -332,9 +585,7 @@ int reverse(Rev& R, int lo, int hi, int slot, int free) {
             }
             if (t == hi - 1 && !R.started) {
                 if ((rc = fwd(a, src, a->u[buf]))) return rc;
-                k_terminal<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->u[buf], R.target, a->lam[R.cur], a->bnd,
-                                                                        R.Jpart, a->L);
-                ATRY(a, cudaGetLastError());
+                if ((rc = terminal(a, a->u[buf], R.target, a->lam[R.cur], R.Jpart))) return rc;
                 R.started = true;
             }
             if ((rc = adj_step(R, src))) return rc;
@@ -376,7 +627,7 @@ extern "C" const char* scafes_adj_last_error(const scafes_adj* a) { return a ? a
 extern "C" void scafes_adj_destroy(scafes_adj* a) {
     if (!a) return;
     if (a->stream) cudaStreamSynchronize(a->stream);
-    double* bufs[] = {a->kx, a->ky, a->kz, a->u[0], a->u[1], a->lam[0], a->lam[1], a->gx, a->gy, a->gz,
+    double* bufs[] = {a->kx, a->ky, a->kz, a->dg, a->u[0], a->u[1], a->lam[0], a->lam[1], a->gx, a->gy, a->gz,
                       a->bnd, a->snaps, a->work, a->part};
     for (double* b : bufs) cudaFree(b);
     if (a->e0) cudaEventDestroy(a->e0);
@@ -431,6 +682,25 @@ extern "C" int scafes_adj_create(const int n_nodes[3], const double coord_first[
     return SCAFES_OK;
 }
 
+extern "C" int scafes_adj_set_precision(scafes_adj* a, int precision) {
+    if (!a) return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_set_precision: NULL handle");
+    if (precision != SCAFES_PREC_F64 && precision != SCAFES_PREC_F32X2)
+        return afail(a, SCAFES_ERR_UNSUPPORTED, "scafes_adj_set_precision: precision %d (F64 or F32X2 only)", precision);
+    if (precision == SCAFES_PREC_F32X2 && !a->dg) {
+        cudaError_t e = cudaMalloc(&a->dg, field_bytes(a));
+        if (e == cudaSuccess) e = cudaMemsetAsync(a->dg, 0, field_bytes(a), a->stream);
+        if (e != cudaSuccess) {
+            cudaFree(a->dg);
+            a->dg = nullptr;
+            return afail(a, e == cudaErrorMemoryAllocation ? SCAFES_ERR_NOMEM : SCAFES_ERR_CUDA,
+                         "scafes_adj_set_precision: %s", cudaGetErrorString(e));
+        }
+    }
+    a->precision = precision;
+    a->have_k = false;
+    return SCAFES_OK;
+}
+
 extern "C" int scafes_adj_set_conductivity(scafes_adj* a, const double* k, size_t n) {
     if (!a || !k) return afail(a, SCAFES_ERR_ARG, "scafes_adj_set_conductivity: NULL argument");
     if (n != (size_t)a->L.nx * a->L.ny * a->L.nz)
@@ -438,7 +708,12 @@ extern "C" int scafes_adj_set_conductivity(scafes_adj* a, const double* k, size_
                      (size_t)a->L.nx * a->L.ny * a->L.nz);
     int rc = upload_dense(a, k, a->work);
     if (rc) return rc;
-    k_faces<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->work, a->kx, a->ky, a->kz, a->L, a->w[0], a->w[1], a->w[2]);
+    if (pairs(a))
+        k_prep_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->work, P2(a->kx), P2(a->ky), P2(a->kz), P2(a->dg),
+                                                               a->L, a->w[0], a->w[1], a->w[2]);
+    else
+        k_faces<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->work, a->kx, a->ky, a->kz, a->L, a->w[0], a->w[1],
+                                                             a->w[2]);
     ATRY(a, cudaGetLastError());
     ATRY(a, cudaStreamSynchronize(a->stream));
     a->have_k = true;
@@ -451,6 +726,7 @@ extern "C" int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps, 
     if (!a->have_k) return afail(a, SCAFES_ERR_STATE, "scafes_adj_forward: set the conductivity first");
     int rc = upload_dense(a, u0, a->u[0]);
     if (rc) return rc;
+    if ((rc = to_sweep_type(a, a->u[0]))) return rc;
     a->fwd_steps = 0;
     ATRY(a, cudaEventRecord(a->e0, a->stream));
     int cur = 0;
@@ -459,6 +735,7 @@ extern "C" int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps, 
         cur ^= 1;
     }
     ATRY(a, cudaEventRecord(a->e1, a->stream));
+    if ((rc = from_sweep_type(a, a->u[cur]))) return rc;
     if ((rc = download_dense(a, a->u[cur], uT))) return rc;
     ATRY(a, cudaStreamSynchronize(a->stream));
     ATRY(a, cudaEventElapsedTime(&a->fwd_ms, a->e0, a->e1));
@@ -476,6 +753,7 @@ extern "C" int scafes_adj_gradient(scafes_adj* a, const double* u0, const double
     const size_t fb = field_bytes(a);
     int rc = upload_dense(a, u0, snap(a, 0));
     if (rc) return rc;
+    if ((rc = to_sweep_type(a, snap(a, 0)))) return rc;
     // The target goes to u[1]'s slot only transiently: keep it in `work`.
     if ((rc = upload_dense(a, target, a->work))) return rc;
     ATRY(a, cudaMemsetAsync(a->gx, 0, fb, a->stream));
@@ -486,8 +764,13 @@ extern "C" int scafes_adj_gradient(scafes_adj* a, const double* u0, const double
     ATRY(a, cudaEventRecord(a->e0, a->stream));
     Rev R{a, a->work, n_steps, 0, false, a->part};
     if ((rc = reverse(R, 0, n_steps, 0, free))) return rc;
-    k_finalize<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->gx, a->gy, a->gz, a->lam[R.cur], a->bnd, a->u[0],
-                                                            a->u[1], a->L, a->w[0], a->w[1], a->w[2]);
+    if (pairs(a))
+        k_finalize_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(a->gx), P2(a->gy), P2(a->gz), P2(a->lam[R.cur]),
+                                                                   P2(a->bnd), a->u[0], a->u[1], a->L, a->w[0],
+                                                                   a->w[1], a->w[2]);
+    else
+        k_finalize<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->gx, a->gy, a->gz, a->lam[R.cur], a->bnd, a->u[0],
+                                                                a->u[1], a->L, a->w[0], a->w[1], a->w[2]);
     ATRY(a, cudaGetLastError());
     ATRY(a, cudaEventRecord(a->e1, a->stream));
     std::vector<double> part(a->part_n);

@@ -116,3 +116,63 @@ def test_adjoint_gradient_vs_central_differences(gpu):
             fd_u = (J_of(k, u0 + eps * du) - J_of(k, u0 - eps * du)) / (2 * eps)
             assert abs(fd_k - float(np.sum(gk * dk))) <= 1e-6 * abs(fd_k), seed
             assert abs(fd_u - float(np.sum(gu * du))) <= 1e-6 * abs(fd_u), seed
+
+
+@pytest.mark.gpu
+def test_adjoint_f32x2_matches_oracle_and_f64(gpu):
+    """The compensated FP32-pair sweeps (diagonal form of the same update)
+    against the FP64 oracle: forward state and gradients to 1e-10 relative
+    max-norm (pair arithmetic carries ~48 bits; the diagonal form rounds
+    differently from the flux form), J to 1e-11."""
+    M = gpu
+    n, T = (12, 10, 9), 30
+    k, tau, u0, target = kheat_problem(n, T, 7)
+    g = O.make_grid(n, tau=tau)
+    uT_ref, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
+    J_ref, gk_ref, gu_ref = O.kheat_adjoint(g, k, traj, target)
+    for snaps in (2, 5, 64):
+        with M.Adjoint(n, tau, snaps, precision="f32x2") as a:
+            a.set_conductivity(k)
+            uT = a.forward(u0, T)
+            J, gk, gu = a.gradient(u0, target, T)
+            st = a.stats()
+        assert cases.rel_err(uT, uT_ref) <= 1e-11, snaps
+        assert abs(J - J_ref) <= 1e-11 * abs(J_ref), snaps
+        assert cases.rel_err(gk, gk_ref) <= 1e-10, snaps
+        assert cases.rel_err(gu, gu_ref) <= 1e-10, snaps
+        assert st["forward_steps"] == M.Adjoint.schedule_cost(T, snaps)
+
+
+@pytest.mark.gpu
+def test_adjoint_f32x2_gradient_vs_central_differences(gpu):
+    M = gpu
+    n, T = (20, 18, 16), 40
+    k, tau, u0, target = kheat_problem(n, T, 11)
+    with M.Adjoint(n, tau, 6, precision="f32x2") as a:
+        a.set_conductivity(k)
+        J, gk, gu = a.gradient(u0, target, T)
+    # The differences use FP64 forward solves: J's rounding noise in pair
+    # arithmetic (~1e-13 relative) over 2 eps would swamp a 1e-6 check.
+    with M.Adjoint(n, tau, 2) as a:
+
+        def J_of(kk, uu):
+            a.set_conductivity(kk)
+            uT = a.forward(uu, T)
+            return 0.5 * float(np.sum((uT - target) ** 2))
+
+        for seed in range(4):
+            rng = np.random.default_rng(2000 + seed)
+            dk = rng.standard_normal(k.shape) * k
+            du = rng.standard_normal(k.shape)
+            eps = 1e-6
+            fd_k = (J_of(k + eps * dk, u0) - J_of(k - eps * dk, u0)) / (2 * eps)
+            fd_u = (J_of(k, u0 + eps * du) - J_of(k, u0 - eps * du)) / (2 * eps)
+            assert abs(fd_k - float(np.sum(gk * dk))) <= 1e-6 * abs(fd_k), seed
+            assert abs(fd_u - float(np.sum(gu * du))) <= 1e-6 * abs(fd_u), seed
+
+
+@pytest.mark.gpu
+def test_adjoint_rejects_unsupported_precision(gpu):
+    M = gpu
+    with pytest.raises(M.ScafesError):
+        M.Adjoint((8, 8, 8), 1e-3, 2, precision="f32")
