@@ -60,6 +60,10 @@ def parse_args():
     ap.add_argument("--adj-n", type=int, default=256)
     ap.add_argument("--adj-time-steps", type=int, default=2000)
     ap.add_argument("--adj-fd-directions", type=int, default=16)
+    ap.add_argument("--no-multifield", action="store_true")
+    ap.add_argument("--lame-n", type=int, default=384)
+    ap.add_argument("--yee-n", type=int, default=512)
+    ap.add_argument("--mf-time-steps", type=int, default=100)
     return ap.parse_args()
 
 
@@ -363,6 +367,48 @@ def run_adjoint(M, args, dist: Dist):
     return out
 
 
+# ---- multi-field leapfrog workloads ------------------------------------------
+
+def run_multifield(M, args, dist: Dist, hbm_peak: float):
+    """Lame-Navier 384^3 FP64 (lambda=1, mu=0.5, rho=1, seeded Gaussian bump,
+    seed 3) and Yee 512^3 FP32 and FP64 (eps=mu=1, Courant 0.5, seeded point
+    dipole, seed 4): GLUP/s over a timed run of leapfrog steps.  Algorithmic
+    bytes per node update: Lame 72 (u^n and u^{n-1} read, u^{n+1} written,
+    3 components), Yee 6 fields read + written (96 B FP64, 48 B FP32)."""
+    from masterthesis_gb300 import workloads as W
+    T = args.mf_time_steps
+    out = {}
+    n = (args.lame_n,) * 3
+    u0 = W.gaussian_bump_displacement(n, seed=3)
+    with M.MultiField(M.MF_LAME, n, W.lame_tau(n), (1.0, 0.5, 1.0)) as mf:
+        for c in range(3):
+            mf.upload(c, u0[c])
+            mf.upload(3 + c, u0[c])
+        del u0
+        mf.step(5)
+        dist.barrier()
+        mf.step(T)
+        ms = dist.max(mf.last_ms())
+    lup = float(np.prod(n)) * T
+    g = dist.world * lup / (ms * 1e-3) / 1e9
+    out["lame_f64"] = {"workload": f"Lame-Navier {n[0]}^3 FP64, leapfrog, {T} steps", "value": g, "unit": UNIT,
+                       "hbm_frac": 72 * g / hbm_peak, "bytes_per_lup": 72, "ms": ms}
+    n = (args.yee_n,) * 3
+    tau, src, par = W.yee_setup(n)
+    for prec, bpl in (("f32", 48), ("f64", 96)):
+        with M.MultiField(M.MF_YEE, n, tau, par, precision=prec, src=src) as mf:
+            mf.step(5)
+            dist.barrier()
+            mf.step(T)
+            ms = dist.max(mf.last_ms())
+        lup = float(np.prod(n)) * T
+        g = dist.world * lup / (ms * 1e-3) / 1e9
+        out[f"yee_{prec}"] = {"workload": f"Yee FDTD {n[0]}^3 {prec.upper()}, PEC, point dipole, {T} steps",
+                              "value": g, "unit": UNIT, "hbm_frac": bpl * g / hbm_peak, "bytes_per_lup": bpl,
+                              "ms": ms}
+    return out
+
+
 # ---- GPU arm ----------------------------------------------------------------
 
 def run_ours(args, dist: Dist):
@@ -476,6 +522,7 @@ def run_ours(args, dist: Dist):
 
     batched = None if args.no_batched else run_batched(M, args, dist, hbm_peak)
     adjoint = None if args.no_adjoint else run_adjoint(M, args, dist)
+    multifield = None if args.no_multifield else run_multifield(M, args, dist, hbm_peak)
 
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
@@ -496,6 +543,8 @@ def run_ours(args, dist: Dist):
         res["batched"] = batched
     if adjoint:
         res["adjoint"] = adjoint
+    if multifield:
+        res["multifield"] = multifield
     if clk:
         res["clocks"] = clk
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
