@@ -463,7 +463,9 @@ def run_ours(args, dist: Dist):
     launch_s = dt / (args.steps * T)
     hbm_peak, peak_src = measured_peaks()
     achieved_gbs = B_PER_LUP["f64"] * nn / launch_s / 1e9
-    traffic = ncu_traffic("star7_tma<PolF64>")
+    # DRAM bytes per launch from the committed ncu summary of this kernel at
+    # this grid size (null when no capture of this size exists).
+    traffic = ncu_traffic(f"star7_tma<PolF64>@{args.n}")
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
