@@ -79,7 +79,39 @@ enum scafes_border {
      * the border update of tests/system/HeatEqnFdmStencilWidthOne/
      * HeatEqnFdmStencilWidthOne.hpp:136-163 (s = +1 at min faces, -1 at max
      * faces, last face in direction order wins). */
-    SCAFES_BORDER_MIRROR_POW2 = 1
+    SCAFES_BORDER_MIRROR_POW2 = 1,
+    /* A linear rule per border class (the set of faces a node lies on),
+     * from a table set with scafes_gpu_set_border_forms: the Neumann and
+     * Cauchy updateBorder of tests/system/HeatEqnFDM/{Neumann,Cauchy}/
+     * {Neumann,Cauchy}.hpp and tests/system/PennesBioheatEqnFDM/
+     * {Neumann,Cauchy}/{Neumann,Cauchy}.hpp (Dirichlet at the min faces, a
+     * flux condition with the mirrored neighbour at the max faces), or any
+     * other rule of the same shape. */
+    SCAFES_BORDER_TABLE = 2
+};
+
+/* One border class's rule, evaluated in FP64 on border nodes:
+ *   u_new = cu*u + sum_d cn[d]*u_d + cf*F(time(t-1))
+ *           + cg_old*G(time(t-1)) + cg_new*G(time(t))
+ * with neighbours d = x-, x+, y-, y+, z-, z+ (a neighbour outside the grid
+ * must have weight 0).  A class is a 6-bit mask of the faces a node lies on:
+ * bit 0 x == 0, bit 1 x == nx-1, bit 2 y == 0, bit 3 y == ny-1, bit 4
+ * z == 0, bit 5 z == nz-1; entry 0 (inner nodes) is unused.  Dirichlet is
+ * cg_new = 1 with every other weight 0. */
+typedef struct scafes_border_form {
+    double cu;
+    double cn[6];
+    double cf;
+    double cg_old;
+    double cg_new;
+} scafes_border_form;
+
+#define SCAFES_BORDER_CLASSES 64
+
+/* Flux-condition kinds of scafes_border_forms_flux. */
+enum scafes_flux_kind {
+    SCAFES_FLUX_NEUMANN = 0, /* -lambda du/dn = G              (Neumann.hpp) */
+    SCAFES_FLUX_CAUCHY = 1   /* -lambda du/dn = alpha u - G    (Cauchy.hpp)  */
 };
 
 /* Configuration of one plain (single-instance) problem.
@@ -119,6 +151,19 @@ typedef struct scafes_handle scafes_handle;
 int scafes_star7_heat_coeffs(scafes_cfg* cfg, double coeff_a, double rho_c,
                              double perf);
 
+/* Fills the 64 border rules of the reference's flux-border system tests
+ * for the grid, tau and inner coefficients of *cfg (call
+ * scafes_star7_heat_coeffs first): nodes on a min face (an index 0) take
+ * Dirichlet u_new = G(time(t)); the others take the inner update with, in
+ * each direction p where the node is on the max face, the missing
+ * neighbour replaced by the inner one and the flux term
+ *   - cp[p]*(2 h_p/lambda) * G(time(t-1))          (Neumann)
+ *   - cp[p]*(2 h_p/lambda) * (alpha*u - G(time(t-1)))   (Cauchy)
+ * (tests/system/HeatEqnFDM/Neumann/Neumann.hpp and Cauchy/Cauchy.hpp, the
+ * Pennes variants add the perfusion already contained in c0). */
+int scafes_border_forms_flux(const scafes_cfg* cfg, int kind, double lambda,
+                             double alpha, scafes_border_form forms[64]);
+
 /* Allocates device memory for the problem of *cfg.  Replaces the field
  * allocation of the Problem constructor (src/ScaFES_Problem.hpp:1604-1674). */
 int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out);
@@ -129,6 +174,12 @@ int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out);
  * the host).  Known-field slots not uploaded read as 0. */
 int scafes_gpu_upload(scafes_handle* h, int field, const double* host,
                       size_t n);
+
+/* Sets the border rules of a SCAFES_BORDER_TABLE problem (64 entries,
+ * indexed by class mask).  A rule with cf != 0 needs a source field; one
+ * with cg_old or cg_new != 0 reads G = G_A + time*G_B. */
+int scafes_gpu_set_border_forms(scafes_handle* h,
+                                const scafes_border_form forms[64]);
 
 /* Advances the unknown field by n_steps time steps (one step = the update
  * phase of one iteration of iterateOverTime, src/ScaFES_Problem.hpp:

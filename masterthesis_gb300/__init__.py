@@ -24,7 +24,8 @@ PRECISIONS = {"f64": PREC_F64, "f32x2": PREC_F32X2, "f32": PREC_F32, "f64e": PRE
 # enum scafes_field
 FIELD_U, FIELD_F_A, FIELD_F_B, FIELD_G_A, FIELD_G_B, FIELD_E_A, FIELD_E_B = range(7)
 # enum scafes_border
-BORDER_DIRICHLET, BORDER_MIRROR_POW2 = 0, 1
+BORDER_DIRICHLET, BORDER_MIRROR_POW2, BORDER_TABLE = 0, 1, 2
+FLUX_NEUMANN, FLUX_CAUCHY = 0, 1
 
 STATUS = {0: "SCAFES_OK", -1: "SCAFES_ERR_ARG", -2: "SCAFES_ERR_CUDA", -3: "SCAFES_ERR_STATE",
           -4: "SCAFES_ERR_UNSUPPORTED", -5: "SCAFES_ERR_NOMEM", -6: "SCAFES_ERR_TIMEOUT"}
@@ -34,6 +35,15 @@ class ScafesError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"{STATUS.get(code, code)}: {msg}")
         self.code = code
+
+
+class BorderForm(C.Structure):
+    """Mirror of ``struct scafes_border_form`` (one border class's rule)."""
+    _fields_ = [("cu", C.c_double), ("cn", C.c_double * 6), ("cf", C.c_double), ("cg_old", C.c_double),
+                ("cg_new", C.c_double)]
+
+
+BorderForms = BorderForm * 64
 
 
 class Cfg(C.Structure):
@@ -67,6 +77,9 @@ def lib() -> C.CDLL:
         vp, dp = C.c_void_p, C.POINTER(C.c_double)
         L.scafes_star7_heat_coeffs.argtypes = [C.POINTER(Cfg), C.c_double, C.c_double, C.c_double]
         L.scafes_gpu_create.argtypes = [C.POINTER(Cfg), C.POINTER(vp)]
+        L.scafes_border_forms_flux.argtypes = [C.POINTER(Cfg), C.c_int, C.c_double, C.c_double,
+                                               C.POINTER(BorderForm)]
+        L.scafes_gpu_set_border_forms.argtypes = [vp, C.POINTER(BorderForm)]
         L.scafes_gpu_upload.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_step.argtypes = [vp, C.c_int]
@@ -136,6 +149,14 @@ def make_cfg(n, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), tau=0.0, t_start=0.
     return c
 
 
+def border_forms_flux(cfg: Cfg, kind: int, lam: float = 1.0, alpha: float = 1.0):
+    """The 64 border rules of the reference's Neumann / Cauchy system tests
+    for cfg (scafes_border_forms_flux)."""
+    forms = BorderForms()
+    _check(lib().scafes_border_forms_flux(C.byref(cfg), kind, lam, alpha, forms))
+    return forms
+
+
 class Plain:
     """One single-instance problem on the GPU (owns a scafes_handle)."""
 
@@ -149,6 +170,9 @@ class Plain:
     @property
     def shape(self):
         return (self.n[2], self.n[1], self.n[0])
+
+    def set_border_forms(self, forms):
+        _check(lib().scafes_gpu_set_border_forms(self.h, forms), self.h)
 
     def upload(self, field: int, arr: np.ndarray):
         a = np.ascontiguousarray(arr, dtype=np.float64)

@@ -82,6 +82,7 @@ batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ 
         J.gval = P::from_double(I.gconst);
         J.L = I.L;
         J.time_old = J.time_new = J.corr = Split{0.0, 0.f, 0.f};
+        J.table = nullptr;
         if (!star7_tile<P, SRC_A, SCAFES_BORDER_DIRICHLET, BY, R>(J, c, w.tx * BX, w.ty * BY, w.z0, w.z1, st, bar,
                                                                  base, status))
             break;

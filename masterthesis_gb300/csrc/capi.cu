@@ -60,6 +60,10 @@ struct scafes_handle {
     int launches = 0;
     int t = 0;
     bool uploaded = false;
+    // Border rules of a SCAFES_BORDER_TABLE problem (device copy) and whether
+    // any rule reads the source field.
+    scafes_border_form* table = nullptr;
+    bool table_needs_f = false;
     std::string err;
 };
 
@@ -114,7 +118,8 @@ static int validate(const scafes_cfg* c) {
     if (c->precision != SCAFES_PREC_F64 && c->precision != SCAFES_PREC_F32X2 &&
         c->precision != SCAFES_PREC_F32)
         return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: precision %d not supported", c->precision);
-    if (c->border != SCAFES_BORDER_DIRICHLET && c->border != SCAFES_BORDER_MIRROR_POW2)
+    if (c->border != SCAFES_BORDER_DIRICHLET && c->border != SCAFES_BORDER_MIRROR_POW2 &&
+        c->border != SCAFES_BORDER_TABLE)
         return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: border kind %d not supported", c->border);
     if (c->tile < 0 || c->tile > STAR7_NUM_TILES)
         return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_create: tile=%d out of range [0, %d]", c->tile,
@@ -129,6 +134,7 @@ extern "C" void scafes_gpu_destroy(scafes_handle* h) {
     cudaFree(h->status);
     for (int i = 0; i < SCAFES_FIELD_COUNT; ++i) cudaFree(h->fld[i]);
     cudaFree(h->stage);
+    cudaFree(h->table);
     cudaFree(h->red);
     if (h->red_host) cudaFreeHost(h->red_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -357,9 +363,18 @@ static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
     a.gb = h->has[SCAFES_FIELD_G_B] ? h->fld[SCAFES_FIELD_G_B] : nullptr;
     a.gconst = 0.0;
     a.c = make_star7_coeffs(h->cfg.c0, h->cfg.cp, h->cfg.cf);
+    a.table = h->table;
     if (!h->has[SCAFES_FIELD_F_A] && h->has[SCAFES_FIELD_F_B])
         return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
                     "scafes_gpu_step: upload F_A (possibly zeros) when F_B is used");
+    if (h->cfg.border == SCAFES_BORDER_TABLE) {
+        if (!h->table)
+            return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_step: set the border rules first "
+                                                   "(scafes_gpu_set_border_forms)");
+        if (h->table_needs_f && (a.fa == nullptr || h->cfg.cf == 0.0))
+            return fail(&h->err, SCAFES_ERR_STATE,
+                        "scafes_gpu_step: a border rule reads the source F, but no F_A is uploaded or cf == 0");
+    }
     if (timed) CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
     a.status = h->status;
     for (int s = 0; s < n_steps; ++s) {
@@ -379,6 +394,76 @@ static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
         CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
         h->timed = true;
         h->launches = n_steps;
+    }
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_set_border_forms(scafes_handle* h, const scafes_border_form forms[64]) {
+    if (!h || !forms) return fail(h ? &h->err : nullptr, SCAFES_ERR_ARG, "scafes_gpu_set_border_forms: NULL argument");
+    if (h->cfg.border != SCAFES_BORDER_TABLE)
+        return fail(&h->err, SCAFES_ERR_STATE,
+                    "scafes_gpu_set_border_forms: the problem was created with border kind %d, not "
+                    "SCAFES_BORDER_TABLE", h->cfg.border);
+    // A weight on a neighbour that a class's nodes do not have would read
+    // the zero halo silently: refuse it.
+    bool needs_f = false;
+    for (int m = 1; m < SCAFES_BORDER_CLASSES; ++m) {
+        for (int d = 0; d < 6; ++d)
+            if ((m >> d) & 1 && forms[m].cn[d] != 0.0)
+                return fail(&h->err, SCAFES_ERR_ARG,
+                            "scafes_gpu_set_border_forms: class %d weights neighbour %d, which lies outside the grid",
+                            m, d);
+        if ((m & 3) == 3 || (m & 12) == 12 || (m & 48) == 48)
+            continue;  // a node cannot be on both faces of an axis (n >= 3)
+        needs_f = needs_f || forms[m].cf != 0.0;
+    }
+    if (!h->table) CUDA_TRY(h, cudaMalloc(&h->table, sizeof(scafes_border_form) * SCAFES_BORDER_CLASSES));
+    CUDA_TRY(h, cudaMemcpyAsync(h->table, forms, sizeof(scafes_border_form) * SCAFES_BORDER_CLASSES,
+                                cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->table_needs_f = needs_f;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_border_forms_flux(const scafes_cfg* cfg, int kind, double lambda, double alpha,
+                                        scafes_border_form forms[64]) {
+    if (!cfg || !forms || cfg->dim != 3 || lambda == 0.0)
+        return fail(nullptr, SCAFES_ERR_ARG, "scafes_border_forms_flux: bad arguments");
+    if (kind != SCAFES_FLUX_NEUMANN && kind != SCAFES_FLUX_CAUCHY)
+        return fail(nullptr, SCAFES_ERR_ARG, "scafes_border_forms_flux: kind %d", kind);
+    double h[3];
+    for (int p = 0; p < 3; ++p) {
+        if (cfg->n_nodes[p] < 3) return fail(nullptr, SCAFES_ERR_ARG, "scafes_border_forms_flux: n_nodes[%d] < 3", p);
+        h[p] = (cfg->coord_last[p] - cfg->coord_first[p]) / (cfg->n_nodes[p] - 1);
+    }
+    for (int m = 0; m < SCAFES_BORDER_CLASSES; ++m) {
+        scafes_border_form& F = forms[m];
+        F = scafes_border_form{};
+        if (m == 0) continue;
+        if (m & (1 | 4 | 16)) {  // on a min face: Dirichlet (Neumann.hpp / Cauchy.hpp "index 0" branch)
+            F.cg_new = 1.0;
+            continue;
+        }
+        // Max faces only: the inner update, with the missing neighbour of each
+        // max-face direction replaced by the inner one plus the flux term.
+        F.cu = cfg->c0;
+        F.cf = cfg->cf;
+        for (int p = 0; p < 3; ++p) {
+            const bool on_max = (m >> (2 * p + 1)) & 1;
+            if (on_max) {
+                F.cn[2 * p] = 2.0 * cfg->cp[p];
+                const double flux = cfg->cp[p] * (2.0 * h[p] / lambda);
+                if (kind == SCAFES_FLUX_NEUMANN) {
+                    F.cg_old -= flux;
+                } else {
+                    F.cu -= flux * alpha;
+                    F.cg_old += flux;
+                }
+            } else {
+                F.cn[2 * p] = cfg->cp[p];
+                F.cn[2 * p + 1] = cfg->cp[p];
+            }
+        }
     }
     return SCAFES_OK;
 }

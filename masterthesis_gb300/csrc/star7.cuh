@@ -5,6 +5,7 @@
 #include <cuda.h>
 
 #include "scafes_common.cuh"
+#include "../../include/scafes_gb300.h"
 
 namespace scafes {
 
@@ -72,6 +73,7 @@ struct Star7Launch {
     double time_old;      // time(t)   : F is read at the old time
     double time_new;      // time(t+1) : G is read at the new time
     double mirror_corr;   // 2^t for SCAFES_BORDER_MIRROR_POW2
+    const scafes_border_form* table;  // device rules for SCAFES_BORDER_TABLE
 };
 
 // Enqueues one sweep (one time step) on `stream`.  Returns cudaSuccess or the

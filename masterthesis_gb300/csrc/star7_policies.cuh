@@ -14,6 +14,7 @@ struct PolF64 {
     using T = double;
     static __device__ __forceinline__ T zero() { return 0.0; }
     static __device__ __forceinline__ T from_double(double d) { return d; }
+    static __device__ __forceinline__ double to_double(T v) { return v; }
     template <bool HAS_F>
     static __device__ __forceinline__ T star(const Star7Coeffs& c, T u, T w, T e,
                                              T s, T n, T b, T t, T f) {
@@ -36,6 +37,7 @@ struct PolF32 {
     using T = float;
     static __device__ __forceinline__ T zero() { return 0.0f; }
     static __device__ __forceinline__ T from_double(double d) { return (float)d; }
+    static __device__ __forceinline__ double to_double(T v) { return (double)v; }
     template <bool HAS_F>
     static __device__ __forceinline__ T star(const Star7Coeffs& c, T u, T w, T e,
                                              T s, T n, T b, T t, T f) {
@@ -71,6 +73,7 @@ struct PolF32x2 {
         f2 p = split_double(d);
         return make_float2(p.hi, p.lo);
     }
+    static __device__ __forceinline__ double to_double(T v) { return (double)v.x + (double)v.y; }
     template <bool HAS_F>
     static __device__ __forceinline__ T star(const Star7Coeffs& c, T u, T w, T e,
                                              T s, T n, T b, T t, T f) {

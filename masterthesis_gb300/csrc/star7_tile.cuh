@@ -51,7 +51,36 @@ struct TileJob {
     T gval;                  // border value when ga is null
     Layout L;
     Split time_old, time_new, corr;  // time(t), time(t+1), mirror correction
+    const scafes_border_form* table;  // border rules (SCAFES_BORDER_TABLE)
 };
+
+// The table rule of a border node, in FP64 whatever the element type (border
+// nodes are a thin layer; the rule needs the reference's rounding, not
+// speed).  mask: faces the node lies on; off: its element offset.
+template <class P, bool HAS_F, bool HAS_FB>
+__device__ __noinline__ typename P::T table_rule(const TileJob<typename P::T>& J, int mask, long long off,
+                                                  typename P::T u, typename P::T w, typename P::T e,
+                                                  typename P::T s, typename P::T n, typename P::T b,
+                                                  typename P::T t) {
+    const scafes_border_form& R = J.table[mask];
+    double v = R.cu * P::to_double(u);
+    v = fma(R.cn[0], P::to_double(w), v);
+    v = fma(R.cn[1], P::to_double(e), v);
+    v = fma(R.cn[2], P::to_double(s), v);
+    v = fma(R.cn[3], P::to_double(n), v);
+    v = fma(R.cn[4], P::to_double(b), v);
+    v = fma(R.cn[5], P::to_double(t), v);
+    if (HAS_F) {
+        double f = P::to_double(J.fa[off]);
+        if (HAS_FB) f = fma(J.time_old.d, P::to_double(J.fb[off]), f);
+        v = fma(R.cf, f, v);
+    }
+    const double g = J.ga ? P::to_double(J.ga[off]) : P::to_double(J.gval);
+    const double gb = J.gb ? P::to_double(J.gb[off]) : 0.0;
+    v = fma(R.cg_old, fma(J.time_old.d, gb, g), v);
+    v = fma(R.cg_new, fma(J.time_new.d, gb, g), v);
+    return P::from_double(v);
+}
 
 // Initialises the ring's mbarriers (thread 0) -- once per CTA.
 template <class T, int BY>
@@ -154,7 +183,11 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 if (HAS_F && live) f = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
                 T v = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
                 if (!INNER && live && (xb || y == 0 || y == L.ny - 1)) {
-                    if (BORDER == SCAFES_BORDER_DIRICHLET) {
+                    if (BORDER == SCAFES_BORDER_TABLE) {
+                        const int mask = (x == 0) | ((x == L.nx - 1) << 1) | ((y == 0) << 2) |
+                                         ((y == L.ny - 1) << 3);
+                        v = table_rule<P, HAS_F, has_fb>(J, mask, off, cur[k], w, e, s, n, below[k], above[k]);
+                    } else if (BORDER == SCAFES_BORDER_DIRICHLET) {
                         v = J.ga ? J.ga[off] : J.gval;
                         if (has_gb) v = P::src(v, J.gb[off], J.time_new, true);
                     } else {
@@ -192,6 +225,10 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                         T f = P::zero();
                         if (HAS_F) f = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
                         v = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
+                    } else if (BORDER == SCAFES_BORDER_TABLE) {
+                        const int mask = (x == 0) | ((x == L.nx - 1) << 1) | ((y == 0) << 2) |
+                                         ((y == L.ny - 1) << 3) | ((z == 0) << 4) | ((z == L.nz - 1) << 5);
+                        v = table_rule<P, HAS_F, has_fb>(J, mask, off, cur[k], w, e, s, n, below[k], above[k]);
                     } else if (BORDER == SCAFES_BORDER_DIRICHLET) {
                         // Border values are stored in the element type, so
                         // this branch does no FP64 work on the FP32 paths.

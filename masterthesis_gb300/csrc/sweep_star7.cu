@@ -17,7 +17,7 @@ star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
           const typename P::T* __restrict__ fa, const typename P::T* __restrict__ fb,
           const typename P::T* __restrict__ ga, const typename P::T* __restrict__ gb, typename P::T gval,
           Layout L, Star7Coeffs c, Split time_old, Split time_new,
-          Split corr, int zchunk, int* __restrict__ status)
+          Split corr, const scafes_border_form* __restrict__ table, int zchunk, int* __restrict__ status)
 {
     using T = typename P::T;
     using G = Tile<T, BY>;
@@ -25,7 +25,7 @@ star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
     T* st = reinterpret_cast<T*>(smem_raw);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NSTAGE * G::STRIDE * G::ESZ);
     ring_init<T, BY>(bar);
-    TileJob<T> J{&tm, un, fa, fb, ga, gb, gval, L, time_old, time_new, corr};
+    TileJob<T> J{&tm, un, fa, fb, ga, gb, gval, L, time_old, time_new, corr, table};
     const int z0 = blockIdx.z * zchunk;
     const int z1 = min(z0 + zchunk, L.nz);
     uint32_t base = 0;
@@ -117,7 +117,7 @@ static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
     kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, (T*)a.un, (const T*)a.fa, (const T*)a.fb, (const T*)a.ga,
                                            (const T*)a.gb, gval, L,
                                            a.c, make_split(a.time_old), make_split(a.time_new),
-                                           make_split(a.mirror_corr), zchunk, a.status);
+                                           make_split(a.mirror_corr), a.table, zchunk, a.status);
     return cudaGetLastError();
 }
 
@@ -141,8 +141,14 @@ static cudaError_t launch_src(const Star7Launch& a, cudaStream_t stream) {
 
 template <class P>
 static cudaError_t launch_prec(const Star7Launch& a, cudaStream_t stream) {
-    if (a.border == SCAFES_BORDER_DIRICHLET) return launch_src<P, SCAFES_BORDER_DIRICHLET>(a, stream);
-    return launch_src<P, SCAFES_BORDER_MIRROR_POW2>(a, stream);
+    switch (a.border) {
+        case SCAFES_BORDER_DIRICHLET: return launch_src<P, SCAFES_BORDER_DIRICHLET>(a, stream);
+        case SCAFES_BORDER_MIRROR_POW2: return launch_src<P, SCAFES_BORDER_MIRROR_POW2>(a, stream);
+        case SCAFES_BORDER_TABLE:
+            if (a.table == nullptr) return cudaErrorInvalidValue;
+            return launch_src<P, SCAFES_BORDER_TABLE>(a, stream);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_star7(const Star7Launch& a, cudaStream_t stream) {

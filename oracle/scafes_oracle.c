@@ -92,6 +92,15 @@ static double known_at(orc_known kf, size_t m, double time)
         v += kf.b * tmp;
         return v;
     }
+    if (kf.form == 2) {
+        /* tests/system/HeatEqnFDM/Cauchy/TimeLinSpaceLin/TimeLinSpaceLin.hpp
+         * evalBorder, flux nodes: G = (1 + sum x) * (ALPHA*(1+t))
+         * + LAMBDA*(1+t) with base = 1 + sum x, a = ALPHA, b = LAMBDA. */
+        double v = kf.base[m];
+        v *= kf.a * (1.0 + time);
+        v += kf.b * (1.0 + time);
+        return v;
+    }
     return kf.base[m] * (kf.a + kf.b * time);
 }
 
@@ -132,6 +141,86 @@ int orc_heat_dirichlet(const orc_grid* g, double coeff_a, double rho_c,
                     for (int p = 0; p < g->dim; ++p) {
                         const double s = uo[m - stride[p]] + uo[m + stride[p]] - 2.0 * uo[m];
                         v += g->tau * coeff_a * s / (g->h[p] * g->h[p]);
+                    }
+                    if (use_perf) v -= g->tau * perf_q1 * perf_w * uo[m];
+                    v += g->tau * (1.0 / rho_c) * known_at(f_src, m, t_old);
+                    un[m] = v;
+                }
+            }
+        }
+        double* tmp = uo; uo = un; un = tmp;
+    }
+    if (uo != u) memcpy(u, uo, nn * sizeof(double));
+    free(w);
+    return 0;
+}
+
+int orc_heat_flux(const orc_grid* g, double coeff_a, double rho_c, double perf_q1,
+                  double perf_w, double lambda, double alpha, int kind, int nsteps,
+                  double* u, orc_known f_src, orc_known g_dir, orc_known g_flux,
+                  int nthreads)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const int nn3[3] = {nx, ny, nz};
+    const size_t nn = n_total(g);
+    if (kind != 0 && kind != 1) return -2;
+    double* w = (double*)malloc(nn * sizeof(double));
+    if (!w) return -1;
+    const int use_perf = (perf_q1 != 0.0 || perf_w != 0.0);
+    const long stride[3] = {1, nx, (long)nx * ny};
+    set_threads(nthreads);
+    double* uo = u;
+    double* un = w;
+    for (int t = 1; t <= nsteps; ++t) {
+        const double t_new = orc_time(g, t);
+        const double t_old = orc_time(g, t - 1);
+#pragma omp parallel for schedule(static)
+        for (int k = 0; k < nz; ++k) {
+            for (int j = 0; j < ny; ++j) {
+                for (int i = 0; i < nx; ++i) {
+                    const size_t m = IDX(i, j, k, nx, ny);
+                    const int idx[3] = {i, j, k};
+                    if (!orc_is_border(g, i, j, k)) {
+                        /* HeatEqnFDM.hpp:207-217 / PennesBioheatEqnFDM.hpp:155-167 */
+                        double v = uo[m];
+                        for (int p = 0; p < g->dim; ++p) {
+                            const double s = uo[m - stride[p]] + uo[m + stride[p]] - 2.0 * uo[m];
+                            v += g->tau * coeff_a * s / (g->h[p] * g->h[p]);
+                        }
+                        if (use_perf) v -= g->tau * perf_q1 * perf_w * uo[m];
+                        v += g->tau * (1.0 / rho_c) * known_at(f_src, m, t_old);
+                        un[m] = v;
+                        continue;
+                    }
+                    /* Neumann.hpp / Cauchy.hpp updateBorder: an index 0 in any
+                     * direction -> Dirichlet knownDf(1) (time t). */
+                    int at_min = 0;
+                    for (int p = 0; p < g->dim; ++p)
+                        if (idx[p] == 0) at_min = 1;
+                    if (at_min) {
+                        un[m] = known_at(g_dir, m, t_new);
+                        continue;
+                    }
+                    /* Otherwise the inner update with, in each direction of a
+                     * max face, the missing neighbour replaced by the inner one
+                     * and the flux term of knownDfOld(1). */
+                    const double gold = known_at(g_flux, m, t_old);
+                    double v = uo[m];
+                    for (int p = 0; p < g->dim; ++p) {
+                        const double hp = g->h[p];
+                        double s;
+                        if (idx[p] == nn3[p] - 1) {
+                            if (kind == 0)
+                                s = uo[m - stride[p]] + uo[m - stride[p]] - ((2.0 * hp / lambda) * gold)
+                                    - 2.0 * uo[m];
+                            else
+                                s = uo[m - stride[p]] + uo[m - stride[p]]
+                                    - ((2.0 * hp / lambda) * alpha * uo[m])
+                                    + ((2.0 * hp / lambda) * gold) - 2.0 * uo[m];
+                        } else {
+                            s = uo[m - stride[p]] + uo[m + stride[p]] - 2.0 * uo[m];
+                        }
+                        v += g->tau * coeff_a * s / (hp * hp);
                     }
                     if (use_perf) v -= g->tau * perf_q1 * perf_w * uo[m];
                     v += g->tau * (1.0 / rho_c) * known_at(f_src, m, t_old);

@@ -49,6 +49,7 @@ void orc_coords(const orc_grid* g, int i, int j, int k, double* x);
  *   form 1: base*a + b*(base*(1 + time)) (PennesBioheatEqnFDM/Dirichlet/
  *           TimeLinSpaceLin/TimeLinSpaceLin.hpp:82-91 f, with
  *           a = RHO*C and b = RHO_BLOOD*C_BLOOD*W) */
+/*   form 2: base*(a*(1 + time)) + b*(1 + time)  (Cauchy flux field)   */
 typedef struct orc_known {
     const double* base;
     int form;
@@ -64,6 +65,21 @@ typedef struct orc_known {
 int orc_heat_dirichlet(const orc_grid* g, double coeff_a, double rho_c,
                        double perf_q1, double perf_w, int nsteps, double* u,
                        orc_known f_src, orc_known g_bdry, int nthreads);
+
+/* Heat / Pennes with the flux-condition border of the reference's system
+ * tests (kind 0: tests/system/HeatEqnFDM/Neumann/Neumann.hpp and
+ * tests/system/PennesBioheatEqnFDM/Neumann/Neumann.hpp; kind 1: the
+ * Cauchy.hpp files beside them): a border node with an index 0 takes
+ * Dirichlet g_dir at time(t); the others take the inner update where, in
+ * each direction of a max face, the missing neighbour is the inner one and
+ * the flux of g_flux at time(t-1) enters (- (2h/lambda) G for Neumann,
+ * - (2h/lambda) alpha u + (2h/lambda) G for Cauchy), in the reference's
+ * operation order.  Known-field form 2 (base*(a*(1+t)) + b*(1+t)) is the
+ * Cauchy flux field of Cauchy/TimeLinSpaceLin. */
+int orc_heat_flux(const orc_grid* g, double coeff_a, double rho_c, double perf_q1,
+                  double perf_w, double lambda, double alpha, int kind, int nsteps,
+                  double* u, orc_known f_src, orc_known g_dir, orc_known g_flux,
+                  int nthreads);
 
 /* Variable-coefficient Pennes bioheat (examples/MRIDataPBHEqnFDM/
  * MRIDataPBHEqnFDM.hpp:143-169) with scalar rho, c, k, rho_b, c_b, omega,

@@ -64,6 +64,14 @@ def main():
     r = O.run_ref("ref_pennes_timelin", n, T, tmp)
     cases["pennes_timelin"] = dict(n=n, nsteps=T, t_end=1.0, final=r)
 
+    # Flux-condition borders: tests/system/{HeatEqnFDM,PennesBioheatEqnFDM}/{Neumann,Cauchy}/
+    # TimeLinSpaceLin/RUN_3D.sh.in (8^3, 300 steps, t in [0,1]) plus a non-cubic grid.
+    for name in ("heat_neumann", "heat_cauchy", "pennes_neumann", "pennes_cauchy"):
+        r = O.run_ref(f"ref_{name}", n, T, tmp)
+        cases[name] = dict(n=n, nsteps=T, t_end=1.0, final=r)
+    r = O.run_ref("ref_heat_neumann", (10, 8, 6), 320, tmp)
+    cases["heat_neumann_10x8x6"] = dict(n=(10, 8, 6), nsteps=320, t_end=1.0, final=r)
+
     # tests/system/HeatEqnFdmStencilWidthVar/TESTMATRIX_RUN_3D.sh.in: 32^3, 20 steps.
     n, T = (32, 32, 32), 20
     r = O.run_ref("ref_stencil_width_var", n, T, tmp, nfields=3)

@@ -123,3 +123,30 @@ def test_kheat_adjoint_matches_finite_differences():
         fd_u = (J_of(k, u0 + eps * du) - J_of(k, u0 - eps * du)) / (2 * eps)
         assert abs(fd_k - np.sum(gk * dk)) <= 1e-6 * max(abs(fd_k), 1e-12)
         assert abs(fd_u - np.sum(gu * du)) <= 1e-6 * max(abs(fd_u), 1e-12)
+
+
+def flux_case(name):
+    """Inputs of a flux-border TimeLinSpaceLin golden case (the known fields
+    of tests/system/{HeatEqnFDM,PennesBioheatEqnFDM}/{Neumann,Cauchy}/
+    TimeLinSpaceLin/TimeLinSpaceLin.hpp in the oracle's known-field forms)."""
+    d = load_golden(name)
+    n, T = tuple(d["n"]), int(d["nsteps"])
+    g = O.make_grid(n, tau=float(d["t_end"]) / T)
+    x, y, z = O.coords(g)
+    S = np.broadcast_to(((1.0 + x) + y) + z, (n[2], n[1], n[0])).copy()
+    pennes = name.startswith("pennes")
+    kind = 1 if "cauchy" in name else 0
+    f = (S, 1, 1.0, 1.0) if pennes else (S, 0, 1.0, 0.0)
+    g_flux = (S, 2, 1.0, 1.0) if kind == 1 else (np.full(S.shape, -1.0), 0, 1.0, 1.0)
+    perf = dict(perf_q1=1.0, perf_w=1.0) if pennes else {}
+    return d, g, S, T, kind, f, g_flux, perf
+
+
+@pytest.mark.parametrize("name", ["heat_neumann", "heat_cauchy", "pennes_neumann", "pennes_cauchy",
+                                  "heat_neumann_10x8x6"])
+def test_flux_border_bit_exact(name):
+    d, g, S, T, kind, f, g_flux, perf = flux_case(name)
+    u = O.heat_flux(g, S * 1.0, T, kind, f=f, g_dir=(S, 0, 1.0, 1.0), g_flux=g_flux, **perf)
+    assert np.array_equal(u, d["final"])
+    exact = S * (1.0 + O.lib().orc_time(g, T))
+    assert np.max(np.abs(u - exact)) / np.max(np.abs(exact)) < 1e-14
