@@ -32,6 +32,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <iostream>
 #include <map>
 #include <sstream>
@@ -268,6 +269,48 @@ private:
         return F;
     }
 
+    // The table rule of one border node's recorded form, or why there is
+    // none: u_new = cu*u + sum_d cn[d]*u_d + cf*(the inner source)
+    //               + cg_old*G(old) + cg_new*G(new), G one known field.
+    std::string tableRule(const gpu::Sym& s1, const gpu::Sym& s2, const Form& F, const std::vector<Affine>& aff,
+                          int& gfield, scafes_border_form& r) const {
+        if (!same(s1, s2)) return "the rule changes between time steps";
+        if (s1.constant() != 0.0) return "a constant term";
+        double cf = 0.0;
+        bool have_cf = false;
+        std::map<std::pair<int, int>, double> src;
+        for (const auto& kv : s1.terms()) {
+            const auto& k = kv.first;
+            if (k.kind == 0) {
+                if (k.a != 0) return "several unknown fields";
+                const int nz = (k.b != 0) + (k.c != 0) + (k.d != 0);
+                const int mag = std::abs(k.b) + std::abs(k.c) + std::abs(k.d);
+                if (nz == 0) { r.cu += kv.second; continue; }
+                if (nz != 1 || mag != 1) return "a neighbour beyond the 7-point star";
+                const int p = k.b ? 0 : (k.c ? 1 : 2);
+                const int sgn = k.b + k.c + k.d;
+                r.cn[2 * p + (sgn > 0 ? 1 : 0)] += kv.second;
+                continue;
+            }
+            if (aff[k.a].zero) continue;  // a known field that is 0 everywhere
+            if (F.known.count({k.a, k.b})) { src[{k.a, k.b}] += kv.second; continue; }
+            if (gfield == -1) gfield = k.a;
+            if (k.a != gfield) return "more than one border known field";
+            (k.b ? r.cg_old : r.cg_new) += kv.second;
+        }
+        // The source terms must be a multiple of the inner update's source.
+        for (const auto& kv : F.known) {
+            if (aff[kv.first.first].zero) continue;
+            const auto it = src.find(kv.first);
+            const double c = it == src.end() ? 0.0 : it->second;
+            const double ratio = c / kv.second;
+            if (!have_cf) { cf = ratio; have_cf = true; }
+            else if (ratio != cf) return "source terms that are not a multiple of the inner source";
+        }
+        r.cf = cf;
+        return std::string();
+    }
+
     void fitAffine(std::vector<Affine>& aff, std::vector<CT>& k0, std::vector<CT>& k1) {
         const std::size_t nf = mNames.size();
         const double t0 = time(0), tau = mParams.tau();
@@ -307,6 +350,7 @@ private:
     bool mPrepared = false;
     scafes_cfg mCfg = {};
     std::vector<double> mFa, mFb, mGa, mGb;
+    scafes_border_form mForms[SCAFES_BORDER_CLASSES] = {};
     scafes_handle* mHandle = nullptr;
     std::map<int, double> mErrLinf;
     double mGpuMs = 0.0;
@@ -405,8 +449,17 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     if (first) throw std::runtime_error("ScaFES::Problem: the grid has no inner nodes");
     Form F = starForm(inner);
 
-    // Border: every global-border node, at steps 1 and 2.
-    int border = -1, gfield = -1, gwhen = 0;
+    // Border: every global-border node, at steps 1 and 2.  Three device
+    // forms are tried at once: Dirichlet from one known field, the
+    // StencilWidthOne mirror rule, and a table of one linear rule per border
+    // class (the set of faces the node lies on) -- the reference's Neumann
+    // and Cauchy borders.
+    int gfield = -1, gwhen = 0;
+    bool dir_ok = true, mir_ok = true, tab_ok = true;
+    std::string tab_why;
+    scafes_border_form forms[SCAFES_BORDER_CLASSES] = {};
+    bool seen[SCAFES_BORDER_CLASSES] = {};
+    int tab_g = -1;  // the one known field the table rules read as G
     for (long long m = 0; m < mN; ++m) {
         const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
         if (!isBorder(n)) continue;
@@ -415,26 +468,48 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
         gpu::Sym s2 = record<true>(n, 2, err)[0];
         if (!err.empty()) throw std::runtime_error("ScaFES::Problem: " + err);
         if (s1.bad()) throw std::runtime_error("ScaFES::Problem: updateBorder is not linear: " + describe(s1));
-        // Dirichlet: u_new = K_j.
         const auto& tt = s1.terms();
-        if (tt.size() == 1 && tt[0].first.kind == 1 && tt[0].second == 1.0 && s1.constant() == 0.0 && same(s1, s2)) {
-            if (border == -1) { border = SCAFES_BORDER_DIRICHLET; gfield = tt[0].first.a; gwhen = tt[0].first.b; }
-            if (border == SCAFES_BORDER_DIRICHLET && gfield == tt[0].first.a && gwhen == tt[0].first.b) continue;
-        }
+        // Dirichlet: u_new = K_j.
+        const bool dir = tt.size() == 1 && tt[0].first.kind == 1 && tt[0].second == 1.0 && s1.constant() == 0.0 &&
+                         same(s1, s2) && (gfield == -1 || (gfield == tt[0].first.a && gwhen == tt[0].first.b));
+        if (dir && gfield == -1) { gfield = tt[0].first.a; gwhen = tt[0].first.b; }
+        dir_ok = dir_ok && dir;
         // StencilWidthOne mirror: u_new = u + u(opposite) + s*2^(t-1).
         bool mirror = tt.size() == 2 && s1.constant() != 0.0 && s2.constant() == 2.0 * s1.constant() &&
                       std::fabs(s1.constant()) == 1.0;
-        if (mirror) {
+        if (mirror)
             for (const auto& kv : tt)
                 if (kv.first.kind != 0 || kv.second != 1.0) mirror = false;
+        mir_ok = mir_ok && mirror;
+        if (!tab_ok) {
+            if (!dir_ok && !mir_ok)
+                throw std::runtime_error("ScaFES::Problem: updateBorder at node has no device form (" + tab_why +
+                                         "): " + describe(s1));
+            continue;
         }
-        if (mirror) {
-            if (border == -1) border = SCAFES_BORDER_MIRROR_POW2;
-            if (border == SCAFES_BORDER_MIRROR_POW2) continue;
+        // Table rule of this node's class.
+        int mask = 0;
+        for (std::size_t p = 0; p < DIM; ++p) {
+            if (n[p] == g.idxNodeFirst(p)) mask |= 1 << (2 * p);
+            if (n[p] == g.idxNodeLast(p)) mask |= 1 << (2 * p + 1);
         }
-        throw std::runtime_error("ScaFES::Problem: updateBorder at node has no device form: " + describe(s1));
+        scafes_border_form r = {};
+        std::string why = tableRule(s1, s2, F, aff, tab_g, r);
+        if (why.empty() && seen[mask] && std::memcmp(&r, &forms[mask], sizeof(r)) != 0)
+            why = "the rule differs between nodes on the same faces";
+        if (!why.empty()) {
+            tab_ok = false;
+            tab_why = why;
+            if (!dir_ok && !mir_ok)
+                throw std::runtime_error("ScaFES::Problem: updateBorder at node has no device form (" + why + "): " +
+                                         describe(s1));
+            continue;
+        }
+        forms[mask] = r;
+        seen[mask] = true;
     }
-    if (border == -1) border = SCAFES_BORDER_DIRICHLET;
+    int border = dir_ok ? SCAFES_BORDER_DIRICHLET : mir_ok ? SCAFES_BORDER_MIRROR_POW2 : SCAFES_BORDER_TABLE;
+    if (border == SCAFES_BORDER_TABLE) std::copy(forms, forms + SCAFES_BORDER_CLASSES, mForms);
     mWallClockTimes["record"] += std::chrono::duration<double>(clock::now() - t_rec).count();
 
     // 4. Device run.
@@ -476,6 +551,18 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     cfg.cf = has_f ? 1.0 : 0.0;
     if (has_f) mFa.swap(fa);
     if (has_fb) mFb.swap(fb);
+    if (border == SCAFES_BORDER_TABLE && tab_g >= 0) {
+        const Affine& A = aff[tab_g];
+        if (A.a.empty())
+            throw std::runtime_error("ScaFES::Problem: border field " + mNames[tab_g] + " is not affine in time");
+        mGa = A.a;
+        if (A.timed) mGb = A.b;
+    }
+    bool table_reads_f = false;
+    if (border == SCAFES_BORDER_TABLE)
+        for (int c = 1; c < SCAFES_BORDER_CLASSES; ++c) table_reads_f = table_reads_f || mForms[c].cf != 0.0;
+    if (table_reads_f && !has_f)
+        throw std::runtime_error("ScaFES::Problem: updateBorder reads a source the inner update does not have");
     if (border == SCAFES_BORDER_DIRICHLET && gfield >= 0 && !aff[gfield].zero) {
         const Affine& A = aff[gfield];
         if (A.a.empty())
@@ -489,7 +576,8 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     std::ostringstream os;
     os << "star7 c0=" << cfg.c0 << " cp=(" << cfg.cp[0] << "," << cfg.cp[1] << "," << cfg.cp[2] << ")"
        << " source=" << (has_f ? (has_fb ? "affine" : "static") : "none")
-       << " border=" << (border == SCAFES_BORDER_DIRICHLET ? "dirichlet" : "mirror");
+       << " border=" << (border == SCAFES_BORDER_DIRICHLET ? "dirichlet"
+                         : border == SCAFES_BORDER_MIRROR_POW2 ? "mirror" : "table");
     mSummary = os.str();
     mPrepared = true;
 }
@@ -503,6 +591,7 @@ void Problem<OWNPRBLM, CT, DIM>::iterateOverTime() {
     scafes_cfg cfg = mCfg;
     if (mHandle) { scafes_gpu_destroy(mHandle); mHandle = nullptr; }
     check(scafes_gpu_create(&cfg, &mHandle));
+    if (cfg.border == SCAFES_BORDER_TABLE) check(scafes_gpu_set_border_forms(mHandle, mForms));
     if (!mFa.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_F_A, mFa.data(), mFa.size()));
     if (!mFb.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_F_B, mFb.data(), mFb.size()));
     if (!mGa.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_G_A, mGa.data(), mGa.size()));

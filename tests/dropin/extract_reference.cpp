@@ -5,13 +5,14 @@
 // the matching reference main3D.cpp:
 //   1 HeatEqnFDM/Dirichlet/TimeLinSpaceLin        2 PennesBioheatEqnFDM/Dirichlet/TimeLinSpaceLin
 //   3 HeatEqnFdmStencilWidthOne                   4 HeatEqnFDM/Neumann/TimeLinSpaceLin
-//   5 PropagationFromLeftLowerCorner
+//   5 PropagationFromLeftLowerCorner              6 HeatEqnFDM/Cauchy/TimeLinSpaceLin
+//   7 PennesBioheatEqnFDM/Neumann/TimeLinSpaceLin 8 PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin
 #include <iostream>
 #include <string>
 #include <vector>
 
 #include "ScaFES.hpp"
-#if PROBLEM == 1 || PROBLEM == 2 || PROBLEM == 4
+#if PROBLEM == 1 || PROBLEM == 2 || PROBLEM == 4 || PROBLEM == 6 || PROBLEM == 7 || PROBLEM == 8
 #include "TimeLinSpaceLin.hpp"
 #define CLASS TimeLinSpaceLin
 #elif PROBLEM == 3

@@ -8,6 +8,10 @@
 //   MirrorPow2 -- the 2/7 averaging stencil with the mirrored border,
 //                 exact solution 2^n (i+j+k) (tests/system/HeatEqnFdmStencilWidthOne)
 //   HeatSine   -- heat equation, Dirichlet 0, u0 = sin(pi x) sin(pi y) sin(pi z)
+//   HeatFlux<KIND> -- heat equation, Dirichlet at the min faces and a Neumann
+//                 (KIND 0) or Cauchy (KIND 1) flux condition at the max faces,
+//                 exact solution (1+t)(1+x+y+z)
+//                 (tests/system/HeatEqnFDM/{Neumann,Cauchy}/TimeLinSpaceLin)
 #pragma once
 
 #include <cmath>
@@ -197,6 +201,87 @@ public:
     void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>&,
                       const ScaFES::Ntuple<int, DIM>& n, const int&) {
         vNew[0](n) = this->knownDf(1, n);
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};
+
+template <typename CT, std::size_t DIM, int KIND>
+class HeatFlux : public ScaFES::Problem<HeatFlux<CT, DIM, KIND>, CT, DIM> {
+    using Base = ScaFES::Problem<HeatFlux<CT, DIM, KIND>, CT, DIM>;
+public:
+    using Base::Base;
+    const double RHO = 1.0, C = 1.0, LAMBDA = 1.0, ALPHA = 1.0;
+    bool onMin(const ScaFES::Ntuple<int, DIM>& n) const {
+        for (std::size_t p = 0; p < DIM; ++p)
+            if (n[p] == 0) return true;
+        return false;
+    }
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        const double s = HeatLin<CT, DIM>::lin(this->coordinates(n));
+        v[0](n) = s * (RHO * C);
+        v[1](n) = 0.0;
+        v[2](n) = s * (1.0 + this->time(t));
+    }
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        const double s = HeatLin<CT, DIM>::lin(this->coordinates(n));
+        const double tt = this->time(t);
+        v[0](n) = s * (RHO * C);
+        if (onMin(n)) v[1](n) = s * (1.0 + tt);
+        else if (KIND == 0) v[1](n) = -1.0 * LAMBDA * (1.0 + tt);
+        else v[1](n) = s * (ALPHA * (1.0 + tt)) + LAMBDA * (1.0 + tt);
+        v[2](n) = s * (1.0 + tt);
+    }
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        v[0](n) = HeatLin<CT, DIM>::lin(this->coordinates(n)) * (1.0 + this->time(t));
+    }
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>& o, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        initInner<TT>(v, o, n, t);
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        vNew[0](n) = vOld[0](n);
+        for (std::size_t p = 0; p < DIM; ++p)
+            vNew[0](n) += this->tau() * (LAMBDA / (RHO * C)) *
+                          (vOld[0](this->connect(n, 2 * p)) + vOld[0](this->connect(n, 2 * p + 1)) - 2.0 * vOld[0](n)) /
+                          (this->gridsize(p) * this->gridsize(p));
+        vNew[0](n) += this->tau() * (1.0 / (RHO * C)) * this->knownDfOld(0, n);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                      const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        if (onMin(n)) {
+            vNew[0](n) = this->knownDf(1, n);
+            return;
+        }
+        vNew[0](n) = vOld[0](n);
+        for (std::size_t p = 0; p < DIM; ++p) {
+            const double h = this->gridsize(p);
+            if (n[p] == this->nNodes(p) - 1) {
+                // The missing outer neighbour is the mirrored inner one; the
+                // flux condition enters through the border field.
+                if (KIND == 0)
+                    vNew[0](n) += this->tau() * (LAMBDA / (RHO * C)) *
+                                  (vOld[0](this->connect(n, 2 * p)) + vOld[0](this->connect(n, 2 * p)) -
+                                   ((2.0 * h / LAMBDA) * this->knownDfOld(1, n)) - 2.0 * vOld[0](n)) / (h * h);
+                else
+                    vNew[0](n) += this->tau() * (LAMBDA / (RHO * C)) *
+                                  (vOld[0](this->connect(n, 2 * p)) + vOld[0](this->connect(n, 2 * p)) -
+                                   ((2.0 * h / LAMBDA) * ALPHA * vOld[0](n)) +
+                                   ((2.0 * h / LAMBDA) * this->knownDfOld(1, n)) - 2.0 * vOld[0](n)) / (h * h);
+            } else {
+                vNew[0](n) += this->tau() * (LAMBDA / (RHO * C)) *
+                              (vOld[0](this->connect(n, 2 * p)) + vOld[0](this->connect(n, 2 * p + 1)) - 2.0 * vOld[0](n)) /
+                              (h * h);
+            }
+        }
+        vNew[0](n) += this->tau() * (1.0 / (RHO * C)) * this->knownDfOld(0, n);
     }
     template <typename TT>
     void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}

@@ -1,6 +1,7 @@
 // Runs one problem of problems.hpp through the drop-in ScaFES::Problem
 // (test infrastructure).  Usage:
-//   run_problem <heat_lin|pennes_lin|mirror_pow2|heat_sine> out.bin [--extract-only] [ScaFES options...]
+//   run_problem <heat_lin|pennes_lin|mirror_pow2|heat_sine|heat_neumann|heat_cauchy> out.bin
+//               [--extract-only] [ScaFES options...]
 // Writes the final iterate as raw doubles (x fastest); with --extract-only
 // prints the device form of the update instead (no GPU needed).
 #include <cstdio>
@@ -47,6 +48,14 @@ int main(int argc, char** argv) {
         const std::vector<bool> known{true, true, false};
         if (which == "heat_lin") {
             HeatLin<double, 3> p(params, gg, false, names, sw, known, {0, 0, 0}, {0, 0, 0}, wr, {false, false, true});
+            return run(p, out, extract);
+        }
+        if (which == "heat_neumann") {
+            HeatFlux<double, 3, 0> p(params, gg, false, names, sw, known, {0, 0, 0}, {0, 0, 0}, wr, {false, false, true});
+            return run(p, out, extract);
+        }
+        if (which == "heat_cauchy") {
+            HeatFlux<double, 3, 1> p(params, gg, false, names, sw, known, {0, 0, 0}, {0, 0, 0}, wr, {false, false, true});
             return run(p, out, extract);
         }
         if (which == "pennes_lin") {

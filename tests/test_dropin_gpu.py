@@ -58,3 +58,16 @@ def test_dropin_heat_sine_config1_vs_oracle(run_problem, tmp_path):
     u0[O.border_mask(g)] = 0.0
     ref = O.heat_dirichlet(g, u0, T)
     assert cases.rel_err(u, ref) <= 1e-12
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+@pytest.mark.parametrize("name,golden", [("heat_neumann", "heat_neumann"), ("heat_cauchy", "heat_cauchy"),
+                                         ("heat_neumann", "heat_neumann_10x8x6")])
+def test_dropin_flux_border_matches_reference(run_problem, tmp_path, name, golden, prec):
+    """Neumann / Cauchy border problems through the drop-in Problem: the
+    border rules are extracted per border class and run as a rule table."""
+    d = load_golden(golden)
+    n = tuple(int(v) for v in d["n"])
+    u, out = run(run_problem, name, tmp_path / "u.bin", n, f"--nNodes={n[0]}x{n[1]}x{n[2]}",
+                 f"--nTimesteps={int(d['nsteps'])}", f"--endtime={float(d['t_end'])!r}", f"--gpuPrecision={prec}")
+    assert cases.rel_err(u, d["final"]) <= 1e-12

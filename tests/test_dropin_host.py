@@ -29,6 +29,8 @@ def form(exe, *args):
     ("heat_lin", ["c0=0.02 ", "cp=(0.163333,0.163333,0.163333)", "source=static", "border=dirichlet"]),
     ("pennes_lin", ["c0=0.0166667", "source=affine", "border=dirichlet"]),
     ("mirror_pow2", ["c0=0.285714", "source=none", "border=mirror"]),
+    ("heat_neumann", ["c0=0.02 ", "source=static", "border=table"]),
+    ("heat_cauchy", ["c0=0.02 ", "source=static", "border=table"]),
 ])
 def test_extracted_form(run_problem, name, expect):
     s = form(run_problem, name, "/dev/null", "--extract-only", "--nNodes=8x8x8", "--nTimesteps=300", "--endtime=1")
@@ -42,7 +44,14 @@ REF_CASES = [
     (2, ["PennesBioheatEqnFDM", "PennesBioheatEqnFDM/Dirichlet", "PennesBioheatEqnFDM/Dirichlet/TimeLinSpaceLin"],
      "source=affine", "border=dirichlet"),
     (3, ["HeatEqnFdmStencilWidthOne"], "c0=0.285714", "border=mirror"),
-    (4, ["HeatEqnFDM", "HeatEqnFDM/Neumann", "HeatEqnFDM/Neumann/TimeLinSpaceLin"], "REFUSED", "updateBorder"),
+    (4, ["HeatEqnFDM", "HeatEqnFDM/Neumann", "HeatEqnFDM/Neumann/TimeLinSpaceLin"], "FORM star7 c0=0.02 ",
+     "border=table"),
+    (6, ["HeatEqnFDM", "HeatEqnFDM/Cauchy", "HeatEqnFDM/Cauchy/TimeLinSpaceLin"], "FORM star7 c0=0.02 ",
+     "border=table"),
+    (7, ["PennesBioheatEqnFDM", "PennesBioheatEqnFDM/Neumann", "PennesBioheatEqnFDM/Neumann/TimeLinSpaceLin"],
+     "source=affine", "border=table"),
+    (8, ["PennesBioheatEqnFDM", "PennesBioheatEqnFDM/Radiation",
+         "PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin"], "REFUSED", "not linear"),
     (5, ["PropagationFromLeftLowerCorner"], "REFUSED", "branches on the value"),
 ]
 
