@@ -263,28 +263,44 @@ __global__ void k_prep_x2(const double* __restrict__ k, float2* __restrict__ kx,
     }
 }
 
+// One thread marches a 16-plane chunk of one (x, y) column and keeps the
+// z-neighbours (u and the z-face conductivity of the plane below) in
+// registers, so each plane issues its loads for the plane above while the
+// current node is computed.
 __global__ void __launch_bounds__(AX * AY)
 k_forward_x2(const float2* __restrict__ u, float2* __restrict__ un, const float2* __restrict__ kx,
              const float2* __restrict__ ky, const float2* __restrict__ kz, const float2* __restrict__ dg, Layout L) {
     const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
     if (x >= L.nx || y >= L.ny) return;
-    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
     const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
-    for (int z = zb; z < ze; ++z) {
-        const long long o = L.idx(x, y, z);
-        const float2 uc = u[o];
-        if (colb || z == 0 || z == L.nz - 1) {
+    long long o = L.idx(x, y, zb);
+    if (x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1) {
+        for (int z = zb; z < ze; ++z, o += L.plane) un[o] = u[o];
+        return;
+    }
+    const float2 zero = make_float2(0.f, 0.f);
+    float2 ub = zb > 0 ? u[o - L.plane] : zero;
+    float2 kzb = zb > 0 ? kz[o - L.plane] : zero;
+    float2 uc = u[o];
+#pragma unroll 2
+    for (int z = zb; z < ze; ++z, o += L.plane) {
+        const float2 ua = z + 1 < L.nz ? u[o + L.plane] : zero;
+        const float2 kzc = kz[o];
+        if (z == 0 || z == L.nz - 1) {
             un[o] = uc;
-            continue;
+        } else {
+            f2 acc = pmul(dg[o], uc);
+            pacc(acc, pmul(kx[o], u[o + 1]));
+            pacc(acc, pmul(kx[o - 1], u[o - 1]));
+            pacc(acc, pmul(ky[o], u[o + L.pitch]));
+            pacc(acc, pmul(ky[o - L.pitch], u[o - L.pitch]));
+            pacc(acc, pmul(kzc, ua));
+            pacc(acc, pmul(kzb, ub));
+            un[o] = pnorm(acc);
         }
-        f2 acc = pmul(dg[o], uc);
-        pacc(acc, pmul(kx[o], u[o + 1]));
-        pacc(acc, pmul(kx[o - 1], u[o - 1]));
-        pacc(acc, pmul(ky[o], u[o + L.pitch]));
-        pacc(acc, pmul(ky[o - L.pitch], u[o - L.pitch]));
-        pacc(acc, pmul(kz[o], u[o + L.plane]));
-        pacc(acc, pmul(kz[o - L.plane], u[o - L.plane]));
-        un[o] = pnorm(acc);
+        ub = uc;
+        uc = ua;
+        kzb = kzc;
     }
 }
 
@@ -311,37 +327,48 @@ k_adjoint_x2(const float2* __restrict__ lam, float2* __restrict__ lamn, const fl
     const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
     const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
     const float2 zero = make_float2(0.f, 0.f);
-    for (int z = zb; z < ze; ++z) {
-        const long long o = L.idx(x, y, z);
+    long long o = L.idx(x, y, zb);
+    // z-neighbours in registers: lambda below / here, u here, the z-face
+    // conductivity below.
+    float2 lb = zb > 0 ? lam[o - L.plane] : zero;
+    float2 lc = lam[o];  // zero on border nodes
+    float2 uc = u[o];
+    float2 kzb = zb > 0 ? kz[o - L.plane] : zero;
+#pragma unroll 2
+    for (int z = zb; z < ze; ++z, o += L.plane) {
+        const bool top = z + 1 < L.nz;
+        const float2 la = top ? lam[o + L.plane] : zero;
+        const float2 ua = top ? u[o + L.plane] : zero;
+        const float2 kzc = kz[o];
         const bool border = colb || z == 0 || z == L.nz - 1;
-        const float2 lc = lam[o];  // zero on border nodes
-        const float2 uc = u[o];
         const float2 lxp = x + 1 < L.nx ? lam[o + 1] : zero, lxm = x > 0 ? lam[o - 1] : zero;
         const float2 lyp = y + 1 < L.ny ? lam[o + L.pitch] : zero, lym = y > 0 ? lam[o - L.pitch] : zero;
-        const float2 lzp = z + 1 < L.nz ? lam[o + L.plane] : zero, lzm = z > 0 ? lam[o - L.plane] : zero;
         if (x + 1 < L.nx) gx[o] = gacc(gx[o], u[o + 1], uc, lc, lxp);
         if (y + 1 < L.ny) gy[o] = gacc(gy[o], u[o + L.pitch], uc, lc, lyp);
-        if (z + 1 < L.nz) gz[o] = gacc(gz[o], u[o + L.plane], uc, lc, lzp);
-        const float2 kxp = kx[o], kyp = ky[o], kzp = kz[o];
+        if (top) gz[o] = gacc(gz[o], ua, uc, lc, la);
+        const float2 kxp = kx[o], kyp = ky[o];
         const float2 kxm = x > 0 ? kx[o - 1] : zero, kym = y > 0 ? ky[o - L.pitch] : zero;
-        const float2 kzm = z > 0 ? kz[o - L.plane] : zero;
         f2 acc = border ? f2{0.f, 0.f} : pmul(dg[o], lc);
         pacc(acc, pmul(kxp, lxp));
         pacc(acc, pmul(kxm, lxm));
         pacc(acc, pmul(kyp, lyp));
         pacc(acc, pmul(kym, lym));
-        pacc(acc, pmul(kzp, lzp));
-        pacc(acc, pmul(kzm, lzm));
+        pacc(acc, pmul(kzc, la));
+        pacc(acc, pmul(kzb, lb));
         if (border) {
             // Border rows of the update are the identity: lambda on the border
             // only collects what the inner neighbours pass back.
-            const float2 b = bnd[o];
-            pacc(acc, {b.x, b.y});
+            const float2 bo = bnd[o];
+            pacc(acc, {bo.x, bo.y});
             bnd[o] = pnorm(acc);
             lamn[o] = zero;
         } else {
             lamn[o] = pnorm(acc);
         }
+        lb = lc;
+        lc = la;
+        uc = ua;
+        kzb = kzc;
     }
 }
 
