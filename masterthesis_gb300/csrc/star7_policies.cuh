@@ -30,6 +30,16 @@ struct PolF64 {
     }
     static __device__ __forceinline__ T src(T fa, T fb, const Split& time, bool has_b) {
         return has_b ? fa + time.d * fb : fa;
+    }    // All R rows of one thread (row k's s/n neighbours are rows k-1/k+1,
+    // ym/yp beyond the ends).
+    template <bool HAS_F, int R>
+    static __device__ __forceinline__ void star_rows(const Star7Coeffs& c, const T (&below)[R], const T (&cur)[R],
+                                                     const T (&above)[R], T ym, T yp, const T (&w)[R],
+                                                     const T (&e)[R], const T (&f)[R], T (&v)[R]) {
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+            v[k] = star<HAS_F>(c, cur[k], w[k], e[k], k == 0 ? ym : cur[k - 1], k == R - 1 ? yp : cur[k + 1],
+                               below[k], above[k], f[k]);
     }
 };
 
@@ -53,6 +63,16 @@ struct PolF32 {
     }
     static __device__ __forceinline__ T src(T fa, T fb, const Split& time, bool has_b) {
         return has_b ? fmaf(time.hi, fb, fa) : fa;
+    }    // All R rows of one thread (row k's s/n neighbours are rows k-1/k+1,
+    // ym/yp beyond the ends).
+    template <bool HAS_F, int R>
+    static __device__ __forceinline__ void star_rows(const Star7Coeffs& c, const T (&below)[R], const T (&cur)[R],
+                                                     const T (&above)[R], T ym, T yp, const T (&w)[R],
+                                                     const T (&e)[R], const T (&f)[R], T (&v)[R]) {
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+            v[k] = star<HAS_F>(c, cur[k], w[k], e[k], k == 0 ? ym : cur[k - 1], k == R - 1 ? yp : cur[k + 1],
+                               below[k], above[k], f[k]);
     }
 };
 
@@ -124,6 +144,102 @@ struct PolF32x2 {
         f2 out = fast_two_sum(hi, r);
         return make_float2(out.hi, out.lo);
     }
+    // Two rows at once on the paired FP32 instructions of sm_100+ (FFMA2,
+    // FADD2, FMUL2): component .x carries row k, .y row k+1, with exactly the
+    // operations of star() per component, so the results are bit-identical
+    // while half the arithmetic instructions are issued.  The main products
+    // are formed negated (a negated coefficient times the value is exact),
+    // so the FMA TwoProd takes -p without a separate negation; TwoSum and
+    // FastTwoSum are symmetric under negation, and the result is negated
+    // back at the end.
+    template <bool HAS_F>
+    static __device__ __forceinline__ void star2(const Star7Coeffs& c, T u0, T u1, T w0, T w1, T e0, T e1,
+                                                 T s0, T s1, T n0, T n1, T b0, T b1, T t0, T t1, T f0, T f1,
+                                                 T& o0, T& o1) {
+        const float2 M1 = make_float2(-1.f, -1.f);
+        auto bc = [](float v) { return make_float2(v, v); };
+        auto sub = [&](float2 a, float2 b) { return __ffma2_rn(b, M1, a); };  // a - b, one rounding
+        auto tsum = [&](float2 a, float2 b, float2& err) {
+            const float2 sm = __fadd2_rn(a, b);
+            const float2 bb = sub(sm, a);
+            err = __fadd2_rn(sub(a, sub(sm, bb)), sub(b, bb));
+            return sm;
+        };
+        auto hi = [](T a, T b) { return make_float2(a.x, b.x); };
+        auto lo = [](T a, T b) { return make_float2(a.y, b.y); };
+        // Axis sums: exact hi sums + FP32 tails.
+        float2 ex, ey, ez;
+        const float2 SX = tsum(hi(w0, w1), hi(e0, e1), ex);
+        const float2 SY = tsum(hi(s0, s1), hi(n0, n1), ey);
+        const float2 SZ = tsum(hi(b0, b1), hi(t0, t1), ez);
+        const float2 TX = __fadd2_rn(ex, __fadd2_rn(lo(w0, w1), lo(e0, e1)));
+        const float2 TY = __fadd2_rn(ey, __fadd2_rn(lo(s0, s1), lo(n0, n1)));
+        const float2 TZ = __fadd2_rn(ez, __fadd2_rn(lo(b0, b1), lo(t0, t1)));
+        const float2 UH = hi(u0, u1), UL = lo(u0, u1);
+        // Negated main products and their (positive) FP32 tails.
+        const float2 NP0 = __fmul2_rn(bc(-c.c0h), UH);
+        float2 R0 = __ffma2_rn(bc(c.c0h), UH, NP0);
+        R0 = __ffma2_rn(bc(c.c0l), UH, R0);
+        R0 = __ffma2_rn(bc(c.c0h), UL, R0);
+        R0 = __ffma2_rn(bc(c.c0ll), UH, R0);
+        const float2 NPX = __fmul2_rn(bc(-c.cxh), SX);
+        float2 RX = __ffma2_rn(bc(c.cxh), SX, NPX);
+        RX = __ffma2_rn(bc(c.cxl), SX, RX);
+        RX = __ffma2_rn(bc(c.cxh), TX, RX);
+        RX = __ffma2_rn(bc(c.cxll), SX, RX);
+        const float2 NPY = __fmul2_rn(bc(-c.cyh), SY);
+        float2 RY = __ffma2_rn(bc(c.cyh), SY, NPY);
+        RY = __ffma2_rn(bc(c.cyl), SY, RY);
+        RY = __ffma2_rn(bc(c.cyh), TY, RY);
+        RY = __ffma2_rn(bc(c.cyll), SY, RY);
+        const float2 NPZ = __fmul2_rn(bc(-c.czh), SZ);
+        float2 RZ = __ffma2_rn(bc(c.czh), SZ, NPZ);
+        RZ = __ffma2_rn(bc(c.czl), SZ, RZ);
+        RZ = __ffma2_rn(bc(c.czh), TZ, RZ);
+        RZ = __ffma2_rn(bc(c.czll), SZ, RZ);
+        // Exact sum of the negated products.
+        float2 a1, a2, a3;
+        const float2 H1 = tsum(NP0, NPX, a1);
+        const float2 H2 = tsum(H1, NPY, a2);
+        float2 NH = tsum(H2, NPZ, a3);
+        // Negated tail: -(((r0 + rx) + (ry + rz)) + ((a1 + a2) + a3)).
+        const float2 rt = __fadd2_rn(__fadd2_rn(R0, RX), __fadd2_rn(RY, RZ));
+        float2 NR = sub(__fadd2_rn(__fadd2_rn(a1, a2), a3), rt);
+        if (HAS_F) {
+            const float2 FH = hi(f0, f1), FL = lo(f0, f1);
+            const float2 NPF = __fmul2_rn(bc(-c.cfh), FH);
+            float2 RF = __ffma2_rn(bc(c.cfh), FH, NPF);
+            RF = __ffma2_rn(bc(c.cfl), FH, RF);
+            RF = __ffma2_rn(bc(c.cfh), FL, RF);
+            RF = __ffma2_rn(bc(c.cfll), FH, RF);
+            float2 a4;
+            NH = tsum(NH, NPF, a4);
+            NR = sub(NR, sub(RF, a4));
+        }
+        // FastTwoSum of the negated pair, then negate back.
+        const float2 S = __fadd2_rn(NH, NR);
+        const float2 E = sub(NR, sub(S, NH));
+        o0 = make_float2(-S.x, -E.x);
+        o1 = make_float2(-S.y, -E.y);
+    }
+
+    template <bool HAS_F, int R>
+    static __device__ __forceinline__ void star_rows(const Star7Coeffs& c, const T (&below)[R], const T (&cur)[R],
+                                                     const T (&above)[R], T ym, T yp, const T (&w)[R],
+                                                     const T (&e)[R], const T (&f)[R], T (&v)[R]) {
+#pragma unroll
+        for (int k = 0; k + 1 < R; k += 2) {
+            const T s0 = k == 0 ? ym : cur[k - 1];
+            const T n1 = k + 1 == R - 1 ? yp : cur[k + 2];
+            star2<HAS_F>(c, cur[k], cur[k + 1], w[k], w[k + 1], e[k], e[k + 1], s0, cur[k], cur[k + 1], n1,
+                         below[k], below[k + 1], above[k], above[k + 1], f[k], f[k + 1], v[k], v[k + 1]);
+        }
+        if (R % 2 == 1) {
+            const int k = R - 1;
+            v[k] = star<HAS_F>(c, cur[k], w[k], e[k], k == 0 ? ym : cur[k - 1], yp, below[k], above[k], f[k]);
+        }
+    }
+
     static __device__ __forceinline__ T mirror(T u, T uo, const Split& corr) {
         // (u + uo) - corr with corr a power of two (exact in FP32).
         f2 s = two_sum(u.x, uo.x);

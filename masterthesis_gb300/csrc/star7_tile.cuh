@@ -170,26 +170,33 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
         auto rows = [&](auto all_inner) {
             constexpr bool INNER = decltype(all_inner)::value;
             const long long o0 = (long long)z * L.plane + (long long)yb * L.pitch + x;
+            T w[R], e[R], f[R], v[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const long long off = o0 + (long long)k * L.pitch;
+                const bool live = INNER || (xin && yb + k < L.ny);
+                w[k] = pl[(rb + k) * G::W - 1];
+                e[k] = pl[(rb + k) * G::W + 1];
+                f[k] = P::zero();
+                if (HAS_F && live) f[k] = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
+            }
+            P::template star_rows<HAS_F, R>(c, below, cur, above, ym, yp, w, e, f, v);
 #pragma unroll
             for (int k = 0; k < R; ++k) {
                 const long long off = o0 + (long long)k * L.pitch;
                 const int y = yb + k;
                 const bool live = INNER || (xin && y < L.ny);
-                const T s = (k == 0) ? ym : cur[k - 1];
-                const T n = (k == R - 1) ? yp : cur[k + 1];
-                const T w = pl[(rb + k) * G::W - 1];
-                const T e = pl[(rb + k) * G::W + 1];
-                T f = P::zero();
-                if (HAS_F && live) f = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
-                T v = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
                 if (!INNER && live && (xb || y == 0 || y == L.ny - 1)) {
+                    const T s = (k == 0) ? ym : cur[k - 1];
+                    const T n = (k == R - 1) ? yp : cur[k + 1];
                     if (BORDER == SCAFES_BORDER_TABLE) {
                         const int mask = (x == 0) | ((x == L.nx - 1) << 1) | ((y == 0) << 2) |
                                          ((y == L.ny - 1) << 3);
-                        v = table_rule<P, HAS_F, has_fb>(J, mask, off, cur[k], w, e, s, n, below[k], above[k]);
+                        v[k] = table_rule<P, HAS_F, has_fb>(J, mask, off, cur[k], w[k], e[k], s, n, below[k],
+                                                            above[k]);
                     } else if (BORDER == SCAFES_BORDER_DIRICHLET) {
-                        v = J.ga ? J.ga[off] : J.gval;
-                        if (has_gb) v = P::src(v, J.gb[off], J.time_new, true);
+                        v[k] = J.ga ? J.ga[off] : J.gval;
+                        if (has_gb) v[k] = P::src(v[k], J.gb[off], J.time_new, true);
                     } else {
                         // Mirror rule of an x or y face (see the z-border
                         // path below for the face order).
@@ -197,12 +204,12 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                         bool minus;
                         if (y == L.ny - 1)      { opp = s; minus = true; }
                         else if (y == 0)        { opp = n; minus = false; }
-                        else if (x == L.nx - 1) { opp = w; minus = true; }
-                        else                    { opp = e; minus = false; }
-                        v = P::mirror(cur[k], opp, minus ? negated(J.corr) : J.corr);
+                        else if (x == L.nx - 1) { opp = w[k]; minus = true; }
+                        else                    { opp = e[k]; minus = false; }
+                        v[k] = P::mirror(cur[k], opp, minus ? negated(J.corr) : J.corr);
                     }
                 }
-                if (live) J.un[off] = v;
+                if (live) J.un[off] = v[k];
             }
         };
         if (ok && !zb) {
