@@ -334,6 +334,28 @@ int scafes_mf_last_ms(const scafes_mf* h, float* ms);
 const char* scafes_mf_last_error(const scafes_mf* h);
 void scafes_mf_destroy(scafes_mf* h);
 
+/* ---- wider stencils, one width per field -----------------------------------
+ *
+ * The averaging update of the reference's per-field stencil-width test,
+ * tests/system/HeatEqnFdmStencilWidthVar/HeatEqnFdmStencilWidthVar.hpp:
+ * 120-165 (widths per data field as in src/ScaFES_Problem.hpp:1495-1514):
+ * every node, inner or border, takes
+ *   u' = 2 + (sum of the values within `width` nodes along each axis,
+ *             truncated at the grid's faces, + u - cc) / count,
+ * cc = the sum of the signed offsets added, count = 1 + values added,
+ * evaluated in the reference's order (bit-exact). */
+#define SCAFES_WIDE_MAX_WIDTH 8
+typedef struct scafes_wide scafes_wide;
+int scafes_wide_create(const int n_nodes[3], int n_fields, const int* widths,
+                       void* stream, scafes_wide** out);
+int scafes_wide_upload(scafes_wide* h, int field, const double* host, size_t n);
+/* n_steps updates of every field (one launch per field per step). */
+int scafes_wide_step(scafes_wide* h, int n_steps);
+int scafes_wide_download(scafes_wide* h, int field, double* host, size_t n);
+int scafes_wide_last_ms(const scafes_wide* h, float* ms);
+const char* scafes_wide_last_error(const scafes_wide* h);
+void scafes_wide_destroy(scafes_wide* h);
+
 /* ---- adjoint (gradients) -------------------------------------------------
  *
  * Replaces the reference's ADOL-C gradient path (src/ScaFES_Problem.hpp:

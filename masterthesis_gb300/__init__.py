@@ -410,6 +410,71 @@ class Adjoint:
             pass
 
 
+class Wide:
+    """Fields with their own stencil width under the averaging update of the
+    reference's StencilWidthVar test (owns a scafes_wide)."""
+
+    def __init__(self, n, widths, stream=None):
+        L = lib()
+        if not getattr(L, "_wide_set", False):
+            vp, dp = C.c_void_p, C.POINTER(C.c_double)
+            L.scafes_wide_create.argtypes = [C.c_int * 3, C.c_int, C.POINTER(C.c_int), vp, C.POINTER(vp)]
+            L.scafes_wide_upload.argtypes = [vp, C.c_int, dp, C.c_size_t]
+            L.scafes_wide_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
+            L.scafes_wide_step.argtypes = [vp, C.c_int]
+            L.scafes_wide_last_ms.argtypes = [vp, C.POINTER(C.c_float)]
+            L.scafes_wide_last_error.argtypes = [vp]
+            L.scafes_wide_last_error.restype = C.c_char_p
+            L.scafes_wide_destroy.argtypes = [vp]
+            L.scafes_wide_destroy.restype = None
+            L._wide_set = True
+        self.shape = (n[2], n[1], n[0])
+        w = (C.c_int * len(widths))(*widths)
+        h = C.c_void_p()
+        rc = L.scafes_wide_create((C.c_int * 3)(*n), len(widths), w, stream, C.byref(h))
+        if rc != 0:
+            raise ScafesError(rc, (L.scafes_last_error() or b"").decode())
+        self.h = h
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise ScafesError(rc, (lib().scafes_wide_last_error(self.h) or b"").decode())
+
+    def upload(self, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self._chk(lib().scafes_wide_upload(self.h, field, _dp(a), a.size))
+
+    def download(self, field):
+        a = np.empty(self.shape)
+        self._chk(lib().scafes_wide_download(self.h, field, _dp(a), a.size))
+        return a
+
+    def step(self, n_steps):
+        self._chk(lib().scafes_wide_step(self.h, n_steps))
+
+    def last_ms(self):
+        v = C.c_float()
+        self._chk(lib().scafes_wide_last_ms(self.h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.h:
+            lib().scafes_wide_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 MF_LAME, MF_YEE = 0, 1
 
 
