@@ -41,6 +41,7 @@ extern "C" {
 #define SCAFES_ERR_UNSUPPORTED (-4) /* configuration no kernel covers      */
 #define SCAFES_ERR_NOMEM (-5)       /* device or host allocation failed    */
 #define SCAFES_ERR_TIMEOUT (-6)     /* a bounded device wait ran out       */
+#define SCAFES_ERR_IO (-7)          /* a file could not be read or written */
 
 /* ---- arithmetic / storage of the unknown field ------------------------- */
 enum scafes_precision {
@@ -174,6 +175,33 @@ int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out);
  * the host).  Known-field slots not uploaded read as 0. */
 int scafes_gpu_upload(scafes_handle* h, int field, const double* host,
                       size_t n);
+
+/* ---- snapshots (replaces the NetCDF writer of writeDfsToFile,
+ * src/ScaFES_Problem.hpp:4254-4340, and the init-file read of :4427) ------
+ *
+ * scafes_gpu_step_snapshots runs n_steps like scafes_gpu_step and writes
+ * the iterate to `path` (created or truncated) at the current step if
+ * flags has SCAFES_SNAP_START, after every step t with t % interval == 0
+ * (interval > 0; the reference's nTimesteps/nSnapshots rule for
+ * LIKE_GIVEN_AT_CL), and after the last step if flags has SCAFES_SNAP_END.
+ * Each snapshot is copied into a device buffer, then to pinned host memory
+ * on a second stream, and written while the next steps run.  The device and
+ * pinned buffers are allocated on the first call and kept by the handle.
+ * Synchronises the handle's stream before it returns.
+ *
+ * File: a 32-byte header (8 bytes "SCAFESS1", int32 version 1, int32
+ * n_nodes[3], 8 reserved bytes), then per snapshot an int64 step, an FP64
+ * time and nx*ny*nz FP64 values, x fastest (little-endian). */
+#define SCAFES_SNAP_START 1
+#define SCAFES_SNAP_END 2
+int scafes_gpu_step_snapshots(scafes_handle* h, int n_steps, int interval,
+                              int flags, const char* path);
+/* Grid size and number of snapshots in a snapshot file (host only). */
+int scafes_snapshot_info(const char* path, int n_nodes[3], int* count);
+/* Snapshot `index` of a file into a dense host array (n = nx*ny*nz), with
+ * its step and time; usable as the initial iterate of scafes_gpu_upload. */
+int scafes_snapshot_read(const char* path, int index, double* host, size_t n,
+                         long long* step, double* time);
 
 /* Sets the border rules of a SCAFES_BORDER_TABLE problem (64 entries,
  * indexed by class mask).  A rule with cf != 0 needs a source field; one

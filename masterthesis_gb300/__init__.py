@@ -80,6 +80,10 @@ def lib() -> C.CDLL:
         L.scafes_border_forms_flux.argtypes = [C.POINTER(Cfg), C.c_int, C.c_double, C.c_double,
                                                C.POINTER(BorderForm)]
         L.scafes_gpu_set_border_forms.argtypes = [vp, C.POINTER(BorderForm)]
+        L.scafes_gpu_step_snapshots.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_char_p]
+        L.scafes_snapshot_info.argtypes = [C.c_char_p, C.c_int * 3, C.POINTER(C.c_int)]
+        L.scafes_snapshot_read.argtypes = [C.c_char_p, C.c_int, dp, C.c_size_t, C.POINTER(C.c_longlong),
+                                           C.POINTER(C.c_double)]
         L.scafes_gpu_upload.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_step.argtypes = [vp, C.c_int]
@@ -149,6 +153,25 @@ def make_cfg(n, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), tau=0.0, t_start=0.
     return c
 
 
+SNAP_START, SNAP_END = 1, 2
+
+
+def snapshot_info(path):
+    """(n_nodes, count) of a snapshot file written by Plain.step_snapshots."""
+    n, cnt = (C.c_int * 3)(), C.c_int()
+    _check(lib().scafes_snapshot_info(str(path).encode(), n, C.byref(cnt)))
+    return tuple(n), cnt.value
+
+
+def snapshot_read(path, index):
+    """(field (nz, ny, nx), step, time) of snapshot `index`."""
+    n, _ = snapshot_info(path)
+    a = np.empty((n[2], n[1], n[0]))
+    st, tm = C.c_longlong(), C.c_double()
+    _check(lib().scafes_snapshot_read(str(path).encode(), index, _dp(a), a.size, C.byref(st), C.byref(tm)))
+    return a, st.value, tm.value
+
+
 def border_forms_flux(cfg: Cfg, kind: int, lam: float = 1.0, alpha: float = 1.0):
     """The 64 border rules of the reference's Neumann / Cauchy system tests
     for cfg (scafes_border_forms_flux)."""
@@ -170,6 +193,9 @@ class Plain:
     @property
     def shape(self):
         return (self.n[2], self.n[1], self.n[0])
+
+    def step_snapshots(self, n_steps: int, interval: int, path, flags: int = SNAP_START | SNAP_END):
+        _check(lib().scafes_gpu_step_snapshots(self.h, n_steps, interval, flags, str(path).encode()), self.h)
 
     def set_border_forms(self, forms):
         _check(lib().scafes_gpu_set_border_forms(self.h, forms), self.h)

@@ -6,6 +6,7 @@
 // buffers of the unknown field (the old/new pair swapped by
 // swapPointersOfUnknownDfs, :3273-3316) plus the known fields.
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -64,6 +65,12 @@ struct scafes_handle {
     // any rule reads the source field.
     scafes_border_form* table = nullptr;
     bool table_needs_f = false;
+    // Snapshot writer (allocated on first use): a dense FP64 copy of the
+    // iterate on the device, two pinned host buffers, a copy stream.
+    double* snap_dev = nullptr;
+    double* snap_host[2] = {nullptr, nullptr};
+    cudaStream_t snap_stream = nullptr;
+    cudaEvent_t snap_conv = nullptr, snap_copied[2] = {nullptr, nullptr};
     std::string err;
 };
 
@@ -135,6 +142,13 @@ extern "C" void scafes_gpu_destroy(scafes_handle* h) {
     for (int i = 0; i < SCAFES_FIELD_COUNT; ++i) cudaFree(h->fld[i]);
     cudaFree(h->stage);
     cudaFree(h->table);
+    cudaFree(h->snap_dev);
+    for (int i = 0; i < 2; ++i) {
+        if (h->snap_host[i]) cudaFreeHost(h->snap_host[i]);
+        if (h->snap_copied[i]) cudaEventDestroy(h->snap_copied[i]);
+    }
+    if (h->snap_conv) cudaEventDestroy(h->snap_conv);
+    if (h->snap_stream) cudaStreamDestroy(h->snap_stream);
     cudaFree(h->red);
     if (h->red_host) cudaFreeHost(h->red_host);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -474,6 +488,165 @@ extern "C" int scafes_gpu_step(scafes_handle* h, int n_steps) {
     if (!h->uploaded)
         return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_step: upload the unknown field first");
     return step_impl(h, n_steps, h->tile, true);
+}
+
+// ---- snapshots ----------------------------------------------------------------
+
+namespace {
+
+const char kSnapMagic[8] = {'S', 'C', 'A', 'F', 'E', 'S', 'S', '1'};
+
+struct SnapHeader {
+    char magic[8];
+    int32_t version;
+    int32_t n[3];
+    int32_t reserved[2];
+};
+
+struct SnapRecord {
+    int64_t step;
+    double time;
+};
+
+int snap_setup(scafes_handle* h) {
+    if (h->snap_dev) return SCAFES_OK;
+    const size_t bytes = n_nodes(h) * sizeof(double);
+    CUDA_TRY(h, cudaMalloc(&h->snap_dev, bytes));
+    for (int i = 0; i < 2; ++i) {
+        CUDA_TRY(h, cudaMallocHost(&h->snap_host[i], bytes));
+        CUDA_TRY(h, cudaEventCreateWithFlags(&h->snap_copied[i], cudaEventDisableTiming));
+    }
+    CUDA_TRY(h, cudaEventCreateWithFlags(&h->snap_conv, cudaEventDisableTiming));
+    CUDA_TRY(h, cudaStreamCreateWithFlags(&h->snap_stream, cudaStreamNonBlocking));
+    return SCAFES_OK;
+}
+
+// Enqueues the copy of the current iterate into pinned buffer b: dense FP64
+// on the device (on the compute stream, after the previous copy out of the
+// device buffer finished), then device -> host on the copy stream.
+int snap_enqueue(scafes_handle* h, int b, int prev) {
+    const Layout& L = h->L;
+    if (prev >= 0) CUDA_TRY(h, cudaStreamWaitEvent(h->stream, h->snap_copied[prev], 0));
+    if (h->cfg.precision == SCAFES_PREC_F64)
+        CUDA_TRY(h, cudaMemcpy2DAsync(h->snap_dev, (size_t)L.nx * sizeof(double), h->u[h->cur],
+                                      (size_t)L.pitch * sizeof(double), (size_t)L.nx * sizeof(double),
+                                      (size_t)L.ny * L.nz, cudaMemcpyDeviceToDevice, h->stream));
+    else
+        CUDA_TRY(h, convert_from_device(h->cfg.precision, h->u[h->cur], h->snap_dev, L, h->stream));
+    CUDA_TRY(h, cudaEventRecord(h->snap_conv, h->stream));
+    CUDA_TRY(h, cudaStreamWaitEvent(h->snap_stream, h->snap_conv, 0));
+    CUDA_TRY(h, cudaMemcpyAsync(h->snap_host[b], h->snap_dev, n_nodes(h) * sizeof(double), cudaMemcpyDeviceToHost,
+                                h->snap_stream));
+    CUDA_TRY(h, cudaEventRecord(h->snap_copied[b], h->snap_stream));
+    return SCAFES_OK;
+}
+
+// Waits for pinned buffer b and appends it to the file.
+int snap_write(scafes_handle* h, FILE* f, int b, long long step) {
+    CUDA_TRY(h, cudaEventSynchronize(h->snap_copied[b]));
+    SnapRecord r{(int64_t)step, h->cfg.t_start + step * h->cfg.tau};
+    const size_t n = n_nodes(h);
+    if (std::fwrite(&r, sizeof(r), 1, f) != 1 || std::fwrite(h->snap_host[b], sizeof(double), n, f) != n)
+        return fail(&h->err, SCAFES_ERR_IO, "scafes_gpu_step_snapshots: writing the snapshot of step %lld failed",
+                    step);
+    return SCAFES_OK;
+}
+
+}  // namespace
+
+extern "C" int scafes_gpu_step_snapshots(scafes_handle* h, int n_steps, int interval, int flags, const char* path) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_step_snapshots: handle is NULL");
+    if (n_steps < 0 || interval < 0 || !path)
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_step_snapshots: bad arguments");
+    if (!h->uploaded)
+        return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_step_snapshots: upload the unknown field first");
+    int rc = snap_setup(h);
+    if (rc) return rc;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(&h->err, SCAFES_ERR_IO, "scafes_gpu_step_snapshots: cannot open %s for writing", path);
+    SnapHeader hd{};
+    std::memcpy(hd.magic, kSnapMagic, sizeof(kSnapMagic));
+    hd.version = 1;
+    hd.n[0] = h->L.nx; hd.n[1] = h->L.ny; hd.n[2] = h->L.nz;
+    if (std::fwrite(&hd, sizeof(hd), 1, f) != 1) {
+        std::fclose(f);
+        return fail(&h->err, SCAFES_ERR_IO, "scafes_gpu_step_snapshots: cannot write %s", path);
+    }
+    // Snapshot points: the current step (START), every step t with
+    // t % interval == 0 (the reference's nTimesteps/nSnapshots rule), the
+    // last step (END).  A snapshot is written while the next steps run.
+    const long long t0 = h->t, t1 = h->t + (long long)n_steps;
+    int pending = -1, b = 0;
+    long long pending_step = 0, done = t0;
+    CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
+    auto snap = [&](long long t) -> int {
+        int r = snap_enqueue(h, b, pending);
+        if (r == SCAFES_OK && pending >= 0) r = snap_write(h, f, pending, pending_step);
+        pending = b;
+        pending_step = t;
+        b ^= 1;
+        return r;
+    };
+    if (flags & SCAFES_SNAP_START) rc = snap(t0);
+    for (long long t = t0 + 1; t <= t1 && rc == SCAFES_OK; ++t) {
+        const bool at = (interval > 0 && t % interval == 0) || (t == t1 && (flags & SCAFES_SNAP_END));
+        if (!at) continue;
+        rc = step_impl(h, (int)(t - done), h->tile, false);
+        done = t;
+        if (rc == SCAFES_OK) rc = snap(t);
+    }
+    if (rc == SCAFES_OK && done < t1) rc = step_impl(h, (int)(t1 - done), h->tile, false);
+    if (rc == SCAFES_OK) {
+        cudaError_t e = cudaEventRecord(h->ev1, h->stream);
+        if (e != cudaSuccess) rc = fail(&h->err, SCAFES_ERR_CUDA, "scafes_gpu_step_snapshots: %s", cudaGetErrorString(e));
+    }
+    if (rc == SCAFES_OK && pending >= 0) rc = snap_write(h, f, pending, pending_step);
+    if (std::fclose(f) != 0 && rc == SCAFES_OK)
+        rc = fail(&h->err, SCAFES_ERR_IO, "scafes_gpu_step_snapshots: closing %s failed", path);
+    if (rc) return rc;
+    h->timed = true;
+    h->launches = n_steps;
+    return check_status(h);
+}
+
+extern "C" int scafes_snapshot_info(const char* path, int n_nodes_out[3], int* count) {
+    if (!path || !n_nodes_out || !count) return fail(nullptr, SCAFES_ERR_ARG, "scafes_snapshot_info: NULL argument");
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(nullptr, SCAFES_ERR_IO, "scafes_snapshot_info: cannot open %s", path);
+    SnapHeader hd{};
+    const bool ok = std::fread(&hd, sizeof(hd), 1, f) == 1 && std::memcmp(hd.magic, kSnapMagic, 8) == 0 &&
+                    hd.version == 1 && hd.n[0] > 0 && hd.n[1] > 0 && hd.n[2] > 0;
+    long long size = -1;
+    if (ok && std::fseek(f, 0, SEEK_END) == 0) size = std::ftell(f);
+    std::fclose(f);
+    if (!ok || size < 0) return fail(nullptr, SCAFES_ERR_IO, "scafes_snapshot_info: %s is not a snapshot file", path);
+    const long long rec = (long long)sizeof(SnapRecord) + (long long)hd.n[0] * hd.n[1] * hd.n[2] * 8;
+    for (int p = 0; p < 3; ++p) n_nodes_out[p] = hd.n[p];
+    *count = (int)((size - (long long)sizeof(hd)) / rec);
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_snapshot_read(const char* path, int index, double* host, size_t n, long long* step,
+                                    double* time) {
+    int nn[3], count = 0;
+    int rc = scafes_snapshot_info(path, nn, &count);
+    if (rc) return rc;
+    const size_t total = (size_t)nn[0] * nn[1] * nn[2];
+    if (!host || n != total)
+        return fail(nullptr, SCAFES_ERR_ARG, "scafes_snapshot_read: expected %zu values, got %zu", total, n);
+    if (index < 0 || index >= count)
+        return fail(nullptr, SCAFES_ERR_ARG, "scafes_snapshot_read: index %d out of [0, %d)", index, count);
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(nullptr, SCAFES_ERR_IO, "scafes_snapshot_read: cannot open %s", path);
+    const long long off = (long long)sizeof(SnapHeader) + (long long)index * ((long long)sizeof(SnapRecord) + 8LL * total);
+    SnapRecord r{};
+    const bool ok = std::fseek(f, off, SEEK_SET) == 0 && std::fread(&r, sizeof(r), 1, f) == 1 &&
+                    std::fread(host, sizeof(double), total, f) == total;
+    std::fclose(f);
+    if (!ok) return fail(nullptr, SCAFES_ERR_IO, "scafes_snapshot_read: %s is truncated", path);
+    if (step) *step = r.step;
+    if (time) *time = r.time;
+    return SCAFES_OK;
 }
 
 extern "C" int scafes_gpu_autotune(scafes_handle* h, int n_steps, int* chosen, float* ms_per_tile) {

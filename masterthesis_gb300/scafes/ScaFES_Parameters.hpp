@@ -8,6 +8,8 @@
 //   --gpuPrecision=f64|f32x2|f32   arithmetic of the unknown field (f64)
 //   --gpuTile=0..4                 sweep tile variant, 0 = default
 //   --gpuAutotune=0|1              time the tile variants before running
+//   --gpuSnapshotFile=PATH         where fields with writeToFile != NEVER
+//                                  are written (default scafes_<field>.snap)
 #ifndef SCAFES_GB300_PARAMETERS_HPP
 #define SCAFES_GB300_PARAMETERS_HPP
 
@@ -49,6 +51,8 @@ public:
             else if (key == "gpuPrecision") mGpuPrecision = val;
             else if (key == "gpuTile") mGpuTile = std::atoi(val.c_str());
             else if (key == "gpuAutotune") mGpuAutotune = std::atoi(val.c_str()) != 0;
+            else if (key == "nSnapshots") mNsnapshots = std::atoi(val.c_str());
+            else if (key == "gpuSnapshotFile") mGpuSnapshotFile = val;
         }
         mNnodes.resize(mDim, mNnodes.empty() ? 32 : mNnodes.back());
         mCoordNodeFirst.resize(mDim, 0.0);
@@ -73,6 +77,8 @@ public:
     const std::string& gpuPrecision() const { return mGpuPrecision; }
     const int& gpuTile() const { return mGpuTile; }
     bool gpuAutotune() const { return mGpuAutotune; }
+    const int& nSnapshots() const { return mNsnapshots; }
+    const std::string& gpuSnapshotFile() const { return mGpuSnapshotFile; }
     // The reference's single-rank answers.
     int rank() const { return 0; }
     int rankOutput() const { return 0; }
@@ -91,6 +97,8 @@ public:
     void setGpuPrecision(const std::string& p) { mGpuPrecision = p; }
     void setGpuTile(int t) { mGpuTile = t; }
     void setGpuAutotune(bool a) { mGpuAutotune = a; }
+    void setNsnapshots(int n) { mNsnapshots = n; }
+    void setGpuSnapshotFile(const std::string& f) { mGpuSnapshotFile = f; }
 
 private:
     template <typename T>
@@ -118,6 +126,8 @@ private:
     std::string mGpuPrecision = "f64";
     int mGpuTile = 0;
     bool mGpuAutotune = false;
+    int mNsnapshots = 1;  // the reference's default (src/ScaFES_Parameters.hpp:446)
+    std::string mGpuSnapshotFile;
 };
 
 }  // namespace ScaFES

@@ -67,8 +67,8 @@ public:
             const std::vector<bool>& checkConvergence = std::vector<bool>())
         : mParams(params), mGG(gg), mUseLeapfrog(useLeapfrog), mNames(nameDatafield),
           mStencilWidth(stencilWidth), mIsKnown(isKnownDf), mComputeError(computeError),
-          mVectParamsCurr(geomparamsInit) {
-        (void)nLayers; (void)defaultValue; (void)writeToFile; (void)checkConvergence;
+          mVectParamsCurr(geomparamsInit), mWriteToFile(writeToFile) {
+        (void)nLayers; (void)defaultValue; (void)checkConvergence;
         // Argument checks of the reference constructor (:1400-1423).
         const std::size_t nf = nameDatafield.size();
         if (nf == 0 || stencilWidth.size() != nf || isKnownDf.size() != nf)
@@ -351,6 +351,8 @@ private:
     scafes_cfg mCfg = {};
     std::vector<double> mFa, mFb, mGa, mGb;
     scafes_border_form mForms[SCAFES_BORDER_CLASSES] = {};
+    std::vector<ScaFES::WriteHowOften> mWriteToFile;
+    std::string mSnapshotFile;
     scafes_handle* mHandle = nullptr;
     std::map<int, double> mErrLinf;
     double mGpuMs = 0.0;
@@ -601,7 +603,32 @@ void Problem<OWNPRBLM, CT, DIM>::iterateOverTime() {
     int tile = cfg.tile;
     if (mParams.gpuAutotune()) check(scafes_gpu_autotune(mHandle, 5, &tile, nullptr));
     auto t_upd = clock::now();
-    check(scafes_gpu_step(mHandle, T));
+    // Field output (writeDfsToFile, reference :4254-4340): the unknown field's
+    // WriteHowOften maps to the snapshot writer, which copies and writes
+    // while the sweeps run.
+    const int uw = mUnknownIdx[0];
+    const WriteHowOften how = (std::size_t)uw < mWriteToFile.size() ? mWriteToFile[uw] : WriteHowOften::NEVER;
+    if (how == WriteHowOften::NEVER) {
+        check(scafes_gpu_step(mHandle, T));
+    } else {
+        int interval = 0, flags = 0;
+        switch (how) {
+            case WriteHowOften::AT_START: flags = SCAFES_SNAP_START; break;
+            case WriteHowOften::AT_END: flags = SCAFES_SNAP_END; break;
+            case WriteHowOften::AT_START_AND_END: flags = SCAFES_SNAP_START | SCAFES_SNAP_END; break;
+            case WriteHowOften::LIKE_GIVEN_AT_CL:
+                interval = T;
+                if (mParams.nSnapshots() > 0 && mParams.nSnapshots() <= T) interval = T / mParams.nSnapshots();
+                flags = SCAFES_SNAP_START;
+                break;
+            default: interval = 1; flags = SCAFES_SNAP_START; break;  // ALWAYS
+        }
+        if (interval < 1) interval = 1;
+        const std::string path = mParams.gpuSnapshotFile().empty() ? "scafes_" + mNames[uw] + ".snap"
+                                                                   : mParams.gpuSnapshotFile();
+        check(scafes_gpu_step_snapshots(mHandle, T, interval, flags, path.c_str()));
+        mSnapshotFile = path;
+    }
     std::vector<double> uT((std::size_t)mN);
     check(scafes_gpu_download(mHandle, SCAFES_FIELD_U, uT.data(), uT.size()));
     mWallClockTimes["update"] += std::chrono::duration<double>(clock::now() - t_upd).count();

@@ -32,12 +32,16 @@ int run(P& ppp, const std::string& out, bool extract) {
 int main(int argc, char** argv) {
     if (argc < 3) return 2;
     const std::string which = argv[1], out = argv[2];
-    bool extract = false;
-    for (int i = 3; i < argc; ++i) if (!std::strcmp(argv[i], "--extract-only")) extract = true;
+    bool extract = false, write_cl = false;
+    for (int i = 3; i < argc; ++i) {
+        if (!std::strcmp(argv[i], "--extract-only")) extract = true;
+        if (!std::strcmp(argv[i], "--write-like-cl")) write_cl = true;  // U written per --nSnapshots
+    }
     try {
         ScaFES::Parameters params(argc, argv);
         ScaFES::GridGlobal<3> gg(params);
         std::vector<ScaFES::WriteHowOften> wr(3, ScaFES::WriteHowOften::NEVER);
+        if (write_cl) wr[2] = ScaFES::WriteHowOften::LIKE_GIVEN_AT_CL;
         if (which == "mirror_pow2") {
             MirrorPow2<double, 3> p(params, gg, false, {"A"}, {1}, {false}, {0}, {0.0},
                                     std::vector<ScaFES::WriteHowOften>(1, ScaFES::WriteHowOften::NEVER), {true});

@@ -71,3 +71,21 @@ def test_dropin_flux_border_matches_reference(run_problem, tmp_path, name, golde
     u, out = run(run_problem, name, tmp_path / "u.bin", n, f"--nNodes={n[0]}x{n[1]}x{n[2]}",
                  f"--nTimesteps={int(d['nsteps'])}", f"--endtime={float(d['t_end'])!r}", f"--gpuPrecision={prec}")
     assert cases.rel_err(u, d["final"]) <= 1e-12
+
+
+def test_dropin_writes_snapshots_like_given_at_cl(gpu, run_problem, tmp_path):
+    """writeToFile = LIKE_GIVEN_AT_CL with --nSnapshots=3 over 300 steps
+    writes the unknown field at steps 0, 100, 200 and 300 (the reference's
+    nTimesteps/nSnapshots rule); the last one is the final iterate."""
+    M = gpu
+    d = load_golden("heat_timelin")
+    n = tuple(int(v) for v in d["n"])
+    snap = tmp_path / "u.snap"
+    u, _ = run(run_problem, "heat_lin", tmp_path / "u.bin", n, f"--nNodes={n[0]}x{n[1]}x{n[2]}",
+               f"--nTimesteps={int(d['nsteps'])}", f"--endtime={float(d['t_end'])!r}", "--nSnapshots=3",
+               f"--gpuSnapshotFile={snap}", "--write-like-cl")
+    assert M.snapshot_info(snap) == (n, 4)
+    steps = [M.snapshot_read(snap, k)[1] for k in range(4)]
+    assert steps == [0, 100, 200, 300]
+    assert np.array_equal(M.snapshot_read(snap, 3)[0], u)
+    assert cases.rel_err(u, d["final"]) <= 1e-12
