@@ -47,18 +47,18 @@ struct BatchItem {
     short z0, z1;  // planes [z0, z1)
 };
 
-template <class P, int BY, int R>
+template <class P, int BY, int R, int NS>
 __global__ void __launch_bounds__(BX * (BY / R))
 batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ maps, int map_stride,
             const BatchItem* __restrict__ items, int n_items, typename P::T* __restrict__ pool, int cur,
             int* __restrict__ counter, int* __restrict__ status) {
     using T = typename P::T;
-    using G = Tile<T, BY>;
+    using G = Tile<T, BY, NS>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* st = reinterpret_cast<T*>(smem_raw);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NSTAGE * G::STRIDE * G::ESZ);
-    int& s_item = *reinterpret_cast<int*>(bar + NSTAGE);  // after the ring (see smem_bytes)
-    ring_init<T, BY>(bar);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NS * G::STRIDE * G::ESZ);
+    int& s_item = *reinterpret_cast<int*>(bar + NS);  // after the ring (see smem_bytes)
+    ring_init<NS>(bar);
     const int tid = threadIdx.y * BX + threadIdx.x;
     uint32_t base = 0;
     for (;;) {
@@ -83,15 +83,15 @@ batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ 
         J.L = I.L;
         J.time_old = J.time_new = J.corr = Split{0.0, 0.f, 0.f};
         J.table = nullptr;
-        if (!star7_tile<P, SRC_A, SCAFES_BORDER_DIRICHLET, BY, R>(J, c, w.tx * BX, w.ty * BY, w.z0, w.z1, st, bar,
+        if (!star7_tile<P, SRC_A, SCAFES_BORDER_DIRICHLET, BY, R, NS>(J, c, w.tx * BX, w.ty * BY, w.z0, w.z1, st, bar,
                                                                  base, status))
             break;
     }
 }
 
 // The tile ring plus one int for the work-item broadcast.
-template <class T, int BY>
-size_t smem_bytes() { return Tile<T, BY>::SMEM + 16; }
+template <class T, int BY, int NS>
+size_t smem_bytes() { return Tile<T, BY, NS>::SMEM + 16; }
 
 }  // namespace
 
@@ -170,10 +170,10 @@ template <class P>
 KernelInfo kinfo_prec(int tile) {
     using T = typename P::T;
     switch (tile) {
-        case 0: return {(const void*)batch_star7<P, kTiles[0].by, kTiles[0].r>, dim3(BX, kTiles[0].by / kTiles[0].r), smem_bytes<T, kTiles[0].by>()};
-        case 1: return {(const void*)batch_star7<P, kTiles[1].by, kTiles[1].r>, dim3(BX, kTiles[1].by / kTiles[1].r), smem_bytes<T, kTiles[1].by>()};
-        case 2: return {(const void*)batch_star7<P, kTiles[2].by, kTiles[2].r>, dim3(BX, kTiles[2].by / kTiles[2].r), smem_bytes<T, kTiles[2].by>()};
-        default: return {(const void*)batch_star7<P, kTiles[3].by, kTiles[3].r>, dim3(BX, kTiles[3].by / kTiles[3].r), smem_bytes<T, kTiles[3].by>()};
+        case 0: return {(const void*)batch_star7<P, kTiles[0].by, kTiles[0].r, kTiles[0].ns>, dim3(BX, kTiles[0].by / kTiles[0].r), smem_bytes<T, kTiles[0].by, kTiles[0].ns>()};
+        case 1: return {(const void*)batch_star7<P, kTiles[1].by, kTiles[1].r, kTiles[1].ns>, dim3(BX, kTiles[1].by / kTiles[1].r), smem_bytes<T, kTiles[1].by, kTiles[1].ns>()};
+        case 2: return {(const void*)batch_star7<P, kTiles[2].by, kTiles[2].r, kTiles[2].ns>, dim3(BX, kTiles[2].by / kTiles[2].r), smem_bytes<T, kTiles[2].by, kTiles[2].ns>()};
+        default: return {(const void*)batch_star7<P, kTiles[3].by, kTiles[3].r, kTiles[3].ns>, dim3(BX, kTiles[3].by / kTiles[3].r), smem_bytes<T, kTiles[3].by, kTiles[3].ns>()};
     }
 }
 

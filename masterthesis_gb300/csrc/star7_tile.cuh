@@ -4,7 +4,7 @@
 // (a persistent CTA works through many tiles of many instances).
 //
 // Mapping: one elected thread streams the tile's planes (with a one-node
-// halo in x and y, x padded to 16 bytes) into an NSTAGE-deep ring of
+// halo in x and y, x padded to 16 bytes) into an NS-deep ring of
 // stages with 3D TMA loads, each stage completing on its own mbarrier.
 // Each thread owns R consecutive rows of one column and keeps u(z-1),
 // u(z), u(z+1) of them in registers (the z-marching queue); y-neighbours
@@ -22,9 +22,9 @@
 namespace scafes {
 
 constexpr int BX = 32;
-constexpr int NSTAGE = 8;  // power of two: stage/phase indices are shifts
-
-template <class T, int BY>
+// NS: stages of the shared-memory ring, a power of two (stage and phase
+// indices are shifts).  Fewer stages leave room for more CTAs per SM.
+template <class T, int BY, int NS>
 struct Tile {
     static constexpr int ESZ = (int)sizeof(T);
     static constexpr int LP = 16 / ESZ;          // left halo padded to 16 bytes
@@ -32,12 +32,13 @@ struct Tile {
     static constexpr int H = BY + 2;             // box height (rows)
     static constexpr uint32_t TX_BYTES = W * H * ESZ;
     static constexpr int STRIDE = ((W * H * ESZ + 127) / 128) * 128 / ESZ;  // elements per stage
-    static constexpr size_t SMEM = (size_t)NSTAGE * STRIDE * ESZ + NSTAGE * sizeof(uint64_t);
+    static constexpr size_t SMEM = (size_t)NS * STRIDE * ESZ + NS * sizeof(uint64_t);
 };
 
-// Tile variants {BY, R}: CTA tile 32 x BY, R rows per thread.
-struct TileShape { int by, r; };
-constexpr TileShape kTiles[STAR7_NUM_TILES] = {{8, 1}, {16, 2}, {32, 4}, {16, 4}};
+// Tile variants {BY, R, NS}: CTA tile 32 x BY, R rows per thread, NS ring
+// stages.
+struct TileShape { int by, r, ns; };
+constexpr TileShape kTiles[STAR7_NUM_TILES] = {{8, 1, 8}, {16, 2, 8}, {32, 4, 8}, {16, 4, 4}};
 
 // Everything one tile needs besides its position.
 template <class T>
@@ -83,10 +84,10 @@ __device__ __noinline__ typename P::T table_rule(const TileJob<typename P::T>& J
 }
 
 // Initialises the ring's mbarriers (thread 0) -- once per CTA.
-template <class T, int BY>
+template <int NS>
 __device__ __forceinline__ void ring_init(uint64_t* bar) {
     if (threadIdx.x == 0 && threadIdx.y == 0) {
-        for (int s = 0; s < NSTAGE; ++s) mbar_init(&bar[s], 1);
+        for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -101,13 +102,13 @@ enum : int { SRC_NONE = 0, SRC_A = 1, SRC_AB = 2 };
 // and phase of every plane); it is advanced by the planes this tile used.
 // Returns false (and records SCAFES_ERR_TIMEOUT) when a stage never
 // arrived; the caller must then stop.
-template <class P, int SRC, int BORDER, int BY, int R>
+template <class P, int SRC, int BORDER, int BY, int R, int NS>
 __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, const Star7Coeffs& c,
                                            int x0, int y0, int z0, int z1,
                                            typename P::T* st, uint64_t* bar, uint32_t& base,
                                            int* status) {
     using T = typename P::T;
-    using G = Tile<T, BY>;
+    using G = Tile<T, BY, NS>;
     constexpr bool HAS_F = SRC != SRC_NONE;
     constexpr bool has_fb = SRC == SRC_AB;
     const Layout& L = J.L;
@@ -120,10 +121,10 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
     const uint32_t b0 = base;
 
     if (tid == 0) {
-        const int pre = np < NSTAGE ? np : NSTAGE;
+        const int pre = np < NS ? np : NS;
         fence_proxy_async_smem();
         for (int p = 0; p < pre; ++p) {
-            const uint32_t s = (b0 + p) & (NSTAGE - 1);
+            const uint32_t s = (b0 + p) & (NS - 1);
             mbar_arrive_expect_tx(&bar[s], G::TX_BYTES);
             tma_load_3d(st + s * G::STRIDE, J.tm, x0 - G::LP, y0 - 1, z0 - 1 + p, &bar[s]);
         }
@@ -135,8 +136,8 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
     // The whole 32 x BY tile holds inner columns: no per-node border tests.
     const bool tile_inner = x0 >= 1 && x0 + BX <= L.nx - 1 && y0 >= 1 && y0 + BY <= L.ny - 1;
     const int cc = G::LP + tx;  // this thread's column inside a stage row
-    auto slot = [&](int p) { return (b0 + (uint32_t)p) & (NSTAGE - 1); };
-    auto phase = [&](int p) { return ((b0 + (uint32_t)p) / NSTAGE) & 1; };
+    auto slot = [&](int p) { return (b0 + (uint32_t)p) & (NS - 1); };
+    auto phase = [&](int p) { return ((b0 + (uint32_t)p) / NS) & 1; };
 
     bool ok = bounded_wait(&bar[slot(0)], phase(0));
     ok = bounded_wait(&bar[slot(1)], phase(1)) && ok;
@@ -258,10 +259,10 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 }
             }
         }
-        // Everyone is done with plane p-1: its stage takes plane p-1+NSTAGE.
+        // Everyone is done with plane p-1: its stage takes plane p-1+NS.
         if (!__syncthreads_and(ok)) return false;
         if (tid == 0) {
-            const int pn = p - 1 + NSTAGE;
+            const int pn = p - 1 + NS;
             if (pn < np) {
                 const uint32_t s = slot(pn);
                 fence_proxy_async_smem();
@@ -284,7 +285,7 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
         if (tid == 0) {
             // A stage never completed: report, drain what was issued, stop.
             atomicExch(status, SCAFES_ERR_TIMEOUT);
-            for (int q = (p > 0 ? p - 1 : 0); q < np && q < p - 1 + NSTAGE; ++q)
+            for (int q = (p > 0 ? p - 1 : 0); q < np && q < p - 1 + NS; ++q)
                 bounded_wait(&bar[slot(q)], phase(q), kWaitLimitNs / 8);
         }
         return false;

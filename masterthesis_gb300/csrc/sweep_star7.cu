@@ -11,7 +11,7 @@
 
 namespace scafes {
 
-template <class P, int SRC, int BORDER, int BY, int R>
+template <class P, int SRC, int BORDER, int BY, int R, int NS>
 __global__ void __launch_bounds__(BX * (BY / R))
 star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un,
           const typename P::T* __restrict__ fa, const typename P::T* __restrict__ fb,
@@ -20,16 +20,16 @@ star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
           Split corr, const scafes_border_form* __restrict__ table, int zchunk, int* __restrict__ status)
 {
     using T = typename P::T;
-    using G = Tile<T, BY>;
+    using G = Tile<T, BY, NS>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* st = reinterpret_cast<T*>(smem_raw);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NSTAGE * G::STRIDE * G::ESZ);
-    ring_init<T, BY>(bar);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NS * G::STRIDE * G::ESZ);
+    ring_init<NS>(bar);
     TileJob<T> J{&tm, un, fa, fb, ga, gb, gval, L, time_old, time_new, corr, table};
     const int z0 = blockIdx.z * zchunk;
     const int z1 = min(z0 + zchunk, L.nz);
     uint32_t base = 0;
-    star7_tile<P, SRC, BORDER, BY, R>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
+    star7_tile<P, SRC, BORDER, BY, R, NS>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
 }
 
 // ---- host side ---------------------------------------------------------------
@@ -94,12 +94,12 @@ static inline void to_elem(double d, float2& out) {
     out = make_float2(p.hi, p.lo);
 }
 
-template <class P, int SRC, int BORDER, int BY, int R>
+template <class P, int SRC, int BORDER, int BY, int R, int NS>
 static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
     using T = typename P::T;
-    using G = Tile<T, BY>;
+    using G = Tile<T, BY, NS>;
     const Layout& L = a.L;
-    auto kern = star7_tma<P, SRC, BORDER, BY, R>;
+    auto kern = star7_tma<P, SRC, BORDER, BY, R, NS>;
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
@@ -124,10 +124,10 @@ static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
 template <class P, int SRC, int BORDER>
 static cudaError_t launch_tile(const Star7Launch& a, cudaStream_t stream) {
     switch (a.tile) {
-        case 0: return launch_typed<P, SRC, BORDER, kTiles[0].by, kTiles[0].r>(a, stream);
-        case 1: return launch_typed<P, SRC, BORDER, kTiles[1].by, kTiles[1].r>(a, stream);
-        case 2: return launch_typed<P, SRC, BORDER, kTiles[2].by, kTiles[2].r>(a, stream);
-        case 3: return launch_typed<P, SRC, BORDER, kTiles[3].by, kTiles[3].r>(a, stream);
+        case 0: return launch_typed<P, SRC, BORDER, kTiles[0].by, kTiles[0].r, kTiles[0].ns>(a, stream);
+        case 1: return launch_typed<P, SRC, BORDER, kTiles[1].by, kTiles[1].r, kTiles[1].ns>(a, stream);
+        case 2: return launch_typed<P, SRC, BORDER, kTiles[2].by, kTiles[2].r, kTiles[2].ns>(a, stream);
+        case 3: return launch_typed<P, SRC, BORDER, kTiles[3].by, kTiles[3].r, kTiles[3].ns>(a, stream);
         default: return cudaErrorInvalidValue;
     }
 }
