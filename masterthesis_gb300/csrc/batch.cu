@@ -47,11 +47,12 @@ struct BatchItem {
     short z0, z1;  // planes [z0, z1)
 };
 
+// The persistent loop: pull work items until the step's queue is empty.
 template <class P, int BY, int R, int NS>
-__global__ void __launch_bounds__(BX * (BY / R))
-batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ maps, int map_stride,
-            const BatchItem* __restrict__ items, int n_items, typename P::T* __restrict__ pool, int cur,
-            int* __restrict__ counter, int* __restrict__ status) {
+__device__ __forceinline__ void batch_loop(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ maps,
+                                           int map_stride, const BatchItem* __restrict__ items, int n_items,
+                                           typename P::T* __restrict__ pool, int cur, int* __restrict__ counter,
+                                           int* __restrict__ status) {
     using T = typename P::T;
     using G = Tile<T, BY, NS>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -84,9 +85,29 @@ batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ 
         J.time_old = J.time_new = J.corr = Split{0.0, 0.f, 0.f};
         J.table = nullptr;
         if (!star7_tile<P, SRC_A, SCAFES_BORDER_DIRICHLET, BY, R, NS>(J, c, w.tx * BX, w.ty * BY, w.z0, w.z1, st, bar,
-                                                                 base, status))
+                                                                     base, status))
             break;
     }
+}
+
+template <class P, int BY, int R, int NS>
+__global__ void __launch_bounds__(BX * (BY / R))
+batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ maps, int map_stride,
+            const BatchItem* __restrict__ items, int n_items, typename P::T* __restrict__ pool, int cur,
+            int* __restrict__ counter, int* __restrict__ status) {
+    batch_loop<P, BY, R, NS>(inst, maps, map_stride, items, n_items, pool, cur, counter, status);
+}
+
+// FP64 variant with a register cap of 64 (1024 threads' worth of CTAs per
+// SM): the FP64 pipe needs every resident warp it can get, and the cap
+// costs these kernels no spills.  The FP32 policies keep the compiler's
+// choice (a cap spills the pair kernels' row pairs and measured slower).
+template <int BY, int R, int NS>
+__global__ void __launch_bounds__(BX * (BY / R), 1024 / (BX * (BY / R)))
+batch_star7_f64(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ maps, int map_stride,
+                const BatchItem* __restrict__ items, int n_items, double* __restrict__ pool, int cur,
+                int* __restrict__ counter, int* __restrict__ status) {
+    batch_loop<PolF64, BY, R, NS>(inst, maps, map_stride, items, n_items, pool, cur, counter, status);
 }
 
 // The tile ring plus one int for the work-item broadcast.
@@ -166,14 +187,22 @@ struct KernelInfo {
     size_t smem;
 };
 
+// The kernel of (policy, tile): the FP64 policy takes the register-capped
+// variant.
+template <class P, int BY, int R, int NS>
+const void* batch_kernel() {
+    if constexpr (std::is_same<P, PolF64>::value) return (const void*)batch_star7_f64<BY, R, NS>;
+    else return (const void*)batch_star7<P, BY, R, NS>;
+}
+
 template <class P>
 KernelInfo kinfo_prec(int tile) {
     using T = typename P::T;
     switch (tile) {
-        case 0: return {(const void*)batch_star7<P, kTiles[0].by, kTiles[0].r, kTiles[0].ns>, dim3(BX, kTiles[0].by / kTiles[0].r), smem_bytes<T, kTiles[0].by, kTiles[0].ns>()};
-        case 1: return {(const void*)batch_star7<P, kTiles[1].by, kTiles[1].r, kTiles[1].ns>, dim3(BX, kTiles[1].by / kTiles[1].r), smem_bytes<T, kTiles[1].by, kTiles[1].ns>()};
-        case 2: return {(const void*)batch_star7<P, kTiles[2].by, kTiles[2].r, kTiles[2].ns>, dim3(BX, kTiles[2].by / kTiles[2].r), smem_bytes<T, kTiles[2].by, kTiles[2].ns>()};
-        default: return {(const void*)batch_star7<P, kTiles[3].by, kTiles[3].r, kTiles[3].ns>, dim3(BX, kTiles[3].by / kTiles[3].r), smem_bytes<T, kTiles[3].by, kTiles[3].ns>()};
+        case 0: return {batch_kernel<P, kTiles[0].by, kTiles[0].r, kTiles[0].ns>(), dim3(BX, kTiles[0].by / kTiles[0].r), smem_bytes<T, kTiles[0].by, kTiles[0].ns>()};
+        case 1: return {batch_kernel<P, kTiles[1].by, kTiles[1].r, kTiles[1].ns>(), dim3(BX, kTiles[1].by / kTiles[1].r), smem_bytes<T, kTiles[1].by, kTiles[1].ns>()};
+        case 2: return {batch_kernel<P, kTiles[2].by, kTiles[2].r, kTiles[2].ns>(), dim3(BX, kTiles[2].by / kTiles[2].r), smem_bytes<T, kTiles[2].by, kTiles[2].ns>()};
+        default: return {batch_kernel<P, kTiles[3].by, kTiles[3].r, kTiles[3].ns>(), dim3(BX, kTiles[3].by / kTiles[3].r), smem_bytes<T, kTiles[3].by, kTiles[3].ns>()};
     }
 }
 
