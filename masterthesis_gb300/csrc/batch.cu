@@ -54,7 +54,7 @@ __device__ __forceinline__ void batch_loop(const BatchInst* __restrict__ inst, c
                                            typename P::T* __restrict__ pool, int cur, int* __restrict__ counter,
                                            int* __restrict__ status) {
     using T = typename P::T;
-    using G = Tile<T, BY, NS>;
+    using G = Tile<T, BY, NS, true>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* st = reinterpret_cast<T*>(smem_raw);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NS * G::STRIDE * G::ESZ);
@@ -74,7 +74,8 @@ __device__ __forceinline__ void batch_loop(const BatchInst* __restrict__ inst, c
         // pool could alias them and force a reload per node.
         const Star7Coeffs c = I.c;
         TileJob<T> J;
-        J.tm = maps + (long long)(2 * w.inst + cur) * map_stride;
+        J.tm = maps + (long long)(3 * w.inst + cur) * map_stride;
+        J.tmf = maps + (long long)(3 * w.inst + 2) * map_stride;
         J.un = pool + I.off_u[cur ^ 1];
         J.fa = pool + I.off_f;
         J.fb = nullptr;
@@ -84,7 +85,7 @@ __device__ __forceinline__ void batch_loop(const BatchInst* __restrict__ inst, c
         J.L = I.L;
         J.time_old = J.time_new = J.corr = Split{0.0, 0.f, 0.f};
         J.table = nullptr;
-        if (!star7_tile<P, SRC_A, SCAFES_BORDER_DIRICHLET, BY, R, NS>(J, c, w.tx * BX, w.ty * BY, w.z0, w.z1, st, bar,
+        if (!star7_tile<P, SRC_A, SCAFES_BORDER_DIRICHLET, BY, R, NS, true>(J, c, w.tx * BX, w.ty * BY, w.z0, w.z1, st, bar,
                                                                      base, status))
             break;
     }
@@ -112,7 +113,7 @@ batch_star7_f64(const BatchInst* __restrict__ inst, const CUtensorMap* __restric
 
 // The tile ring plus one int for the work-item broadcast.
 template <class T, int BY, int NS>
-size_t smem_bytes() { return Tile<T, BY, NS>::SMEM + 16; }
+size_t smem_bytes() { return Tile<T, BY, NS, true>::SMEM + 16; }
 
 }  // namespace
 
@@ -124,7 +125,8 @@ struct scafes_batch {
     BatchInst* dinst = nullptr;
     void* pool = nullptr;
     size_t pool_elems = 0;
-    // Tensor maps: [inst][buf][tile] on the device and on the host.
+    // Tensor maps: [inst][iterate 0, iterate 1, source][tile] on the device
+    // and on the host.
     std::vector<CUtensorMap> hmaps;
     CUtensorMap* dmaps = nullptr;
     // Work items per tile variant.
@@ -199,10 +201,10 @@ template <class P>
 KernelInfo kinfo_prec(int tile) {
     using T = typename P::T;
     switch (tile) {
-        case 0: return {batch_kernel<P, kTiles[0].by, kTiles[0].r, kTiles[0].ns>(), dim3(BX, kTiles[0].by / kTiles[0].r), smem_bytes<T, kTiles[0].by, kTiles[0].ns>()};
-        case 1: return {batch_kernel<P, kTiles[1].by, kTiles[1].r, kTiles[1].ns>(), dim3(BX, kTiles[1].by / kTiles[1].r), smem_bytes<T, kTiles[1].by, kTiles[1].ns>()};
-        case 2: return {batch_kernel<P, kTiles[2].by, kTiles[2].r, kTiles[2].ns>(), dim3(BX, kTiles[2].by / kTiles[2].r), smem_bytes<T, kTiles[2].by, kTiles[2].ns>()};
-        default: return {batch_kernel<P, kTiles[3].by, kTiles[3].r, kTiles[3].ns>(), dim3(BX, kTiles[3].by / kTiles[3].r), smem_bytes<T, kTiles[3].by, kTiles[3].ns>()};
+        case 0: return {batch_kernel<P, kTiles[0].by, kTiles[0].r, ring_stages(kTiles[0].ns, true)>(), dim3(BX, kTiles[0].by / kTiles[0].r), smem_bytes<T, kTiles[0].by, ring_stages(kTiles[0].ns, true)>()};
+        case 1: return {batch_kernel<P, kTiles[1].by, kTiles[1].r, ring_stages(kTiles[1].ns, true)>(), dim3(BX, kTiles[1].by / kTiles[1].r), smem_bytes<T, kTiles[1].by, ring_stages(kTiles[1].ns, true)>()};
+        case 2: return {batch_kernel<P, kTiles[2].by, kTiles[2].r, ring_stages(kTiles[2].ns, true)>(), dim3(BX, kTiles[2].by / kTiles[2].r), smem_bytes<T, kTiles[2].by, ring_stages(kTiles[2].ns, true)>()};
+        default: return {batch_kernel<P, kTiles[3].by, kTiles[3].r, ring_stages(kTiles[3].ns, true)>(), dim3(BX, kTiles[3].by / kTiles[3].r), smem_bytes<T, kTiles[3].by, ring_stages(kTiles[3].ns, true)>()};
     }
 }
 
@@ -369,17 +371,20 @@ extern "C" int scafes_batch_create(const scafes_batch_instance* in, int n_inst, 
         bfail(nullptr, SCAFES_ERR_CUDA, "scafes_batch_create: %s", cudaGetErrorString(e));
         return bail(SCAFES_ERR_CUDA);
     }
-    // Tensor maps of every instance, buffer and tile variant.
-    b->hmaps.resize((size_t)n_inst * 2 * STAR7_NUM_TILES);
+    // Tensor maps of every instance, field (two iterates with halo boxes,
+    // the source with a 32 x BY box) and tile variant.
+    b->hmaps.resize((size_t)n_inst * 3 * STAR7_NUM_TILES);
     for (int i = 0; i < n_inst; ++i) {
         const Layout& L = b->hinst[i].L;
-        for (int buf = 0; buf < 2; ++buf)
+        for (int buf = 0; buf < 3; ++buf)
             for (int tile = 0; tile < STAR7_NUM_TILES; ++tile) {
-                char* base = (char*)b->pool + (size_t)b->hinst[i].off_u[buf] * b->esz;
-                CUresult r = make_tensor_map_3d(&b->hmaps[((size_t)i * 2 + buf) * STAR7_NUM_TILES + tile], base,
+                const long long off = buf < 2 ? b->hinst[i].off_u[buf] : b->hinst[i].off_f;
+                char* base = (char*)b->pool + (size_t)off * b->esz;
+                const int bw = buf < 2 ? star7_box_width(precision) : BX;
+                const int bh = buf < 2 ? star7_box_height(tile) : star7_box_height(tile) - 2;
+                CUresult r = make_tensor_map_3d(&b->hmaps[((size_t)i * 3 + buf) * STAR7_NUM_TILES + tile], base,
                                                 (int)b->esz, L.nx, L.ny, L.nz, (size_t)L.pitch * b->esz,
-                                                (size_t)L.plane * b->esz, star7_box_width(precision),
-                                                star7_box_height(tile));
+                                                (size_t)L.plane * b->esz, bw, bh);
                 if (r != CUDA_SUCCESS) {
                     bfail(nullptr, SCAFES_ERR_CUDA, "scafes_batch_create: cuTensorMapEncodeTiled failed (%d)", (int)r);
                     return bail(SCAFES_ERR_CUDA);
@@ -502,7 +507,9 @@ extern "C" int scafes_batch_step_looped(scafes_batch* b, int n_steps) {
             a.border = SCAFES_BORDER_DIRICHLET;
             a.tile = star7_default_tile(I.L);
             a.L = I.L;
-            a.tm_uo = &b->hmaps[((size_t)i * 2 + b->cur) * STAR7_NUM_TILES + a.tile];
+            a.tm_uo = &b->hmaps[((size_t)i * 3 + b->cur) * STAR7_NUM_TILES + a.tile];
+            a.tm_f = &b->hmaps[((size_t)i * 3 + 2) * STAR7_NUM_TILES + a.tile];
+            a.table = nullptr;
             a.status = b->status;
             a.uo = (char*)b->pool + (size_t)I.off_u[b->cur] * b->esz;
             a.un = (char*)b->pool + (size_t)I.off_u[b->cur ^ 1] * b->esz;

@@ -44,6 +44,8 @@ struct scafes_handle {
     void* u[2] = {nullptr, nullptr};
     CUtensorMap tm[2][STAR7_NUM_TILES];   // TMA descriptors of u[0], u[1] per tile
     bool tm_ok[2][STAR7_NUM_TILES] = {};
+    CUtensorMap tmf[STAR7_NUM_TILES];     // TMA descriptors of F_A (box 32 x BY) per tile
+    bool tmf_ok[STAR7_NUM_TILES] = {};
     int tile = 0;                         // tile variant of the sweep
     int* status = nullptr;                // device status word of the kernels
     int cur = 0;
@@ -363,6 +365,22 @@ static const CUtensorMap* tensor_map(scafes_handle* h, int buf, int tile) {
     return &h->tm[buf][tile];
 }
 
+// TMA descriptor of the source F_A for tile variant `tile`: a 32 x BY box
+// without halo (the F_A slot keeps its device buffer once uploaded).
+static const CUtensorMap* source_map(scafes_handle* h, int tile) {
+    if (!h->tmf_ok[tile]) {
+        CUresult r = make_tensor_map_3d(&h->tmf[tile], h->fld[SCAFES_FIELD_F_A], (int)h->esz, h->L.nx, h->L.ny,
+                                        h->L.nz, (size_t)h->L.pitch * h->esz, (size_t)h->L.plane * h->esz, BX,
+                                        star7_box_height(tile) - 2);
+        if (r != CUDA_SUCCESS) {
+            fail(&h->err, SCAFES_ERR_CUDA, "cuTensorMapEncodeTiled (source) failed (%d)", (int)r);
+            return nullptr;
+        }
+        h->tmf_ok[tile] = true;
+    }
+    return &h->tmf[tile];
+}
+
 static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
     Star7Launch a;
     a.precision = h->cfg.precision;
@@ -378,6 +396,8 @@ static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
     a.gconst = 0.0;
     a.c = make_star7_coeffs(h->cfg.c0, h->cfg.cp, h->cfg.cf);
     a.table = h->table;
+    a.tm_f = nullptr;
+    if (a.fa && !a.fb && h->cfg.cf != 0.0 && !(a.tm_f = source_map(h, tile))) return SCAFES_ERR_CUDA;
     if (!h->has[SCAFES_FIELD_F_A] && h->has[SCAFES_FIELD_F_B])
         return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
                     "scafes_gpu_step: upload F_A (possibly zeros) when F_B is used");

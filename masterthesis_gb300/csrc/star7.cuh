@@ -16,6 +16,9 @@ constexpr int STAR7_NUM_TILES = 4;
 // Coefficients of u_new = c0*u + sum_p cp*(u_{p-}+u_{p+}) + cf*F, in double
 // and split into FP32 triples (hi + lo + lo2, ~72 bits) for the
 // compensated path.
+// Width (nodes along x) of every sweep tile: one warp per row.
+constexpr int BX = 32;
+
 struct Star7Coeffs {
     double c0, cx, cy, cz, cf;
     float c0h, c0l, c0ll, cxh, cxl, cxll, cyh, cyl, cyll, czh, czl, czll, cfh, cfl, cfll;
@@ -61,6 +64,7 @@ struct Star7Launch {
     int tile;             // tile variant 0 .. STAR7_NUM_TILES-1
     Layout L;
     const CUtensorMap* tm_uo;  // TMA descriptor of the old iterate
+    const CUtensorMap* tm_f;   // TMA descriptor of F_A, box 32 x BY of the tile (F_A-only sources)
     int* status;          // device status word (0 = ok)
     const void* uo;       // old iterate (element type per precision)
     void* un;             // new iterate

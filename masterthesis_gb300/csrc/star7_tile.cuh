@@ -21,19 +21,26 @@
 
 namespace scafes {
 
-constexpr int BX = 32;
 // NS: stages of the shared-memory ring, a power of two (stage and phase
 // indices are shifts).  Fewer stages leave room for more CTAs per SM.
-template <class T, int BY, int NS>
+// FS: each stage also holds the source F_A of its plane (a 32 x BY box
+// without halo), streamed by TMA with the iterate instead of read per node.
+template <class T, int BY, int NS, bool FS = false>
 struct Tile {
     static constexpr int ESZ = (int)sizeof(T);
     static constexpr int LP = 16 / ESZ;          // left halo padded to 16 bytes
     static constexpr int W = BX + 2 * LP;        // box width (elements)
     static constexpr int H = BY + 2;             // box height (rows)
     static constexpr uint32_t TX_BYTES = W * H * ESZ;
-    static constexpr int STRIDE = ((W * H * ESZ + 127) / 128) * 128 / ESZ;  // elements per stage
+    static constexpr int USTRIDE = ((W * H * ESZ + 127) / 128) * 128 / ESZ;  // iterate box, elements
+    static constexpr uint32_t F_BYTES = FS ? BX * BY * ESZ : 0;
+    static constexpr int STRIDE = USTRIDE + (FS ? ((BX * BY * ESZ + 127) / 128) * 128 / ESZ : 0);
     static constexpr size_t SMEM = (size_t)NS * STRIDE * ESZ + NS * sizeof(uint64_t);
 };
+
+// Ring depth of a kernel: tiles that also stage F_A use 4 stages (their
+// stages are larger; 4 keep 2-3 planes in flight).
+constexpr int ring_stages(int ns, bool fs) { return fs ? 4 : ns; }
 
 // Tile variants {BY, R, NS}: CTA tile 32 x BY, R rows per thread, NS ring
 // stages.
@@ -44,6 +51,7 @@ constexpr TileShape kTiles[STAR7_NUM_TILES] = {{8, 1, 8}, {16, 2, 8}, {32, 4, 8}
 template <class T>
 struct TileJob {
     const CUtensorMap* tm;   // TMA descriptor of the old iterate
+    const CUtensorMap* tmf;  // TMA descriptor of F_A (box 32 x BY), staged tiles only
     T* un;                   // new iterate
     const T* fa;             // source F_A or null
     const T* fb;             // source F_B or null
@@ -102,15 +110,16 @@ enum : int { SRC_NONE = 0, SRC_A = 1, SRC_AB = 2 };
 // and phase of every plane); it is advanced by the planes this tile used.
 // Returns false (and records SCAFES_ERR_TIMEOUT) when a stage never
 // arrived; the caller must then stop.
-template <class P, int SRC, int BORDER, int BY, int R, int NS>
+template <class P, int SRC, int BORDER, int BY, int R, int NS, bool FS>
 __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, const Star7Coeffs& c,
                                            int x0, int y0, int z0, int z1,
                                            typename P::T* st, uint64_t* bar, uint32_t& base,
                                            int* status) {
     using T = typename P::T;
-    using G = Tile<T, BY, NS>;
+    using G = Tile<T, BY, NS, FS>;
     constexpr bool HAS_F = SRC != SRC_NONE;
     constexpr bool has_fb = SRC == SRC_AB;
+    static_assert(!FS || SRC == SRC_A, "only F_A is staged");
     const Layout& L = J.L;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * BX + tx;
@@ -120,14 +129,19 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
     const int np = z1 - z0 + 2;  // planes z0-1 .. z1 (index p <-> z = z0 - 1 + p)
     const uint32_t b0 = base;
 
+    // Streams plane q (z = z0 - 1 + q) into its stage; the planes that are
+    // computed (1 <= q <= np - 2) bring their F_A box along.
+    auto issue = [&](int q) {
+        const uint32_t s = (b0 + (uint32_t)q) & (NS - 1);
+        const bool wf = FS && q >= 1 && q <= np - 2;
+        mbar_arrive_expect_tx(&bar[s], G::TX_BYTES + (wf ? G::F_BYTES : 0u));
+        tma_load_3d(st + s * G::STRIDE, J.tm, x0 - G::LP, y0 - 1, z0 - 1 + q, &bar[s]);
+        if (wf) tma_load_3d(st + s * G::STRIDE + G::USTRIDE, J.tmf, x0, y0, z0 - 1 + q, &bar[s]);
+    };
     if (tid == 0) {
         const int pre = np < NS ? np : NS;
         fence_proxy_async_smem();
-        for (int p = 0; p < pre; ++p) {
-            const uint32_t s = (b0 + p) & (NS - 1);
-            mbar_arrive_expect_tx(&bar[s], G::TX_BYTES);
-            tma_load_3d(st + s * G::STRIDE, J.tm, x0 - G::LP, y0 - 1, z0 - 1 + p, &bar[s]);
-        }
+        for (int p = 0; p < pre; ++p) issue(p);
     }
 
     const bool xin = x < L.nx;
@@ -179,7 +193,10 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 w[k] = pl[(rb + k) * G::W - 1];
                 e[k] = pl[(rb + k) * G::W + 1];
                 f[k] = P::zero();
-                if (HAS_F && live) f[k] = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
+                if (FS)
+                    f[k] = st[slot(p) * G::STRIDE + G::USTRIDE + (ty * R + k) * BX + tx];
+                else if (HAS_F && live)
+                    f[k] = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
             }
             P::template star_rows<HAS_F, R>(c, below, cur, above, ym, yp, w, e, f, v);
 #pragma unroll
@@ -264,10 +281,8 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
         if (tid == 0) {
             const int pn = p - 1 + NS;
             if (pn < np) {
-                const uint32_t s = slot(pn);
                 fence_proxy_async_smem();
-                mbar_arrive_expect_tx(&bar[s], G::TX_BYTES);
-                tma_load_3d(st + s * G::STRIDE, J.tm, x0 - G::LP, y0 - 1, z0 - 1 + pn, &bar[s]);
+                issue(pn);
             }
         }
         ++p;

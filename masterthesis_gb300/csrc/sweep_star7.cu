@@ -11,25 +11,26 @@
 
 namespace scafes {
 
-template <class P, int SRC, int BORDER, int BY, int R, int NS>
+template <class P, int SRC, int BORDER, int BY, int R, int NS, bool FS>
 __global__ void __launch_bounds__(BX * (BY / R))
-star7_tma(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un,
+star7_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmf,
+          typename P::T* __restrict__ un,
           const typename P::T* __restrict__ fa, const typename P::T* __restrict__ fb,
           const typename P::T* __restrict__ ga, const typename P::T* __restrict__ gb, typename P::T gval,
           Layout L, Star7Coeffs c, Split time_old, Split time_new,
           Split corr, const scafes_border_form* __restrict__ table, int zchunk, int* __restrict__ status)
 {
     using T = typename P::T;
-    using G = Tile<T, BY, NS>;
+    using G = Tile<T, BY, NS, FS>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     T* st = reinterpret_cast<T*>(smem_raw);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NS * G::STRIDE * G::ESZ);
     ring_init<NS>(bar);
-    TileJob<T> J{&tm, un, fa, fb, ga, gb, gval, L, time_old, time_new, corr, table};
+    TileJob<T> J{&tm, &tmf, un, fa, fb, ga, gb, gval, L, time_old, time_new, corr, table};
     const int z0 = blockIdx.z * zchunk;
     const int z1 = min(z0 + zchunk, L.nz);
     uint32_t base = 0;
-    star7_tile<P, SRC, BORDER, BY, R, NS>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
+    star7_tile<P, SRC, BORDER, BY, R, NS, FS>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
 }
 
 // ---- host side ---------------------------------------------------------------
@@ -94,12 +95,15 @@ static inline void to_elem(double d, float2& out) {
     out = make_float2(p.hi, p.lo);
 }
 
-template <class P, int SRC, int BORDER, int BY, int R, int NS>
+template <class P, int SRC, int BORDER, int BY, int R, int NS0>
 static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
     using T = typename P::T;
-    using G = Tile<T, BY, NS>;
+    constexpr bool FS = SRC == SRC_A;  // a source without a time term is staged with the iterate
+    constexpr int NS = ring_stages(NS0, FS);
+    using G = Tile<T, BY, NS, FS>;
     const Layout& L = a.L;
-    auto kern = star7_tma<P, SRC, BORDER, BY, R, NS>;
+    if (FS && a.tm_f == nullptr) return cudaErrorInvalidValue;
+    auto kern = star7_tma<P, SRC, BORDER, BY, R, NS, FS>;
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
@@ -114,7 +118,7 @@ static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
     const int zchunk = choose_zchunk(L, BY);
     dim3 block(BX, BY / R, 1);
     dim3 grid((L.nx + BX - 1) / BX, (L.ny + BY - 1) / BY, (L.nz + zchunk - 1) / zchunk);
-    kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, (T*)a.un, (const T*)a.fa, (const T*)a.fb, (const T*)a.ga,
+    kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, FS ? *a.tm_f : *a.tm_uo, (T*)a.un, (const T*)a.fa, (const T*)a.fb, (const T*)a.ga,
                                            (const T*)a.gb, gval, L,
                                            a.c, make_split(a.time_old), make_split(a.time_new),
                                            make_split(a.mirror_corr), a.table, zchunk, a.status);
