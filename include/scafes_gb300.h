@@ -63,11 +63,15 @@ enum scafes_field {
     SCAFES_FIELD_U = 0,   /* the unknown data field (iterate)            */
     SCAFES_FIELD_F_A = 1, /* source F(t) = F_A + time(t) * F_B            */
     SCAFES_FIELD_F_B = 2,
-    SCAFES_FIELD_G_A = 3, /* border value G(t) = G_A + time(t) * G_B      */
-    SCAFES_FIELD_G_B = 4,
+    SCAFES_FIELD_G_A = 3, /* border value G(t) = G_A + s * G_B          */
+    SCAFES_FIELD_G_B = 4, /*   (+ s^2 G_C + s^3 G_D + s^4 G_E), s = time(t) */
+                          /*   by default (scafes_gpu_set_border_time_basis) */
     SCAFES_FIELD_E_A = 5, /* exact solution E(t) = E_A + time(t) * E_B,   */
     SCAFES_FIELD_E_B = 6, /* only read by scafes_gpu_err_linf            */
-    SCAFES_FIELD_COUNT = 7
+    SCAFES_FIELD_G_C = 7, /* higher time orders of G, stored in FP64;    */
+    SCAFES_FIELD_G_D = 8, /* read by SCAFES_BORDER_TABLE rules only      */
+    SCAFES_FIELD_G_E = 9,
+    SCAFES_FIELD_COUNT = 10
 };
 
 /* ---- border (updateBorder) kinds --------------------------------------- */
@@ -93,26 +97,30 @@ enum scafes_border {
 
 /* One border class's rule, evaluated in FP64 on border nodes:
  *   u_new = cu*u + sum_d cn[d]*u_d + cf*F(time(t-1))
- *           + cg_old*G(time(t-1)) + cg_new*G(time(t))
+ *           + cg_old*G(time(t-1)) + cg_new*G(time(t)) + cu4*u^4
  * with neighbours d = x-, x+, y-, y+, z-, z+ (a neighbour outside the grid
  * must have weight 0).  A class is a 6-bit mask of the faces a node lies on:
  * bit 0 x == 0, bit 1 x == nx-1, bit 2 y == 0, bit 3 y == ny-1, bit 4
  * z == 0, bit 5 z == nz-1; entry 0 (inner nodes) is unused.  Dirichlet is
- * cg_new = 1 with every other weight 0. */
+ * cg_new = 1 with every other weight 0.  The u^4 term is the radiative
+ * flux of tests/system/PennesBioheatEqnFDM/Radiation/Radiation.hpp. */
 typedef struct scafes_border_form {
     double cu;
     double cn[6];
     double cf;
     double cg_old;
     double cg_new;
+    double cu4;
 } scafes_border_form;
 
 #define SCAFES_BORDER_CLASSES 64
 
 /* Flux-condition kinds of scafes_border_forms_flux. */
 enum scafes_flux_kind {
-    SCAFES_FLUX_NEUMANN = 0, /* -lambda du/dn = G              (Neumann.hpp) */
-    SCAFES_FLUX_CAUCHY = 1   /* -lambda du/dn = alpha u - G    (Cauchy.hpp)  */
+    SCAFES_FLUX_NEUMANN = 0,  /* -lambda du/dn = G             (Neumann.hpp)   */
+    SCAFES_FLUX_CAUCHY = 1,   /* -lambda du/dn = alpha u - G   (Cauchy.hpp)    */
+    SCAFES_FLUX_RADIATION = 2 /* -lambda du/dn = alpha u^4 - G (Radiation.hpp,
+                                 alpha = epsilon * sigma)                     */
 };
 
 /* Configuration of one plain (single-instance) problem.
@@ -160,6 +168,7 @@ int scafes_star7_heat_coeffs(scafes_cfg* cfg, double coeff_a, double rho_c,
  * neighbour replaced by the inner one and the flux term
  *   - cp[p]*(2 h_p/lambda) * G(time(t-1))          (Neumann)
  *   - cp[p]*(2 h_p/lambda) * (alpha*u - G(time(t-1)))   (Cauchy)
+ *   - cp[p]*(2 h_p/lambda) * (alpha*u^4 - G(time(t-1))) (Radiation)
  * (tests/system/HeatEqnFDM/Neumann/Neumann.hpp and Cauchy/Cauchy.hpp, the
  * Pennes variants add the perfusion already contained in c0). */
 int scafes_border_forms_flux(const scafes_cfg* cfg, int kind, double lambda,
@@ -205,9 +214,22 @@ int scafes_snapshot_read(const char* path, int index, double* host, size_t n,
 
 /* Sets the border rules of a SCAFES_BORDER_TABLE problem (64 entries,
  * indexed by class mask).  A rule with cf != 0 needs a source field; one
- * with cg_old or cg_new != 0 reads G = G_A + time*G_B. */
+ * with cg_old or cg_new != 0 reads G (slots G_A .. G_E). */
 int scafes_gpu_set_border_forms(scafes_handle* h,
                                 const scafes_border_form forms[64]);
+
+/* Time variable of the border field G of a SCAFES_BORDER_TABLE problem:
+ *   G(t) = G_A + s*(G_B + s*(G_C + s*(G_D + s*G_E))),
+ *   s = (time(t) - t_center) * t_rate   (two FP64 roundings, no FMA),
+ * Horner in FP64 with FMA; slots not uploaded are 0.  Default t_center = 0,
+ * t_rate = 1 (s = time(t)).  A polynomial fitted over the run's time span
+ * with s in [-1, 1] represents a known field up to quartic in time, such as
+ * the radiative border field of tests/system/PennesBioheatEqnFDM/Radiation/
+ * TimeLinSpaceLin/TimeLinSpaceLin.hpp evalBorder.  Dirichlet and mirror
+ * problems keep G = G_A + time*G_B and refuse another basis or the slots
+ * G_C .. G_E at step time. */
+int scafes_gpu_set_border_time_basis(scafes_handle* h, double t_center,
+                                     double t_rate);
 
 /* Advances the unknown field by n_steps time steps (one step = the update
  * phase of one iteration of iterateOverTime, src/ScaFES_Problem.hpp:

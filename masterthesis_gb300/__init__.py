@@ -22,10 +22,10 @@ LIB_PATH = PKG / "libscafes_gb300.so"
 PREC_F64, PREC_F32X2, PREC_F32, PREC_F64E = 0, 1, 2, 3
 PRECISIONS = {"f64": PREC_F64, "f32x2": PREC_F32X2, "f32": PREC_F32, "f64e": PREC_F64E}
 # enum scafes_field
-FIELD_U, FIELD_F_A, FIELD_F_B, FIELD_G_A, FIELD_G_B, FIELD_E_A, FIELD_E_B = range(7)
+FIELD_U, FIELD_F_A, FIELD_F_B, FIELD_G_A, FIELD_G_B, FIELD_E_A, FIELD_E_B, FIELD_G_C, FIELD_G_D, FIELD_G_E = range(10)
 # enum scafes_border
 BORDER_DIRICHLET, BORDER_MIRROR_POW2, BORDER_TABLE = 0, 1, 2
-FLUX_NEUMANN, FLUX_CAUCHY = 0, 1
+FLUX_NEUMANN, FLUX_CAUCHY, FLUX_RADIATION = 0, 1, 2
 
 STATUS = {0: "SCAFES_OK", -1: "SCAFES_ERR_ARG", -2: "SCAFES_ERR_CUDA", -3: "SCAFES_ERR_STATE",
           -4: "SCAFES_ERR_UNSUPPORTED", -5: "SCAFES_ERR_NOMEM", -6: "SCAFES_ERR_TIMEOUT"}
@@ -40,7 +40,7 @@ class ScafesError(RuntimeError):
 class BorderForm(C.Structure):
     """Mirror of ``struct scafes_border_form`` (one border class's rule)."""
     _fields_ = [("cu", C.c_double), ("cn", C.c_double * 6), ("cf", C.c_double), ("cg_old", C.c_double),
-                ("cg_new", C.c_double)]
+                ("cg_new", C.c_double), ("cu4", C.c_double)]
 
 
 BorderForms = BorderForm * 64
@@ -80,6 +80,7 @@ def lib() -> C.CDLL:
         L.scafes_border_forms_flux.argtypes = [C.POINTER(Cfg), C.c_int, C.c_double, C.c_double,
                                                C.POINTER(BorderForm)]
         L.scafes_gpu_set_border_forms.argtypes = [vp, C.POINTER(BorderForm)]
+        L.scafes_gpu_set_border_time_basis.argtypes = [vp, C.c_double, C.c_double]
         L.scafes_gpu_step_snapshots.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_char_p]
         L.scafes_snapshot_info.argtypes = [C.c_char_p, C.c_int * 3, C.POINTER(C.c_int)]
         L.scafes_snapshot_read.argtypes = [C.c_char_p, C.c_int, dp, C.c_size_t, C.POINTER(C.c_longlong),
@@ -173,8 +174,8 @@ def snapshot_read(path, index):
 
 
 def border_forms_flux(cfg: Cfg, kind: int, lam: float = 1.0, alpha: float = 1.0):
-    """The 64 border rules of the reference's Neumann / Cauchy system tests
-    for cfg (scafes_border_forms_flux)."""
+    """The 64 border rules of the reference's Neumann / Cauchy / Radiation
+    system tests for cfg (scafes_border_forms_flux)."""
     forms = BorderForms()
     _check(lib().scafes_border_forms_flux(C.byref(cfg), kind, lam, alpha, forms))
     return forms
@@ -199,6 +200,10 @@ class Plain:
 
     def set_border_forms(self, forms):
         _check(lib().scafes_gpu_set_border_forms(self.h, forms), self.h)
+
+    def set_border_time_basis(self, t_center: float, t_rate: float):
+        """G(t) = sum_k G_k s^k with s = (time(t) - t_center) * t_rate."""
+        _check(lib().scafes_gpu_set_border_time_basis(self.h, t_center, t_rate), self.h)
 
     def upload(self, field: int, arr: np.ndarray):
         a = np.ascontiguousarray(arr, dtype=np.float64)

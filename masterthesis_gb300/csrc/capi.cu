@@ -5,6 +5,7 @@
 // constructor allocates (src/ScaFES_Problem.hpp:1604-1674): two ping-pong
 // buffers of the unknown field (the old/new pair swapped by
 // swapPointersOfUnknownDfs, :3273-3316) plus the known fields.
+#include <cmath>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -65,7 +66,8 @@ struct scafes_handle {
     bool uploaded = false;
     // Border rules of a SCAFES_BORDER_TABLE problem (device copy) and whether
     // any rule reads the source field.
-    scafes_border_form* table = nullptr;
+    BorderTable* table = nullptr;          // device copy of table_host
+    BorderTable table_host;
     bool table_needs_f = false;
     // Snapshot writer (allocated on first use): a dense FP64 copy of the
     // iterate on the device, two pinned host buffers, a copy stream.
@@ -212,7 +214,16 @@ extern "C" int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out) {
 // Exact-solution slots stay double (only the error check reads them);
 // source and border slots use the element type of the unknown field.
 static bool slot_is_double(int field) {
-    return field == SCAFES_FIELD_E_A || field == SCAFES_FIELD_E_B;
+    return field == SCAFES_FIELD_E_A || field == SCAFES_FIELD_E_B || field >= SCAFES_FIELD_G_C;
+}
+
+// Copies the host image of the border table (rules, higher time orders of
+// G, time basis) to the device, once the rules exist there.
+static int sync_table(scafes_handle* h) {
+    if (!h->table) return SCAFES_OK;
+    CUDA_TRY(h, cudaMemcpyAsync(h->table, &h->table_host, sizeof(BorderTable), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SCAFES_OK;
 }
 
 static int ensure_stage(scafes_handle* h) {
@@ -321,6 +332,11 @@ extern "C" int scafes_gpu_upload(scafes_handle* h, int field, const double* host
         rc = h2d(h, h->fld[field], dbl ? SCAFES_PREC_F64 : h->cfg.precision, host);
         if (rc) return rc;
         h->has[field] = true;
+        if (field >= SCAFES_FIELD_G_C) {
+            h->table_host.g_hi[field - SCAFES_FIELD_G_C] = (const double*)h->fld[field];
+            rc = sync_table(h);
+            if (rc) return rc;
+        }
     }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return SCAFES_OK;
@@ -401,6 +417,12 @@ static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
     if (!h->has[SCAFES_FIELD_F_A] && h->has[SCAFES_FIELD_F_B])
         return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
                     "scafes_gpu_step: upload F_A (possibly zeros) when F_B is used");
+    const bool g_hi = h->has[SCAFES_FIELD_G_C] || h->has[SCAFES_FIELD_G_D] || h->has[SCAFES_FIELD_G_E];
+    if (h->cfg.border != SCAFES_BORDER_TABLE &&
+        (g_hi || h->table_host.t_center != 0.0 || h->table_host.t_rate != 1.0))
+        return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                    "scafes_gpu_step: higher time orders of G (slots G_C..G_E) or another time basis need "
+                    "SCAFES_BORDER_TABLE; this border reads G = G_A + time*G_B");
     if (h->cfg.border == SCAFES_BORDER_TABLE) {
         if (!h->table)
             return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_step: set the border rules first "
@@ -451,19 +473,29 @@ extern "C" int scafes_gpu_set_border_forms(scafes_handle* h, const scafes_border
             continue;  // a node cannot be on both faces of an axis (n >= 3)
         needs_f = needs_f || forms[m].cf != 0.0;
     }
-    if (!h->table) CUDA_TRY(h, cudaMalloc(&h->table, sizeof(scafes_border_form) * SCAFES_BORDER_CLASSES));
-    CUDA_TRY(h, cudaMemcpyAsync(h->table, forms, sizeof(scafes_border_form) * SCAFES_BORDER_CLASSES,
-                                cudaMemcpyHostToDevice, h->stream));
-    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (!h->table) CUDA_TRY(h, cudaMalloc(&h->table, sizeof(BorderTable)));
+    std::memcpy(h->table_host.rule, forms, sizeof(scafes_border_form) * SCAFES_BORDER_CLASSES);
+    const int rc = sync_table(h);
+    if (rc) return rc;
     h->table_needs_f = needs_f;
     return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_set_border_time_basis(scafes_handle* h, double t_center, double t_rate) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_set_border_time_basis: handle is NULL");
+    if (!std::isfinite(t_center) || !std::isfinite(t_rate) || t_rate == 0.0)
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_set_border_time_basis: t_center=%g, t_rate=%g", t_center,
+                    t_rate);
+    h->table_host.t_center = t_center;
+    h->table_host.t_rate = t_rate;
+    return sync_table(h);
 }
 
 extern "C" int scafes_border_forms_flux(const scafes_cfg* cfg, int kind, double lambda, double alpha,
                                         scafes_border_form forms[64]) {
     if (!cfg || !forms || cfg->dim != 3 || lambda == 0.0)
         return fail(nullptr, SCAFES_ERR_ARG, "scafes_border_forms_flux: bad arguments");
-    if (kind != SCAFES_FLUX_NEUMANN && kind != SCAFES_FLUX_CAUCHY)
+    if (kind != SCAFES_FLUX_NEUMANN && kind != SCAFES_FLUX_CAUCHY && kind != SCAFES_FLUX_RADIATION)
         return fail(nullptr, SCAFES_ERR_ARG, "scafes_border_forms_flux: kind %d", kind);
     double h[3];
     for (int p = 0; p < 3; ++p) {
@@ -474,7 +506,7 @@ extern "C" int scafes_border_forms_flux(const scafes_cfg* cfg, int kind, double 
         scafes_border_form& F = forms[m];
         F = scafes_border_form{};
         if (m == 0) continue;
-        if (m & (1 | 4 | 16)) {  // on a min face: Dirichlet (Neumann.hpp / Cauchy.hpp "index 0" branch)
+        if (m & (1 | 4 | 16)) {  // on a min face: Dirichlet (the "index 0" branch of Neumann.hpp, Cauchy.hpp, Radiation.hpp)
             F.cg_new = 1.0;
             continue;
         }
@@ -489,8 +521,11 @@ extern "C" int scafes_border_forms_flux(const scafes_cfg* cfg, int kind, double 
                 const double flux = cfg->cp[p] * (2.0 * h[p] / lambda);
                 if (kind == SCAFES_FLUX_NEUMANN) {
                     F.cg_old -= flux;
-                } else {
+                } else if (kind == SCAFES_FLUX_CAUCHY) {
                     F.cu -= flux * alpha;
+                    F.cg_old += flux;
+                } else {
+                    F.cu4 -= flux * alpha;
                     F.cg_old += flux;
                 }
             } else {

@@ -58,6 +58,15 @@ int star7_box_height(int tile);
 // Tile variant used when none is chosen: {32,4} on large grids, {8,1} else.
 int star7_default_tile(const Layout& L);
 
+// Device block of a SCAFES_BORDER_TABLE problem: the rule of each border
+// class and the border field's higher time orders and time variable
+// (scafes_gpu_set_border_time_basis).
+struct BorderTable {
+    scafes_border_form rule[SCAFES_BORDER_CLASSES];
+    const double* g_hi[3] = {nullptr, nullptr, nullptr};  // G_C, G_D, G_E (FP64) or null
+    double t_center = 0.0, t_rate = 1.0;
+};
+
 struct Star7Launch {
     int precision;        // enum scafes_precision
     int border;           // enum scafes_border
@@ -77,7 +86,7 @@ struct Star7Launch {
     double time_old;      // time(t)   : F is read at the old time
     double time_new;      // time(t+1) : G is read at the new time
     double mirror_corr;   // 2^t for SCAFES_BORDER_MIRROR_POW2
-    const scafes_border_form* table;  // device rules for SCAFES_BORDER_TABLE
+    const BorderTable* table;  // device rules for SCAFES_BORDER_TABLE
 };
 
 // Enqueues one sweep (one time step) on `stream`.  Returns cudaSuccess or the

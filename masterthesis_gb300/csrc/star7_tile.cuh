@@ -60,7 +60,7 @@ struct TileJob {
     T gval;                  // border value when ga is null
     Layout L;
     Split time_old, time_new, corr;  // time(t), time(t+1), mirror correction
-    const scafes_border_form* table;  // border rules (SCAFES_BORDER_TABLE)
+    const BorderTable* table;  // border rules (SCAFES_BORDER_TABLE)
 };
 
 // The table rule of a border node, in FP64 whatever the element type (border
@@ -71,8 +71,10 @@ __device__ __noinline__ typename P::T table_rule(const TileJob<typename P::T>& J
                                                   typename P::T u, typename P::T w, typename P::T e,
                                                   typename P::T s, typename P::T n, typename P::T b,
                                                   typename P::T t) {
-    const scafes_border_form& R = J.table[mask];
-    double v = R.cu * P::to_double(u);
+    const BorderTable& B = *J.table;
+    const scafes_border_form& R = B.rule[mask];
+    const double ud = P::to_double(u);
+    double v = R.cu * ud;
     v = fma(R.cn[0], P::to_double(w), v);
     v = fma(R.cn[1], P::to_double(e), v);
     v = fma(R.cn[2], P::to_double(s), v);
@@ -84,10 +86,26 @@ __device__ __noinline__ typename P::T table_rule(const TileJob<typename P::T>& J
         if (HAS_FB) f = fma(J.time_old.d, P::to_double(J.fb[off]), f);
         v = fma(R.cf, f, v);
     }
-    const double g = J.ga ? P::to_double(J.ga[off]) : P::to_double(J.gval);
-    const double gb = J.gb ? P::to_double(J.gb[off]) : 0.0;
-    v = fma(R.cg_old, fma(J.time_old.d, gb, g), v);
-    v = fma(R.cg_new, fma(J.time_new.d, gb, g), v);
+    // G(t) = G_A + s (G_B + s (G_C + s (G_D + s G_E))), s = (time - tc) * rate;
+    // with the default basis and no higher orders this is G_A + time * G_B.
+    const double g0 = J.ga ? P::to_double(J.ga[off]) : P::to_double(J.gval);
+    const double g1 = J.gb ? P::to_double(J.gb[off]) : 0.0;
+    double gh[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) gh[k] = B.g_hi[k] ? B.g_hi[k][off] : 0.0;
+    auto G = [&](double time) {
+        const double s = __dmul_rn(__dsub_rn(time, B.t_center), B.t_rate);
+        double g = fma(gh[2], s, gh[1]);
+        g = fma(g, s, gh[0]);
+        g = fma(g, s, g1);
+        return fma(g, s, g0);
+    };
+    v = fma(R.cg_old, G(J.time_old.d), v);
+    v = fma(R.cg_new, G(J.time_new.d), v);
+    if (R.cu4 != 0.0) {
+        const double u2 = ud * ud;
+        v = fma(R.cu4, u2 * u2, v);
+    }
     return P::from_double(v);
 }
 

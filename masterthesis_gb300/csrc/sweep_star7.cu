@@ -18,7 +18,7 @@ star7_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtens
           const typename P::T* __restrict__ fa, const typename P::T* __restrict__ fb,
           const typename P::T* __restrict__ ga, const typename P::T* __restrict__ gb, typename P::T gval,
           Layout L, Star7Coeffs c, Split time_old, Split time_new,
-          Split corr, const scafes_border_form* __restrict__ table, int zchunk, int* __restrict__ status)
+          Split corr, const BorderTable* __restrict__ table, int zchunk, int* __restrict__ status)
 {
     using T = typename P::T;
     using G = Tile<T, BY, NS, FS>;

@@ -224,6 +224,7 @@ private:
         for (const auto& kv : s.terms()) {
             const auto& k = kv.first;
             if (k.kind == 0) os << " + " << kv.second << "*U" << k.a << "(" << k.b << "," << k.c << "," << k.d << ")";
+            else if (k.kind == 2) os << " + " << kv.second << "*U" << k.a << "(0,0,0)^" << k.b;
             else os << " + " << kv.second << "*K" << k.a << (k.b ? "(old)" : "(new)");
         }
         if (s.bad()) os << " [non-linear]";
@@ -251,6 +252,7 @@ private:
         for (const auto& kv : s.terms()) {
             const auto& k = kv.first;
             if (k.kind == 1) { F.known[{k.a, k.b}] += kv.second; continue; }
+            if (k.kind == 2) throw std::runtime_error("ScaFES::Problem: updateInner is not linear in the unknowns: " + describe(s));
             if (k.a != 0) throw std::runtime_error("ScaFES::Problem: updateInner couples several unknown fields");
             const int nz = (k.b != 0) + (k.c != 0) + (k.d != 0);
             const int mag = std::abs(k.b) + std::abs(k.c) + std::abs(k.d);
@@ -271,7 +273,7 @@ private:
 
     // The table rule of one border node's recorded form, or why there is
     // none: u_new = cu*u + sum_d cn[d]*u_d + cf*(the inner source)
-    //               + cg_old*G(old) + cg_new*G(new), G one known field.
+    //               + cg_old*G(old) + cg_new*G(new) + cu4*u^4, G one known field.
     std::string tableRule(const gpu::Sym& s1, const gpu::Sym& s2, const Form& F, const std::vector<Affine>& aff,
                           int& gfield, scafes_border_form& r) const {
         if (!same(s1, s2)) return "the rule changes between time steps";
@@ -281,6 +283,12 @@ private:
         std::map<std::pair<int, int>, double> src;
         for (const auto& kv : s1.terms()) {
             const auto& k = kv.first;
+            if (k.kind == 2) {
+                if (k.a != 0) return "several unknown fields";
+                if (k.b != 4) return "a power of the node's unknown other than 1 and 4";
+                r.cu4 += kv.second;
+                continue;
+            }
             if (k.kind == 0) {
                 if (k.a != 0) return "several unknown fields";
                 const int nz = (k.b != 0) + (k.c != 0) + (k.d != 0);
@@ -330,6 +338,80 @@ private:
         }
     }
 
+    // Known field f as a polynomial of degree <= 4 in
+    //   s = (time(t) - t_center) * t_rate,  s in [-1, 1] over steps 0..T
+    // (the device's time basis of G, scafes_gpu_set_border_time_basis):
+    // interpolation at five Chebyshev points of the run, rounded to steps,
+    // checked at three other steps.  Fills mGa, mGb, mGhi and the basis, or
+    // throws if the field is not such a polynomial (to 1e-11 relative).
+    void fitTimePolynomial(int f) {
+        const int T = mParams.nTimesteps();
+        const double ta = time(0), tb = time(T);
+        mGcenter = 0.5 * (ta + tb);
+        mGrate = tb > ta ? 2.0 / (tb - ta) : 1.0;
+        std::vector<int> steps;
+        if (T <= 4) {
+            for (int k = 0; k <= T; ++k) steps.push_back(k);
+        } else {
+            const double pi = 3.14159265358979323846;
+            for (int j = 0; j < 5; ++j)
+                steps.push_back((int)std::lround(0.5 * T * (1.0 - std::cos((2 * j + 1) * pi / 10.0))));
+        }
+        const int np = (int)steps.size();
+        // Inverse of the Vandermonde matrix V[j][k] = s_j^k (Gauss-Jordan,
+        // partial pivoting; at most 5 x 5).
+        double V[5][10] = {};
+        for (int j = 0; j < np; ++j) {
+            const double sj = (time(steps[j]) - mGcenter) * mGrate;
+            double pw = 1.0;
+            for (int k = 0; k < np; ++k, pw *= sj) V[j][k] = pw;
+            V[j][np + j] = 1.0;
+        }
+        for (int c = 0; c < np; ++c) {
+            int piv = c;
+            for (int r = c + 1; r < np; ++r)
+                if (std::fabs(V[r][c]) > std::fabs(V[piv][c])) piv = r;
+            if (V[piv][c] == 0.0) throw std::runtime_error("ScaFES::Problem: time samples of a border field coincide");
+            for (int k = 0; k < 2 * np; ++k) std::swap(V[c][k], V[piv][k]);
+            const double d = V[c][c];
+            for (int k = 0; k < 2 * np; ++k) V[c][k] /= d;
+            for (int r = 0; r < np; ++r) {
+                if (r == c || V[r][c] == 0.0) continue;
+                const double q = V[r][c];
+                for (int k = 0; k < 2 * np; ++k) V[r][k] -= q * V[c][k];
+            }
+        }
+        std::vector<double> co[5];
+        for (int k = 0; k < 5; ++k) co[k].assign((std::size_t)mN, 0.0);
+        std::vector<double> vmax((std::size_t)mN, 1.0);
+        for (int j = 0; j < np; ++j) {
+            evalKnownAt(steps[j]);
+            for (long long m = 0; m < mN; ++m) {
+                const double v = (double)mKnownNewStore[f * mN + m];
+                vmax[m] = std::max(vmax[m], std::fabs(v));
+                for (int k = 0; k < np; ++k) co[k][m] += V[k][np + j] * v;
+            }
+        }
+        if (T > 4) {
+            for (int t : {1, T / 3, (2 * T) / 3 + 1}) {
+                evalKnownAt(t);
+                const double st = (time(t) - mGcenter) * mGrate;
+                for (long long m = 0; m < mN; ++m) {
+                    double p = co[4][m];
+                    for (int k = 3; k >= 0; --k) p = std::fma(p, st, co[k][m]);
+                    const double v = (double)mKnownNewStore[f * mN + m];
+                    if (std::fabs(p - v) > 1e-11 * vmax[m])
+                        throw std::runtime_error("ScaFES::Problem: border field " + mNames[f] +
+                                                 " is neither affine nor a polynomial of degree <= 4 in time");
+                }
+            }
+        }
+        mGa.swap(co[0]);
+        mGb.swap(co[1]);
+        for (int k = 0; k < 3; ++k) mGhi[k].swap(co[2 + k]);
+        mGpoly = true;
+    }
+
     int precisionCode() const {
         const std::string& p = mParams.gpuPrecision();
         if (p == "f64") return SCAFES_PREC_F64;
@@ -350,6 +432,9 @@ private:
     bool mPrepared = false;
     scafes_cfg mCfg = {};
     std::vector<double> mFa, mFb, mGa, mGb;
+    std::vector<double> mGhi[3];       // G_C .. G_E of a polynomial-in-time border field
+    bool mGpoly = false;
+    double mGcenter = 0.0, mGrate = 1.0;
     scafes_border_form mForms[SCAFES_BORDER_CLASSES] = {};
     std::vector<ScaFES::WriteHowOften> mWriteToFile;
     std::string mSnapshotFile;
@@ -555,10 +640,12 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     if (has_fb) mFb.swap(fb);
     if (border == SCAFES_BORDER_TABLE && tab_g >= 0) {
         const Affine& A = aff[tab_g];
-        if (A.a.empty())
-            throw std::runtime_error("ScaFES::Problem: border field " + mNames[tab_g] + " is not affine in time");
-        mGa = A.a;
-        if (A.timed) mGb = A.b;
+        if (A.a.empty()) {
+            fitTimePolynomial(tab_g);
+        } else {
+            mGa = A.a;
+            if (A.timed) mGb = A.b;
+        }
     }
     bool table_reads_f = false;
     if (border == SCAFES_BORDER_TABLE)
@@ -580,6 +667,12 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
        << " source=" << (has_f ? (has_fb ? "affine" : "static") : "none")
        << " border=" << (border == SCAFES_BORDER_DIRICHLET ? "dirichlet"
                          : border == SCAFES_BORDER_MIRROR_POW2 ? "mirror" : "table");
+    if (mGpoly) os << " G=quartic-in-time";
+    if (border == SCAFES_BORDER_TABLE) {
+        bool u4 = false;
+        for (int c = 1; c < SCAFES_BORDER_CLASSES; ++c) u4 = u4 || mForms[c].cu4 != 0.0;
+        if (u4) os << " u^4";
+    }
     mSummary = os.str();
     mPrepared = true;
 }
@@ -598,6 +691,11 @@ void Problem<OWNPRBLM, CT, DIM>::iterateOverTime() {
     if (!mFb.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_F_B, mFb.data(), mFb.size()));
     if (!mGa.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_G_A, mGa.data(), mGa.size()));
     if (!mGb.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_G_B, mGb.data(), mGb.size()));
+    if (mGpoly) {
+        for (int k = 0; k < 3; ++k)
+            check(scafes_gpu_upload(mHandle, SCAFES_FIELD_G_C + k, mGhi[k].data(), mGhi[k].size()));
+        check(scafes_gpu_set_border_time_basis(mHandle, mGcenter, mGrate));
+    }
     std::vector<double> u0(mUnknownNewStore.begin(), mUnknownNewStore.end());
     check(scafes_gpu_upload(mHandle, SCAFES_FIELD_U, u0.data(), u0.size()));
     int tile = cfg.tile;

@@ -5,12 +5,16 @@
 // ADOL-C's adouble (:5646-5652).  The drop-in Problem uses the same hook:
 // it instantiates updateInner<Sym> / updateBorder<Sym>, where reading
 // vOld[f](n) yields the symbol "unknown field f at offset n - centre", and
-// the arithmetic of the callback builds a linear form
-//     sum_k a_k * U_{f_k}(centre + d_k) + sum_j b_j * K_j(t or t-1) + c.
-// Anything that is not linear in the unknowns (a product of two
-// non-constant forms, a non-constant argument to pow/exp/...) marks the
-// form as non-linear; such a callback cannot be mapped to a stencil kernel
-// and the Problem refuses it with an error (there is no CPU fallback).
+// the arithmetic of the callback builds a form
+//     sum_k a_k * U_{f_k}(centre + d_k) + sum_j b_j * K_j(t or t-1) + c
+//     + sum_{p=2..4} e_p * U_f(centre)^p.
+// The powers of the node's own unknown come from products of forms that
+// hold nothing but that unknown (the u^4 radiative flux of
+// tests/system/PennesBioheatEqnFDM/Radiation/Radiation.hpp:146-159).  Any
+// other product of two non-constant forms, a power above 4, or a
+// non-constant argument to pow/exp/... marks the form as non-linear; such a
+// callback cannot be mapped to a stencil kernel and the Problem refuses it
+// with an error (there is no CPU fallback).
 //
 // Known fields enter through ScaFES::gpu::Known, the value returned by
 // knownDf/knownDfNew/knownDfOld: it carries both the numeric value (so the
@@ -27,7 +31,8 @@ namespace ScaFES {
 namespace gpu {
 
 // A term key: kind 0 = unknown field `a` at offset (b, c, d);
-//             kind 1 = known field `a` at time level `b` (0 new, 1 old).
+//             kind 1 = known field `a` at time level `b` (0 new, 1 old);
+//             kind 2 = unknown field `a` at the centre node, to the power b.
 struct TermKey {
     int kind, a, b, c, d;
     bool operator==(const TermKey& o) const {
@@ -82,7 +87,7 @@ public:
             *this = o;
             scale(k);
         } else {
-            bad_ = true;
+            *this = centre_product(*this, o);
         }
         return *this;
     }
@@ -103,6 +108,40 @@ public:
     Sym operator+() const { return *this; }
 
 private:
+    // Coefficients 0..4 of a form that is a polynomial in the centre unknown
+    // of one field; false for anything else.
+    static bool centre_poly(const Sym& s, int& field, double co[5]) {
+        if (s.bad_) return false;
+        field = -1;
+        for (int p = 0; p < 5; ++p) co[p] = 0.0;
+        co[0] = s.c_;
+        for (const auto& kv : s.t_) {
+            const TermKey& k = kv.first;
+            int power;
+            if (k.kind == 0 && k.b == 0 && k.c == 0 && k.d == 0) power = 1;
+            else if (k.kind == 2) power = k.b;
+            else return false;
+            if (field != -1 && k.a != field) return false;
+            field = k.a;
+            co[power] += kv.second;
+        }
+        return true;
+    }
+    static Sym centre_product(const Sym& a, const Sym& b) {
+        int fa, fb;
+        double ca[5], cb[5], cr[9] = {};
+        if (!centre_poly(a, fa, ca) || !centre_poly(b, fb, cb) || fa != fb) return nonlinear();
+        for (int i = 0; i < 5; ++i)
+            for (int j = 0; j < 5; ++j) cr[i + j] += ca[i] * cb[j];
+        for (int p = 5; p < 9; ++p)
+            if (cr[p] != 0.0) return nonlinear();
+        Sym r(cr[0]);
+        if (cr[1] != 0.0) r.t_.push_back({{0, fa, 0, 0, 0}, cr[1]});
+        for (int p = 2; p < 5; ++p)
+            if (cr[p] != 0.0) r.t_.push_back({{2, fa, p, 0, 0}, cr[p]});
+        return r;
+    }
+
     void add(const TermKey& k, double v) {
         for (auto& kv : t_) {
             if (kv.first == k) {
@@ -167,6 +206,11 @@ inline Sym abs(const Sym& a) { return fabs(a); }
 inline Sym pow(const Sym& a, const Sym& b) {
     if (a.is_const() && b.is_const()) return Sym(std::pow(a.constant(), b.constant()));
     if (b.is_const() && b.constant() == 1.0) return a;
+    if (b.is_const() && (b.constant() == 2.0 || b.constant() == 3.0 || b.constant() == 4.0)) {
+        Sym r = a;
+        for (int p = 1; p < (int)b.constant(); ++p) r *= a;  // non-linear unless a is the centre unknown
+        return r;
+    }
     return Sym::nonlinear();
 }
 

@@ -69,6 +69,8 @@ def lib():
         L.orc_pennes_mri.argtypes = [C.POINTER(Grid)] + [C.c_double] * 7 + [dp, dp, C.c_int, dp, C.c_int]
         L.orc_heat_flux.argtypes = [C.POINTER(Grid)] + [C.c_double] * 6 + [C.c_int, C.c_int, dp, Known, Known,
                                                                          Known, C.c_int]
+        L.orc_heat_radiation.argtypes = [C.POINTER(Grid)] + [C.c_double] * 7 + [C.c_int, dp, Known, Known,
+                                                                              Known, C.c_int]
         L.orc_stencil_width_one.argtypes = [C.POINTER(Grid), C.c_int, dp, C.c_int]
         L.orc_stencil_width_var.argtypes = [C.POINTER(Grid), C.c_int, C.c_int, dp, C.c_int]
         L.orc_kheat_forward.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.c_int]
@@ -146,6 +148,18 @@ def heat_flux(g: Grid, u0, nsteps, kind, coeff_a=1.0, rho_c=1.0, perf_q1=0.0, pe
     ks = [Known(_p(b), k[1], k[2], k[3]) for b, k in zip(keep, (f, g_dir, g_flux))]
     _check(lib().orc_heat_flux(C.byref(g), coeff_a, rho_c, perf_q1, perf_w, lam, alpha, kind, nsteps,
                                _p(u), ks[0], ks[1], ks[2], nthreads), "heat_flux")
+    return u
+
+
+def heat_radiation(g: Grid, u0, nsteps, coeff_a=1.0, rho_c=1.0, perf_q1=0.0, perf_w=0.0, lam=1.0,
+                   epsilon=1.0, sigma=1.0, f=(None, 0, 1.0, 0.0), g_dir=(None, 0, 1.0, 0.0),
+                   g_flux=(None, 0, 1.0, 0.0), nthreads=0):
+    """Radiation border (Radiation.hpp); f, g_dir, g_flux as for heat_flux."""
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    keep = [np.ascontiguousarray(k[0], dtype=np.float64) if k[0] is not None else None for k in (f, g_dir, g_flux)]
+    ks = [Known(_p(b), k[1], k[2], k[3]) for b, k in zip(keep, (f, g_dir, g_flux))]
+    _check(lib().orc_heat_radiation(C.byref(g), coeff_a, rho_c, perf_q1, perf_w, lam, epsilon, sigma, nsteps,
+                                    _p(u), ks[0], ks[1], ks[2], nthreads), "heat_radiation")
     return u
 
 

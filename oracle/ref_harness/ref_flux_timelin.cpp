@@ -1,8 +1,9 @@
 // Reference driver run of a flux-border system test: the TimeLinSpaceLin
 // problem of tests/system/HeatEqnFDM/{Neumann,Cauchy} or
-// tests/system/PennesBioheatEqnFDM/{Neumann,Cauchy} -- which one is chosen
-// by the include path the Makefile gives (each directory defines its own
-// TimeLinSpaceLin class on top of its Neumann.hpp / Cauchy.hpp).  Same field
+// tests/system/PennesBioheatEqnFDM/{Neumann,Cauchy,Radiation} -- which one
+// is chosen by the include path the Makefile gives (each directory defines
+// its own TimeLinSpaceLin class on top of its Neumann.hpp / Cauchy.hpp /
+// Radiation.hpp).  Same field
 // set as the reference's main3D.cpp of those directories.
 #include "harness.hpp"
 #include "TimeLinSpaceLin.hpp"

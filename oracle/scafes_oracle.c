@@ -92,6 +92,18 @@ static double known_at(orc_known kf, size_t m, double time)
         v += kf.b * tmp;
         return v;
     }
+    if (kf.form == 3) {
+        /* tests/system/PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin/
+         * TimeLinSpaceLin.hpp evalBorder, radiation nodes:
+         * G = ((1 + sum x)(1 + t))^4 * (SIGMA*EPSILON) + LAMBDA*(1+t)
+         * with base = 1 + sum x, a = SIGMA*EPSILON, b = LAMBDA. */
+        double v = kf.base[m];
+        v *= (1.0 + time);
+        v = v * v * v * v;
+        v *= kf.a;
+        v += kf.b * (1.0 + time);
+        return v;
+    }
     if (kf.form == 2) {
         /* tests/system/HeatEqnFDM/Cauchy/TimeLinSpaceLin/TimeLinSpaceLin.hpp
          * evalBorder, flux nodes: G = (1 + sum x) * (ALPHA*(1+t))
@@ -155,15 +167,16 @@ int orc_heat_dirichlet(const orc_grid* g, double coeff_a, double rho_c,
     return 0;
 }
 
-int orc_heat_flux(const orc_grid* g, double coeff_a, double rho_c, double perf_q1,
-                  double perf_w, double lambda, double alpha, int kind, int nsteps,
-                  double* u, orc_known f_src, orc_known g_dir, orc_known g_flux,
-                  int nthreads)
+/* kind 0 Neumann, 1 Cauchy (alpha), 2 Radiation (epsilon, sigma). */
+static int heat_flux_impl(const orc_grid* g, double coeff_a, double rho_c, double perf_q1,
+                          double perf_w, double lambda, double alpha, double epsilon,
+                          double sigma, int kind, int nsteps, double* u, orc_known f_src,
+                          orc_known g_dir, orc_known g_flux, int nthreads)
 {
     const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
     const int nn3[3] = {nx, ny, nz};
     const size_t nn = n_total(g);
-    if (kind != 0 && kind != 1) return -2;
+    if (kind < 0 || kind > 2) return -2;
     double* w = (double*)malloc(nn * sizeof(double));
     if (!w) return -1;
     const int use_perf = (perf_q1 != 0.0 || perf_w != 0.0);
@@ -192,8 +205,8 @@ int orc_heat_flux(const orc_grid* g, double coeff_a, double rho_c, double perf_q
                         un[m] = v;
                         continue;
                     }
-                    /* Neumann.hpp / Cauchy.hpp updateBorder: an index 0 in any
-                     * direction -> Dirichlet knownDf(1) (time t). */
+                    /* Neumann.hpp / Cauchy.hpp / Radiation.hpp updateBorder: an
+                     * index 0 in any direction -> Dirichlet knownDf(1) (time t). */
                     int at_min = 0;
                     for (int p = 0; p < g->dim; ++p)
                         if (idx[p] == 0) at_min = 1;
@@ -210,9 +223,15 @@ int orc_heat_flux(const orc_grid* g, double coeff_a, double rho_c, double perf_q
                         const double hp = g->h[p];
                         double s;
                         if (idx[p] == nn3[p] - 1) {
+                            const double um = uo[m];
                             if (kind == 0)
                                 s = uo[m - stride[p]] + uo[m - stride[p]] - ((2.0 * hp / lambda) * gold)
                                     - 2.0 * uo[m];
+                            else if (kind == 2)
+                                /* Radiation.hpp:146-159 */
+                                s = uo[m - stride[p]] + uo[m - stride[p]]
+                                    - ((2.0 * hp / lambda) * epsilon * sigma * um * um * um * um)
+                                    + ((2.0 * hp / lambda) * gold) - 2.0 * um;
                             else
                                 s = uo[m - stride[p]] + uo[m - stride[p]]
                                     - ((2.0 * hp / lambda) * alpha * uo[m])
@@ -233,6 +252,25 @@ int orc_heat_flux(const orc_grid* g, double coeff_a, double rho_c, double perf_q
     if (uo != u) memcpy(u, uo, nn * sizeof(double));
     free(w);
     return 0;
+}
+
+int orc_heat_flux(const orc_grid* g, double coeff_a, double rho_c, double perf_q1,
+                  double perf_w, double lambda, double alpha, int kind, int nsteps,
+                  double* u, orc_known f_src, orc_known g_dir, orc_known g_flux,
+                  int nthreads)
+{
+    if (kind != 0 && kind != 1) return -2;
+    return heat_flux_impl(g, coeff_a, rho_c, perf_q1, perf_w, lambda, alpha, 0.0, 0.0, kind,
+                          nsteps, u, f_src, g_dir, g_flux, nthreads);
+}
+
+int orc_heat_radiation(const orc_grid* g, double coeff_a, double rho_c, double perf_q1,
+                       double perf_w, double lambda, double epsilon, double sigma, int nsteps,
+                       double* u, orc_known f_src, orc_known g_dir, orc_known g_flux,
+                       int nthreads)
+{
+    return heat_flux_impl(g, coeff_a, rho_c, perf_q1, perf_w, lambda, 0.0, epsilon, sigma, 2,
+                          nsteps, u, f_src, g_dir, g_flux, nthreads);
 }
 
 int orc_pennes_mri(const orc_grid* g, double rho, double c, double k,

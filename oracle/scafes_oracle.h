@@ -50,6 +50,7 @@ void orc_coords(const orc_grid* g, int i, int j, int k, double* x);
  *           TimeLinSpaceLin/TimeLinSpaceLin.hpp:82-91 f, with
  *           a = RHO*C and b = RHO_BLOOD*C_BLOOD*W) */
 /*   form 2: base*(a*(1 + time)) + b*(1 + time)  (Cauchy flux field)   */
+/*   form 3: (base*(1 + time))^4 * a + b*(1 + time)  (Radiation field)  */
 typedef struct orc_known {
     const double* base;
     int form;
@@ -80,6 +81,16 @@ int orc_heat_flux(const orc_grid* g, double coeff_a, double rho_c, double perf_q
                   double perf_w, double lambda, double alpha, int kind, int nsteps,
                   double* u, orc_known f_src, orc_known g_dir, orc_known g_flux,
                   int nthreads);
+
+/* Pennes with the radiation border of tests/system/PennesBioheatEqnFDM/
+ * Radiation/Radiation.hpp:126-174: as orc_heat_flux, with the max-face
+ * flux - (2h/lambda) epsilon sigma u^4 + (2h/lambda) G in the reference's
+ * operation order.  Known-field form 3 is the radiation field of
+ * Radiation/TimeLinSpaceLin. */
+int orc_heat_radiation(const orc_grid* g, double coeff_a, double rho_c, double perf_q1,
+                       double perf_w, double lambda, double epsilon, double sigma, int nsteps,
+                       double* u, orc_known f_src, orc_known g_dir, orc_known g_flux,
+                       int nthreads);
 
 /* Variable-coefficient Pennes bioheat (examples/MRIDataPBHEqnFDM/
  * MRIDataPBHEqnFDM.hpp:143-169) with scalar rho, c, k, rho_b, c_b, omega,

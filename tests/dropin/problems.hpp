@@ -12,6 +12,10 @@
 //                 (KIND 0) or Cauchy (KIND 1) flux condition at the max faces,
 //                 exact solution (1+t)(1+x+y+z)
 //                 (tests/system/HeatEqnFDM/{Neumann,Cauchy}/TimeLinSpaceLin)
+//   PennesRadiation -- Pennes bioheat, Dirichlet at the min faces and the
+//                 radiation condition -lambda du/dn = eps sigma u^4 - G at the
+//                 max faces, G quartic in time, exact solution (1+t)(1+x+y+z)
+//                 (tests/system/PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin)
 #pragma once
 
 #include <cmath>
@@ -281,6 +285,84 @@ public:
                               (h * h);
             }
         }
+        vNew[0](n) += this->tau() * (1.0 / (RHO * C)) * this->knownDfOld(0, n);
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};
+
+template <typename CT, std::size_t DIM>
+class PennesRadiation : public ScaFES::Problem<PennesRadiation<CT, DIM>, CT, DIM> {
+    using Base = ScaFES::Problem<PennesRadiation<CT, DIM>, CT, DIM>;
+public:
+    using Base::Base;
+    const double RHO = 1.0, C = 1.0, LAMBDA = 1.0, RHO_B = 1.0, C_B = 1.0, W = 1.0, SIGMA = 1.0, EPS = 1.0;
+    bool onMin(const ScaFES::Ntuple<int, DIM>& n) const {
+        for (std::size_t p = 0; p < DIM; ++p)
+            if (n[p] == 0) return true;
+        return false;
+    }
+    double source(double s, double tt) const { return s * (RHO * C) + RHO_B * C_B * W * (s * (1.0 + tt)); }
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        const double s = HeatLin<CT, DIM>::lin(this->coordinates(n));
+        v[0](n) = source(s, this->time(t));
+        v[1](n) = 0.0;
+        v[2](n) = s * (1.0 + this->time(t));
+    }
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>& v, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        const double s = HeatLin<CT, DIM>::lin(this->coordinates(n));
+        const double tt = this->time(t), y = s * (1.0 + tt);
+        v[0](n) = source(s, tt);
+        v[1](n) = onMin(n) ? y : (y * y) * (y * y) * (SIGMA * EPS) + LAMBDA * (1.0 + tt);
+        v[2](n) = y;
+    }
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        v[0](n) = HeatLin<CT, DIM>::lin(this->coordinates(n)) * (1.0 + this->time(t));
+    }
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>& o, const ScaFES::Ntuple<int, DIM>& n, const int& t) {
+        initInner<TT>(v, o, n, t);
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        vNew[0](n) = vOld[0](n);
+        for (std::size_t p = 0; p < DIM; ++p)
+            vNew[0](n) += this->tau() * (LAMBDA / (RHO * C)) *
+                          (vOld[0](this->connect(n, 2 * p)) + vOld[0](this->connect(n, 2 * p + 1)) - 2.0 * vOld[0](n)) /
+                          (this->gridsize(p) * this->gridsize(p));
+        vNew[0](n) -= this->tau() * ((RHO_B * C_B) / (RHO * C)) * W * vOld[0](n);
+        vNew[0](n) += this->tau() * (1.0 / (RHO * C)) * this->knownDfOld(0, n);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                      const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        using std::pow;
+        if (onMin(n)) {
+            vNew[0](n) = this->knownDf(1, n);
+            return;
+        }
+        vNew[0](n) = vOld[0](n);
+        for (std::size_t p = 0; p < DIM; ++p) {
+            const double h = this->gridsize(p);
+            if (n[p] == this->nNodes(p) - 1) {
+                // Mirrored inner neighbour; radiative loss eps sigma u^4 and
+                // the border field enter as the flux.
+                const double k = 2.0 * h / LAMBDA;
+                vNew[0](n) += this->tau() * (LAMBDA / (RHO * C)) *
+                              (2.0 * vOld[0](this->connect(n, 2 * p)) - k * (EPS * SIGMA) * pow(vOld[0](n), 4.0) +
+                               k * this->knownDfOld(1, n) - 2.0 * vOld[0](n)) / (h * h);
+            } else {
+                vNew[0](n) += this->tau() * (LAMBDA / (RHO * C)) *
+                              (vOld[0](this->connect(n, 2 * p)) + vOld[0](this->connect(n, 2 * p + 1)) - 2.0 * vOld[0](n)) /
+                              (h * h);
+            }
+        }
+        vNew[0](n) -= this->tau() * ((RHO_B * C_B) / (RHO * C)) * W * vOld[0](n);
         vNew[0](n) += this->tau() * (1.0 / (RHO * C)) * this->knownDfOld(0, n);
     }
     template <typename TT>

@@ -62,6 +62,11 @@ int main(int argc, char** argv) {
             HeatFlux<double, 3, 1> p(params, gg, false, names, sw, known, {0, 0, 0}, {0, 0, 0}, wr, {false, false, true});
             return run(p, out, extract);
         }
+        if (which == "pennes_radiation") {
+            PennesRadiation<double, 3> p(params, gg, false, names, sw, known, {0, 0, 0}, {0, 0, 0}, wr,
+                                         {false, false, true});
+            return run(p, out, extract);
+        }
         if (which == "pennes_lin") {
             PennesLin<double, 3> p(params, gg, false, names, sw, known, {0, 0, 0}, {0, 0, 0}, wr, {false, false, true});
             return run(p, out, extract);

@@ -72,6 +72,15 @@ def main():
     r = O.run_ref("ref_heat_neumann", (10, 8, 6), 320, tmp)
     cases["heat_neumann_10x8x6"] = dict(n=(10, 8, 6), nsteps=320, t_end=1.0, final=r)
 
+    # Radiation border: tests/system/PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin/RUN_3D.sh.in
+    # (8^3, 50000 steps, t in [0,1]) plus a non-cubic grid.  The explicit u^4 flux bounds
+    # the step: at a corner the linearised factor is 1 - tau * 8 u^3 * sum_p 1/h_p, which
+    # must stay above -1 (u reaches 8; sum 1/h_p = 21 on both grids, so T > 43000).
+    r = O.run_ref("ref_pennes_radiation", n, 50000, tmp)
+    cases["pennes_radiation"] = dict(n=n, nsteps=50000, t_end=1.0, final=r)
+    r = O.run_ref("ref_pennes_radiation", (10, 8, 6), 60000, tmp)
+    cases["pennes_radiation_10x8x6"] = dict(n=(10, 8, 6), nsteps=60000, t_end=1.0, final=r)
+
     # tests/system/HeatEqnFdmStencilWidthVar/TESTMATRIX_RUN_3D.sh.in: 32^3, 20 steps.
     n, T = (32, 32, 32), 20
     r = O.run_ref("ref_stencil_width_var", n, T, tmp, nfields=3)

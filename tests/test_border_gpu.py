@@ -15,7 +15,7 @@ import pytest
 
 import cases
 import oracle as O
-from test_oracle_golden import flux_case
+from test_oracle_golden import flux_case, radiation_case
 
 pytestmark = pytest.mark.gpu
 
@@ -93,6 +93,76 @@ def test_flux_border_noisy(gpu, kind, prec):
     u = run_table(M, g, n, u0, T, kind, f, (gdir, 0, 1.0, -0.5), (gflx, 0, 0.5, 1.5), prec,
                   (coeff_a, 1.0, 0.0), lam=lam, alpha=alpha)
     assert cases.rel_err(u, ref) <= 1e-12, (kind, prec)
+
+
+# FP32 storage: one rounding of u (relative 6e-8, values up to 16) per step,
+# forgotten at the slowest diffusion rate (about 3 pi^2 per unit time, 6e-4
+# per step here) -- a worst-case bias bound of 3e-8 / 6e-4 = 5e-5.
+RAD_TOL = {"f64": 1e-12, "f32x2": 1e-12, "f32": 1e-4}
+
+
+def radiation_g(S, x0, t_center, t_rate):
+    """Coefficients G_A .. G_E in s = (t - t_center) * t_rate of the border
+    field of Radiation/TimeLinSpaceLin: S (1 + t) on min-face nodes,
+    S^4 (1 + t)^4 + (1 + t) elsewhere; 1 + t = A + B s."""
+    A, B = 1.0 + t_center, 1.0 / t_rate
+    binom = (1, 4, 6, 4, 1)
+    co = [S ** 4 * (binom[k] * A ** (4 - k) * B ** k) for k in range(5)]
+    co[0] = co[0] + A
+    co[1] = co[1] + B
+    dirichlet = [S * A, S * B, 0.0 * S, 0.0 * S, 0.0 * S]
+    return [np.where(x0, d, c) for d, c in zip(dirichlet, co)]
+
+
+@pytest.mark.parametrize("name", ["pennes_radiation", "pennes_radiation_10x8x6"])
+@pytest.mark.parametrize("basis", [(0.0, 1.0), (0.5, 2.0)])
+@pytest.mark.parametrize("prec", ["f64", "f32x2", "f32"])
+def test_radiation_border_golden(gpu, name, basis, prec):
+    """The reference's Radiation system test: u^4 flux weights from
+    scafes_border_forms_flux, the quartic-in-time border field as G_A .. G_E
+    in the time basis `basis`, against the reference's own final iterate."""
+    M = gpu
+    d, g, S, T = radiation_case(name)
+    n = tuple(d["n"])
+    shape = (n[2], n[1], n[0])
+    cfg = M.make_cfg(n, tau=g.tau, precision=M.PRECISIONS[prec], border=M.BORDER_TABLE, heat=(1.0, 1.0, 1.0))
+    forms = M.border_forms_flux(cfg, M.FLUX_RADIATION, 1.0, 1.0)
+    x0 = np.zeros(shape, dtype=bool)
+    x0[:, :, 0] = x0[:, 0, :] = x0[0, :, :] = True
+    fa, fb = affine((S, 1, 1.0, 1.0), shape)
+    with M.Plain(cfg) as p:
+        p.set_border_forms(forms)
+        p.set_border_time_basis(*basis)
+        p.upload(M.FIELD_F_A, fa)
+        p.upload(M.FIELD_F_B, fb)
+        for slot, c in zip((M.FIELD_G_A, M.FIELD_G_B, M.FIELD_G_C, M.FIELD_G_D, M.FIELD_G_E),
+                           radiation_g(S, x0, *basis)):
+            p.upload(slot, c)
+        p.upload(M.FIELD_U, S * 1.0)
+        p.step(T)
+        u = p.download()
+    assert np.all(np.isfinite(u))
+    assert cases.rel_err(u, d["final"]) <= RAD_TOL[prec], (name, basis, prec)
+
+
+def test_border_time_basis_rules(gpu):
+    """Higher time orders of G and a non-default basis are TABLE-only; a
+    zero rate is refused."""
+    M = gpu
+    n = (8, 8, 8)
+    dcfg = M.make_cfg(n, tau=1e-3, heat=(1.0, 1.0, 0.0))
+    with M.Plain(dcfg) as p:
+        p.upload(M.FIELD_U, np.zeros((8, 8, 8)))
+        with pytest.raises(M.ScafesError):
+            p.set_border_time_basis(0.0, 0.0)
+        p.upload(M.FIELD_G_C, np.ones((8, 8, 8)))
+        with pytest.raises(M.ScafesError):
+            p.step(1)
+    with M.Plain(dcfg) as p:
+        p.upload(M.FIELD_U, np.zeros((8, 8, 8)))
+        p.set_border_time_basis(1.0, 1.0)
+        with pytest.raises(M.ScafesError):
+            p.step(1)
 
 
 def test_border_table_errors(gpu):

@@ -87,17 +87,17 @@ def test_heat_coeffs_helper(native):
 def test_border_forms_flux_match_reference_rules(native):
     """scafes_border_forms_flux on the host: Dirichlet at min faces, the
     mirrored neighbour and the flux weight at max faces (Neumann.hpp /
-    Cauchy.hpp of the heat system tests)."""
+    Cauchy.hpp / Radiation.hpp of the system tests)."""
     M = native
     n = (10, 8, 6)
     cfg = M.make_cfg(n, tau=1e-3, border=M.BORDER_TABLE, heat=(1.0, 1.0, 0.0))
     h = [1.0 / (m - 1) for m in n]
-    for kind, alpha in ((M.FLUX_NEUMANN, 0.0), (M.FLUX_CAUCHY, 0.7)):
+    for kind, alpha in ((M.FLUX_NEUMANN, 0.0), (M.FLUX_CAUCHY, 0.7), (M.FLUX_RADIATION, 0.3)):
         F = M.border_forms_flux(cfg, kind, 2.0, alpha)
         for m in range(1, 64):
             r = F[m]
             if m & (1 | 4 | 16):
-                assert (r.cu, list(r.cn), r.cf, r.cg_old, r.cg_new) == (0.0, [0.0] * 6, 0.0, 0.0, 1.0)
+                assert (r.cu, list(r.cn), r.cf, r.cg_old, r.cg_new, r.cu4) == (0.0, [0.0] * 6, 0.0, 0.0, 1.0, 0.0)
                 continue
             flux = 0.0
             for p in range(3):
@@ -108,8 +108,12 @@ def test_border_forms_flux_match_reference_rules(native):
                     assert r.cn[2 * p] == r.cn[2 * p + 1] == cfg.cp[p]
             assert r.cf == cfg.cf and r.cg_new == 0.0
             if kind == M.FLUX_NEUMANN:
-                assert abs(r.cg_old + flux) < 1e-15 and r.cu == cfg.c0
-            else:
+                assert abs(r.cg_old + flux) < 1e-15 and r.cu == cfg.c0 and r.cu4 == 0.0
+            elif kind == M.FLUX_CAUCHY:
                 assert abs(r.cg_old - flux) < 1e-15 and abs(r.cu - (cfg.c0 - alpha * flux)) < 1e-15
+                assert r.cu4 == 0.0
+            else:
+                assert abs(r.cg_old - flux) < 1e-15 and r.cu == cfg.c0
+                assert abs(r.cu4 + alpha * flux) < 1e-15
     with pytest.raises(M.ScafesError):
         M.border_forms_flux(cfg, 7, 1.0, 1.0)

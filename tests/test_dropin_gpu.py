@@ -73,6 +73,20 @@ def test_dropin_flux_border_matches_reference(run_problem, tmp_path, name, golde
     assert cases.rel_err(u, d["final"]) <= 1e-12
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+@pytest.mark.parametrize("golden", ["pennes_radiation", "pennes_radiation_10x8x6"])
+def test_dropin_radiation_border_matches_reference(run_problem, tmp_path, golden, prec):
+    """The radiation border through the drop-in Problem: the u^4 flux is
+    recorded into the rule table and the quartic-in-time border field is
+    fitted in the device's time basis; against the reference's own final
+    iterate of Radiation/TimeLinSpaceLin."""
+    d = load_golden(golden)
+    n = tuple(int(v) for v in d["n"])
+    u, out = run(run_problem, "pennes_radiation", tmp_path / "u.bin", n, f"--nNodes={n[0]}x{n[1]}x{n[2]}",
+                 f"--nTimesteps={int(d['nsteps'])}", f"--endtime={float(d['t_end'])!r}", f"--gpuPrecision={prec}")
+    assert cases.rel_err(u, d["final"]) <= 1e-12
+
+
 def test_dropin_writes_snapshots_like_given_at_cl(gpu, run_problem, tmp_path):
     """writeToFile = LIKE_GIVEN_AT_CL with --nSnapshots=3 over 300 steps
     writes the unknown field at steps 0, 100, 200 and 300 (the reference's

@@ -31,6 +31,7 @@ def form(exe, *args):
     ("mirror_pow2", ["c0=0.285714", "source=none", "border=mirror"]),
     ("heat_neumann", ["c0=0.02 ", "source=static", "border=table"]),
     ("heat_cauchy", ["c0=0.02 ", "source=static", "border=table"]),
+    ("pennes_radiation", ["source=affine", "border=table", "G=quartic-in-time", "u^4"]),
 ])
 def test_extracted_form(run_problem, name, expect):
     s = form(run_problem, name, "/dev/null", "--extract-only", "--nNodes=8x8x8", "--nTimesteps=300", "--endtime=1")
@@ -51,7 +52,7 @@ REF_CASES = [
     (7, ["PennesBioheatEqnFDM", "PennesBioheatEqnFDM/Neumann", "PennesBioheatEqnFDM/Neumann/TimeLinSpaceLin"],
      "source=affine", "border=table"),
     (8, ["PennesBioheatEqnFDM", "PennesBioheatEqnFDM/Radiation",
-         "PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin"], "REFUSED", "not linear"),
+         "PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin"], "border=table G=quartic-in-time u^4", "source=affine"),
     (5, ["PropagationFromLeftLowerCorner"], "REFUSED", "branches on the value"),
 ]
 

@@ -142,6 +142,30 @@ def flux_case(name):
     return d, g, S, T, kind, f, g_flux, perf
 
 
+def radiation_case(name):
+    """Inputs of a radiation-border golden case (tests/system/
+    PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin/TimeLinSpaceLin.hpp: f as
+    in the Pennes Dirichlet case, G = (1 + sum x)(1 + t) at min-face nodes
+    and ((1 + sum x)(1 + t))^4 SIGMA EPSILON + LAMBDA (1 + t) elsewhere, with
+    LAMBDA = SIGMA = EPSILON = 1)."""
+    d = load_golden(name)
+    n, T = tuple(d["n"]), int(d["nsteps"])
+    g = O.make_grid(n, tau=float(d["t_end"]) / T)
+    x, y, z = O.coords(g)
+    S = np.broadcast_to(((1.0 + x) + y) + z, (n[2], n[1], n[0])).copy()
+    return d, g, S, T
+
+
+@pytest.mark.parametrize("name", ["pennes_radiation", "pennes_radiation_10x8x6"])
+def test_radiation_border_bit_exact(name):
+    d, g, S, T = radiation_case(name)
+    u = O.heat_radiation(g, S * 1.0, T, perf_q1=1.0, perf_w=1.0, f=(S, 1, 1.0, 1.0), g_dir=(S, 0, 1.0, 1.0),
+                         g_flux=(S, 3, 1.0, 1.0))
+    assert np.array_equal(u, d["final"])
+    exact = S * (1.0 + O.lib().orc_time(g, T))
+    assert np.max(np.abs(u - exact)) / np.max(np.abs(exact)) < 1e-13
+
+
 @pytest.mark.parametrize("name", ["heat_neumann", "heat_cauchy", "pennes_neumann", "pennes_cauchy",
                                   "heat_neumann_10x8x6"])
 def test_flux_border_bit_exact(name):
