@@ -101,7 +101,8 @@ enum scafes_border {
  * with neighbours d = x-, x+, y-, y+, z-, z+ (a neighbour outside the grid
  * must have weight 0).  A class is a 6-bit mask of the faces a node lies on:
  * bit 0 x == 0, bit 1 x == nx-1, bit 2 y == 0, bit 3 y == ny-1, bit 4
- * z == 0, bit 5 z == nz-1; entry 0 (inner nodes) is unused.  Dirichlet is
+ * z == 0, bit 5 z == nz-1; entry 0 is the rule of border nodes on no face
+ * (only with n_layers_at_border > 1, else unused).  Dirichlet is
  * cg_new = 1 with every other weight 0.  The u^4 term is the radiative
  * flux of tests/system/PennesBioheatEqnFDM/Radiation/Radiation.hpp. */
 typedef struct scafes_border_form {
@@ -140,7 +141,10 @@ typedef struct scafes_cfg {
     double coord_last[3];
     double tau;              /* time step size */
     double t_start;          /* time of iterate 0 */
-    int n_layers_at_border;  /* must be 1 (reference default) */
+    int n_layers_at_border;  /* nLayersAtBorder: nodes within this many of a
+                                face are border nodes (src/ScaFES_Problem.hpp:
+                                3952-3971); 1 (reference default) .. min(n)/2;
+                                the mirror border takes 1 only */
     int precision;           /* enum scafes_precision */
     int border;              /* enum scafes_border */
     int tile;                /* sweep tile variant 1..4, 0 = default
@@ -170,7 +174,8 @@ int scafes_star7_heat_coeffs(scafes_cfg* cfg, double coeff_a, double rho_c,
  *   - cp[p]*(2 h_p/lambda) * (alpha*u - G(time(t-1)))   (Cauchy)
  *   - cp[p]*(2 h_p/lambda) * (alpha*u^4 - G(time(t-1))) (Radiation)
  * (tests/system/HeatEqnFDM/Neumann/Neumann.hpp and Cauchy/Cauchy.hpp, the
- * Pennes variants add the perfusion already contained in c0). */
+ * Pennes variants add the perfusion already contained in c0).  Entry 0
+ * (border nodes on no face) gets the inner update. */
 int scafes_border_forms_flux(const scafes_cfg* cfg, int kind, double lambda,
                              double alpha, scafes_border_form forms[64]);
 

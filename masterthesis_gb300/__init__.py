@@ -131,7 +131,7 @@ def _dp(a: np.ndarray):
 
 def make_cfg(n, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), tau=0.0, t_start=0.0,
              precision="f64", border=BORDER_DIRICHLET, c0=None, cp=None, cf=0.0,
-             heat=None, stream=None, tile=0) -> Cfg:
+             heat=None, stream=None, tile=0, n_layers=1) -> Cfg:
     """Builds a scafes_cfg.  ``heat=(coeff_a, rho_c, perf)`` fills the heat /
     Pennes coefficients via scafes_star7_heat_coeffs; otherwise give c0/cp/cf."""
     c = Cfg()
@@ -140,7 +140,7 @@ def make_cfg(n, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), tau=0.0, t_start=0.
     c.coord_first[:] = list(first)
     c.coord_last[:] = list(last)
     c.tau, c.t_start = tau, t_start
-    c.n_layers_at_border = 1
+    c.n_layers_at_border = n_layers
     c.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     c.border = border
     c.tile = tile

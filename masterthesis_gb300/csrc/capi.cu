@@ -123,9 +123,15 @@ static int validate(const scafes_cfg* c) {
         if (c->n_nodes[p] < 3 || c->n_nodes[p] > (1 << 20))
             return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_create: n_nodes[%d]=%d out of range [3, 2^20]",
                         p, c->n_nodes[p]);
-    if (c->n_layers_at_border != 1)
+    int nmin = c->n_nodes[0];
+    for (int p = 1; p < 3; ++p) nmin = c->n_nodes[p] < nmin ? c->n_nodes[p] : nmin;
+    if (c->n_layers_at_border < 1 || 2 * c->n_layers_at_border > nmin)
+        return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_create: n_layers_at_border=%d out of [1, %d]",
+                    c->n_layers_at_border, nmin / 2);
+    if (c->n_layers_at_border != 1 && c->border == SCAFES_BORDER_MIRROR_POW2)
         return fail(nullptr, SCAFES_ERR_UNSUPPORTED,
-                    "scafes_gpu_create: n_layers_at_border=%d (only 1 is supported)", c->n_layers_at_border);
+                    "scafes_gpu_create: the mirror border is a one-layer rule (n_layers_at_border=%d)",
+                    c->n_layers_at_border);
     if (c->precision != SCAFES_PREC_F64 && c->precision != SCAFES_PREC_F32X2 &&
         c->precision != SCAFES_PREC_F32)
         return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: precision %d not supported", c->precision);
@@ -170,6 +176,7 @@ extern "C" int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out) {
     if (!h) return fail(nullptr, SCAFES_ERR_NOMEM, "scafes_gpu_create: out of host memory");
     h->cfg = *cfg;
     h->L = make_layout(cfg->n_nodes[0], cfg->n_nodes[1], cfg->n_nodes[2]);
+    h->L.nl = cfg->n_layers_at_border;
     h->esz = element_size(cfg->precision);
     const size_t bytes = (size_t)h->L.size() * h->esz;
     auto bail = [&](int code, const char* what, cudaError_t e) {
@@ -473,6 +480,9 @@ extern "C" int scafes_gpu_set_border_forms(scafes_handle* h, const scafes_border
             continue;  // a node cannot be on both faces of an axis (n >= 3)
         needs_f = needs_f || forms[m].cf != 0.0;
     }
+    // With more than one border layer, class 0 is the rule of the border
+    // nodes that lie on no face.
+    if (h->L.nl > 1) needs_f = needs_f || forms[0].cf != 0.0;
     if (!h->table) CUDA_TRY(h, cudaMalloc(&h->table, sizeof(BorderTable)));
     std::memcpy(h->table_host.rule, forms, sizeof(scafes_border_form) * SCAFES_BORDER_CLASSES);
     const int rc = sync_table(h);
@@ -505,7 +515,8 @@ extern "C" int scafes_border_forms_flux(const scafes_cfg* cfg, int kind, double 
     for (int m = 0; m < SCAFES_BORDER_CLASSES; ++m) {
         scafes_border_form& F = forms[m];
         F = scafes_border_form{};
-        if (m == 0) continue;
+        // Class 0 (border nodes on no face, n_layers_at_border > 1) takes
+        // the branch of the max-face classes with no face: the inner update.
         if (m & (1 | 4 | 16)) {  // on a min face: Dirichlet (the "index 0" branch of Neumann.hpp, Cauchy.hpp, Radiation.hpp)
             F.cg_new = 1.0;
             continue;

@@ -22,6 +22,8 @@ struct Layout {
     int nx, ny, nz;
     int pitch;          // elements per row
     long long plane;    // elements per z-plane (pitch * ny)
+    int nl;             // border layers: a node is a border node when it lies
+                        // within nl nodes of a face (nLayersAtBorder)
     __host__ __device__ long long idx(int i, int j, int k) const {
         return (long long)k * plane + (long long)j * pitch + i;
     }
@@ -33,6 +35,7 @@ inline Layout make_layout(int nx, int ny, int nz) {
     L.nx = nx; L.ny = ny; L.nz = nz;
     L.pitch = row_pitch(nx);
     L.plane = (long long)L.pitch * ny;
+    L.nl = 1;
     return L;
 }
 

@@ -163,10 +163,11 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
     }
 
     const bool xin = x < L.nx;
-    const bool xb = (x == 0 || x == L.nx - 1);
+    // Border nodes: within L.nl nodes of a face (src/ScaFES_Problem.hpp:3952-3971).
+    const bool xb = (x < L.nl || x > L.nx - 1 - L.nl);
     const bool has_gb = (J.gb != nullptr);
     // The whole 32 x BY tile holds inner columns: no per-node border tests.
-    const bool tile_inner = x0 >= 1 && x0 + BX <= L.nx - 1 && y0 >= 1 && y0 + BY <= L.ny - 1;
+    const bool tile_inner = x0 >= L.nl && x0 + BX <= L.nx - L.nl && y0 >= L.nl && y0 + BY <= L.ny - L.nl;
     const int cc = G::LP + tx;  // this thread's column inside a stage row
     auto slot = [&](int p) { return (b0 + (uint32_t)p) & (NS - 1); };
     auto phase = [&](int p) { return ((b0 + (uint32_t)p) / NS) & 1; };
@@ -193,7 +194,7 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
         const T* pa = st + sa * G::STRIDE + cc;
 #pragma unroll
         for (int k = 0; k < R; ++k) above[k] = pa[(rb + k) * G::W];
-        const bool zb = (z == 0 || z == L.nz - 1);
+        const bool zb = (z < L.nl || z > L.nz - 1 - L.nl);
         const T ym = pl[(rb - 1) * G::W];
         const T yp = pl[(rb + R) * G::W];
         // A plane that is not a z-border plane.  Every node takes the star;
@@ -222,7 +223,7 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 const long long off = o0 + (long long)k * L.pitch;
                 const int y = yb + k;
                 const bool live = INNER || (xin && y < L.ny);
-                if (!INNER && live && (xb || y == 0 || y == L.ny - 1)) {
+                if (!INNER && live && (xb || y < L.nl || y > L.ny - 1 - L.nl)) {
                     const T s = (k == 0) ? ym : cur[k - 1];
                     const T n = (k == R - 1) ? yp : cur[k + 1];
                     if (BORDER == SCAFES_BORDER_TABLE) {
@@ -262,7 +263,7 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                     const T n = (k == R - 1) ? yp : cur[k + 1];
                     const T w = pl[(rb + k) * G::W - 1];
                     const T e = pl[(rb + k) * G::W + 1];
-                    const bool border = xb || zb || y == 0 || y == L.ny - 1;
+                    const bool border = xb || zb || y < L.nl || y > L.ny - 1 - L.nl;
                     T v;
                     if (!border) {
                         T f = P::zero();

@@ -649,7 +649,7 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     }
     bool table_reads_f = false;
     if (border == SCAFES_BORDER_TABLE)
-        for (int c = 1; c < SCAFES_BORDER_CLASSES; ++c) table_reads_f = table_reads_f || mForms[c].cf != 0.0;
+        for (int c = 0; c < SCAFES_BORDER_CLASSES; ++c) table_reads_f = table_reads_f || mForms[c].cf != 0.0;
     if (table_reads_f && !has_f)
         throw std::runtime_error("ScaFES::Problem: updateBorder reads a source the inner update does not have");
     if (border == SCAFES_BORDER_DIRICHLET && gfield >= 0 && !aff[gfield].zero) {

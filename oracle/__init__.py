@@ -228,7 +228,7 @@ def ref_available(name: str) -> bool:
 
 def run_ref(name: str, n, nsteps, workdir, t_start=0.0, t_end=1.0, tau=0.0,
             first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), inputs=None, extra=(), nfields=1,
-            threads=1) -> np.ndarray:
+            threads=1, n_layers=1) -> np.ndarray:
     """Runs oracle/_ref/<name> and returns its final field(s), shape
     (nfields, nz, ny, nx) (or (nz, ny, nx) for one field)."""
     workdir = Path(workdir)
@@ -241,7 +241,7 @@ def run_ref(name: str, n, nsteps, workdir, t_start=0.0, t_end=1.0, tau=0.0,
         np.ascontiguousarray(inputs, dtype=np.float64).tofile(inp)
         args.append(str(inp))
     args += [repr(float(v)) for v in extra]
-    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), HARNESS_NLAYERS=str(n_layers))
     subprocess.run(args, check=True, capture_output=True, env=env)
     nz, ny, nx = n[2], n[1], n[0]
     v = np.fromfile(out, dtype=np.float64)

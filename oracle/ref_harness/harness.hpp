@@ -94,7 +94,9 @@ inline void apply(ScaFES::Parameters& p, const Config& c, int dim) {
     HARNESS_SET(p, mTimeIntervalEnd) = c.t_end;
     // src/ScaFES_Parameters.hpp:789 (tau from the interval when not given).
     HARNESS_SET(p, mTau) = (c.tau > 0.0) ? c.tau : (c.t_end - c.t_start) / c.nsteps;
-    HARNESS_SET(p, mNlayersAtBorder) = 1;
+    // nLayersAtBorder: 1 (the reference default) unless HARNESS_NLAYERS says otherwise.
+    const char* nl = std::getenv("HARNESS_NLAYERS");
+    HARNESS_SET(p, mNlayersAtBorder) = nl ? std::atoi(nl) : 1;
     HARNESS_SET(p, gOutputLevelMax) = 0;
     HARNESS_SET(p, gOutputLevelCurr) = 0;
 }

@@ -81,6 +81,15 @@ def main():
     r = O.run_ref("ref_pennes_radiation", (10, 8, 6), 60000, tmp)
     cases["pennes_radiation_10x8x6"] = dict(n=(10, 8, 6), nsteps=60000, t_end=1.0, final=r)
 
+    # nLayersAtBorder > 1 (src/ScaFES_Problem.hpp:3952-3971): the same system tests with
+    # two or three border layers on a 12x10x9 grid (steps within the stability limits).
+    nb = (12, 10, 9)
+    for name, ref, T, nl in (("heat_timelin_nl2", "ref_heat_timelin", 800, 2),
+                             ("heat_neumann_nl3", "ref_heat_neumann", 800, 3),
+                             ("pennes_radiation_nl2", "ref_pennes_radiation", 60000, 2)):
+        r = O.run_ref(ref, nb, T, tmp, n_layers=nl)
+        cases[name] = dict(n=nb, nsteps=T, t_end=1.0, n_layers=nl, final=r)
+
     # tests/system/HeatEqnFdmStencilWidthVar/TESTMATRIX_RUN_3D.sh.in: 32^3, 20 steps.
     n, T = (32, 32, 32), 20
     r = O.run_ref("ref_stencil_width_var", n, T, tmp, nfields=3)

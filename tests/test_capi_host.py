@@ -50,7 +50,9 @@ def _create(M, **kw):
     (dict(dim=2), -4),
     (dict(n_nodes=(2, 8, 8)), -1),
     (dict(n_nodes=(8, 8, 0)), -1),
-    (dict(n_layers_at_border=2), -4),
+    (dict(n_layers_at_border=0), -1),
+    (dict(n_layers_at_border=5), -1),             # more than half of the smallest axis (8)
+    (dict(n_layers_at_border=2, border=1), -4),   # the mirror rule has one layer
     (dict(precision=17), -4),
     (dict(border=9), -4),
     (dict(tile=5), -1),

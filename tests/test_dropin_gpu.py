@@ -87,6 +87,19 @@ def test_dropin_radiation_border_matches_reference(run_problem, tmp_path, golden
     assert cases.rel_err(u, d["final"]) <= 1e-12
 
 
+@pytest.mark.parametrize("name,golden", [("heat_lin", "heat_timelin_nl2"), ("heat_neumann", "heat_neumann_nl3"),
+                                         ("pennes_radiation", "pennes_radiation_nl2")])
+def test_dropin_border_layers_match_reference(run_problem, tmp_path, name, golden):
+    """--nLayersAtBorder=2/3: the drop-in classifies border nodes by layer
+    and records a rule for the border nodes on no face (class 0)."""
+    d = load_golden(golden)
+    n = tuple(int(v) for v in d["n"])
+    u, out = run(run_problem, name, tmp_path / "u.bin", n, f"--nNodes={n[0]}x{n[1]}x{n[2]}",
+                 f"--nTimesteps={int(d['nsteps'])}", f"--endtime={float(d['t_end'])!r}",
+                 f"--nLayersAtBorder={int(d['n_layers'])}", "--gpuPrecision=f64")
+    assert cases.rel_err(u, d["final"]) <= 1e-12
+
+
 def test_dropin_writes_snapshots_like_given_at_cl(gpu, run_problem, tmp_path):
     """writeToFile = LIKE_GIVEN_AT_CL with --nSnapshots=3 over 300 steps
     writes the unknown field at steps 0, 100, 200 and 300 (the reference's

@@ -166,6 +166,37 @@ def test_radiation_border_bit_exact(name):
     assert np.max(np.abs(u - exact)) / np.max(np.abs(exact)) < 1e-13
 
 
+def layers_case(name):
+    """Inputs of a golden case with nLayersAtBorder > 1: the TimeLinSpaceLin
+    problems of HeatEqnFDM/Dirichlet, HeatEqnFDM/Neumann and
+    PennesBioheatEqnFDM/Radiation with two or three border layers."""
+    d = load_golden(name)
+    n, T, nl = tuple(d["n"]), int(d["nsteps"]), int(d["n_layers"])
+    g = O.make_grid(n, tau=float(d["t_end"]) / T, n_layers=nl)
+    x, y, z = O.coords(g)
+    S = np.broadcast_to(((1.0 + x) + y) + z, (n[2], n[1], n[0])).copy()
+    return d, g, S, T, nl
+
+
+def layers_oracle(name, g, S, T):
+    if name.startswith("heat_timelin"):
+        return O.heat_dirichlet(g, S * 1.0, T, f_base=S, g_base=S, g_a=1.0, g_b=1.0)
+    if name.startswith("heat_neumann"):
+        return O.heat_flux(g, S * 1.0, T, 0, f=(S, 0, 1.0, 0.0), g_dir=(S, 0, 1.0, 1.0),
+                           g_flux=(np.full(S.shape, -1.0), 0, 1.0, 1.0))
+    return O.heat_radiation(g, S * 1.0, T, perf_q1=1.0, perf_w=1.0, f=(S, 1, 1.0, 1.0), g_dir=(S, 0, 1.0, 1.0),
+                            g_flux=(S, 3, 1.0, 1.0))
+
+
+@pytest.mark.parametrize("name", ["heat_timelin_nl2", "heat_neumann_nl3", "pennes_radiation_nl2"])
+def test_border_layers_bit_exact(name):
+    d, g, S, T, nl = layers_case(name)
+    u = layers_oracle(name, g, S, T)
+    assert np.array_equal(u, d["final"])
+    exact = S * (1.0 + O.lib().orc_time(g, T))
+    assert np.max(np.abs(u - exact)) / np.max(np.abs(exact)) < 1e-13
+
+
 @pytest.mark.parametrize("name", ["heat_neumann", "heat_cauchy", "pennes_neumann", "pennes_cauchy",
                                   "heat_neumann_10x8x6"])
 def test_flux_border_bit_exact(name):
