@@ -405,6 +405,7 @@ static const CUtensorMap* source_map(scafes_handle* h, int tile) {
 }
 
 static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
+    if (h->L.nl != 1) tile = STAR7_MULTI_LAYER_TILE;  // the only variant built for several layers
     Star7Launch a;
     a.precision = h->cfg.precision;
     a.border = h->cfg.border;

@@ -12,6 +12,9 @@ namespace scafes {
 // Number of CTA tile variants of the plain sweep (32 x BY columns, R rows
 // per thread): {8,1}, {16,2}, {32,4}, {16,4}.
 constexpr int STAR7_NUM_TILES = 4;
+// The one tile variant built for more than one border layer; a launch with
+// L.nl != 1 must use it (its TMA descriptors are encoded for that tile).
+constexpr int STAR7_MULTI_LAYER_TILE = 1;
 
 // Coefficients of u_new = c0*u + sum_p cp*(u_{p-}+u_{p+}) + cf*F, in double
 // and split into FP32 triples (hi + lo + lo2, ~72 bits) for the

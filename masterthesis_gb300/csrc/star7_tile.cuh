@@ -128,7 +128,7 @@ enum : int { SRC_NONE = 0, SRC_A = 1, SRC_AB = 2 };
 // and phase of every plane); it is advanced by the planes this tile used.
 // Returns false (and records SCAFES_ERR_TIMEOUT) when a stage never
 // arrived; the caller must then stop.
-template <class P, int SRC, int BORDER, int BY, int R, int NS, bool FS>
+template <class P, int SRC, int BORDER, int BY, int R, int NS, bool FS, bool ML = false>
 __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, const Star7Coeffs& c,
                                            int x0, int y0, int z0, int z1,
                                            typename P::T* st, uint64_t* bar, uint32_t& base,
@@ -163,11 +163,15 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
     }
 
     const bool xin = x < L.nx;
-    // Border nodes: within L.nl nodes of a face (src/ScaFES_Problem.hpp:3952-3971).
-    const bool xb = (x < L.nl || x > L.nx - 1 - L.nl);
+    // Border nodes: within nl nodes of a face (src/ScaFES_Problem.hpp:
+    // 3952-3971).  ML kernels read nl from the layout; the others are built
+    // for one layer, the reference's default, which keeps the tests out of
+    // the registers of the hot loop.
+    const int nl = ML ? L.nl : 1;
+    const bool xb = (x < nl || x > L.nx - 1 - nl);
     const bool has_gb = (J.gb != nullptr);
     // The whole 32 x BY tile holds inner columns: no per-node border tests.
-    const bool tile_inner = x0 >= L.nl && x0 + BX <= L.nx - L.nl && y0 >= L.nl && y0 + BY <= L.ny - L.nl;
+    const bool tile_inner = x0 >= nl && x0 + BX <= L.nx - nl && y0 >= nl && y0 + BY <= L.ny - nl;
     const int cc = G::LP + tx;  // this thread's column inside a stage row
     auto slot = [&](int p) { return (b0 + (uint32_t)p) & (NS - 1); };
     auto phase = [&](int p) { return ((b0 + (uint32_t)p) / NS) & 1; };
@@ -194,7 +198,7 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
         const T* pa = st + sa * G::STRIDE + cc;
 #pragma unroll
         for (int k = 0; k < R; ++k) above[k] = pa[(rb + k) * G::W];
-        const bool zb = (z < L.nl || z > L.nz - 1 - L.nl);
+        const bool zb = (z < nl || z > L.nz - 1 - nl);
         const T ym = pl[(rb - 1) * G::W];
         const T yp = pl[(rb + R) * G::W];
         // A plane that is not a z-border plane.  Every node takes the star;
@@ -223,7 +227,7 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 const long long off = o0 + (long long)k * L.pitch;
                 const int y = yb + k;
                 const bool live = INNER || (xin && y < L.ny);
-                if (!INNER && live && (xb || y < L.nl || y > L.ny - 1 - L.nl)) {
+                if (!INNER && live && (xb || y < nl || y > L.ny - 1 - nl)) {
                     const T s = (k == 0) ? ym : cur[k - 1];
                     const T n = (k == R - 1) ? yp : cur[k + 1];
                     if (BORDER == SCAFES_BORDER_TABLE) {
@@ -263,7 +267,7 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                     const T n = (k == R - 1) ? yp : cur[k + 1];
                     const T w = pl[(rb + k) * G::W - 1];
                     const T e = pl[(rb + k) * G::W + 1];
-                    const bool border = xb || zb || y < L.nl || y > L.ny - 1 - L.nl;
+                    const bool border = xb || zb || y < nl || y > L.ny - 1 - nl;
                     T v;
                     if (!border) {
                         T f = P::zero();

@@ -1,0 +1,10 @@
+// Sweep kernels of the PolF64 element type (see sweep_star7_impl.cuh).
+#include "sweep_star7_impl.cuh"
+
+namespace scafes {
+
+cudaError_t launch_star7_f64(const Star7Launch& a, cudaStream_t stream) {
+    return launch_prec<PolF64>(a, stream);
+}
+
+}  // namespace scafes

@@ -1,0 +1,136 @@
+// Sweep kernel template and its launch dispatch, included by one
+// translation unit per element type (sweep_star7_f64.cu, _f32x2.cu, _f32.cu)
+// so that the instantiations compile in parallel.
+#pragma once
+
+#include "star7_tile.cuh"
+
+namespace scafes {
+
+template <class P, int SRC, int BORDER, int BY, int R, int NS, bool FS, bool ML>
+__global__ void __launch_bounds__(BX * (BY / R))
+star7_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmf,
+          typename P::T* __restrict__ un,
+          const typename P::T* __restrict__ fa, const typename P::T* __restrict__ fb,
+          const typename P::T* __restrict__ ga, const typename P::T* __restrict__ gb, typename P::T gval,
+          Layout L, Star7Coeffs c, Split time_old, Split time_new,
+          Split corr, const BorderTable* __restrict__ table, int zchunk, int* __restrict__ status)
+{
+    using T = typename P::T;
+    using G = Tile<T, BY, NS, FS>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* st = reinterpret_cast<T*>(smem_raw);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NS * G::STRIDE * G::ESZ);
+    // After a sweep gave up on a TMA load (status set), the results are
+    // invalid until the host reads the status: later sweeps return at once
+    // instead of each waiting out its own limit.
+    if (__syncthreads_or(threadIdx.x == 0 && threadIdx.y == 0 && *(volatile int*)status != 0)) return;
+    ring_init<NS>(bar);
+    TileJob<T> J{&tm, &tmf, un, fa, fb, ga, gb, gval, L, time_old, time_new, corr, table};
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(z0 + zchunk, L.nz);
+    uint32_t base = 0;
+    star7_tile<P, SRC, BORDER, BY, R, NS, FS, ML>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
+}
+
+// ---- host side ---------------------------------------------------------------
+
+static int num_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// z-chunk length: 16 planes keep ~8 CTAs per SM streaming with two halo
+// planes per chunk; shorter chunks give enough CTAs on small grids.
+static int choose_zchunk(const Layout& L, int by) {
+    const long long tiles = (long long)((L.nx + BX - 1) / BX) * ((L.ny + by - 1) / by);
+    const long long want = (long long)num_sms() * 16;
+    int zc = 16;
+    while (zc > 4 && tiles * ((L.nz + zc - 1) / zc) < want) zc >>= 1;
+    return zc;
+}
+
+// A double as the element type of a precision (host side).
+static inline void to_elem(double d, double& out) { out = d; }
+static inline void to_elem(double d, float& out) { out = (float)d; }
+static inline void to_elem(double d, float2& out) {
+    f2 p = split_double(d);
+    out = make_float2(p.hi, p.lo);
+}
+
+template <class P, int SRC, int BORDER, int BY, int R, int NS0, bool ML>
+static cudaError_t launch_typed(const Star7Launch& a, cudaStream_t stream) {
+    using T = typename P::T;
+    constexpr bool FS = SRC == SRC_A;  // a source without a time term is staged with the iterate
+    constexpr int NS = ring_stages(NS0, FS);
+    using G = Tile<T, BY, NS, FS>;
+    const Layout& L = a.L;
+    if (FS && a.tm_f == nullptr) return cudaErrorInvalidValue;
+    auto kern = star7_tma<P, SRC, BORDER, BY, R, NS, FS, ML>;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
+        // The ring lives in shared memory: ask for the largest carveout so
+        // that occupancy is not capped by a small L1/shared split.
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             cudaSharedmemCarveoutMaxShared);
+        attr = true;
+    }
+    T gval;
+    to_elem(a.gconst, gval);
+    const int zchunk = choose_zchunk(L, BY);
+    dim3 block(BX, BY / R, 1);
+    dim3 grid((L.nx + BX - 1) / BX, (L.ny + BY - 1) / BY, (L.nz + zchunk - 1) / zchunk);
+    kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, FS ? *a.tm_f : *a.tm_uo, (T*)a.un, (const T*)a.fa, (const T*)a.fb, (const T*)a.ga,
+                                           (const T*)a.gb, gval, L,
+                                           a.c, make_split(a.time_old), make_split(a.time_new),
+                                           make_split(a.mirror_corr), a.table, zchunk, a.status);
+    return cudaGetLastError();
+}
+
+template <class P, int SRC, int BORDER>
+static cudaError_t launch_tile(const Star7Launch& a, cudaStream_t stream) {
+    if (a.L.nl != 1) {
+        // More than one border layer (rare; not a bandwidth case): one tile
+        // variant reads the layer count from the layout.  Its TMA boxes must
+        // be the ones the descriptors were encoded for, so any other tile is
+        // refused here rather than launched.
+        constexpr int T1 = STAR7_MULTI_LAYER_TILE;
+        if (BORDER == SCAFES_BORDER_MIRROR_POW2 || a.tile != T1) return cudaErrorInvalidValue;
+        return launch_typed<P, SRC, BORDER, kTiles[T1].by, kTiles[T1].r, kTiles[T1].ns, true>(a, stream);
+    }
+    switch (a.tile) {
+        case 0: return launch_typed<P, SRC, BORDER, kTiles[0].by, kTiles[0].r, kTiles[0].ns, false>(a, stream);
+        case 1: return launch_typed<P, SRC, BORDER, kTiles[1].by, kTiles[1].r, kTiles[1].ns, false>(a, stream);
+        case 2: return launch_typed<P, SRC, BORDER, kTiles[2].by, kTiles[2].r, kTiles[2].ns, false>(a, stream);
+        case 3: return launch_typed<P, SRC, BORDER, kTiles[3].by, kTiles[3].r, kTiles[3].ns, false>(a, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <class P, int BORDER>
+static cudaError_t launch_src(const Star7Launch& a, cudaStream_t stream) {
+    if (a.fa == nullptr || a.c.cf == 0.0) return launch_tile<P, SRC_NONE, BORDER>(a, stream);
+    if (a.fb == nullptr) return launch_tile<P, SRC_A, BORDER>(a, stream);
+    return launch_tile<P, SRC_AB, BORDER>(a, stream);
+}
+
+template <class P>
+cudaError_t launch_prec(const Star7Launch& a, cudaStream_t stream) {
+    switch (a.border) {
+        case SCAFES_BORDER_DIRICHLET: return launch_src<P, SCAFES_BORDER_DIRICHLET>(a, stream);
+        case SCAFES_BORDER_MIRROR_POW2: return launch_src<P, SCAFES_BORDER_MIRROR_POW2>(a, stream);
+        case SCAFES_BORDER_TABLE:
+            if (a.table == nullptr) return cudaErrorInvalidValue;
+            return launch_src<P, SCAFES_BORDER_TABLE>(a, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace scafes
