@@ -350,6 +350,27 @@ int scafes_batch_info(const scafes_batch* b, int* n_items, int* launches,
 const char* scafes_batch_last_error(const scafes_batch* b);
 void scafes_batch_destroy(scafes_batch* b);
 
+/* The same ensemble assembled one instance at a time, the shape of the
+ * reference's callers that start one run per parameter set
+ * (examples/MRIDataPBHEqnFDM/startMCMCFit.py): create, enqueue every
+ * instance with its initial iterate u0 and source f (n_nodes values each,
+ * x fastest; f may be NULL for F = 0), then run.  The first run builds one
+ * scafes_batch from the enqueued instances (enqueue after it is refused)
+ * and every run advances all instances by n_steps (scafes_batch_step). */
+typedef struct scafes_gpu_batch scafes_gpu_batch;
+int scafes_gpu_batch_create(int precision, void* stream, scafes_gpu_batch** out);
+int scafes_gpu_batch_enqueue(scafes_gpu_batch* q, const scafes_batch_instance* inst,
+                             const double* u0, const double* f, int* index);
+int scafes_gpu_batch_run(scafes_gpu_batch* q, int n_steps);
+/* The current iterate of instance `index` (synchronises the stream). */
+int scafes_gpu_batch_download(scafes_gpu_batch* q, int index, double* host,
+                              size_t n);
+/* The underlying ensemble once the first run built it (else NULL), for
+ * scafes_batch_autotune / _last_ms / _info. */
+scafes_batch* scafes_gpu_batch_ensemble(scafes_gpu_batch* q);
+const char* scafes_gpu_batch_last_error(const scafes_gpu_batch* q);
+void scafes_gpu_batch_destroy(scafes_gpu_batch* q);
+
 /* ---- multi-field leapfrog workloads -------------------------------------
  *
  * Problems with several unknown fields and a second ("leapfrog") update
@@ -447,6 +468,12 @@ int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps,
 int scafes_adj_gradient(scafes_adj* a, const double* u0, const double* target,
                         int n_steps, double* J, double* grad_k,
                         double* grad_u0, size_t n);
+/* The backward entry for any objective of u_T: given the forward solve
+ * from u0 over n_steps and the cotangent dJ_duT = dJ/du_T (n values),
+ * writes dJ/dk and dJ/du0 (the vector-Jacobian product of u0, k -> u_T),
+ * with the same checkpoint schedule as scafes_adj_gradient. */
+int scafes_adj_backward(scafes_adj* a, const double* u0, const double* dJ_duT,
+                        int n_steps, double* grad_k, double* grad_u0, size_t n);
 /* ms of the last forward solve and gradient, forward steps the last call
  * ran (including recomputation), adjoint steps, snapshots. */
 int scafes_adj_stats(const scafes_adj* a, float* forward_ms, float* gradient_ms,

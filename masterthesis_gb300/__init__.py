@@ -286,6 +286,64 @@ def batch_instance(n, tau, coeff_a, rho_c=1.0, perf=0.0, g_value=0.0,
     return bi
 
 
+class BatchQueue:
+    """An ensemble assembled one instance at a time (owns a
+    scafes_gpu_batch: create / enqueue / run)."""
+
+    def __init__(self, precision="f64", stream=None):
+        L = lib()
+        if not getattr(L, "_q_set", False):
+            vp, dp = C.c_void_p, C.POINTER(C.c_double)
+            L.scafes_gpu_batch_create.argtypes = [C.c_int, vp, C.POINTER(vp)]
+            L.scafes_gpu_batch_enqueue.argtypes = [vp, C.POINTER(BatchInstance), dp, dp, C.POINTER(C.c_int)]
+            L.scafes_gpu_batch_run.argtypes = [vp, C.c_int]
+            L.scafes_gpu_batch_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
+            L.scafes_gpu_batch_ensemble.argtypes = [vp]
+            L.scafes_gpu_batch_ensemble.restype = vp
+            L.scafes_gpu_batch_last_error.argtypes = [vp]
+            L.scafes_gpu_batch_last_error.restype = C.c_char_p
+            L.scafes_gpu_batch_destroy.argtypes = [vp]
+            L.scafes_gpu_batch_destroy.restype = None
+            L._q_set = True
+        prec = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        h = C.c_void_p()
+        _check(L.scafes_gpu_batch_create(prec, stream, C.byref(h)))
+        self.h = h
+        self.shapes = []
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise ScafesError(rc, (lib().scafes_gpu_batch_last_error(self.h) or b"").decode())
+
+    def enqueue(self, inst: BatchInstance, u0, f=None) -> int:
+        a = np.ascontiguousarray(u0, dtype=np.float64)
+        fa = None if f is None else np.ascontiguousarray(f, dtype=np.float64)
+        idx = C.c_int()
+        self._chk(lib().scafes_gpu_batch_enqueue(self.h, C.byref(inst), _dp(a), _dp(fa) if fa is not None else None,
+                                                 C.byref(idx)))
+        self.shapes.append((inst.n_nodes[2], inst.n_nodes[1], inst.n_nodes[0]))
+        return idx.value
+
+    def run(self, n_steps: int):
+        self._chk(lib().scafes_gpu_batch_run(self.h, n_steps))
+
+    def download(self, index: int) -> np.ndarray:
+        a = np.empty(self.shapes[index], dtype=np.float64)
+        self._chk(lib().scafes_gpu_batch_download(self.h, index, _dp(a), a.size))
+        return a
+
+    def close(self):
+        if self.h:
+            lib().scafes_gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 class Batch:
     """An ensemble of independent instances advanced together (owns a
     scafes_batch)."""
@@ -366,6 +424,7 @@ class Adjoint:
             L.scafes_adj_set_conductivity.argtypes = [vp, dp, C.c_size_t]
             L.scafes_adj_forward.argtypes = [vp, dp, C.c_int, dp, C.c_size_t]
             L.scafes_adj_gradient.argtypes = [vp, dp, dp, C.c_int, dp, dp, dp, C.c_size_t]
+            L.scafes_adj_backward.argtypes = [vp, dp, dp, C.c_int, dp, dp, C.c_size_t]
             L.scafes_adj_stats.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_float),
                                            C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_int)]
             L.scafes_adj_schedule_cost.argtypes = [C.c_int, C.c_int]
@@ -408,6 +467,14 @@ class Adjoint:
         J = C.c_double()
         self._chk(lib().scafes_adj_gradient(self.h, _dp(a), _dp(t), n_steps, C.byref(J), _dp(gk), _dp(gu), gk.size))
         return J.value, gk, gu
+
+    def backward(self, u0, dJ_duT, n_steps):
+        """dJ/dk and dJ/du0 for a given cotangent dJ/du_T (scafes_adj_backward)."""
+        a = np.ascontiguousarray(u0, dtype=np.float64)
+        s = np.ascontiguousarray(dJ_duT, dtype=np.float64)
+        gk, gu = np.empty(self.shape), np.empty(self.shape)
+        self._chk(lib().scafes_adj_backward(self.h, _dp(a), _dp(s), n_steps, _dp(gk), _dp(gu), gk.size))
+        return gk, gu
 
     def stats(self) -> dict:
         f, g = C.c_float(), C.c_float()

@@ -131,10 +131,12 @@ k_adjoint(const double* __restrict__ lam, double* __restrict__ lamn, const doubl
     }
 }
 
-// lambda_T = u_T - target: inner part into lam, border part into bnd;
-// per-CTA partial sums of 0.5 (u_T - target)^2 into part.
+// lambda_T = u_T - target (or the given cotangent when `seed`): inner part
+// into lam, border part into bnd; per-CTA partial sums of 0.5 (u_T -
+// target)^2 into part (0 when `seed`).
 __global__ void k_terminal(const double* __restrict__ uT, const double* __restrict__ target,
-                           double* __restrict__ lam, double* __restrict__ bnd, double* __restrict__ part, Layout L) {
+                           double* __restrict__ lam, double* __restrict__ bnd, double* __restrict__ part, Layout L,
+                           bool seed) {
     __shared__ double sh[AX * AY];
     const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
     double acc = 0.0;
@@ -142,8 +144,8 @@ __global__ void k_terminal(const double* __restrict__ uT, const double* __restri
         const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
         for (int z = 0; z < L.nz; ++z) {
             const long long o = L.idx(x, y, z);
-            const double d = uT[o] - target[o];
-            acc += 0.5 * d * d;
+            const double d = seed ? target[o] : uT[o] - target[o];
+            if (!seed) acc += 0.5 * d * d;
             const bool border = colb || z == 0 || z == L.nz - 1;
             lam[o] = border ? 0.0 : d;
             bnd[o] = border ? d : 0.0;
@@ -372,10 +374,11 @@ k_adjoint_x2(const float2* __restrict__ lam, float2* __restrict__ lamn, const fl
     }
 }
 
-// lambda_T = u_T - target (u_T pairs, target FP64): inner part into lam,
-// border part into bnd, per-CTA partial sums of J into part.
+// lambda_T = u_T - target or the cotangent (u_T pairs, target FP64): inner
+// part into lam, border part into bnd, per-CTA partial sums of J into part.
 __global__ void k_terminal_x2(const float2* __restrict__ uT, const double* __restrict__ target,
-                              float2* __restrict__ lam, float2* __restrict__ bnd, double* __restrict__ part, Layout L) {
+                              float2* __restrict__ lam, float2* __restrict__ bnd, double* __restrict__ part, Layout L,
+                              bool seed) {
     __shared__ double sh[AX * AY];
     const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
     double acc = 0.0;
@@ -383,8 +386,8 @@ __global__ void k_terminal_x2(const float2* __restrict__ uT, const double* __res
         const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
         for (int z = 0; z < L.nz; ++z) {
             const long long o = L.idx(x, y, z);
-            const double d = pjoin(uT[o]) - target[o];
-            acc += 0.5 * d * d;
+            const double d = seed ? target[o] : pjoin(uT[o]) - target[o];
+            if (!seed) acc += 0.5 * d * d;
             const bool border = colb || z == 0 || z == L.nz - 1;
             lam[o] = border ? make_float2(0.f, 0.f) : psplit(d);
             bnd[o] = border ? psplit(d) : make_float2(0.f, 0.f);
@@ -488,11 +491,12 @@ int fwd(scafes_adj* a, const double* src, double* dst) {
 }
 
 // lambda_T, the border part of dJ/du0 and the partial sums of J from u_T.
-int terminal(scafes_adj* a, const double* uT, const double* target, double* lam, double* Jpart) {
+int terminal(scafes_adj* a, const double* uT, const double* target, double* lam, double* Jpart, bool seed) {
     if (pairs(a))
-        k_terminal_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(uT), target, P2(lam), P2(a->bnd), Jpart, a->L);
+        k_terminal_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(uT), target, P2(lam), P2(a->bnd), Jpart, a->L,
+                                                                   seed);
     else
-        k_terminal<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(uT, target, lam, a->bnd, Jpart, a->L);
+        k_terminal<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(uT, target, lam, a->bnd, Jpart, a->L, seed);
     ATRY(a, cudaGetLastError());
     return SCAFES_OK;
 }
@@ -564,11 +568,12 @@ int schedule_slots(int n_snap, int n_steps) {
 
 struct Rev {
     scafes_adj* a;
-    const double* target;
+    const double* target;  // J's target, or dJ/du_T itself when `seed`
     int T;
     int cur;  // lambda buffer holding lambda_b
     bool started;
     double* Jpart;
+    bool seed;
 };
 
 int adj_step(Rev& R, const double* u_t) {
@@ -595,7 +600,7 @@ int reverse(Rev& R, int lo, int hi, int slot, int free) {
         if (!R.started) {
             // Bottom of the first descent: u_T from u_{T-1} gives J and lambda_T.
             if ((rc = fwd(a, snap(a, slot), a->u[0]))) return rc;
-            if ((rc = terminal(a, a->u[0], R.target, a->lam[R.cur], R.Jpart))) return rc;
+            if ((rc = terminal(a, a->u[0], R.target, a->lam[R.cur], R.Jpart, R.seed))) return rc;
             R.started = true;
         }
         return adj_step(R, snap(a, slot));
@@ -612,7 +617,7 @@ int reverse(Rev& R, int lo, int hi, int slot, int free) {
             }
             if (t == hi - 1 && !R.started) {
                 if ((rc = fwd(a, src, a->u[buf]))) return rc;
-                if ((rc = terminal(a, a->u[buf], R.target, a->lam[R.cur], R.Jpart))) return rc;
+                if ((rc = terminal(a, a->u[buf], R.target, a->lam[R.cur], R.Jpart, R.seed))) return rc;
                 R.started = true;
             }
             if ((rc = adj_step(R, src))) return rc;
@@ -769,12 +774,14 @@ extern "C" int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps, 
     return SCAFES_OK;
 }
 
-extern "C" int scafes_adj_gradient(scafes_adj* a, const double* u0, const double* target, int n_steps, double* J,
-                                   double* grad_k, double* grad_u0, size_t n) {
-    if (!a || !u0 || !target || !J || !grad_k || !grad_u0 || n_steps < 1)
-        return afail(a, SCAFES_ERR_ARG, "scafes_adj_gradient: bad arguments");
-    if (n != (size_t)a->L.nx * a->L.ny * a->L.nz) return afail(a, SCAFES_ERR_ARG, "scafes_adj_gradient: wrong size");
-    if (!a->have_k) return afail(a, SCAFES_ERR_STATE, "scafes_adj_gradient: set the conductivity first");
+// The reverse sweep from u0 over n_steps: `target` is J's target
+// (J = 0.5 |u_T - target|^2) or, with `seed`, the cotangent dJ/du_T.
+static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const double* target, bool seed,
+                         int n_steps, double* J, double* grad_k, double* grad_u0, size_t n) {
+    if (!a || !u0 || !target || !grad_k || !grad_u0 || n_steps < 1)
+        return afail(a, SCAFES_ERR_ARG, "%s: bad arguments", who);
+    if (n != (size_t)a->L.nx * a->L.ny * a->L.nz) return afail(a, SCAFES_ERR_ARG, "%s: wrong size", who);
+    if (!a->have_k) return afail(a, SCAFES_ERR_STATE, "%s: set the conductivity first", who);
     const int free = schedule_slots(a->n_snap, n_steps);
     build_schedule(a, n_steps, free);
     const size_t fb = field_bytes(a);
@@ -789,7 +796,7 @@ extern "C" int scafes_adj_gradient(scafes_adj* a, const double* u0, const double
     a->fwd_steps = 0;
     a->adj_steps = 0;
     ATRY(a, cudaEventRecord(a->e0, a->stream));
-    Rev R{a, a->work, n_steps, 0, false, a->part};
+    Rev R{a, a->work, n_steps, 0, false, a->part, seed};
     if ((rc = reverse(R, 0, n_steps, 0, free))) return rc;
     if (pairs(a))
         k_finalize_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(a->gx), P2(a->gy), P2(a->gz), P2(a->lam[R.cur]),
@@ -806,10 +813,23 @@ extern "C" int scafes_adj_gradient(scafes_adj* a, const double* u0, const double
     if ((rc = download_dense(a, a->u[1], grad_u0))) return rc;
     ATRY(a, cudaStreamSynchronize(a->stream));
     ATRY(a, cudaEventElapsedTime(&a->grad_ms, a->e0, a->e1));
-    double s = 0.0;
-    for (double v : part) s += v;
-    *J = s;
+    if (J) {
+        double s = 0.0;
+        for (double v : part) s += v;
+        *J = s;
+    }
     return SCAFES_OK;
+}
+
+extern "C" int scafes_adj_gradient(scafes_adj* a, const double* u0, const double* target, int n_steps, double* J,
+                                   double* grad_k, double* grad_u0, size_t n) {
+    if (!J) return afail(a, SCAFES_ERR_ARG, "scafes_adj_gradient: bad arguments");
+    return gradient_impl(a, "scafes_adj_gradient", u0, target, false, n_steps, J, grad_k, grad_u0, n);
+}
+
+extern "C" int scafes_adj_backward(scafes_adj* a, const double* u0, const double* dJ_duT, int n_steps,
+                                   double* grad_k, double* grad_u0, size_t n) {
+    return gradient_impl(a, "scafes_adj_backward", u0, dJ_duT, true, n_steps, nullptr, grad_k, grad_u0, n);
 }
 
 extern "C" int scafes_adj_stats(const scafes_adj* a, float* forward_ms, float* gradient_ms, long long* forward_steps,

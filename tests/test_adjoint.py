@@ -82,6 +82,39 @@ def test_adjoint_matches_oracle_all_snapshot_counts(gpu):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+def test_adjoint_backward_with_cotangent(gpu, prec):
+    """scafes_adj_backward (any dJ/du_T): with dJ/du_T = u_T - target it
+    gives scafes_adj_gradient's results bit for bit; for a random cotangent s
+    it is the vector-Jacobian product -- u_T is linear in u0, so
+    <s, u_T(u0 + d) - u_T(u0)> = <dJ/du0, d> to 1e-10 relative -- and it
+    matches the oracle's adjoint run with target u_T - s (1e-11 FP64,
+    1e-10 f32x2, as the other oracle comparisons)."""
+    M = gpu
+    n, T = (16, 12, 10), 30
+    k, tau, u0, target = kheat_problem(n, T, 21)
+    rng = np.random.default_rng(22)
+    s = rng.uniform(-1.0, 1.0, u0.shape)
+    d = rng.uniform(-1.0, 1.0, u0.shape)
+    with M.Adjoint(n, tau, 5, precision=prec) as a:
+        a.set_conductivity(k)
+        J, gk, gu = a.gradient(u0, target, T)
+        uT = a.forward(u0, T)
+        gk2, gu2 = a.backward(u0, uT - target, T)
+        assert np.array_equal(gk, gk2) and np.array_equal(gu, gu2)
+        gks, gus = a.backward(u0, s, T)
+        duT = a.forward(u0 + d, T) - uT
+    lhs, rhs = float(np.sum(s * duT)), float(np.sum(gus * d))
+    assert abs(lhs - rhs) <= 1e-10 * np.sum(np.abs(s * duT)), (lhs, rhs)
+    g = O.make_grid(n, tau=tau)
+    uT_ref, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
+    _, gk_ref, gu_ref = O.kheat_adjoint(g, k, traj, uT_ref - s)
+    tol = 1e-11 if prec == "f64" else 1e-10
+    assert cases.rel_err(gks, gk_ref) <= tol
+    assert cases.rel_err(gus, gu_ref) <= tol
+
+
+@pytest.mark.gpu
 def test_adjoint_forward_matches_oracle(gpu):
     M = gpu
     n, T = (17, 9, 13), 25

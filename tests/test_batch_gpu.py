@@ -48,6 +48,33 @@ def test_batch_matches_oracle_per_instance(gpu, prec):
             assert cases.rel_err(b.download(i), oracle_run(s, T)) <= 1e-12, (i, s["n"])
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+def test_batch_queue_equals_batch(gpu, prec):
+    """scafes_gpu_batch_create / _enqueue / _run: the instances enqueued one
+    by one give the scafes_batch results bit for bit, across two runs; a
+    late enqueue is refused."""
+    M = gpu
+    specs = small_ensemble(n_inst=5, seed=6)
+    with make_batch(M, specs, prec) as b:
+        b.step(9)
+        b.step(4)
+        want = [b.download(i) for i in range(len(specs))]
+    with M.BatchQueue(prec) as q:
+        for i, s in enumerate(specs):
+            shape = (s["n"][2], s["n"][1], s["n"][0])
+            assert q.enqueue(W.pennes_batch_instance(s), np.full(shape, W.T_ARTERIAL), W.pennes_source(s)) == i
+        q.run(9)
+        q.run(4)
+        for i in range(len(specs)):
+            assert np.array_equal(q.download(i), want[i]), i
+        s = specs[0]
+        with pytest.raises(M.ScafesError):
+            q.enqueue(W.pennes_batch_instance(s), np.zeros((s["n"][2], s["n"][1], s["n"][0])))
+    with M.BatchQueue(prec) as q:
+        with pytest.raises(M.ScafesError):
+            q.run(1)                                    # nothing enqueued
+
+
 def test_batch_equals_looped_and_all_schedules(gpu):
     M = gpu
     specs = small_ensemble(n_inst=9, seed=4)
