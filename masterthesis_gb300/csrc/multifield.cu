@@ -118,6 +118,145 @@ k_yee_e(T* __restrict__ ex, T* __restrict__ ey, T* __restrict__ ez, const T* __r
     }
 }
 
+// One Yee step (H half step, then E with the new H) in one pass over the
+// fields, for FP32 where the two-kernel form is bandwidth- and
+// latency-bound (it moves 72 bytes per cell and step; this moves the 48 of
+// reading E, H and writing E, H once).  Reads the old set, writes the other
+// (ping-pong: a CTA recomputes the new H of its x-1 / y-1 halo from old
+// values that its neighbours must not have overwritten yet).  A CTA owns a
+// YX x YY column tile and marches z-planes zchunk at a time: per plane it
+// computes the new H on the tile plus a one-cell halo on the low x and y
+// sides (from E of planes z and z+1 staged in shared memory), then the new
+// E of its own columns from the new H of planes z (shared) and z-1 (kept in
+// registers).  Same operations, in the same order, as k_yee_h + k_yee_e.
+constexpr int YX = 32, YY = 8;
+
+template <class T>
+__global__ void __launch_bounds__(YX * YY, 4)
+k_yee_fused(const T* __restrict__ exo, const T* __restrict__ eyo, const T* __restrict__ ezo,
+            const T* __restrict__ hxo, const T* __restrict__ hyo, const T* __restrict__ hzo,
+            T* __restrict__ exn, T* __restrict__ eyn, T* __restrict__ ezn,
+            T* __restrict__ hxn, T* __restrict__ hyn, T* __restrict__ hzn,
+            Layout L, T ch, long long src, T src_val, int zchunk) {
+    constexpr int EW = YX + 2, EH = YY + 2;  // E region: x0-1 .. x0+YX, y0-1 .. y0+YY
+    constexpr int HW = YX + 1, HH = YY + 1;  // new-H region: x0-1 .. x0+YX-1, y0-1 .. y0+YY-1
+    constexpr int NT = YX * YY;
+    constexpr int EPT = (EW * EH + NT - 1) / NT;  // E cells staged per thread
+    constexpr int HPT = (HW * HH + NT - 1) / NT;  // new-H cells per thread
+    __shared__ T se[2][3][EH][EW];  // E of planes z (cur) and z+1
+    __shared__ T sh[3][HH][HW];     // new H of plane z
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * YX + tx;
+    const int x0 = blockIdx.x * YX, y0 = blockIdx.y * YY;
+    const int z0 = blockIdx.z * zchunk, z1 = min(z0 + zchunk, L.nz);
+    const int zs = z0 > 0 ? z0 - 1 : 0;  // plane z0-1 only gives the new H below z0
+
+    T ra[EPT][3];
+    auto fetch = [&](int z) {  // E of plane z (zero outside the grid) into registers
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            const int i = tid + k * NT;
+            const int x = x0 - 1 + i % EW, y = y0 - 1 + i / EW;
+            ra[k][0] = ra[k][1] = ra[k][2] = T(0);
+            if (i < EW * EH && z < L.nz && x >= 0 && x < L.nx && y >= 0 && y < L.ny) {
+                const long long m = L.idx(x, y, z);
+                ra[k][0] = exo[m];
+                ra[k][1] = eyo[m];
+                ra[k][2] = ezo[m];
+            }
+        }
+    };
+    auto stage = [&](int buf) {
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            const int i = tid + k * NT;
+            if (i < EW * EH)
+                for (int c = 0; c < 3; ++c) se[buf][c][i / EW][i % EW] = ra[k][c];
+        }
+    };
+    // Old H of this thread's new-H cells, one plane ahead (registers).
+    T rh[HPT][3];
+    auto fetch_h = [&](int z) {
+#pragma unroll
+        for (int k = 0; k < HPT; ++k) {
+            const int i = tid + k * NT;
+            const int gx = x0 - 1 + i % HW, gy = y0 - 1 + i / HW;
+            rh[k][0] = rh[k][1] = rh[k][2] = T(0);
+            if (i < HW * HH && z < L.nz && gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny) {
+                const long long m = L.idx(gx, gy, z);
+                rh[k][0] = hxo[m];
+                rh[k][1] = hyo[m];
+                rh[k][2] = hzo[m];
+            }
+        }
+    };
+    fetch_h(zs);
+    fetch(zs);
+    stage(0);
+    fetch(zs + 1);
+    stage(1);
+    int cur = 0;
+    const int x = x0 + tx, y = y0 + ty;
+    const bool live = x < L.nx && y < L.ny;
+    T hx_prev = T(0), hy_prev = T(0);
+    for (int z = zs; z < z1; ++z) {
+        __syncthreads();   // planes z and z+1 staged
+        T hc[HPT][3];
+#pragma unroll
+        for (int k = 0; k < HPT; ++k)
+            for (int c = 0; c < 3; ++c) hc[k][c] = rh[k][c];
+        fetch(z + 2);      // in flight while this plane is computed
+        fetch_h(z + 1);
+        const int nx_ = cur ^ 1;
+#pragma unroll
+        for (int k = 0; k < HPT; ++k) {
+            const int i = tid + k * NT;
+            if (i >= HW * HH) break;
+            const int lx = i % HW, ly = i / HW;
+            const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+            T vhx = T(0), vhy = T(0), vhz = T(0);
+            if (gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny) {
+                vhx = hc[k][0];
+                vhy = hc[k][1];
+                vhz = hc[k][2];
+                const T ex0 = se[cur][0][ly][lx], ey0 = se[cur][1][ly][lx], ez0 = se[cur][2][ly][lx];
+                const bool xi = gx + 1 < L.nx, yi = gy + 1 < L.ny, zi = z + 1 < L.nz;
+                if (yi && zi) vhx -= ch * ((se[cur][2][ly + 1][lx] - ez0) - (se[nx_][1][ly][lx] - ey0));
+                if (xi && zi) vhy -= ch * ((se[nx_][0][ly][lx] - ex0) - (se[cur][2][ly][lx + 1] - ez0));
+                if (xi && yi) vhz -= ch * ((se[cur][1][ly][lx + 1] - ey0) - (se[cur][0][ly + 1][lx] - ex0));
+            }
+            sh[0][ly][lx] = vhx;
+            sh[1][ly][lx] = vhy;
+            sh[2][ly][lx] = vhz;
+        }
+        __syncthreads();
+        const int lx = tx + 1, ly = ty + 1;
+        if (live && z >= z0) {
+            const long long m = L.idx(x, y, z);
+            const T hx = sh[0][ly][lx], hy = sh[1][ly][lx], hz = sh[2][ly][lx];
+            hxn[m] = hx;
+            hyn[m] = hy;
+            hzn[m] = hz;
+            T ex = se[cur][0][ly][lx], ey = se[cur][1][ly][lx], ez = se[cur][2][ly][lx];
+            const bool xin = x > 0 && x + 1 < L.nx, yin = y > 0 && y + 1 < L.ny, zin = z > 0 && z + 1 < L.nz;
+            if (x + 1 < L.nx && yin && zin) ex += ch * ((hz - sh[2][ly - 1][lx]) - (hy - hy_prev));
+            if (y + 1 < L.ny && xin && zin) ey += ch * ((hx - hx_prev) - (hz - sh[2][ly][lx - 1]));
+            if (z + 1 < L.nz && xin && yin) {
+                T v = ez + ch * ((hy - sh[1][ly][lx - 1]) - (hx - sh[0][ly - 1][lx]));
+                if (m == src) v -= src_val;
+                ez = v;
+            }
+            exn[m] = ex;
+            eyn[m] = ey;
+            ezn[m] = ez;
+        }
+        hx_prev = sh[0][ly][lx];
+        hy_prev = sh[1][ly][lx];
+        __syncthreads();   // done with se[cur] and sh
+        stage(cur);        // plane z+2 replaces plane z
+        cur ^= 1;
+    }
+}
+
 template <class T>
 __global__ void k_dense_to_field(const double* __restrict__ d, T* __restrict__ f, Layout L) {
     const long long n = (long long)L.nx * L.ny * L.nz;
@@ -150,7 +289,8 @@ struct scafes_mf {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    int cur = 0;              // Lame: which half of mem holds u^n
+    int cur = 0;              // Lame: which half of mem holds u^n;
+                              // FP32 Yee: which set of 6 fields is current
     int t = 0;
     bool timed = false;
     std::string err;
@@ -176,6 +316,22 @@ int mfail(scafes_mf* h, int code, const char* fmt, ...) {
             return mfail(h, SCAFES_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
                          __FILE__, __LINE__);                                                  \
     } while (0)
+
+// z-planes per CTA of the fused Yee step: long chunks (the plane below a
+// chunk is recomputed), shorter ones while the grid has few column tiles.
+int yee_zchunk(const Layout& L) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    const long long tiles = (long long)((L.nx + YX - 1) / YX) * ((L.ny + YY - 1) / YY);
+    int zc = 32;
+    while (zc > 4 && tiles * ((L.nz + zc - 1) / zc) < (long long)sms * 8) zc >>= 1;
+    return zc;
+}
 
 dim3 mgrid(const Layout& L) { return dim3((L.nx + MX - 1) / MX, (L.ny + MY - 1) / MY, (L.nz + MZ - 1) / MZ); }
 
@@ -218,10 +374,12 @@ extern "C" int scafes_mf_create(const scafes_mf_cfg* cfg, scafes_mf** out) {
     h->L = make_layout(cfg->n_nodes[0], cfg->n_nodes[1], cfg->n_nodes[2]);
     h->esz = cfg->precision == SCAFES_PREC_F32 ? 4 : 8;
     h->nfields = 6;  // Lame: u^n (3) + u^{n-1} (3); Yee: Ex..Hz
+    // The fused FP32 Yee step reads one set of six fields and writes another.
+    const int sets = (cfg->kind == SCAFES_MF_YEE && h->esz == 4) ? 2 : 1;
     cudaError_t e = cudaSuccess;
     if (cfg->stream) h->stream = (cudaStream_t)cfg->stream;
     else { e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking); h->own_stream = true; }
-    const size_t bytes = (size_t)h->nfields * h->L.size() * h->esz;
+    const size_t bytes = (size_t)sets * h->nfields * h->L.size() * h->esz;
     if (e == cudaSuccess) e = cudaMalloc(&h->mem, bytes);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->mem, 0, bytes, h->stream);
     if (e == cudaSuccess) e = cudaMalloc(&h->stage, (size_t)h->L.nx * h->L.ny * h->L.nz * sizeof(double));
@@ -240,7 +398,7 @@ extern "C" int scafes_mf_create(const scafes_mf_cfg* cfg, scafes_mf** out) {
 
 // Lame fields 0..2 are u^n, 3..5 u^{n-1}; the halves swap every step.
 static int phys_field(const scafes_mf* h, int field) {
-    if (h->cfg.kind != SCAFES_MF_LAME) return field;
+    if (h->cfg.kind != SCAFES_MF_LAME) return h->cur * 6 + field;  // Yee: the current set
     const int half = field / 3, comp = field % 3;
     return ((half ^ h->cur) * 3) + comp;
 }
@@ -315,11 +473,17 @@ extern "C" int scafes_mf_step(scafes_mf* h, int n_steps) {
                                                                           src, sv);
             } else {
                 float* f[6];
-                for (int i = 0; i < 6; ++i) f[i] = (float*)field_ptr(h, i);
-                k_yee_h<float><<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L,
-                                                                         (float)ch);
-                k_yee_e<float><<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L,
-                                                                         (float)ch, src, (float)sv);
+                float* g[6];
+                for (int i = 0; i < 6; ++i) {
+                    f[i] = (float*)field_ptr(h, h->cur * 6 + i);
+                    g[i] = (float*)field_ptr(h, (h->cur ^ 1) * 6 + i);
+                }
+                const int zc = yee_zchunk(L);
+                const dim3 grid((L.nx + YX - 1) / YX, (L.ny + YY - 1) / YY, (L.nz + zc - 1) / zc);
+                k_yee_fused<float><<<grid, dim3(YX, YY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], g[0], g[1],
+                                                                         g[2], g[3], g[4], g[5], L, (float)ch, src,
+                                                                         (float)sv, zc);
+                h->cur ^= 1;
             }
             MTRY(h, cudaGetLastError());
             h->t += 1;

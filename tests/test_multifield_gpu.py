@@ -53,10 +53,13 @@ def yee_fields_zero(n):
     return np.zeros((6, n[2], n[1], n[0]))
 
 
-@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f32", 1e-4)])
-def test_yee_matches_oracle(gpu, prec, tol):
+@pytest.mark.parametrize("prec,tol,n", [("f64", 1e-12, (20, 18, 16)), ("f32", 1e-4, (20, 18, 16)),
+                                        ("f32", 1e-4, (37, 29, 41)), ("f64", 1e-12, (37, 29, 41))])
+def test_yee_matches_oracle(gpu, prec, tol, n):
+    """FP32 runs the fused one-pass step (tiles, halos and z-chunks cut
+    across these odd sizes), FP64 the two-kernel step."""
     M = gpu
-    n, T = (20, 18, 16), 80
+    T = 80
     tau, src, par = W.yee_setup(n)
     with M.MultiField(M.MF_YEE, n, tau, par, precision=prec, src=src) as mf:
         mf.step(T)
