@@ -22,6 +22,7 @@
 #include <string>
 
 #include "scafes_common.cuh"
+#include "tma.cuh"
 #include "../../include/scafes_gb300.h"
 
 using namespace scafes;
@@ -118,130 +119,164 @@ k_yee_e(T* __restrict__ ex, T* __restrict__ ey, T* __restrict__ ez, const T* __r
     }
 }
 
-// One Yee step (H half step, then E with the new H) in one pass over the
-// fields, for FP32 where the two-kernel form is bandwidth- and
-// latency-bound (it moves 72 bytes per cell and step; this moves the 48 of
-// reading E, H and writing E, H once).  Reads the old set, writes the other
-// (ping-pong: a CTA recomputes the new H of its x-1 / y-1 halo from old
-// values that its neighbours must not have overwritten yet).  A CTA owns a
-// YX x YY column tile and marches z-planes zchunk at a time: per plane it
-// computes the new H on the tile plus a one-cell halo on the low x and y
-// sides (from E of planes z and z+1 staged in shared memory), then the new
-// E of its own columns from the new H of planes z (shared) and z-1 (kept in
-// registers).  Same operations, in the same order, as k_yee_h + k_yee_e.
+// One FP32 Yee step (H half step, then E with the new H) in one pass over
+// the fields, where the two-kernel form is bandwidth- and latency-bound (it
+// moves 72 bytes per cell and step; this moves the 48 of reading E, H and
+// writing E, H once).  It reads the old set of six fields and writes the
+// other (ping-pong: a CTA recomputes the new H of its x-1 / y-1 halo from
+// old values that its neighbours must not have overwritten yet).
+//
+// A CTA owns a YX x YY column tile and marches z-planes.  TMA brings, per
+// plane, a box of each old E field (rows y0-1 .. y0+YY) and of each old H
+// field (rows y0-1 .. y0+YY-1), columns x0-4 .. x0+YX+3 (x0-4 keeps the
+// 16-byte alignment TMA needs; out-of-grid cells read as 0 and are never
+// used): E through a ring of three planes (z, z+1, z+2 in flight), H through
+// two.  Per plane the CTA computes the new H on the tile plus a one-cell halo
+// on the low x and y sides, then the new E of its own columns from the new H
+// of plane z (shared) and z-1 (registers).  Same operations, in the same
+// order, as k_yee_h + k_yee_e.  Every wait is bounded; on a timeout the
+// kernel records the status, drains its loads and returns.
 constexpr int YX = 32, YY = 8;
+constexpr int YBW = YX + 8;                            // box width (x0-4 .. x0+YX+3)
+constexpr int YE_BOX = YBW * (YY + 2);                 // E box: rows y0-1 .. y0+YY
+constexpr int YH_BOX = YBW * (YY + 1);                 // H box: rows y0-1 .. y0+YY-1
+constexpr int YE_PAD = (YE_BOX * 4 + 127) / 128 * 32;  // floats per E box, 128-byte aligned
+constexpr int YH_PAD = (YH_BOX * 4 + 127) / 128 * 32;
+constexpr int YHS = YX + 1, YHN = YHS * (YY + 1);     // new-H cells: x0-1 .. x0+YX-1, y0-1 ..
+constexpr size_t YEE_SMEM = (size_t)(9 * YE_PAD + 6 * YH_PAD + 6 * YH_BOX) * 4 + 5 * 8;
 
-template <class T>
 __global__ void __launch_bounds__(YX * YY, 4)
-k_yee_fused(const T* __restrict__ exo, const T* __restrict__ eyo, const T* __restrict__ ezo,
-            const T* __restrict__ hxo, const T* __restrict__ hyo, const T* __restrict__ hzo,
-            T* __restrict__ exn, T* __restrict__ eyn, T* __restrict__ ezn,
-            T* __restrict__ hxn, T* __restrict__ hyn, T* __restrict__ hzn,
-            Layout L, T ch, long long src, T src_val, int zchunk) {
-    constexpr int EW = YX + 2, EH = YY + 2;  // E region: x0-1 .. x0+YX, y0-1 .. y0+YY
-    constexpr int HW = YX + 1, HH = YY + 1;  // new-H region: x0-1 .. x0+YX-1, y0-1 .. y0+YY-1
+k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUtensorMap tey,
+          const __grid_constant__ CUtensorMap tez, const __grid_constant__ CUtensorMap thx,
+          const __grid_constant__ CUtensorMap thy, const __grid_constant__ CUtensorMap thz,
+          float* __restrict__ exn, float* __restrict__ eyn, float* __restrict__ ezn,
+          float* __restrict__ hxn, float* __restrict__ hyn, float* __restrict__ hzn,
+          Layout L, float ch, long long src, float src_val, int zchunk, int* __restrict__ status) {
     constexpr int NT = YX * YY;
-    constexpr int EPT = (EW * EH + NT - 1) / NT;  // E cells staged per thread
-    constexpr int HPT = (HW * HH + NT - 1) / NT;  // new-H cells per thread
-    __shared__ T se[2][3][EH][EW];  // E of planes z (cur) and z+1
-    __shared__ T sh[3][HH][HW];     // new H of plane z
+    constexpr int HPT = (YHN + NT - 1) / NT;
+    extern __shared__ __align__(128) float ysm[];
+    float* se = ysm;                   // [3 slots][ex, ey, ez][YE_PAD]
+    float* sho = se + 9 * YE_PAD;      // [2 slots][hx, hy, hz][YH_PAD]   old H
+    float* shn = sho + 6 * YH_PAD;     // [2 slots][hx, hy, hz][YH_BOX]   new H
+    uint64_t* bar = reinterpret_cast<uint64_t*>(shn + 6 * YH_BOX);  // E slots 0-2, H slots 3-4
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * YX + tx;
     const int x0 = blockIdx.x * YX, y0 = blockIdx.y * YY;
     const int z0 = blockIdx.z * zchunk, z1 = min(z0 + zchunk, L.nz);
     const int zs = z0 > 0 ? z0 - 1 : 0;  // plane z0-1 only gives the new H below z0
+    const int np = z1 - zs;              // planes whose new H is computed
 
-    T ra[EPT][3];
-    auto fetch = [&](int z) {  // E of plane z (zero outside the grid) into registers
-#pragma unroll
-        for (int k = 0; k < EPT; ++k) {
-            const int i = tid + k * NT;
-            const int x = x0 - 1 + i % EW, y = y0 - 1 + i / EW;
-            ra[k][0] = ra[k][1] = ra[k][2] = T(0);
-            if (i < EW * EH && z < L.nz && x >= 0 && x < L.nx && y >= 0 && y < L.ny) {
-                const long long m = L.idx(x, y, z);
-                ra[k][0] = exo[m];
-                ra[k][1] = eyo[m];
-                ra[k][2] = ezo[m];
-            }
-        }
+    // A sweep after one that timed out has nothing valid to work on.
+    if (__syncthreads_or(tid == 0 && *(volatile int*)status != 0)) return;
+    if (tid == 0) {
+        for (int b = 0; b < 5; ++b) mbar_init(&bar[b], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    auto issue_e = [&](int p) {  // old E of plane zs+p into ring slot p % 3
+        uint64_t* b = &bar[p % 3];
+        float* d = se + (p % 3) * 3 * YE_PAD;
+        mbar_arrive_expect_tx(b, 3u * YE_BOX * 4u);
+        tma_load_3d(d, &tex, x0 - 4, y0 - 1, zs + p, b);
+        tma_load_3d(d + YE_PAD, &tey, x0 - 4, y0 - 1, zs + p, b);
+        tma_load_3d(d + 2 * YE_PAD, &tez, x0 - 4, y0 - 1, zs + p, b);
     };
-    auto stage = [&](int buf) {
-#pragma unroll
-        for (int k = 0; k < EPT; ++k) {
-            const int i = tid + k * NT;
-            if (i < EW * EH)
-                for (int c = 0; c < 3; ++c) se[buf][c][i / EW][i % EW] = ra[k][c];
-        }
+    auto issue_h = [&](int p) {  // old H of plane zs+p into slot p % 2
+        uint64_t* b = &bar[3 + p % 2];
+        float* d = sho + (p % 2) * 3 * YH_PAD;
+        mbar_arrive_expect_tx(b, 3u * YH_BOX * 4u);
+        tma_load_3d(d, &thx, x0 - 4, y0 - 1, zs + p, b);
+        tma_load_3d(d + YH_PAD, &thy, x0 - 4, y0 - 1, zs + p, b);
+        tma_load_3d(d + 2 * YH_PAD, &thz, x0 - 4, y0 - 1, zs + p, b);
     };
-    // Old H of this thread's new-H cells, one plane ahead (registers).
-    T rh[HPT][3];
-    auto fetch_h = [&](int z) {
+    // E planes 0 .. np and H planes 0 .. np-1 are loaded, each exactly once.
+    if (tid == 0) {
+        issue_e(0);
+        issue_e(1);
+        issue_h(0);
+    }
+
+    // Per-thread constants: the new-H cells this thread computes (box index,
+    // in-grid and boundary tests) and its own column.
+    int hb[HPT];
+    bool hin[HPT], hxi[HPT], hyi[HPT];
 #pragma unroll
-        for (int k = 0; k < HPT; ++k) {
-            const int i = tid + k * NT;
-            const int gx = x0 - 1 + i % HW, gy = y0 - 1 + i / HW;
-            rh[k][0] = rh[k][1] = rh[k][2] = T(0);
-            if (i < HW * HH && z < L.nz && gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny) {
-                const long long m = L.idx(gx, gy, z);
-                rh[k][0] = hxo[m];
-                rh[k][1] = hyo[m];
-                rh[k][2] = hzo[m];
-            }
-        }
-    };
-    fetch_h(zs);
-    fetch(zs);
-    stage(0);
-    fetch(zs + 1);
-    stage(1);
-    int cur = 0;
+    for (int k = 0; k < HPT; ++k) {
+        const int i = tid + k * NT;
+        const int lx = i % YHS, ly = i / YHS;
+        const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+        hb[k] = ly * YBW + lx + 3;
+        hin[k] = i < YHN && gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
+        hxi[k] = gx + 1 < L.nx;
+        hyi[k] = gy + 1 < L.ny;
+    }
     const int x = x0 + tx, y = y0 + ty;
     const bool live = x < L.nx && y < L.ny;
-    T hx_prev = T(0), hy_prev = T(0);
-    for (int z = zs; z < z1; ++z) {
-        __syncthreads();   // planes z and z+1 staged
-        T hc[HPT][3];
-#pragma unroll
-        for (int k = 0; k < HPT; ++k)
-            for (int c = 0; c < 3; ++c) hc[k][c] = rh[k][c];
-        fetch(z + 2);      // in flight while this plane is computed
-        fetch_h(z + 1);
-        const int nx_ = cur ^ 1;
-#pragma unroll
-        for (int k = 0; k < HPT; ++k) {
-            const int i = tid + k * NT;
-            if (i >= HW * HH) break;
-            const int lx = i % HW, ly = i / HW;
-            const int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
-            T vhx = T(0), vhy = T(0), vhz = T(0);
-            if (gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny) {
-                vhx = hc[k][0];
-                vhy = hc[k][1];
-                vhz = hc[k][2];
-                const T ex0 = se[cur][0][ly][lx], ey0 = se[cur][1][ly][lx], ez0 = se[cur][2][ly][lx];
-                const bool xi = gx + 1 < L.nx, yi = gy + 1 < L.ny, zi = z + 1 < L.nz;
-                if (yi && zi) vhx -= ch * ((se[cur][2][ly + 1][lx] - ez0) - (se[nx_][1][ly][lx] - ey0));
-                if (xi && zi) vhy -= ch * ((se[nx_][0][ly][lx] - ex0) - (se[cur][2][ly][lx + 1] - ez0));
-                if (xi && yi) vhz -= ch * ((se[cur][1][ly][lx + 1] - ey0) - (se[cur][0][ly + 1][lx] - ex0));
-            }
-            sh[0][ly][lx] = vhx;
-            sh[1][ly][lx] = vhy;
-            sh[2][ly][lx] = vhz;
+    const long long oo = (long long)y * L.pitch + x;
+    const int ob = (ty + 1) * YBW + tx + 4;  // own cell in a box
+    const bool ex_upd = x + 1 < L.nx && y > 0 && y + 1 < L.ny;
+    const bool ey_upd = y + 1 < L.ny && x > 0 && x + 1 < L.nx;
+    const bool ez_upd = x > 0 && x + 1 < L.nx && y > 0 && y + 1 < L.ny;
+
+    bool ok = bounded_wait(&bar[0], 0);  // E plane 0
+    float hx_prev = 0.f, hy_prev = 0.f;
+    for (int p = 0; p < np; ++p) {
+        const int z = zs + p;
+        __syncthreads();  // iteration p-1 is done with the slots refilled below
+        if (tid == 0) {
+            fence_proxy_async_smem();
+            if (p + 2 <= np) issue_e(p + 2);
+            if (p + 1 < np) issue_h(p + 1);
         }
-        __syncthreads();
-        const int lx = tx + 1, ly = ty + 1;
+        ok = bounded_wait(&bar[(p + 1) % 3], ((p + 1) / 3) & 1) && ok;  // E plane p+1
+        ok = bounded_wait(&bar[3 + p % 2], (p / 2) & 1) && ok;          // old H plane p
+        const float* ea = se + (p % 3) * 3 * YE_PAD;
+        const float* eb = se + ((p + 1) % 3) * 3 * YE_PAD;
+        const float* ho = sho + (p % 2) * 3 * YH_PAD;
+        float* hn = shn + (p % 2) * 3 * YH_BOX;
+        const bool zi = z + 1 < L.nz;
+        if (ok) {
+#pragma unroll
+            for (int k = 0; k < HPT; ++k) {
+                if (tid + k * NT >= YHN) break;
+                const int b = hb[k];
+                float vhx = 0.f, vhy = 0.f, vhz = 0.f;
+                if (hin[k]) {
+                    vhx = ho[b];
+                    vhy = ho[YH_PAD + b];
+                    vhz = ho[2 * YH_PAD + b];
+                    const float ex0 = ea[b], ey0 = ea[YE_PAD + b], ez0 = ea[2 * YE_PAD + b];
+                    if (hyi[k] && zi) vhx -= ch * ((ea[2 * YE_PAD + b + YBW] - ez0) - (eb[YE_PAD + b] - ey0));
+                    if (hxi[k] && zi) vhy -= ch * ((eb[b] - ex0) - (ea[2 * YE_PAD + b + 1] - ez0));
+                    if (hxi[k] && hyi[k]) vhz -= ch * ((ea[YE_PAD + b + 1] - ey0) - (ea[b + YBW] - ex0));
+                }
+                hn[b] = vhx;
+                hn[YH_BOX + b] = vhy;
+                hn[2 * YH_BOX + b] = vhz;
+            }
+        }
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) {
+                // A load never completed: report, drain what was issued, stop.
+                atomicExch(status, SCAFES_ERR_TIMEOUT);
+                bounded_wait(&bar[(p + 1) % 3], ((p + 1) / 3) & 1, kWaitLimitNs / 8);
+                bounded_wait(&bar[3 + p % 2], (p / 2) & 1, kWaitLimitNs / 8);
+                if (p + 2 <= np) bounded_wait(&bar[(p + 2) % 3], ((p + 2) / 3) & 1, kWaitLimitNs / 8);
+                if (p + 1 < np) bounded_wait(&bar[3 + (p + 1) % 2], ((p + 1) / 2) & 1, kWaitLimitNs / 8);
+            }
+            return;
+        }
+        const float hx = hn[ob], hy = hn[YH_BOX + ob], hz = hn[2 * YH_BOX + ob];
         if (live && z >= z0) {
-            const long long m = L.idx(x, y, z);
-            const T hx = sh[0][ly][lx], hy = sh[1][ly][lx], hz = sh[2][ly][lx];
+            const long long m = (long long)z * L.plane + oo;
             hxn[m] = hx;
             hyn[m] = hy;
             hzn[m] = hz;
-            T ex = se[cur][0][ly][lx], ey = se[cur][1][ly][lx], ez = se[cur][2][ly][lx];
-            const bool xin = x > 0 && x + 1 < L.nx, yin = y > 0 && y + 1 < L.ny, zin = z > 0 && z + 1 < L.nz;
-            if (x + 1 < L.nx && yin && zin) ex += ch * ((hz - sh[2][ly - 1][lx]) - (hy - hy_prev));
-            if (y + 1 < L.ny && xin && zin) ey += ch * ((hx - hx_prev) - (hz - sh[2][ly][lx - 1]));
-            if (z + 1 < L.nz && xin && yin) {
-                T v = ez + ch * ((hy - sh[1][ly][lx - 1]) - (hx - sh[0][ly - 1][lx]));
+            float ex = ea[ob], ey = ea[YE_PAD + ob], ez = ea[2 * YE_PAD + ob];
+            const bool zin = z > 0 && zi;
+            if (ex_upd && zin) ex += ch * ((hz - hn[2 * YH_BOX + ob - YBW]) - (hy - hy_prev));
+            if (ey_upd && zin) ey += ch * ((hx - hx_prev) - (hz - hn[2 * YH_BOX + ob - 1]));
+            if (ez_upd && zi) {
+                float v = ez + ch * ((hy - hn[YH_BOX + ob - 1]) - (hx - hn[ob - YBW]));
                 if (m == src) v -= src_val;
                 ez = v;
             }
@@ -249,11 +284,8 @@ k_yee_fused(const T* __restrict__ exo, const T* __restrict__ eyo, const T* __res
             eyn[m] = ey;
             ezn[m] = ez;
         }
-        hx_prev = sh[0][ly][lx];
-        hy_prev = sh[1][ly][lx];
-        __syncthreads();   // done with se[cur] and sh
-        stage(cur);        // plane z+2 replaces plane z
-        cur ^= 1;
+        hx_prev = hx;
+        hy_prev = hy;
     }
 }
 
@@ -293,6 +325,9 @@ struct scafes_mf {
                               // FP32 Yee: which set of 6 fields is current
     int t = 0;
     bool timed = false;
+    int* status = nullptr;    // device status word of the TMA sweeps (0 = ok)
+    CUtensorMap ytm[2][6];    // FP32 Yee: per field set, the TMA maps of Ex..Hz
+    bool ytm_ok = false;
     std::string err;
 };
 
@@ -346,6 +381,7 @@ extern "C" void scafes_mf_destroy(scafes_mf* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     cudaFree(h->mem);
     cudaFree(h->stage);
+    cudaFree(h->status);
     if (h->e0) cudaEventDestroy(h->e0);
     if (h->e1) cudaEventDestroy(h->e1);
     if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
@@ -368,6 +404,12 @@ extern "C" int scafes_mf_create(const scafes_mf_cfg* cfg, scafes_mf** out) {
         for (int p = 0; p < 3; ++p)
             if (cfg->src[p] < 0 || cfg->src[p] >= cfg->n_nodes[p])
                 return mfail(nullptr, SCAFES_ERR_ARG, "scafes_mf_create: source index out of the grid");
+    if (cfg->kind == SCAFES_MF_YEE && cfg->precision == SCAFES_PREC_F32) {
+        const Layout Lp = make_layout(cfg->n_nodes[0], cfg->n_nodes[1], cfg->n_nodes[2]);
+        if (Lp.plane > 0x7fffffffLL)  // the fused step keeps in-plane offsets in 32 bits
+            return mfail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_mf_create: a z-plane of %lld cells is too large",
+                         Lp.plane);
+    }
     scafes_mf* h = new (std::nothrow) scafes_mf();
     if (!h) return mfail(nullptr, SCAFES_ERR_NOMEM, "scafes_mf_create: out of host memory");
     h->cfg = *cfg;
@@ -383,6 +425,8 @@ extern "C" int scafes_mf_create(const scafes_mf_cfg* cfg, scafes_mf** out) {
     if (e == cudaSuccess) e = cudaMalloc(&h->mem, bytes);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->mem, 0, bytes, h->stream);
     if (e == cudaSuccess) e = cudaMalloc(&h->stage, (size_t)h->L.nx * h->L.ny * h->L.nz * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&h->status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->status, 0, sizeof(int), h->stream);
     if (e == cudaSuccess) e = cudaEventCreate(&h->e0);
     if (e == cudaSuccess) e = cudaEventCreate(&h->e1);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -403,6 +447,34 @@ static int phys_field(const scafes_mf* h, int field) {
     return ((half ^ h->cur) * 3) + comp;
 }
 
+// Reads and clears the status word of the TMA sweeps.
+static int mf_status(scafes_mf* h) {
+    int st = 0;
+    MTRY(h, cudaMemcpyAsync(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    MTRY(h, cudaStreamSynchronize(h->stream));
+    if (st != 0) {
+        cudaMemsetAsync(h->status, 0, sizeof(int), h->stream);
+        return mfail(h, SCAFES_ERR_TIMEOUT, "a Yee sweep gave up waiting for its TMA loads; results are invalid");
+    }
+    return SCAFES_OK;
+}
+
+// TMA maps of both field sets (FP32 Yee): E fields with a box of YY+2 rows,
+// H fields with YY+1, YBW columns.
+static int yee_maps(scafes_mf* h) {
+    if (h->ytm_ok) return SCAFES_OK;
+    const Layout& L = h->L;
+    for (int set = 0; set < 2; ++set)
+        for (int f = 0; f < 6; ++f) {
+            const CUresult r = make_tensor_map_3d(&h->ytm[set][f], field_ptr(h, set * 6 + f), 4, L.nx, L.ny, L.nz,
+                                                  (size_t)L.pitch * 4, (size_t)L.plane * 4, YBW,
+                                                  f < 3 ? YY + 2 : YY + 1);
+            if (r != CUDA_SUCCESS) return mfail(h, SCAFES_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+        }
+    h->ytm_ok = true;
+    return SCAFES_OK;
+}
+
 extern "C" int scafes_mf_upload(scafes_mf* h, int field, const double* host, size_t n) {
     if (!h || !host) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_upload: NULL argument");
     if (field < 0 || field >= h->nfields) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_upload: field %d", field);
@@ -421,6 +493,8 @@ extern "C" int scafes_mf_download(scafes_mf* h, int field, double* host, size_t 
     if (!h || !host) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_download: NULL argument");
     if (field < 0 || field >= h->nfields) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_download: field %d", field);
     if (n != (size_t)h->L.nx * h->L.ny * h->L.nz) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_download: wrong size");
+    const int st = mf_status(h);
+    if (st) return st;
     const char* f = field_ptr(h, phys_field(h, field));
     if (h->esz == 8) k_field_to_dense<double><<<256, 256, 0, h->stream>>>((const double*)f, h->stage, h->L);
     else k_field_to_dense<float><<<256, 256, 0, h->stream>>>((const float*)f, h->stage, h->L);
@@ -472,17 +546,16 @@ extern "C" int scafes_mf_step(scafes_mf* h, int n_steps) {
                 k_yee_e<double><<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L, ch,
                                                                           src, sv);
             } else {
-                float* f[6];
+                const int rc = yee_maps(h);
+                if (rc) return rc;
                 float* g[6];
-                for (int i = 0; i < 6; ++i) {
-                    f[i] = (float*)field_ptr(h, h->cur * 6 + i);
-                    g[i] = (float*)field_ptr(h, (h->cur ^ 1) * 6 + i);
-                }
+                for (int i = 0; i < 6; ++i) g[i] = (float*)field_ptr(h, (h->cur ^ 1) * 6 + i);
+                const CUtensorMap* t = h->ytm[h->cur];
                 const int zc = yee_zchunk(L);
                 const dim3 grid((L.nx + YX - 1) / YX, (L.ny + YY - 1) / YY, (L.nz + zc - 1) / zc);
-                k_yee_fused<float><<<grid, dim3(YX, YY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], g[0], g[1],
-                                                                         g[2], g[3], g[4], g[5], L, (float)ch, src,
-                                                                         (float)sv, zc);
+                k_yee_tma<<<grid, dim3(YX, YY), YEE_SMEM, h->stream>>>(t[0], t[1], t[2], t[3], t[4], t[5], g[0], g[1],
+                                                                       g[2], g[3], g[4], g[5], L, (float)ch, src,
+                                                                       (float)sv, zc, h->status);
                 h->cur ^= 1;
             }
             MTRY(h, cudaGetLastError());
