@@ -172,17 +172,17 @@ k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUten
         fence_barrier_init();
     }
     __syncthreads();
-    auto issue_e = [&](int p) {  // old E of plane zs+p into ring slot p % 3
-        uint64_t* b = &bar[p % 3];
-        float* d = se + (p % 3) * 3 * YE_PAD;
+    auto issue_e = [&](int p, int slot) {  // old E of plane zs+p into a ring slot
+        uint64_t* b = &bar[slot];
+        float* d = se + slot * 3 * YE_PAD;
         mbar_arrive_expect_tx(b, 3u * YE_BOX * 4u);
         tma_load_3d(d, &tex, x0 - 4, y0 - 1, zs + p, b);
         tma_load_3d(d + YE_PAD, &tey, x0 - 4, y0 - 1, zs + p, b);
         tma_load_3d(d + 2 * YE_PAD, &tez, x0 - 4, y0 - 1, zs + p, b);
     };
     auto issue_h = [&](int p) {  // old H of plane zs+p into slot p % 2
-        uint64_t* b = &bar[3 + p % 2];
-        float* d = sho + (p % 2) * 3 * YH_PAD;
+        uint64_t* b = &bar[3 + (p & 1)];
+        float* d = sho + (p & 1) * 3 * YH_PAD;
         mbar_arrive_expect_tx(b, 3u * YH_BOX * 4u);
         tma_load_3d(d, &thx, x0 - 4, y0 - 1, zs + p, b);
         tma_load_3d(d + YH_PAD, &thy, x0 - 4, y0 - 1, zs + p, b);
@@ -190,8 +190,8 @@ k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUten
     };
     // E planes 0 .. np and H planes 0 .. np-1 are loaded, each exactly once.
     if (tid == 0) {
-        issue_e(0);
-        issue_e(1);
+        issue_e(0, 0);
+        issue_e(1, 1);
         issue_h(0);
     }
 
@@ -217,22 +217,28 @@ k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUten
     const bool ey_upd = y + 1 < L.ny && x > 0 && x + 1 < L.nx;
     const bool ez_upd = x > 0 && x + 1 < L.nx && y > 0 && y + 1 < L.ny;
 
+    // Ring state without divisions: s0, s1, s2 are the slots of E planes
+    // p, p+1, p+2; bit s of eph is the parity of slot s's next phase.
+    int s0 = 0, s1 = 1, s2 = 2;
+    uint32_t eph = 0;
     bool ok = bounded_wait(&bar[0], 0);  // E plane 0
+    eph ^= 1u;
     float hx_prev = 0.f, hy_prev = 0.f;
     for (int p = 0; p < np; ++p) {
         const int z = zs + p;
         __syncthreads();  // iteration p-1 is done with the slots refilled below
         if (tid == 0) {
             fence_proxy_async_smem();
-            if (p + 2 <= np) issue_e(p + 2);
+            if (p + 2 <= np) issue_e(p + 2, s2);
             if (p + 1 < np) issue_h(p + 1);
         }
-        ok = bounded_wait(&bar[(p + 1) % 3], ((p + 1) / 3) & 1) && ok;  // E plane p+1
-        ok = bounded_wait(&bar[3 + p % 2], (p / 2) & 1) && ok;          // old H plane p
-        const float* ea = se + (p % 3) * 3 * YE_PAD;
-        const float* eb = se + ((p + 1) % 3) * 3 * YE_PAD;
-        const float* ho = sho + (p % 2) * 3 * YH_PAD;
-        float* hn = shn + (p % 2) * 3 * YH_BOX;
+        ok = bounded_wait(&bar[s1], (eph >> s1) & 1u) && ok;   // E plane p+1
+        eph ^= 1u << s1;
+        ok = bounded_wait(&bar[3 + (p & 1)], (p >> 1) & 1) && ok;  // old H plane p
+        const float* ea = se + s0 * 3 * YE_PAD;
+        const float* eb = se + s1 * 3 * YE_PAD;
+        const float* ho = sho + (p & 1) * 3 * YH_PAD;
+        float* hn = shn + (p & 1) * 3 * YH_BOX;
         const bool zi = z + 1 < L.nz;
         if (ok) {
 #pragma unroll
@@ -257,11 +263,13 @@ k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUten
         if (!__syncthreads_and(ok)) {
             if (tid == 0) {
                 // A load never completed: report, drain what was issued, stop.
+                // (eph already counts the wait on s1, so its pending phase
+                // has the other parity.)
                 atomicExch(status, SCAFES_ERR_TIMEOUT);
-                bounded_wait(&bar[(p + 1) % 3], ((p + 1) / 3) & 1, kWaitLimitNs / 8);
-                bounded_wait(&bar[3 + p % 2], (p / 2) & 1, kWaitLimitNs / 8);
-                if (p + 2 <= np) bounded_wait(&bar[(p + 2) % 3], ((p + 2) / 3) & 1, kWaitLimitNs / 8);
-                if (p + 1 < np) bounded_wait(&bar[3 + (p + 1) % 2], ((p + 1) / 2) & 1, kWaitLimitNs / 8);
+                bounded_wait(&bar[s1], ((eph >> s1) & 1u) ^ 1u, kWaitLimitNs / 8);
+                bounded_wait(&bar[3 + (p & 1)], (p >> 1) & 1, kWaitLimitNs / 8);
+                if (p + 2 <= np) bounded_wait(&bar[s2], (eph >> s2) & 1u, kWaitLimitNs / 8);
+                if (p + 1 < np) bounded_wait(&bar[3 + ((p + 1) & 1)], ((p + 1) >> 1) & 1, kWaitLimitNs / 8);
             }
             return;
         }
@@ -286,6 +294,10 @@ k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUten
         }
         hx_prev = hx;
         hy_prev = hy;
+        const int t = s0;
+        s0 = s1;
+        s1 = s2;
+        s2 = t;
     }
 }
 
