@@ -435,7 +435,8 @@ def run_ours(args, dist: Dist):
                          stream=stream.cuda_stream)
         with M.Plain(cfg) as p:
             p.upload(M.FIELD_U, u0)
-            tuned[prec] = p.autotune(10)  # picks the sweep's CTA tile variant
+            # picks the sweep's CTA tile variant and the temporal blocking depth
+            tuned[prec] = p.autotune(10) + (p.temporal_depth,)
             for _ in range(warmup):
                 p.step(T)
             stream.synchronize()
@@ -535,7 +536,8 @@ def run_ours(args, dist: Dist):
                    "nodes": [n, n, n], "time_steps_per_step": T, "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2 (1 GiB per field), no flush"},
         "e2e": e2e, "roofline": roofline, "gpu_launches": launches,
-        "autotune": {k: {"tile": v[0], "ms_per_sweep_by_tile": v[1]} for k, v in tuned.items()},
+        "autotune": {k: {"tile": v[0], "ms_per_sweep_by_tile": v[1], "temporal_depth": v[2]}
+                     for k, v in tuned.items()},
         "error": {"f64_vs_oracle": "<=1e-12 rel max-norm (tests, 64^3 x 200 and golden cases)",
                   "note": "f64 is the reference's arithmetic with FMA contraction"},
     }

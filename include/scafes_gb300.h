@@ -250,11 +250,24 @@ int scafes_gpu_download(scafes_handle* h, int field, double* host, size_t n);
  * n_steps sweeps with each tile variant of the sweep kernel (32 x BY CTA
  * tile, R rows per thread) on the uploaded problem, keeps the fastest for
  * later scafes_gpu_step calls and returns it (1-based) in *chosen and the
- * per-variant ms per step in ms_per_tile[4] (may be NULL).  The iterate and
- * the step counter are restored afterwards.  Allocates one temporary copy
- * of the iterate. */
+ * per-variant ms per step in ms_per_tile[4] (may be NULL); then times
+ * temporal blocking depth 2 where the problem allows it and keeps it if it
+ * is faster per step (scafes_gpu_temporal_depth).  The iterate and the step
+ * counter are restored afterwards.  Allocates one temporary copy of the
+ * iterate. */
 int scafes_gpu_autotune(scafes_handle* h, int n_steps, int* chosen,
                         float* ms_per_tile);
+
+/* Temporal blocking of scafes_gpu_step: depth 1 runs one sweep per step;
+ * depth 2 runs one pass per two steps (each CTA recomputes the
+ * intermediate step on a one-node halo in shared memory, so the field is
+ * read and written once per two steps; same results bit for bit).  Depth 2
+ * applies to Dirichlet problems with one border layer and no F_B; other
+ * problems, and an odd last step, run depth 1.  Default 1;
+ * scafes_gpu_autotune keeps depth 2 when it is faster.  _temporal_depth
+ * gives the depth that scafes_gpu_step will use. */
+int scafes_gpu_set_temporal_depth(scafes_handle* h, int depth);
+int scafes_gpu_temporal_depth(const scafes_handle* h, int* depth);
 
 /* Number of steps taken since the last upload of the unknown field. */
 int scafes_gpu_timestep(const scafes_handle* h, int* t);

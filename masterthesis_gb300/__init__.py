@@ -89,6 +89,8 @@ def lib() -> C.CDLL:
         L.scafes_gpu_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_step.argtypes = [vp, C.c_int]
         L.scafes_gpu_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
+        L.scafes_gpu_set_temporal_depth.argtypes = [vp, C.c_int]
+        L.scafes_gpu_temporal_depth.argtypes = [vp, C.POINTER(C.c_int)]
         L.scafes_gpu_timestep.argtypes = [vp, C.POINTER(C.c_int)]
         L.scafes_gpu_err_linf.argtypes = [vp, dp, dp]
         L.scafes_gpu_last_step_ms.argtypes = [vp, C.POINTER(C.c_float)]
@@ -197,6 +199,15 @@ class Plain:
 
     def step_snapshots(self, n_steps: int, interval: int, path, flags: int = SNAP_START | SNAP_END):
         _check(lib().scafes_gpu_step_snapshots(self.h, n_steps, interval, flags, str(path).encode()), self.h)
+
+    def set_temporal_depth(self, depth: int):
+        _check(lib().scafes_gpu_set_temporal_depth(self.h, depth), self.h)
+
+    @property
+    def temporal_depth(self) -> int:
+        d = C.c_int()
+        _check(lib().scafes_gpu_temporal_depth(self.h, C.byref(d)), self.h)
+        return d.value
 
     def set_border_forms(self, forms):
         _check(lib().scafes_gpu_set_border_forms(self.h, forms), self.h)

@@ -48,6 +48,9 @@ struct scafes_handle {
     CUtensorMap tmf[STAR7_NUM_TILES];     // TMA descriptors of F_A (box 32 x BY) per tile
     bool tmf_ok[STAR7_NUM_TILES] = {};
     int tile = 0;                         // tile variant of the sweep
+    int depth = 1;                        // temporal blocking depth (1 or 2)
+    CUtensorMap tm_tb[2];                 // TMA descriptors of u[0], u[1] for depth-2 passes
+    bool tm_tb_ok[2] = {};
     int* status = nullptr;                // device status word of the kernels
     int cur = 0;
     void* fld[SCAFES_FIELD_COUNT] = {};   // known slots (U slot unused here)
@@ -404,7 +407,23 @@ static const CUtensorMap* source_map(scafes_handle* h, int tile) {
     return &h->tmf[tile];
 }
 
-static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
+// TMA descriptor of buffer `buf` for the depth-2 pass (encoded on first use).
+static const CUtensorMap* tb_map(scafes_handle* h, int buf) {
+    if (!h->tm_tb_ok[buf]) {
+        int bw = 0, bh = 0;
+        star7_tb_box(h->cfg.precision, &bw, &bh);
+        CUresult r = make_tensor_map_3d(&h->tm_tb[buf], h->u[buf], (int)h->esz, h->L.nx, h->L.ny, h->L.nz,
+                                        (size_t)h->L.pitch * h->esz, (size_t)h->L.plane * h->esz, bw, bh);
+        if (r != CUDA_SUCCESS) {
+            fail(&h->err, SCAFES_ERR_CUDA, "cuTensorMapEncodeTiled (depth 2) failed (%d)", (int)r);
+            return nullptr;
+        }
+        h->tm_tb_ok[buf] = true;
+    }
+    return &h->tm_tb[buf];
+}
+
+static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed, int depth) {
     if (h->L.nl != 1) tile = STAR7_MULTI_LAYER_TILE;  // the only variant built for several layers
     Star7Launch a;
     a.precision = h->cfg.precision;
@@ -439,26 +458,55 @@ static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed) {
             return fail(&h->err, SCAFES_ERR_STATE,
                         "scafes_gpu_step: a border rule reads the source F, but no F_A is uploaded or cf == 0");
     }
+    a.tm_tb = nullptr;
+    const bool tb = depth == 2 && star7_tb_eligible(a);
+    if (tb)
+        for (int b = 0; b < 2; ++b)
+            if (!tb_map(h, b)) return SCAFES_ERR_CUDA;
     if (timed) CUDA_TRY(h, cudaEventRecord(h->ev0, h->stream));
     a.status = h->status;
-    for (int s = 0; s < n_steps; ++s) {
+    int launches = 0;
+    for (int s = 0; s < n_steps;) {
         a.tm_uo = &h->tm[h->cur][tile];
         a.uo = h->u[h->cur];
         a.un = h->u[h->cur ^ 1];
         a.time_old = h->cfg.t_start + h->t * h->cfg.tau;          // time(t)
         a.time_new = h->cfg.t_start + (h->t + 1) * h->cfg.tau;    // time(t+1)
+        a.time_new2 = h->cfg.t_start + (h->t + 2) * h->cfg.tau;   // time(t+2)
         a.mirror_corr = ldexp(1.0, h->t);                          // 2^(t_new - 1)
-        cudaError_t e = launch_star7(a, h->stream);
+        const int adv = (tb && n_steps - s >= 2) ? 2 : 1;
+        a.tm_tb = adv == 2 ? &h->tm_tb[h->cur] : nullptr;
+        cudaError_t e = adv == 2 ? launch_star7_tb(a, h->stream) : launch_star7(a, h->stream);
         if (e != cudaSuccess)
             return fail(&h->err, SCAFES_ERR_CUDA, "scafes_gpu_step: launch failed: %s", cudaGetErrorString(e));
         h->cur ^= 1;
-        h->t += 1;
+        h->t += adv;
+        s += adv;
+        ++launches;
     }
     if (timed) {
         CUDA_TRY(h, cudaEventRecord(h->ev1, h->stream));
         h->timed = true;
-        h->launches = n_steps;
+        h->launches = launches;
     }
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_set_temporal_depth(scafes_handle* h, int depth) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_set_temporal_depth: handle is NULL");
+    if (depth != 1 && depth != 2)
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_set_temporal_depth: depth %d (1 or 2)", depth);
+    h->depth = depth;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_temporal_depth(const scafes_handle* h, int* depth) {
+    if (!h || !depth) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_temporal_depth: NULL argument");
+    Star7Launch a;
+    a.border = h->cfg.border;
+    a.L = h->L;
+    a.fb = h->has[SCAFES_FIELD_F_B] ? h->fld[SCAFES_FIELD_F_B] : nullptr;
+    *depth = (h->depth == 2 && star7_tb_eligible(a)) ? 2 : 1;
     return SCAFES_OK;
 }
 
@@ -554,7 +602,7 @@ extern "C" int scafes_gpu_step(scafes_handle* h, int n_steps) {
     if (n_steps < 0) return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_step: n_steps=%d < 0", n_steps);
     if (!h->uploaded)
         return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_step: upload the unknown field first");
-    return step_impl(h, n_steps, h->tile, true);
+    return step_impl(h, n_steps, h->tile, true, h->depth);
 }
 
 // ---- snapshots ----------------------------------------------------------------
@@ -658,11 +706,11 @@ extern "C" int scafes_gpu_step_snapshots(scafes_handle* h, int n_steps, int inte
     for (long long t = t0 + 1; t <= t1 && rc == SCAFES_OK; ++t) {
         const bool at = (interval > 0 && t % interval == 0) || (t == t1 && (flags & SCAFES_SNAP_END));
         if (!at) continue;
-        rc = step_impl(h, (int)(t - done), h->tile, false);
+        rc = step_impl(h, (int)(t - done), h->tile, false, h->depth);
         done = t;
         if (rc == SCAFES_OK) rc = snap(t);
     }
-    if (rc == SCAFES_OK && done < t1) rc = step_impl(h, (int)(t1 - done), h->tile, false);
+    if (rc == SCAFES_OK && done < t1) rc = step_impl(h, (int)(t1 - done), h->tile, false, h->depth);
     if (rc == SCAFES_OK) {
         cudaError_t e = cudaEventRecord(h->ev1, h->stream);
         if (e != cudaSuccess) rc = fail(&h->err, SCAFES_ERR_CUDA, "scafes_gpu_step_snapshots: %s", cudaGetErrorString(e));
@@ -731,8 +779,8 @@ extern "C" int scafes_gpu_autotune(scafes_handle* h, int n_steps, int* chosen, f
     int best = h->tile, rc = SCAFES_OK;
     float best_ms = 0.f;
     for (int tile = 0; tile < STAR7_NUM_TILES && e == cudaSuccess && rc == SCAFES_OK; ++tile) {
-        rc = step_impl(h, 1, tile, false);  // warm-up (and first-use setup)
-        if (rc == SCAFES_OK) rc = step_impl(h, n_steps, tile, true);
+        rc = step_impl(h, 1, tile, false, 1);  // warm-up (and first-use setup)
+        if (rc == SCAFES_OK) rc = step_impl(h, n_steps, tile, true, 1);
         float ms = 0.f;
         if (rc == SCAFES_OK) {
             e = cudaEventSynchronize(h->ev1);
@@ -743,6 +791,25 @@ extern "C" int scafes_gpu_autotune(scafes_handle* h, int n_steps, int* chosen, f
             best_ms = ms;
             best = tile;
         }
+    }
+    // Temporal blocking: depth 2 (its own tile) against the best depth-1 tile.
+    int best_depth = 1;
+    int dep = 0;
+    const int n2 = n_steps + (n_steps & 1);
+    if (e == cudaSuccess && rc == SCAFES_OK && scafes_gpu_temporal_depth(h, &dep) == SCAFES_OK) {
+        const int keep = h->depth;
+        h->depth = 2;
+        if (scafes_gpu_temporal_depth(h, &dep) == SCAFES_OK && dep == 2) {
+            rc = step_impl(h, 2, best, false, 2);
+            if (rc == SCAFES_OK) rc = step_impl(h, n2, best, true, 2);
+            float ms = 0.f;
+            if (rc == SCAFES_OK) {
+                e = cudaEventSynchronize(h->ev1);
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+            }
+            if (rc == SCAFES_OK && e == cudaSuccess && ms / n2 < best_ms / n_steps) best_depth = 2;
+        }
+        h->depth = keep;
     }
     if (e == cudaSuccess) e = cudaMemcpyAsync(h->u[cur_save], save, bytes, cudaMemcpyDeviceToDevice, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -756,6 +823,7 @@ extern "C" int scafes_gpu_autotune(scafes_handle* h, int n_steps, int* chosen, f
     rc = check_status(h);
     if (rc) return rc;
     h->tile = best;
+    h->depth = best_depth;
     if (chosen) *chosen = best + 1;
     return SCAFES_OK;
 }

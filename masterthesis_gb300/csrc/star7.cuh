@@ -88,6 +88,8 @@ struct Star7Launch {
     Star7Coeffs c;
     double time_old;      // time(t)   : F is read at the old time
     double time_new;      // time(t+1) : G is read at the new time
+    double time_new2;     // time(t+2) : the second step of a depth-2 pass
+    const CUtensorMap* tm_tb;  // TMA descriptor of the old iterate for depth-2 passes
     double mirror_corr;   // 2^t for SCAFES_BORDER_MIRROR_POW2
     const BorderTable* table;  // device rules for SCAFES_BORDER_TABLE
 };
@@ -95,6 +97,16 @@ struct Star7Launch {
 // Enqueues one sweep (one time step) on `stream`.  Returns cudaSuccess or the
 // launch error.
 cudaError_t launch_star7(const Star7Launch& a, cudaStream_t stream);
+
+// Enqueues one depth-2 pass (two time steps; star7_tb.cuh) on `stream`:
+// Dirichlet border, one border layer, no time-dependent source, a.tm_tb
+// encoded by star7_tb_box.  Returns cudaErrorInvalidValue for any other
+// problem.
+cudaError_t launch_star7_tb(const Star7Launch& a, cudaStream_t stream);
+// TMA box (width, rows) of the depth-2 pass for a precision.
+void star7_tb_box(int precision, int* width, int* rows);
+// Whether a problem can take depth-2 passes.
+bool star7_tb_eligible(const Star7Launch& a);
 
 // Conversions between host-layout doubles (dense, x fastest) staged on the
 // device and the padded device layout of each precision.

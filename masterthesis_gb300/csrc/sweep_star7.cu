@@ -9,6 +9,7 @@
 // Each CTA runs one tile (star7_tile.cuh) over a chunk of z-planes; the
 // kernels are instantiated per element type in sweep_star7_{f64,f32x2,f32}.cu.
 // This file holds the host helpers and the dispatch on the element type.
+#include "star7_tb.cuh"
 #include "star7_tile.cuh"
 
 namespace scafes {
@@ -47,6 +48,28 @@ int star7_default_tile(const Layout& L) {
 cudaError_t launch_star7_f64(const Star7Launch& a, cudaStream_t stream);
 cudaError_t launch_star7_f32(const Star7Launch& a, cudaStream_t stream);
 cudaError_t launch_star7_f32x2(const Star7Launch& a, cudaStream_t stream);
+cudaError_t launch_star7_tb_f64(const Star7Launch& a, cudaStream_t stream);
+cudaError_t launch_star7_tb_f32(const Star7Launch& a, cudaStream_t stream);
+cudaError_t launch_star7_tb_f32x2(const Star7Launch& a, cudaStream_t stream);
+
+bool star7_tb_eligible(const Star7Launch& a) {
+    return a.border == SCAFES_BORDER_DIRICHLET && a.L.nl == 1 && a.fb == nullptr;
+}
+
+void star7_tb_box(int precision, int* width, int* rows) {
+    const int esz = (int)element_size(precision);
+    *width = tb_bw(esz);
+    *rows = TB_BH;
+}
+
+cudaError_t launch_star7_tb(const Star7Launch& a, cudaStream_t stream) {
+    switch (a.precision) {
+        case SCAFES_PREC_F64: return launch_star7_tb_f64(a, stream);
+        case SCAFES_PREC_F32: return launch_star7_tb_f32(a, stream);
+        case SCAFES_PREC_F32X2: return launch_star7_tb_f32x2(a, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
 
 cudaError_t launch_star7(const Star7Launch& a, cudaStream_t stream) {
     switch (a.precision) {

@@ -7,4 +7,8 @@ cudaError_t launch_star7_f32x2(const Star7Launch& a, cudaStream_t stream) {
     return launch_prec<PolF32x2>(a, stream);
 }
 
+cudaError_t launch_star7_tb_f32x2(const Star7Launch& a, cudaStream_t stream) {
+    return launch_tb_prec<PolF32x2>(a, stream);
+}
+
 }  // namespace scafes

@@ -7,4 +7,8 @@ cudaError_t launch_star7_f64(const Star7Launch& a, cudaStream_t stream) {
     return launch_prec<PolF64>(a, stream);
 }
 
+cudaError_t launch_star7_tb_f64(const Star7Launch& a, cudaStream_t stream) {
+    return launch_tb_prec<PolF64>(a, stream);
+}
+
 }  // namespace scafes

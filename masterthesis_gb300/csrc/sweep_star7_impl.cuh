@@ -3,6 +3,7 @@
 // so that the instantiations compile in parallel.
 #pragma once
 
+#include "star7_tb.cuh"
 #include "star7_tile.cuh"
 
 namespace scafes {
@@ -119,6 +120,45 @@ static cudaError_t launch_src(const Star7Launch& a, cudaStream_t stream) {
     if (a.fa == nullptr || a.c.cf == 0.0) return launch_tile<P, SRC_NONE, BORDER>(a, stream);
     if (a.fb == nullptr) return launch_tile<P, SRC_A, BORDER>(a, stream);
     return launch_tile<P, SRC_AB, BORDER>(a, stream);
+}
+
+// z-planes per CTA of a depth-2 pass: long chunks (each recomputes two
+// intermediate planes and reads four extra input planes), shorter ones
+// while the grid has few column tiles.
+static int tb_zchunk(const Layout& L) {
+    const long long tiles = (long long)((L.nx + TB_X - 1) / TB_X) * ((L.ny + TB_Y - 1) / TB_Y);
+    int zc = 64;
+    while (zc > 8 && tiles * ((L.nz + zc - 1) / zc) < (long long)num_sms() * 8) zc >>= 1;
+    return zc;
+}
+
+template <class P, bool HAS_F>
+static cudaError_t launch_tb_typed(const Star7Launch& a, cudaStream_t stream) {
+    using T = typename P::T;
+    auto kern = star7_tb2<P, HAS_F>;
+    constexpr size_t SMEM = tb_smem(sizeof(T));
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        attr = true;
+    }
+    T gval;
+    to_elem(a.gconst, gval);
+    const Layout& L = a.L;
+    const int zc = tb_zchunk(L);
+    const dim3 grid((L.nx + TB_X - 1) / TB_X, (L.ny + TB_Y - 1) / TB_Y, (L.nz + zc - 1) / zc);
+    kern<<<grid, dim3(TB_X, TB_TY), SMEM, stream>>>(*a.tm_tb, (T*)a.un, (const T*)a.fa, (const T*)a.ga,
+                                                     (const T*)a.gb, gval, L, a.c, make_split(a.time_new),
+                                                     make_split(a.time_new2), zc, a.status);
+    return cudaGetLastError();
+}
+
+template <class P>
+cudaError_t launch_tb_prec(const Star7Launch& a, cudaStream_t stream) {
+    if (!star7_tb_eligible(a) || a.tm_tb == nullptr) return cudaErrorInvalidValue;
+    if (a.fa == nullptr || a.c.cf == 0.0) return launch_tb_typed<P, false>(a, stream);
+    return launch_tb_typed<P, true>(a, stream);
 }
 
 template <class P>
