@@ -243,8 +243,10 @@ def run_batched(M, args, dist: Dist, hbm_peak: float):
     T = args.batch_time_steps
     out = {"workload": f"Pennes ensemble: {len(specs)} instances, sizes {{32,48,...,160}}^3 (seed 8), "
                        f"FP64, {T} steps, Dirichlet 37, Gaussian source"}
+    f64_final = []
     for prec in ("f64", "f32x2"):
         b = M.Batch([W.pennes_batch_instance(s) for s in specs], precision=prec)
+        err = None
         try:
             for i, s in enumerate(specs):
                 b.upload(i, M.FIELD_F_A, W.pennes_source(s))
@@ -259,6 +261,19 @@ def run_batched(M, args, dist: Dist, hbm_peak: float):
             b.step_looped(T)
             ms_l = dist.max(b.last_ms())
             launches_l = b.info()["launches"]
+            # The pair result's distance to the FP64 one after the
+            # workload's T steps (a fresh start from the initial iterate).
+            for i, s in enumerate(specs):
+                b.upload(i, M.FIELD_U, np.full((s["n"][2], s["n"][1], s["n"][0]), W.T_ARTERIAL))
+            b.step(T)
+            if prec == "f64":
+                f64_final = [b.download(i) for i in range(len(specs))]
+            else:
+                err = 0.0
+                for i in range(len(specs)):
+                    ref = f64_final[i]
+                    err = max(err, float(np.max(np.abs(b.download(i) - ref))) / float(np.max(np.abs(ref))))
+                f64_final = []
         finally:
             b.close()
         lup = nodes * T
@@ -268,6 +283,9 @@ def run_batched(M, args, dist: Dist, hbm_peak: float):
                      "hbm_frac": 24 * lup / (ms_b * 1e-3) / 1e9 / hbm_peak, "ms": ms_b, "looped_ms": ms_l,
                      "nodes": nodes, "tile": tile, "ctas_per_sm": ctas, "launches": launches_b,
                      "looped_launches": launches_l}
+        if err is not None:
+            out[prec]["max_rel_err_vs_f64"] = err
+            out[prec]["steps_compared"] = T
     return out
 
 

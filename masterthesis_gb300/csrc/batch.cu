@@ -15,6 +15,7 @@
 // picks the tile variant and the CTAs per SM.  For comparison,
 // scafes_batch_step_looped runs the reference's schedule on the GPU: one
 // plain launch per instance per step.
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <map>
@@ -38,8 +39,20 @@ struct BatchInst {
     long long off_u[2];  // element offsets of the two iterates in the pool
     long long off_f;     // element offset of the source field
     Star7Coeffs c;
-    double gconst;
+    double gconst;       // Dirichlet value the kernels write (0 in deviation form)
+    // Deviation form of the FP32-based element types: the device holds
+    // u - shift and F + fshift, fshift = shift * (c0 + 2 sum cp - 1) / cf,
+    // which is the same update (a constant Dirichlet value g makes
+    // u' - g = c0 (u - g) + sum cp (nb - g) + cf (F + g (c0 + 2 sum cp - 1) / cf)).
+    // A field near a large constant value then keeps its pair precision
+    // for the deviation.  FP64 keeps shift = 0: the reference's arithmetic.
+    double shift, fshift;
 };
+
+__global__ void k_add_scalar(double* __restrict__ a, size_t n, double v) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        a[i] += v;
+}
 
 struct BatchItem {
     int inst;
@@ -355,6 +368,13 @@ extern "C" int scafes_batch_create(const scafes_batch_instance* in, int n_inst, 
         I.off_f = (long long)total; total += sz;
         I.c = make_star7_coeffs(in[i].c0, in[i].cp, in[i].cf);
         I.gconst = in[i].g_value;
+        I.shift = I.fshift = 0.0;
+        const double k = in[i].c0 + 2.0 * (in[i].cp[0] + in[i].cp[1] + in[i].cp[2]) - 1.0;
+        if (precision != SCAFES_PREC_F64 && in[i].g_value != 0.0 && (k == 0.0 || in[i].cf != 0.0)) {
+            I.shift = in[i].g_value;
+            I.fshift = k == 0.0 ? 0.0 : in[i].g_value * k / in[i].cf;
+            I.gconst = 0.0;
+        }
     }
     b->pool_elems = total;
     if ((e = cudaMalloc(&b->pool, total * b->esz)) != cudaSuccess) {
@@ -370,6 +390,40 @@ extern "C" int scafes_batch_create(const scafes_batch_instance* in, int n_inst, 
         (e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess) {
         bfail(nullptr, SCAFES_ERR_CUDA, "scafes_batch_create: %s", cudaGetErrorString(e));
         return bail(SCAFES_ERR_CUDA);
+    }
+    // Fields not uploaded read as 0: in deviation form that is -shift for
+    // the iterates and fshift for the source.
+    {
+        size_t most = 0;
+        for (const BatchInst& I : b->hinst)
+            if (I.shift != 0.0) most = std::max(most, (size_t)I.L.nx * I.L.ny * I.L.nz);
+        if (most > 0) {
+            double* stage = nullptr;
+            e = cudaMalloc(&stage, most * sizeof(double));
+            for (size_t i = 0; i < b->hinst.size() && e == cudaSuccess; ++i) {
+                const BatchInst& I = b->hinst[i];
+                if (I.shift == 0.0) continue;
+                const size_t nn = (size_t)I.L.nx * I.L.ny * I.L.nz;
+                const double fill[3] = {-I.shift, -I.shift, I.fshift};
+                const long long offs[3] = {I.off_u[0], I.off_u[1], I.off_f};
+                for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+                    e = cudaMemsetAsync(stage, 0, nn * sizeof(double), b->stream);
+                    if (e == cudaSuccess) {
+                        k_add_scalar<<<256, 256, 0, b->stream>>>(stage, nn, fill[k]);
+                        e = cudaGetLastError();
+                    }
+                    if (e == cudaSuccess)
+                        e = convert_to_device(precision, stage, (char*)b->pool + (size_t)offs[k] * b->esz, I.L,
+                                              b->stream);
+                }
+            }
+            if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+            cudaFree(stage);
+            if (e != cudaSuccess) {
+                bfail(nullptr, SCAFES_ERR_CUDA, "scafes_batch_create: %s", cudaGetErrorString(e));
+                return bail(SCAFES_ERR_CUDA);
+            }
+        }
     }
     // Tensor maps of every instance, field (two iterates with halo boxes,
     // the source with a 32 x BY box) and tile variant.
@@ -431,11 +485,22 @@ static int transfer(scafes_batch* b, int i, int field, double* host, size_t n, b
     double* stage = nullptr;
     BTRY(b, cudaMalloc(&stage, nn * sizeof(double)));
     cudaError_t e;
+    // Deviation form (FP32-based types): the iterate is held as u - shift,
+    // the source as F + fshift.
+    const double add = field == SCAFES_FIELD_U ? -I.shift : I.fshift;
     if (up) {
         e = cudaMemcpyAsync(stage, host, nn * sizeof(double), cudaMemcpyHostToDevice, b->stream);
+        if (e == cudaSuccess && add != 0.0) {
+            k_add_scalar<<<256, 256, 0, b->stream>>>(stage, nn, add);
+            e = cudaGetLastError();
+        }
         if (e == cudaSuccess) e = convert_to_device(b->precision, stage, dev, I.L, b->stream);
     } else {
         e = convert_from_device(b->precision, dev, stage, I.L, b->stream);
+        if (e == cudaSuccess && add != 0.0) {
+            k_add_scalar<<<256, 256, 0, b->stream>>>(stage, nn, -add);
+            e = cudaGetLastError();
+        }
         if (e == cudaSuccess) e = cudaMemcpyAsync(host, stage, nn * sizeof(double), cudaMemcpyDeviceToHost, b->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);

@@ -75,6 +75,33 @@ def test_batch_queue_equals_batch(gpu, prec):
             q.run(1)                                    # nothing enqueued
 
 
+@pytest.mark.parametrize("prec", ["f32x2", "f32"])
+def test_batch_deviation_form_round_trips(gpu, prec):
+    """The FP32-based types hold u - g and F + fshift on the device (g the
+    Dirichlet value): uploads and downloads give back the caller's values, a
+    source that is never uploaded reads as 0 (to the element type's
+    precision of the offset), and the results match FP64
+    (1e-12 for pairs, 2e-5 for FP32 -- their usual bounds)."""
+    M = gpu
+    specs = small_ensemble(n_inst=4, seed=9)
+    tol = 1e-12 if prec == "f32x2" else 2e-5
+    with M.Batch([W.pennes_batch_instance(s) for s in specs], precision=prec) as b, \
+            M.Batch([W.pennes_batch_instance(s) for s in specs], precision="f64") as r:
+        for i, s in enumerate(specs):
+            shape = (s["n"][2], s["n"][1], s["n"][0])
+            u0 = np.full(shape, W.T_ARTERIAL) + np.random.default_rng(i).uniform(-0.5, 0.5, shape)
+            b.upload(i, M.FIELD_U, u0)
+            r.upload(i, M.FIELD_U, u0)
+            if prec == "f32x2":
+                assert cases.rel_err(b.download(i), u0) <= 1e-15
+            # the source offset round-trips to pair (FP32) precision of fshift
+            assert np.max(np.abs(b.download(i, M.FIELD_F_A))) <= (1e-14 if prec == "f32x2" else 1e-6)
+        b.step(40)
+        r.step(40)
+        for i in range(len(specs)):
+            assert cases.rel_err(b.download(i), r.download(i)) <= tol, i
+
+
 def test_batch_equals_looped_and_all_schedules(gpu):
     M = gpu
     specs = small_ensemble(n_inst=9, seed=4)
