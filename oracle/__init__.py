@@ -71,6 +71,7 @@ def lib():
                                                                          Known, C.c_int]
         L.orc_heat_radiation.argtypes = [C.POINTER(Grid)] + [C.c_double] * 7 + [C.c_int, dp, Known, Known,
                                                                               Known, C.c_int]
+        L.orc_kheat_tangent.argtypes = [C.POINTER(Grid), dp, dp, C.c_int, dp, dp, C.c_int]
         L.orc_stencil_width_one.argtypes = [C.POINTER(Grid), C.c_int, dp, C.c_int]
         L.orc_stencil_width_var.argtypes = [C.POINTER(Grid), C.c_int, C.c_int, dp, C.c_int]
         L.orc_kheat_forward.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.c_int]
@@ -190,6 +191,16 @@ def kheat_forward(g: Grid, k, u0, nsteps, keep_traj=False, nthreads=0):
     traj = np.empty((nsteps + 1,) + u.shape, dtype=np.float64) if keep_traj else None
     _check(lib().orc_kheat_forward(C.byref(g), _p(k), nsteps, _p(u), _p(traj), nthreads), "kheat_forward")
     return (u, traj) if keep_traj else u
+
+
+def kheat_tangent(g: Grid, k, dk, u0, du0, nsteps, nthreads=0):
+    """Forward-mode AD of the variable-k solve: (u_T, du_T) along (dk, du0)."""
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    du = np.ascontiguousarray(du0, dtype=np.float64).copy()
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    dk = np.ascontiguousarray(dk, dtype=np.float64)
+    _check(lib().orc_kheat_tangent(C.byref(g), _p(k), _p(dk), nsteps, _p(u), _p(du), nthreads), "kheat_tangent")
+    return u, du
 
 
 def kheat_adjoint(g: Grid, k, traj, target, nthreads=0):

@@ -476,6 +476,69 @@ int orc_kheat_forward(const orc_grid* g, const double* k, int nsteps,
     return 0;
 }
 
+/* Forward-mode automatic differentiation of orc_kheat_forward: every
+ * value is a dual number (value, derivative along one direction) and every
+ * operation of kheat_step is applied to duals -- the forward vector mode
+ * the reference runs through ADOL-C (fov_forward, src/ScaFES_Problem.hpp:
+ * 6633-6747), here with one direction and a project-written dual type. */
+typedef struct { double v, d; } orc_dual;
+
+static orc_dual dadd(orc_dual a, orc_dual b) { orc_dual r = {a.v + b.v, a.d + b.d}; return r; }
+static orc_dual dsub(orc_dual a, orc_dual b) { orc_dual r = {a.v - b.v, a.d - b.d}; return r; }
+static orc_dual dmul(orc_dual a, orc_dual b) { orc_dual r = {a.v * b.v, a.d * b.v + a.v * b.d}; return r; }
+static orc_dual dconst(double c) { orc_dual r = {c, 0.0}; return r; }
+
+static void kheat_step_dual(const orc_grid* g, const orc_dual* k, const orc_dual* uo, orc_dual* un)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const long stride[3] = {1, nx, (long)nx * ny};
+#pragma omp parallel for schedule(static)
+    for (int kk = 0; kk < nz; ++kk) {
+        for (int j = 0; j < ny; ++j) {
+            for (int i = 0; i < nx; ++i) {
+                const size_t m = IDX(i, j, kk, nx, ny);
+                if (orc_is_border(g, i, j, kk)) { un[m] = uo[m]; continue; }
+                orc_dual v = uo[m];
+                for (int p = 0; p < g->dim; ++p) {
+                    const orc_dual c = dconst(g->tau / (g->h[p] * g->h[p]));
+                    const orc_dual kp = dmul(dconst(0.5), dadd(k[m], k[m + stride[p]]));
+                    const orc_dual km = dmul(dconst(0.5), dadd(k[m], k[m - stride[p]]));
+                    v = dadd(v, dmul(c, dsub(dmul(kp, dsub(uo[m + stride[p]], uo[m])),
+                                             dmul(km, dsub(uo[m], uo[m - stride[p]])))));
+                }
+                un[m] = v;
+            }
+        }
+    }
+}
+
+int orc_kheat_tangent(const orc_grid* g, const double* k, const double* dk, int nsteps,
+                      double* u, double* du, int nthreads)
+{
+    const size_t nn = n_total(g);
+    orc_dual* kd = (orc_dual*)malloc(nn * sizeof(orc_dual));
+    orc_dual* a = (orc_dual*)malloc(nn * sizeof(orc_dual));
+    orc_dual* b = (orc_dual*)malloc(nn * sizeof(orc_dual));
+    if (!kd || !a || !b) { free(kd); free(a); free(b); return -1; }
+    set_threads(nthreads);
+    for (size_t m = 0; m < nn; ++m) {
+        kd[m].v = k[m];
+        kd[m].d = dk[m];
+        a[m].v = u[m];
+        a[m].d = du[m];
+    }
+    for (int t = 1; t <= nsteps; ++t) {
+        kheat_step_dual(g, kd, a, b);
+        orc_dual* tmp = a; a = b; b = tmp;
+    }
+    for (size_t m = 0; m < nn; ++m) {
+        u[m] = a[m].v;
+        du[m] = a[m].d;
+    }
+    free(kd); free(a); free(b);
+    return 0;
+}
+
 int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
                       const double* traj, const double* target,
                       double* grad_k, double* grad_u0, double* j_out,

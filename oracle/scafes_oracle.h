@@ -123,6 +123,14 @@ void orc_err_linf(const double* u, const double* exact, size_t n,
 int orc_kheat_forward(const orc_grid* g, const double* k, int nsteps,
                       double* u, double* traj, int nthreads);
 
+/* Forward-mode AD (dual numbers) of orc_kheat_forward along one direction:
+ * on entry u = u0, du = the u0 direction, dk = the k direction; on exit
+ * u = u_T and du = its derivative.  The same mode as the reference's ADOL-C
+ * gradient (fov_forward, src/ScaFES_Problem.hpp:6633-6747), so
+ * <u_T - target, du> checks the adjoint's <dJ/dk, dk> + <dJ/du0, du0>. */
+int orc_kheat_tangent(const orc_grid* g, const double* k, const double* dk, int nsteps,
+                      double* u, double* du, int nthreads);
+
 /* Adjoint of orc_kheat_forward for J = 0.5 ||u_T - target||^2.
  * traj holds the nsteps+1 forward iterates. Outputs dJ/dk and dJ/du0 and
  * returns J in *j_out. */

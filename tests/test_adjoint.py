@@ -115,6 +115,31 @@ def test_adjoint_backward_with_cotangent(gpu, prec):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-11), ("f32x2", 1e-9)])
+def test_adjoint_matches_forward_mode_ad_32(gpu, prec, tol):
+    """The GPU gradient at 32^3 (checkpointed, 8 snapshots over 60 steps)
+    against forward-mode AD of the forward solve on the CPU (dual numbers:
+    the mode of the reference's ADOL-C gradient, which is not available):
+    <dJ/dk, dk> + <dJ/du0, du0> = <u_T - target, du_T> on 4 seeded
+    directions, to 1e-11 (FP64) and 1e-9 (pairs, whose gradient fields are
+    within 1e-10 of FP64)."""
+    M = gpu
+    n, T = (32, 32, 32), 60
+    k, tau, u0, target = kheat_problem(n, T, 13)
+    with M.Adjoint(n, tau, 8, precision=prec) as a:
+        a.set_conductivity(k)
+        _, gk, gu = a.gradient(u0, target, T)
+    g = O.make_grid(n, tau=tau)
+    for seed in range(4):
+        dk = np.random.default_rng(500 + seed).standard_normal(u0.shape)
+        du0 = np.random.default_rng(600 + seed).standard_normal(u0.shape)
+        uT, duT = O.kheat_tangent(g, k, dk, u0, du0, T)
+        dJ = float(np.sum((uT - target) * duT))
+        adj = float(np.sum(gk * dk) + np.sum(gu * du0))
+        assert abs(dJ - adj) <= tol * abs(dJ), (seed, dJ, adj)
+
+
+@pytest.mark.gpu
 def test_adjoint_forward_matches_oracle(gpu):
     M = gpu
     n, T = (17, 9, 13), 25

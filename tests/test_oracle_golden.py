@@ -125,6 +125,32 @@ def test_kheat_adjoint_matches_finite_differences():
         assert abs(fd_u - np.sum(gu * du)) <= 1e-6 * max(abs(fd_u), 1e-12)
 
 
+def test_kheat_adjoint_matches_forward_mode_ad():
+    """The oracle's adjoint against forward-mode AD of the forward solve (a
+    dual-number restatement: the reference's ADOL-C gradient path is forward
+    vector mode, fov_forward, and ADOL-C is not available here).  Exact
+    derivatives on both sides: agreement to rounding, 1e-11 relative, at
+    32^3 -- the size the reference's gradient is quoted at."""
+    n, T = (32, 32, 32), 20
+    h2 = sum((m - 1) ** 2 for m in n)
+    g = O.make_grid(n, tau=0.4 / (2.0 * h2))
+    rng = np.random.default_rng(7)
+    shape = (n[2], n[1], n[0])
+    k = np.exp(0.3 * rng.standard_normal(shape))
+    u0 = rng.uniform(-1, 1, shape)
+    target = rng.uniform(-1, 1, shape)
+    _, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
+    _, gk, gu = O.kheat_adjoint(g, k, traj, target)
+    for seed in range(2):
+        dk = np.random.default_rng(300 + seed).standard_normal(shape)
+        du0 = np.random.default_rng(400 + seed).standard_normal(shape)
+        uT, duT = O.kheat_tangent(g, k, dk, u0, du0, T)
+        assert np.array_equal(uT, traj[-1])  # the value part is the forward solve
+        dJ = float(np.sum((uT - target) * duT))
+        adj = float(np.sum(gk * dk) + np.sum(gu * du0))
+        assert abs(dJ - adj) <= 1e-11 * abs(dJ), (dJ, adj)
+
+
 def flux_case(name):
     """Inputs of a flux-border TimeLinSpaceLin golden case (the known fields
     of tests/system/{HeatEqnFDM,PennesBioheatEqnFDM}/{Neumann,Cauchy}/
