@@ -251,9 +251,13 @@ static int ensure_stage(scafes_handle* h) {
 static int h2d(scafes_handle* h, void* dst, int prec, const double* host) {
     const Layout& L = h->L;
     if (prec == SCAFES_PREC_F64) {
-        CUDA_TRY(h, cudaMemcpy2DAsync(dst, (size_t)L.pitch * sizeof(double), host,
-                                      (size_t)L.nx * sizeof(double), (size_t)L.nx * sizeof(double),
-                                      (size_t)L.ny * L.nz, cudaMemcpyHostToDevice, h->stream));
+        if (L.pitch == L.nx)  // unpadded rows: one contiguous copy
+            CUDA_TRY(h, cudaMemcpyAsync(dst, host, (size_t)L.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                        h->stream));
+        else
+            CUDA_TRY(h, cudaMemcpy2DAsync(dst, (size_t)L.pitch * sizeof(double), host,
+                                          (size_t)L.nx * sizeof(double), (size_t)L.nx * sizeof(double),
+                                          (size_t)L.ny * L.nz, cudaMemcpyHostToDevice, h->stream));
         return SCAFES_OK;
     }
     int rc = ensure_stage(h);
@@ -277,9 +281,13 @@ static int h2d(scafes_handle* h, void* dst, int prec, const double* host) {
 static int d2h(scafes_handle* h, const void* src, int prec, double* host) {
     const Layout& L = h->L;
     if (prec == SCAFES_PREC_F64) {
-        CUDA_TRY(h, cudaMemcpy2DAsync(host, (size_t)L.nx * sizeof(double), src,
-                                      (size_t)L.pitch * sizeof(double), (size_t)L.nx * sizeof(double),
-                                      (size_t)L.ny * L.nz, cudaMemcpyDeviceToHost, h->stream));
+        if (L.pitch == L.nx)
+            CUDA_TRY(h, cudaMemcpyAsync(host, src, (size_t)L.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        h->stream));
+        else
+            CUDA_TRY(h, cudaMemcpy2DAsync(host, (size_t)L.nx * sizeof(double), src,
+                                          (size_t)L.pitch * sizeof(double), (size_t)L.nx * sizeof(double),
+                                          (size_t)L.ny * L.nz, cudaMemcpyDeviceToHost, h->stream));
         return SCAFES_OK;
     }
     int rc = ensure_stage(h);
