@@ -524,6 +524,17 @@ int scafes_err_linf_noalloc(const double* u, const double* exact, long long n,
  * the benchmark reports beside the HBM roofline. */
 int scafes_probe_pipe_rates(double* fp64_gops, double* fp32_gops);
 
+/* Failure-detection checks (no fault involved).  scafes_probe_wait_timeout
+ * runs the bounded device wait of the sweep kernels on an mbarrier that
+ * never completes, with a limit of limit_us (1 .. 1e6): *status receives
+ * the status the kernel recorded (SCAFES_ERR_TIMEOUT) and *waited_ms the
+ * time it waited.  scafes_gpu_inject_status writes `code` (<= 0) into a
+ * handle's device status word, as a sweep that gave up does: later sweeps
+ * of the handle skip their work and the next download reports the status
+ * (and clears it). */
+int scafes_probe_wait_timeout(unsigned limit_us, int* status, double* waited_ms);
+int scafes_gpu_inject_status(scafes_handle* h, int code);
+
 #ifdef __cplusplus
 }
 #endif

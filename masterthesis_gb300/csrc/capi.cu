@@ -500,6 +500,14 @@ static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed, int de
     return SCAFES_OK;
 }
 
+extern "C" int scafes_gpu_inject_status(scafes_handle* h, int code) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_inject_status: handle is NULL");
+    if (code > 0) return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_inject_status: code %d > 0", code);
+    CUDA_TRY(h, cudaMemcpyAsync(h->status, &code, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return SCAFES_OK;
+}
+
 extern "C" int scafes_gpu_set_temporal_depth(scafes_handle* h, int depth) {
     if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_set_temporal_depth: handle is NULL");
     if (depth != 1 && depth != 2)

@@ -4,6 +4,7 @@
 // benchmark reports that bound beside the HBM one.
 #include <cuda_runtime.h>
 
+#include "tma.cuh"
 #include "../../include/scafes_gb300.h"
 
 namespace {
@@ -32,7 +33,59 @@ __global__ void k_ffma_rate(float* out, float a, float b) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// One CTA waits, with the bounded wait of the sweep kernels, on an
+// mbarrier that nothing arrives at: the wait must give up after limit_ns
+// and the kernel report it in the status word, as a sweep whose TMA load
+// never completed does.
+__global__ void k_wait_probe(unsigned long long limit_ns, int* status, unsigned long long* waited_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        scafes::mbar_init(&bar, 1);
+        scafes::fence_barrier_init();
+    }
+    __syncthreads();
+    const unsigned long long t0 = scafes::global_timer_ns();
+    const bool ok = scafes::bounded_wait(&bar, 0, limit_ns);
+    if (!__syncthreads_and(ok) && threadIdx.x == 0) {
+        atomicExch(status, SCAFES_ERR_TIMEOUT);
+        *waited_ns = scafes::global_timer_ns() - t0;
+    }
+}
+
 }  // namespace
+
+// No counterpart in the reference: exercises the timeout path of the
+// bounded device waits without any fault (no load is ever issued; the
+// barrier simply never completes).  limit_us in [1, 1e6].  Writes the
+// status the kernel recorded (SCAFES_ERR_TIMEOUT expected) and the time it
+// waited; synchronises the device.
+extern "C" int scafes_probe_wait_timeout(unsigned limit_us, int* status, double* waited_ms) {
+    if (!status || !waited_ms || limit_us < 1 || limit_us > 1000000) return SCAFES_ERR_ARG;
+    int* d_status = nullptr;
+    unsigned long long* d_waited = nullptr;
+    if (cudaMalloc(&d_status, sizeof(int)) != cudaSuccess) return SCAFES_ERR_CUDA;
+    if (cudaMalloc(&d_waited, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaFree(d_status);
+        return SCAFES_ERR_CUDA;
+    }
+    int st = 0;
+    unsigned long long w = 0;
+    cudaError_t e = cudaMemset(d_status, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(d_waited, 0, sizeof(unsigned long long));
+    if (e == cudaSuccess) {
+        k_wait_probe<<<1, 64>>>((unsigned long long)limit_us * 1000ull, d_status, d_waited);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&st, d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&w, d_waited, sizeof(w), cudaMemcpyDeviceToHost);
+    cudaFree(d_status);
+    cudaFree(d_waited);
+    if (e != cudaSuccess) return SCAFES_ERR_CUDA;
+    *status = st;
+    *waited_ms = (double)w * 1e-6;
+    return SCAFES_OK;
+}
 
 // No counterpart in the reference: a measurement utility for the roofline.
 extern "C" int scafes_probe_pipe_rates(double* fp64_gops, double* fp32_gops) {
