@@ -53,6 +53,8 @@ public:
             else if (key == "gpuAutotune") mGpuAutotune = std::atoi(val.c_str()) != 0;
             else if (key == "nSnapshots") mNsnapshots = std::atoi(val.c_str());
             else if (key == "gpuSnapshotFile") mGpuSnapshotFile = val;
+            else if (key == "initfile") { mNameInitFile = val; mReadInitFile = true; }
+            else if (key == "initfileIndex") mInitFileIndex = std::atoi(val.c_str());
         }
         mNnodes.resize(mDim, mNnodes.empty() ? 32 : mNnodes.back());
         mCoordNodeFirst.resize(mDim, 0.0);
@@ -83,7 +85,14 @@ public:
     int rank() const { return 0; }
     int rankOutput() const { return 0; }
     bool enabledAdolc() const { return false; }
-    bool readInitFile() const { return false; }
+    // --initfile (src/ScaFES_Parameters.hpp:518, 937-941): the unknown
+    // fields start from a file instead of initInner/initBorder.  Here the
+    // file is a snapshot file of the GPU path (scafes_gpu_step_snapshots);
+    // --initfileIndex picks the snapshot (default 0, the reference's
+    // readDfsFromFile(0); -1 = the last one).
+    const bool& readInitFile() const { return mReadInitFile; }
+    const std::string& nameInitFile() const { return mNameInitFile; }
+    const int& initFileIndex() const { return mInitFileIndex; }
 
     void setDim(int d) { mDim = d; mNnodes.resize(d, 32); mCoordNodeFirst.resize(d, 0.0); mCoordNodeLast.resize(d, 1.0); }
     void setNnodes(const std::vector<int>& n) { mNnodes = n; }
@@ -99,6 +108,11 @@ public:
     void setGpuAutotune(bool a) { mGpuAutotune = a; }
     void setNsnapshots(int n) { mNsnapshots = n; }
     void setGpuSnapshotFile(const std::string& f) { mGpuSnapshotFile = f; }
+    void setInitFile(const std::string& f, int index = 0) {
+        mNameInitFile = f;
+        mReadInitFile = !f.empty();
+        mInitFileIndex = index;
+    }
 
 private:
     template <typename T>
@@ -128,6 +142,9 @@ private:
     bool mGpuAutotune = false;
     int mNsnapshots = 1;  // the reference's default (src/ScaFES_Parameters.hpp:446)
     std::string mGpuSnapshotFile;
+    std::string mNameInitFile = "EMPTYINITFILE";  // the reference's default name (:451)
+    bool mReadInitFile = false;
+    int mInitFileIndex = 0;
 };
 
 }  // namespace ScaFES

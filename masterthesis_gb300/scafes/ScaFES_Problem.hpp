@@ -480,11 +480,33 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     }
     mWallClockTimes["evalKnownDf"] += std::chrono::duration<double>(clock::now() - t_eval).count();
 
-    // 2. Initial iterate (time step 0) on the host.
+    // 2. Initial iterate (time step 0) on the host: initInner/initBorder,
+    // or a snapshot file with --initfile (evalInitPbPhase, :2766-2790,
+    // readDfsFromFile :4427).
     auto t_init = clock::now();
     std::copy(k0.begin(), k0.end(), mKnownNewStore.begin());
     mKnownOldStore = k0;
-    {
+    if (mParams.readInitFile()) {
+        int nn[3] = {0, 0, 0}, count = 0;
+        const std::string& path = mParams.nameInitFile();
+        if (scafes_snapshot_info(path.c_str(), nn, &count) != SCAFES_OK)
+            throw std::runtime_error("ScaFES::Problem: cannot read init file " + path + ": " + scafes_last_error());
+        for (std::size_t p = 0; p < DIM; ++p)
+            if (nn[p] != g.nNodes(p))
+                throw std::runtime_error("ScaFES::Problem: init file " + path + " holds another grid");
+        int idx = mParams.initFileIndex();
+        if (idx < 0) idx += count;
+        if (idx < 0 || idx >= count)
+            throw std::runtime_error("ScaFES::Problem: init file " + path + " has no snapshot " +
+                                     std::to_string(mParams.initFileIndex()));
+        std::vector<double> u((std::size_t)mN);
+        long long step = 0;
+        double t_file = 0.0;
+        if (scafes_snapshot_read(path.c_str(), idx, u.data(), u.size(), &step, &t_file) != SCAFES_OK)
+            throw std::runtime_error("ScaFES::Problem: cannot read init file " + path + ": " + scafes_last_error());
+        for (long long m = 0; m < mN; ++m) mUnknownNewStore[m] = (CT)u[m];
+        for (auto& df : mVectUnknownDfsDomNew) df.time() = (CT)time(0);
+    } else {
         OWNPRBLM* self = static_cast<OWNPRBLM*>(this);
         for (auto& df : mVectUnknownDfsDomNew) df.time() = (CT)time(0);
 #ifdef _OPENMP

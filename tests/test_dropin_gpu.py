@@ -116,3 +116,30 @@ def test_dropin_writes_snapshots_like_given_at_cl(gpu, run_problem, tmp_path):
     assert steps == [0, 100, 200, 300]
     assert np.array_equal(M.snapshot_read(snap, 3)[0], u)
     assert cases.rel_err(u, d["final"]) <= 1e-12
+
+
+def test_dropin_restarts_from_init_file(gpu, run_problem, tmp_path):
+    """--initfile (the reference's restart: evalInitPbPhase reads the
+    unknown fields from a file instead of calling initInner/initBorder):
+    a run of the last 200 steps started from the snapshot at step 100 of a
+    300-step run, with --starttime at that step's time, ends where the full
+    run ends (1e-12; tau is recomputed from the shorter interval, so the
+    last bits may differ).  A missing or mismatched file is refused."""
+    d = load_golden("heat_timelin")
+    n = tuple(int(v) for v in d["n"])
+    snap = tmp_path / "u.snap"
+    full, _ = run(run_problem, "heat_lin", tmp_path / "u.bin", n, f"--nNodes={n[0]}x{n[1]}x{n[2]}",
+                  "--nTimesteps=300", "--endtime=1.0", "--nSnapshots=3", f"--gpuSnapshotFile={snap}",
+                  "--write-like-cl")
+    t100 = 100 * (1.0 / 300)
+    part, out = run(run_problem, "heat_lin", tmp_path / "v.bin", n, f"--nNodes={n[0]}x{n[1]}x{n[2]}",
+                    "--nTimesteps=200", f"--starttime={t100!r}", "--endtime=1.0", f"--initfile={snap}",
+                    "--initfileIndex=1")
+    assert cases.rel_err(part, full) <= 1e-12
+    res = subprocess.run([str(run_problem), "heat_lin", str(tmp_path / "w.bin"), "--nNodes=9x8x8",
+                          "--nTimesteps=10", f"--initfile={snap}"], capture_output=True, text=True, timeout=120)
+    assert res.returncode != 0 and "another grid" in (res.stdout + res.stderr)
+    res = subprocess.run([str(run_problem), "heat_lin", str(tmp_path / "w.bin"), f"--nNodes={n[0]}x{n[1]}x{n[2]}",
+                          "--nTimesteps=10", f"--initfile={tmp_path / 'missing.snap'}"],
+                         capture_output=True, text=True, timeout=120)
+    assert res.returncode != 0 and "init file" in (res.stdout + res.stderr)
