@@ -502,21 +502,26 @@ def run_ours(args, dist: Dist):
     cfg = M.make_cfg((n, n, n), tau=tau, precision="f64", heat=(1.0, 1.0, 0.0), stream=stream.cuda_stream,
                      tile=tuned["f64"][0])
     e2e_times = []
+    parts = np.zeros(3)  # upload, upload-to-download (steps), download (s)
     with M.Plain(cfg) as p:
         for it in range(1 + args.steps):
             dist.barrier()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             p.upload(M.FIELD_U, u0)
+            ta = time.perf_counter()
             p.step(T)
+            tb = time.perf_counter()
             p.download(M.FIELD_U, out)
             t1 = time.perf_counter()
             if it > 0:
                 e2e_times.append(t1 - t0)
+                parts += (ta - t0, tb - ta, t1 - tb)
     e2e_dt = dist.max(sum(e2e_times))
     e2e = {"value": dist.world * nn * T * len(e2e_times) / e2e_dt / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": nn * 8, "d2h_bytes_per_step": nn * 8,
            "ms_per_step": e2e_dt / len(e2e_times) * 1e3,
+           "ms_upload_enqueue_download": [float(v) for v in parts / len(e2e_times) * 1e3],
            "path": f"scafes_gpu_upload + scafes_gpu_step({T}) + scafes_gpu_download, pinned host buffers"}
 
     variants = {}

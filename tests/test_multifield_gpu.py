@@ -70,6 +70,22 @@ def test_yee_matches_oracle(gpu, prec, tol, n):
     assert cases.rel_err(f, ref) <= tol
 
 
+def test_yee_f32_fused_matches_f64_at_256(gpu):
+    """256^3, 60 steps: the fused FP32 step (8 z-chunks of 32 planes, 64
+    column tiles per plane) against the FP64 two-kernel step, all six fields,
+    1e-4 relative max-norm as for the small FP32 case."""
+    M = gpu
+    n, T = (256, 256, 256), 60
+    tau, src, par = W.yee_setup(n)
+    out = {}
+    for prec in ("f32", "f64"):
+        with M.MultiField(M.MF_YEE, n, tau, par, precision=prec, src=src) as mf:
+            mf.step(T)
+            out[prec] = np.stack([mf.download(i) for i in range(6)])
+    assert np.max(np.abs(out["f64"])) > 0.0
+    assert cases.rel_err(out["f32"], out["f64"]) <= 1e-4
+
+
 def test_yee_energy_bounded_after_source(gpu):
     """After the pulse the PEC cavity holds its energy (leapfrog: conserved
     up to O(tau) oscillation) -- no growth."""
