@@ -230,6 +230,66 @@ def cpu_sample_glups(n: int, target_s: float, max_sweeps: int = 50):
     return n ** 3 * sweeps / dt / 1e9, threads, sweeps, dt
 
 
+def cpu_section_baselines(args) -> dict:
+    """CPU baselines of the other workloads (the oracle's restatements, all
+    host threads), each timed on a bounded sample of its workload:
+    batched -- the first 16 ensemble instances x 50 steps; adjoint -- the
+    forward solve and the adjoint at 64^3 x 200 steps (every state stored);
+    Lame 96^3 x 10 steps; Yee 128^3 x 20 steps."""
+    import oracle as O
+    from masterthesis_gb300 import workloads as W
+    threads = os.cpu_count() or 1
+    out = {}
+    # Batched ensemble: instance by instance, as the reference runs them.
+    specs = W.pennes_ensemble(n_inst=args.batch_instances, seed=8)[:16]
+    T = 50
+    lup, t0 = 0, time.perf_counter()
+    for sp in specs:
+        n = sp["n"]
+        shape = (n[2], n[1], n[0])
+        g = O.make_grid(n, tau=sp["tau"])
+        u0 = np.full(shape, W.T_ARTERIAL)
+        O.pennes_mri(g, u0, T, 1.0, 1.0, sp["k"], 1.0, 1.0, sp["w_b"], W.T_ARTERIAL, sp["q"], u0, nthreads=threads)
+        lup += int(np.prod(n)) * T
+    dt = time.perf_counter() - t0
+    out["batched"] = {"value": lup / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                      "sample": f"first {len(specs)} instances x {T} steps, one after the other ({dt:.1f} s)"}
+    # Adjoint: forward solve and gradient (every state stored) at 64^3.
+    n, T = (64, 64, 64), 200
+    rng = np.random.default_rng(5)
+    shape = (64, 64, 64)
+    k = np.exp(0.3 * rng.standard_normal(shape))
+    tau = 0.9 / (2.0 * k.max() * sum((m - 1) ** 2 for m in n))
+    g = O.make_grid(n, tau=tau)
+    u0 = rng.uniform(-1.0, 1.0, shape)
+    t0 = time.perf_counter()
+    _, traj = O.kheat_forward(g, k, u0, T, keep_traj=True, nthreads=threads)
+    t1 = time.perf_counter()
+    O.kheat_adjoint(g, k, traj, np.zeros(shape), nthreads=threads)
+    t2 = time.perf_counter()
+    out["adjoint"] = {"value": 64 ** 3 * T / (t1 - t0) / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                      "gradient_over_forward": (t2 - t0) / (t1 - t0),
+                      "sample": f"64^3 x {T} steps, forward {1e3 * (t1 - t0):.0f} ms, adjoint {1e3 * (t2 - t1):.0f} ms"}
+    # Lame and Yee.
+    n, T = (96, 96, 96), 10
+    u0 = W.gaussian_bump_displacement(n, seed=3)
+    g = O.make_grid(n, tau=W.lame_tau(n))
+    t0 = time.perf_counter()
+    O.lame(g, u0, u0.copy(), T, 1.0, 0.5, 1.0, nthreads=threads)
+    dt = time.perf_counter() - t0
+    out["lame_f64"] = {"value": 96 ** 3 * T / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                       "sample": f"96^3 x {T} steps ({dt:.1f} s)"}
+    n, T = (128, 128, 128), 20
+    tau, src, par = W.yee_setup(n)
+    g = O.make_grid(n, tau=tau)
+    t0 = time.perf_counter()
+    O.yee(g, np.zeros((6, 128, 128, 128)), T, src, *par, nthreads=threads)
+    dt = time.perf_counter() - t0
+    out["yee_f64"] = {"value": 128 ** 3 * T / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                      "sample": f"128^3 x {T} steps ({dt:.1f} s)"}
+    return out
+
+
 # ---- batched ensemble ---------------------------------------------------------
 
 def run_batched(M, args, dist: Dist, hbm_peak: float):
@@ -579,6 +639,14 @@ def run_ours(args, dist: Dist):
         res["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                "sample": f"{sweeps} sweeps of the {n}^3 workload ({cdt:.1f} s), "
                                          f"C restatement of the reference update (oracle/), OpenMP"}
+        # The other workloads' CPU baselines sit beside their GPU numbers.
+        sec = cpu_section_baselines(args)
+        if batched:
+            batched["cpu_baseline"] = sec["batched"]
+        if adjoint:
+            adjoint["cpu_baseline"] = sec["adjoint"]
+        if multifield:
+            multifield["cpu_baseline"] = {"lame_f64": sec["lame_f64"], "yee_f64": sec["yee_f64"]}
     return res
 
 
