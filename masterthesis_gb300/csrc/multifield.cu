@@ -377,6 +377,7 @@ int yee_zchunk(const Layout& L) {
     const long long tiles = (long long)((L.nx + YX - 1) / YX) * ((L.ny + YY - 1) / YY);
     int zc = 32;
     while (zc > 4 && tiles * ((L.nz + zc - 1) / zc) < (long long)sms * 8) zc >>= 1;
+    while ((L.nz + zc - 1) / zc > 65535) zc <<= 1;  // grid.z limit
     return zc;
 }
 

@@ -54,6 +54,7 @@ static int choose_zchunk(const Layout& L, int by) {
     const long long want = (long long)num_sms() * 16;
     int zc = 16;
     while (zc > 4 && tiles * ((L.nz + zc - 1) / zc) < want) zc >>= 1;
+    while ((L.nz + zc - 1) / zc > 65535) zc <<= 1;  // grid.z limit
     return zc;
 }
 
@@ -129,6 +130,7 @@ static int tb_zchunk(const Layout& L) {
     const long long tiles = (long long)((L.nx + TB_X - 1) / TB_X) * ((L.ny + TB_Y - 1) / TB_Y);
     int zc = 64;
     while (zc > 8 && tiles * ((L.nz + zc - 1) / zc) < (long long)num_sms() * 8) zc >>= 1;
+    while ((L.nz + zc - 1) / zc > 65535) zc <<= 1;  // grid.z limit
     return zc;
 }
 

@@ -33,10 +33,10 @@ namespace {
 constexpr int WX = 32, WY = 8, WZ = 16;
 
 __global__ void __launch_bounds__(WX * WY)
-k_wide(const double* __restrict__ u, double* __restrict__ un, Layout L, int w) {
+k_wide(const double* __restrict__ u, double* __restrict__ un, Layout L, int w, int wz) {
     const int x = blockIdx.x * WX + threadIdx.x, y = blockIdx.y * WY + threadIdx.y;
     if (x >= L.nx || y >= L.ny) return;
-    const int zb = blockIdx.z * WZ, ze = min(zb + WZ, L.nz);
+    const int zb = blockIdx.z * wz, ze = min(zb + wz, L.nz);
     const int ms_x = min(x, w), me_x = min(L.nx - 1 - x, w);
     const int ms_y = min(y, w), me_y = min(L.ny - 1 - y, w);
     for (int z = zb; z < ze; ++z) {
@@ -186,11 +186,14 @@ extern "C" int scafes_wide_step(scafes_wide* h, int n_steps) {
     if (!h) return wfail(nullptr, SCAFES_ERR_ARG, "scafes_wide_step: handle is NULL");
     if (n_steps < 0) return wfail(h, SCAFES_ERR_ARG, "scafes_wide_step: n_steps=%d < 0", n_steps);
     const Layout& L = h->L;
-    const dim3 grid((L.nx + WX - 1) / WX, (L.ny + WY - 1) / WY, (L.nz + WZ - 1) / WZ);
+    int wz = WZ;
+    while ((L.nz + wz - 1) / wz > 65535) wz <<= 1;  // grid.z limit
+    const dim3 grid((L.nx + WX - 1) / WX, (L.ny + WY - 1) / WY, (L.nz + wz - 1) / wz);
     WTRY(h, cudaEventRecord(h->e0, h->stream));
     for (int s = 0; s < n_steps; ++s) {
         for (size_t f = 0; f < h->widths.size(); ++f) {
-            k_wide<<<grid, dim3(WX, WY), 0, h->stream>>>(h->buf[h->cur][f], h->buf[h->cur ^ 1][f], L, h->widths[f]);
+            k_wide<<<grid, dim3(WX, WY), 0, h->stream>>>(h->buf[h->cur][f], h->buf[h->cur ^ 1][f], L, h->widths[f],
+                                                         wz);
             WTRY(h, cudaGetLastError());
         }
         h->cur ^= 1;

@@ -89,6 +89,26 @@ def test_ragged_shapes_vs_oracle(gpu, n):
         assert cases.rel_err(u, ref) <= TOL[prec], prec
 
 
+@pytest.mark.parametrize("n", [(1 << 20, 3, 3), (3, 65536, 3), (5, 3, 1 << 17), (1000, 999, 3)])
+def test_extreme_shapes_vs_oracle(gpu, n):
+    """Axis extents at the large end of what a handle takes (x up to 2^20
+    nodes, long y and z axes, a thin slab): TMA boxes, tile counts and
+    z-chunks at their extremes, against the oracle."""
+    M = gpu
+    rng = np.random.default_rng(7)
+    shape = (n[2], n[1], n[0])
+    tau = 0.9 / (2.0 * sum((m - 1) ** 2 for m in n))
+    g = O.make_grid(n, tau=tau)
+    u0 = rng.uniform(-1.0, 1.0, shape)
+    gA = rng.uniform(-1.0, 1.0, shape)
+    T = 3
+    ref = O.heat_dirichlet(g, u0, T, g_base=gA)
+    for prec in PRECS:
+        cfg = M.make_cfg(n, tau=tau, precision=prec, heat=(1.0, 1.0, 0.0))
+        u = cases.run(cfg, {M.FIELD_G_A: gA, M.FIELD_U: u0}, T)
+        assert cases.rel_err(u, ref) <= TOL[prec], prec
+
+
 @pytest.mark.parametrize("tile", [1, 2, 3, 4])
 @pytest.mark.parametrize("prec", PRECS)
 def test_every_tile_variant(gpu, tile, prec):
