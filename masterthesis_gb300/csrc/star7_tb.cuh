@@ -33,6 +33,8 @@ constexpr int TB_NS = 4;                   // input ring: planes q-1, q in use, 
 constexpr int TB_U1W = TB_X + 2, TB_U1H = TB_Y + 2, TB_U1 = TB_U1W * TB_U1H;  // intermediate region
 constexpr int TB_BH = TB_Y + 4;            // input box rows: y0-2 .. y0+TB_Y+1
 constexpr int TB_HALO = 2 * TB_U1W + 2 * TB_Y;  // intermediate cells around the output tile
+static_assert(TB_Y == TB_TY * TB_R, "each thread row owns TB_R tile rows");
+static_assert(TB_HALO <= TB_X * TB_TY, "one halo cell per thread at most");
 
 // Left pad of the input box in elements (16 bytes of alignment, at least
 // the two halo nodes) and its width.
@@ -143,32 +145,36 @@ star7_tb2(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
     sl[2] = 3;  // plane z0+1
     sl[3] = 0;  // plane z0+2
 
+    // A load never completed: report, drain whatever may still be in flight
+    // (both phases of every slot: a completed phase returns at once; an
+    // error path may spend a second here).
+    auto fail = [&]() {
+        if (tid == 0) {
+            atomicExch(status, SCAFES_ERR_TIMEOUT);
+            for (int b = 0; b < TB_NS; ++b) {
+                bounded_wait(&bar[b], (ph >> b) & 1u, kWaitLimitNs / 16);
+                bounded_wait(&bar[b], ((ph >> b) & 1u) ^ 1u, kWaitLimitNs / 16);
+            }
+        }
+    };
     // (A loop unrolled by three with rotating queue roles instead of the
     // register moves below took more registers and ran slower.)
     for (int q = z0; q <= z1 + 1; ++q) {
         const int i_q = q - z0 + 2;  // index of input plane q
-        if (q > z0) {
-            __syncthreads();  // the previous plane's reads are done: refill its slot
-            if (tid == 0) {
-                fence_proxy_async_smem();
-                if (i_q + 2 < n_in) issue(i_q + 2, sl[3]);
-            }
+        // One barrier per plane: the previous plane's reads are done (its
+        // slot may be refilled) and every wait so far succeeded.  A plane
+        // whose wait failed is computed on whatever arrived; the next
+        // barrier (or the one after the loop) stops the CTA and reports it.
+        if (!__syncthreads_and(ok)) {
+            fail();
+            return;
+        }
+        if (q > z0 && tid == 0) {
+            fence_proxy_async_smem();
+            if (i_q + 2 < n_in) issue(i_q + 2, sl[3]);
         }
         ok = bounded_wait(&bar[sl[1]], (ph >> sl[1]) & 1u) && ok;  // input plane q
         ph ^= 1u << sl[1];
-        if (!__syncthreads_and(ok)) {
-            if (tid == 0) {
-                atomicExch(status, SCAFES_ERR_TIMEOUT);
-                // Drain whatever may still be in flight: both phases of every
-                // slot (a completed phase returns at once; an error path may
-                // spend a second here).
-                for (int b = 0; b < TB_NS; ++b) {
-                    bounded_wait(&bar[b], (ph >> b) & 1u, kWaitLimitNs / 16);
-                    bounded_wait(&bar[b], ((ph >> b) & 1u) ^ 1u, kWaitLimitNs / 16);
-                }
-            }
-            return;
-        }
         const T* pc = sin + sl[0] * SLOT;  // input plane q-1
         const T* pa = sin + sl[1] * SLOT;  // input plane q
         T* w1 = su1 + ((q - 1) & 1) * TB_U1;        // receives the intermediate plane q-1
@@ -264,6 +270,7 @@ star7_tb2(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
         sl[2] = sl[3];
         sl[3] = s0;
     }
+    if (!__syncthreads_and(ok)) fail();  // the last plane's wait
 }
 
 }  // namespace scafes
