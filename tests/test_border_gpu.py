@@ -149,6 +149,47 @@ def run_radiation(M, d, g, S, T, basis, prec, n_layers=1):
         return p.download()
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+def test_radiation_border_noisy(gpu, prec):
+    """Seeded data on a non-cubic grid (37 x 21 x 19): random iterate,
+    source and border field base, lambda, epsilon*sigma != 1, the radiation
+    field (base (1 + t))^4 a + b (1 + t) as G_A .. G_E in the default time
+    basis; against the oracle's restatement of Radiation.hpp (1e-12)."""
+    M = gpu
+    n, T = (37, 21, 19), 80
+    rng = np.random.default_rng(61)
+    shape = (n[2], n[1], n[0])
+    h2 = sum((m - 1) ** 2 for m in n)
+    tau = 0.3 / (2.0 * h2)
+    g = O.make_grid(n, tau=tau)
+    u0 = rng.uniform(0.5, 1.5, shape)
+    fb = rng.uniform(-1.0, 1.0, shape)
+    base = rng.uniform(0.5, 1.5, shape)
+    gdir = rng.uniform(-1.0, 1.0, shape)
+    lam, eps, sig, a, b = 0.8, 0.7, 0.9, 0.6, 1.3
+    ref = O.heat_radiation(g, u0, T, coeff_a=1.1, lam=lam, epsilon=eps, sigma=sig, f=(fb, 0, 1.0, 0.0),
+                           g_dir=(gdir, 0, 1.0, 0.0), g_flux=(base, 3, a, b))
+    cfg = M.make_cfg(n, tau=tau, precision=prec, border=M.BORDER_TABLE, heat=(1.1, 1.0, 0.0))
+    forms = M.border_forms_flux(cfg, M.FLUX_RADIATION, lam, eps * sig)
+    x0 = np.zeros(shape, dtype=bool)
+    x0[:, :, 0] = x0[:, 0, :] = x0[0, :, :] = True
+    binom = (1, 4, 6, 4, 1)
+    co = [a * base ** 4 * binom[k] for k in range(5)]   # (base (1+t))^4 a in powers of t
+    co[0] = co[0] + b
+    co[1] = co[1] + b
+    zero = np.zeros(shape)
+    gco = [np.where(x0, gdir, co[0])] + [np.where(x0, zero, c) for c in co[1:]]
+    with M.Plain(cfg) as p:
+        p.set_border_forms(forms)
+        p.upload(M.FIELD_F_A, fb)
+        for slot, c in zip((M.FIELD_G_A, M.FIELD_G_B, M.FIELD_G_C, M.FIELD_G_D, M.FIELD_G_E), gco):
+            p.upload(slot, c)
+        p.upload(M.FIELD_U, u0)
+        p.step(T)
+        u = p.download()
+    assert cases.rel_err(u, ref) <= 1e-12, prec
+
+
 def test_border_time_basis_rules(gpu):
     """Higher time orders of G and a non-default basis are TABLE-only; a
     zero rate is refused."""
