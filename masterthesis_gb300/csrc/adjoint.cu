@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "scafes_common.cuh"
+#include "tma.cuh"
 #include "../../include/scafes_gb300.h"
 
 using namespace scafes;
@@ -265,45 +266,119 @@ __global__ void k_prep_x2(const double* __restrict__ k, float2* __restrict__ kx,
     }
 }
 
-// One thread marches a 16-plane chunk of one (x, y) column and keeps the
-// z-neighbours (u and the z-face conductivity of the plane below) in
-// registers, so each plane issues its loads for the plane above while the
-// current node is computed.
-__global__ void __launch_bounds__(AX * AY)
-k_forward_x2(const float2* __restrict__ u, float2* __restrict__ un, const float2* __restrict__ kx,
-             const float2* __restrict__ ky, const float2* __restrict__ kz, const float2* __restrict__ dg, Layout L) {
-    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
-    if (x >= L.nx || y >= L.ny) return;
-    const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
-    long long o = L.idx(x, y, zb);
-    if (x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1) {
-        for (int z = zb; z < ze; ++z, o += L.plane) un[o] = u[o];
-        return;
+// One forward step on FP32 pairs, u' = d u + sum_f K_f u_nb over the six
+// faces (border nodes copied), with every operand staged through TMA: a
+// column-per-thread kernel with plain loads stalled on their latency (ncu:
+// long-scoreboard stalls, 0.63 of HBM).  A CTA owns an FTX x FTY column tile
+// and marches FZ_ planes; per plane one mbarrier covers five boxes -- u with
+// a one-node halo (x from x0-2 for 16-byte alignment), the x faces from
+// x0-2, the y faces from row y0-1, the z faces and the diagonal of the tile
+// -- in a ring of four planes (planes z, z+1 in use, z+2, z+3 in flight).
+// u and the z face of the plane below come from register queues.  The
+// products are accumulated in a fixed order (diagonal, +x, -x, +y, -y, +z,
+// -z), which the reverse sweep's recomputation repeats bit for bit.  Every
+// wait is bounded (status word, drain, return).
+constexpr int FTX = 32, FTY = 8, FZ_ = 32, FNS = 4;
+constexpr int FUW = FTX + 4, FUH = FTY + 2;             // u box: x0-2 .. x0+33, y0-1 .. y0+8
+constexpr int FXW = FTX + 4, FXH = FTY;                 // x faces: x0-2 .. x0+33, own rows
+constexpr int FYW = FTX, FYH = FTY + 1;                 // y faces: own columns, y0-1 .. y0+7
+constexpr int FKW = FTX, FKH = FTY;                     // z faces, diagonal: the tile
+constexpr int pad16(int n) { return (n + 15) / 16 * 16; }  // float2 count -> 128-byte multiple
+constexpr int FO_U = 0, FO_X = pad16(FUW * FUH), FO_Y = FO_X + pad16(FXW * FXH);
+constexpr int FO_Z = FO_Y + pad16(FYW * FYH), FO_D = FO_Z + pad16(FKW * FKH);
+constexpr int FSLOT = FO_D + pad16(FKW * FKH);          // float2 per ring slot
+constexpr uint32_t FTX_BYTES = (uint32_t)(FUW * FUH + FXW * FXH + FYW * FYH + 2 * FKW * FKH) * 8u;
+constexpr size_t FSMEM = (size_t)FNS * FSLOT * 8 + FNS * 8;
+
+__global__ void __launch_bounds__(FTX * FTY)
+k_forward_x2_tma(const __grid_constant__ CUtensorMap tu, const __grid_constant__ CUtensorMap tkx,
+                 const __grid_constant__ CUtensorMap tky, const __grid_constant__ CUtensorMap tkz,
+                 const __grid_constant__ CUtensorMap tdg, float2* __restrict__ un, Layout L,
+                 int* __restrict__ status) {
+    extern __shared__ __align__(128) float2 fsm[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(fsm + FNS * FSLOT);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FTX + tx;
+    const int x0 = blockIdx.x * FTX, y0 = blockIdx.y * FTY;
+    const int z0 = blockIdx.z * FZ_, z1 = min(z0 + FZ_, L.nz);
+    if (__syncthreads_or(tid == 0 && *(volatile int*)status != 0)) return;
+    if (tid == 0) {
+        for (int b = 0; b < FNS; ++b) scafes::mbar_init(&bar[b], 1);
+        scafes::fence_barrier_init();
     }
+    __syncthreads();
+    // Input plane j is z0-1+j (j = 0 .. n_in-1), in ring slot j % FNS.
+    const int n_in = z1 - z0 + 2;
+    auto issue = [&](int j) {
+        const int s = j & (FNS - 1), z = z0 - 1 + j;
+        float2* d = fsm + s * FSLOT;
+        scafes::mbar_arrive_expect_tx(&bar[s], FTX_BYTES);
+        scafes::tma_load_3d(d + FO_U, &tu, x0 - 2, y0 - 1, z, &bar[s]);
+        scafes::tma_load_3d(d + FO_X, &tkx, x0 - 2, y0, z, &bar[s]);
+        scafes::tma_load_3d(d + FO_Y, &tky, x0, y0 - 1, z, &bar[s]);
+        scafes::tma_load_3d(d + FO_Z, &tkz, x0, y0, z, &bar[s]);
+        scafes::tma_load_3d(d + FO_D, &tdg, x0, y0, z, &bar[s]);
+    };
+    if (tid == 0)
+        for (int j = 0; j < FNS && j < n_in; ++j) issue(j);
+    auto wait = [&](int j) { return scafes::bounded_wait(&bar[j & (FNS - 1)], (uint32_t)(j >> 2) & 1u); };
+    auto fail = [&](int last_issued) {
+        if (tid == 0) {
+            atomicExch(status, SCAFES_ERR_TIMEOUT);
+            // Only the last FNS planes issued can still be in flight (a slot
+            // is refilled only after its previous plane was waited on).
+            for (int j = last_issued - (FNS - 1); j <= last_issued; ++j)
+                if (j >= 0 && j < n_in)
+                    scafes::bounded_wait(&bar[j & (FNS - 1)], (uint32_t)(j >> 2) & 1u, scafes::kWaitLimitNs / 16);
+        }
+    };
+    const int x = x0 + tx, y = y0 + ty;
+    const bool live = x < L.nx && y < L.ny;
+    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+    const int bu = (ty + 1) * FUW + tx + 2, bx = ty * FXW + tx + 2, by = (ty + 1) * FYW + tx, bk = ty * FKW + tx;
     const float2 zero = make_float2(0.f, 0.f);
-    float2 ub = zb > 0 ? u[o - L.plane] : zero;
-    float2 kzb = zb > 0 ? kz[o - L.plane] : zero;
-    float2 uc = u[o];
-#pragma unroll 2
-    for (int z = zb; z < ze; ++z, o += L.plane) {
-        const float2 ua = z + 1 < L.nz ? u[o + L.plane] : zero;
-        const float2 kzc = kz[o];
-        if (z == 0 || z == L.nz - 1) {
-            un[o] = uc;
-        } else {
-            f2 acc = pmul(dg[o], uc);
-            pacc(acc, pmul(kx[o], u[o + 1]));
-            pacc(acc, pmul(kx[o - 1], u[o - 1]));
-            pacc(acc, pmul(ky[o], u[o + L.pitch]));
-            pacc(acc, pmul(ky[o - L.pitch], u[o - L.pitch]));
-            pacc(acc, pmul(kzc, ua));
-            pacc(acc, pmul(kzb, ub));
-            un[o] = pnorm(acc);
+    bool ok = wait(0);
+    const float2* s0 = fsm;
+    float2 ub = z0 > 0 ? s0[FO_U + bu] : zero;  // plane z0-1
+    float2 kzb = z0 > 0 ? s0[FO_Z + bk] : zero;
+    ok = wait(1) && ok;
+    float2 uc = fsm[FSLOT + FO_U + bu];         // plane z0
+    int issued = FNS - 1;
+    for (int z = z0; z < z1; ++z) {
+        const int jc = z - z0 + 1;  // input plane of z
+        if (!__syncthreads_and(ok)) {  // plane z-1's slot is free; all waits so far succeeded
+            fail(issued);
+            return;
+        }
+        if (tid == 0 && jc + 3 < n_in && jc + 3 > issued) {
+            scafes::fence_proxy_async_smem();
+            issue(jc + 3);
+            issued = jc + 3;
+        }
+        ok = wait(jc + 1) && ok;  // plane z+1 (its u above this node)
+        const float2* sc = fsm + (jc & (FNS - 1)) * FSLOT;
+        const float2* sa = fsm + ((jc + 1) & (FNS - 1)) * FSLOT;
+        const float2 ua = z + 1 < L.nz ? sa[FO_U + bu] : zero;
+        const float2 kzc = sc[FO_Z + bk];
+        if (live) {
+            const long long o = L.idx(x, y, z);
+            if (colb || z == 0 || z == L.nz - 1) {
+                un[o] = uc;
+            } else {
+                f2 acc = pmul(sc[FO_D + bk], uc);
+                pacc(acc, pmul(sc[FO_X + bx], sc[FO_U + bu + 1]));
+                pacc(acc, pmul(sc[FO_X + bx - 1], sc[FO_U + bu - 1]));
+                pacc(acc, pmul(sc[FO_Y + by], sc[FO_U + bu + FUW]));
+                pacc(acc, pmul(sc[FO_Y + by - FYW], sc[FO_U + bu - FUW]));
+                pacc(acc, pmul(kzc, ua));
+                pacc(acc, pmul(kzb, ub));
+                un[o] = pnorm(acc);
+            }
         }
         ub = uc;
         uc = ua;
         kzb = kzc;
     }
+    if (!__syncthreads_and(ok)) fail(issued);
 }
 
 // G += (u_nb - u_c) (l_c - l_nb), renormalised.
@@ -446,6 +521,13 @@ struct scafes_adj {
     int tab_n = 0, tab_s = 0;
     std::vector<long long> cost;
     std::vector<int> split;
+    // The pair forward step's TMA descriptors: one per u-shaped buffer it
+    // reads (u[0], u[1], snapshot slots; encoded on first use) and the four
+    // coefficient fields.
+    std::vector<std::pair<const void*, CUtensorMap>> umaps;
+    CUtensorMap cmaps[4];
+    bool cmaps_ok = false;
+    int* status = nullptr;     // device word: nonzero once a bounded wait ran out
     std::string err;
 };
 
@@ -479,11 +561,55 @@ bool pairs(const scafes_adj* a) { return a->precision == SCAFES_PREC_F32X2; }
 const float2* P2(const double* p) { return reinterpret_cast<const float2*>(p); }
 float2* P2(double* p) { return reinterpret_cast<float2*>(p); }
 
+// Descriptor of an FP32-pair field for a box of bw x bh nodes.
+int pair_map(scafes_adj* a, CUtensorMap* m, const void* base, int bw, int bh) {
+    const CUresult r = scafes::make_tensor_map_3d(m, base, 8, a->L.nx, a->L.ny, a->L.nz, (size_t)a->L.pitch * 8,
+                                                  (size_t)a->L.plane * 8, bw, bh);
+    if (r != CUDA_SUCCESS) return afail(a, SCAFES_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return SCAFES_OK;
+}
+
+const CUtensorMap* u_map(scafes_adj* a, const double* src) {
+    for (const auto& e : a->umaps)
+        if (e.first == src) return &e.second;
+    CUtensorMap m;
+    if (pair_map(a, &m, src, FUW, FUH)) return nullptr;
+    a->umaps.emplace_back(src, m);
+    return &a->umaps.back().second;
+}
+
+int fwd_x2_tma(scafes_adj* a, const double* src, double* dst) {
+    if (!a->cmaps_ok) {
+        int rc = pair_map(a, &a->cmaps[0], a->kx, FXW, FXH);
+        if (!rc) rc = pair_map(a, &a->cmaps[1], a->ky, FYW, FYH);
+        if (!rc) rc = pair_map(a, &a->cmaps[2], a->kz, FKW, FKH);
+        if (!rc) rc = pair_map(a, &a->cmaps[3], a->dg, FKW, FKH);
+        if (rc) return rc;
+        ATRY(a, cudaFuncSetAttribute(k_forward_x2_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FSMEM));
+        a->cmaps_ok = true;
+    }
+    const CUtensorMap* mu = u_map(a, src);
+    if (!mu) return SCAFES_ERR_CUDA;
+    const dim3 grid((a->L.nx + FTX - 1) / FTX, (a->L.ny + FTY - 1) / FTY, (a->L.nz + FZ_ - 1) / FZ_);
+    k_forward_x2_tma<<<grid, dim3(FTX, FTY), FSMEM, a->stream>>>(*mu, a->cmaps[0], a->cmaps[1], a->cmaps[2],
+                                                                  a->cmaps[3], P2(dst), a->L, a->status);
+    return SCAFES_OK;
+}
+
+// Reads and clears the device status word (the stream is synchronised).
+int check_status(scafes_adj* a, const char* who) {
+    int st = 0;
+    ATRY(a, cudaMemcpy(&st, a->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st == 0) return SCAFES_OK;
+    ATRY(a, cudaMemset(a->status, 0, sizeof(int)));
+    return afail(a, st, "%s: a bounded device wait ran out (status %d); the result is invalid", who, st);
+}
+
 int fwd(scafes_adj* a, const double* src, double* dst) {
-    if (pairs(a))
-        k_forward_x2<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(P2(src), P2(dst), P2(a->kx), P2(a->ky), P2(a->kz),
-                                                                  P2(a->dg), a->L);
-    else
+    if (pairs(a)) {
+        const int rc = fwd_x2_tma(a, src, dst);
+        if (rc) return rc;
+    } else
         k_forward<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(src, dst, a->kx, a->ky, a->kz, a->L);
     ATRY(a, cudaGetLastError());
     ++a->fwd_steps;
@@ -662,6 +788,7 @@ extern "C" void scafes_adj_destroy(scafes_adj* a) {
     double* bufs[] = {a->kx, a->ky, a->kz, a->dg, a->u[0], a->u[1], a->lam[0], a->lam[1], a->gx, a->gy, a->gz,
                       a->bnd, a->snaps, a->work, a->part};
     for (double* b : bufs) cudaFree(b);
+    cudaFree(a->status);
     if (a->e0) cudaEventDestroy(a->e0);
     if (a->e1) cudaEventDestroy(a->e1);
     if (a->own_stream && a->stream) cudaStreamDestroy(a->stream);
@@ -698,6 +825,8 @@ extern "C" int scafes_adj_create(const int n_nodes[3], const double coord_first[
     if (e == cudaSuccess) e = cudaMalloc(&a->snaps, fb * (size_t)n_snapshots);
     a->part_n = grid2(a->L).x * grid2(a->L).y;
     if (e == cudaSuccess) e = cudaMalloc(&a->part, sizeof(double) * a->part_n);
+    if (e == cudaSuccess) e = cudaMalloc(&a->status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(a->status, 0, sizeof(int), a->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(a->snaps, 0, fb * (size_t)n_snapshots, a->stream);
     for (double** f : fields)
         if (e == cudaSuccess) e = cudaMemsetAsync(*f, 0, fb, a->stream);
@@ -770,6 +899,7 @@ extern "C" int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps, 
     if ((rc = from_sweep_type(a, a->u[cur]))) return rc;
     if ((rc = download_dense(a, a->u[cur], uT))) return rc;
     ATRY(a, cudaStreamSynchronize(a->stream));
+    if ((rc = check_status(a, "scafes_adj_forward"))) return rc;
     ATRY(a, cudaEventElapsedTime(&a->fwd_ms, a->e0, a->e1));
     return SCAFES_OK;
 }
@@ -812,6 +942,7 @@ static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const
     if ((rc = download_dense(a, a->u[0], grad_k))) return rc;
     if ((rc = download_dense(a, a->u[1], grad_u0))) return rc;
     ATRY(a, cudaStreamSynchronize(a->stream));
+    if ((rc = check_status(a, who))) return rc;
     ATRY(a, cudaEventElapsedTime(&a->grad_ms, a->e0, a->e1));
     if (J) {
         double s = 0.0;
