@@ -394,59 +394,144 @@ __device__ __forceinline__ float2 gacc(float2 G, float2 unb, float2 uc, float2 l
     return pnorm(acc);
 }
 
-__global__ void __launch_bounds__(AX * AY)
-k_adjoint_x2(const float2* __restrict__ lam, float2* __restrict__ lamn, const float2* __restrict__ u,
-             const float2* __restrict__ kx, const float2* __restrict__ ky, const float2* __restrict__ kz,
-             const float2* __restrict__ dg, float2* __restrict__ gx, float2* __restrict__ gy, float2* __restrict__ gz,
-             float2* __restrict__ bnd, Layout L) {
-    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
-    if (x >= L.nx || y >= L.ny) return;
+// One adjoint step on FP32 pairs: lambda' = A^T lambda (the transposed
+// diagonal form; border rows pass what they receive into bnd) and the face
+// gradients G_f += (u_nb - u_c)(lambda_c - lambda_nb) at the state u_t.
+// The read-only operands are staged through TMA on the forward step's tile
+// (RTX x RTY columns, RZ_ planes, a ring of four planes on four
+// mbarriers).  Per plane one mbarrier covers six boxes: lambda with a
+// one-node halo (x from x0-2), u with the +x / +y neighbours (x0 .. x0+33,
+// y0 .. y0+8), the x faces from x0-2, the y faces from row y0-1, the z
+// faces and the diagonal.  lambda and the z face of the plane below come
+// from register queues; the gradient accumulators are read with plain
+// loads one plane ahead and written back in place.  Out-of-range box
+// elements read as zero: a neighbour outside the grid contributes nothing.
+// Every wait is bounded (status word, drain, return).
+constexpr int RTX = FTX, RTY = FTY, RZ_ = FZ_, RNS = FNS;
+constexpr int RLW = FUW, RLH = FUH;                       // lambda box: the forward's u box
+constexpr int RUW = RTX + 2, RUH = RTY + 1;               // u box: x0 .. x0+33, y0 .. y0+8
+constexpr int RO_L = 0, RO_U = pad16(RLW * RLH), RO_X = RO_U + pad16(RUW * RUH);
+constexpr int RO_Y = RO_X + pad16(FXW * FXH), RO_Z = RO_Y + pad16(FYW * FYH), RO_D = RO_Z + pad16(FKW * FKH);
+constexpr int RSLOT = RO_D + pad16(FKW * FKH);
+constexpr uint32_t RTX_BYTES = (uint32_t)(RLW * RLH + RUW * RUH + FXW * FXH + FYW * FYH + 2 * FKW * FKH) * 8u;
+constexpr size_t RSMEM = (size_t)RNS * RSLOT * 8 + RNS * 8;
+static_assert(RSLOT * 8 % 128 == 0 && RO_U * 8 % 128 == 0 && RO_X * 8 % 128 == 0, "TMA destinations 128-byte aligned");
+static_assert(RUW * 8 % 16 == 0, "TMA box rows are multiples of 16 bytes");
+
+__global__ void __launch_bounds__(RTX * RTY)
+k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__ CUtensorMap tu,
+                 const __grid_constant__ CUtensorMap tkx, const __grid_constant__ CUtensorMap tky,
+                 const __grid_constant__ CUtensorMap tkz, const __grid_constant__ CUtensorMap tdg,
+                 float2* __restrict__ lamn, float2* __restrict__ gx, float2* __restrict__ gy, float2* __restrict__ gz,
+                 float2* __restrict__ bnd, Layout L, int* __restrict__ status) {
+    extern __shared__ __align__(128) float2 rsm[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(rsm + RNS * RSLOT);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * RTX + tx;
+    const int x0 = blockIdx.x * RTX, y0 = blockIdx.y * RTY;
+    const int z0 = blockIdx.z * RZ_, z1 = min(z0 + RZ_, L.nz);
+    if (__syncthreads_or(tid == 0 && *(volatile int*)status != 0)) return;
+    if (tid == 0) {
+        for (int b = 0; b < RNS; ++b) scafes::mbar_init(&bar[b], 1);
+        scafes::fence_barrier_init();
+    }
+    __syncthreads();
+    // Input plane j is z0-1+j (j = 0 .. n_in-1), in ring slot j % RNS.
+    const int n_in = z1 - z0 + 2;
+    auto issue = [&](int j) {
+        const int s = j & (RNS - 1), z = z0 - 1 + j;
+        float2* d = rsm + s * RSLOT;
+        scafes::mbar_arrive_expect_tx(&bar[s], RTX_BYTES);
+        scafes::tma_load_3d(d + RO_L, &tl, x0 - 2, y0 - 1, z, &bar[s]);
+        scafes::tma_load_3d(d + RO_U, &tu, x0, y0, z, &bar[s]);
+        scafes::tma_load_3d(d + RO_X, &tkx, x0 - 2, y0, z, &bar[s]);
+        scafes::tma_load_3d(d + RO_Y, &tky, x0, y0 - 1, z, &bar[s]);
+        scafes::tma_load_3d(d + RO_Z, &tkz, x0, y0, z, &bar[s]);
+        scafes::tma_load_3d(d + RO_D, &tdg, x0, y0, z, &bar[s]);
+    };
+    if (tid == 0)
+        for (int j = 0; j < RNS && j < n_in; ++j) issue(j);
+    auto wait = [&](int j) { return scafes::bounded_wait(&bar[j & (RNS - 1)], (uint32_t)(j >> 2) & 1u); };
+    auto fail = [&](int last_issued) {
+        if (tid == 0) {
+            atomicExch(status, SCAFES_ERR_TIMEOUT);
+            for (int j = last_issued - (RNS - 1); j <= last_issued; ++j)
+                if (j >= 0 && j < n_in)
+                    scafes::bounded_wait(&bar[j & (RNS - 1)], (uint32_t)(j >> 2) & 1u, scafes::kWaitLimitNs / 16);
+        }
+    };
+    const int x = x0 + tx, y = y0 + ty;
+    const bool live = x < L.nx && y < L.ny;
     const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
-    const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
+    const int bl = (ty + 1) * RLW + tx + 2, bu = ty * RUW + tx, bx = ty * FXW + tx + 2, by = (ty + 1) * FYW + tx;
+    const int bk = ty * FKW + tx;
     const float2 zero = make_float2(0.f, 0.f);
-    long long o = L.idx(x, y, zb);
-    // z-neighbours in registers: lambda below / here, u here, the z-face
-    // conductivity below.
-    float2 lb = zb > 0 ? lam[o - L.plane] : zero;
-    float2 lc = lam[o];  // zero on border nodes
-    float2 uc = u[o];
-    float2 kzb = zb > 0 ? kz[o - L.plane] : zero;
-#pragma unroll 2
-    for (int z = zb; z < ze; ++z, o += L.plane) {
+    long long o = live ? L.idx(x, y, z0) : 0;
+    float2 gxn = zero, gyn = zero, gzn = zero;
+    if (live) {
+        gxn = gx[o];
+        gyn = gy[o];
+        gzn = gz[o];
+    }
+    bool ok = wait(0);
+    float2 lb = z0 > 0 ? rsm[RO_L + bl] : zero;  // plane z0-1
+    float2 kzb = z0 > 0 ? rsm[RO_Z + bk] : zero;
+    ok = wait(1) && ok;
+    int issued = RNS - 1;
+    for (int z = z0; z < z1; ++z, o += L.plane) {
+        const int jc = z - z0 + 1;  // input plane of z
+        if (!__syncthreads_and(ok)) {  // plane z-1's slot is free; all waits so far succeeded
+            fail(issued);
+            return;
+        }
+        if (tid == 0 && jc + 3 < n_in && jc + 3 > issued) {
+            scafes::fence_proxy_async_smem();
+            issue(jc + 3);
+            issued = jc + 3;
+        }
+        const float2 gxc = gxn, gyc = gyn, gzc = gzn;
+        if (live && z + 1 < z1) {
+            gxn = gx[o + L.plane];
+            gyn = gy[o + L.plane];
+            gzn = gz[o + L.plane];
+        }
+        ok = wait(jc + 1) && ok;  // plane z+1
+        const float2* sc = rsm + (jc & (RNS - 1)) * RSLOT;
+        const float2* sa = rsm + ((jc + 1) & (RNS - 1)) * RSLOT;
         const bool top = z + 1 < L.nz;
-        const float2 la = top ? lam[o + L.plane] : zero;
-        const float2 ua = top ? u[o + L.plane] : zero;
-        const float2 kzc = kz[o];
-        const bool border = colb || z == 0 || z == L.nz - 1;
-        const float2 lxp = x + 1 < L.nx ? lam[o + 1] : zero, lxm = x > 0 ? lam[o - 1] : zero;
-        const float2 lyp = y + 1 < L.ny ? lam[o + L.pitch] : zero, lym = y > 0 ? lam[o - L.pitch] : zero;
-        if (x + 1 < L.nx) gx[o] = gacc(gx[o], u[o + 1], uc, lc, lxp);
-        if (y + 1 < L.ny) gy[o] = gacc(gy[o], u[o + L.pitch], uc, lc, lyp);
-        if (top) gz[o] = gacc(gz[o], ua, uc, lc, la);
-        const float2 kxp = kx[o], kyp = ky[o];
-        const float2 kxm = x > 0 ? kx[o - 1] : zero, kym = y > 0 ? ky[o - L.pitch] : zero;
-        f2 acc = border ? f2{0.f, 0.f} : pmul(dg[o], lc);
-        pacc(acc, pmul(kxp, lxp));
-        pacc(acc, pmul(kxm, lxm));
-        pacc(acc, pmul(kyp, lyp));
-        pacc(acc, pmul(kym, lym));
-        pacc(acc, pmul(kzc, la));
-        pacc(acc, pmul(kzb, lb));
-        if (border) {
-            // Border rows of the update are the identity: lambda on the border
-            // only collects what the inner neighbours pass back.
-            const float2 bo = bnd[o];
-            pacc(acc, {bo.x, bo.y});
-            bnd[o] = pnorm(acc);
-            lamn[o] = zero;
-        } else {
-            lamn[o] = pnorm(acc);
+        const float2 la = top ? sa[RO_L + bl] : zero;
+        const float2 lc = sc[RO_L + bl];
+        const float2 kzc = sc[RO_Z + bk];
+        if (live) {
+            const float2 ua = top ? sa[RO_U + bu] : zero;
+            const float2 uc = sc[RO_U + bu];
+            const bool border = colb || z == 0 || z == L.nz - 1;
+            const float2 lxp = sc[RO_L + bl + 1], lxm = sc[RO_L + bl - 1];
+            const float2 lyp = sc[RO_L + bl + RLW], lym = sc[RO_L + bl - RLW];
+            if (x + 1 < L.nx) gx[o] = gacc(gxc, sc[RO_U + bu + 1], uc, lc, lxp);
+            if (y + 1 < L.ny) gy[o] = gacc(gyc, sc[RO_U + bu + RUW], uc, lc, lyp);
+            if (top) gz[o] = gacc(gzc, ua, uc, lc, la);
+            const float2 kxp = sc[RO_X + bx], kyp = sc[RO_Y + by];
+            const float2 kxm = sc[RO_X + bx - 1], kym = sc[RO_Y + by - FYW];
+            f2 acc = border ? f2{0.f, 0.f} : pmul(sc[RO_D + bk], lc);
+            pacc(acc, pmul(kxp, lxp));
+            pacc(acc, pmul(kxm, lxm));
+            pacc(acc, pmul(kyp, lyp));
+            pacc(acc, pmul(kym, lym));
+            pacc(acc, pmul(kzc, la));
+            pacc(acc, pmul(kzb, lb));
+            if (border) {
+                const float2 bo = bnd[o];
+                pacc(acc, {bo.x, bo.y});
+                bnd[o] = pnorm(acc);
+                lamn[o] = zero;
+            } else {
+                lamn[o] = pnorm(acc);
+            }
         }
         lb = lc;
-        lc = la;
-        uc = ua;
         kzb = kzc;
     }
+    if (!__syncthreads_and(ok)) fail(issued);
 }
 
 // lambda_T = u_T - target or the cotangent (u_T pairs, target FP64): inner
@@ -521,10 +606,11 @@ struct scafes_adj {
     int tab_n = 0, tab_s = 0;
     std::vector<long long> cost;
     std::vector<int> split;
-    // The pair forward step's TMA descriptors: one per u-shaped buffer it
-    // reads (u[0], u[1], snapshot slots; encoded on first use) and the four
-    // coefficient fields.
-    std::vector<std::pair<const void*, CUtensorMap>> umaps;
+    // The pair steps' TMA descriptors: one per state buffer and box shape
+    // (u[0], u[1], snapshot slots, lambda; encoded on first use) and the
+    // four coefficient fields.
+    struct StateMap { const void* base; int box; CUtensorMap map; };
+    std::vector<StateMap> umaps;
     CUtensorMap cmaps[4];
     bool cmaps_ok = false;
     int* status = nullptr;     // device word: nonzero once a bounded wait ran out
@@ -569,29 +655,47 @@ int pair_map(scafes_adj* a, CUtensorMap* m, const void* base, int bw, int bh) {
     return SCAFES_OK;
 }
 
-const CUtensorMap* u_map(scafes_adj* a, const double* src) {
+// State boxes: a one-node halo (the forward step's u, the adjoint step's
+// lambda) or the +x / +y neighbours only (the adjoint step's u).
+enum { BOX_HALO = 0, BOX_UPPER = 1 };
+
+// Copies the descriptor of `src` for `box` into *out (the cache may grow,
+// so no pointer into it is handed out).
+int state_map(scafes_adj* a, const double* src, int box, CUtensorMap* out) {
     for (const auto& e : a->umaps)
-        if (e.first == src) return &e.second;
-    CUtensorMap m;
-    if (pair_map(a, &m, src, FUW, FUH)) return nullptr;
-    a->umaps.emplace_back(src, m);
-    return &a->umaps.back().second;
+        if (e.base == src && e.box == box) {
+            *out = e.map;
+            return SCAFES_OK;
+        }
+    scafes_adj::StateMap m{src, box, {}};
+    if (int rc = box == BOX_HALO ? pair_map(a, &m.map, src, FUW, FUH) : pair_map(a, &m.map, src, RUW, RUH))
+        return rc;
+    a->umaps.push_back(m);
+    *out = m.map;
+    return SCAFES_OK;
+}
+
+int coefficient_maps(scafes_adj* a) {
+    if (a->cmaps_ok) return SCAFES_OK;
+    int rc = pair_map(a, &a->cmaps[0], a->kx, FXW, FXH);
+    if (!rc) rc = pair_map(a, &a->cmaps[1], a->ky, FYW, FYH);
+    if (!rc) rc = pair_map(a, &a->cmaps[2], a->kz, FKW, FKH);
+    if (!rc) rc = pair_map(a, &a->cmaps[3], a->dg, FKW, FKH);
+    if (rc) return rc;
+    ATRY(a, cudaFuncSetAttribute(k_forward_x2_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FSMEM));
+    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RSMEM));
+    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared));
+    a->cmaps_ok = true;
+    return SCAFES_OK;
 }
 
 int fwd_x2_tma(scafes_adj* a, const double* src, double* dst) {
-    if (!a->cmaps_ok) {
-        int rc = pair_map(a, &a->cmaps[0], a->kx, FXW, FXH);
-        if (!rc) rc = pair_map(a, &a->cmaps[1], a->ky, FYW, FYH);
-        if (!rc) rc = pair_map(a, &a->cmaps[2], a->kz, FKW, FKH);
-        if (!rc) rc = pair_map(a, &a->cmaps[3], a->dg, FKW, FKH);
-        if (rc) return rc;
-        ATRY(a, cudaFuncSetAttribute(k_forward_x2_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FSMEM));
-        a->cmaps_ok = true;
-    }
-    const CUtensorMap* mu = u_map(a, src);
-    if (!mu) return SCAFES_ERR_CUDA;
+    if (int rc = coefficient_maps(a)) return rc;
+    CUtensorMap mu;
+    if (int rc = state_map(a, src, BOX_HALO, &mu)) return rc;
     const dim3 grid((a->L.nx + FTX - 1) / FTX, (a->L.ny + FTY - 1) / FTY, (a->L.nz + FZ_ - 1) / FZ_);
-    k_forward_x2_tma<<<grid, dim3(FTX, FTY), FSMEM, a->stream>>>(*mu, a->cmaps[0], a->cmaps[1], a->cmaps[2],
+    k_forward_x2_tma<<<grid, dim3(FTX, FTY), FSMEM, a->stream>>>(mu, a->cmaps[0], a->cmaps[1], a->cmaps[2],
                                                                   a->cmaps[3], P2(dst), a->L, a->status);
     return SCAFES_OK;
 }
@@ -704,11 +808,16 @@ struct Rev {
 
 int adj_step(Rev& R, const double* u_t) {
     scafes_adj* a = R.a;
-    if (pairs(a))
-        k_adjoint_x2<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(
-            P2(a->lam[R.cur]), P2(a->lam[R.cur ^ 1]), P2(u_t), P2(a->kx), P2(a->ky), P2(a->kz), P2(a->dg), P2(a->gx),
-            P2(a->gy), P2(a->gz), P2(a->bnd), a->L);
-    else
+    if (pairs(a)) {
+        if (int rc = coefficient_maps(a)) return rc;
+        CUtensorMap ml, mu;
+        if (int rc = state_map(a, a->lam[R.cur], BOX_HALO, &ml)) return rc;
+        if (int rc = state_map(a, u_t, BOX_UPPER, &mu)) return rc;
+        const dim3 grid((a->L.nx + RTX - 1) / RTX, (a->L.ny + RTY - 1) / RTY, (a->L.nz + RZ_ - 1) / RZ_);
+        k_adjoint_x2_tma<<<grid, dim3(RTX, RTY), RSMEM, a->stream>>>(
+            ml, mu, a->cmaps[0], a->cmaps[1], a->cmaps[2], a->cmaps[3], P2(a->lam[R.cur ^ 1]), P2(a->gx),
+            P2(a->gy), P2(a->gz), P2(a->bnd), a->L, a->status);
+    } else
         k_adjoint<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(a->lam[R.cur], a->lam[R.cur ^ 1], u_t, a->kx, a->ky,
                                                                a->kz, a->gx, a->gy, a->gz, a->bnd, a->L);
     ATRY(a, cudaGetLastError());

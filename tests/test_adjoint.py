@@ -202,6 +202,28 @@ def test_adjoint_f32x2_matches_oracle_and_f64(gpu):
 
 
 @pytest.mark.gpu
+def test_adjoint_f32x2_several_tiles_match_oracle(gpu):
+    """The pair steps march 32 x 8 column tiles over 32-plane chunks: a grid
+    of 3 x 3 tiles and 3 chunks with ragged last tiles in every direction
+    (one-column, three-row and one-plane remainders) against the FP64
+    oracle at the same 1e-10 / 1e-11 bars."""
+    M = gpu
+    n, T = (65, 19, 65), 12
+    k, tau, u0, target = kheat_problem(n, T, 17)
+    g = O.make_grid(n, tau=tau)
+    uT_ref, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
+    J_ref, gk_ref, gu_ref = O.kheat_adjoint(g, k, traj, target)
+    with M.Adjoint(n, tau, 4, precision="f32x2") as a:
+        a.set_conductivity(k)
+        uT = a.forward(u0, T)
+        J, gk, gu = a.gradient(u0, target, T)
+    assert cases.rel_err(uT, uT_ref) <= 1e-11
+    assert abs(J - J_ref) <= 1e-11 * abs(J_ref)
+    assert cases.rel_err(gk, gk_ref) <= 1e-10
+    assert cases.rel_err(gu, gu_ref) <= 1e-10
+
+
+@pytest.mark.gpu
 def test_adjoint_f32x2_gradient_vs_central_differences(gpu):
     M = gpu
     n, T = (20, 18, 16), 40
