@@ -534,6 +534,11 @@ int scafes_probe_pipe_rates(double* fp64_gops, double* fp32_gops);
  * (and clears it). */
 int scafes_probe_wait_timeout(unsigned limit_us, int* status, double* waited_ms);
 int scafes_gpu_inject_status(scafes_handle* h, int code);
+/* The same for an adjoint handle: its FP32-pair forward and adjoint steps
+ * skip their work while the word is set, and the next scafes_adj_forward /
+ * scafes_adj_gradient / scafes_adj_backward returns the status (and clears
+ * it). */
+int scafes_adj_inject_status(scafes_adj* a, int code);
 
 #ifdef __cplusplus
 }

@@ -700,12 +700,14 @@ int fwd_x2_tma(scafes_adj* a, const double* src, double* dst) {
     return SCAFES_OK;
 }
 
-// Reads and clears the device status word (the stream is synchronised).
+// Reads the device status word after the work queued so far and clears it.
 int check_status(scafes_adj* a, const char* who) {
     int st = 0;
-    ATRY(a, cudaMemcpy(&st, a->status, sizeof(int), cudaMemcpyDeviceToHost));
+    ATRY(a, cudaMemcpyAsync(&st, a->status, sizeof(int), cudaMemcpyDeviceToHost, a->stream));
+    ATRY(a, cudaStreamSynchronize(a->stream));
     if (st == 0) return SCAFES_OK;
-    ATRY(a, cudaMemset(a->status, 0, sizeof(int)));
+    ATRY(a, cudaMemsetAsync(a->status, 0, sizeof(int), a->stream));
+    ATRY(a, cudaStreamSynchronize(a->stream));
     return afail(a, st, "%s: a bounded device wait ran out (status %d); the result is invalid", who, st);
 }
 
@@ -1070,6 +1072,14 @@ extern "C" int scafes_adj_gradient(scafes_adj* a, const double* u0, const double
 extern "C" int scafes_adj_backward(scafes_adj* a, const double* u0, const double* dJ_duT, int n_steps,
                                    double* grad_k, double* grad_u0, size_t n) {
     return gradient_impl(a, "scafes_adj_backward", u0, dJ_duT, true, n_steps, nullptr, grad_k, grad_u0, n);
+}
+
+extern "C" int scafes_adj_inject_status(scafes_adj* a, int code) {
+    if (!a) return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_inject_status: NULL handle");
+    if (code > 0) return afail(a, SCAFES_ERR_ARG, "scafes_adj_inject_status: code %d > 0", code);
+    ATRY(a, cudaMemcpyAsync(a->status, &code, sizeof(int), cudaMemcpyHostToDevice, a->stream));
+    ATRY(a, cudaStreamSynchronize(a->stream));
+    return SCAFES_OK;
 }
 
 extern "C" int scafes_adj_stats(const scafes_adj* a, float* forward_ms, float* gradient_ms, long long* forward_steps,

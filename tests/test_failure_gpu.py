@@ -67,3 +67,37 @@ def test_status_skips_sweeps_and_is_reported_once(gpu):
         p.step(T)
         u = p.download()
     assert cases.rel_err(u, O.heat_dirichlet(O.make_grid(n, tau=tau), u0, T)) <= 1e-12
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+def test_adjoint_status_is_reported_and_cleared(gpu, prec):
+    """An adjoint handle's status word: set (as a pair step that gave up
+    sets it), the next forward solve and the next gradient each report it
+    once -- the pair steps skip their work meanwhile -- and the runs after
+    that give the same bits as on a fresh handle."""
+    M = gpu
+    n, T = (40, 18, 36), 8
+    rng = np.random.default_rng(9)
+    shape = (n[2], n[1], n[0])
+    k = np.exp(0.3 * rng.standard_normal(shape))
+    u0, target = rng.uniform(-1.0, 1.0, shape), rng.uniform(-1.0, 1.0, shape)
+    tau = 0.4 / (2.0 * float(k.max()) * sum((m - 1) ** 2 for m in n))
+    inj = M.lib().scafes_adj_inject_status
+    inj.argtypes = [C.c_void_p, C.c_int]
+    with M.Adjoint(n, tau, 4, precision=prec) as a:
+        a.set_conductivity(k)
+        uT_ref = a.forward(u0, T)
+        J_ref, gk_ref, gu_ref = a.gradient(u0, target, T)
+    with M.Adjoint(n, tau, 4, precision=prec) as a:
+        a.set_conductivity(k)
+        assert inj(a.h, TIMEOUT) == 0
+        with pytest.raises(M.ScafesError) as ex:
+            a.forward(u0, T)
+        assert ex.value.code == TIMEOUT
+        assert np.array_equal(a.forward(u0, T), uT_ref)
+        assert inj(a.h, TIMEOUT) == 0
+        with pytest.raises(M.ScafesError) as ex:
+            a.gradient(u0, target, T)
+        assert ex.value.code == TIMEOUT
+        J, gk, gu = a.gradient(u0, target, T)
+    assert J == J_ref and np.array_equal(gk, gk_ref) and np.array_equal(gu, gu_ref)
