@@ -474,6 +474,8 @@ int scafes_adj_create(const int n_nodes[3], const double coord_first[3],
 int scafes_adj_set_precision(scafes_adj* a, int precision);
 /* Conductivity k at the nodes (dense host array, x fastest). */
 int scafes_adj_set_conductivity(scafes_adj* a, const double* k, size_t n);
+/* The same with k at every node (k > 0). */
+int scafes_adj_set_conductivity_uniform(scafes_adj* a, double k);
 /* Plain forward solve u0 -> u_T (n_steps steps); times itself. */
 int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps,
                        double* uT, size_t n);
@@ -496,6 +498,26 @@ int scafes_adj_stats(const scafes_adj* a, float* forward_ms, float* gradient_ms,
 long long scafes_adj_schedule_cost(int n_steps, int n_snapshots);
 const char* scafes_adj_last_error(const scafes_adj* a);
 void scafes_adj_destroy(scafes_adj* a);
+
+/* The backward entry of a plain handle, replacing the ADOL-C tape the
+ * reference records around updateInner (src/ScaFES_Problem.hpp:5843-5967,
+ * :6633-6747).  For a heat problem (the heat form c0 = 1 - 2 sum cp,
+ * cp[p] = tau*a/h_p^2, no source, the Dirichlet border with one layer and a
+ * value constant in time) run over the h->t steps since its last upload of
+ * the unknown field, and a cotangent dJ_du_T = dJ/du_T (n = nx*ny*nz host
+ * values, x fastest), writes dJ_dk -- the gradient with respect to the
+ * conductivity as a field, k(x) = a being the handle's problem, in the
+ * flux form of the adjoint engine above (so sum dJ_dk = dJ/da) -- and
+ * dJ_du0.  Forward states are recomputed from n_checkpoints >= 2 snapshots
+ * on the binomial schedule, in the handle's precision (F64 or F32X2).  The
+ * initial iterate comes from the copy scafes_gpu_keep_initial keeps; its
+ * border nodes must equal the Dirichlet value (SCAFES_ERR_UNSUPPORTED
+ * otherwise).  scafes_gpu_keep_initial(h, 1) makes every later upload of
+ * the unknown field also keep an FP64 copy on the device (one more field of
+ * device memory); 0 frees it. */
+int scafes_gpu_keep_initial(scafes_handle* h, int on);
+int scafes_gpu_adjoint(scafes_handle* h, const double* dJ_du_T, double* dJ_dk,
+                       double* dJ_du0, int n_checkpoints);
 
 /* No counterpart in the reference.  The same max-norm check as
  * scafes_gpu_err_linf, for callers that must not allocate device memory at

@@ -88,6 +88,8 @@ def lib() -> C.CDLL:
         L.scafes_gpu_upload.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_step.argtypes = [vp, C.c_int]
+        L.scafes_gpu_keep_initial.argtypes = [vp, C.c_int]
+        L.scafes_gpu_adjoint.argtypes = [vp, dp, dp, dp, C.c_int]
         L.scafes_gpu_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
         L.scafes_gpu_set_temporal_depth.argtypes = [vp, C.c_int]
         L.scafes_gpu_temporal_depth.argtypes = [vp, C.POINTER(C.c_int)]
@@ -229,6 +231,22 @@ class Plain:
 
     def step(self, n_steps: int):
         _check(lib().scafes_gpu_step(self.h, n_steps), self.h)
+
+    def keep_initial(self, on: bool = True):
+        """Keeps an FP64 device copy of every later upload of the unknown
+        field: the state adjoint() starts from."""
+        _check(lib().scafes_gpu_keep_initial(self.h, int(on)), self.h)
+
+    def adjoint(self, dJ_du_T: np.ndarray, n_checkpoints: int = 45):
+        """The backward entry: (dJ/dk, dJ/du0) of the steps run since the
+        last upload, for the cotangent dJ/du_T (heat problems with a
+        Dirichlet border constant in time; see scafes_gpu_adjoint)."""
+        g = np.ascontiguousarray(dJ_du_T, dtype=np.float64)
+        if g.size != int(np.prod(self.n)):
+            raise ValueError(f"cotangent has {g.size} values, grid has {int(np.prod(self.n))}")
+        gk, gu = np.empty(self.shape), np.empty(self.shape)
+        _check(lib().scafes_gpu_adjoint(self.h, _dp(g), _dp(gk), _dp(gu), n_checkpoints), self.h)
+        return gk, gu
 
     def autotune(self, n_steps: int = 20):
         """Picks the fastest sweep tile variant on this problem; returns
@@ -433,6 +451,7 @@ class Adjoint:
             L.scafes_adj_create.argtypes = [i3, d3, d3, C.c_double, C.c_int, vp, C.POINTER(vp)]
             L.scafes_adj_set_precision.argtypes = [vp, C.c_int]
             L.scafes_adj_set_conductivity.argtypes = [vp, dp, C.c_size_t]
+            L.scafes_adj_set_conductivity_uniform.argtypes = [vp, C.c_double]
             L.scafes_adj_forward.argtypes = [vp, dp, C.c_int, dp, C.c_size_t]
             L.scafes_adj_gradient.argtypes = [vp, dp, dp, C.c_int, dp, dp, dp, C.c_size_t]
             L.scafes_adj_backward.argtypes = [vp, dp, dp, C.c_int, dp, dp, C.c_size_t]
@@ -464,6 +483,9 @@ class Adjoint:
     def set_conductivity(self, k):
         a = np.ascontiguousarray(k, dtype=np.float64)
         self._chk(lib().scafes_adj_set_conductivity(self.h, _dp(a), a.size))
+
+    def set_conductivity_uniform(self, k: float):
+        self._chk(lib().scafes_adj_set_conductivity_uniform(self.h, float(k)))
 
     def forward(self, u0, n_steps):
         a = np.ascontiguousarray(u0, dtype=np.float64)

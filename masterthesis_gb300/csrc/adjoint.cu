@@ -20,12 +20,14 @@
 // in device memory; the split points follow the optimal binomial schedule
 // (Griewank & Walther, "Algorithm 799: revolve", ACM TOMS 26(1), 2000),
 // computed here by dynamic programming over (steps, free snapshots).
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
 
+#include "adjoint.cuh"
 #include "scafes_common.cuh"
 #include "tma.cuh"
 #include "../../include/scafes_gb300.h"
@@ -973,13 +975,15 @@ extern "C" int scafes_adj_set_precision(scafes_adj* a, int precision) {
     return SCAFES_OK;
 }
 
-extern "C" int scafes_adj_set_conductivity(scafes_adj* a, const double* k, size_t n) {
-    if (!a || !k) return afail(a, SCAFES_ERR_ARG, "scafes_adj_set_conductivity: NULL argument");
-    if (n != (size_t)a->L.nx * a->L.ny * a->L.nz)
-        return afail(a, SCAFES_ERR_ARG, "scafes_adj_set_conductivity: expected %zu values",
-                     (size_t)a->L.nx * a->L.ny * a->L.nz);
-    int rc = upload_dense(a, k, a->work);
-    if (rc) return rc;
+namespace {
+
+__global__ void k_fill(double* __restrict__ f, long long n, double v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        f[i] = v;
+}
+
+// Face conductivities (and the pair diagonal) from the node values in `work`.
+int prepare_faces(scafes_adj* a) {
     if (pairs(a))
         k_prep_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->work, P2(a->kx), P2(a->ky), P2(a->kz), P2(a->dg),
                                                                a->L, a->w[0], a->w[1], a->w[2]);
@@ -990,6 +994,27 @@ extern "C" int scafes_adj_set_conductivity(scafes_adj* a, const double* k, size_
     ATRY(a, cudaStreamSynchronize(a->stream));
     a->have_k = true;
     return SCAFES_OK;
+}
+
+}  // namespace
+
+extern "C" int scafes_adj_set_conductivity(scafes_adj* a, const double* k, size_t n) {
+    if (!a || !k) return afail(a, SCAFES_ERR_ARG, "scafes_adj_set_conductivity: NULL argument");
+    if (n != (size_t)a->L.nx * a->L.ny * a->L.nz)
+        return afail(a, SCAFES_ERR_ARG, "scafes_adj_set_conductivity: expected %zu values",
+                     (size_t)a->L.nx * a->L.ny * a->L.nz);
+    int rc = upload_dense(a, k, a->work);
+    if (rc) return rc;
+    return prepare_faces(a);
+}
+
+extern "C" int scafes_adj_set_conductivity_uniform(scafes_adj* a, double k) {
+    if (!a) return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_set_conductivity_uniform: NULL handle");
+    if (!(k > 0.0) || !std::isfinite(k))
+        return afail(a, SCAFES_ERR_ARG, "scafes_adj_set_conductivity_uniform: k = %g must be finite and > 0", k);
+    k_fill<<<1024, 256, 0, a->stream>>>(a->work, a->L.size(), k);
+    ATRY(a, cudaGetLastError());
+    return prepare_faces(a);
 }
 
 extern "C" int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps, double* uT, size_t n) {
@@ -1017,8 +1042,9 @@ extern "C" int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps, 
 
 // The reverse sweep from u0 over n_steps: `target` is J's target
 // (J = 0.5 |u_T - target|^2) or, with `seed`, the cotangent dJ/du_T.
+// With u0_dev, u0 is a device field in the handle's padded FP64 layout.
 static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const double* target, bool seed,
-                         int n_steps, double* J, double* grad_k, double* grad_u0, size_t n) {
+                         int n_steps, double* J, double* grad_k, double* grad_u0, size_t n, bool u0_dev = false) {
     if (!a || !u0 || !target || !grad_k || !grad_u0 || n_steps < 1)
         return afail(a, SCAFES_ERR_ARG, "%s: bad arguments", who);
     if (n != (size_t)a->L.nx * a->L.ny * a->L.nz) return afail(a, SCAFES_ERR_ARG, "%s: wrong size", who);
@@ -1026,8 +1052,11 @@ static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const
     const int free = schedule_slots(a->n_snap, n_steps);
     build_schedule(a, n_steps, free);
     const size_t fb = field_bytes(a);
-    int rc = upload_dense(a, u0, snap(a, 0));
-    if (rc) return rc;
+    int rc = SCAFES_OK;
+    if (u0_dev)
+        ATRY(a, cudaMemcpyAsync(snap(a, 0), u0, fb, cudaMemcpyDeviceToDevice, a->stream));
+    else if ((rc = upload_dense(a, u0, snap(a, 0))))
+        return rc;
     if ((rc = to_sweep_type(a, snap(a, 0)))) return rc;
     // The target goes to u[1]'s slot only transiently: keep it in `work`.
     if ((rc = upload_dense(a, target, a->work))) return rc;
@@ -1073,6 +1102,13 @@ extern "C" int scafes_adj_backward(scafes_adj* a, const double* u0, const double
                                    double* grad_k, double* grad_u0, size_t n) {
     return gradient_impl(a, "scafes_adj_backward", u0, dJ_duT, true, n_steps, nullptr, grad_k, grad_u0, n);
 }
+
+namespace scafes {
+int adj_backward_device_u0(scafes_adj* a, const double* u0_dev, const double* dJ_duT, int n_steps, double* grad_k,
+                           double* grad_u0, size_t n) {
+    return gradient_impl(a, "scafes_gpu_adjoint", u0_dev, dJ_duT, true, n_steps, nullptr, grad_k, grad_u0, n, true);
+}
+}  // namespace scafes
 
 extern "C" int scafes_adj_inject_status(scafes_adj* a, int code) {
     if (!a) return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_inject_status: NULL handle");

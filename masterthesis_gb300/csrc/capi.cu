@@ -12,6 +12,7 @@
 #include <cstring>
 #include <string>
 
+#include "adjoint.cuh"
 #include "star7.cuh"
 #include "tma.cuh"
 #include "../../include/scafes_gb300.h"
@@ -78,6 +79,15 @@ struct scafes_handle {
     double* snap_host[2] = {nullptr, nullptr};
     cudaStream_t snap_stream = nullptr;
     cudaEvent_t snap_conv = nullptr, snap_copied[2] = {nullptr, nullptr};
+    // Backward entry: with keep_initial, every upload of the unknown field
+    // also lands as FP64 in u0keep, the state scafes_gpu_adjoint starts
+    // from; the adjoint engine is created on first use.
+    bool keep_initial = false;
+    bool u0keep_valid = false;
+    double* u0keep = nullptr;
+    int* mismatch = nullptr;               // border check of scafes_gpu_adjoint
+    scafes_adj* adj = nullptr;
+    int adj_snaps = 0, adj_prec = -1;
     std::string err;
 };
 
@@ -150,6 +160,9 @@ static int validate(const scafes_cfg* c) {
 extern "C" void scafes_gpu_destroy(scafes_handle* h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    scafes_adj_destroy(h->adj);
+    cudaFree(h->u0keep);
+    cudaFree(h->mismatch);
     for (int i = 0; i < 2; ++i) cudaFree(h->u[i]);
     cudaFree(h->status);
     for (int i = 0; i < SCAFES_FIELD_COUNT; ++i) cudaFree(h->fld[i]);
@@ -337,6 +350,12 @@ extern "C" int scafes_gpu_upload(scafes_handle* h, int field, const double* host
     if (field == SCAFES_FIELD_U) {
         rc = h2d(h, h->u[0], h->cfg.precision, host);
         if (rc) return rc;
+        h->u0keep_valid = false;
+        if (h->keep_initial) {
+            if (!h->u0keep) CUDA_TRY(h, cudaMalloc(&h->u0keep, (size_t)h->L.size() * sizeof(double)));
+            if ((rc = h2d(h, h->u0keep, SCAFES_PREC_F64, host))) return rc;
+            h->u0keep_valid = true;
+        }
         h->cur = 0;
         h->t = 0;
         h->uploaded = true;
@@ -961,4 +980,114 @@ extern "C" int scafes_gpu_err_linf(scafes_handle* h, double* err, double* max_re
     *err = h->red_host[0];
     *max_ref = h->red_host[1];
     return check_status(h);
+}
+
+// ---- backward entry -------------------------------------------------------
+
+// Counts the global-border nodes where the initial iterate differs from the
+// Dirichlet value G_A (0 where G_A was not uploaded).  With pairs, G_A holds
+// FP32 pairs and the iterate is compared as the pair it becomes.
+__global__ void k_border_mismatch(const double* __restrict__ u0, const void* __restrict__ ga, int pairs, Layout L,
+                                  int* __restrict__ count) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+    int bad = 0;
+    for (int z = 0; z < L.nz; ++z) {
+        if (!colb && z != 0 && z != L.nz - 1) continue;
+        const long long o = L.idx(x, y, z);
+        double u = u0[o], g = 0.0;
+        if (pairs) {
+            const f2 p = split_double(u);
+            u = (double)p.hi + (double)p.lo;
+            if (ga) g = (double)((const float2*)ga)[o].x + (double)((const float2*)ga)[o].y;
+        } else if (ga) {
+            g = ((const double*)ga)[o];
+        }
+        bad += u != g;
+    }
+    if (bad) atomicAdd(count, bad);
+}
+
+extern "C" int scafes_gpu_keep_initial(scafes_handle* h, int on) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_keep_initial: handle is NULL");
+    h->keep_initial = on != 0;
+    if (!h->keep_initial) {
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        cudaFree(h->u0keep);
+        h->u0keep = nullptr;
+        h->u0keep_valid = false;
+    }
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_adjoint(scafes_handle* h, const double* dJ_du_T, double* dJ_dk, double* dJ_du0,
+                                  int n_checkpoints) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_adjoint: handle is NULL");
+    if (!dJ_du_T || !dJ_dk || !dJ_du0) return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_adjoint: NULL array");
+    if (n_checkpoints < 2)
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_adjoint: n_checkpoints = %d (at least 2)", n_checkpoints);
+    const scafes_cfg& c = h->cfg;
+    if (c.precision != SCAFES_PREC_F64 && c.precision != SCAFES_PREC_F32X2)
+        return fail(&h->err, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_adjoint: precision %d (F64 or F32X2 only)",
+                    c.precision);
+    if (c.border != SCAFES_BORDER_DIRICHLET || c.n_layers_at_border != 1)
+        return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                    "scafes_gpu_adjoint: the Dirichlet border with one border layer only");
+    if (h->has[SCAFES_FIELD_G_B])
+        return fail(&h->err, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_adjoint: the border value must not depend on time");
+    if (c.cf != 0.0 && (h->has[SCAFES_FIELD_F_A] || h->has[SCAFES_FIELD_F_B]))
+        return fail(&h->err, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_adjoint: problems with a source are not covered");
+    // The inner update must be the heat form c0 = 1 - 2 sum cp, cp[p] = tau a / h_p^2: then it is the flux form
+    // with the uniform conductivity a.
+    double a = 0.0, sum_cp = 0.0;
+    for (int p = 0; p < 3; ++p) {
+        const double hp = (c.coord_last[p] - c.coord_first[p]) / (c.n_nodes[p] - 1);
+        const double ap = c.cp[p] * hp * hp / c.tau;
+        if (p == 0) a = ap;
+        else if (std::fabs(ap - a) > 1e-12 * std::fabs(a))
+            return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                        "scafes_gpu_adjoint: cp[%d] is not tau*a/h^2 for the a of cp[0] (anisotropic heat)", p);
+        sum_cp += c.cp[p];
+    }
+    if (!(a > 0.0) || std::fabs(c.c0 - (1.0 - 2.0 * sum_cp)) > 1e-12)
+        return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                    "scafes_gpu_adjoint: the inner update is not the heat form (c0 = 1 - 2 sum cp, a > 0)");
+    if (!h->u0keep_valid)
+        return fail(&h->err, SCAFES_ERR_STATE,
+                    "scafes_gpu_adjoint: call scafes_gpu_keep_initial(h, 1) before uploading the initial iterate");
+    if (h->t < 1) return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_adjoint: no step since the upload");
+    // The border is held at the initial iterate's values: they must be the Dirichlet value.
+    if (!h->mismatch) CUDA_TRY(h, cudaMalloc(&h->mismatch, sizeof(int)));
+    CUDA_TRY(h, cudaMemsetAsync(h->mismatch, 0, sizeof(int), h->stream));
+    const void* ga = h->has[SCAFES_FIELD_G_A] ? h->fld[SCAFES_FIELD_G_A] : nullptr;
+    const dim3 blk(32, 8), grd((h->L.nx + 31) / 32, (h->L.ny + 7) / 8);
+    k_border_mismatch<<<grd, blk, 0, h->stream>>>(h->u0keep, ga, c.precision == SCAFES_PREC_F32X2, h->L,
+                                                  h->mismatch);
+    CUDA_TRY(h, cudaGetLastError());
+    int bad = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&bad, h->mismatch, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (bad)
+        return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                    "scafes_gpu_adjoint: %d border nodes of the initial iterate differ from the Dirichlet value", bad);
+    if (!h->adj || h->adj_snaps != n_checkpoints || h->adj_prec != c.precision) {
+        scafes_adj_destroy(h->adj);
+        h->adj = nullptr;
+        int rc = scafes_adj_create(c.n_nodes, c.coord_first, c.coord_last, c.tau, n_checkpoints, h->stream, &h->adj);
+        if (!rc) rc = scafes_adj_set_precision(h->adj, c.precision);
+        if (!rc) rc = scafes_adj_set_conductivity_uniform(h->adj, a);
+        if (rc) {
+            fail(&h->err, rc, "scafes_gpu_adjoint: %s",
+                 h->adj ? scafes_adj_last_error(h->adj) : scafes_last_error());
+            scafes_adj_destroy(h->adj);
+            h->adj = nullptr;
+            return rc;
+        }
+        h->adj_snaps = n_checkpoints;
+        h->adj_prec = c.precision;
+    }
+    const int rc = scafes::adj_backward_device_u0(h->adj, h->u0keep, dJ_du_T, h->t, dJ_dk, dJ_du0, n_nodes(h));
+    if (rc) return fail(&h->err, rc, "%s", scafes_adj_last_error(h->adj));
+    return SCAFES_OK;
 }

@@ -256,3 +256,85 @@ def test_adjoint_rejects_unsupported_precision(gpu):
     M = gpu
     with pytest.raises(M.ScafesError):
         M.Adjoint((8, 8, 8), 1e-3, 2, precision="f32")
+
+
+def plain_heat_case(n, T, a, seed):
+    rng = np.random.default_rng(seed)
+    shape = (n[2], n[1], n[0])
+    tau = 0.9 / (2.0 * a * sum((m - 1) ** 2 for m in n))
+    g = O.make_grid(n, tau=tau)
+    u0 = rng.uniform(-1.0, 1.0, shape)
+    u0[O.border_mask(g)] = 0.0
+    return g, tau, u0, rng.uniform(-1.0, 1.0, shape)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-11), ("f32x2", 1e-10)])
+def test_plain_handle_backward_entry_matches_oracle(gpu, prec, tol):
+    """scafes_gpu_adjoint on a plain heat handle (coefficient a, Dirichlet
+    0): the forward iterate equals the flux-form solve with k = a, and the
+    gradients for the cotangent u_T - target are the oracle's dJ/dk, dJ/du0
+    of J = 0.5 |u_T - target|^2 at k = a, with 6 checkpoints over 25 steps
+    (recomputation), then again with enough for every state."""
+    M = gpu
+    n, T, a = (20, 17, 15), 25, 0.7
+    g, tau, u0, target = plain_heat_case(n, T, a, 31)
+    k = np.full(u0.shape, a)
+    uT_ref, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
+    _, gk_ref, gu_ref = O.kheat_adjoint(g, k, traj, target)
+    with M.Plain(M.make_cfg(n, tau=tau, precision=prec, heat=(a, 1.0, 0.0))) as p:
+        p.keep_initial()
+        p.upload(M.FIELD_U, u0)
+        p.step(T)
+        uT = p.download()
+        for ckpt in (6, 32):
+            gk, gu = p.adjoint(uT - target, ckpt)
+            assert cases.rel_err(gk, gk_ref) <= tol, ckpt
+            assert cases.rel_err(gu, gu_ref) <= tol, ckpt
+    assert cases.rel_err(uT, uT_ref) <= (1e-12 if prec == "f64" else 1e-11)
+
+
+@pytest.mark.gpu
+def test_plain_handle_backward_entry_refuses_what_it_does_not_cover(gpu):
+    """Status codes, no fault: no kept initial iterate or no step (STATE),
+    a border that differs from the Dirichlet value, a source, the Pennes
+    perfusion term or the mirror border (UNSUPPORTED); the handle still
+    steps correctly afterwards."""
+    M = gpu
+    STATE, UNSUPPORTED = -3, -4
+    n, T, a = (12, 10, 9), 6, 1.0
+    g, tau, u0, target = plain_heat_case(n, T, a, 5)
+    cot = np.ones(u0.shape)
+
+    def code(p):
+        with pytest.raises(M.ScafesError) as ex:
+            p.adjoint(cot, 4)
+        return ex.value.code
+
+    with M.Plain(M.make_cfg(n, tau=tau, heat=(a, 1.0, 0.0))) as p:
+        p.upload(M.FIELD_U, u0)
+        p.step(T)
+        assert code(p) == STATE                        # no kept initial iterate
+        p.keep_initial()
+        p.upload(M.FIELD_U, u0)
+        assert code(p) == STATE                        # no step since the upload
+        bad = u0.copy()
+        bad[0, 0, 0] = 0.5
+        p.upload(M.FIELD_U, bad)
+        p.step(T)
+        assert code(p) == UNSUPPORTED                  # border differs from G = 0
+        p.upload(M.FIELD_U, u0)
+        p.step(T)
+        u = p.download()
+    assert cases.rel_err(u, O.heat_dirichlet(g, u0, T)) <= 1e-12
+    with M.Plain(M.make_cfg(n, tau=tau, heat=(a, 1.0, 0.0))) as p:
+        p.keep_initial()
+        p.upload(M.FIELD_F_A, np.ones(u0.shape))
+        p.upload(M.FIELD_U, u0)
+        p.step(T)
+        assert code(p) == UNSUPPORTED                  # a source
+    with M.Plain(M.make_cfg(n, tau=tau, heat=(a, 1.0, 0.3))) as p:
+        p.keep_initial()
+        p.upload(M.FIELD_U, u0)
+        p.step(T)
+        assert code(p) == UNSUPPORTED                  # perfusion: not the heat form
