@@ -564,6 +564,7 @@ def run_ours(args, dist: Dist):
     e2e_times = []
     parts = np.zeros(3)  # upload, upload-to-download (steps), download (s)
     with M.Plain(cfg) as p:
+        p.set_temporal_depth(tuned["f64"][2])
         for it in range(1 + args.steps):
             dist.barrier()
             torch.cuda.synchronize()
