@@ -75,6 +75,19 @@ def test_null_arguments(native):
     L.scafes_gpu_destroy(None)  # no-op
 
 
+def test_backward_entries_check_arguments_first(native):
+    """The backward entry, its kept initial iterate and the adjoint handle's
+    hooks refuse a NULL handle with SCAFES_ERR_ARG before any CUDA call."""
+    L = native.lib()  # the binding declares the plain handle's entries
+    L.scafes_adj_set_conductivity_uniform.argtypes = [C.c_void_p, C.c_double]
+    L.scafes_adj_inject_status.argtypes = [C.c_void_p, C.c_int]
+    assert L.scafes_gpu_adjoint(None, None, None, None, 8) == -1
+    assert L.scafes_gpu_keep_initial(None, 1) == -1
+    assert L.scafes_adj_set_conductivity_uniform(None, 1.0) == -1
+    assert L.scafes_adj_inject_status(None, -6) == -1
+    assert L.scafes_last_error()
+
+
 def test_heat_coeffs_helper(native):
     M = native
     n, tau = (11, 21, 31), 1e-5
