@@ -533,8 +533,9 @@ int scafes_gpu_adjoint(scafes_handle* h, const double* dJ_du_T, double* dJ_dk,
  * rejected with SCAFES_ERR_ARG and a message in scafes_last_error().  The
  * call is asynchronous on `stream` (NULL = legacy default stream).  The
  * first call on a device looks up the array's device address
- * (cudaGetSymbolAddress, which may load the module), so make that first
- * call before any stream capture.  All calls share the array: calls that
+ * (cudaGetSymbolAddress, which may load the module), and so does the first
+ * call after that device's context was replaced (cudaDeviceReset): make
+ * those calls before any stream capture.  All calls share the array: calls that
  * overlap on the GPU (e.g. on two streams without ordering) race on it and
  * give wrong results. */
 #define SCAFES_ERR_LINF_NOALLOC_MAX_N (16384LL * 32768LL)

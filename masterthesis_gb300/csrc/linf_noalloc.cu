@@ -46,7 +46,16 @@ int reject(int code, const char* what) {
 // has to start at zero; the previous call's values are simply overwritten.
 static __device__ __align__(256) double g_linf_scratch[2 * kMaxBlocks];
 
-double* g_scratch_addr[kMaxDevices] = {};
+// Per device: the scratch address and the ID of the CUDA context it belongs
+// to.  A module's device addresses are only valid in the context that loaded
+// it; after cudaDeviceReset (or any teardown of the primary context) the next
+// context loads the module again, possibly elsewhere, so an address is reused
+// only while the current context is the one it was looked up in.
+struct ScratchSlot {
+    unsigned long long ctx_id;
+    double* ptr;
+};
+ScratchSlot g_scratch[kMaxDevices] = {};
 std::mutex g_setup_mutex;
 
 __device__ __forceinline__ double to_inf_if_nan(double d) {
@@ -101,9 +110,38 @@ k_linf_final(const double* __restrict__ part, int nb, double* __restrict__ out) 
     }
 }
 
-// Device address of the scratch array on the current device.  The first
-// call on a device looks it up (cudaGetSymbolAddress, which may load the
-// module); later calls reuse the cached address.
+// ID of the current CUDA context (cuCtxGetCurrent + cuCtxGetId, reached
+// through the runtime's driver entry points, so the library needs no link
+// against libcuda).  Returns false when the driver does not provide them.
+using PfnCtxGetCurrent = int (*)(void**);
+using PfnCtxGetId = int (*)(void*, unsigned long long*);
+
+bool current_context_id(unsigned long long* id) {
+    static PfnCtxGetCurrent get_current = nullptr;
+    static PfnCtxGetId get_id = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<PfnCtxGetCurrent>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<PfnCtxGetId>(p);
+    }
+    if (!get_current || !get_id) return false;
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, id) == 0;
+}
+
+// Device address of the scratch array in the current context.  The first
+// call on a device, and the first call after that device's context was
+// replaced, looks it up (cudaGetSymbolAddress, which may load the module);
+// later calls in the same context reuse it.
 int scratch_on_current_device(double** ptr) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess)
@@ -111,13 +149,27 @@ int scratch_on_current_device(double** ptr) {
     if (dev < 0 || dev >= kMaxDevices)
         return reject(SCAFES_ERR_UNSUPPORTED, "scafes_err_linf_noalloc: device ordinal above 63");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_linf_scratch) != cudaSuccess || !p)
-            return reject(SCAFES_ERR_CUDA, "scafes_err_linf_noalloc: cudaGetSymbolAddress of the scratch failed");
-        g_scratch_addr[dev] = static_cast<double*>(p);
+    ScratchSlot& slot = g_scratch[dev];
+    unsigned long long id = 0;
+    if (slot.ptr && current_context_id(&id) && slot.ctx_id == id) {
+        *ptr = slot.ptr;
+        return SCAFES_OK;
     }
-    *ptr = g_scratch_addr[dev];
+    // First call on this device, or its context changed since the lookup:
+    // look the address up in the current context (this makes the device's
+    // primary context current if none is) and remember which context it was.
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_linf_scratch) != cudaSuccess || !p)
+        return reject(SCAFES_ERR_CUDA, "scafes_err_linf_noalloc: cudaGetSymbolAddress of the scratch failed");
+    slot.ptr = static_cast<double*>(p);
+    // Without the driver's context IDs, every call looks the address up again.
+    slot.ctx_id = current_context_id(&id) ? id : 0;
+    if (slot.ctx_id == 0) {
+        *ptr = slot.ptr;
+        slot.ptr = nullptr;
+        return SCAFES_OK;
+    }
+    *ptr = slot.ptr;
     return SCAFES_OK;
 }
 

@@ -32,10 +32,19 @@ def build(force: bool = False) -> Path:
     return LIB_PATH
 
 
-def build_ref(reference: str = "/root/reference") -> bool:
+def reference_dir() -> str | None:
+    """The reference checkout, from the SCAFES_REFERENCE_DIR environment
+    variable (default: a ``reference`` directory beside this repository's
+    parent); None where it is absent."""
+    cand = os.environ.get("SCAFES_REFERENCE_DIR") or str(HERE.parents[1] / "reference")
+    return cand if Path(cand, "src", "ScaFES_Problem.hpp").exists() else None
+
+
+def build_ref(reference: str | None = None) -> bool:
     """Compile the reference-driver programs into oracle/_ref (only where the
     reference checkout exists)."""
-    if not Path(reference, "src", "ScaFES_Problem.hpp").exists():
+    reference = reference or reference_dir()
+    if reference is None or not Path(reference, "src", "ScaFES_Problem.hpp").exists():
         return False
     subprocess.run(["make", "-C", str(HERE), "-j8", "ref", f"REF={reference}"], check=True,
                    capture_output=True)
@@ -66,6 +75,10 @@ def lib():
                                     C.c_double, C.c_double, C.c_int]
         L.orc_heat_dirichlet.argtypes = [C.POINTER(Grid), C.c_double, C.c_double, C.c_double,
                                          C.c_double, C.c_int, dp, Known, Known, C.c_int]
+        L.orc_heat_dirichlet_ws.argtypes = [C.POINTER(Grid), C.c_double, C.c_double, C.c_double,
+                                            C.c_double, C.c_int, dp, dp, Known, Known, C.c_int]
+        L.orc_first_touch.argtypes = [dp, C.c_size_t, C.c_int]
+        L.orc_first_touch.restype = None
         L.orc_pennes_mri.argtypes = [C.POINTER(Grid)] + [C.c_double] * 7 + [dp, dp, C.c_int, dp, C.c_int]
         L.orc_heat_flux.argtypes = [C.POINTER(Grid)] + [C.c_double] * 6 + [C.c_int, C.c_int, dp, Known, Known,
                                                                          Known, C.c_int]
@@ -79,7 +92,7 @@ def lib():
         L.orc_lame.argtypes = [C.POINTER(Grid), C.c_double, C.c_double, C.c_double, C.c_int, dp, dp, C.c_int]
         L.orc_yee.argtypes = [C.POINTER(Grid), C.c_int, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                               C.c_double, C.c_double, C.c_int]
-        for f in ("orc_heat_dirichlet", "orc_pennes_mri", "orc_stencil_width_one",
+        for f in ("orc_heat_dirichlet", "orc_heat_dirichlet_ws", "orc_pennes_mri", "orc_stencil_width_one",
                   "orc_stencil_width_var", "orc_kheat_forward", "orc_kheat_adjoint", "orc_lame", "orc_yee"):
             getattr(L, f).restype = C.c_int
         L.orc_time.restype = C.c_double
@@ -137,6 +150,27 @@ def heat_dirichlet(g: Grid, u0, nsteps, coeff_a=1.0, rho_c=1.0, perf_q1=0.0, per
     _check(lib().orc_heat_dirichlet(C.byref(g), coeff_a, rho_c, perf_q1, perf_w, nsteps,
                                     _p(u), fk, gk, nthreads), "heat_dirichlet")
     return u
+
+
+def first_touched(shape, nthreads=0) -> np.ndarray:
+    """An uninitialised float64 array whose pages the OpenMP threads of the
+    sweeps have already mapped (zeros)."""
+    a = np.empty(shape, dtype=np.float64)
+    lib().orc_first_touch(_p(a), a.size, nthreads)
+    return a
+
+
+def heat_dirichlet_ws(g: Grid, u, w, nsteps, coeff_a=1.0, rho_c=1.0, nthreads=0):
+    """heat_dirichlet on caller-owned C-contiguous float64 fields u, w (no
+    copy, no allocation): returns the array holding iterate nsteps (u for
+    even nsteps, w for odd)."""
+    for a in (u, w):
+        if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != g.n[0] * g.n[1] * g.n[2]:
+            raise ValueError("heat_dirichlet_ws needs C-contiguous float64 fields of the grid's size")
+    none = Known(None, 0, 1.0, 0.0)
+    _check(lib().orc_heat_dirichlet_ws(C.byref(g), coeff_a, rho_c, 0.0, 0.0, nsteps, _p(u), _p(w), none, none,
+                                       nthreads), "heat_dirichlet_ws")
+    return u if nsteps % 2 == 0 else w
 
 
 def heat_flux(g: Grid, u0, nsteps, kind, coeff_a=1.0, rho_c=1.0, perf_q1=0.0, perf_w=0.0, lam=1.0,

@@ -121,14 +121,13 @@ static size_t n_total(const orc_grid* g)
     return (size_t)g->n[0] * g->n[1] * g->n[2];
 }
 
-int orc_heat_dirichlet(const orc_grid* g, double coeff_a, double rho_c,
-                       double perf_q1, double perf_w, int nsteps, double* u,
-                       orc_known f_src, orc_known g_bdry, int nthreads)
+/* The sweeps of orc_heat_dirichlet on the caller's two fields: iterate t
+ * is in u for even t and in w for odd t. */
+static void heat_dirichlet_pp(const orc_grid* g, double coeff_a, double rho_c,
+                              double perf_q1, double perf_w, int nsteps, double* u,
+                              double* w, orc_known f_src, orc_known g_bdry, int nthreads)
 {
     const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
-    const size_t nn = n_total(g);
-    double* w = (double*)malloc(nn * sizeof(double));
-    if (!w) return -1;
     const int use_perf = (perf_q1 != 0.0 || perf_w != 0.0);
     const long sx = 1, sy = nx, sz = (long)nx * ny;
     const long stride[3] = {sx, sy, sz};
@@ -162,9 +161,38 @@ int orc_heat_dirichlet(const orc_grid* g, double coeff_a, double rho_c,
         }
         double* tmp = uo; uo = un; un = tmp;
     }
-    if (uo != u) memcpy(u, uo, nn * sizeof(double));
+}
+
+int orc_heat_dirichlet(const orc_grid* g, double coeff_a, double rho_c,
+                       double perf_q1, double perf_w, int nsteps, double* u,
+                       orc_known f_src, orc_known g_bdry, int nthreads)
+{
+    const size_t nn = n_total(g);
+    double* w = (double*)malloc(nn * sizeof(double));
+    if (!w) return -1;
+    heat_dirichlet_pp(g, coeff_a, rho_c, perf_q1, perf_w, nsteps, u, w, f_src, g_bdry, nthreads);
+    if (nsteps % 2 == 1) memcpy(u, w, nn * sizeof(double));
     free(w);
     return 0;
+}
+
+int orc_heat_dirichlet_ws(const orc_grid* g, double coeff_a, double rho_c,
+                          double perf_q1, double perf_w, int nsteps, double* u,
+                          double* w, orc_known f_src, orc_known g_bdry, int nthreads)
+{
+    if (!u || !w || nsteps < 0) return -2;
+    heat_dirichlet_pp(g, coeff_a, rho_c, perf_q1, perf_w, nsteps, u, w, f_src, g_bdry, nthreads);
+    return 0;
+}
+
+void orc_first_touch(double* a, size_t n, int nthreads)
+{
+    set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < (long)((n + 4095) / 4096); ++k) {
+        const size_t lo = (size_t)k * 4096, hi = lo + 4096 < n ? lo + 4096 : n;
+        for (size_t m = lo; m < hi; ++m) a[m] = 0.0;
+    }
 }
 
 /* kind 0 Neumann, 1 Cauchy (alpha), 2 Radiation (epsilon, sigma). */

@@ -67,6 +67,18 @@ int orc_heat_dirichlet(const orc_grid* g, double coeff_a, double rho_c,
                        double perf_q1, double perf_w, int nsteps, double* u,
                        orc_known f_src, orc_known g_bdry, int nthreads);
 
+/* The same sweeps on caller-owned fields, allocating nothing: u holds the
+ * t = 0 iterate on entry, w is a second field of the same size; on exit the
+ * t = nsteps iterate is in u when nsteps is even and in w when it is odd
+ * (the other field holds iterate nsteps - 1).  For timing the sweeps alone. */
+int orc_heat_dirichlet_ws(const orc_grid* g, double coeff_a, double rho_c,
+                          double perf_q1, double perf_w, int nsteps, double* u,
+                          double* w, orc_known f_src, orc_known g_bdry, int nthreads);
+
+/* Writes zeros into a[0..n) from the threads of a static OpenMP schedule,
+ * so that the pages are mapped before a timed region. */
+void orc_first_touch(double* a, size_t n, int nthreads);
+
 /* Heat / Pennes with the flux-condition border of the reference's system
  * tests (kind 0: tests/system/HeatEqnFDM/Neumann/Neumann.hpp and
  * tests/system/PennesBioheatEqnFDM/Neumann/Neumann.hpp; kind 1: the

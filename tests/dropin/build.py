@@ -1,13 +1,17 @@
 """Compiles the drop-in test programs (test infrastructure)."""
 from __future__ import annotations
 
+import os
 import shutil
 import subprocess
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parents[2]
 HERE = Path(__file__).resolve().parent
-REFERENCE = Path("/root/reference")
+# The reference checkout (only present where the reference is mounted; the
+# tests that read it skip elsewhere): SCAFES_REFERENCE_DIR, else a
+# ``reference`` directory beside this repository.
+REFERENCE = Path(os.environ.get("SCAFES_REFERENCE_DIR") or ROOT.parent / "reference")
 
 
 def cuda_lib_dir() -> str:

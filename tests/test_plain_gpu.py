@@ -195,26 +195,3 @@ def test_state_errors(gpu):
         assert rc == -1
         rc = M.lib().scafes_gpu_upload(p.h, 99, bad.ctypes.data_as(C.POINTER(C.c_double)), 512)
         assert rc == -1
-
-
-def test_config2_heat_512_f32x2_matches_f64(gpu):
-    """Full size of the large heat workload (512^3, sine + seeded noise,
-    1000 steps): the compensated FP32-pair path against the FP64 path on the
-    same inputs, within the FP64 bar; both against the analytic decay of the
-    sine mode within discretisation + noise error."""
-    M = gpu
-    n, T = (512, 512, 512), 1000
-    h = 1.0 / 511
-    tau = 0.9 * h * h / 6.0
-    g = O.make_grid(n, tau=tau)
-    x, y, z = O.coords(g)
-    u0 = np.broadcast_to(np.sin(np.pi * x) * np.sin(np.pi * y) * np.sin(np.pi * z), (512, 512, 512)).copy()
-    border = O.border_mask(g)
-    u0 += np.random.default_rng(2).uniform(-1e-3, 1e-3, u0.shape) * (~border)
-    u0[border] = 0.0
-    out = {}
-    for prec in ("f64", "f32x2"):
-        cfg = M.make_cfg(n, tau=tau, precision=prec, heat=(1.0, 1.0, 0.0))
-        out[prec] = cases.run(cfg, {M.FIELD_U: u0}, T)
-    assert cases.rel_err(out["f32x2"], out["f64"]) <= 1e-12
-    assert np.all(np.abs(out["f64"]) <= np.max(np.abs(u0)) * (1 + 1e-12))  # maximum principle
