@@ -57,6 +57,14 @@ class Grid(C.Structure):
                 ("t_start", C.c_double), ("n_layers", C.c_int)]
 
 
+class Tissue(C.Structure):
+    _fields_ = [(f, C.POINTER(C.c_double)) for f in ("rho", "c", "k", "rho_b", "c_b", "omega", "t_blood", "q",
+                                                      "surface")] + \
+               [("zmax_kind", C.c_int)] + [(f, C.c_double) for f in ("q_bc", "q_skull", "h_conv", "t_amb",
+                                                                     "epsilon", "sigma")] + \
+               [("border", C.c_int), ("g_bdry", C.POINTER(C.c_double))]
+
+
 class Known(C.Structure):
     _fields_ = [("base", C.POINTER(C.c_double)), ("form", C.c_int), ("a", C.c_double),
                 ("b", C.c_double)]
@@ -85,6 +93,8 @@ def lib():
         L.orc_heat_radiation.argtypes = [C.POINTER(Grid)] + [C.c_double] * 7 + [C.c_int, dp, Known, Known,
                                                                               Known, C.c_int]
         L.orc_kheat_tangent.argtypes = [C.POINTER(Grid), dp, dp, C.c_int, dp, dp, C.c_int]
+        L.orc_pennes_tissue.argtypes = [C.POINTER(Grid), C.POINTER(Tissue), C.c_int, dp, C.c_int]
+        L.orc_pennes_tissue.restype = C.c_int
         L.orc_stencil_width_one.argtypes = [C.POINTER(Grid), C.c_int, dp, C.c_int]
         L.orc_stencil_width_var.argtypes = [C.POINTER(Grid), C.c_int, C.c_int, dp, C.c_int]
         L.orc_kheat_forward.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.c_int]
@@ -205,6 +215,47 @@ def pennes_mri(g: Grid, u0, nsteps, rho, c, k, rho_b, c_b, omega, t_blood, q, g_
     _check(lib().orc_pennes_mri(C.byref(g), rho, c, k, rho_b, c_b, omega, t_blood, _p(q), _p(gb),
                                 nsteps, _p(u), nthreads), "pennes_mri")
     return u
+
+
+TISSUE_FIELDS = ("rho", "c", "k", "rho_b", "c_b", "omega", "t_blood", "q")
+
+
+def pennes_tissue(g: Grid, u0, nsteps, fields: dict, surface=None, zmax_kind=0, q_bc=0.0, q_skull=0.0,
+                  h_conv=0.0, t_amb=0.0, epsilon=0.0, sigma=5.670373e-8, g_bdry=None, nthreads=0):
+    """The reference's tissue examples (orc_pennes_tissue): ``fields`` maps
+    each name of TISSUE_FIELDS to an array over the nodes (or a scalar);
+    g_bdry given => Dirichlet border from it, else the examples' flux
+    border."""
+    shape = (g.n[2], g.n[1], g.n[0])
+    keep = {}
+    for name in TISSUE_FIELDS:
+        keep[name] = np.ascontiguousarray(np.broadcast_to(np.asarray(fields.get(name, 0.0), dtype=np.float64),
+                                                          shape))
+    if surface is not None:
+        keep["surface"] = np.ascontiguousarray(np.broadcast_to(np.asarray(surface, dtype=np.float64), shape))
+    if g_bdry is not None:
+        keep["g_bdry"] = np.ascontiguousarray(np.broadcast_to(np.asarray(g_bdry, dtype=np.float64), shape))
+    ts = Tissue(*[_p(keep[n]) for n in TISSUE_FIELDS], _p(keep.get("surface")), zmax_kind, q_bc, q_skull,
+                h_conv, t_amb, epsilon, sigma, 1 if g_bdry is not None else 0, _p(keep.get("g_bdry")))
+    u = np.ascontiguousarray(u0, dtype=np.float64).copy()
+    _check(lib().orc_pennes_tissue(C.byref(g), C.byref(ts), nsteps, _p(u), nthreads), "pennes_tissue")
+    return u
+
+
+def tumour_fields(g: Grid, P: dict) -> dict:
+    """Per-node fields of the tumour example (TumorHeatEqnFDM.hpp:234-252):
+    omega and Q from the sphere test, the tissue constants everywhere;
+    P holds the example's Parameters (RHO, C, K, ... as in its .ini)."""
+    x, y, z = coords(g)
+    radius = P["DIAMETER"] / 2.0
+    centre = (g.last[0] / 2.0, g.last[1] / 2.0, g.last[2] - P["DEPTH"])
+    d = 0.0 + (x - centre[0]) * (x - centre[0])
+    d = d + (y - centre[1]) * (y - centre[1])
+    d = d + (z - centre[2]) * (z - centre[2])
+    inside = np.broadcast_to(d <= radius * radius, (g.n[2], g.n[1], g.n[0]))
+    return {"rho": P["RHO"], "c": P["C"], "k": P["K"], "rho_b": P["RHO_B"], "c_b": P["C_PB"],
+            "omega": np.where(inside, P["OMEGA_B_TUMOR"], P["OMEGA_B_BRAIN"]),
+            "t_blood": P["T_A"], "q": np.where(inside, P["Q_TUMOR"], P["Q_BRAIN"])}
 
 
 def stencil_width_one(g: Grid, u0, nsteps, nthreads=0):

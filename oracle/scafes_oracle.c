@@ -344,6 +344,104 @@ int orc_pennes_mri(const orc_grid* g, double rho, double c, double k,
     return 0;
 }
 
+/* One flux term of the reference's tissue examples in direction p at a
+ * border node: the bracket (...) / (h*h) of MRIDataPBHEqnFDM.hpp:189-262
+ * and TumorHeatEqnFDM.hpp:303-346, with the missing neighbour replaced. */
+static double tissue_bracket(const orc_grid* g, const orc_tissue* ts, const double* uo, size_t m,
+                             long sp, int p, int at_min, int at_max, double k, double v_partial)
+{
+    const double h = g->h[p];
+    const double u = uo[m];
+    if (at_max) {
+        const double a = uo[m - sp];
+        if (p == g->dim - 1) {
+            if (ts->zmax_kind == 1) {
+                /* TumorHeatEqnFDM.hpp:307-317: Cauchy. */
+                return ((a + a) - ((2.0 * h / k) * ts->h_conv * (u - ts->t_amb))) - 2.0 * u;
+            }
+            if (ts->surface && (int)ts->surface[m] == 1) {
+                /* MRIDataPBHEqnFDM.hpp:197-217: open skull, Cauchy and
+                 * radiation; the radiated temperature is the partially
+                 * updated vNew of this node. */
+                const double tempOld = v_partial + 273.15;
+                const double tempOldPow4 = tempOld * tempOld * tempOld * tempOld;
+                const double tempAmb = ts->t_amb + 273.15;
+                const double tempAmbPow4 = tempAmb * tempAmb * tempAmb * tempAmb;
+                return (((a + a) - ((2.0 * h / k) * ts->h_conv * (u - ts->t_amb)))
+                        - ((2.0 * h / k) * ts->epsilon * ts->sigma * (tempOldPow4 - tempAmbPow4)))
+                       - 2.0 * u;
+            }
+            /* MRIDataPBHEqnFDM.hpp:219-229: closed skull, Neumann. */
+            return ((a + a) - ((2.0 * h / k) * (-1.0 * ts->q_skull))) - 2.0 * u;
+        }
+        /* Neumann at the other max faces. */
+        return ((a + a) - ((2.0 * h / k) * (-1.0 * ts->q_bc))) - 2.0 * u;
+    }
+    if (at_min) {
+        /* Neumann at the min faces (MRIDataPBHEqnFDM.hpp:244-253). */
+        const double b = uo[m + sp];
+        return ((b + ((2.0 * h / k) * ts->q_bc)) + b) - 2.0 * u;
+    }
+    return (uo[m - sp] + uo[m + sp]) - 2.0 * u;
+}
+
+int orc_pennes_tissue(const orc_grid* g, const orc_tissue* ts, int nsteps, double* u,
+                      int nthreads)
+{
+    const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+    const int nn3[3] = {nx, ny, nz};
+    const size_t nn = n_total(g);
+    if (!ts || !ts->rho || !ts->c || !ts->k || !ts->rho_b || !ts->c_b || !ts->omega || !ts->t_blood)
+        return -2;
+    if (ts->border == 1 && !ts->g_bdry) return -2;
+    double* w = (double*)malloc(nn * sizeof(double));
+    if (!w) return -1;
+    const long stride[3] = {1, nx, (long)nx * ny};
+    set_threads(nthreads);
+    double* uo = u;
+    double* un = w;
+    for (int t = 1; t <= nsteps; ++t) {
+#pragma omp parallel for schedule(static)
+        for (int kk = 0; kk < nz; ++kk) {
+            for (int j = 0; j < ny; ++j) {
+                for (int i = 0; i < nx; ++i) {
+                    const size_t m = IDX(i, j, kk, nx, ny);
+                    const int idx[3] = {i, j, kk};
+                    const int border = orc_is_border(g, i, j, kk);
+                    if (border && ts->border == 1) {
+                        un[m] = ts->g_bdry[m];
+                        continue;
+                    }
+                    /* MRIDataPBHEqnFDM.hpp:147-154 (TumorHeatEqnFDM.hpp:
+                     * 234-252 with the tissue constants in every node). */
+                    const double rho = ts->rho[m], c = ts->c[m], k = ts->k[m];
+                    const double rho_blood = ts->rho_b[m], c_blood = ts->c_b[m];
+                    const double omega = ts->omega[m], T_blood = ts->t_blood[m];
+                    const double q = ts->q ? ts->q[m] : 0.0;
+                    double v = uo[m];
+                    for (int p = 0; p < g->dim; ++p) {
+                        double br;
+                        if (!border) {
+                            br = uo[m - stride[p]] + uo[m + stride[p]] - 2.0 * uo[m];
+                        } else {
+                            br = tissue_bracket(g, ts, uo, m, stride[p], p, idx[p] == 0,
+                                                idx[p] == nn3[p] - 1, k, v);
+                        }
+                        v += g->tau * (k / (rho * c)) * br / (g->h[p] * g->h[p]);
+                    }
+                    v += g->tau * ((rho_blood * c_blood) / (rho * c)) * omega * (T_blood - uo[m]);
+                    v += g->tau * (1.0 / (rho * c)) * q;
+                    un[m] = v;
+                }
+            }
+        }
+        double* tmp = uo; uo = un; un = tmp;
+    }
+    if (uo != u) memcpy(u, uo, nn * sizeof(double));
+    free(w);
+    return 0;
+}
+
 int orc_stencil_width_one(const orc_grid* g, int nsteps, double* u,
                           int nthreads)
 {

@@ -112,6 +112,30 @@ int orc_pennes_mri(const orc_grid* g, double rho, double c, double k,
                    const double* q, const double* g_bdry, int nsteps,
                    double* u, int nthreads);
 
+/* Pennes bioheat with every coefficient a field over the nodes -- the
+ * updateInner/updateBorder of the reference's tissue examples,
+ * examples/MRIDataPBHEqnFDM/MRIDataPBHEqnFDM.hpp:143-275 (known fields
+ * rho, c, lambda, rho_blood, c_blood, omega, T_blood, q, surface) and
+ * examples/TumorHeatEqnFDM/TumorHeatEqnFDM.hpp:234-353 (constants, with
+ * omega and Q chosen per node by the tumour sphere), in the reference's
+ * operation order.  border 0: the examples' flux border -- Neumann with
+ * q_bc at the min faces and the x, y max faces; at the z max face
+ * Neumann with q_skull (MRI, surface 0 or NULL), Cauchy and radiation with
+ * h_conv, t_amb, epsilon, sigma (MRI, surface 1; the radiated temperature
+ * is the partially updated node value, as in the reference), or Cauchy
+ * with h_conv, t_amb (zmax_kind 1, the tumour); border 1: Dirichlet from
+ * g_bdry. */
+typedef struct orc_tissue {
+    const double *rho, *c, *k, *rho_b, *c_b, *omega, *t_blood, *q;
+    const double* surface;
+    int zmax_kind;
+    double q_bc, q_skull, h_conv, t_amb, epsilon, sigma;
+    int border;
+    const double* g_bdry;
+} orc_tissue;
+int orc_pennes_tissue(const orc_grid* g, const orc_tissue* ts, int nsteps, double* u,
+                      int nthreads);
+
 /* HeatEqnFdmStencilWidthOne (tests/system/HeatEqnFdmStencilWidthOne/
  * HeatEqnFdmStencilWidthOne.hpp:120-163). */
 int orc_stencil_width_one(const orc_grid* g, int nsteps, double* u,

@@ -97,3 +97,31 @@ def run(cfg, fields, nsteps):
 
 def rel_err(a, ref):
     return float(np.max(np.abs(a - ref)) / max(np.max(np.abs(ref)), 1e-300))
+
+
+# ---- the reference's tissue examples (tests/golden/tissue_*.npz) -------------
+
+TUMOUR_ORDER = ("RHO", "C", "K", "Q_BRAIN", "Q_TUMOR", "RHO_B", "C_PB", "OMEGA_B_BRAIN", "OMEGA_B_TUMOR", "T_I",
+                "H", "T_INF", "Q_BC", "DIAMETER", "DEPTH", "T_A")
+MRI_ORDER = ("H", "T_INF", "Q_BC", "Q_SKULL", "EPSILON", "T_INIT")
+
+
+def tissue_case(name):
+    """(golden dict, oracle grid, tissue fields, border keywords of
+    oracle.pennes_tissue, initial iterate) of one tissue golden case."""
+    d = load_golden(name)
+    n = tuple(int(v) for v in d["n"])
+    g = O.make_grid(n, last=tuple(d["last"]), tau=float(d["tau"]))
+    shape = (n[2], n[1], n[0])
+    if name == "tissue_tumour":
+        P = dict(zip(TUMOUR_ORDER, d["params"]))
+        fields = O.tumour_fields(g, P)
+        kw = dict(zmax_kind=1, q_bc=P["Q_BC"], h_conv=P["H"], t_amb=P["T_INF"])
+        u0 = np.full(shape, P["T_I"])
+    else:
+        P = dict(zip(MRI_ORDER, d["params"]))
+        fields = dict(zip(O.TISSUE_FIELDS, d["fields"]))
+        kw = dict(surface=d["surface"], zmax_kind=0, q_bc=P["Q_BC"], q_skull=P["Q_SKULL"], h_conv=P["H"],
+                  t_amb=P["T_INF"], epsilon=P["EPSILON"])
+        u0 = np.full(shape, P["T_INIT"])
+    return d, g, fields, kw, u0

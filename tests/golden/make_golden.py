@@ -7,7 +7,7 @@ headers by ``make -C oracle ref`` -- and stores its inputs and final iterate.
 
 Run from the repository root (needs the reference checkout for the build):
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [--tissue]
 
 The .npz files are committed; the GPU machine never runs this script.
 """
@@ -117,6 +117,58 @@ def main():
     cases["pennes_mri"] = dict(n=n, nsteps=T, tau=tau, t_end=tau * T, u0=u0, q=q, g=gb,
                                params=params, final=r)
 
+    cases.update(tissue_cases(tmp))
+    save(cases)
+
+
+# The reference's tissue examples (examples/TumorHeatEqnFDM, examples/
+# MRIDataPBHEqnFDM), compiled unmodified: per-node coefficients and the
+# examples' own flux borders.
+TUMOUR_PARAMS = dict(RHO=1040.0, C=3650.0, K=0.6, Q_BRAIN=25000.0, Q_TUMOR=60000.0, RHO_B=1052.0, C_PB=3800.0,
+                     OMEGA_B_BRAIN=0.004, OMEGA_B_TUMOR=0.0007, T_I=37.0, H=10.0, T_INF=22.4, Q_BC=0.0,
+                     DIAMETER=0.01, DEPTH=0.008, T_A=37.0)
+TUMOUR_ORDER = ("RHO", "C", "K", "Q_BRAIN", "Q_TUMOR", "RHO_B", "C_PB", "OMEGA_B_BRAIN", "OMEGA_B_TUMOR", "T_I",
+                "H", "T_INF", "Q_BC", "DIAMETER", "DEPTH", "T_A")
+MRI_ORDER = ("H", "T_INF", "Q_BC", "Q_SKULL", "EPSILON", "T_INIT")
+
+
+def mri_fields(n, seed):
+    """Seeded tissue fields of the MRI example over the nodes (uniform per
+    node in physiological ranges), in oracle.TISSUE_FIELDS order."""
+    shape = (n[2], n[1], n[0])
+    rng = np.random.default_rng(seed)
+    ranges = {"rho": (1000, 1100), "c": (3500, 3800), "k": (0.4, 0.6), "rho_b": (1040, 1060),
+              "c_b": (3700, 3900), "omega": (0.001, 0.005), "t_blood": (36.5, 37.5), "q": (1e4, 3e4)}
+    return np.stack([rng.uniform(*ranges[k], shape) for k in O.TISSUE_FIELDS])
+
+
+def tissue_cases(tmp):
+    cases = {}
+    # Tumour example on its domain (0.06 x 0.03 x 0.03 m, Parameters.ini.in values, a
+    # hotter tumour), coarser grid, 200 steps of 5 s (below the stability limit).
+    n, T, tau, last = (20, 12, 12), 200, 5.0, (0.06, 0.03, 0.03)
+    P = TUMOUR_PARAMS
+    r = O.run_ref("ref_tumor_example", n, T, tmp, tau=tau, t_end=tau * T, last=last, inputs=np.zeros(1),
+                  extra=[P[k] for k in TUMOUR_ORDER])
+    cases["tissue_tumour"] = dict(n=n, nsteps=T, tau=tau, t_end=tau * T, last=last,
+                                  params=np.array([P[k] for k in TUMOUR_ORDER]), final=r)
+    # MRI example with seeded coefficient fields: closed skull (linear borders) and an
+    # open-skull patch on the z-max face (convection + radiation).
+    n, T, tau, last = (14, 12, 10), 100, 5.0, (0.05, 0.04, 0.03)
+    par = dict(H=10.0, T_INF=22.0, Q_BC=5.0, Q_SKULL=-3.0, EPSILON=0.98, T_INIT=37.0)
+    fields = mri_fields(n, 31)
+    for name, patch in (("tissue_mri_closed", False), ("tissue_mri_open", True)):
+        surface = np.zeros((n[2], n[1], n[0]))
+        if patch:
+            surface[-1, 3:9, 4:10] = 1.0
+        r = O.run_ref("ref_mri_example", n, T, tmp, tau=tau, t_end=tau * T, last=last,
+                      inputs=np.concatenate([fields, surface[None]]), extra=[par[k] for k in MRI_ORDER])
+        cases[name] = dict(n=n, nsteps=T, tau=tau, t_end=tau * T, last=last, fields=fields, surface=surface,
+                           params=np.array([par[k] for k in MRI_ORDER]), final=r)
+    return cases
+
+
+def save(cases):
     for name, c in cases.items():
         arrays = {k: np.asarray(v) for k, v in c.items()}
         np.savez_compressed(OUT / f"{name}.npz", **arrays)
@@ -124,4 +176,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["--tissue"]:   # only the tissue-example cases
+        save(tissue_cases(tempfile.mkdtemp()))
+    else:
+        main()

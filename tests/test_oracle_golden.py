@@ -231,3 +231,16 @@ def test_flux_border_bit_exact(name):
     assert np.array_equal(u, d["final"])
     exact = S * (1.0 + O.lib().orc_time(g, T))
     assert np.max(np.abs(u - exact)) / np.max(np.abs(exact)) < 1e-14
+
+
+@pytest.mark.parametrize("name", ["tissue_tumour", "tissue_mri_closed", "tissue_mri_open"])
+def test_tissue_examples_bit_exact(name):
+    """The oracle's restatement of the reference's tissue examples
+    (examples/TumorHeatEqnFDM/TumorHeatEqnFDM.hpp:234-353, examples/
+    MRIDataPBHEqnFDM/MRIDataPBHEqnFDM.hpp:143-275: coefficients per node,
+    Neumann / Cauchy / radiation borders) against the reference's own classes
+    run by its Problem::iterateOverTime, bit for bit."""
+    import cases
+    d, g, fields, kw, u0 = cases.tissue_case(name)
+    u = O.pennes_tissue(g, u0, int(d["nsteps"]), fields, **kw)
+    assert np.array_equal(u, d["final"])
