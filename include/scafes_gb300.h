@@ -71,7 +71,10 @@ enum scafes_field {
     SCAFES_FIELD_G_C = 7, /* higher time orders of G, stored in FP64;    */
     SCAFES_FIELD_G_D = 8, /* read by SCAFES_BORDER_TABLE rules only      */
     SCAFES_FIELD_G_E = 9,
-    SCAFES_FIELD_COUNT = 10
+    SCAFES_FIELD_C0 = 10, /* centre coefficient per node   } variable-    */
+    SCAFES_FIELD_CA = 11, /* axis scale per node           } coefficient  */
+                          /* update, see scafes_cfg                        */
+    SCAFES_FIELD_COUNT = 12
 };
 
 /* ---- border (updateBorder) kinds --------------------------------------- */
@@ -92,8 +95,24 @@ enum scafes_border {
      * {Neumann,Cauchy}/{Neumann,Cauchy}.hpp (Dirichlet at the min faces, a
      * flux condition with the mirrored neighbour at the max faces), or any
      * other rule of the same shape. */
-    SCAFES_BORDER_TABLE = 2
+    SCAFES_BORDER_TABLE = 2,
+    /* One linear rule per border node (scafes_gpu_set_border_node_rules):
+     * borders whose rule changes from node to node, such as the Neumann and
+     * Cauchy faces of the reference's tissue examples, whose coefficients
+     * are fields (examples/MRIDataPBHEqnFDM/MRIDataPBHEqnFDM.hpp:172-275,
+     * examples/TumorHeatEqnFDM/TumorHeatEqnFDM.hpp:278-353).  Needs the
+     * variable-coefficient update (slots C0 and CA uploaded). */
+    SCAFES_BORDER_NODES = 3
 };
+
+/* The rule of one border node of a SCAFES_BORDER_NODES problem, evaluated
+ * in FP64:  u_new = cu*u + sum_d cn[d]*u_d + cst,  neighbours d = x-, x+,
+ * y-, y+, z-, z+ (a neighbour outside the grid must have weight 0). */
+typedef struct scafes_border_node_rule {
+    double cu;
+    double cn[6];
+    double cst;
+} scafes_border_node_rule;
 
 /* One border class's rule, evaluated in FP64 on border nodes:
  *   u_new = cu*u + sum_d cn[d]*u_d + cf*F(time(t-1))
@@ -133,7 +152,20 @@ enum scafes_flux_kind {
  *   cp[p] = tau*a/h_p^2, c0 = 1 - 2*sum_p cp[p], cf = tau/(rho*c);
  * Pennes (tests/system/PennesBioheatEqnFDM/PennesBioheatEqnFDM.hpp:153-168)
  * additionally subtracts tau*(rho_b*c_b/(rho*c))*W from c0.
- * scafes_star7_heat_coeffs() fills them from the physical parameters. */
+ * scafes_star7_heat_coeffs() fills them from the physical parameters.
+ *
+ * Variable coefficients: once both slots SCAFES_FIELD_C0 and
+ * SCAFES_FIELD_CA are uploaded, the inner update is
+ *   u_new = C0(x)*u + CA(x) * sum_p cp[p]*(u_{p-} + u_{p+}) + cf*F_A(x),
+ * c0 is unused and cp[p] are the axis factors (1/h_p^2 for the Pennes
+ * update with CA = tau*lambda/(rho*c)): the updateInner of the reference's
+ * tissue examples, whose conductivity, heat capacity, perfusion and heat
+ * source are fields over the nodes (examples/MRIDataPBHEqnFDM/
+ * MRIDataPBHEqnFDM.hpp:143-169; examples/TumorHeatEqnFDM/
+ * TumorHeatEqnFDM.hpp:234-270, where perfusion and source change inside
+ * the tumour sphere).  C0, CA and F_A are streamed by TMA with the iterate.
+ * It takes F64 or F32, one border layer, a static source (no F_B) and the
+ * Dirichlet, table or per-node border. */
 typedef struct scafes_cfg {
     int dim;                 /* must be 3 */
     int n_nodes[3];          /* nodes per axis, each >= 3 */
@@ -222,6 +254,20 @@ int scafes_snapshot_read(const char* path, int index, double* host, size_t n,
  * with cg_old or cg_new != 0 reads G (slots G_A .. G_E). */
 int scafes_gpu_set_border_forms(scafes_handle* h,
                                 const scafes_border_form forms[64]);
+
+/* Border nodes of the grid of *cfg (within n_layers_at_border of a face):
+ * the number of rules scafes_gpu_set_border_node_rules takes. */
+int scafes_border_node_count(const scafes_cfg* cfg, long long* count);
+
+/* Sets the per-node border rules of a SCAFES_BORDER_NODES problem: one rule
+ * per border node, the border nodes in Fortran order (x fastest, i.e. the
+ * order of idx = i + nx*(j + ny*k) restricted to border nodes);
+ * n = scafes_border_node_count.  Replaces the per-node updateBorder calls
+ * of evalTypeTwoAt (src/ScaFES_Problem.hpp:5399-5476) for borders that are
+ * linear in the iterate with coefficients that change from node to node.
+ * Copies the rules to the device (FP64, 64 bytes per border node). */
+int scafes_gpu_set_border_node_rules(scafes_handle* h, const scafes_border_node_rule* rules,
+                                     size_t n);
 
 /* Time variable of the border field G of a SCAFES_BORDER_TABLE problem:
  *   G(t) = G_A + s*(G_B + s*(G_C + s*(G_D + s*G_E))),

@@ -22,9 +22,10 @@ LIB_PATH = PKG / "libscafes_gb300.so"
 PREC_F64, PREC_F32X2, PREC_F32, PREC_F64E = 0, 1, 2, 3
 PRECISIONS = {"f64": PREC_F64, "f32x2": PREC_F32X2, "f32": PREC_F32, "f64e": PREC_F64E}
 # enum scafes_field
-FIELD_U, FIELD_F_A, FIELD_F_B, FIELD_G_A, FIELD_G_B, FIELD_E_A, FIELD_E_B, FIELD_G_C, FIELD_G_D, FIELD_G_E = range(10)
+(FIELD_U, FIELD_F_A, FIELD_F_B, FIELD_G_A, FIELD_G_B, FIELD_E_A, FIELD_E_B, FIELD_G_C, FIELD_G_D, FIELD_G_E,
+ FIELD_C0, FIELD_CA) = range(12)
 # enum scafes_border
-BORDER_DIRICHLET, BORDER_MIRROR_POW2, BORDER_TABLE = 0, 1, 2
+BORDER_DIRICHLET, BORDER_MIRROR_POW2, BORDER_TABLE, BORDER_NODES = 0, 1, 2, 3
 FLUX_NEUMANN, FLUX_CAUCHY, FLUX_RADIATION = 0, 1, 2
 
 STATUS = {0: "SCAFES_OK", -1: "SCAFES_ERR_ARG", -2: "SCAFES_ERR_CUDA", -3: "SCAFES_ERR_STATE",
@@ -44,6 +45,23 @@ class BorderForm(C.Structure):
 
 
 BorderForms = BorderForm * 64
+
+
+class NodeRule(C.Structure):
+    """Mirror of ``struct scafes_border_node_rule`` (one border node's rule)."""
+    _fields_ = [("cu", C.c_double), ("cn", C.c_double * 6), ("cst", C.c_double)]
+
+
+def node_rules_array(cu, cn, cst) -> np.ndarray:
+    """The (m, 8) array of per-node border rules (cu, cn[0..5], cst) that
+    set_border_node_rules takes, from arrays over the border nodes in
+    Fortran order: cu (m,), cn (m, 6), cst (m,)."""
+    m = len(cu)
+    raw = np.empty((m, 8), dtype=np.float64)
+    raw[:, 0] = cu
+    raw[:, 1:7] = cn
+    raw[:, 7] = cst
+    return raw
 
 
 class Cfg(C.Structure):
@@ -81,6 +99,8 @@ def lib() -> C.CDLL:
                                                C.POINTER(BorderForm)]
         L.scafes_gpu_set_border_forms.argtypes = [vp, C.POINTER(BorderForm)]
         L.scafes_gpu_set_border_time_basis.argtypes = [vp, C.c_double, C.c_double]
+        L.scafes_border_node_count.argtypes = [C.POINTER(Cfg), C.POINTER(C.c_longlong)]
+        L.scafes_gpu_set_border_node_rules.argtypes = [vp, dp, C.c_size_t]
         L.scafes_gpu_step_snapshots.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_char_p]
         L.scafes_snapshot_info.argtypes = [C.c_char_p, C.c_int * 3, C.POINTER(C.c_int)]
         L.scafes_snapshot_read.argtypes = [C.c_char_p, C.c_int, dp, C.c_size_t, C.POINTER(C.c_longlong),
@@ -131,6 +151,12 @@ def _check(rc: int, h=None):
 
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def border_node_count(cfg: "Cfg") -> int:
+    n = C.c_longlong()
+    _check(lib().scafes_border_node_count(C.byref(cfg), C.byref(n)))
+    return n.value
 
 
 def make_cfg(n, first=(0.0, 0.0, 0.0), last=(1.0, 1.0, 1.0), tau=0.0, t_start=0.0,
@@ -213,6 +239,14 @@ class Plain:
 
     def set_border_forms(self, forms):
         _check(lib().scafes_gpu_set_border_forms(self.h, forms), self.h)
+
+    def set_border_node_rules(self, rules: np.ndarray):
+        """Per-node border rules (SCAFES_BORDER_NODES): an array (m, 8) of
+        (cu, cn[0..5], cst) over the border nodes in Fortran order."""
+        r = np.ascontiguousarray(rules, dtype=np.float64)
+        if r.ndim != 2 or r.shape[1] != 8:
+            raise ValueError("node rules must have shape (border nodes, 8)")
+        _check(lib().scafes_gpu_set_border_node_rules(self.h, _dp(r), r.shape[0]), self.h)
 
     def set_border_time_basis(self, t_center: float, t_rate: float):
         """G(t) = sum_k G_k s^k with s = (time(t) - t_center) * t_rate."""

@@ -48,6 +48,9 @@ struct scafes_handle {
     bool tm_ok[2][STAR7_NUM_TILES] = {};
     CUtensorMap tmf[STAR7_NUM_TILES];     // TMA descriptors of F_A (box 32 x BY) per tile
     bool tmf_ok[STAR7_NUM_TILES] = {};
+    CUtensorMap tmc[2][STAR7_NUM_TILES];  // TMA descriptors of C0 and CA (box 32 x BY) per tile
+    bool tmc_ok[2][STAR7_NUM_TILES] = {};
+    scafes_border_node_rule* nodes = nullptr;  // per-node border rules (SCAFES_BORDER_NODES)
     int tile = 0;                         // tile variant of the sweep
     int depth = 1;                        // temporal blocking depth (1 or 2)
     CUtensorMap tm_tb[2];                 // TMA descriptors of u[0], u[1] for depth-2 passes
@@ -149,8 +152,11 @@ static int validate(const scafes_cfg* c) {
         c->precision != SCAFES_PREC_F32)
         return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: precision %d not supported", c->precision);
     if (c->border != SCAFES_BORDER_DIRICHLET && c->border != SCAFES_BORDER_MIRROR_POW2 &&
-        c->border != SCAFES_BORDER_TABLE)
+        c->border != SCAFES_BORDER_TABLE && c->border != SCAFES_BORDER_NODES)
         return fail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_gpu_create: border kind %d not supported", c->border);
+    if (c->border == SCAFES_BORDER_NODES && (c->n_layers_at_border != 1 || c->precision == SCAFES_PREC_F32X2))
+        return fail(nullptr, SCAFES_ERR_UNSUPPORTED,
+                    "scafes_gpu_create: per-node border rules take one border layer and F64 or F32");
     if (c->tile < 0 || c->tile > STAR7_NUM_TILES)
         return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_create: tile=%d out of range [0, %d]", c->tile,
                     STAR7_NUM_TILES);
@@ -168,6 +174,7 @@ extern "C" void scafes_gpu_destroy(scafes_handle* h) {
     for (int i = 0; i < SCAFES_FIELD_COUNT; ++i) cudaFree(h->fld[i]);
     cudaFree(h->stage);
     cudaFree(h->table);
+    cudaFree(h->nodes);
     cudaFree(h->snap_dev);
     for (int i = 0; i < 2; ++i) {
         if (h->snap_host[i]) cudaFreeHost(h->snap_host[i]);
@@ -237,7 +244,8 @@ extern "C" int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out) {
 // Exact-solution slots stay double (only the error check reads them);
 // source and border slots use the element type of the unknown field.
 static bool slot_is_double(int field) {
-    return field == SCAFES_FIELD_E_A || field == SCAFES_FIELD_E_B || field >= SCAFES_FIELD_G_C;
+    return field == SCAFES_FIELD_E_A || field == SCAFES_FIELD_E_B ||
+           (field >= SCAFES_FIELD_G_C && field <= SCAFES_FIELD_G_E);
 }
 
 // Copies the host image of the border table (rules, higher time orders of
@@ -369,7 +377,7 @@ extern "C" int scafes_gpu_upload(scafes_handle* h, int field, const double* host
         rc = h2d(h, h->fld[field], dbl ? SCAFES_PREC_F64 : h->cfg.precision, host);
         if (rc) return rc;
         h->has[field] = true;
-        if (field >= SCAFES_FIELD_G_C) {
+        if (field >= SCAFES_FIELD_G_C && field <= SCAFES_FIELD_G_E) {
             h->table_host.g_hi[field - SCAFES_FIELD_G_C] = (const double*)h->fld[field];
             rc = sync_table(h);
             if (rc) return rc;
@@ -434,6 +442,27 @@ static const CUtensorMap* source_map(scafes_handle* h, int tile) {
     return &h->tmf[tile];
 }
 
+// TMA descriptor of coefficient slot C0 (k = 0) or CA (k = 1) for tile
+// variant `tile`: a 32 x BY box without halo, like the source.
+static const CUtensorMap* coeff_map(scafes_handle* h, int k, int tile) {
+    if (!h->tmc_ok[k][tile]) {
+        CUresult r = make_tensor_map_3d(&h->tmc[k][tile], h->fld[k == 0 ? SCAFES_FIELD_C0 : SCAFES_FIELD_CA],
+                                        (int)h->esz, h->L.nx, h->L.ny, h->L.nz, (size_t)h->L.pitch * h->esz,
+                                        (size_t)h->L.plane * h->esz, BX, star7_box_height(tile) - 2);
+        if (r != CUDA_SUCCESS) {
+            fail(&h->err, SCAFES_ERR_CUDA, "cuTensorMapEncodeTiled (coefficients) failed (%d)", (int)r);
+            return nullptr;
+        }
+        h->tmc_ok[k][tile] = true;
+    }
+    return &h->tmc[k][tile];
+}
+
+// Whether the handle runs the variable-coefficient update (C0 and CA uploaded).
+static bool var_coeffs(const scafes_handle* h) {
+    return h->has[SCAFES_FIELD_C0] && h->has[SCAFES_FIELD_CA];
+}
+
 // TMA descriptor of buffer `buf` for the depth-2 pass (encoded on first use).
 static const CUtensorMap* tb_map(scafes_handle* h, int buf) {
     if (!h->tm_tb_ok[buf]) {
@@ -484,6 +513,38 @@ static int step_impl(scafes_handle* h, int n_steps, int tile, bool timed, int de
         if (h->table_needs_f && (a.fa == nullptr || h->cfg.cf == 0.0))
             return fail(&h->err, SCAFES_ERR_STATE,
                         "scafes_gpu_step: a border rule reads the source F, but no F_A is uploaded or cf == 0");
+    }
+    a.vc = var_coeffs(h);
+    if (h->has[SCAFES_FIELD_C0] != h->has[SCAFES_FIELD_CA])
+        return fail(&h->err, SCAFES_ERR_STATE,
+                    "scafes_gpu_step: the variable-coefficient update needs both slots C0 and CA uploaded");
+    if (h->cfg.border == SCAFES_BORDER_NODES) {
+        if (!a.vc)
+            return fail(&h->err, SCAFES_ERR_STATE,
+                        "scafes_gpu_step: per-node border rules need the coefficient slots C0 and CA");
+        if (!h->nodes)
+            return fail(&h->err, SCAFES_ERR_STATE,
+                        "scafes_gpu_step: set the per-node border rules first (scafes_gpu_set_border_node_rules)");
+        a.nodes = h->nodes;
+    }
+    if (a.vc) {
+        if (h->cfg.precision == SCAFES_PREC_F32X2)
+            return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                        "scafes_gpu_step: the variable-coefficient update runs in F64 or F32, not F32X2");
+        if (h->L.nl != 1)
+            return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                        "scafes_gpu_step: the variable-coefficient update takes one border layer");
+        if (a.fb)
+            return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                        "scafes_gpu_step: the variable-coefficient update takes a static source (no F_B)");
+        if (a.fa && h->cfg.cf != 0.0 && h->cfg.cf != 1.0)
+            return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                        "scafes_gpu_step: with variable coefficients the source enters with cf = 1 (fold other "
+                        "factors into F_A) or cf = 0");
+        if (h->cfg.border == SCAFES_BORDER_MIRROR_POW2)
+            return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                        "scafes_gpu_step: the variable-coefficient update takes the Dirichlet, table or per-node border");
+        if (!(a.tm_c0 = coeff_map(h, 0, tile)) || !(a.tm_ca = coeff_map(h, 1, tile))) return SCAFES_ERR_CUDA;
     }
     a.tm_tb = nullptr;
     const bool tb = depth == 2 && star7_tb_eligible(a);
@@ -541,6 +602,7 @@ extern "C" int scafes_gpu_temporal_depth(const scafes_handle* h, int* depth) {
     a.border = h->cfg.border;
     a.L = h->L;
     a.fb = h->has[SCAFES_FIELD_F_B] ? h->fld[SCAFES_FIELD_F_B] : nullptr;
+    a.vc = var_coeffs(h);
     *depth = (h->depth == 2 && star7_tb_eligible(a)) ? 2 : 1;
     return SCAFES_OK;
 }
@@ -572,6 +634,50 @@ extern "C" int scafes_gpu_set_border_forms(scafes_handle* h, const scafes_border
     const int rc = sync_table(h);
     if (rc) return rc;
     h->table_needs_f = needs_f;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_border_node_count(const scafes_cfg* cfg, long long* count) {
+    if (!cfg || !count) return fail(nullptr, SCAFES_ERR_ARG, "scafes_border_node_count: NULL argument");
+    const int nl = cfg->n_layers_at_border;
+    for (int p = 0; p < 3; ++p)
+        if (cfg->n_nodes[p] < 3 || nl < 1 || 2 * nl > cfg->n_nodes[p])
+            return fail(nullptr, SCAFES_ERR_ARG, "scafes_border_node_count: n_nodes / n_layers_at_border out of range");
+    *count = border_node_count(cfg->n_nodes[0], cfg->n_nodes[1], cfg->n_nodes[2], nl);
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_set_border_node_rules(scafes_handle* h, const scafes_border_node_rule* rules, size_t n) {
+    if (!h || !rules)
+        return fail(h ? &h->err : nullptr, SCAFES_ERR_ARG, "scafes_gpu_set_border_node_rules: NULL argument");
+    if (h->cfg.border != SCAFES_BORDER_NODES)
+        return fail(&h->err, SCAFES_ERR_STATE,
+                    "scafes_gpu_set_border_node_rules: the problem was created with border kind %d, not "
+                    "SCAFES_BORDER_NODES", h->cfg.border);
+    const long long count = border_node_count(h->L.nx, h->L.ny, h->L.nz, h->L.nl);
+    if ((long long)n != count)
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_set_border_node_rules: expected %lld rules, got %zu", count,
+                    n);
+    // A weight on a neighbour outside the grid would read the zero halo
+    // silently: refuse it (faces in direction order x-, x+, y-, y+, z-, z+).
+    long long r = 0;
+    for (int z = 0; z < h->L.nz; ++z)
+        for (int y = 0; y < h->L.ny; ++y)
+            for (int x = 0; x < h->L.nx; ++x) {
+                const bool inner = x > 0 && x < h->L.nx - 1 && y > 0 && y < h->L.ny - 1 && z > 0 && z < h->L.nz - 1;
+                if (inner) continue;
+                const bool out[6] = {x == 0, x == h->L.nx - 1, y == 0, y == h->L.ny - 1, z == 0, z == h->L.nz - 1};
+                for (int d = 0; d < 6; ++d)
+                    if (out[d] && rules[r].cn[d] != 0.0)
+                        return fail(&h->err, SCAFES_ERR_ARG,
+                                    "scafes_gpu_set_border_node_rules: the rule of node (%d,%d,%d) weights neighbour "
+                                    "%d, which lies outside the grid", x, y, z, d);
+                ++r;
+            }
+    if (!h->nodes) CUDA_TRY(h, cudaMalloc(&h->nodes, (size_t)count * sizeof(scafes_border_node_rule)));
+    CUDA_TRY(h, cudaMemcpyAsync(h->nodes, rules, (size_t)count * sizeof(scafes_border_node_rule),
+                                cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return SCAFES_OK;
 }
 
@@ -1025,6 +1131,9 @@ extern "C" int scafes_gpu_adjoint(scafes_handle* h, const double* dJ_du_T, doubl
                                   int n_checkpoints) {
     if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_adjoint: handle is NULL");
     if (!dJ_du_T || !dJ_dk || !dJ_du0) return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_adjoint: NULL array");
+    if (h->has[SCAFES_FIELD_C0] || h->has[SCAFES_FIELD_CA])
+        return fail(&h->err, SCAFES_ERR_UNSUPPORTED,
+                    "scafes_gpu_adjoint: problems with coefficient fields are not covered");
     if (n_checkpoints < 2)
         return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_adjoint: n_checkpoints = %d (at least 2)", n_checkpoints);
     const scafes_cfg& c = h->cfg;

@@ -70,6 +70,29 @@ struct BorderTable {
     double t_center = 0.0, t_rate = 1.0;
 };
 
+// Border nodes (within nl of a face) of an nx x ny x nz grid.
+__host__ __device__ inline long long border_node_count(int nx, int ny, int nz, int nl) {
+    const long long full = (long long)nx * ny * nz;
+    const long long in = (long long)(nx - 2 * nl) * (ny - 2 * nl) * (nz - 2 * nl);
+    return full - (in > 0 ? in : 0);
+}
+
+// Position of border node (x, y, z) among the border nodes in Fortran order
+// (x fastest).  A plane within nl of a z face is all border nodes; another
+// plane has nl full rows at each y face and 2*nl nodes in every other row.
+__host__ __device__ inline long long border_node_index(const Layout& L, int x, int y, int z) {
+    const int nl = L.nl;
+    const long long pb = (long long)L.nx * L.ny;                                   // border plane
+    const long long pi = 2LL * nl * L.nx + (long long)(L.ny - 2 * nl) * 2 * nl;   // other plane
+    const int zb = (z < nl ? z : nl) + (z > L.nz - nl ? z - (L.nz - nl) : 0);  // border planes below z
+    long long idx = (long long)zb * pb + (long long)(z - zb) * pi;
+    if (z < nl || z >= L.nz - nl) return idx + (long long)y * L.nx + x;
+    const int yb = (y < nl ? y : nl) + (y > L.ny - nl ? y - (L.ny - nl) : 0);  // full rows below y
+    idx += (long long)yb * L.nx + (long long)(y - yb) * 2 * nl;
+    if (y < nl || y >= L.ny - nl) return idx + x;
+    return idx + (x < nl ? x : nl + (x - (L.nx - nl)));
+}
+
 struct Star7Launch {
     int precision;        // enum scafes_precision
     int border;           // enum scafes_border
@@ -92,6 +115,12 @@ struct Star7Launch {
     const CUtensorMap* tm_tb;  // TMA descriptor of the old iterate for depth-2 passes
     double mirror_corr;   // 2^t for SCAFES_BORDER_MIRROR_POW2
     const BorderTable* table;  // device rules for SCAFES_BORDER_TABLE
+    // Variable coefficients (slots C0 and CA uploaded): C0, CA staged by TMA
+    // with the iterate (boxes 32 x BY of the tile), like F_A.
+    bool vc = false;
+    const CUtensorMap* tm_c0 = nullptr;
+    const CUtensorMap* tm_ca = nullptr;
+    const scafes_border_node_rule* nodes = nullptr;  // SCAFES_BORDER_NODES rules
 };
 
 // Enqueues one sweep (one time step) on `stream`.  Returns cudaSuccess or the

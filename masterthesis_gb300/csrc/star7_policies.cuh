@@ -30,7 +30,21 @@ struct PolF64 {
     }
     static __device__ __forceinline__ T src(T fa, T fb, const Split& time, bool has_b) {
         return has_b ? fa + time.d * fb : fa;
-    }    // All R rows of one thread (row k's s/n neighbours are rows k-1/k+1,
+    }
+
+    // Variable coefficients: c0x * u + cax * (cx (w+e) + cy (s+n) + cz (b+t))
+    // + f, with the node's own C0 and CA and the source with weight 1
+    // (8 FP64 operations).
+    template <bool HAS_F>
+    static __device__ __forceinline__ T star_vc(const Star7Coeffs& c, T u, T w, T e, T s, T n, T b, T t, T f,
+                                                T c0x, T cax) {
+        double l = c.cx * (w + e);
+        l = fma(c.cy, s + n, l);
+        l = fma(c.cz, b + t, l);
+        const double v = HAS_F ? fma(c0x, u, f) : c0x * u;
+        return fma(cax, l, v);
+    }
+    // All R rows of one thread (row k's s/n neighbours are rows k-1/k+1,
     // ym/yp beyond the ends).
     template <bool HAS_F, int R>
     static __device__ __forceinline__ void star_rows(const Star7Coeffs& c, const T (&below)[R], const T (&cur)[R],
@@ -63,7 +77,17 @@ struct PolF32 {
     }
     static __device__ __forceinline__ T src(T fa, T fb, const Split& time, bool has_b) {
         return has_b ? fmaf(time.hi, fb, fa) : fa;
-    }    // All R rows of one thread (row k's s/n neighbours are rows k-1/k+1,
+    }
+    template <bool HAS_F>
+    static __device__ __forceinline__ T star_vc(const Star7Coeffs& c, T u, T w, T e, T s, T n, T b, T t, T f,
+                                                T c0x, T cax) {
+        float l = c.cxh * (w + e);
+        l = fmaf(c.cyh, s + n, l);
+        l = fmaf(c.czh, b + t, l);
+        const float v = HAS_F ? fmaf(c0x, u, f) : c0x * u;
+        return fmaf(cax, l, v);
+    }
+    // All R rows of one thread (row k's s/n neighbours are rows k-1/k+1,
     // ym/yp beyond the ends).
     template <bool HAS_F, int R>
     static __device__ __forceinline__ void star_rows(const Star7Coeffs& c, const T (&below)[R], const T (&cur)[R],

@@ -25,7 +25,9 @@ namespace scafes {
 // indices are shifts).  Fewer stages leave room for more CTAs per SM.
 // FS: each stage also holds the source F_A of its plane (a 32 x BY box
 // without halo), streamed by TMA with the iterate instead of read per node.
-template <class T, int BY, int NS, bool FS = false>
+// VC: each stage also holds the coefficient fields C0 and CA of its plane
+// (two more 32 x BY boxes), for the variable-coefficient update.
+template <class T, int BY, int NS, bool FS = false, bool VC = false>
 struct Tile {
     static constexpr int ESZ = (int)sizeof(T);
     static constexpr int LP = 16 / ESZ;          // left halo padded to 16 bytes
@@ -33,8 +35,12 @@ struct Tile {
     static constexpr int H = BY + 2;             // box height (rows)
     static constexpr uint32_t TX_BYTES = W * H * ESZ;
     static constexpr int USTRIDE = ((W * H * ESZ + 127) / 128) * 128 / ESZ;  // iterate box, elements
-    static constexpr uint32_t F_BYTES = FS ? BX * BY * ESZ : 0;
-    static constexpr int STRIDE = USTRIDE + (FS ? ((BX * BY * ESZ + 127) / 128) * 128 / ESZ : 0);
+    static constexpr int XSTRIDE = ((BX * BY * ESZ + 127) / 128) * 128 / ESZ;  // one extra box, elements
+    static constexpr int NXB = (FS ? 1 : 0) + (VC ? 2 : 0);  // extra boxes per stage
+    static constexpr uint32_t X_BYTES = NXB * BX * BY * ESZ;
+    static constexpr int C0OFF = USTRIDE + (FS ? XSTRIDE : 0);  // C0 box inside a stage
+    static constexpr int CAOFF = C0OFF + XSTRIDE;                // CA box
+    static constexpr int STRIDE = USTRIDE + NXB * XSTRIDE;
     static constexpr size_t SMEM = (size_t)NS * STRIDE * ESZ + NS * sizeof(uint64_t);
 };
 
@@ -61,7 +67,28 @@ struct TileJob {
     Layout L;
     Split time_old, time_new, corr;  // time(t), time(t+1), mirror correction
     const BorderTable* table;  // border rules (SCAFES_BORDER_TABLE)
+    const CUtensorMap* tmc0 = nullptr;  // TMA descriptors of C0, CA (box 32 x BY), VC tiles only
+    const CUtensorMap* tmca = nullptr;
+    const scafes_border_node_rule* nodes = nullptr;  // per-node rules (SCAFES_BORDER_NODES)
 };
+
+// The rule of one border node of a SCAFES_BORDER_NODES problem, in FP64
+// whatever the element type: u_new = cu*u + sum_d cn[d]*u_d + cst.
+template <class P>
+__device__ __noinline__ typename P::T node_rule(const TileJob<typename P::T>& J, int x, int y, int z,
+                                                 typename P::T u, typename P::T w, typename P::T e,
+                                                 typename P::T s, typename P::T n, typename P::T b,
+                                                 typename P::T t) {
+    const scafes_border_node_rule& R = J.nodes[border_node_index(J.L, x, y, z)];
+    double v = fma(R.cu, P::to_double(u), R.cst);
+    v = fma(R.cn[0], P::to_double(w), v);
+    v = fma(R.cn[1], P::to_double(e), v);
+    v = fma(R.cn[2], P::to_double(s), v);
+    v = fma(R.cn[3], P::to_double(n), v);
+    v = fma(R.cn[4], P::to_double(b), v);
+    v = fma(R.cn[5], P::to_double(t), v);
+    return P::from_double(v);
+}
 
 // The table rule of a border node, in FP64 whatever the element type (border
 // nodes are a thin layer; the rule needs the reference's rounding, not
@@ -128,16 +155,18 @@ enum : int { SRC_NONE = 0, SRC_A = 1, SRC_AB = 2 };
 // and phase of every plane); it is advanced by the planes this tile used.
 // Returns false (and records SCAFES_ERR_TIMEOUT) when a stage never
 // arrived; the caller must then stop.
-template <class P, int SRC, int BORDER, int BY, int R, int NS, bool FS, bool ML = false>
+template <class P, int SRC, int BORDER, int BY, int R, int NS, bool FS, bool ML = false, bool VC = false>
 __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, const Star7Coeffs& c,
                                            int x0, int y0, int z0, int z1,
                                            typename P::T* st, uint64_t* bar, uint32_t& base,
                                            int* status) {
     using T = typename P::T;
-    using G = Tile<T, BY, NS, FS>;
+    using G = Tile<T, BY, NS, FS, VC>;
     constexpr bool HAS_F = SRC != SRC_NONE;
     constexpr bool has_fb = SRC == SRC_AB;
     static_assert(!FS || SRC == SRC_A, "only F_A is staged");
+    static_assert(!VC || SRC != SRC_AB, "the variable-coefficient update takes a static source");
+    static_assert(BORDER != SCAFES_BORDER_NODES || VC, "per-node border rules come with variable coefficients");
     const Layout& L = J.L;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * BX + tx;
@@ -151,10 +180,14 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
     // computed (1 <= q <= np - 2) bring their F_A box along.
     auto issue = [&](int q) {
         const uint32_t s = (b0 + (uint32_t)q) & (NS - 1);
-        const bool wf = FS && q >= 1 && q <= np - 2;
-        mbar_arrive_expect_tx(&bar[s], G::TX_BYTES + (wf ? G::F_BYTES : 0u));
+        const bool wx = G::NXB > 0 && q >= 1 && q <= np - 2;
+        mbar_arrive_expect_tx(&bar[s], G::TX_BYTES + (wx ? G::X_BYTES : 0u));
         tma_load_3d(st + s * G::STRIDE, J.tm, x0 - G::LP, y0 - 1, z0 - 1 + q, &bar[s]);
-        if (wf) tma_load_3d(st + s * G::STRIDE + G::USTRIDE, J.tmf, x0, y0, z0 - 1 + q, &bar[s]);
+        if (wx && FS) tma_load_3d(st + s * G::STRIDE + G::USTRIDE, J.tmf, x0, y0, z0 - 1 + q, &bar[s]);
+        if (wx && VC) {
+            tma_load_3d(st + s * G::STRIDE + G::C0OFF, J.tmc0, x0, y0, z0 - 1 + q, &bar[s]);
+            tma_load_3d(st + s * G::STRIDE + G::CAOFF, J.tmca, x0, y0, z0 - 1 + q, &bar[s]);
+        }
     };
     if (tid == 0) {
         const int pre = np < NS ? np : NS;
@@ -221,7 +254,17 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 else if (HAS_F && live)
                     f[k] = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
             }
-            P::template star_rows<HAS_F, R>(c, below, cur, above, ym, yp, w, e, f, v);
+            if constexpr (VC) {
+                const T* c0b = st + slot(p) * G::STRIDE + G::C0OFF + ty * R * BX + tx;
+                const T* cab = st + slot(p) * G::STRIDE + G::CAOFF + ty * R * BX + tx;
+#pragma unroll
+                for (int k = 0; k < R; ++k)
+                    v[k] = P::template star_vc<HAS_F>(c, cur[k], w[k], e[k], k == 0 ? ym : cur[k - 1],
+                                                      k == R - 1 ? yp : cur[k + 1], below[k], above[k], f[k],
+                                                      c0b[k * BX], cab[k * BX]);
+            } else {
+                P::template star_rows<HAS_F, R>(c, below, cur, above, ym, yp, w, e, f, v);
+            }
 #pragma unroll
             for (int k = 0; k < R; ++k) {
                 const long long off = o0 + (long long)k * L.pitch;
@@ -230,7 +273,9 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 if (!INNER && live && (xb || y < nl || y > L.ny - 1 - nl)) {
                     const T s = (k == 0) ? ym : cur[k - 1];
                     const T n = (k == R - 1) ? yp : cur[k + 1];
-                    if (BORDER == SCAFES_BORDER_TABLE) {
+                    if (BORDER == SCAFES_BORDER_NODES) {
+                        v[k] = node_rule<P>(J, x, y, z, cur[k], w[k], e[k], s, n, below[k], above[k]);
+                    } else if (BORDER == SCAFES_BORDER_TABLE) {
                         const int mask = (x == 0) | ((x == L.nx - 1) << 1) | ((y == 0) << 2) |
                                          ((y == L.ny - 1) << 3);
                         v[k] = table_rule<P, HAS_F, has_fb>(J, mask, off, cur[k], w[k], e[k], s, n, below[k],
@@ -272,7 +317,16 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                     if (!border) {
                         T f = P::zero();
                         if (HAS_F) f = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
-                        v = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
+                        if constexpr (VC) {
+                            const int bo = (ty * R + k) * BX + tx;
+                            v = P::template star_vc<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f,
+                                                           st[slot(p) * G::STRIDE + G::C0OFF + bo],
+                                                           st[slot(p) * G::STRIDE + G::CAOFF + bo]);
+                        } else {
+                            v = P::template star<HAS_F>(c, cur[k], w, e, s, n, below[k], above[k], f);
+                        }
+                    } else if (BORDER == SCAFES_BORDER_NODES) {
+                        v = node_rule<P>(J, x, y, z, cur[k], w, e, s, n, below[k], above[k]);
                     } else if (BORDER == SCAFES_BORDER_TABLE) {
                         const int mask = (x == 0) | ((x == L.nx - 1) << 1) | ((y == 0) << 2) |
                                          ((y == L.ny - 1) << 3) | ((z == 0) << 4) | ((z == L.nz - 1) << 5);

@@ -53,7 +53,7 @@ cudaError_t launch_star7_tb_f32(const Star7Launch& a, cudaStream_t stream);
 cudaError_t launch_star7_tb_f32x2(const Star7Launch& a, cudaStream_t stream);
 
 bool star7_tb_eligible(const Star7Launch& a) {
-    return a.border == SCAFES_BORDER_DIRICHLET && a.L.nl == 1 && a.fb == nullptr;
+    return a.border == SCAFES_BORDER_DIRICHLET && a.L.nl == 1 && a.fb == nullptr && !a.vc;
 }
 
 void star7_tb_box(int precision, int* width, int* rows) {

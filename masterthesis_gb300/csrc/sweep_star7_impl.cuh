@@ -34,6 +34,35 @@ star7_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtens
     star7_tile<P, SRC, BORDER, BY, R, NS, FS, ML>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
 }
 
+// The variable-coefficient sweep: as star7_tma, with the coefficient fields
+// C0 and CA staged by TMA with every plane (and F_A with them when the
+// source is present), and the Dirichlet, table or per-node border.
+template <class P, int SRC, int BORDER, int BY, int R, int NS>
+__global__ void __launch_bounds__(BX * (BY / R))
+star7_vc_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmf,
+             const __grid_constant__ CUtensorMap tmc0, const __grid_constant__ CUtensorMap tmca,
+             typename P::T* __restrict__ un, const typename P::T* __restrict__ fa,
+             const typename P::T* __restrict__ ga, typename P::T gval, Layout L, Star7Coeffs c, Split time_old,
+             Split time_new, const BorderTable* __restrict__ table,
+             const scafes_border_node_rule* __restrict__ nodes, int zchunk, int* __restrict__ status)
+{
+    using T = typename P::T;
+    constexpr bool FS = SRC == SRC_A;
+    using G = Tile<T, BY, NS, FS, true>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    T* st = reinterpret_cast<T*>(smem_raw);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw + (size_t)NS * G::STRIDE * G::ESZ);
+    if (__syncthreads_or(threadIdx.x == 0 && threadIdx.y == 0 && *(volatile int*)status != 0)) return;
+    ring_init<NS>(bar);
+    TileJob<T> J{&tm, &tmf, un, fa, nullptr, ga, nullptr, gval, L, time_old, time_new, Split{0.0, 0.f, 0.f}, table,
+                 &tmc0, &tmca, nodes};
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(z0 + zchunk, L.nz);
+    uint32_t base = 0;
+    star7_tile<P, SRC, BORDER, BY, R, NS, FS, false, true>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st,
+                                                           bar, base, status);
+}
+
 // ---- host side ---------------------------------------------------------------
 
 static int num_sms() {
@@ -116,6 +145,74 @@ static cudaError_t launch_tile(const Star7Launch& a, cudaStream_t stream) {
     }
 }
 
+// Stages of the variable-coefficient ring: each stage holds up to three
+// extra boxes, so four stages keep shared memory within a few CTAs per SM.
+constexpr int kVcStages = 4;
+
+template <class P, int SRC, int BORDER, int BY, int R>
+static cudaError_t launch_vc_typed(const Star7Launch& a, cudaStream_t stream) {
+    using T = typename P::T;
+    constexpr bool FS = SRC == SRC_A;
+    constexpr int NS = kVcStages;
+    using G = Tile<T, BY, NS, FS, true>;
+    const Layout& L = a.L;
+    if ((FS && a.tm_f == nullptr) || a.tm_c0 == nullptr || a.tm_ca == nullptr) return cudaErrorInvalidValue;
+    auto kern = star7_vc_tma<P, SRC, BORDER, BY, R, NS>;
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::SMEM);
+        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        attr = true;
+    }
+    T gval;
+    to_elem(a.gconst, gval);
+    const int zchunk = choose_zchunk(L, BY);
+    dim3 block(BX, BY / R, 1);
+    dim3 grid((L.nx + BX - 1) / BX, (L.ny + BY - 1) / BY, (L.nz + zchunk - 1) / zchunk);
+    kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, FS ? *a.tm_f : *a.tm_uo, *a.tm_c0, *a.tm_ca, (T*)a.un,
+                                           (const T*)a.fa, (const T*)a.ga, gval, L, a.c, make_split(a.time_old),
+                                           make_split(a.time_new), a.table, a.nodes, zchunk, a.status);
+    return cudaGetLastError();
+}
+
+template <class P, int SRC, int BORDER>
+static cudaError_t launch_vc_tile(const Star7Launch& a, cudaStream_t stream) {
+    switch (a.tile) {
+        case 0: return launch_vc_typed<P, SRC, BORDER, kTiles[0].by, kTiles[0].r>(a, stream);
+        case 1: return launch_vc_typed<P, SRC, BORDER, kTiles[1].by, kTiles[1].r>(a, stream);
+        case 2: return launch_vc_typed<P, SRC, BORDER, kTiles[2].by, kTiles[2].r>(a, stream);
+        case 3: return launch_vc_typed<P, SRC, BORDER, kTiles[3].by, kTiles[3].r>(a, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <class P, int BORDER>
+static cudaError_t launch_vc_src(const Star7Launch& a, cudaStream_t stream) {
+    if (a.fb != nullptr) return cudaErrorInvalidValue;  // static source only
+    if (a.fa == nullptr || a.c.cf == 0.0) return launch_vc_tile<P, SRC_NONE, BORDER>(a, stream);
+    return launch_vc_tile<P, SRC_A, BORDER>(a, stream);
+}
+
+// The variable-coefficient family: FP64 and FP32, one border layer.
+template <class P>
+static cudaError_t launch_vc(const Star7Launch& a, cudaStream_t stream) {
+    if constexpr (std::is_same<P, PolF32x2>::value) {
+        return cudaErrorInvalidValue;
+    } else {
+        if (a.L.nl != 1) return cudaErrorInvalidValue;
+        switch (a.border) {
+            case SCAFES_BORDER_DIRICHLET: return launch_vc_src<P, SCAFES_BORDER_DIRICHLET>(a, stream);
+            case SCAFES_BORDER_TABLE:
+                if (a.table == nullptr) return cudaErrorInvalidValue;
+                return launch_vc_src<P, SCAFES_BORDER_TABLE>(a, stream);
+            case SCAFES_BORDER_NODES:
+                if (a.nodes == nullptr) return cudaErrorInvalidValue;
+                return launch_vc_src<P, SCAFES_BORDER_NODES>(a, stream);
+            default: return cudaErrorInvalidValue;
+        }
+    }
+}
+
 template <class P, int BORDER>
 static cudaError_t launch_src(const Star7Launch& a, cudaStream_t stream) {
     if (a.fa == nullptr || a.c.cf == 0.0) return launch_tile<P, SRC_NONE, BORDER>(a, stream);
@@ -165,6 +262,7 @@ cudaError_t launch_tb_prec(const Star7Launch& a, cudaStream_t stream) {
 
 template <class P>
 cudaError_t launch_prec(const Star7Launch& a, cudaStream_t stream) {
+    if (a.vc) return launch_vc<P>(a, stream);
     switch (a.border) {
         case SCAFES_BORDER_DIRICHLET: return launch_src<P, SCAFES_BORDER_DIRICHLET>(a, stream);
         case SCAFES_BORDER_MIRROR_POW2: return launch_src<P, SCAFES_BORDER_MIRROR_POW2>(a, stream);
