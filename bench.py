@@ -66,6 +66,10 @@ def parse_args():
     ap.add_argument("--mf-time-steps", type=int, default=100)
     ap.add_argument("--no-oracle-error", action="store_true",
                     help="skip the errors against the CPU oracle (each section states one by default)")
+    ap.add_argument("--temporal-depth", choices=["auto", "1", "2"], default="auto",
+                    help="temporal blocking depth of the plain sweep (auto: the autotuner's choice)")
+    ap.add_argument("--no-tissue", action="store_true")
+    ap.add_argument("--tissue-n", type=int, default=512)
     ap.add_argument("--ref-sweeps", type=int, default=10,
                     help="sweeps of the 512^3 field per step of the reference arm (even)")
     return ap.parse_args()
@@ -169,15 +173,20 @@ def pipe_peaks():
     return f64.value, f32.value
 
 
-def ncu_traffic(kernel_key: str):
-    """Per-launch DRAM bytes (read + write) of one ncu capture, from the
-    committed profile summary of that kernel."""
+def ncu_figure(name: str, kernel_key: str):
+    """One figure of an ncu capture (e.g. traffic_bytes_per_launch, the DRAM
+    bytes read + written per launch), from the committed profile summary of
+    that kernel."""
     for p in sorted((ROOT / "profiles").glob("*.md")):
         txt = p.read_text()
-        m = re.search(rf"traffic_bytes_per_launch\[{re.escape(kernel_key)}\]:\s*([0-9.eE+]+)", txt)
+        m = re.search(rf"{re.escape(name)}\[{re.escape(kernel_key)}\]:\s*([0-9.eE+]+)", txt)
         if m:
             return float(m.group(1))
     return None
+
+
+def ncu_traffic(kernel_key: str):
+    return ncu_figure("traffic_bytes_per_launch", kernel_key)
 
 
 # ---- GPU clock sampling during the timed region -----------------------------
@@ -586,6 +595,97 @@ def run_multifield(M, args, dist: Dist, hbm_peak: float):
     return out
 
 
+# ---- variable coefficients (the tissue examples' update) ----------------------
+
+TISSUE_LAST = (0.05, 0.04, 0.03)          # domain of the MRI-data example's golden case (m)
+TISSUE_FLUX = {"zmax_kind": 0, "q_bc": 5.0, "q_skull": -3.0}
+TISSUE_FP64_OPS = 8                       # 3 DADD, 1 DMUL, 4 DFMA per inner node
+
+
+def tissue_arrays(n: int, seed: int = 31):
+    """The MRI-data Pennes update on n^3 nodes of the 5 x 4 x 3 cm domain:
+    seeded coefficient fields over the nodes (workloads.tissue_fields_slab)
+    folded slab by slab into C0, CA and the source F, Neumann borders as
+    per-node rules.  Returns (C0, CA, F, rules, cp, tau)."""
+    from masterthesis_gb300 import workloads as W
+    nn = (n, n, n)
+    tau = W.tissue_tau(nn, TISSUE_LAST)
+    h = [TISSUE_LAST[p] / (n - 1) for p in range(3)]
+    C0, CA, F = (np.empty((n, n, n)) for _ in range(3))
+    rules = []
+    for z0 in range(0, n, 32):
+        z1 = min(n, z0 + 32)
+        d = W.tissue_device_form(nn, h, tau, W.tissue_fields_slab(nn, z0, z1, seed), z0, TISSUE_FLUX)
+        C0[z0:z1], CA[z0:z1], F[z0:z1] = d["C0"], d["CA"], d["F"]
+        rules.append(d["rules"])
+    return C0, CA, F, np.concatenate(rules), d["cp"], tau
+
+
+def tissue_problem(M, arrays, prec: str):
+    """An open Plain handle of the tissue problem (initial temperature 37)."""
+    C0, CA, F, rules, cp, tau = arrays
+    n = C0.shape[0]
+    cfg = M.make_cfg((n, n, n), last=TISSUE_LAST, tau=tau, precision=prec, border=M.BORDER_NODES, c0=0.0, cp=cp,
+                     cf=1.0)
+    p = M.Plain(cfg)
+    p.upload(M.FIELD_C0, C0)
+    p.upload(M.FIELD_CA, CA)
+    p.upload(M.FIELD_F_A, F)
+    p.set_border_node_rules(rules)
+    p.upload(M.FIELD_U, np.full((n, n, n), 37.0))
+    return p
+
+
+def run_tissue(M, args, dist: Dist, hbm_peak: float, fp64_peak):
+    """Variable-coefficient Pennes (the MRI-data example's update): 512^3,
+    eight seeded coefficient fields folded into C0, CA and the source F,
+    per-node Neumann border rules, 200 steps, FP64 and FP32.  Algorithmic
+    bytes per node update: the iterate read and written plus C0, CA, F read
+    (40 B FP64, 20 B FP32).  Error: the same construction at 96^3 x 100
+    steps against the oracle's restatement of the example."""
+    n, T = args.tissue_n, 200
+    out = {"workload": f"tissue Pennes (MRI-data example's update), {n}^3, coefficients per node (seed 31), "
+                       f"Neumann borders per node, {T} steps"}
+    arrays = tissue_arrays(n)
+    for prec, bpl in (("f64", 40), ("f32", 20)):
+        p = tissue_problem(M, arrays, prec)
+        try:
+            tile, _ = p.autotune(5)
+            p.step(T)  # warm-up
+            dist.barrier()
+            p.step(T)
+            ms = dist.max(p.last_step_ms())
+        finally:
+            p.close()
+        lup = float(n) ** 3 * T
+        g = dist.world * lup / (ms * 1e-3) / 1e9
+        out[prec] = {"value": g, "unit": UNIT, "hbm_frac": bpl * g / hbm_peak, "bytes_per_lup": bpl, "ms": ms,
+                     "tile": tile}
+        if prec == "f64" and fp64_peak:
+            out[prec]["fp64_pipe_frac"] = TISSUE_FP64_OPS * g / fp64_peak
+    if not args.no_oracle_error and dist.rank == 0:
+        import oracle as O
+        from masterthesis_gb300 import workloads as W
+        m, Te = 96, 100
+        nn = (m, m, m)
+        f = W.tissue_fields_slab(nn, 0, m, 31)
+        tau = W.tissue_tau(nn, TISSUE_LAST)
+        g = O.make_grid(nn, last=TISSUE_LAST, tau=tau)
+        ref = O.pennes_tissue(g, np.full((m, m, m), 37.0), Te, f, zmax_kind=0, q_bc=TISSUE_FLUX["q_bc"],
+                              q_skull=TISSUE_FLUX["q_skull"], nthreads=os.cpu_count() or 1)
+        small = tissue_arrays(m)
+        for prec in ("f64", "f32"):
+            p = tissue_problem(M, small, prec)
+            try:
+                p.step(Te)
+                out[prec]["error_vs_oracle"] = {"max_rel": rel_err(p.download(), ref),
+                                                "sample": f"{m}^3 x {Te} steps, same construction"}
+            finally:
+                p.close()
+    del arrays
+    return out
+
+
 # ---- GPU arm ----------------------------------------------------------------
 
 def run_ours(args, dist: Dist):
@@ -613,7 +713,10 @@ def run_ours(args, dist: Dist):
         with M.Plain(cfg) as p:
             p.upload(M.FIELD_U, u0)
             # picks the sweep's CTA tile variant and the temporal blocking depth
-            tuned[prec] = p.autotune(10) + (p.temporal_depth,)
+            tile_ms = p.autotune(10)
+            if args.temporal_depth != "auto":
+                p.set_temporal_depth(int(args.temporal_depth))
+            tuned[prec] = tile_ms + (p.temporal_depth,)
             for _ in range(warmup):
                 p.step(T)
             stream.synchronize()
@@ -643,7 +746,8 @@ def run_ours(args, dist: Dist):
     achieved_gbs = B_PER_LUP["f64"] * nn / launch_s / 1e9
     # DRAM bytes per launch from the committed ncu summary of this kernel at
     # this grid size (null when no capture of this size exists).
-    traffic = ncu_traffic(f"star7_tma<PolF64>@{args.n}")
+    key = f"star7_tma<PolF64>@{args.n}"
+    traffic = ncu_traffic(key)
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic,
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
@@ -655,6 +759,9 @@ def run_ours(args, dist: Dist):
         roofline["fp64_pipe"] = {"achieved_gops": ach, "peak_gops": fp64_peak, "frac": ach / fp64_peak,
                                  "ops_per_lup": FP64_OPS_PER_LUP, "fp32_fma_gops": fp32_peak,
                                  "peak_source": "measured live (scafes_probe_pipe_rates)",
+                                 "ncu": {"fp64_ops_per_lup": ncu_figure("fp64_ops_per_lup", key),
+                                         "fp64_pipe_active": ncu_figure("fp64_pipe_active", key),
+                                         "source": "profiles/star7_f64_heat512.md"},
                                  "note": "the FP64 issue rate, not HBM, binds this kernel on GB300"}
 
     # e2e through the C ABI with host buffers.
@@ -705,6 +812,7 @@ def run_ours(args, dist: Dist):
         for prec in ("f32x2", "f32"):
             variants[prec]["rel_err_vs_f64"] = rel_err(finals[prec], finals["f64"])
 
+    tissue = None if args.no_tissue else run_tissue(M, args, dist, hbm_peak, fp64_peak)
     batched = None if args.no_batched else run_batched(M, args, dist, hbm_peak)
     adjoint = None if args.no_adjoint else run_adjoint(M, args, dist)
     multifield = None if args.no_multifield else run_multifield(M, args, dist, hbm_peak)
@@ -743,6 +851,8 @@ def run_ours(args, dist: Dist):
             variants[prec]["rel_err_vs_oracle"] = error[f"{prec}_vs_oracle"]
     if variants:
         res["variants"] = variants
+    if tissue:
+        res["tissue"] = tissue
     if batched:
         res["batched"] = batched
     if adjoint:

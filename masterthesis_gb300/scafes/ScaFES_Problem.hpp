@@ -68,7 +68,7 @@ public:
         : mParams(params), mGG(gg), mUseLeapfrog(useLeapfrog), mNames(nameDatafield),
           mStencilWidth(stencilWidth), mIsKnown(isKnownDf), mComputeError(computeError),
           mVectParamsCurr(geomparamsInit), mWriteToFile(writeToFile) {
-        (void)nLayers; (void)defaultValue; (void)checkConvergence;
+        (void)nLayers; (void)checkConvergence;
         // Argument checks of the reference constructor (:1400-1423).
         const std::size_t nf = nameDatafield.size();
         if (nf == 0 || stencilWidth.size() != nf || isKnownDf.size() != nf)
@@ -90,6 +90,15 @@ public:
         for (std::size_t f = 0; f < nf; ++f) {
             mVectKnownDfsDomNew.emplace_back(nameDatafield[f], &mGG, mKnownNewStore.data() + f * mN, stencilWidth[f]);
             mVectKnownDfsDomOld.emplace_back(nameDatafield[f], &mGG, mKnownOldStore.data() + f * mN, stencilWidth[f]);
+        }
+        // Each unknown field starts at its default value, which the init
+        // callbacks then overwrite where they write (the reference resets
+        // the unknown fields to defaultValue before evalInitPbPhase,
+        // src/ScaFES_Problem.hpp:2999-3027, 2623).
+        for (std::size_t u = 0; u < nu; ++u) {
+            const int f = mUnknownIdx[u];
+            if ((std::size_t)f < defaultValue.size())
+                std::fill(mUnknownNewStore.begin() + u * mN, mUnknownNewStore.begin() + (u + 1) * mN, defaultValue[f]);
         }
         for (std::size_t u = 0; u < nu; ++u) {
             const int f = mUnknownIdx[u];
@@ -143,6 +152,42 @@ public:
     const std::string& deviceForm() {
         prepareDevice();
         return mSummary;
+    }
+
+    // Runs the same host part and writes everything the device run would
+    // receive -- the configuration, the border rules and every field it
+    // uploads except the initial iterate -- to `path` as named FP64
+    // arrays (16-byte name, int64 count, values).  Two problem classes
+    // whose files are equal byte for byte run the same device computation.
+    void dumpDeviceForm(const std::string& path) {
+        prepareDevice();
+        FILE* f = std::fopen(path.c_str(), "wb");
+        if (!f) throw std::runtime_error("ScaFES::Problem: cannot write " + path);
+        auto put = [&](const char* name, const double* v, long long n) {
+            char tag[16] = {};
+            std::strncpy(tag, name, sizeof(tag) - 1);
+            std::fwrite(tag, 1, sizeof(tag), f);
+            std::fwrite(&n, sizeof(n), 1, f);
+            if (n > 0) std::fwrite(v, sizeof(double), (std::size_t)n, f);
+        };
+        const scafes_cfg& c = mCfg;
+        const double cfgv[] = {(double)c.n_nodes[0], (double)c.n_nodes[1], (double)c.n_nodes[2],
+                               c.coord_first[0], c.coord_first[1], c.coord_first[2],
+                               c.coord_last[0], c.coord_last[1], c.coord_last[2], c.tau, c.t_start,
+                               (double)c.n_layers_at_border, (double)c.precision, (double)c.border,
+                               c.c0, c.cp[0], c.cp[1], c.cp[2], c.cf, mGcenter, mGrate, mGpoly ? 1.0 : 0.0};
+        put("cfg", cfgv, (long long)(sizeof(cfgv) / sizeof(double)));
+        if (c.border == SCAFES_BORDER_TABLE)
+            put("forms", &mForms[0].cu, (long long)(sizeof(mForms) / sizeof(double)));
+        put("F_A", mFa.data(), (long long)mFa.size());
+        put("F_B", mFb.data(), (long long)mFb.size());
+        put("G_A", mGa.data(), (long long)mGa.size());
+        put("G_B", mGb.data(), (long long)mGb.size());
+        for (int k = 0; k < 3; ++k) put(k == 0 ? "G_C" : k == 1 ? "G_D" : "G_E", mGhi[k].data(), (long long)mGhi[k].size());
+        put("C0", mC0.data(), (long long)mC0.size());
+        put("CA", mCA.data(), (long long)mCA.size());
+        put("node_rules", mNodeRules.empty() ? nullptr : &mNodeRules[0].cu, (long long)mNodeRules.size() * 8);
+        if (std::fclose(f) != 0) throw std::runtime_error("ScaFES::Problem: cannot write " + path);
     }
 
 protected:
@@ -209,11 +254,14 @@ private:
         }
         OWNPRBLM* self = static_cast<OWNPRBLM*>(this);
         gpu::comparison_on_unknown() = false;
+        gpu::converted_unknown() = false;
         if (BORDER) self->template updateBorder<gpu::Sym>(vNew, vOld, n, t);
         else self->template updateInner<gpu::Sym>(vNew, vOld, n, t);
         err = rec.error;
         if (err.empty() && gpu::comparison_on_unknown())
             err = "update callback branches on the value of an unknown (not a linear stencil)";
+        if (err.empty() && gpu::converted_unknown())
+            err = "update callback turns an unknown into a number (not a linear stencil)";
         return rec.out;
     }
 
@@ -316,6 +364,35 @@ private:
             else if (ratio != cf) return "source terms that are not a multiple of the inner source";
         }
         r.cf = cf;
+        return std::string();
+    }
+
+    // The rule of one border node alone (SCAFES_BORDER_NODES):
+    //   u_new = cu*u + sum_d cn[d]*u_d + cst,
+    // known fields folded into cst with their value at the node (so they must
+    // not change in time), or why there is none.
+    std::string nodeRule(const gpu::Sym& s1, const gpu::Sym& s2, const std::vector<Affine>& aff, long long m,
+                         scafes_border_node_rule& r) const {
+        if (!same(s1, s2)) return "the rule changes between time steps";
+        r.cst = s1.constant();
+        for (const auto& kv : s1.terms()) {
+            const auto& k = kv.first;
+            if (k.kind == 2) return "a power of the node's unknown";
+            if (k.kind == 0) {
+                if (k.a != 0) return "several unknown fields";
+                const int nz = (k.b != 0) + (k.c != 0) + (k.d != 0);
+                const int mag = std::abs(k.b) + std::abs(k.c) + std::abs(k.d);
+                if (nz == 0) { r.cu += kv.second; continue; }
+                if (nz != 1 || mag != 1) return "a neighbour beyond the 7-point star";
+                const int p = k.b ? 0 : (k.c ? 1 : 2);
+                r.cn[2 * p + ((k.b + k.c + k.d) > 0 ? 1 : 0)] += kv.second;
+                continue;
+            }
+            const Affine& A = aff[k.a];
+            if (A.zero) continue;
+            if (A.a.empty() || A.timed) return "a known field that changes in time";
+            r.cst += kv.second * A.a[m];
+        }
         return std::string();
     }
 
@@ -432,6 +509,8 @@ private:
     bool mPrepared = false;
     scafes_cfg mCfg = {};
     std::vector<double> mFa, mFb, mGa, mGb;
+    std::vector<double> mC0, mCA;                      // coefficient slots (variable coefficients)
+    std::vector<scafes_border_node_rule> mNodeRules;   // per-node border rules
     std::vector<double> mGhi[3];       // G_C .. G_E of a polynomial-in-time border field
     bool mGpoly = false;
     double mGcenter = 0.0, mGrate = 1.0;
@@ -524,6 +603,7 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     auto t_rec = clock::now();
     std::copy(k1.begin(), k1.end(), mKnownNewStore.begin());
     std::string err;
+    // Probe nodes: the inner form must not change between time steps.
     std::vector<ScaFES_IntNtuple> probes;
     {
         ScaFES_IntNtuple lo(1), hi, mid;
@@ -541,34 +621,127 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
             probes.push_back(r);
         }
     }
-    gpu::Sym inner;
-    bool first = true;
-    for (int t = 1; t <= 2; ++t) {
-        for (const auto& n : probes) {
+    for (const auto& n : probes) {
+        if (isBorder(n)) continue;
+        gpu::Sym s1 = record<false>(n, 1, err)[0];
+        if (!err.empty()) throw std::runtime_error("ScaFES::Problem: " + err);
+        gpu::Sym s2 = record<false>(n, 2, err)[0];
+        if (!err.empty()) throw std::runtime_error("ScaFES::Problem: " + err);
+        if (!same(s1, s2))
+            throw std::runtime_error("ScaFES::Problem: updateInner changes between time steps: " + describe(s1) +
+                                     " vs " + describe(s2));
+    }
+
+    // Every inner node at step 1: its 7-point star, and its source
+    // F(t_old) = cst + sum_j b_j K_j as F_A + time * F_B.  When every node
+    // has the same star the device runs the constant-coefficient sweep; when
+    // the coefficients change from node to node (coefficients read from
+    // known fields or from the node's coordinates, as in the reference's
+    // tissue examples) it runs the variable-coefficient sweep with the
+    // per-node centre weight C0 and axis scale CA.
+    std::vector<double> fa((std::size_t)mN, 0.0), fb;
+    std::vector<double> c0n((std::size_t)mN, 0.0), cpn[3];
+    for (int p = 0; p < 3; ++p) cpn[p].assign((std::size_t)mN, 0.0);
+    bool any_timed = false;
+    for (std::size_t f = 0; f < nf; ++f) any_timed = any_timed || (mIsKnown[f] && aff[f].timed);
+    if (any_timed) fb.assign((std::size_t)mN, 0.0);
+    Form F0;
+    bool have_first = false, uniform = true, has_f = false, has_fb = false;
+    std::string inner_err;
+    {
+        // The first inner node's form is the reference the others compare with.
+        for (long long m = 0; m < mN && !have_first; ++m) {
+            const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
             if (isBorder(n)) continue;
-            gpu::Sym s = record<false>(n, t, err)[0];
+            gpu::Sym s = record<false>(n, 1, err)[0];
             if (!err.empty()) throw std::runtime_error("ScaFES::Problem: " + err);
-            if (first) { inner = s; first = false; }
-            else if (!same(s, inner))
-                throw std::runtime_error("ScaFES::Problem: updateInner differs between nodes or time steps "
-                                         "(variable coefficients are not mapped to a device kernel): " +
-                                         describe(inner) + " vs " + describe(s));
+            F0 = starForm(s);
+            have_first = true;
+        }
+        if (!have_first) throw std::runtime_error("ScaFES::Problem: the grid has no inner nodes");
+    }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) reduction(&& : uniform) reduction(|| : has_f, has_fb)
+#endif
+    for (long long m = 0; m < mN; ++m) {
+        const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
+        if (isBorder(n)) continue;
+        std::string e;
+        Form F;
+        try {
+            gpu::Sym s = record<false>(n, 1, e)[0];
+            if (e.empty()) F = starForm(s);
+        } catch (const std::exception& x) {
+            e = x.what();
+        }
+        if (e.empty()) {
+            bool same_form = F.c0 == F0.c0 && F.cst == F0.cst && F.known.size() == F0.known.size();
+            for (int p = 0; p < 3; ++p) same_form = same_form && F.cp[p] == F0.cp[p];
+            c0n[m] = F.c0;
+            for (int p = 0; p < 3; ++p) cpn[p][m] = F.cp[p];
+            double va = F.cst, vb = 0.0;
+            if (F.cst != 0.0) has_f = true;
+            for (const auto& kv : F.known) {
+                const auto it = F0.known.find(kv.first);
+                same_form = same_form && it != F0.known.end() && it->second == kv.second;
+                const int j = kv.first.first;
+                const Affine& A = aff[j];
+                if (A.zero) continue;
+                if (A.a.empty()) {
+                    e = "known field " + mNames[j] + " is not affine in time; the device path takes affine known fields";
+                    break;
+                }
+                has_f = true;
+                const bool is_new = kv.first.second == 0;
+                va += kv.second * (A.a[m] + (is_new ? mParams.tau() * A.b[m] : 0.0));
+                if (A.timed) {
+                    vb += kv.second * A.b[m];
+                    has_fb = true;
+                }
+            }
+            fa[m] = va;
+            if (!fb.empty()) fb[m] = vb;
+            uniform = uniform && same_form;
+        }
+        if (!e.empty()) {
+#ifdef _OPENMP
+#pragma omp critical(scafes_inner_error)
+#endif
+            if (inner_err.empty()) inner_err = e;
         }
     }
-    if (first) throw std::runtime_error("ScaFES::Problem: the grid has no inner nodes");
-    Form F = starForm(inner);
+    if (!inner_err.empty()) throw std::runtime_error("ScaFES::Problem: " + inner_err);
+    // Border rules of the table kind read the inner source at border nodes:
+    // with one inner form, its source is defined there as well.
+    if (uniform) {
+        for (long long m = 0; m < mN; ++m) {
+            if (!isBorder(g.idxNodeScalar2TupleStyleFortran(m))) continue;
+            double va = F0.cst, vb = 0.0;
+            for (const auto& kv : F0.known) {
+                const Affine& A = aff[kv.first.first];
+                if (A.zero || A.a.empty()) continue;
+                va += kv.second * (A.a[m] + (kv.first.second == 0 ? mParams.tau() * A.b[m] : 0.0));
+                if (A.timed) vb += kv.second * A.b[m];
+            }
+            fa[m] = va;
+            if (!fb.empty()) fb[m] = vb;
+        }
+    }
 
-    // Border: every global-border node, at steps 1 and 2.  Three device
+    // Border: every global-border node, at steps 1 and 2.  Four device
     // forms are tried at once: Dirichlet from one known field, the
-    // StencilWidthOne mirror rule, and a table of one linear rule per border
+    // StencilWidthOne mirror rule, a table of one linear rule per border
     // class (the set of faces the node lies on) -- the reference's Neumann
-    // and Cauchy borders.
+    // and Cauchy borders -- and one linear rule per border node (borders
+    // whose coefficients change from node to node, such as the flux faces
+    // of the tissue examples).
     int gfield = -1, gwhen = 0;
-    bool dir_ok = true, mir_ok = true, tab_ok = true;
-    std::string tab_why;
+    bool dir_ok = true, mir_ok = true, tab_ok = true, nodes_ok = true;
+    std::string tab_why, nodes_why;
     scafes_border_form forms[SCAFES_BORDER_CLASSES] = {};
     bool seen[SCAFES_BORDER_CLASSES] = {};
     int tab_g = -1;  // the one known field the table rules read as G
+    std::vector<scafes_border_node_rule> node_rules;
     for (long long m = 0; m < mN; ++m) {
         const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
         if (!isBorder(n)) continue;
@@ -590,38 +763,50 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
             for (const auto& kv : tt)
                 if (kv.first.kind != 0 || kv.second != 1.0) mirror = false;
         mir_ok = mir_ok && mirror;
-        if (!tab_ok) {
-            if (!dir_ok && !mir_ok)
-                throw std::runtime_error("ScaFES::Problem: updateBorder at node has no device form (" + tab_why +
-                                         "): " + describe(s1));
-            continue;
+        // The rule of this node alone.
+        if (nodes_ok) {
+            scafes_border_node_rule r = {};
+            std::string why = nodeRule(s1, s2, aff, m, r);
+            if (!why.empty()) {
+                nodes_ok = false;
+                nodes_why = why;
+                node_rules.clear();
+            } else {
+                node_rules.push_back(r);
+            }
         }
-        // Table rule of this node's class.
-        int mask = 0;
-        for (std::size_t p = 0; p < DIM; ++p) {
-            if (n[p] == g.idxNodeFirst(p)) mask |= 1 << (2 * p);
-            if (n[p] == g.idxNodeLast(p)) mask |= 1 << (2 * p + 1);
+        if (tab_ok) {
+            // Table rule of this node's class.
+            int mask = 0;
+            for (std::size_t p = 0; p < DIM; ++p) {
+                if (n[p] == g.idxNodeFirst(p)) mask |= 1 << (2 * p);
+                if (n[p] == g.idxNodeLast(p)) mask |= 1 << (2 * p + 1);
+            }
+            scafes_border_form r = {};
+            std::string why = uniform ? tableRule(s1, s2, F0, aff, tab_g, r)
+                                      : std::string("the inner update has variable coefficients");
+            if (why.empty() && seen[mask] && std::memcmp(&r, &forms[mask], sizeof(r)) != 0)
+                why = "the rule differs between nodes on the same faces";
+            if (!why.empty()) {
+                tab_ok = false;
+                tab_why = why;
+            } else {
+                forms[mask] = r;
+                seen[mask] = true;
+            }
         }
-        scafes_border_form r = {};
-        std::string why = tableRule(s1, s2, F, aff, tab_g, r);
-        if (why.empty() && seen[mask] && std::memcmp(&r, &forms[mask], sizeof(r)) != 0)
-            why = "the rule differs between nodes on the same faces";
-        if (!why.empty()) {
-            tab_ok = false;
-            tab_why = why;
-            if (!dir_ok && !mir_ok)
-                throw std::runtime_error("ScaFES::Problem: updateBorder at node has no device form (" + why + "): " +
-                                         describe(s1));
-            continue;
-        }
-        forms[mask] = r;
-        seen[mask] = true;
+        if (!dir_ok && !mir_ok && !tab_ok && !nodes_ok)
+            throw std::runtime_error("ScaFES::Problem: updateBorder at node has no device form (" + tab_why + "; " +
+                                     nodes_why + "): " + describe(s1));
     }
-    int border = dir_ok ? SCAFES_BORDER_DIRICHLET : mir_ok ? SCAFES_BORDER_MIRROR_POW2 : SCAFES_BORDER_TABLE;
+    int border = dir_ok ? SCAFES_BORDER_DIRICHLET
+                 : mir_ok ? SCAFES_BORDER_MIRROR_POW2
+                 : tab_ok ? SCAFES_BORDER_TABLE : SCAFES_BORDER_NODES;
     if (border == SCAFES_BORDER_TABLE) std::copy(forms, forms + SCAFES_BORDER_CLASSES, mForms);
+    if (border == SCAFES_BORDER_NODES) mNodeRules.swap(node_rules);
     mWallClockTimes["record"] += std::chrono::duration<double>(clock::now() - t_rec).count();
 
-    // 4. Device run.
+    // 4. Device configuration.
     scafes_cfg cfg = {};
     cfg.dim = 3;
     for (int p = 0; p < 3; ++p) {
@@ -635,27 +820,43 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     cfg.precision = precisionCode();
     cfg.border = border;
     cfg.tile = mParams.gpuTile();
-    cfg.c0 = F.c0;
-    for (int p = 0; p < 3; ++p) cfg.cp[p] = F.cp[p];
-    // Source: F(t_old) = cst + sum_j b_j K_j(t_old or t_new).
-    std::vector<double> fa((std::size_t)mN, F.cst), fb;
-    bool has_f = F.cst != 0.0, has_fb = false;
-    for (const auto& kv : F.known) {
-        const int j = kv.first.first;
-        const bool is_new = kv.first.second == 0;
-        const double bj = kv.second;
-        const Affine& A = aff[j];
-        if (A.zero) continue;
-        if (A.a.empty())
-            throw std::runtime_error("ScaFES::Problem: known field " + mNames[j] +
-                                     " is not affine in time; the device path takes affine known fields");
-        has_f = true;
-        if (A.timed && fb.empty()) fb.assign((std::size_t)mN, 0.0);
+    const bool vc = !uniform || border == SCAFES_BORDER_NODES;
+    if (!vc) {
+        cfg.c0 = F0.c0;
+        for (int p = 0; p < 3; ++p) cfg.cp[p] = F0.cp[p];
+    } else {
+        if (border == SCAFES_BORDER_MIRROR_POW2)
+            throw std::runtime_error("ScaFES::Problem: variable coefficients with the mirror border have no device form");
+        if (has_fb)
+            throw std::runtime_error("ScaFES::Problem: variable coefficients take a source constant in time; "
+                                     "a known field of the source changes with time");
+        if (cfg.precision == SCAFES_PREC_F32X2)
+            throw std::runtime_error("ScaFES::Problem: variable coefficients run with --gpuPrecision f64 or f32");
+        // C0 = the node's centre weight, CA = its x-axis weight; the axis
+        // factors cp[p] are the ratios of the axis weights, which must be
+        // the same at every inner node (to rounding).
+        const long long m0 = [&] {
+            for (long long m = 0; m < mN; ++m)
+                if (!isBorder(g.idxNodeScalar2TupleStyleFortran(m)) && cpn[0][m] != 0.0) return m;
+            return -1LL;
+        }();
+        double kappa[3] = {1.0, 0.0, 0.0};
+        if (m0 >= 0)
+            for (int p = 1; p < 3; ++p) kappa[p] = cpn[p][m0] / cpn[0][m0];
+        mC0.assign((std::size_t)mN, 0.0);
+        mCA.assign((std::size_t)mN, 0.0);
         for (long long m = 0; m < mN; ++m) {
-            fa[m] += bj * (A.a[m] + (is_new ? mParams.tau() * A.b[m] : 0.0));
-            if (A.timed) fb[m] += bj * A.b[m];
+            if (isBorder(g.idxNodeScalar2TupleStyleFortran(m))) continue;
+            const double ca = cpn[0][m];
+            for (int p = 1; p < 3; ++p)
+                if (std::fabs(ca * kappa[p] - cpn[p][m]) > 1e-13 * std::fabs(cpn[p][m]))
+                    throw std::runtime_error("ScaFES::Problem: the axis weights of updateInner do not share one "
+                                             "ratio over the nodes (anisotropic coefficients have no device form)");
+            mC0[m] = c0n[m];
+            mCA[m] = ca;
         }
-        has_fb = has_fb || A.timed;
+        cfg.c0 = 0.0;
+        for (int p = 0; p < 3; ++p) cfg.cp[p] = kappa[p];
     }
     cfg.cf = has_f ? 1.0 : 0.0;
     if (has_f) mFa.swap(fa);
@@ -685,10 +886,14 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     }
     mCfg = cfg;
     std::ostringstream os;
-    os << "star7 c0=" << cfg.c0 << " cp=(" << cfg.cp[0] << "," << cfg.cp[1] << "," << cfg.cp[2] << ")"
-       << " source=" << (has_f ? (has_fb ? "affine" : "static") : "none")
+    if (vc)
+        os << "star7-vc cp=(" << cfg.cp[0] << "," << cfg.cp[1] << "," << cfg.cp[2] << ")" << (uniform ? " uniform" : "");
+    else
+        os << "star7 c0=" << cfg.c0 << " cp=(" << cfg.cp[0] << "," << cfg.cp[1] << "," << cfg.cp[2] << ")";
+    os << " source=" << (has_f ? (has_fb ? "affine" : "static") : "none")
        << " border=" << (border == SCAFES_BORDER_DIRICHLET ? "dirichlet"
-                         : border == SCAFES_BORDER_MIRROR_POW2 ? "mirror" : "table");
+                         : border == SCAFES_BORDER_MIRROR_POW2 ? "mirror"
+                         : border == SCAFES_BORDER_TABLE ? "table" : "nodes");
     if (mGpoly) os << " G=quartic-in-time";
     if (border == SCAFES_BORDER_TABLE) {
         bool u4 = false;
@@ -709,6 +914,12 @@ void Problem<OWNPRBLM, CT, DIM>::iterateOverTime() {
     if (mHandle) { scafes_gpu_destroy(mHandle); mHandle = nullptr; }
     check(scafes_gpu_create(&cfg, &mHandle));
     if (cfg.border == SCAFES_BORDER_TABLE) check(scafes_gpu_set_border_forms(mHandle, mForms));
+    if (cfg.border == SCAFES_BORDER_NODES)
+        check(scafes_gpu_set_border_node_rules(mHandle, mNodeRules.data(), mNodeRules.size()));
+    if (!mC0.empty()) {
+        check(scafes_gpu_upload(mHandle, SCAFES_FIELD_C0, mC0.data(), mC0.size()));
+        check(scafes_gpu_upload(mHandle, SCAFES_FIELD_CA, mCA.data(), mCA.size()));
+    }
     if (!mFa.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_F_A, mFa.data(), mFa.size()));
     if (!mFb.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_F_B, mFb.data(), mFb.size()));
     if (!mGa.empty()) check(scafes_gpu_upload(mHandle, SCAFES_FIELD_G_A, mGa.data(), mGa.size()));

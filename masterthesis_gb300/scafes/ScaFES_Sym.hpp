@@ -30,6 +30,15 @@
 namespace ScaFES {
 namespace gpu {
 
+// Set when a callback converts a form that holds unknowns to a number (a
+// branch or an elementary function on the value of an unknown, or an
+// assignment of such a form to a CT variable): such a callback is not a
+// linear stencil, and the Problem refuses it.
+inline bool& converted_unknown() {
+    static thread_local bool flag = false;
+    return flag;
+}
+
 // A term key: kind 0 = unknown field `a` at offset (b, c, d);
 //             kind 1 = known field `a` at time level `b` (0 new, 1 old);
 //             kind 2 = unknown field `a` at the centre node, to the power b.
@@ -63,6 +72,13 @@ public:
     }
 
     bool is_const() const { return t_.empty() && !bad_; }
+    // The number a form stands for: its constant, when it holds no unknown.
+    // Converting a form with unknowns yields its constant part and marks the
+    // recording as not a stencil (converted_unknown).
+    operator double() const {
+        if (!is_const()) converted_unknown() = true;
+        return c_;
+    }
     bool bad() const { return bad_; }
     double constant() const { return c_; }
     const std::vector<std::pair<TermKey, double>>& terms() const { return t_; }
@@ -165,6 +181,16 @@ inline Sym operator+(Sym a, const Sym& b) { return a += b; }
 inline Sym operator-(Sym a, const Sym& b) { return a -= b; }
 inline Sym operator*(Sym a, const Sym& b) { return a *= b; }
 inline Sym operator/(Sym a, const Sym& b) { return a /= b; }
+// Mixed forms with a number: exact matches, so that the built-in double
+// operators (reachable through Sym's conversion) never compete.
+inline Sym operator+(Sym a, double b) { return a += Sym(b); }
+inline Sym operator+(double a, const Sym& b) { return Sym(a) += b; }
+inline Sym operator-(Sym a, double b) { return a -= Sym(b); }
+inline Sym operator-(double a, const Sym& b) { return Sym(a) -= b; }
+inline Sym operator*(Sym a, double b) { return a *= Sym(b); }
+inline Sym operator*(double a, const Sym& b) { return Sym(a) *= b; }
+inline Sym operator/(Sym a, double b) { return a /= Sym(b); }
+inline Sym operator/(double a, const Sym& b) { return Sym(a) /= b; }
 
 // Comparisons are only meaningful between constants.  A branch on the value
 // of an unknown is not a stencil: it sets a per-thread flag that the
@@ -180,7 +206,9 @@ inline bool& comparison_on_unknown() {
             return false;                                                     \
         }                                                                     \
         return a.constant() OP b.constant();                                  \
-    }
+    }                                                                         \
+    inline bool operator OP(const Sym& a, double b) { return a OP Sym(b); }   \
+    inline bool operator OP(double a, const Sym& b) { return Sym(a) OP b; }
 SCAFES_SYM_CMP(<)
 SCAFES_SYM_CMP(<=)
 SCAFES_SYM_CMP(>)
@@ -203,6 +231,9 @@ SCAFES_SYM_UNARY(tan)
 SCAFES_SYM_UNARY(fabs)
 #undef SCAFES_SYM_UNARY
 inline Sym abs(const Sym& a) { return fabs(a); }
+inline Sym pow(const Sym& a, const Sym& b);
+inline Sym pow(const Sym& a, double b) { return pow(a, Sym(b)); }
+inline Sym pow(const Sym& a, int b) { return pow(a, Sym(b)); }
 inline Sym pow(const Sym& a, const Sym& b) {
     if (a.is_const() && b.is_const()) return Sym(std::pow(a.constant(), b.constant()));
     if (b.is_const() && b.constant() == 1.0) return a;

@@ -8,7 +8,10 @@ workloads the engine is measured on:
   seeded uniform noise at inner nodes, border 0 (the plain heat workloads);
 * ``pennes_ensemble``: independent Pennes bioheat instances with seeded
   grid sizes, conductivity, perfusion and a Gaussian heat source each
-  (the batched ensemble workload).
+  (the batched ensemble workload);
+* ``tissue_fields_slab`` / ``tissue_device_form``: Pennes bioheat with every
+  coefficient a field over the nodes and the flux borders of the reference's
+  tissue examples (the variable-coefficient workload).
 """
 from __future__ import annotations
 
@@ -124,3 +127,92 @@ def yee_setup(n, seed: int = 4, courant: float = 0.5):
     freq = 4.0
     w = 1.0 / freq
     return tau, src, (1.0, 2.0 * w, w, freq)
+
+
+# ---- tissue workloads (coefficients per node) ----------------------------------
+
+TISSUE_FIELDS = ("rho", "c", "k", "rho_b", "c_b", "omega", "t_blood", "q")
+TISSUE_RANGES = {"rho": (1000.0, 1100.0), "c": (3500.0, 3800.0), "k": (0.4, 0.6), "rho_b": (1040.0, 1060.0),
+                 "c_b": (3700.0, 3900.0), "omega": (0.001, 0.005), "t_blood": (36.5, 37.5), "q": (1e4, 3e4)}
+
+
+def tissue_fields_slab(n, z0: int, z1: int, seed: int) -> dict:
+    """Seeded tissue coefficients of planes z0..z1-1 of an nx x ny x nz grid
+    (the known fields of the MRI-data Pennes example: density, heat capacity,
+    conductivity, blood density and heat capacity, perfusion, blood
+    temperature, metabolic heat), uniform per node in physiological ranges;
+    each plane has its own stream, so slabs of any size give the same
+    field."""
+    nx, ny = n[0], n[1]
+    out = {k: np.empty((z1 - z0, ny, nx)) for k in TISSUE_FIELDS}
+    for z in range(z0, z1):
+        rng = np.random.default_rng((seed, z))
+        for k in TISSUE_FIELDS:
+            out[k][z - z0] = rng.uniform(*TISSUE_RANGES[k], (ny, nx))
+    return out
+
+
+def tissue_device_form(n, h, tau, fields: dict, z0: int = 0, flux: dict | None = None):
+    """The device form of the tissue examples' update on planes z0.. of the
+    grid (the form the drop-in Problem records from their callbacks):
+
+      inner node:  C0 = 1 - 2 sum_p s_p - tau P,  CA = tau a,
+                   F  = tau P T_b + tau q/(rho c)   (source weight cf = 1),
+      with a = k/(rho c), s_p = tau a/h_p^2, P = rho_b c_b omega/(rho c), and
+      the axis factors cp = 1/h_p^2;
+      border node (flux border, when `flux` is given): the examples' bracket
+      per axis -- the missing neighbour replaced by the inner one plus a
+      flux term: Neumann q_bc at the min faces and the x, y max faces, at the
+      z max face Neumann q_skull (zmax_kind 0) or Cauchy h_conv, t_amb
+      (zmax_kind 1) -- as one rule (cu, cn[6], cst) per border node, the
+      border nodes of the slab in Fortran order.
+
+    fields maps TISSUE_FIELDS to arrays (or scalars) over the slab's planes.
+    Returns dict C0, CA, F (slab arrays), cp, rules ((m, 8) or None)."""
+    nzs = next(np.shape(v)[0] for v in fields.values() if np.ndim(v) == 3)
+    shape = (nzs, n[1], n[0])
+    f = {k: np.broadcast_to(np.asarray(fields[k], dtype=np.float64), shape) for k in TISSUE_FIELDS}
+    rho_c = f["rho"] * f["c"]
+    a = f["k"] / rho_c
+    P = (f["rho_b"] * f["c_b"]) / rho_c * f["omega"]
+    s = [tau * a / (hp * hp) for hp in h]
+    out = {"C0": 1.0 - 2.0 * (s[0] + s[1] + s[2]) - tau * P, "CA": tau * a,
+           "F": tau * P * f["t_blood"] + tau * (1.0 / rho_c) * f["q"], "cp": [1.0 / (hp * hp) for hp in h],
+           "rules": None}
+    if flux is None:
+        return out
+    kz, ky, kx = np.meshgrid(np.arange(z0, z0 + nzs), np.arange(n[1]), np.arange(n[0]), indexing="ij")
+    pos = (kx, ky, kz)
+    border = (kx == 0) | (kx == n[0] - 1) | (ky == 0) | (ky == n[1] - 1) | (kz == 0) | (kz == n[2] - 1)
+    cu = 1.0 - tau * P
+    cst = out["F"].copy()
+    cn = np.zeros((6,) + shape)
+    for p in range(3):
+        at_min = pos[p] == 0
+        at_max = pos[p] == n[p] - 1
+        fl = s[p] * (2.0 * h[p] / f["k"])
+        cu = cu - 2.0 * s[p]
+        cn[2 * p] = np.where(at_min, 0.0, np.where(at_max, 2.0 * s[p], s[p]))
+        cn[2 * p + 1] = np.where(at_max, 0.0, np.where(at_min, 2.0 * s[p], s[p]))
+        if p == 2 and flux.get("zmax_kind", 0) == 1:
+            cu = cu - np.where(at_max, fl * flux["h_conv"], 0.0)
+            cst = cst + np.where(at_max, fl * flux["h_conv"] * flux["t_amb"], 0.0)
+        else:
+            q_max = flux.get("q_skull", 0.0) if p == 2 else flux.get("q_bc", 0.0)
+            cst = cst + np.where(at_max, fl * q_max, 0.0)
+        cst = cst + np.where(at_min, fl * flux.get("q_bc", 0.0), 0.0)
+    sel = border.ravel()
+    rules = np.empty((int(sel.sum()), 8))
+    rules[:, 0] = np.broadcast_to(cu, shape).ravel()[sel]
+    for d in range(6):
+        rules[:, 1 + d] = cn[d].ravel()[sel]
+    rules[:, 7] = cst.ravel()[sel]
+    out["rules"] = rules
+    return out
+
+
+def tissue_tau(n, last, safety: float = 0.9) -> float:
+    """`safety` times the stability limit of the tissue update for the
+    largest diffusivity the seeded fields reach (k/(rho c) <= 0.6/3.5e6)."""
+    a_max = TISSUE_RANGES["k"][1] / (TISSUE_RANGES["rho"][0] * TISSUE_RANGES["c"][0])
+    return safety / (2.0 * a_max * sum(((m - 1) / L) ** 2 for m, L in zip(n, last)))

@@ -128,62 +128,17 @@ def tissue_case(name):
 
 
 def tissue_device_inputs(g, fields, kw):
-    """The device form of the tissue examples' update (what the drop-in
-    Problem extracts from the callbacks): coefficient slots C0, CA, the
-    source F_A (cf = 1), the axis factors cp = 1/h_p^2 and, for the flux
-    border, one rule per border node in Fortran order (cu, cn[6], cst).
-
-    Inner node:  C0 = 1 - 2 sum_p s_p - tau P,  CA = tau a,
-                 F = tau P T_b + tau q/(rho c),
-    with a = k/(rho c), s_p = tau a / h_p^2, P = rho_b c_b omega/(rho c).
-    Border node: the examples' bracket per axis -- the missing neighbour
-    replaced by the inner one plus the flux term (Neumann q at min faces and
-    the x, y max faces, q_skull or Cauchy h_conv at the z max face)."""
-    shape = (g.n[2], g.n[1], g.n[0])
-    f = {k: np.broadcast_to(np.asarray(v, dtype=np.float64), shape) for k, v in fields.items()}
-    tau = g.tau
-    rho_c = f["rho"] * f["c"]
-    a = f["k"] / rho_c
-    P = (f["rho_b"] * f["c_b"]) / rho_c * f["omega"]
-    h = [g.h[p] for p in range(3)]
-    s = [tau * a / (hp * hp) for hp in h]
-    c0 = 1.0 - 2.0 * (s[0] + s[1] + s[2]) - tau * P
-    ca = tau * a
-    src = tau * P * f["t_blood"] + tau * (1.0 / rho_c) * f["q"]
-    cp = [1.0 / (hp * hp) for hp in h]
-    border = O.border_mask(g)
-    # Per-node rules over all nodes, then the border nodes in Fortran order.
-    cu = 1.0 - tau * P
-    cst = src.copy()
-    cn = np.zeros((6,) + shape)
-    nz, ny, nx = shape
-    idx = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
-    pos = (idx[2], idx[1], idx[0])  # x, y, z indices
-    zmax_kind = kw.get("zmax_kind", 0)
-    for p in range(3):
-        at_min = pos[p] == 0
-        at_max = pos[p] == g.n[p] - 1
-        flux = s[p] * (2.0 * h[p] / f["k"])
-        cu = cu - 2.0 * s[p]
-        cn[2 * p] = np.where(at_min, 0.0, np.where(at_max, 2.0 * s[p], s[p]))
-        cn[2 * p + 1] = np.where(at_max, 0.0, np.where(at_min, 2.0 * s[p], s[p]))
-        q_max = kw.get("q_bc", 0.0)
-        if p == 2 and zmax_kind == 0:
-            q_max = kw.get("q_skull", 0.0)
-        if p == 2 and zmax_kind == 1:
-            cu = cu - np.where(at_max, flux * kw["h_conv"], 0.0)
-            cst = cst + np.where(at_max, flux * kw["h_conv"] * kw["t_amb"], 0.0)
-        else:
-            cst = cst + np.where(at_max, flux * q_max, 0.0)
-        cst = cst + np.where(at_min, flux * kw.get("q_bc", 0.0), 0.0)
-    sel = border.ravel()
-    rules = np.empty((int(sel.sum()), 8))
-    rules[:, 0] = np.broadcast_to(cu, shape).ravel()[sel]
-    for d in range(6):
-        rules[:, 1 + d] = cn[d].ravel()[sel]
-    rules[:, 7] = cst.ravel()[sel]
-    return {"C0": np.ascontiguousarray(c0), "CA": np.ascontiguousarray(ca), "F": np.ascontiguousarray(src),
-            "cp": cp, "rules": rules}
+    """The device form of the tissue examples' update on grid g
+    (workloads.tissue_device_form on the whole grid; kw: the border keywords
+    of oracle.pennes_tissue, empty for a Dirichlet border)."""
+    from masterthesis_gb300 import workloads as W
+    n = (g.n[0], g.n[1], g.n[2])
+    shape = (n[2], n[1], n[0])
+    full = {k: np.broadcast_to(np.asarray(v, dtype=np.float64), shape) for k, v in fields.items()}
+    flux = None if not kw else {k: kw[k] for k in ("zmax_kind", "q_bc", "q_skull", "h_conv", "t_amb") if k in kw}
+    d = W.tissue_device_form(n, [g.h[0], g.h[1], g.h[2]], g.tau, full, 0, flux)
+    return {"C0": np.ascontiguousarray(d["C0"]), "CA": np.ascontiguousarray(d["CA"]),
+            "F": np.ascontiguousarray(d["F"]), "cp": d["cp"], "rules": d["rules"]}
 
 
 def run_tissue(cfg_kw, g, dev, u0, nsteps, border="nodes", g_bdry=None, tile=0, precision="f64"):

@@ -34,3 +34,35 @@ def compile_cpp(src: Path, out: Path, extra: list[str] | None = None) -> Path:
     if res.returncode != 0:
         raise RuntimeError(f"g++ failed for {src.name}:\n{res.stderr[-4000:]}")
     return out
+
+
+def read_device_form(path) -> dict:
+    """The named FP64 arrays of a Problem::dumpDeviceForm file."""
+    import numpy as np
+    b = Path(path).read_bytes()
+    out, i = {}, 0
+    while i < len(b):
+        name = b[i:i + 16].split(b"\0")[0].decode()
+        n = int(np.frombuffer(b[i + 16:i + 24], dtype=np.int64)[0])
+        i += 24
+        out[name] = np.frombuffer(b[i:i + 8 * n], dtype=np.float64)
+        i += 8 * n
+    return out
+
+
+def tissue_args(golden: dict, workdir: Path) -> list[str]:
+    """Command-line options of run_problem / extract_reference for a tissue
+    golden case: the grid, the time axis, the example's constants and (MRI)
+    its known fields written to a raw FP64 file."""
+    import numpy as np
+    n = [int(v) for v in golden["n"]]
+    last = [float(v) for v in golden["last"]]
+    args = [f"--nNodes={n[0]}x{n[1]}x{n[2]}", f"--coordNodeLast={last[0]!r}x{last[1]!r}x{last[2]!r}",
+            f"--tau={float(golden['tau'])!r}", f"--nTimesteps={int(golden['nsteps'])}",
+            f"--endtime={float(golden['t_end'])!r}",
+            "--params=" + ",".join(repr(float(v)) for v in golden["params"])]
+    if "fields" in golden:
+        path = Path(workdir) / "fields.bin"
+        np.concatenate([golden["fields"].ravel(), golden["surface"].ravel()]).tofile(path)
+        args.append(f"--fields={path}")
+    return args

@@ -16,6 +16,15 @@
 //                 radiation condition -lambda du/dn = eps sigma u^4 - G at the
 //                 max faces, G quartic in time, exact solution (1+t)(1+x+y+z)
 //                 (tests/system/PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin)
+//   TissueTumour -- Pennes bioheat whose perfusion and metabolic heat take
+//                 another value inside a tumour sphere, Neumann faces and a
+//                 convective (Cauchy) z-max face (examples/TumorHeatEqnFDM)
+//   TissueMri  -- Pennes bioheat with every coefficient a known field over
+//                 the nodes, Neumann faces, a closed-skull (Neumann) z-max
+//                 face and convection + radiation where the "surface" field
+//                 is 1 (examples/MRIDataPBHEqnFDM)
+// The tissue classes evaluate their expressions in the examples' operation
+// order, so that the recorded weights are the same doubles.
 #pragma once
 
 #include <cmath>
@@ -316,7 +325,7 @@ public:
         const double s = HeatLin<CT, DIM>::lin(this->coordinates(n));
         const double tt = this->time(t), y = s * (1.0 + tt);
         v[0](n) = source(s, tt);
-        v[1](n) = onMin(n) ? y : (y * y) * (y * y) * (SIGMA * EPS) + LAMBDA * (1.0 + tt);
+        v[1](n) = onMin(n) ? y : ((y * y) * y) * y * (SIGMA * EPS) + LAMBDA * (1.0 + tt);
         v[2](n) = y;
     }
     template <typename TT>
@@ -364,6 +373,167 @@ public:
         }
         vNew[0](n) -= this->tau() * ((RHO_B * C_B) / (RHO * C)) * W * vOld[0](n);
         vNew[0](n) += this->tau() * (1.0 / (RHO * C)) * this->knownDfOld(0, n);
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};
+
+
+// The tissue examples' update of one node: the axis brackets (a missing
+// neighbour replaced by the inner one plus a flux term at a border face),
+// then perfusion and heat source.  zmax(...) gives the z-max face's bracket.
+template <class Prob, typename TT, std::size_t DIM, class ZMax>
+void tissue_update(Prob& pb, std::vector<ScaFES::DataField<TT, DIM>>& vNew,
+                   const std::vector<ScaFES::DataField<TT, DIM>>& vOld, const ScaFES::Ntuple<int, DIM>& n,
+                   bool border, double rho, double c, double k, double rho_b, double c_b, double omega,
+                   double t_b, double q, double q_bc, ZMax zmax) {
+    const auto& U = vOld[0];
+    vNew[0](n) = U(n);
+    for (std::size_t p = 0; p < DIM; ++p) {
+        const double h = pb.gridsize(p);
+        const double cf = pb.tau() * (k / (rho * c));
+        if (border && n.elem(p) == pb.nNodes(p) - 1) {
+            if (p == DIM - 1) {
+                vNew[0](n) += cf * zmax(U(pb.connect(n, 2 * p)), U(n), h, k, vNew[0](n)) / (h * h);
+            } else {
+                vNew[0](n) += cf * (U(pb.connect(n, 2 * p)) + U(pb.connect(n, 2 * p)) - ((2.0 * h / k) * (-1.0 * q_bc)) -
+                                    2.0 * U(n)) / (h * h);
+            }
+        } else if (border && n.elem(p) == 0) {
+            vNew[0](n) += cf * (U(pb.connect(n, 2 * p + 1)) + ((2.0 * h / k) * q_bc) + U(pb.connect(n, 2 * p + 1)) -
+                                2.0 * U(n)) / (h * h);
+        } else {
+            vNew[0](n) += cf * (U(pb.connect(n, 2 * p)) + U(pb.connect(n, 2 * p + 1)) - 2.0 * U(n)) / (h * h);
+        }
+    }
+    vNew[0](n) += pb.tau() * ((rho_b * c_b) / (rho * c)) * omega * (t_b - U(n));
+    vNew[0](n) += pb.tau() * (1.0 / (rho * c)) * q;
+}
+
+template <typename CT, std::size_t DIM>
+class TissueTumour : public ScaFES::Problem<TissueTumour<CT, DIM>, CT, DIM> {
+    using Base = ScaFES::Problem<TissueTumour<CT, DIM>, CT, DIM>;
+public:
+    using Base::Base;
+    // RHO C K Q_BRAIN Q_TUMOR RHO_B C_PB OMEGA_B_BRAIN OMEGA_B_TUMOR T_I H T_INF Q_BC DIAMETER DEPTH T_A
+    double P[16] = {};
+    double radius = 0.0;
+    ScaFES::Ntuple<double, DIM> centre;
+    void setParams(const std::vector<double>& v) {
+        for (int i = 0; i < 16; ++i) P[i] = v.at(i);
+        radius = P[13] / 2.0;
+        for (std::size_t p = 0; p < DIM; ++p)
+            centre[p] = p == DIM - 1 ? this->params().coordNodeLast()[p] - P[14] : this->params().coordNodeLast()[p] / 2.0;
+    }
+    void sphere(const ScaFES::Ntuple<int, DIM>& n, double& omega, double& q) const {
+        const ScaFES::Ntuple<double, DIM> x = this->coordinates(n);
+        double d = 0.0;
+        for (std::size_t p = 0; p < DIM; ++p) d += (x[p] - centre[p]) * (x[p] - centre[p]);
+        const bool in = d <= radius * radius;
+        omega = in ? P[8] : P[7];
+        q = in ? P[4] : P[3];
+    }
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>& n,
+                   const int&) {
+        v[0](n) = P[9];
+    }
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>& o, const ScaFES::Ntuple<int, DIM>& n,
+                    const int& t) {
+        initInner<TT>(v, o, n, t);
+    }
+    template <typename TT>
+    void update(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                const ScaFES::Ntuple<int, DIM>& n, bool border) {
+        double omega, q;
+        sphere(n, omega, q);
+        const double H = P[10], T_INF = P[11];
+        auto cauchy = [&](const TT& a, const TT& u, double h, double k, const TT&) {
+            return a + a - ((2.0 * h / k) * H * (u - T_INF)) - 2.0 * u;
+        };
+        tissue_update(*this, vNew, vOld, n, border, P[0], P[1], P[2], P[5], P[6], omega, P[15], q, P[12], cauchy);
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        update<TT>(vNew, vOld, n, false);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                      const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        update<TT>(vNew, vOld, n, true);
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};
+
+template <typename CT, std::size_t DIM>
+class TissueMri : public ScaFES::Problem<TissueMri<CT, DIM>, CT, DIM> {
+    using Base = ScaFES::Problem<TissueMri<CT, DIM>, CT, DIM>;
+public:
+    using Base::Base;
+    double H = 0.0, T_AMB = 0.0, Q_BC = 0.0, Q_SKULL = 0.0, EPSILON = 0.0;
+    const double SIGMA = 5.670373e-8;
+    void setParams(const std::vector<double>& v) {
+        H = v.at(0); T_AMB = v.at(1); Q_BC = v.at(2); Q_SKULL = v.at(3); EPSILON = v.at(4);
+    }
+    // The nine known fields (rho, c, lambda, rho_blood, c_blood, omega,
+    // T_blood, q, surface), n values each, x fastest.
+    void setFields(const std::vector<double>& f) {
+        const auto& g = this->globalGrid().discreteDomain();
+        const long long nn = g.nNodesTotal();
+        for (long long m = 0; m < nn; ++m) {
+            const ScaFES::Ntuple<int, DIM> n = g.idxNodeScalar2TupleStyleFortran(m);
+            for (int i = 0; i < 9; ++i) {
+                this->mVectKnownDfsDomNew[i](n) = f.at((std::size_t)(i * nn + m));
+                this->mVectKnownDfsDomOld[i](n) = f.at((std::size_t)(i * nn + m));
+            }
+        }
+    }
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<TT>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    template <typename TT>
+    void update(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                const ScaFES::Ntuple<int, DIM>& n, bool border) {
+        CT fld[9];
+        for (int i = 0; i < 9; ++i) fld[i] = this->knownDf(i, n);
+        const int open = (int)fld[8];
+        auto skull = [&](const TT& a, const TT& u, double h, double k, const TT& partial) -> TT {
+            if (open == 1) {
+                const TT t_old = partial + 273.15;
+                const TT t_old4 = t_old * t_old * t_old * t_old;
+                const double t_amb = T_AMB + 273.15;
+                const double t_amb4 = t_amb * t_amb * t_amb * t_amb;
+                return a + a - ((2.0 * h / k) * H * (u - T_AMB)) - ((2.0 * h / k) * EPSILON * SIGMA * (t_old4 - t_amb4)) -
+                       2.0 * u;
+            }
+            return a + a - ((2.0 * h / k) * (-1.0 * Q_SKULL)) - 2.0 * u;
+        };
+        tissue_update(*this, vNew, vOld, n, border, fld[0], fld[1], fld[2], fld[3], fld[4], fld[5], fld[6], fld[7],
+                      Q_BC, skull);
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        update<TT>(vNew, vOld, n, false);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                      const ScaFES::Ntuple<int, DIM>& n, const int&) {
+        update<TT>(vNew, vOld, n, true);
     }
     template <typename TT>
     void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}

@@ -1,18 +1,45 @@
 // Runs one problem of problems.hpp through the drop-in ScaFES::Problem
 // (test infrastructure).  Usage:
-//   run_problem <heat_lin|pennes_lin|mirror_pow2|heat_sine|heat_neumann|heat_cauchy> out.bin
-//               [--extract-only] [ScaFES options...]
+//   run_problem <heat_lin|pennes_lin|mirror_pow2|heat_sine|heat_neumann|heat_cauchy|
+//                pennes_radiation|tumour|mri> out.bin
+//               [--extract-only] [--dump=PATH] [--params=a,b,...] [--fields=PATH]
+//               [ScaFES options...]
 // Writes the final iterate as raw doubles (x fastest); with --extract-only
-// prints the device form of the update instead (no GPU needed).
+// prints the device form of the update instead, with --dump=PATH also
+// writes it to PATH (neither needs a GPU).  --params: the tumour's 16
+// constants, or the MRI example's H T_INF Q_BC Q_SKULL EPSILON T_INIT;
+// --fields: the MRI example's nine known fields, raw FP64.
 #include <cstdio>
 #include <cstring>
 #include <iostream>
+#include <sstream>
+#include <stdexcept>
+#include <vector>
 #include <string>
 
 #include "problems.hpp"
 
+// Options of the tissue problems and of the device-form dump.
+static std::string g_dump;
+static std::vector<double> g_params, g_fields;
+
+static std::vector<double> read_doubles(const std::string& path) {
+    std::vector<double> v;
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) throw std::runtime_error("cannot read " + path);
+    double x;
+    while (std::fread(&x, sizeof(double), 1, f) == 1) v.push_back(x);
+    std::fclose(f);
+    return v;
+}
+
 template <class P>
 int run(P& ppp, const std::string& out, bool extract) {
+    if (!g_dump.empty()) {
+        ppp.dumpDeviceForm(g_dump);
+        std::cout << "FORM " << ppp.deviceForm() << std::endl;
+        return 0;
+    }
     if (extract) {
         std::cout << "FORM " << ppp.deviceForm() << std::endl;
         return 0;
@@ -34,14 +61,42 @@ int main(int argc, char** argv) {
     const std::string which = argv[1], out = argv[2];
     bool extract = false, write_cl = false;
     for (int i = 3; i < argc; ++i) {
-        if (!std::strcmp(argv[i], "--extract-only")) extract = true;
-        if (!std::strcmp(argv[i], "--write-like-cl")) write_cl = true;  // U written per --nSnapshots
+        const std::string a = argv[i];
+        if (a == "--extract-only") extract = true;
+        if (a == "--write-like-cl") write_cl = true;  // U written per --nSnapshots
+        if (a.compare(0, 7, "--dump=") == 0) g_dump = a.substr(7);  // device form to a file, no GPU
+        if (a.compare(0, 9, "--params=") == 0) {                      // comma-separated constants
+            std::stringstream ss(a.substr(9));
+            std::string item;
+            while (std::getline(ss, item, ',')) g_params.push_back(std::atof(item.c_str()));
+        }
+        if (a.compare(0, 9, "--fields=") == 0) g_fields = read_doubles(a.substr(9));  // known fields, raw FP64
     }
     try {
         ScaFES::Parameters params(argc, argv);
         ScaFES::GridGlobal<3> gg(params);
         std::vector<ScaFES::WriteHowOften> wr(3, ScaFES::WriteHowOften::NEVER);
         if (write_cl) wr[2] = ScaFES::WriteHowOften::LIKE_GIVEN_AT_CL;
+        if (which == "tumour") {
+            TissueTumour<double, 3> p(params, gg, false, {"T"}, {1}, {false}, {0}, {0.0},
+                                      std::vector<ScaFES::WriteHowOften>(1, ScaFES::WriteHowOften::NEVER), {true});
+            p.setParams(g_params);
+            return run(p, out, extract);
+        }
+        if (which == "mri") {
+            std::vector<double> dv(10, 0.0);
+            dv[9] = g_params.size() > 5 ? g_params[5] : 0.0;  // initial temperature
+            std::vector<bool> known(10, true);
+            known[9] = false;
+            TissueMri<double, 3> p(params, gg, false,
+                                   {"rho", "c", "lambda", "rho_blood", "c_blood", "omega", "T_blood", "q", "surface", "T"},
+                                   std::vector<int>{0, 0, 0, 0, 0, 0, 0, 0, 0, 1}, known, std::vector<int>(10, 0), dv,
+                                   std::vector<ScaFES::WriteHowOften>(10, ScaFES::WriteHowOften::NEVER),
+                                   std::vector<bool>(10, false));
+            p.setParams(g_params);
+            p.setFields(g_fields);
+            return run(p, out, extract);
+        }
         if (which == "mirror_pow2") {
             MirrorPow2<double, 3> p(params, gg, false, {"A"}, {1}, {false}, {0}, {0.0},
                                     std::vector<ScaFES::WriteHowOften>(1, ScaFES::WriteHowOften::NEVER), {true});

@@ -143,3 +143,18 @@ def test_dropin_restarts_from_init_file(gpu, run_problem, tmp_path):
                           "--nTimesteps=10", f"--initfile={tmp_path / 'missing.snap'}"],
                          capture_output=True, text=True, timeout=120)
     assert res.returncode != 0 and "init file" in (res.stdout + res.stderr)
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f32", 1e-5)])
+@pytest.mark.parametrize("which,golden", [("tumour", "tissue_tumour"), ("mri", "tissue_mri_closed")])
+def test_dropin_tissue_examples_match_reference(run_problem, tmp_path, which, golden, prec, tol):
+    """The tissue examples (coefficients per node, per-node flux borders)
+    through iterateOverTime on the variable-coefficient sweep, against the
+    reference's own classes run by its driver (tests/golden/tissue_*.npz).
+    The restatements' device forms equal the reference classes' bit for bit
+    (test_dropin_host.py)."""
+    from dropin.build import tissue_args
+    d = load_golden(golden)
+    n = tuple(int(v) for v in d["n"])
+    u, out = run(run_problem, which, tmp_path / "u.bin", n, *tissue_args(d, tmp_path), f"--gpuPrecision={prec}")
+    assert cases.rel_err(u, d["final"]) <= tol
