@@ -558,7 +558,10 @@ void scafes_adj_destroy(scafes_adj* a);
  * on the binomial schedule, in the handle's precision (F64 or F32X2).  The
  * initial iterate comes from the copy scafes_gpu_keep_initial keeps; its
  * border nodes must equal the Dirichlet value (SCAFES_ERR_UNSUPPORTED
- * otherwise).  scafes_gpu_keep_initial(h, 1) makes every later upload of
+ * otherwise).  The Dirichlet border resets every border node each step, so
+ * a border value of u0 enters the first step only and dJ_du0 on border
+ * nodes is that step's part (the derivative the reference's own
+ * updateInner/updateBorder give with a differentiable scalar).  scafes_gpu_keep_initial(h, 1) makes every later upload of
  * the unknown field also keep an FP64 copy on the device (one more field of
  * device memory); 0 frees it. */
 int scafes_gpu_keep_initial(scafes_handle* h, int on);

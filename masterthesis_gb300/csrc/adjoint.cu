@@ -808,10 +808,16 @@ struct Rev {
     bool started;
     double* Jpart;
     bool seed;
+    // Border nodes reset to a fixed value every step (a Dirichlet border)
+    // instead of held at u0's values: u0's border then enters only the first
+    // step, and the border part of dJ/du0 is that step's alone.
+    bool reset_border = false;
 };
 
 int adj_step(Rev& R, const double* u_t) {
     scafes_adj* a = R.a;
+    if (R.reset_border && a->adj_steps == R.T - 1)
+        ATRY(a, cudaMemsetAsync(a->bnd, 0, field_bytes(a), a->stream));  // the last step is t = 0 -> 1
     if (pairs(a)) {
         if (int rc = coefficient_maps(a)) return rc;
         CUtensorMap ml, mu;
@@ -1044,7 +1050,8 @@ extern "C" int scafes_adj_forward(scafes_adj* a, const double* u0, int n_steps, 
 // (J = 0.5 |u_T - target|^2) or, with `seed`, the cotangent dJ/du_T.
 // With u0_dev, u0 is a device field in the handle's padded FP64 layout.
 static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const double* target, bool seed,
-                         int n_steps, double* J, double* grad_k, double* grad_u0, size_t n, bool u0_dev = false) {
+                         int n_steps, double* J, double* grad_k, double* grad_u0, size_t n, bool u0_dev = false,
+                         bool reset_border = false) {
     if (!a || !u0 || !target || !grad_k || !grad_u0 || n_steps < 1)
         return afail(a, SCAFES_ERR_ARG, "%s: bad arguments", who);
     if (n != (size_t)a->L.nx * a->L.ny * a->L.nz) return afail(a, SCAFES_ERR_ARG, "%s: wrong size", who);
@@ -1066,7 +1073,7 @@ static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const
     a->fwd_steps = 0;
     a->adj_steps = 0;
     ATRY(a, cudaEventRecord(a->e0, a->stream));
-    Rev R{a, a->work, n_steps, 0, false, a->part, seed};
+    Rev R{a, a->work, n_steps, 0, false, a->part, seed, reset_border};
     if ((rc = reverse(R, 0, n_steps, 0, free))) return rc;
     if (pairs(a))
         k_finalize_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(a->gx), P2(a->gy), P2(a->gz), P2(a->lam[R.cur]),
@@ -1106,7 +1113,8 @@ extern "C" int scafes_adj_backward(scafes_adj* a, const double* u0, const double
 namespace scafes {
 int adj_backward_device_u0(scafes_adj* a, const double* u0_dev, const double* dJ_duT, int n_steps, double* grad_k,
                            double* grad_u0, size_t n) {
-    return gradient_impl(a, "scafes_gpu_adjoint", u0_dev, dJ_duT, true, n_steps, nullptr, grad_k, grad_u0, n, true);
+    return gradient_impl(a, "scafes_gpu_adjoint", u0_dev, dJ_duT, true, n_steps, nullptr, grad_k, grad_u0, n, true,
+                         true);
 }
 }  // namespace scafes
 

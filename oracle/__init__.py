@@ -99,6 +99,8 @@ def lib():
         L.orc_stencil_width_var.argtypes = [C.POINTER(Grid), C.c_int, C.c_int, dp, C.c_int]
         L.orc_kheat_forward.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, C.c_int]
         L.orc_kheat_adjoint.argtypes = [C.POINTER(Grid), dp, C.c_int, dp, dp, dp, dp, dp, C.c_int]
+        L.orc_kheat_adjoint_reset.argtypes = L.orc_kheat_adjoint.argtypes
+        L.orc_kheat_adjoint_reset.restype = C.c_int
         L.orc_lame.argtypes = [C.POINTER(Grid), C.c_double, C.c_double, C.c_double, C.c_int, dp, dp, C.c_int]
         L.orc_yee.argtypes = [C.POINTER(Grid), C.c_int, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                               C.c_double, C.c_double, C.c_int]
@@ -288,15 +290,20 @@ def kheat_tangent(g: Grid, k, dk, u0, du0, nsteps, nthreads=0):
     return u, du
 
 
-def kheat_adjoint(g: Grid, k, traj, target, nthreads=0):
+def kheat_adjoint(g: Grid, k, traj, target, nthreads=0, reset_border=False):
+    """J, dJ/dk, dJ/du0 of J = 0.5 ||u_T - target||^2 for the flux-form
+    solve with trajectory traj.  reset_border: the border is reset to fixed
+    values every step (a Dirichlet border) instead of held at u0's values;
+    u0's border then enters the first step only."""
     nsteps = traj.shape[0] - 1
     k = np.ascontiguousarray(k, dtype=np.float64)
     target = np.ascontiguousarray(target, dtype=np.float64)
     gk = np.empty_like(k)
     gu = np.empty_like(k)
     j = C.c_double(0.0)
-    _check(lib().orc_kheat_adjoint(C.byref(g), _p(k), nsteps, _p(traj), _p(target), _p(gk), _p(gu),
-                                   C.byref(j), nthreads), "kheat_adjoint")
+    fn = lib().orc_kheat_adjoint_reset if reset_border else lib().orc_kheat_adjoint
+    _check(fn(C.byref(g), _p(k), nsteps, _p(traj), _p(target), _p(gk), _p(gu), C.byref(j), nthreads),
+           "kheat_adjoint")
     return j.value, gk, gu
 
 

@@ -665,10 +665,10 @@ int orc_kheat_tangent(const orc_grid* g, const double* k, const double* dk, int 
     return 0;
 }
 
-int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
-                      const double* traj, const double* target,
-                      double* grad_k, double* grad_u0, double* j_out,
-                      int nthreads)
+static int kheat_adjoint_impl(const orc_grid* g, const double* k, int nsteps,
+                              const double* traj, const double* target,
+                              double* grad_k, double* grad_u0, double* j_out,
+                              int reset_border, int nthreads)
 {
     const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
     const size_t nn = n_total(g);
@@ -715,6 +715,11 @@ int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
                         const double dup = has_p ? un[m + stride[p]] - un[m] : 0.0;
                         const double dum = has_m ? un[m - stride[p]] - un[m] : 0.0;
                         if (border) {
+                            /* Held border: its lambda accumulates over all
+                             * steps.  Reset border (Dirichlet): the next
+                             * border value does not depend on this one, so
+                             * only this step's inner neighbours count. */
+                            if (reset_border && p == 0) v = 0.0;
                             v += c * (kmv * lm + kpv * lp);
                         } else {
                             v += c * (kpv * (lp - lt[m]) + kmv * (lm - lt[m]));
@@ -732,6 +737,22 @@ int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
     *j_out = jsum;
     free(lam); free(lam2); free(lt);
     return 0;
+}
+
+int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
+                      const double* traj, const double* target,
+                      double* grad_k, double* grad_u0, double* j_out,
+                      int nthreads)
+{
+    return kheat_adjoint_impl(g, k, nsteps, traj, target, grad_k, grad_u0, j_out, 0, nthreads);
+}
+
+int orc_kheat_adjoint_reset(const orc_grid* g, const double* k, int nsteps,
+                            const double* traj, const double* target,
+                            double* grad_k, double* grad_u0, double* j_out,
+                            int nthreads)
+{
+    return kheat_adjoint_impl(g, k, nsteps, traj, target, grad_k, grad_u0, j_out, 1, nthreads);
 }
 
 /* ---- Lame-Navier (leapfrog) ------------------------------------------- */

@@ -175,6 +175,16 @@ int orc_kheat_adjoint(const orc_grid* g, const double* k, int nsteps,
                       double* grad_k, double* grad_u0, double* j_out,
                       int nthreads);
 
+/* The same adjoint for a border that is reset to a fixed value every step
+ * (the Dirichlet border of the plain heat problem, Dirichlet.hpp:125-131)
+ * instead of held at u0's values: u0's border values enter only the first
+ * step, so dJ/du0 on border nodes is that step's part alone; inner nodes
+ * and dJ/dk are unchanged (the border values themselves are the same). */
+int orc_kheat_adjoint_reset(const orc_grid* g, const double* k, int nsteps,
+                            const double* traj, const double* target,
+                            double* grad_k, double* grad_u0, double* j_out,
+                            int nthreads);
+
 /* Lame-Navier elastic wave, leapfrog in time (no reference counterpart that
  * runs: examples/LameNavierEqnFDM/LameNavierEqnFDM.hpp:23-25 states the
  * reference cannot advance it).  u and uprev hold 3 components of n nodes

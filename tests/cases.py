@@ -159,3 +159,17 @@ def run_tissue(cfg_kw, g, dev, u0, nsteps, border="nodes", g_bdry=None, tile=0, 
         p.upload(M.FIELD_U, u0)
         p.step(nsteps)
         return p.download()
+
+
+def tangent_inputs(n):
+    """Seeded inputs of the gradient golden case (tests/golden/
+    heat_tangent_32.npz): u0 uniform in [-1, 1] with a zero border (seed
+    41), the target (seed 42) and four directions over all nodes (seeds
+    43..46)."""
+    shape = (n[2], n[1], n[0])
+    g = O.make_grid(n)
+    u0 = np.random.default_rng(41).uniform(-1.0, 1.0, shape)
+    u0[O.border_mask(g)] = 0.0
+    target = np.random.default_rng(42).uniform(-1.0, 1.0, shape)
+    dirs = [np.random.default_rng(43 + k).uniform(-1.0, 1.0, shape) for k in range(4)]
+    return u0, target, dirs

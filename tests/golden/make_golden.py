@@ -7,7 +7,7 @@ headers by ``make -C oracle ref`` -- and stores its inputs and final iterate.
 
 Run from the repository root (needs the reference checkout for the build):
 
-    make -C oracle ref && python tests/golden/make_golden.py [--tissue]
+    make -C oracle ref && python tests/golden/make_golden.py [--tissue | --tangent]
 
 The .npz files are committed; the GPU machine never runs this script.
 """
@@ -22,6 +22,9 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(ROOT))
 import oracle as O  # noqa: E402
+
+sys.path.insert(0, str(ROOT / "tests"))
+import cases  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
 
@@ -118,7 +121,31 @@ def main():
                                params=params, final=r)
 
     cases.update(tissue_cases(tmp))
+    cases.update(tangent_cases(tmp))
     save(cases)
+
+
+def tangent_cases(tmp):
+    """Directional derivatives of J = 1/2 ||u_T - target||^2 for the heat
+    update with a zero Dirichlet border, taken through the reference's own
+    updateInner<TT>/updateBorder<TT> with a dual number (ref_heat_tangent):
+    dJ_k = <u_T - target, du_T along d_k>, the numbers the adjoint's
+    <dJ/du0, d_k> must reproduce -- for directions over all nodes (dJ) and
+    the same directions with a zero border (dJ_inner).  A border value of
+    u0 enters only the first step: the Dirichlet border resets it."""
+    n, T = (32, 32, 32), 60
+    tau = 0.9 / (2.0 * sum((m - 1) ** 2 for m in n))
+    u0, target, dirs = cases.tangent_inputs(n)
+    # The four directions over all nodes, then the same with a zero border.
+    border = O.border_mask(O.make_grid(n))
+    inner_dirs = [np.where(border, 0.0, d) for d in dirs]
+    r = O.run_ref("ref_heat_tangent", n, T, tmp, tau=tau, t_end=tau * T,
+                  inputs=np.concatenate([u0.ravel()] + [d.ravel() for d in dirs + inner_dirs]),
+                  extra=[2 * len(dirs)], nfields=1 + 2 * len(dirs))
+    uT = r[0]
+    dJ = np.array([float(np.sum((uT - target) * r[1 + k])) for k in range(2 * len(dirs))])
+    return {"heat_tangent_32": dict(n=n, nsteps=T, tau=tau, t_end=tau * T, uT=uT, dJ=dJ[:len(dirs)],
+                                    dJ_inner=dJ[len(dirs):])}
 
 
 # The reference's tissue examples (examples/TumorHeatEqnFDM, examples/
@@ -178,5 +205,7 @@ def save(cases):
 if __name__ == "__main__":
     if sys.argv[1:] == ["--tissue"]:   # only the tissue-example cases
         save(tissue_cases(tempfile.mkdtemp()))
+    elif sys.argv[1:] == ["--tangent"]:  # only the dual-number gradient case
+        save(tangent_cases(tempfile.mkdtemp()))
     else:
         main()

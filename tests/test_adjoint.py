@@ -281,7 +281,8 @@ def test_plain_handle_backward_entry_matches_oracle(gpu, prec, tol):
     g, tau, u0, target = plain_heat_case(n, T, a, 31)
     k = np.full(u0.shape, a)
     uT_ref, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
-    _, gk_ref, gu_ref = O.kheat_adjoint(g, k, traj, target)
+    # The handle's border is a Dirichlet border (reset every step).
+    _, gk_ref, gu_ref = O.kheat_adjoint(g, k, traj, target, reset_border=True)
     with M.Plain(M.make_cfg(n, tau=tau, precision=prec, heat=(a, 1.0, 0.0))) as p:
         p.keep_initial()
         p.upload(M.FIELD_U, u0)
@@ -338,3 +339,32 @@ def test_plain_handle_backward_entry_refuses_what_it_does_not_cover(gpu):
         p.upload(M.FIELD_U, u0)
         p.step(T)
         assert code(p) == UNSUPPORTED                  # perfusion: not the heat form
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-10), ("f32x2", 1e-9)])
+def test_plain_handle_gradient_matches_reference_dual_numbers(gpu, prec, tol):
+    """dJ/du0 of scafes_gpu_adjoint on the heat problem at 32^3 x 60 steps
+    (checkpointed, 8 snapshots) against directional derivatives taken
+    through the reference's own updateInner<TT>/updateBorder<TT> with a dual
+    number (tests/golden/heat_tangent_32.npz, made by oracle/ref_harness/
+    ref_heat_tangent.cpp from the untouched reference headers):
+    <dJ/du0, d_k> = dJ_k for four seeded directions over all nodes, border
+    included (a border value enters the first step only: the Dirichlet
+    border resets it)."""
+    from conftest import load_golden
+    M = gpu
+    d = load_golden("heat_tangent_32")
+    n = tuple(int(v) for v in d["n"])
+    T, tau = int(d["nsteps"]), float(d["tau"])
+    u0, target, dirs = cases.tangent_inputs(n)
+    with M.Plain(M.make_cfg(n, tau=tau, precision=prec, heat=(1.0, 1.0, 0.0))) as p:
+        p.keep_initial()
+        p.upload(M.FIELD_U, u0)
+        p.step(T)
+        uT = p.download()
+        _, gu = p.adjoint(uT - target, 8)
+    assert cases.rel_err(uT, d["uT"]) <= (1e-12 if prec == "f64" else 1e-11)
+    for dk, ref in zip(dirs, d["dJ"]):
+        got = float(np.sum(gu * dk))
+        assert abs(got - ref) <= tol * float(np.sum(np.abs(gu * dk))), (got, ref)

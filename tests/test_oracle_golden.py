@@ -244,3 +244,37 @@ def test_tissue_examples_bit_exact(name):
     d, g, fields, kw, u0 = cases.tissue_case(name)
     u = O.pennes_tissue(g, u0, int(d["nsteps"]), fields, **kw)
     assert np.array_equal(u, d["final"])
+
+
+def test_oracle_adjoint_matches_reference_dual_numbers():
+    """The oracle's adjoint at k = 1 (the flux-form heat update with a
+    uniform conductivity is the reference's heat update with COEFF_A = 1)
+    against directional derivatives taken through the reference's own
+    updateInner<TT>/updateBorder<TT> with a dual number
+    (tests/golden/heat_tangent_32.npz, oracle/ref_harness/
+    ref_heat_tangent.cpp): <dJ/du0, d_k> = dJ_k for four seeded directions,
+    and the forward solve equals the reference's, to 1e-12."""
+    import cases
+    d = load_golden("heat_tangent_32")
+    n = tuple(int(v) for v in d["n"])
+    T, tau = int(d["nsteps"]), float(d["tau"])
+    u0, target, dirs = cases.tangent_inputs(n)
+    g = O.make_grid(n, tau=tau)
+    k = np.ones_like(u0)
+    uT, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
+    assert np.max(np.abs(uT - d["uT"])) <= 1e-12 * np.max(np.abs(d["uT"]))
+    _, _, gu = O.kheat_adjoint(g, k, traj, target)
+    # The oracle's engine holds border nodes at u0's values, so its dJ/du0
+    # agrees with the Dirichlet problem's on the inner nodes: directions
+    # with a zero border.
+    border = O.border_mask(g)
+    for dk, ref in zip(dirs, d["dJ_inner"]):
+        dk = np.where(border, 0.0, dk)
+        got = float(np.sum(gu * dk))
+        assert abs(got - ref) <= 1e-11 * float(np.sum(np.abs(gu * dk))), (got, ref)
+    # With the border reset every step (the reference's Dirichlet border), the
+    # whole dJ/du0 -- border nodes included -- is the reference's.
+    _, _, gu = O.kheat_adjoint(g, k, traj, target, reset_border=True)
+    for dk, ref in zip(dirs, d["dJ"]):
+        got = float(np.sum(gu * dk))
+        assert abs(got - ref) <= 1e-11 * float(np.sum(np.abs(gu * dk))), (got, ref)
