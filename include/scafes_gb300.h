@@ -591,6 +591,18 @@ int scafes_gpu_adjoint(scafes_handle* h, const double* dJ_du_T, double* dJ_dk,
 int scafes_err_linf_noalloc(const double* u, const double* exact, long long n,
                             double* out, void* stream);
 
+/* No counterpart in the reference.  Page-locked host memory for the host
+ * arrays of uploads and downloads, backed by huge pages: a copy engine
+ * translates every host page it touches, and after a long solve the
+ * translations of a 1 GiB buffer of 64 KB pages are no longer cached (the
+ * first copy measured 45 - 160 ms on GB300 instead of the link's 5.2 ms);
+ * huge pages keep the copies at the link rate.  Allocates at least `bytes`
+ * (rounded up to the huge page size), zeroed; free with scafes_host_free.
+ * The memory is registered with CUDA (cudaHostRegister), so any pointer
+ * into it is pinned host memory for cudaMemcpyAsync. */
+int scafes_host_alloc(size_t bytes, void** out);
+void scafes_host_free(void* p);
+
 /* No counterpart in the reference: measures the FP64 and FP32 FMA issue
  * rates of the current GPU (G op/s) with CUDA events, the compute ceilings
  * the benchmark reports beside the HBM roofline. */

@@ -153,6 +153,35 @@ def _dp(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
+class HostArray:
+    """A float64 numpy array in huge-page pinned host memory
+    (scafes_host_alloc): the host side of uploads and downloads whose copies
+    keep the link rate after long solves.  ``.a`` is the array; close()
+    frees the memory (the array must not be used afterwards)."""
+
+    def __init__(self, shape):
+        L = lib()
+        L.scafes_host_alloc.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+        L.scafes_host_free.argtypes = [C.c_void_p]
+        L.scafes_host_free.restype = None
+        n = int(np.prod(shape))
+        self.p = C.c_void_p()
+        _check(L.scafes_host_alloc(n * 8, C.byref(self.p)))
+        self.a = np.ctypeslib.as_array((C.c_double * n).from_address(self.p.value)).reshape(shape)
+
+    def close(self):
+        if self.p:
+            self.a = None
+            lib().scafes_host_free(self.p)
+            self.p = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 def border_node_count(cfg: "Cfg") -> int:
     n = C.c_longlong()
     _check(lib().scafes_border_node_count(C.byref(cfg), C.byref(n)))

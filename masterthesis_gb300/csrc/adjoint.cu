@@ -25,6 +25,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "adjoint.cuh"
@@ -604,10 +605,8 @@ struct scafes_adj {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     float fwd_ms = 0.f, grad_ms = 0.f;
     long long fwd_steps = 0, adj_steps = 0;
-    // Binomial schedule tables: cost[n][s] and the optimal first split.
-    int tab_n = 0, tab_s = 0;
-    std::vector<long long> cost;
-    std::vector<int> split;
+    // Optimal first splits of the binomial schedule, keyed by (steps, free slots).
+    std::unordered_map<long long, int> split_memo;
     // The pair steps' TMA descriptors: one per state buffer and box shape
     // (u[0], u[1], snapshot slots, lambda; encoded on first use) and the
     // four coefficient fields.
@@ -750,54 +749,54 @@ int from_sweep_type(scafes_adj* a, double* buf) {
     return SCAFES_OK;
 }
 
-// Optimal binomial schedule: cost(n, s) = fewest forward steps that reverse
-// n steps starting from a stored state with s free snapshots;
-// cost(1, s) = 0, cost(n, 0) = n(n-1)/2,
-// cost(n, s) = min_m  m + cost(n - m, s - 1) + cost(m, s).
-void build_schedule(scafes_adj* a, int n, int s) {
-    if (s >= n - 1) return;  // every state gets a slot: split_of answers 1
-    if (n <= a->tab_n && s <= a->tab_s) return;
-    const int N = n, S = s;
-    a->cost.assign((size_t)(N + 1) * (S + 1), 0);
-    a->split.assign((size_t)(N + 1) * (S + 1), 1);
-    auto C = [&](int nn, int ss) -> long long& { return a->cost[(size_t)nn * (S + 1) + ss]; };
-    auto M = [&](int nn, int ss) -> int& { return a->split[(size_t)nn * (S + 1) + ss]; };
-    for (int nn = 1; nn <= N; ++nn) C(nn, 0) = (long long)nn * (nn - 1) / 2;
-    for (int ss = 1; ss <= S; ++ss) {
-        C(1, ss) = 0;
-        for (int nn = 2; nn <= N; ++nn) {
-            if (ss >= nn - 1) {  // a slot for every state: store them all
-                C(nn, ss) = nn - 1;
-                M(nn, ss) = 1;
-                continue;
-            }
-            long long best = -1;
-            int bm = 1;
-            for (int m = 1; m < nn; ++m) {
-                const long long c = m + C(nn - m, ss - 1) + C(m, ss);
-                if (best < 0 || c < best) { best = c; bm = m; }
-            }
-            C(nn, ss) = best;
-            M(nn, ss) = bm;
-        }
+// Optimal binomial schedule.  cost(n, s) = fewest forward steps that
+// reverse n steps starting from a stored state with s free snapshots, the
+// minimum of
+//   cost(1, s) = 0,  cost(n, 0) = n(n-1)/2,
+//   cost(n, s) = min_m  m + cost(n - m, s - 1) + cost(m, s)
+// (advance m steps, store the state, reverse the right part with one slot
+// fewer, then the left part).  Its closed form (Griewank 1992; Griewank &
+// Walther, "Algorithm 799: revolve", ACM TOMS 26(1), 2000): with c = s + 1
+// checkpoints and r the fewest repetitions for which C(c + r, c) >= n,
+//   cost(n, s) = r n - C(c + r, c + 1),
+// which the tests check against the recursion.  The first split of a
+// reversal is an m that attains the minimum, found by a scan and memoised
+// per (n, s): no table grows with the snapshot count, so every slot the
+// caller gives is used.
+long long binomial_cost(long long n, long long s) {
+    if (n <= 1) return 0;
+    if (s <= 0) return n * (n - 1) / 2;
+    if (s >= n - 1) return n - 1;
+    const long long c = s + 1;
+    long long r = 0, beta = 1;  // beta = C(c + r, c)
+    while (beta < n) {
+        ++r;
+        beta = beta * (c + r) / r;
     }
-    a->tab_n = N;
-    a->tab_s = S;
+    return r * n - beta * r / (c + 1);  // C(c + r, c + 1) = C(c + r, c) r / (c + 1)
 }
 
 int split_of(scafes_adj* a, int n, int s) {
     if (s >= n - 1) return 1;
-    return a->split[(size_t)n * (a->tab_s + 1) + s];
+    const long long key = (long long)n * 4194304LL + s;
+    const auto it = a->split_memo.find(key);
+    if (it != a->split_memo.end()) return it->second;
+    const long long best = binomial_cost(n, s);
+    int m_best = 1;
+    for (int m = 1; m < n; ++m)
+        if (m + binomial_cost(n - m, s - 1) + binomial_cost(m, s) == best) {
+            m_best = m;
+            break;
+        }
+    a->split_memo.emplace(key, m_best);
+    return m_best;
 }
 
-// Free snapshot slots the schedule uses: all states when they fit, else at
-// most kMaxSchedSlots (the dynamic program is O(n^2 s); with 128 slots and a
-// few thousand steps the recomputation is already below one extra sweep).
-constexpr int kMaxSchedSlots = 128;
+// Free snapshot slots the schedule uses: all states when they fit, else
+// every slot but the one holding u0.
 int schedule_slots(int n_snap, int n_steps) {
     const int free = n_snap - 1;
-    if (free >= n_steps - 1) return n_steps - 1;
-    return free < kMaxSchedSlots ? free : kMaxSchedSlots;
+    return free >= n_steps - 1 ? n_steps - 1 : free;
 }
 
 struct Rev {
@@ -1057,7 +1056,6 @@ static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const
     if (n != (size_t)a->L.nx * a->L.ny * a->L.nz) return afail(a, SCAFES_ERR_ARG, "%s: wrong size", who);
     if (!a->have_k) return afail(a, SCAFES_ERR_STATE, "%s: set the conductivity first", who);
     const int free = schedule_slots(a->n_snap, n_steps);
-    build_schedule(a, n_steps, free);
     const size_t fb = field_bytes(a);
     int rc = SCAFES_OK;
     if (u0_dev)
@@ -1139,9 +1137,7 @@ extern "C" int scafes_adj_stats(const scafes_adj* a, float* forward_ms, float* g
 
 extern "C" long long scafes_adj_schedule_cost(int n_steps, int n_snapshots) {
     if (n_steps < 1 || n_snapshots < 1) return -1;
-    scafes_adj tmp;
     const int free = schedule_slots(n_snapshots, n_steps);
     if (free >= n_steps - 1) return n_steps;  // one sweep, every state stored
-    build_schedule(&tmp, n_steps, free);
-    return tmp.cost[(size_t)n_steps * (free + 1) + free] + 1;  // + the step that gives u_T
+    return binomial_cost(n_steps, free) + 1;  // + the step that gives u_T
 }

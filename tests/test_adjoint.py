@@ -35,6 +35,26 @@ def test_schedule_cost_matches_brute_force(native, n, snaps):
     assert native.Adjoint.schedule_cost(n, snaps) == brute_cost(n, snaps - 1)
 
 
+def test_schedule_cost_closed_form_against_recursion(native):
+    """The schedule's closed form against the recursion itself on a range
+    of step and snapshot counts (the first tests cover the small corner),
+    and snapshot counts far above the 128 the recursion once capped at."""
+    N, S = 260, 40
+    C = [[0] * (S + 1) for _ in range(N + 1)]
+    for n in range(1, N + 1):
+        C[n][0] = n * (n - 1) // 2
+    for s in range(1, S + 1):
+        for n in range(2, N + 1):
+            C[n][s] = n - 1 if s >= n - 1 else min(m + C[n - m][s - 1] + C[m][s] for m in range(1, n))
+    for s in (1, 2, 3, 7, 19, 40):
+        for n in (2, 3, 17, 64, 129, 200, 260):
+            assert native.Adjoint.schedule_cost(n, s + 1) == C[n][s] + 1 if s < n - 1 else n, (n, s)
+    A = native.Adjoint
+    costs = [A.schedule_cost(2000, s) for s in (45, 128, 256, 512, 1000, 2000)]
+    assert all(a > b for a, b in zip(costs, costs[1:]))
+    assert costs[-1] == 2000 and costs[0] == 4873
+
+
 def test_schedule_cost_store_all_and_monotone(native):
     A = native.Adjoint
     assert A.schedule_cost(2000, 2000) == 2000

@@ -195,3 +195,22 @@ def test_state_errors(gpu):
         assert rc == -1
         rc = M.lib().scafes_gpu_upload(p.h, 99, bad.ctypes.data_as(C.POINTER(C.c_double)), 512)
         assert rc == -1
+
+
+def test_host_alloc_buffers_roundtrip(gpu):
+    """scafes_host_alloc memory (huge-page pinned) as the host side of
+    upload and download: the same results as pageable numpy arrays."""
+    M = gpu
+    n = (40, 33, 29)
+    shape = (n[2], n[1], n[0])
+    u0 = np.random.default_rng(4).uniform(-1.0, 1.0, shape)
+    cfg = M.make_cfg(n, tau=1e-4, heat=(1.0, 1.0, 0.0))
+    with M.HostArray(shape) as hin, M.HostArray(shape) as hout:
+        assert hin.p.value % 4096 == 0 and np.all(hin.a == 0.0)
+        hin.a[...] = u0
+        with M.Plain(cfg) as p:
+            p.upload(M.FIELD_U, hin.a)
+            p.step(7)
+            p.download(M.FIELD_U, hout.a)
+            ref = p.download()
+        assert np.array_equal(hout.a, ref)
