@@ -415,13 +415,14 @@ def smooth_gauss(n, seed):
 def run_adjoint(M, args, dist: Dist):
     """Adjoint workload: flux-form heat with k = exp(0.3 g), g a seeded
     (seed 5) smoothed Gaussian field, 256^3, 2000 steps, u0 = sine mode,
-    target = the forward solve with a second conductivity (seed 6).
-    FP64 sweeps: forward time, gradient time and their ratio for 45
-    snapshots and (when it fits in device memory) for every state stored.
-    Compensated FP32-pair sweeps: the same for 45 snapshots, the gradient's
-    distance to the FP64 gradient, and its ratio to the FP64 forward solve.
-    Both gradients are checked against central differences of J (FP64
-    forward solves) on seeded directions."""
+    target = the forward solve with a second conductivity (seed 6).  For
+    each arithmetic (FP64; compensated FP32 pairs): the forward solve's
+    time, and for 45, 128, 256 and 512 snapshots and (where it fits in
+    device memory) every state stored, the gradient's time, its ratio to
+    the forward solve in the same arithmetic, the forward steps of the
+    binomial schedule and the snapshot memory.  Both gradients are checked
+    against central differences of J (FP64 forward solves) on seeded
+    directions."""
     import torch
     from masterthesis_gb300 import workloads as W
     n = (args.adj_n,) * 3
@@ -432,7 +433,6 @@ def run_adjoint(M, args, dist: Dist):
     u0 = W.heat_sine_noise(n, amp=0.0)
     out = {"workload": f"adjoint heat, k=exp(0.3 g) (seed 5), {n[0]}^3, {T} steps, "
                        f"J=0.5||u_T-u_target||^2, u_target from k seed 6"}
-    free, _ = torch.cuda.mem_get_info()
     field = int(np.prod(n)) * 8
     lups = float(np.prod(n)) * T
 
@@ -452,31 +452,28 @@ def run_adjoint(M, args, dist: Dist):
     with M.Adjoint(n, tau, 2) as a:
         a.set_conductivity(k2)
         target = a.forward(u0, T)
-    f64_ms = forward_ms("f64")
-    out["f64"] = {"forward_ms": f64_ms, "forward_glups": lups / (f64_ms * 1e-3) / 1e9}
-    runs = [("snapshots_45", 45)]
-    if (T + 1) * field + 40 * field < free:
-        runs.append(("store_all", T + 1))
     grads = {}
-    for name, s in runs:
-        J, gk, gu, st = gradient("f64", s)
-        out["f64"][name] = {"gradient_ms": st["gradient_ms"], "cost_ratio": st["gradient_ms"] / f64_ms,
-                            "forward_steps": st["forward_steps"], "adjoint_steps": st["adjoint_steps"],
-                            "snapshot_bytes": s * field, "J": J}
-        grads["f64"] = (J, gk, gu)
-    x2_ms = forward_ms("f32x2")
-    J, gk, gu, st = gradient("f32x2", 45)
-    grads["f32x2"] = (J, gk, gu)
-    J64, gk64, gu64 = grads["f64"]
-    out["f32x2"] = {"forward_ms": x2_ms, "forward_glups": lups / (x2_ms * 1e-3) / 1e9,
-                    "snapshots_45": {"gradient_ms": st["gradient_ms"],
-                                     "cost_ratio_vs_f64_forward": st["gradient_ms"] / f64_ms,
-                                     "cost_ratio_vs_f32x2_forward": st["gradient_ms"] / x2_ms,
+    for prec in ("f64", "f32x2"):
+        f_ms = forward_ms(prec)
+        sec = {"forward_ms": f_ms, "forward_glups": lups / (f_ms * 1e-3) / 1e9, "gradient": {}}
+        torch.cuda.empty_cache()
+        free, _ = torch.cuda.mem_get_info()
+        for snaps in (45, 128, 256, 512, T + 1):
+            if (snaps + 16) * field > free:
+                continue
+            J, gk, gu, st = gradient(prec, snaps)
+            name = "store_all" if snaps == T + 1 else f"snapshots_{snaps}"
+            sec["gradient"][name] = {"gradient_ms": st["gradient_ms"], "cost_ratio": st["gradient_ms"] / f_ms,
                                      "forward_steps": st["forward_steps"], "adjoint_steps": st["adjoint_steps"],
-                                     "snapshot_bytes": 45 * field, "J": J},
-                    "rel_diff_vs_f64": {"J": abs(J - J64) / abs(J64),
-                                        "grad_k": float(np.abs(gk - gk64).max() / np.abs(gk64).max()),
-                                        "grad_u0": float(np.abs(gu - gu64).max() / np.abs(gu64).max())}}
+                                     "snapshot_bytes": snaps * field, "J": J}
+            if snaps == 45:
+                grads[prec] = (J, gk, gu)
+        out[prec] = sec
+    if "f64" in grads and "f32x2" in grads:
+        (J64, gk64, gu64), (J, gk, gu) = grads["f64"], grads["f32x2"]
+        out["f32x2"]["rel_diff_vs_f64"] = {"J": abs(J - J64) / abs(J64),
+                                           "grad_k": float(np.abs(gk - gk64).max() / np.abs(gk64).max()),
+                                           "grad_u0": float(np.abs(gu - gu64).max() / np.abs(gu64).max())}
     # Central differences of J on seeded directions (k relative), FP64.
     errs = {p: [] for p in grads}
     with M.Adjoint(n, tau, 2) as a:

@@ -44,24 +44,35 @@ namespace {
 constexpr int AX = 32, AY = 8;
 
 // Face conductivities K_p[i] = w_p (k_i + k_{i+p}) / 2, zero where i+p is
-// outside the grid.
+// outside the grid, and the diagonal d_i = 1 - sum of the six faces of i.
 __global__ void k_faces(const double* __restrict__ k, double* __restrict__ kx, double* __restrict__ ky,
-                        double* __restrict__ kz, Layout L, double wx, double wy, double wz) {
+                        double* __restrict__ kz, double* __restrict__ dg, Layout L, double wx, double wy,
+                        double wz) {
     const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
     if (x >= L.nx || y >= L.ny) return;
     for (int z = 0; z < L.nz; ++z) {
         const long long o = L.idx(x, y, z);
         const double kc = k[o];
-        kx[o] = x + 1 < L.nx ? wx * 0.5 * (kc + k[o + 1]) : 0.0;
-        ky[o] = y + 1 < L.ny ? wy * 0.5 * (kc + k[o + L.pitch]) : 0.0;
-        kz[o] = z + 1 < L.nz ? wz * 0.5 * (kc + k[o + L.plane]) : 0.0;
+        const double fxp = x + 1 < L.nx ? wx * 0.5 * (kc + k[o + 1]) : 0.0;
+        const double fyp = y + 1 < L.ny ? wy * 0.5 * (kc + k[o + L.pitch]) : 0.0;
+        const double fzp = z + 1 < L.nz ? wz * 0.5 * (kc + k[o + L.plane]) : 0.0;
+        const double fxm = x > 0 ? wx * 0.5 * (k[o - 1] + kc) : 0.0;
+        const double fym = y > 0 ? wy * 0.5 * (k[o - L.pitch] + kc) : 0.0;
+        const double fzm = z > 0 ? wz * 0.5 * (k[o - L.plane] + kc) : 0.0;
+        kx[o] = fxp;
+        ky[o] = fyp;
+        kz[o] = fzp;
+        dg[o] = 1.0 - (((fxp + fxm) + (fyp + fym)) + (fzp + fzm));
     }
 }
 
-// One forward step (inner nodes; border nodes copied).
+// One forward step (inner nodes; border nodes copied), in the diagonal
+// form u'_i = d_i u_i + sum_f K_f u_nb: 7 FP64 operations per node (the
+// flux form takes 12), summed in the order diagonal, +x, -x, +y, -y, +z,
+// -z, which the reverse sweep's recomputation repeats bit for bit.
 __global__ void __launch_bounds__(AX * AY)
 k_forward(const double* __restrict__ u, double* __restrict__ un, const double* __restrict__ kx,
-          const double* __restrict__ ky, const double* __restrict__ kz, Layout L) {
+          const double* __restrict__ ky, const double* __restrict__ kz, const double* __restrict__ dg, Layout L) {
     const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
     if (x >= L.nx || y >= L.ny) return;
     const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
@@ -73,48 +84,68 @@ k_forward(const double* __restrict__ u, double* __restrict__ un, const double* _
             un[o] = uc;
             continue;
         }
-        double v = uc;
-        v = fma(kx[o], u[o + 1] - uc, v);
-        v = fma(-kx[o - 1], uc - u[o - 1], v);
-        v = fma(ky[o], u[o + L.pitch] - uc, v);
-        v = fma(-ky[o - L.pitch], uc - u[o - L.pitch], v);
-        v = fma(kz[o], u[o + L.plane] - uc, v);
-        v = fma(-kz[o - L.plane], uc - u[o - L.plane], v);
+        double v = dg[o] * uc;
+        v = fma(kx[o], u[o + 1], v);
+        v = fma(kx[o - 1], u[o - 1], v);
+        v = fma(ky[o], u[o + L.pitch], v);
+        v = fma(ky[o - L.pitch], u[o - L.pitch], v);
+        v = fma(kz[o], u[o + L.plane], v);
+        v = fma(kz[o - L.plane], u[o - L.plane], v);
         un[o] = v;
     }
 }
 
+// A double as an FP32 pair (split_bits: integer instructions only).
+__device__ __forceinline__ float2 pbits(double d) {
+    const f2 p = split_bits(d);
+    return make_float2(p.hi, p.lo);
+}
+
+// G += (u_nb - u_c) (l_c - l_nb) in FP32-pair arithmetic, renormalised.
+__device__ __forceinline__ float2 gacc(float2 G, float2 unb, float2 uc, float2 lc, float2 lnb);
+
 // One adjoint step: lambda_t from lambda_{t+1} (lam, zero on border nodes)
 // and the forward state u_t; accumulates the face gradients G and, on
-// border nodes, the border part of dJ/du0 (bnd).
+// border nodes, the border part of dJ/du0 (bnd).  lambda' = A^T lambda in
+// the diagonal form (7 FP64 operations per inner node; the matrix is
+// symmetric on the inner nodes).  The face gradients
+//   G_p[i] += (u_{i+p} - u_i)(lambda_i - lambda_{i+p})
+// are FP32 pairs, formed from u and lambda split into pairs with integer
+// instructions (split_bits) and accumulated in pair arithmetic, so that
+// no FP64 operation is spent on them (9 FP64 operations per node in FP64):
+// the step then costs about what a forward step costs.  The centre values'
+// pairs come from the +z neighbour's split of the plane below.
 __global__ void __launch_bounds__(AX * AY)
 k_adjoint(const double* __restrict__ lam, double* __restrict__ lamn, const double* __restrict__ u,
           const double* __restrict__ kx, const double* __restrict__ ky, const double* __restrict__ kz,
-          double* __restrict__ gx, double* __restrict__ gy, double* __restrict__ gz, double* __restrict__ bnd,
-          Layout L) {
+          const double* __restrict__ dg, float2* __restrict__ gx, float2* __restrict__ gy, float2* __restrict__ gz,
+          double* __restrict__ bnd, Layout L) {
     const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
     if (x >= L.nx || y >= L.ny) return;
     const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
     const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
-    for (int z = zb; z < ze; ++z) {
-        const long long o = L.idx(x, y, z);
+    const bool hx = x + 1 < L.nx, hy = y + 1 < L.ny;
+    long long o = L.idx(x, y, zb);
+    float2 puc = pbits(u[o]), plc = pbits(lam[o]);  // pairs of the centre values
+    for (int z = zb; z < ze; ++z, o += L.plane) {
         const bool border = colb || z == 0 || z == L.nz - 1;
+        const bool hz = z + 1 < L.nz;
         const double lc = lam[o];  // zero on border nodes
-        const double uc = u[o];
-        // +x face
-        if (x + 1 < L.nx) gx[o] = fma(u[o + 1] - uc, lc - lam[o + 1], gx[o]);
-        if (y + 1 < L.ny) gy[o] = fma(u[o + L.pitch] - uc, lc - lam[o + L.pitch], gy[o]);
-        if (z + 1 < L.nz) gz[o] = fma(u[o + L.plane] - uc, lc - lam[o + L.plane], gz[o]);
-        double s = 0.0;
-        const double lxp = x + 1 < L.nx ? lam[o + 1] : 0.0, lxm = x > 0 ? lam[o - 1] : 0.0;
-        const double lyp = y + 1 < L.ny ? lam[o + L.pitch] : 0.0, lym = y > 0 ? lam[o - L.pitch] : 0.0;
-        const double lzp = z + 1 < L.nz ? lam[o + L.plane] : 0.0, lzm = z > 0 ? lam[o - L.plane] : 0.0;
+        const double lxp = hx ? lam[o + 1] : 0.0, lxm = x > 0 ? lam[o - 1] : 0.0;
+        const double lyp = hy ? lam[o + L.pitch] : 0.0, lym = y > 0 ? lam[o - L.pitch] : 0.0;
+        const double lzp = hz ? lam[o + L.plane] : 0.0, lzm = z > 0 ? lam[o - L.plane] : 0.0;
         const double kxm = x > 0 ? kx[o - 1] : 0.0, kym = y > 0 ? ky[o - L.pitch] : 0.0;
         const double kzm = z > 0 ? kz[o - L.plane] : 0.0;
+        // Face gradients of the + faces, in pairs.
+        const float2 pua = hz ? pbits(u[o + L.plane]) : make_float2(0.f, 0.f);
+        const float2 pla = pbits(lzp);
+        if (hx) gx[o] = gacc(gx[o], pbits(u[o + 1]), puc, plc, pbits(lxp));
+        if (hy) gy[o] = gacc(gy[o], pbits(u[o + L.pitch]), puc, plc, pbits(lyp));
+        if (hz) gz[o] = gacc(gz[o], pua, puc, plc, pla);
         if (border) {
             // Border rows of the update are the identity: lambda on the border
             // only collects what the inner neighbours pass back.
-            s = fma(kx[o], lxp, s);
+            double s = kx[o] * lxp;
             s = fma(kxm, lxm, s);
             s = fma(ky[o], lyp, s);
             s = fma(kym, lym, s);
@@ -123,15 +154,17 @@ k_adjoint(const double* __restrict__ lam, double* __restrict__ lamn, const doubl
             bnd[o] += s;
             lamn[o] = 0.0;
         } else {
-            double v = lc;
-            v = fma(kx[o], lxp - lc, v);
-            v = fma(kxm, lxm - lc, v);
-            v = fma(ky[o], lyp - lc, v);
-            v = fma(kym, lym - lc, v);
-            v = fma(kz[o], lzp - lc, v);
-            v = fma(kzm, lzm - lc, v);
+            double v = dg[o] * lc;
+            v = fma(kx[o], lxp, v);
+            v = fma(kxm, lxm, v);
+            v = fma(ky[o], lyp, v);
+            v = fma(kym, lym, v);
+            v = fma(kz[o], lzp, v);
+            v = fma(kzm, lzm, v);
             lamn[o] = v;
         }
+        puc = pua;
+        plc = pla;
     }
 }
 
@@ -166,17 +199,19 @@ __global__ void k_terminal(const double* __restrict__ uT, const double* __restri
 }
 
 // dJ/dk_i = sum_p w_p/2 (G_p[i] + G_p[i-p]); dJ/du0 = lambda_0 + border part.
-__global__ void k_finalize(const double* __restrict__ gx, const double* __restrict__ gy,
-                           const double* __restrict__ gz, const double* __restrict__ lam,
+// (FP64 sweeps: the face gradients are FP32 pairs, lambda and bnd FP64.)
+__global__ void k_finalize(const float2* __restrict__ gx, const float2* __restrict__ gy,
+                           const float2* __restrict__ gz, const double* __restrict__ lam,
                            const double* __restrict__ bnd, double* __restrict__ dk, double* __restrict__ du0,
                            Layout L, double wx, double wy, double wz) {
     const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
     if (x >= L.nx || y >= L.ny) return;
+    auto J = [](float2 p) { return join_pair(p.x, p.y); };
     for (int z = 0; z < L.nz; ++z) {
         const long long o = L.idx(x, y, z);
-        double g = 0.5 * wx * (gx[o] + (x > 0 ? gx[o - 1] : 0.0));
-        g += 0.5 * wy * (gy[o] + (y > 0 ? gy[o - L.pitch] : 0.0));
-        g += 0.5 * wz * (gz[o] + (z > 0 ? gz[o - L.plane] : 0.0));
+        double g = 0.5 * wx * (J(gx[o]) + (x > 0 ? J(gx[o - 1]) : 0.0));
+        g += 0.5 * wy * (J(gy[o]) + (y > 0 ? J(gy[o - L.pitch]) : 0.0));
+        g += 0.5 * wz * (J(gz[o]) + (z > 0 ? J(gz[o - L.plane]) : 0.0));
         dk[o] = g;
         du0[o] = lam[o] + bnd[o];
     }
@@ -398,35 +433,60 @@ __device__ __forceinline__ float2 gacc(float2 G, float2 unb, float2 uc, float2 l
 }
 
 // One adjoint step on FP32 pairs: lambda' = A^T lambda (the transposed
-// diagonal form; border rows pass what they receive into bnd) and the face
-// gradients G_f += (u_nb - u_c)(lambda_c - lambda_nb) at the state u_t.
-// The read-only operands are staged through TMA on the forward step's tile
-// (RTX x RTY columns, RZ_ planes, a ring of four planes on four
-// mbarriers).  Per plane one mbarrier covers six boxes: lambda with a
-// one-node halo (x from x0-2), u with the +x / +y neighbours (x0 .. x0+33,
-// y0 .. y0+8), the x faces from x0-2, the y faces from row y0-1, the z
-// faces and the diagonal.  lambda and the z face of the plane below come
-// from register queues; the gradient accumulators are read with plain
-// loads one plane ahead and written back in place.  Out-of-range box
-// elements read as zero: a neighbour outside the grid contributes nothing.
-// Every wait is bounded (status word, drain, return).
+// diagonal form; border rows pass what they receive into bnd) and the
+// conductivity gradient at the state u_t, accumulated per node:
+//   g_i -= sum_p w_p/2 [ P_p(i) + P_p(i-p) ],
+//   P_p(j) = (u_{j+p} - u_j)(lambda_{j+p} - lambda_j),
+// the two faces of node i along each axis (dJ/dk_i directly; one pair per
+// node read and written instead of three face accumulators: 72 bytes per
+// node instead of 104).  A face to a node outside the grid or between two
+// border nodes contributes nothing: lambda is zero there.
+// The operands are staged through TMA on the forward step's tile (RTX x
+// RTY columns, RZ_ planes, a ring of four planes on four mbarriers).  Per
+// plane one mbarrier covers six boxes: lambda and u with a one-node halo
+// (x from x0-2), the x faces from x0-2, the y faces from row y0-1, the z
+// faces and the diagonal.  lambda, u and the z face of the plane below and
+// the z-face product of the plane below come from register queues; g is
+// read with plain loads one plane ahead and written in place.
+// Out-of-range box elements read as zero.  Every wait is bounded (status
+// word, drain, return).
 constexpr int RTX = FTX, RTY = FTY, RZ_ = FZ_, RNS = FNS;
-constexpr int RLW = FUW, RLH = FUH;                       // lambda box: the forward's u box
-constexpr int RUW = RTX + 2, RUH = RTY + 1;               // u box: x0 .. x0+33, y0 .. y0+8
-constexpr int RO_L = 0, RO_U = pad16(RLW * RLH), RO_X = RO_U + pad16(RUW * RUH);
+constexpr int RLW = FUW, RLH = FUH;                       // lambda and u boxes: the forward's u box
+constexpr int RO_L = 0, RO_U = pad16(RLW * RLH), RO_X = RO_U + pad16(RLW * RLH);
 constexpr int RO_Y = RO_X + pad16(FXW * FXH), RO_Z = RO_Y + pad16(FYW * FYH), RO_D = RO_Z + pad16(FKW * FKH);
 constexpr int RSLOT = RO_D + pad16(FKW * FKH);
-constexpr uint32_t RTX_BYTES = (uint32_t)(RLW * RLH + RUW * RUH + FXW * FXH + FYW * FYH + 2 * FKW * FKH) * 8u;
+constexpr uint32_t RTX_BYTES = (uint32_t)(2 * RLW * RLH + FXW * FXH + FYW * FYH + 2 * FKW * FKH) * 8u;
 constexpr size_t RSMEM = (size_t)RNS * RSLOT * 8 + RNS * 8;
 static_assert(RSLOT * 8 % 128 == 0 && RO_U * 8 % 128 == 0 && RO_X * 8 % 128 == 0, "TMA destinations 128-byte aligned");
-static_assert(RUW * 8 % 16 == 0, "TMA box rows are multiples of 16 bytes");
+
+// (u_b - u_a)(l_b - l_a) as an unnormalised pair.
+__device__ __forceinline__ f2 pface(float2 ua, float2 ub, float2 la, float2 lb) {
+    const f2 du = psub(ub, ua);
+    const f2 dl = psub(lb, la);
+    const float p = du.hi * dl.hi;
+    float e = fmaf(du.hi, dl.hi, -p);
+    e = fmaf(du.hi, dl.lo, e);
+    e = fmaf(du.lo, dl.hi, e);
+    return {p, e};
+}
+
+// c * (a + b) for a pair constant c (an axis weight w_p / 2), unnormalised.
+__device__ __forceinline__ f2 pscale2(float2 c, f2 a, f2 b) {
+    f2 s = a;
+    pacc(s, b);
+    const float p = c.x * s.hi;
+    float e = fmaf(c.x, s.hi, -p);
+    e = fmaf(c.x, s.lo, e);
+    e = fmaf(c.y, s.hi, e);
+    return {p, e};
+}
 
 __global__ void __launch_bounds__(RTX * RTY)
 k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__ CUtensorMap tu,
                  const __grid_constant__ CUtensorMap tkx, const __grid_constant__ CUtensorMap tky,
                  const __grid_constant__ CUtensorMap tkz, const __grid_constant__ CUtensorMap tdg,
-                 float2* __restrict__ lamn, float2* __restrict__ gx, float2* __restrict__ gy, float2* __restrict__ gz,
-                 float2* __restrict__ bnd, Layout L, int* __restrict__ status) {
+                 float2* __restrict__ lamn, float2* __restrict__ g, float2* __restrict__ bnd, float2 hx2,
+                 float2 hy2, float2 hz2, Layout L, int* __restrict__ status) {
     extern __shared__ __align__(128) float2 rsm[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(rsm + RNS * RSLOT);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * RTX + tx;
@@ -445,7 +505,7 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
         float2* d = rsm + s * RSLOT;
         scafes::mbar_arrive_expect_tx(&bar[s], RTX_BYTES);
         scafes::tma_load_3d(d + RO_L, &tl, x0 - 2, y0 - 1, z, &bar[s]);
-        scafes::tma_load_3d(d + RO_U, &tu, x0, y0, z, &bar[s]);
+        scafes::tma_load_3d(d + RO_U, &tu, x0 - 2, y0 - 1, z, &bar[s]);
         scafes::tma_load_3d(d + RO_X, &tkx, x0 - 2, y0, z, &bar[s]);
         scafes::tma_load_3d(d + RO_Y, &tky, x0, y0 - 1, z, &bar[s]);
         scafes::tma_load_3d(d + RO_Z, &tkz, x0, y0, z, &bar[s]);
@@ -465,20 +525,18 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
     const int x = x0 + tx, y = y0 + ty;
     const bool live = x < L.nx && y < L.ny;
     const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
-    const int bl = (ty + 1) * RLW + tx + 2, bu = ty * RUW + tx, bx = ty * FXW + tx + 2, by = (ty + 1) * FYW + tx;
+    const int bl = (ty + 1) * RLW + tx + 2, bx = ty * FXW + tx + 2, by = (ty + 1) * FYW + tx;
     const int bk = ty * FKW + tx;
     const float2 zero = make_float2(0.f, 0.f);
     long long o = live ? L.idx(x, y, z0) : 0;
-    float2 gxn = zero, gyn = zero, gzn = zero;
-    if (live) {
-        gxn = gx[o];
-        gyn = gy[o];
-        gzn = gz[o];
-    }
+    float2 gn = live ? g[o] : zero;
     bool ok = wait(0);
     float2 lb = z0 > 0 ? rsm[RO_L + bl] : zero;  // plane z0-1
+    float2 ub = z0 > 0 ? rsm[RO_U + bl] : zero;
     float2 kzb = z0 > 0 ? rsm[RO_Z + bk] : zero;
     ok = wait(1) && ok;
+    // The z-face product of the plane below (face z-1 | z).
+    f2 pzb = z0 > 0 ? pface(ub, rsm[RSLOT + RO_U + bl], lb, rsm[RSLOT + RO_L + bl]) : f2{0.f, 0.f};
     int issued = RNS - 1;
     for (int z = z0; z < z1; ++z, o += L.plane) {
         const int jc = z - z0 + 1;  // input plane of z
@@ -491,28 +549,28 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
             issue(jc + 3);
             issued = jc + 3;
         }
-        const float2 gxc = gxn, gyc = gyn, gzc = gzn;
-        if (live && z + 1 < z1) {
-            gxn = gx[o + L.plane];
-            gyn = gy[o + L.plane];
-            gzn = gz[o + L.plane];
-        }
+        const float2 gc = gn;
+        if (live && z + 1 < z1) gn = g[o + L.plane];
         ok = wait(jc + 1) && ok;  // plane z+1
         const float2* sc = rsm + (jc & (RNS - 1)) * RSLOT;
         const float2* sa = rsm + ((jc + 1) & (RNS - 1)) * RSLOT;
         const bool top = z + 1 < L.nz;
         const float2 la = top ? sa[RO_L + bl] : zero;
-        const float2 lc = sc[RO_L + bl];
+        const float2 ua = top ? sa[RO_U + bl] : zero;
+        const float2 lc = sc[RO_L + bl], uc = sc[RO_U + bl];
         const float2 kzc = sc[RO_Z + bk];
+        const f2 pza = pface(uc, ua, lc, la);  // face z | z+1
         if (live) {
-            const float2 ua = top ? sa[RO_U + bu] : zero;
-            const float2 uc = sc[RO_U + bu];
             const bool border = colb || z == 0 || z == L.nz - 1;
             const float2 lxp = sc[RO_L + bl + 1], lxm = sc[RO_L + bl - 1];
             const float2 lyp = sc[RO_L + bl + RLW], lym = sc[RO_L + bl - RLW];
-            if (x + 1 < L.nx) gx[o] = gacc(gxc, sc[RO_U + bu + 1], uc, lc, lxp);
-            if (y + 1 < L.ny) gy[o] = gacc(gyc, sc[RO_U + bu + RUW], uc, lc, lyp);
-            if (top) gz[o] = gacc(gzc, ua, uc, lc, la);
+            // dJ/dk_i: the two faces along each axis.
+            f2 gk = pscale2(hx2, pface(uc, sc[RO_U + bl + 1], lc, lxp), pface(sc[RO_U + bl - 1], uc, lxm, lc));
+            pacc(gk, pscale2(hy2, pface(uc, sc[RO_U + bl + RLW], lc, lyp), pface(sc[RO_U + bl - RLW], uc, lym, lc)));
+            pacc(gk, pscale2(hz2, pza, pzb));
+            f2 gsum{gc.x, gc.y};
+            pacc(gsum, {-gk.hi, -gk.lo});
+            g[o] = pnorm(gsum);
             const float2 kxp = sc[RO_X + bx], kyp = sc[RO_Y + by];
             const float2 kxm = sc[RO_X + bx - 1], kym = sc[RO_Y + by - FYW];
             f2 acc = border ? f2{0.f, 0.f} : pmul(sc[RO_D + bk], lc);
@@ -532,7 +590,9 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
             }
         }
         lb = lc;
+        ub = uc;
         kzb = kzc;
+        pzb = pza;
     }
     if (!__syncthreads_and(ok)) fail(issued);
 }
@@ -566,18 +626,14 @@ __global__ void k_terminal_x2(const float2* __restrict__ uT, const double* __res
     if (t == 0) part[blockIdx.y * gridDim.x + blockIdx.x] = sh[0];
 }
 
-__global__ void k_finalize_x2(const float2* __restrict__ gx, const float2* __restrict__ gy,
-                              const float2* __restrict__ gz, const float2* __restrict__ lam,
+__global__ void k_finalize_x2(const float2* __restrict__ g, const float2* __restrict__ lam,
                               const float2* __restrict__ bnd, double* __restrict__ dk, double* __restrict__ du0,
-                              Layout L, double wx, double wy, double wz) {
+                              Layout L) {
     const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
     if (x >= L.nx || y >= L.ny) return;
     for (int z = 0; z < L.nz; ++z) {
         const long long o = L.idx(x, y, z);
-        double g = 0.5 * wx * (pjoin(gx[o]) + (x > 0 ? pjoin(gx[o - 1]) : 0.0));
-        g += 0.5 * wy * (pjoin(gy[o]) + (y > 0 ? pjoin(gy[o - L.pitch]) : 0.0));
-        g += 0.5 * wz * (pjoin(gz[o]) + (z > 0 ? pjoin(gz[o - L.plane]) : 0.0));
-        dk[o] = g;
+        dk[o] = pjoin(g[o]);
         du0[o] = pjoin(lam[o]) + pjoin(bnd[o]);
     }
 }
@@ -594,7 +650,7 @@ struct scafes_adj {
     // Every field holds 8 bytes per node: FP64 values, or FP32 pairs when
     // precision is SCAFES_PREC_F32X2.
     double *kx = nullptr, *ky = nullptr, *kz = nullptr;
-    double *dg = nullptr;      // diagonal of the pair form (allocated on demand)
+    double *dg = nullptr;      // diagonal of the update, d_i = 1 - sum of i's faces
     double *u[2] = {nullptr, nullptr}, *lam[2] = {nullptr, nullptr};
     double *gx = nullptr, *gy = nullptr, *gz = nullptr, *bnd = nullptr;
     double *snaps = nullptr;   // n_snap fields
@@ -657,8 +713,8 @@ int pair_map(scafes_adj* a, CUtensorMap* m, const void* base, int bw, int bh) {
 }
 
 // State boxes: a one-node halo (the forward step's u, the adjoint step's
-// lambda) or the +x / +y neighbours only (the adjoint step's u).
-enum { BOX_HALO = 0, BOX_UPPER = 1 };
+// lambda and u).
+enum { BOX_HALO = 0 };
 
 // Copies the descriptor of `src` for `box` into *out (the cache may grow,
 // so no pointer into it is handed out).
@@ -669,7 +725,7 @@ int state_map(scafes_adj* a, const double* src, int box, CUtensorMap* out) {
             return SCAFES_OK;
         }
     scafes_adj::StateMap m{src, box, {}};
-    if (int rc = box == BOX_HALO ? pair_map(a, &m.map, src, FUW, FUH) : pair_map(a, &m.map, src, RUW, RUH))
+    if (int rc = pair_map(a, &m.map, src, FUW, FUH))
         return rc;
     a->umaps.push_back(m);
     *out = m.map;
@@ -717,7 +773,7 @@ int fwd(scafes_adj* a, const double* src, double* dst) {
         const int rc = fwd_x2_tma(a, src, dst);
         if (rc) return rc;
     } else
-        k_forward<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(src, dst, a->kx, a->ky, a->kz, a->L);
+        k_forward<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(src, dst, a->kx, a->ky, a->kz, a->dg, a->L);
     ATRY(a, cudaGetLastError());
     ++a->fwd_steps;
     return SCAFES_OK;
@@ -821,14 +877,19 @@ int adj_step(Rev& R, const double* u_t) {
         if (int rc = coefficient_maps(a)) return rc;
         CUtensorMap ml, mu;
         if (int rc = state_map(a, a->lam[R.cur], BOX_HALO, &ml)) return rc;
-        if (int rc = state_map(a, u_t, BOX_UPPER, &mu)) return rc;
+        if (int rc = state_map(a, u_t, BOX_HALO, &mu)) return rc;
         const dim3 grid((a->L.nx + RTX - 1) / RTX, (a->L.ny + RTY - 1) / RTY, (a->L.nz + RZ_ - 1) / RZ_);
+        auto half = [](double w) {
+            const f2 p = split_double(0.5 * w);
+            return make_float2(p.hi, p.lo);
+        };
         k_adjoint_x2_tma<<<grid, dim3(RTX, RTY), RSMEM, a->stream>>>(
             ml, mu, a->cmaps[0], a->cmaps[1], a->cmaps[2], a->cmaps[3], P2(a->lam[R.cur ^ 1]), P2(a->gx),
-            P2(a->gy), P2(a->gz), P2(a->bnd), a->L, a->status);
+            P2(a->bnd), half(a->w[0]), half(a->w[1]), half(a->w[2]), a->L, a->status);
     } else
         k_adjoint<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(a->lam[R.cur], a->lam[R.cur ^ 1], u_t, a->kx, a->ky,
-                                                               a->kz, a->gx, a->gy, a->gz, a->bnd, a->L);
+                                                               a->kz, a->dg, P2(a->gx), P2(a->gy), P2(a->gz), a->bnd,
+                                                               a->L);
     ATRY(a, cudaGetLastError());
     R.cur ^= 1;
     ++a->adj_steps;
@@ -936,8 +997,8 @@ extern "C" int scafes_adj_create(const int n_nodes[3], const double coord_first[
     cudaError_t e = cudaSuccess;
     if (stream) a->stream = (cudaStream_t)stream;
     else { e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking); a->own_stream = true; }
-    double** fields[] = {&a->kx, &a->ky, &a->kz, &a->u[0], &a->u[1], &a->lam[0], &a->lam[1], &a->gx, &a->gy,
-                         &a->gz, &a->bnd, &a->work};
+    double** fields[] = {&a->kx, &a->ky, &a->kz, &a->dg, &a->u[0], &a->u[1], &a->lam[0], &a->lam[1], &a->gx,
+                         &a->gy, &a->gz, &a->bnd, &a->work};
     for (double** f : fields)
         if (e == cudaSuccess) e = cudaMalloc(f, fb);
     if (e == cudaSuccess) e = cudaMalloc(&a->snaps, fb * (size_t)n_snapshots);
@@ -965,16 +1026,6 @@ extern "C" int scafes_adj_set_precision(scafes_adj* a, int precision) {
     if (!a) return afail(nullptr, SCAFES_ERR_ARG, "scafes_adj_set_precision: NULL handle");
     if (precision != SCAFES_PREC_F64 && precision != SCAFES_PREC_F32X2)
         return afail(a, SCAFES_ERR_UNSUPPORTED, "scafes_adj_set_precision: precision %d (F64 or F32X2 only)", precision);
-    if (precision == SCAFES_PREC_F32X2 && !a->dg) {
-        cudaError_t e = cudaMalloc(&a->dg, field_bytes(a));
-        if (e == cudaSuccess) e = cudaMemsetAsync(a->dg, 0, field_bytes(a), a->stream);
-        if (e != cudaSuccess) {
-            cudaFree(a->dg);
-            a->dg = nullptr;
-            return afail(a, e == cudaErrorMemoryAllocation ? SCAFES_ERR_NOMEM : SCAFES_ERR_CUDA,
-                         "scafes_adj_set_precision: %s", cudaGetErrorString(e));
-        }
-    }
     a->precision = precision;
     a->have_k = false;
     return SCAFES_OK;
@@ -993,8 +1044,8 @@ int prepare_faces(scafes_adj* a) {
         k_prep_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->work, P2(a->kx), P2(a->ky), P2(a->kz), P2(a->dg),
                                                                a->L, a->w[0], a->w[1], a->w[2]);
     else
-        k_faces<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->work, a->kx, a->ky, a->kz, a->L, a->w[0], a->w[1],
-                                                             a->w[2]);
+        k_faces<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->work, a->kx, a->ky, a->kz, a->dg, a->L, a->w[0],
+                                                             a->w[1], a->w[2]);
     ATRY(a, cudaGetLastError());
     ATRY(a, cudaStreamSynchronize(a->stream));
     a->have_k = true;
@@ -1074,12 +1125,12 @@ static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const
     Rev R{a, a->work, n_steps, 0, false, a->part, seed, reset_border};
     if ((rc = reverse(R, 0, n_steps, 0, free))) return rc;
     if (pairs(a))
-        k_finalize_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(a->gx), P2(a->gy), P2(a->gz), P2(a->lam[R.cur]),
-                                                                   P2(a->bnd), a->u[0], a->u[1], a->L, a->w[0],
-                                                                   a->w[1], a->w[2]);
+        k_finalize_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(a->gx), P2(a->lam[R.cur]), P2(a->bnd),
+                                                                   a->u[0], a->u[1], a->L);
     else
-        k_finalize<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(a->gx, a->gy, a->gz, a->lam[R.cur], a->bnd, a->u[0],
-                                                                a->u[1], a->L, a->w[0], a->w[1], a->w[2]);
+        k_finalize<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(a->gx), P2(a->gy), P2(a->gz), a->lam[R.cur],
+                                                                a->bnd, a->u[0], a->u[1], a->L, a->w[0], a->w[1],
+                                                                a->w[2]);
     ATRY(a, cudaGetLastError());
     ATRY(a, cudaEventRecord(a->e1, a->stream));
     std::vector<double> part(a->part_n);
