@@ -469,6 +469,40 @@ int scafes_mf_last_ms(const scafes_mf* h, float* ms);
 const char* scafes_mf_last_error(const scafes_mf* h);
 void scafes_mf_destroy(scafes_mf* h);
 
+/* ---- linear multi-field stencils, optional leapfrog phase --------------------
+ *
+ * The device form of update callbacks that couple several unknown fields,
+ * recorded by the drop-in Problem from updateInner/updateBorder and, for a
+ * leapfrog problem, updateInner2/updateBorder2 (src/ScaFES_Problem.hpp:
+ * 2604-2619 and 2875-2918: the second phase runs on the first phase's
+ * result after a pointer swap):
+ *   u_new[f](i) = cst + sum_k w_k * u_old[src_k](i + (dx_k, dy_k, dz_k)),
+ * offsets in {-1, 0, 1}, one rule per (phase, field, node class): class 0
+ * the inner nodes, classes 1..63 the border nodes by the faces they lie on
+ * (the bit order of scafes_border_form), one border layer.  A field a
+ * phase leaves alone needs the rule u_new[f] = u_old[f] (the reference
+ * copies every node before the update, :5078-5082).  FP64.  One step runs
+ * every phase once; a rule missing at the first step is SCAFES_ERR_STATE. */
+#define SCAFES_LIN_MAX_FIELDS 8
+#define SCAFES_LIN_MAX_TERMS 32
+typedef struct scafes_lin_term {
+    int src;         /* source field */
+    int dx, dy, dz;  /* neighbour offset, each in {-1, 0, 1} */
+    double w;        /* weight */
+} scafes_lin_term;
+typedef struct scafes_lin scafes_lin;
+int scafes_lin_create(const int n_nodes[3], int n_fields, int n_phases, void* stream, scafes_lin** out);
+/* phase 1 or 2; cls 0 (inner) .. 63; n_terms <= SCAFES_LIN_MAX_TERMS.  A
+ * term may not reach beyond a face its class lies on. */
+int scafes_lin_set_rule(scafes_lin* h, int phase, int field, int cls, const scafes_lin_term* terms,
+                        int n_terms, double cst);
+int scafes_lin_upload(scafes_lin* h, int field, const double* host, size_t n);
+int scafes_lin_download(scafes_lin* h, int field, double* host, size_t n);
+int scafes_lin_step(scafes_lin* h, int n_steps);
+int scafes_lin_last_ms(const scafes_lin* h, float* ms);
+const char* scafes_lin_last_error(const scafes_lin* h);
+void scafes_lin_destroy(scafes_lin* h);
+
 /* ---- wider stencils, one width per field -----------------------------------
  *
  * The averaging update of the reference's per-field stencil-width test,

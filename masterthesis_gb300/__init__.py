@@ -752,3 +752,89 @@ class MultiField:
             self.close()
         except Exception:
             pass
+
+
+class LinTerm(C.Structure):
+    """Mirror of ``struct scafes_lin_term``."""
+    _fields_ = [("src", C.c_int), ("dx", C.c_int), ("dy", C.c_int), ("dz", C.c_int), ("w", C.c_double)]
+
+
+LIN_MAX_FIELDS = 8
+LIN_MAX_TERMS = 32
+
+
+def _lin_bind(L):
+    if getattr(L, "_lin_set", False):
+        return
+    vp, dp = C.c_void_p, C.POINTER(C.c_double)
+    L.scafes_lin_create.argtypes = [C.c_int * 3, C.c_int, C.c_int, vp, C.POINTER(vp)]
+    L.scafes_lin_set_rule.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(LinTerm), C.c_int, C.c_double]
+    L.scafes_lin_upload.argtypes = [vp, C.c_int, dp, C.c_size_t]
+    L.scafes_lin_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
+    L.scafes_lin_step.argtypes = [vp, C.c_int]
+    L.scafes_lin_last_ms.argtypes = [vp, C.POINTER(C.c_float)]
+    L.scafes_lin_last_error.argtypes = [vp]
+    L.scafes_lin_last_error.restype = C.c_char_p
+    L.scafes_lin_destroy.argtypes = [vp]
+    L.scafes_lin_destroy.restype = None
+    L._lin_set = True
+
+
+class Linear:
+    """Linear multi-field stencil rules with an optional leapfrog second
+    phase (scafes_lin_*): the device form the drop-in Problem records from
+    callbacks that couple several unknown fields.  Rules are set per
+    (phase 1|2, field, node class 0..63); a term is (src, dx, dy, dz, w)."""
+
+    def __init__(self, n, n_fields, n_phases=1, stream=None):
+        L = lib()
+        _lin_bind(L)
+        self.shape = (n[2], n[1], n[0])
+        h = C.c_void_p()
+        rc = L.scafes_lin_create((C.c_int * 3)(*n), n_fields, n_phases, stream, C.byref(h))
+        if rc != 0:
+            raise ScafesError(rc, (L.scafes_last_error() or b"").decode())
+        self.h = h
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise ScafesError(rc, (lib().scafes_lin_last_error(self.h) or b"").decode())
+
+    def set_rule(self, phase, field, cls, terms, cst=0.0):
+        arr = (LinTerm * max(1, len(terms)))(*[LinTerm(int(s), int(x), int(y), int(z), float(w))
+                                               for s, x, y, z, w in terms])
+        self._chk(lib().scafes_lin_set_rule(self.h, phase, field, cls, arr, len(terms), float(cst)))
+
+    def upload(self, field, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        self._chk(lib().scafes_lin_upload(self.h, field, _dp(a), a.size))
+
+    def download(self, field):
+        a = np.empty(self.shape)
+        self._chk(lib().scafes_lin_download(self.h, field, _dp(a), a.size))
+        return a
+
+    def step(self, n_steps):
+        self._chk(lib().scafes_lin_step(self.h, n_steps))
+
+    def last_ms(self):
+        v = C.c_float()
+        self._chk(lib().scafes_lin_last_ms(self.h, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.h:
+            lib().scafes_lin_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -170,6 +170,26 @@ public:
             std::fwrite(&n, sizeof(n), 1, f);
             if (n > 0) std::fwrite(v, sizeof(double), (std::size_t)n, f);
         };
+        if (mLinear) {
+            // Multi-field rules: per (phase, field, class) the term count,
+            // the constant and (src, dx, dy, dz, w) per term.
+            std::vector<double> r;
+            for (std::size_t s = 0; s < mLinTerms.size(); ++s) {
+                r.push_back((double)mLinTerms[s].size());
+                r.push_back(mLinCst[s]);
+                for (const auto& t : mLinTerms[s]) {
+                    const double q[5] = {(double)t.src, (double)t.dx, (double)t.dy, (double)t.dz, t.w};
+                    r.insert(r.end(), q, q + 5);
+                }
+            }
+            const Grid<DIM>& g = mGG.discreteDomain();
+            const double cfgv[] = {(double)g.nNodes(0), (double)g.nNodes(1), (double)g.nNodes(2),
+                                   (double)mUnknownIdx.size(), (double)mLinPhases};
+            put("lin_cfg", cfgv, 5);
+            put("lin_rules", r.data(), (long long)r.size());
+            if (std::fclose(f) != 0) throw std::runtime_error("ScaFES::Problem: cannot write " + path);
+            return;
+        }
         const scafes_cfg& c = mCfg;
         const double cfgv[] = {(double)c.n_nodes[0], (double)c.n_nodes[1], (double)c.n_nodes[2],
                                c.coord_first[0], c.coord_first[1], c.coord_first[2],
@@ -236,7 +256,7 @@ private:
     }
 
     // Records one update callback at node n for time step t.
-    template <bool BORDER>
+    template <bool BORDER, int PHASE = 1>
     std::vector<gpu::Sym> record(const ScaFES_IntNtuple& n, int t, std::string& err) {
         gpu::Recorder<DIM> rec;
         rec.centre = n;
@@ -255,8 +275,13 @@ private:
         OWNPRBLM* self = static_cast<OWNPRBLM*>(this);
         gpu::comparison_on_unknown() = false;
         gpu::converted_unknown() = false;
-        if (BORDER) self->template updateBorder<gpu::Sym>(vNew, vOld, n, t);
-        else self->template updateInner<gpu::Sym>(vNew, vOld, n, t);
+        if (PHASE == 2) {
+            if (BORDER) self->template updateBorder2<gpu::Sym>(vNew, vOld, n, t);
+            else self->template updateInner2<gpu::Sym>(vNew, vOld, n, t);
+        } else {
+            if (BORDER) self->template updateBorder<gpu::Sym>(vNew, vOld, n, t);
+            else self->template updateInner<gpu::Sym>(vNew, vOld, n, t);
+        }
         err = rec.error;
         if (err.empty() && gpu::comparison_on_unknown())
             err = "update callback branches on the value of an unknown (not a linear stencil)";
@@ -504,6 +529,17 @@ private:
     }
 
     void prepareDevice();
+    // Several unknown fields or a leapfrog second phase: the linear
+    // multi-field rules of scafes_lin_* (one per phase, field and node class).
+    void prepareLinear();
+    void runLinear();
+    std::string linearRule(const gpu::Sym& s, const std::vector<Affine>& aff, std::vector<scafes_lin_term>& terms,
+                           double& cst) const;
+    bool mLinear = false;
+    int mLinPhases = 1;
+    // [phase][field][class] -> terms, constant
+    std::vector<std::vector<scafes_lin_term>> mLinTerms;
+    std::vector<double> mLinCst;
 
     // What prepareDevice hands to the device run.
     bool mPrepared = false;
@@ -527,10 +563,10 @@ template <class OWNPRBLM, typename CT, std::size_t DIM>
 void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     using clock = std::chrono::steady_clock;
     if (mPrepared) return;
-    if (mUseLeapfrog)
-        throw std::runtime_error("ScaFES::Problem: leapfrog problems are not mapped to a device kernel yet");
-    if (mUnknownIdx.size() != 1)
-        throw std::runtime_error("ScaFES::Problem: the device path takes exactly one unknown data field");
+    if (mUseLeapfrog || mUnknownIdx.size() != 1) {
+        prepareLinear();
+        return;
+    }
     const std::size_t nf = mNames.size();
     const Grid<DIM>& g = mGG.discreteDomain();
 
@@ -904,11 +940,197 @@ void Problem<OWNPRBLM, CT, DIM>::prepareDevice() {
     mPrepared = true;
 }
 
+// A recorded form as a rule of the multi-field linear kernel, or why not.
+template <class OWNPRBLM, typename CT, std::size_t DIM>
+std::string Problem<OWNPRBLM, CT, DIM>::linearRule(const gpu::Sym& s, const std::vector<Affine>& aff,
+                                                   std::vector<scafes_lin_term>& terms, double& cst) const {
+    if (s.bad()) return "not linear in the unknowns: " + describe(s);
+    terms.clear();
+    cst = s.constant();
+    for (const auto& kv : s.terms()) {
+        const auto& k = kv.first;
+        if (k.kind == 2) return "a power of an unknown: " + describe(s);
+        if (k.kind == 1) {
+            if (aff[k.a].zero) continue;  // a known field that is 0 everywhere
+            return "a known field (" + mNames[k.a] + ") in a multi-field update: " + describe(s);
+        }
+        if (std::abs(k.b) > 1 || std::abs(k.c) > 1 || std::abs(k.d) > 1)
+            return "a neighbour beyond one node: " + describe(s);
+        terms.push_back(scafes_lin_term{k.a, k.b, k.c, k.d, kv.second});
+    }
+    if ((int)terms.size() > SCAFES_LIN_MAX_TERMS) return "more terms than the device rule holds: " + describe(s);
+    return std::string();
+}
+
+template <class OWNPRBLM, typename CT, std::size_t DIM>
+void Problem<OWNPRBLM, CT, DIM>::prepareLinear() {
+    const std::size_t nu = mUnknownIdx.size();
+    if (nu > SCAFES_LIN_MAX_FIELDS)
+        throw std::runtime_error("ScaFES::Problem: more unknown fields than the multi-field kernel takes");
+    if (mParams.nLayersAtBorder() != 1)
+        throw std::runtime_error("ScaFES::Problem: the multi-field path takes one border layer");
+    for (std::size_t u = 0; u < nu; ++u)
+        if ((std::size_t)mUnknownIdx[u] < mWriteToFile.size() && mWriteToFile[mUnknownIdx[u]] != WriteHowOften::NEVER)
+            throw std::runtime_error("ScaFES::Problem: field output is not available on the multi-field path");
+    const Grid<DIM>& g = mGG.discreteDomain();
+    const std::size_t nf = mNames.size();
+    // Known fields at steps 0 and 1 (a multi-field update may only read
+    // known fields that are 0 everywhere).
+    evalKnownAt(0);
+    std::vector<CT> k0 = mKnownNewStore;
+    evalKnownAt(1);
+    std::vector<CT> k1 = mKnownNewStore;
+    std::vector<Affine> aff;
+    fitAffine(aff, k0, k1);
+    // Initial iterate of every unknown field (initInner/initBorder).
+    std::copy(k0.begin(), k0.end(), mKnownNewStore.begin());
+    mKnownOldStore = k0;
+    {
+        OWNPRBLM* self = static_cast<OWNPRBLM*>(this);
+        for (auto& df : mVectUnknownDfsDomNew) df.time() = (CT)time(0);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static)
+#endif
+        for (long long m = 0; m < mN; ++m) {
+            const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
+            if (isBorder(n)) self->template initBorder<CT>(mVectUnknownDfsDomNew, mVectParamsCurr, n, 0);
+            else self->template initInner<CT>(mVectUnknownDfsDomNew, mVectParamsCurr, n, 0);
+        }
+    }
+    std::copy(k1.begin(), k1.end(), mKnownNewStore.begin());
+    (void)nf;
+    mLinPhases = mUseLeapfrog ? 2 : 1;
+    const std::size_t nrules = (std::size_t)mLinPhases * nu * SCAFES_BORDER_CLASSES;
+    mLinTerms.assign(nrules, {});
+    mLinCst.assign(nrules, 0.0);
+    std::vector<bool> seen(nrules, false);
+    std::string err;
+    auto slot = [&](int ph, std::size_t f, int cls) { return ((std::size_t)ph * nu + f) * SCAFES_BORDER_CLASSES + cls; };
+    auto take = [&](int ph, int cls, const std::vector<gpu::Sym>& out, const char* where) {
+        for (std::size_t f = 0; f < nu; ++f) {
+            std::vector<scafes_lin_term> terms;
+            double cst = 0.0;
+            const std::string why = linearRule(out[f], aff, terms, cst);
+            if (!why.empty())
+                throw std::runtime_error(std::string("ScaFES::Problem: ") + where + " of field " +
+                                         mNames[mUnknownIdx[f]] + ": " + why);
+            const std::size_t s = slot(ph, f, cls);
+            if (!seen[s]) {
+                mLinTerms[s] = terms;
+                mLinCst[s] = cst;
+                seen[s] = true;
+                continue;
+            }
+            bool eq = cst == mLinCst[s] && terms.size() == mLinTerms[s].size();
+            for (std::size_t k = 0; eq && k < terms.size(); ++k) {
+                const auto& a = terms[k];
+                bool found = false;
+                for (const auto& b : mLinTerms[s])
+                    if (a.src == b.src && a.dx == b.dx && a.dy == b.dy && a.dz == b.dz) { found = a.w == b.w; break; }
+                eq = found;
+            }
+            if (!eq)
+                throw std::runtime_error(std::string("ScaFES::Problem: ") + where + " of field " +
+                                         mNames[mUnknownIdx[f]] +
+                                         " differs between nodes of the same class or between time steps "
+                                         "(variable coefficients have no multi-field device form)");
+        }
+    };
+    auto cls_of = [&](const ScaFES_IntNtuple& n) {
+        int mask = 0;
+        for (std::size_t p = 0; p < DIM; ++p) {
+            if (n[p] == g.idxNodeFirst(p)) mask |= 1 << (2 * p);
+            if (n[p] == g.idxNodeLast(p)) mask |= 1 << (2 * p + 1);
+        }
+        return mask;
+    };
+    for (int ph = 0; ph < mLinPhases; ++ph) {
+        for (long long m = 0; m < mN; ++m) {
+            const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
+            const bool border = isBorder(n);
+            // Every border node; inner nodes on the lines through the first,
+            // middle and last inner planes.
+            if (!border) {
+                int on = 0;
+                for (std::size_t p = 0; p < DIM; ++p)
+                    on += n[p] == 1 || n[p] == g.nNodes(p) / 2 || n[p] == g.nNodes(p) - 2;
+                if (on + 1 < (int)DIM) continue;
+            }
+            for (int t = 1; t <= 2; ++t) {
+                std::vector<gpu::Sym> out;
+                if (ph == 0) out = border ? record<true, 1>(n, t, err) : record<false, 1>(n, t, err);
+                else out = border ? record<true, 2>(n, t, err) : record<false, 2>(n, t, err);
+                if (!err.empty()) throw std::runtime_error("ScaFES::Problem: " + err);
+                take(ph, border ? cls_of(n) : 0, out,
+                     ph == 0 ? (border ? "updateBorder" : "updateInner") : (border ? "updateBorder2" : "updateInner2"));
+            }
+        }
+    }
+    std::ostringstream os;
+    os << "linear multi-field fields=" << nu << " phases=" << mLinPhases;
+    mSummary = os.str();
+    mLinear = true;
+    mPrepared = true;
+}
+
+template <class OWNPRBLM, typename CT, std::size_t DIM>
+void Problem<OWNPRBLM, CT, DIM>::runLinear() {
+    const Grid<DIM>& g = mGG.discreteDomain();
+    const std::size_t nu = mUnknownIdx.size();
+    const int T = mParams.nTimesteps();
+    int nn[3];
+    for (int p = 0; p < 3; ++p) nn[p] = g.nNodes(p);
+    scafes_lin* h = nullptr;
+    if (scafes_lin_create(nn, (int)nu, mLinPhases, nullptr, &h) != SCAFES_OK)
+        throw std::runtime_error(std::string("ScaFES::Problem (GPU): ") + scafes_last_error());
+    auto lcheck = [&](int rc) {
+        if (rc != SCAFES_OK) {
+            const std::string msg = scafes_lin_last_error(h);
+            scafes_lin_destroy(h);
+            throw std::runtime_error("ScaFES::Problem (GPU): " + msg);
+        }
+    };
+    for (int ph = 0; ph < mLinPhases; ++ph)
+        for (std::size_t f = 0; f < nu; ++f)
+            for (int c = 0; c < SCAFES_BORDER_CLASSES; ++c) {
+                const std::size_t s = ((std::size_t)ph * nu + f) * SCAFES_BORDER_CLASSES + c;
+                lcheck(scafes_lin_set_rule(h, ph + 1, (int)f, c, mLinTerms[s].data(), (int)mLinTerms[s].size(),
+                                           mLinCst[s]));
+            }
+    std::vector<double> buf((std::size_t)mN);
+    for (std::size_t u = 0; u < nu; ++u) {
+        for (long long m = 0; m < mN; ++m) buf[m] = (double)mUnknownNewStore[u * mN + m];
+        lcheck(scafes_lin_upload(h, (int)u, buf.data(), buf.size()));
+    }
+    lcheck(scafes_lin_step(h, T));
+    float ms = 0.f;
+    lcheck(scafes_lin_last_ms(h, &ms));
+    mGpuMs = ms;
+    for (std::size_t u = 0; u < nu; ++u) {
+        lcheck(scafes_lin_download(h, (int)u, buf.data(), buf.size()));
+        for (long long m = 0; m < mN; ++m) {
+            mUnknownOldStore[u * mN + m] = (CT)buf[m];
+            mUnknownNewStore[u * mN + m] = (CT)buf[m];
+        }
+    }
+    scafes_lin_destroy(h);
+    for (auto& df : mVectUnknownDfsDomOld) df.time() = (CT)time(T);
+    for (auto& df : mVectUnknownDfsDomNew) df.time() = (CT)time(T);
+}
+
 template <class OWNPRBLM, typename CT, std::size_t DIM>
 void Problem<OWNPRBLM, CT, DIM>::iterateOverTime() {
     using clock = std::chrono::steady_clock;
     auto t_all = clock::now();
     prepareDevice();
+    if (mLinear) {
+        runLinear();
+        mWallClockTimes["iterate"] += std::chrono::duration<double>(clock::now() - t_all).count();
+        if (mParams.outputLevel() > 0)
+            std::cout << "ScaFES-GB300: " << mSummary << ", " << mParams.nTimesteps() << " steps in " << mGpuMs
+                      << " ms" << std::endl;
+        return;
+    }
     const int T = mParams.nTimesteps();
     scafes_cfg cfg = mCfg;
     if (mHandle) { scafes_gpu_destroy(mHandle); mHandle = nullptr; }

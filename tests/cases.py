@@ -173,3 +173,35 @@ def tangent_inputs(n):
     target = np.random.default_rng(42).uniform(-1.0, 1.0, shape)
     dirs = [np.random.default_rng(43 + k).uniform(-1.0, 1.0, shape) for k in range(4)]
     return u0, target, dirs
+
+
+def yee_lin_rules(ch):
+    """The plain Yee cavity (oracle/scafes_oracle.c orc_yee without its
+    source) as rules of the linear multi-field kernel: phase 1 the H half
+    step, phase 2 the E step on its result; fields Ex Ey Ez Hx Hy Hz.
+    Returns {(phase, field, cls): terms}; a node class lacks the +p
+    neighbour when bit 2p+1 is set and is not inner in p when bit 2p or
+    2p+1 is set."""
+    rules = {}
+    e = [(1, 0, 0), (0, 1, 0), (0, 0, 1)]
+    for cls in range(64):
+        up = [not (cls >> (2 * p + 1)) & 1 for p in range(3)]
+        inner = [not (cls >> (2 * p)) & 1 and up[p] for p in range(3)]
+        for c in range(3):
+            a, b = (c + 1) % 3, (c + 2) % 3  # H_c from E_b along a and E_a along b
+            if up[a] and up[b]:
+                rules[(1, 3 + c, cls)] = [(3 + c, 0, 0, 0, 1.0), (b, *e[a], -ch), (b, 0, 0, 0, ch),
+                                          (a, *e[b], ch), (a, 0, 0, 0, -ch)]
+            else:
+                rules[(1, 3 + c, cls)] = [(3 + c, 0, 0, 0, 1.0)]
+            rules[(1, c, cls)] = [(c, 0, 0, 0, 1.0)]
+            ma = tuple(-v for v in e[a])
+            mb = tuple(-v for v in e[b])
+            if up[c] and inner[a] and inner[b]:
+                rules[(2, c, cls)] = [(c, 0, 0, 0, 1.0), (3 + b, 0, 0, 0, ch), (3 + b, *ma, -ch),
+                                      (3 + a, 0, 0, 0, -ch), (3 + a, *mb, ch)]
+            else:
+                rules[(2, c, cls)] = [(c, 0, 0, 0, 1.0)]
+            rules[(2, 3 + c, cls)] = [(3 + c, 0, 0, 0, 1.0)]
+    return rules
+

@@ -23,6 +23,13 @@
 //                 the nodes, Neumann faces, a closed-skull (Neumann) z-max
 //                 face and convection + radiation where the "surface" field
 //                 is 1 (examples/MRIDataPBHEqnFDM)
+//   YeeCavity  -- Maxwell's equations in a perfectly conducting box on the
+//                 staggered Yee grid (eps = mu = 1, cubic spacing): six
+//                 unknown fields Ex Ey Ez Hx Hy Hz, the H half step in
+//                 updateInner/updateBorder and the E step in the leapfrog
+//                 second phase updateInner2/updateBorder2, as the reference's
+//                 FDTD example splits them (examples/EMFDTD/EMFDTD.hpp:295-385,
+//                 without its absorbing layers and source)
 // The tissue classes evaluate their expressions in the examples' operation
 // order, so that the recorded weights are the same doubles.
 #pragma once
@@ -539,5 +546,84 @@ public:
     void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
     template <typename TT>
     void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const ScaFES::Ntuple<int, DIM>&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};
+
+// Yee cavity.  Node (i,j,k) holds Ex at (i+1/2, j, k), Hx at (i, j+1/2,
+// k+1/2) and so on; an H component exists where its two staggered
+// directions have a node beyond, an E component where its own direction
+// has one and the two others are inner (tangential E is 0 on the walls
+// and stays at its initial value there).  The initial fields come from
+// setFields (six fields of n nodes, x fastest).
+template <typename CT, std::size_t DIM>
+class YeeCavity : public ScaFES::Problem<YeeCavity<CT, DIM>, CT, DIM> {
+    using Base = ScaFES::Problem<YeeCavity<CT, DIM>, CT, DIM>;
+    using Tup = ScaFES::Ntuple<int, DIM>;
+    std::vector<double> mInit;
+public:
+    using Base::Base;
+    void setFields(const std::vector<double>& f) { mInit = f; }
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>&, const Tup&, const int&) {}
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>&, const Tup&, const int&) {}
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const Tup& n, const int&) {
+        const auto& g = this->globalGrid().discreteDomain();
+        const long long nn = g.nNodesTotal(), m = g.idxNodeTuple2ScalarStyleFortran(n);
+        for (int c = 0; c < 6; ++c) v[c](n) = mInit.empty() ? 0.0 : mInit.at((std::size_t)(c * nn + m));
+    }
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>& o, const Tup& n, const int& t) {
+        initInner<TT>(v, o, n, t);
+    }
+    // Has node n a neighbour in direction +p / is it inner in direction p?
+    bool up(const Tup& n, int p) { return n[p] < this->globalGrid().discreteDomain().idxNodeLast(p); }
+    bool in(const Tup& n, int p) {
+        const auto& g = this->globalGrid().discreteDomain();
+        return n[p] > g.idxNodeFirst(p) && n[p] < g.idxNodeLast(p);
+    }
+    template <typename TT>
+    void hStep(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+               const Tup& n) {
+        const double ch = this->tau() / this->gridsize(0);
+        const Tup px = this->connect(n, 1), py = this->connect(n, 3), pz = this->connect(n, 5);
+        if (up(n, 1) && up(n, 2))
+            vNew[3](n) = vOld[3](n) - ch * ((vOld[2](py) - vOld[2](n)) - (vOld[1](pz) - vOld[1](n)));
+        if (up(n, 0) && up(n, 2))
+            vNew[4](n) = vOld[4](n) - ch * ((vOld[0](pz) - vOld[0](n)) - (vOld[2](px) - vOld[2](n)));
+        if (up(n, 0) && up(n, 1))
+            vNew[5](n) = vOld[5](n) - ch * ((vOld[1](px) - vOld[1](n)) - (vOld[0](py) - vOld[0](n)));
+    }
+    template <typename TT>
+    void eStep(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+               const Tup& n) {
+        const double ch = this->tau() / this->gridsize(0);
+        const Tup mx = this->connect(n, 0), my = this->connect(n, 2), mz = this->connect(n, 4);
+        if (up(n, 0) && in(n, 1) && in(n, 2))
+            vNew[0](n) = vOld[0](n) + ch * ((vOld[5](n) - vOld[5](my)) - (vOld[4](n) - vOld[4](mz)));
+        if (up(n, 1) && in(n, 0) && in(n, 2))
+            vNew[1](n) = vOld[1](n) + ch * ((vOld[3](n) - vOld[3](mz)) - (vOld[5](n) - vOld[5](mx)));
+        if (up(n, 2) && in(n, 0) && in(n, 1))
+            vNew[2](n) = vOld[2](n) + ch * ((vOld[4](n) - vOld[4](mx)) - (vOld[3](n) - vOld[3](my)));
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const Tup& n, const int&) {
+        hStep<TT>(vNew, vOld, n);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                      const Tup& n, const int&) {
+        hStep<TT>(vNew, vOld, n);
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                      const Tup& n, const int&) {
+        eStep<TT>(vNew, vOld, n);
+    }
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                       const Tup& n, const int&) {
+        eStep<TT>(vNew, vOld, n);
+    }
     const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
 };

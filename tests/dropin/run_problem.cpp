@@ -1,14 +1,16 @@
 // Runs one problem of problems.hpp through the drop-in ScaFES::Problem
 // (test infrastructure).  Usage:
 //   run_problem <heat_lin|pennes_lin|mirror_pow2|heat_sine|heat_neumann|heat_cauchy|
-//                pennes_radiation|tumour|mri> out.bin
+//                pennes_radiation|tumour|mri|yee> out.bin
 //               [--extract-only] [--dump=PATH] [--params=a,b,...] [--fields=PATH]
 //               [ScaFES options...]
 // Writes the final iterate as raw doubles (x fastest); with --extract-only
 // prints the device form of the update instead, with --dump=PATH also
 // writes it to PATH (neither needs a GPU).  --params: the tumour's 16
 // constants, or the MRI example's H T_INF Q_BC Q_SKULL EPSILON T_INIT;
-// --fields: the MRI example's nine known fields, raw FP64.
+// --fields: the MRI example's nine known fields, or the Yee cavity's six
+// initial fields, raw FP64.  The final iterate holds every unknown field,
+// one after the other.
 #include <cstdio>
 #include <cstring>
 #include <iostream>
@@ -45,10 +47,11 @@ int run(P& ppp, const std::string& out, bool extract) {
         return 0;
     }
     ppp.iterateOverTime();
-    const auto& df = ppp.latest()[0];
     const auto& g = ppp.globalGrid().discreteDomain();
-    std::vector<double> v((std::size_t)g.nNodesTotal());
-    for (long long m = 0; m < g.nNodesTotal(); ++m) v[m] = df(g.idxNodeScalar2TupleStyleFortran(m));
+    const long long nn = g.nNodesTotal();
+    std::vector<double> v;
+    for (const auto& df : ppp.latest())
+        for (long long m = 0; m < nn; ++m) v.push_back(df(g.idxNodeScalar2TupleStyleFortran(m)));
     FILE* f = std::fopen(out.c_str(), "wb");
     if (!f || std::fwrite(v.data(), sizeof(double), v.size(), f) != v.size()) return 4;
     std::fclose(f);
@@ -94,6 +97,15 @@ int main(int argc, char** argv) {
                                    std::vector<ScaFES::WriteHowOften>(10, ScaFES::WriteHowOften::NEVER),
                                    std::vector<bool>(10, false));
             p.setParams(g_params);
+            p.setFields(g_fields);
+            return run(p, out, extract);
+        }
+        if (which == "yee") {
+            YeeCavity<double, 3> p(params, gg, true, {"Ex", "Ey", "Ez", "Hx", "Hy", "Hz"},
+                                   std::vector<int>(6, 1), std::vector<bool>(6, false), std::vector<int>(6, 0),
+                                   std::vector<double>(6, 0.0),
+                                   std::vector<ScaFES::WriteHowOften>(6, ScaFES::WriteHowOften::NEVER),
+                                   std::vector<bool>(6, false));
             p.setFields(g_fields);
             return run(p, out, extract);
         }
