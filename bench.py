@@ -344,6 +344,7 @@ def run_batched(M, args, dist: Dist, hbm_peak: float):
                 b.upload(i, M.FIELD_F_A, W.pennes_source(s))
                 b.upload(i, M.FIELD_U, np.full((s["n"][2], s["n"][1], s["n"][0]), W.T_ARTERIAL))
             tile, ctas = b.autotune(5)
+            depth = b.temporal_depth()
             nodes = b.info()["nodes"]
             b.step(T)                  # warm-up: captures the graph
             dist.barrier()
@@ -374,8 +375,9 @@ def run_batched(M, args, dist: Dist, hbm_peak: float):
         g_l = dist.world * lup / (ms_l * 1e-3) / 1e9
         out[prec] = {"value": g_b, "unit": UNIT, "looped_value": g_l, "speedup_vs_looped": ms_l / ms_b,
                      "hbm_frac": 24 * lup / (ms_b * 1e-3) / 1e9 / hbm_peak, "ms": ms_b, "looped_ms": ms_l,
-                     "nodes": nodes, "tile": tile, "ctas_per_sm": ctas, "launches": launches_b,
-                     "looped_launches": launches_l}
+                     "nodes": nodes, "tile": tile, "ctas_per_sm": ctas, "temporal_depth": depth["depth"],
+                     "autotune_ms_by_depth": {"1": depth["ms_depth1"], "2": depth["ms_depth2"], "trial_steps": 6},
+                     "launches": launches_b, "looped_launches": launches_l}
         if err is not None:
             out[prec]["max_rel_err_vs_f64"] = err
             out[prec]["steps_compared"] = T

@@ -393,12 +393,22 @@ int scafes_batch_step(scafes_batch* b, int n_steps);
  * for comparison with scafes_batch_step. */
 int scafes_batch_step_looped(scafes_batch* b, int n_steps);
 
-/* Times every tile variant x {occupancy, 1, 2, 4} CTAs per SM for n_steps
- * batched steps, keeps the fastest (iterates restored afterwards). */
+/* Times every tile variant x {occupancy, 1, 2, 4} CTAs per SM at temporal
+ * depth 1, then depth 2 (two steps per pass over each instance with the
+ * plain sweep's depth-2 kernel, one launch per instance and pass on 16
+ * parallel chains of the graph), for n_steps (rounded up to even) batched
+ * steps, and keeps the fastest (iterates restored afterwards). */
 int scafes_batch_autotune(scafes_batch* b, int n_steps, int* tile,
                           int* ctas_per_sm);
 /* Sets the schedule directly: tile 1..4, ctas_per_sm 0 (= occupancy) .. 16. */
 int scafes_batch_set_schedule(scafes_batch* b, int tile, int ctas_per_sm);
+/* Temporal-blocking depth of scafes_batch_step: 1 or 2 (an odd last step
+ * of a depth-2 call runs at depth 1). */
+int scafes_batch_set_temporal_depth(scafes_batch* b, int depth);
+/* The depth in use and the autotuner's best ms per depth (-1 before an
+ * autotune); ms pointers may be NULL. */
+int scafes_batch_temporal_depth(const scafes_batch* b, int* depth, float* ms_depth1,
+                                float* ms_depth2);
 
 /* ms of the last scafes_batch_step / _step_looped call (CUDA events). */
 int scafes_batch_last_ms(const scafes_batch* b, float* ms);

@@ -131,6 +131,9 @@ def lib() -> C.CDLL:
         L.scafes_batch_step_looped.argtypes = [vp, C.c_int]
         L.scafes_batch_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.scafes_batch_set_schedule.argtypes = [vp, C.c_int, C.c_int]
+        L.scafes_batch_set_temporal_depth.argtypes = [vp, C.c_int]
+        L.scafes_batch_temporal_depth.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_float),
+                                                  C.POINTER(C.c_float)]
         L.scafes_batch_last_ms.argtypes = [vp, C.POINTER(C.c_float)]
         L.scafes_batch_info.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                         C.POINTER(C.c_int), C.POINTER(C.c_longlong)]
@@ -470,6 +473,16 @@ class Batch:
 
     def set_schedule(self, tile: int, ctas_per_sm: int = 0):
         _bcheck(lib().scafes_batch_set_schedule(self.h, tile, ctas_per_sm), self.h)
+
+    def set_temporal_depth(self, depth: int):
+        _bcheck(lib().scafes_batch_set_temporal_depth(self.h, depth), self.h)
+
+    def temporal_depth(self) -> dict:
+        """The depth in use and the autotuner's best ms per depth (-1 before
+        an autotune)."""
+        d, m1, m2 = C.c_int(), C.c_float(), C.c_float()
+        _bcheck(lib().scafes_batch_temporal_depth(self.h, C.byref(d), C.byref(m1), C.byref(m2)), self.h)
+        return {"depth": d.value, "ms_depth1": m1.value, "ms_depth2": m2.value}
 
     def last_ms(self) -> float:
         v = C.c_float()

@@ -13,9 +13,10 @@
 // (adjoint) sweep is hand-written: the update is linear in u and its
 // matrix is symmetric on the inner nodes, so the adjoint step has the same
 // stencil as the forward step applied to lambda (zero on border nodes),
-// plus the accumulation of the face-conductivity gradients
-//   G_p[i] += (u_{i+p} - u_i) (lambda_i - lambda_{i+p})
-// from which dJ/dk_i = sum_p (tau/h_p^2)/2 (G_p[i] + G_p[i-p]).
+// plus the accumulation, per node, of the conductivity gradient
+//   dJ/dk_i = sum_p (tau/h_p^2)/2 (G_p[i] + G_p[i-p]),
+//   G_p[j] = sum over steps of (u_{j+p} - u_j) (lambda_j - lambda_{j+p}),
+// the two faces of node i along each axis, in FP32-pair arithmetic.
 // The forward states the adjoint needs are recomputed from snapshots kept
 // in device memory; the split points follow the optimal binomial schedule
 // (Griewank & Walther, "Algorithm 799: revolve", ACM TOMS 26(1), 2000),
@@ -25,6 +26,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <unordered_map>
 #include <vector>
 
@@ -101,73 +103,6 @@ __device__ __forceinline__ float2 pbits(double d) {
     return make_float2(p.hi, p.lo);
 }
 
-// G += (u_nb - u_c) (l_c - l_nb) in FP32-pair arithmetic, renormalised.
-__device__ __forceinline__ float2 gacc(float2 G, float2 unb, float2 uc, float2 lc, float2 lnb);
-
-// One adjoint step: lambda_t from lambda_{t+1} (lam, zero on border nodes)
-// and the forward state u_t; accumulates the face gradients G and, on
-// border nodes, the border part of dJ/du0 (bnd).  lambda' = A^T lambda in
-// the diagonal form (7 FP64 operations per inner node; the matrix is
-// symmetric on the inner nodes).  The face gradients
-//   G_p[i] += (u_{i+p} - u_i)(lambda_i - lambda_{i+p})
-// are FP32 pairs, formed from u and lambda split into pairs with integer
-// instructions (split_bits) and accumulated in pair arithmetic, so that
-// no FP64 operation is spent on them (9 FP64 operations per node in FP64):
-// the step then costs about what a forward step costs.  The centre values'
-// pairs come from the +z neighbour's split of the plane below.
-__global__ void __launch_bounds__(AX * AY)
-k_adjoint(const double* __restrict__ lam, double* __restrict__ lamn, const double* __restrict__ u,
-          const double* __restrict__ kx, const double* __restrict__ ky, const double* __restrict__ kz,
-          const double* __restrict__ dg, float2* __restrict__ gx, float2* __restrict__ gy, float2* __restrict__ gz,
-          double* __restrict__ bnd, Layout L) {
-    const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
-    if (x >= L.nx || y >= L.ny) return;
-    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
-    const int zb = blockIdx.z * 16, ze = min(zb + 16, L.nz);
-    const bool hx = x + 1 < L.nx, hy = y + 1 < L.ny;
-    long long o = L.idx(x, y, zb);
-    float2 puc = pbits(u[o]), plc = pbits(lam[o]);  // pairs of the centre values
-    for (int z = zb; z < ze; ++z, o += L.plane) {
-        const bool border = colb || z == 0 || z == L.nz - 1;
-        const bool hz = z + 1 < L.nz;
-        const double lc = lam[o];  // zero on border nodes
-        const double lxp = hx ? lam[o + 1] : 0.0, lxm = x > 0 ? lam[o - 1] : 0.0;
-        const double lyp = hy ? lam[o + L.pitch] : 0.0, lym = y > 0 ? lam[o - L.pitch] : 0.0;
-        const double lzp = hz ? lam[o + L.plane] : 0.0, lzm = z > 0 ? lam[o - L.plane] : 0.0;
-        const double kxm = x > 0 ? kx[o - 1] : 0.0, kym = y > 0 ? ky[o - L.pitch] : 0.0;
-        const double kzm = z > 0 ? kz[o - L.plane] : 0.0;
-        // Face gradients of the + faces, in pairs.
-        const float2 pua = hz ? pbits(u[o + L.plane]) : make_float2(0.f, 0.f);
-        const float2 pla = pbits(lzp);
-        if (hx) gx[o] = gacc(gx[o], pbits(u[o + 1]), puc, plc, pbits(lxp));
-        if (hy) gy[o] = gacc(gy[o], pbits(u[o + L.pitch]), puc, plc, pbits(lyp));
-        if (hz) gz[o] = gacc(gz[o], pua, puc, plc, pla);
-        if (border) {
-            // Border rows of the update are the identity: lambda on the border
-            // only collects what the inner neighbours pass back.
-            double s = kx[o] * lxp;
-            s = fma(kxm, lxm, s);
-            s = fma(ky[o], lyp, s);
-            s = fma(kym, lym, s);
-            s = fma(kz[o], lzp, s);
-            s = fma(kzm, lzm, s);
-            bnd[o] += s;
-            lamn[o] = 0.0;
-        } else {
-            double v = dg[o] * lc;
-            v = fma(kx[o], lxp, v);
-            v = fma(kxm, lxm, v);
-            v = fma(ky[o], lyp, v);
-            v = fma(kym, lym, v);
-            v = fma(kz[o], lzp, v);
-            v = fma(kzm, lzm, v);
-            lamn[o] = v;
-        }
-        puc = pua;
-        plc = pla;
-    }
-}
-
 // lambda_T = u_T - target (or the given cotangent when `seed`): inner part
 // into lam, border part into bnd; per-CTA partial sums of 0.5 (u_T -
 // target)^2 into part (0 when `seed`).
@@ -198,21 +133,16 @@ __global__ void k_terminal(const double* __restrict__ uT, const double* __restri
     if (t == 0) part[blockIdx.y * gridDim.x + blockIdx.x] = sh[0];
 }
 
-// dJ/dk_i = sum_p w_p/2 (G_p[i] + G_p[i-p]); dJ/du0 = lambda_0 + border part.
-// (FP64 sweeps: the face gradients are FP32 pairs, lambda and bnd FP64.)
-__global__ void k_finalize(const float2* __restrict__ gx, const float2* __restrict__ gy,
-                           const float2* __restrict__ gz, const double* __restrict__ lam,
+// dJ/dk = the per-node gradient pair; dJ/du0 = lambda_0 + border part
+// (FP64 sweeps: lambda and bnd FP64).
+__global__ void k_finalize(const float2* __restrict__ g, const double* __restrict__ lam,
                            const double* __restrict__ bnd, double* __restrict__ dk, double* __restrict__ du0,
-                           Layout L, double wx, double wy, double wz) {
+                           Layout L) {
     const int x = blockIdx.x * AX + threadIdx.x, y = blockIdx.y * AY + threadIdx.y;
     if (x >= L.nx || y >= L.ny) return;
-    auto J = [](float2 p) { return join_pair(p.x, p.y); };
     for (int z = 0; z < L.nz; ++z) {
         const long long o = L.idx(x, y, z);
-        double g = 0.5 * wx * (J(gx[o]) + (x > 0 ? J(gx[o - 1]) : 0.0));
-        g += 0.5 * wy * (J(gy[o]) + (y > 0 ? J(gy[o - L.pitch]) : 0.0));
-        g += 0.5 * wz * (J(gz[o]) + (z > 0 ? J(gz[o - L.plane]) : 0.0));
-        dk[o] = g;
+        dk[o] = join_pair(g[o].x, g[o].y);
         du0[o] = lam[o] + bnd[o];
     }
 }
@@ -419,20 +349,7 @@ k_forward_x2_tma(const __grid_constant__ CUtensorMap tu, const __grid_constant__
     if (!__syncthreads_and(ok)) fail(issued);
 }
 
-// G += (u_nb - u_c) (l_c - l_nb), renormalised.
-__device__ __forceinline__ float2 gacc(float2 G, float2 unb, float2 uc, float2 lc, float2 lnb) {
-    const f2 du = psub(unb, uc);
-    const f2 dl = psub(lc, lnb);
-    const float p = du.hi * dl.hi;
-    float e = fmaf(du.hi, dl.hi, -p);
-    e = fmaf(du.hi, dl.lo, e);
-    e = fmaf(du.lo, dl.hi, e);
-    f2 acc{G.x, G.y};
-    pacc(acc, {p, e});
-    return pnorm(acc);
-}
-
-// One adjoint step on FP32 pairs: lambda' = A^T lambda (the transposed
+// One adjoint step: lambda' = A^T lambda (the transposed
 // diagonal form; border rows pass what they receive into bnd) and the
 // conductivity gradient at the state u_t, accumulated per node:
 //   g_i -= sum_p w_p/2 [ P_p(i) + P_p(i-p) ],
@@ -481,13 +398,26 @@ __device__ __forceinline__ f2 pscale2(float2 c, f2 a, f2 b) {
     return {p, e};
 }
 
+// A stored value as a pair: FP32-pair fields as they are, FP64 fields split
+// with integer instructions.
+__device__ __forceinline__ float2 pview(float2 v) { return v; }
+__device__ __forceinline__ float2 pview(double v) { return pbits(v); }
+
+// E = float2: every field an FP32 pair, the lambda update in pair
+// arithmetic.  E = double: lambda, u, the faces and the diagonal FP64 and
+// the lambda update in FP64 in the order of k_forward (diagonal, +x, -x,
+// +y, -y, +z, -z; 7 FP64 operations per node), the gradient in FP32 pairs
+// from integer splits of u and lambda (no FP64 instruction).
+template <class E>
 __global__ void __launch_bounds__(RTX * RTY)
 k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__ CUtensorMap tu,
                  const __grid_constant__ CUtensorMap tkx, const __grid_constant__ CUtensorMap tky,
                  const __grid_constant__ CUtensorMap tkz, const __grid_constant__ CUtensorMap tdg,
-                 float2* __restrict__ lamn, float2* __restrict__ g, float2* __restrict__ bnd, float2 hx2,
+                 E* __restrict__ lamn, float2* __restrict__ g, E* __restrict__ bnd, float2 hx2,
                  float2 hy2, float2 hz2, Layout L, int* __restrict__ status) {
-    extern __shared__ __align__(128) float2 rsm[];
+    constexpr bool F64 = std::is_same<E, double>::value;
+    extern __shared__ __align__(128) unsigned char rsm_raw[];
+    E* rsm = reinterpret_cast<E*>(rsm_raw);
     uint64_t* bar = reinterpret_cast<uint64_t*>(rsm + RNS * RSLOT);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * RTX + tx;
     const int x0 = blockIdx.x * RTX, y0 = blockIdx.y * RTY;
@@ -502,7 +432,7 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
     const int n_in = z1 - z0 + 2;
     auto issue = [&](int j) {
         const int s = j & (RNS - 1), z = z0 - 1 + j;
-        float2* d = rsm + s * RSLOT;
+        E* d = rsm + s * RSLOT;
         scafes::mbar_arrive_expect_tx(&bar[s], RTX_BYTES);
         scafes::tma_load_3d(d + RO_L, &tl, x0 - 2, y0 - 1, z, &bar[s]);
         scafes::tma_load_3d(d + RO_U, &tu, x0 - 2, y0 - 1, z, &bar[s]);
@@ -528,15 +458,17 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
     const int bl = (ty + 1) * RLW + tx + 2, bx = ty * FXW + tx + 2, by = (ty + 1) * FYW + tx;
     const int bk = ty * FKW + tx;
     const float2 zero = make_float2(0.f, 0.f);
+    const E ezero = E{};
     long long o = live ? L.idx(x, y, z0) : 0;
     float2 gn = live ? g[o] : zero;
     bool ok = wait(0);
-    float2 lb = z0 > 0 ? rsm[RO_L + bl] : zero;  // plane z0-1
-    float2 ub = z0 > 0 ? rsm[RO_U + bl] : zero;
-    float2 kzb = z0 > 0 ? rsm[RO_Z + bk] : zero;
+    E lb = z0 > 0 ? rsm[RO_L + bl] : ezero;  // plane z0-1
+    E ub = z0 > 0 ? rsm[RO_U + bl] : ezero;
+    E kzb = z0 > 0 ? rsm[RO_Z + bk] : ezero;
     ok = wait(1) && ok;
     // The z-face product of the plane below (face z-1 | z).
-    f2 pzb = z0 > 0 ? pface(ub, rsm[RSLOT + RO_U + bl], lb, rsm[RSLOT + RO_L + bl]) : f2{0.f, 0.f};
+    f2 pzb = z0 > 0 ? pface(pview(ub), pview(rsm[RSLOT + RO_U + bl]), pview(lb), pview(rsm[RSLOT + RO_L + bl]))
+                    : f2{0.f, 0.f};
     int issued = RNS - 1;
     for (int z = z0; z < z1; ++z, o += L.plane) {
         const int jc = z - z0 + 1;  // input plane of z
@@ -552,41 +484,61 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
         const float2 gc = gn;
         if (live && z + 1 < z1) gn = g[o + L.plane];
         ok = wait(jc + 1) && ok;  // plane z+1
-        const float2* sc = rsm + (jc & (RNS - 1)) * RSLOT;
-        const float2* sa = rsm + ((jc + 1) & (RNS - 1)) * RSLOT;
+        const E* sc = rsm + (jc & (RNS - 1)) * RSLOT;
+        const E* sa = rsm + ((jc + 1) & (RNS - 1)) * RSLOT;
         const bool top = z + 1 < L.nz;
-        const float2 la = top ? sa[RO_L + bl] : zero;
-        const float2 ua = top ? sa[RO_U + bl] : zero;
-        const float2 lc = sc[RO_L + bl], uc = sc[RO_U + bl];
-        const float2 kzc = sc[RO_Z + bk];
-        const f2 pza = pface(uc, ua, lc, la);  // face z | z+1
+        const E la = top ? sa[RO_L + bl] : ezero;
+        const E ua = top ? sa[RO_U + bl] : ezero;
+        const E lc = sc[RO_L + bl], uc = sc[RO_U + bl];
+        const E kzc = sc[RO_Z + bk];
+        const float2 plc = pview(lc), puc = pview(uc);
+        const f2 pza = pface(puc, pview(ua), plc, pview(la));  // face z | z+1
         if (live) {
             const bool border = colb || z == 0 || z == L.nz - 1;
-            const float2 lxp = sc[RO_L + bl + 1], lxm = sc[RO_L + bl - 1];
-            const float2 lyp = sc[RO_L + bl + RLW], lym = sc[RO_L + bl - RLW];
+            const E lxp = sc[RO_L + bl + 1], lxm = sc[RO_L + bl - 1];
+            const E lyp = sc[RO_L + bl + RLW], lym = sc[RO_L + bl - RLW];
             // dJ/dk_i: the two faces along each axis.
-            f2 gk = pscale2(hx2, pface(uc, sc[RO_U + bl + 1], lc, lxp), pface(sc[RO_U + bl - 1], uc, lxm, lc));
-            pacc(gk, pscale2(hy2, pface(uc, sc[RO_U + bl + RLW], lc, lyp), pface(sc[RO_U + bl - RLW], uc, lym, lc)));
+            f2 gk = pscale2(hx2, pface(puc, pview(sc[RO_U + bl + 1]), plc, pview(lxp)),
+                            pface(pview(sc[RO_U + bl - 1]), puc, pview(lxm), plc));
+            pacc(gk, pscale2(hy2, pface(puc, pview(sc[RO_U + bl + RLW]), plc, pview(lyp)),
+                             pface(pview(sc[RO_U + bl - RLW]), puc, pview(lym), plc)));
             pacc(gk, pscale2(hz2, pza, pzb));
             f2 gsum{gc.x, gc.y};
             pacc(gsum, {-gk.hi, -gk.lo});
             g[o] = pnorm(gsum);
-            const float2 kxp = sc[RO_X + bx], kyp = sc[RO_Y + by];
-            const float2 kxm = sc[RO_X + bx - 1], kym = sc[RO_Y + by - FYW];
-            f2 acc = border ? f2{0.f, 0.f} : pmul(sc[RO_D + bk], lc);
-            pacc(acc, pmul(kxp, lxp));
-            pacc(acc, pmul(kxm, lxm));
-            pacc(acc, pmul(kyp, lyp));
-            pacc(acc, pmul(kym, lym));
-            pacc(acc, pmul(kzc, la));
-            pacc(acc, pmul(kzb, lb));
-            if (border) {
-                const float2 bo = bnd[o];
-                pacc(acc, {bo.x, bo.y});
-                bnd[o] = pnorm(acc);
-                lamn[o] = zero;
+            const E kxp = sc[RO_X + bx], kyp = sc[RO_Y + by];
+            const E kxm = sc[RO_X + bx - 1], kym = sc[RO_Y + by - FYW];
+            if constexpr (F64) {
+                // lambda' in FP64; a border row passes its inflow into bnd.
+                double v = border ? kxp * lxp : sc[RO_D + bk] * lc;
+                if (!border) v = fma(kxp, lxp, v);
+                v = fma(kxm, lxm, v);
+                v = fma(kyp, lyp, v);
+                v = fma(kym, lym, v);
+                v = fma(kzc, la, v);
+                v = fma(kzb, lb, v);
+                if (border) {
+                    bnd[o] += v;
+                    lamn[o] = 0.0;
+                } else {
+                    lamn[o] = v;
+                }
             } else {
-                lamn[o] = pnorm(acc);
+                f2 acc = border ? f2{0.f, 0.f} : pmul(sc[RO_D + bk], lc);
+                pacc(acc, pmul(kxp, lxp));
+                pacc(acc, pmul(kxm, lxm));
+                pacc(acc, pmul(kyp, lyp));
+                pacc(acc, pmul(kym, lym));
+                pacc(acc, pmul(kzc, la));
+                pacc(acc, pmul(kzb, lb));
+                if (border) {
+                    const float2 bo = bnd[o];
+                    pacc(acc, {bo.x, bo.y});
+                    bnd[o] = pnorm(acc);
+                    lamn[o] = zero;
+                } else {
+                    lamn[o] = pnorm(acc);
+                }
             }
         }
         lb = lc;
@@ -652,7 +604,7 @@ struct scafes_adj {
     double *kx = nullptr, *ky = nullptr, *kz = nullptr;
     double *dg = nullptr;      // diagonal of the update, d_i = 1 - sum of i's faces
     double *u[2] = {nullptr, nullptr}, *lam[2] = {nullptr, nullptr};
-    double *gx = nullptr, *gy = nullptr, *gz = nullptr, *bnd = nullptr;
+    double *gx = nullptr, *bnd = nullptr;  // gx: the per-node gradient (an FP32 pair per node)
     double *snaps = nullptr;   // n_snap fields
     double *work = nullptr;    // staging of host arrays (dense doubles)
     double *part = nullptr;    // J partial sums
@@ -704,7 +656,8 @@ bool pairs(const scafes_adj* a) { return a->precision == SCAFES_PREC_F32X2; }
 const float2* P2(const double* p) { return reinterpret_cast<const float2*>(p); }
 float2* P2(double* p) { return reinterpret_cast<float2*>(p); }
 
-// Descriptor of an FP32-pair field for a box of bw x bh nodes.
+// Descriptor of a field of 8-byte elements (FP64 or an FP32 pair) for a box
+// of bw x bh nodes.
 int pair_map(scafes_adj* a, CUtensorMap* m, const void* base, int bw, int bh) {
     const CUresult r = scafes::make_tensor_map_3d(m, base, 8, a->L.nx, a->L.ny, a->L.nz, (size_t)a->L.pitch * 8,
                                                   (size_t)a->L.plane * 8, bw, bh);
@@ -740,8 +693,11 @@ int coefficient_maps(scafes_adj* a) {
     if (!rc) rc = pair_map(a, &a->cmaps[3], a->dg, FKW, FKH);
     if (rc) return rc;
     ATRY(a, cudaFuncSetAttribute(k_forward_x2_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FSMEM));
-    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RSMEM));
-    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma, cudaFuncAttributePreferredSharedMemoryCarveout,
+    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RSMEM));
+    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma<float2>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared));
+    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RSMEM));
+    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma<double>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared));
     a->cmaps_ok = true;
     return SCAFES_OK;
@@ -873,23 +829,23 @@ int adj_step(Rev& R, const double* u_t) {
     scafes_adj* a = R.a;
     if (R.reset_border && a->adj_steps == R.T - 1)
         ATRY(a, cudaMemsetAsync(a->bnd, 0, field_bytes(a), a->stream));  // the last step is t = 0 -> 1
-    if (pairs(a)) {
-        if (int rc = coefficient_maps(a)) return rc;
-        CUtensorMap ml, mu;
-        if (int rc = state_map(a, a->lam[R.cur], BOX_HALO, &ml)) return rc;
-        if (int rc = state_map(a, u_t, BOX_HALO, &mu)) return rc;
-        const dim3 grid((a->L.nx + RTX - 1) / RTX, (a->L.ny + RTY - 1) / RTY, (a->L.nz + RZ_ - 1) / RZ_);
-        auto half = [](double w) {
-            const f2 p = split_double(0.5 * w);
-            return make_float2(p.hi, p.lo);
-        };
-        k_adjoint_x2_tma<<<grid, dim3(RTX, RTY), RSMEM, a->stream>>>(
+    if (int rc = coefficient_maps(a)) return rc;
+    CUtensorMap ml, mu;
+    if (int rc = state_map(a, a->lam[R.cur], BOX_HALO, &ml)) return rc;
+    if (int rc = state_map(a, u_t, BOX_HALO, &mu)) return rc;
+    const dim3 grid((a->L.nx + RTX - 1) / RTX, (a->L.ny + RTY - 1) / RTY, (a->L.nz + RZ_ - 1) / RZ_);
+    auto half = [](double w) {
+        const f2 p = split_double(0.5 * w);
+        return make_float2(p.hi, p.lo);
+    };
+    if (pairs(a))
+        k_adjoint_x2_tma<float2><<<grid, dim3(RTX, RTY), RSMEM, a->stream>>>(
             ml, mu, a->cmaps[0], a->cmaps[1], a->cmaps[2], a->cmaps[3], P2(a->lam[R.cur ^ 1]), P2(a->gx),
             P2(a->bnd), half(a->w[0]), half(a->w[1]), half(a->w[2]), a->L, a->status);
-    } else
-        k_adjoint<<<grid3(a->L), dim3(AX, AY), 0, a->stream>>>(a->lam[R.cur], a->lam[R.cur ^ 1], u_t, a->kx, a->ky,
-                                                               a->kz, a->dg, P2(a->gx), P2(a->gy), P2(a->gz), a->bnd,
-                                                               a->L);
+    else
+        k_adjoint_x2_tma<double><<<grid, dim3(RTX, RTY), RSMEM, a->stream>>>(
+            ml, mu, a->cmaps[0], a->cmaps[1], a->cmaps[2], a->cmaps[3], a->lam[R.cur ^ 1], P2(a->gx), a->bnd,
+            half(a->w[0]), half(a->w[1]), half(a->w[2]), a->L, a->status);
     ATRY(a, cudaGetLastError());
     R.cur ^= 1;
     ++a->adj_steps;
@@ -964,8 +920,8 @@ extern "C" const char* scafes_adj_last_error(const scafes_adj* a) { return a ? a
 extern "C" void scafes_adj_destroy(scafes_adj* a) {
     if (!a) return;
     if (a->stream) cudaStreamSynchronize(a->stream);
-    double* bufs[] = {a->kx, a->ky, a->kz, a->dg, a->u[0], a->u[1], a->lam[0], a->lam[1], a->gx, a->gy, a->gz,
-                      a->bnd, a->snaps, a->work, a->part};
+    double* bufs[] = {a->kx, a->ky, a->kz, a->dg, a->u[0], a->u[1], a->lam[0], a->lam[1], a->gx, a->bnd,
+                      a->snaps, a->work, a->part};
     for (double* b : bufs) cudaFree(b);
     cudaFree(a->status);
     if (a->e0) cudaEventDestroy(a->e0);
@@ -998,7 +954,7 @@ extern "C" int scafes_adj_create(const int n_nodes[3], const double coord_first[
     if (stream) a->stream = (cudaStream_t)stream;
     else { e = cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking); a->own_stream = true; }
     double** fields[] = {&a->kx, &a->ky, &a->kz, &a->dg, &a->u[0], &a->u[1], &a->lam[0], &a->lam[1], &a->gx,
-                         &a->gy, &a->gz, &a->bnd, &a->work};
+                         &a->bnd, &a->work};
     for (double** f : fields)
         if (e == cudaSuccess) e = cudaMalloc(f, fb);
     if (e == cudaSuccess) e = cudaMalloc(&a->snaps, fb * (size_t)n_snapshots);
@@ -1117,8 +1073,6 @@ static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const
     // The target goes to u[1]'s slot only transiently: keep it in `work`.
     if ((rc = upload_dense(a, target, a->work))) return rc;
     ATRY(a, cudaMemsetAsync(a->gx, 0, fb, a->stream));
-    ATRY(a, cudaMemsetAsync(a->gy, 0, fb, a->stream));
-    ATRY(a, cudaMemsetAsync(a->gz, 0, fb, a->stream));
     a->fwd_steps = 0;
     a->adj_steps = 0;
     ATRY(a, cudaEventRecord(a->e0, a->stream));
@@ -1128,9 +1082,8 @@ static int gradient_impl(scafes_adj* a, const char* who, const double* u0, const
         k_finalize_x2<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(a->gx), P2(a->lam[R.cur]), P2(a->bnd),
                                                                    a->u[0], a->u[1], a->L);
     else
-        k_finalize<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(a->gx), P2(a->gy), P2(a->gz), a->lam[R.cur],
-                                                                a->bnd, a->u[0], a->u[1], a->L, a->w[0], a->w[1],
-                                                                a->w[2]);
+        k_finalize<<<grid2(a->L), dim3(AX, AY), 0, a->stream>>>(P2(a->gx), a->lam[R.cur], a->bnd, a->u[0],
+                                                                a->u[1], a->L);
     ATRY(a, cudaGetLastError());
     ATRY(a, cudaEventRecord(a->e1, a->stream));
     std::vector<double> part(a->part_n);

@@ -12,7 +12,11 @@
 // per step) and runs them through the same TMA-fed tile code as the plain
 // sweep.  The time loop (a memset of the counters and n_steps launches) is
 // captured once into a CUDA graph and replayed.  scafes_batch_autotune
-// picks the tile variant and the CTAs per SM.  For comparison,
+// picks the tile variant, the CTAs per SM and the temporal-blocking depth:
+// depth 2 advances each instance two steps per pass over its field with
+// the plain sweep's depth-2 kernel (star7_tb.cuh), one launch per instance
+// and pass, the instances spread over kSideStreams parallel chains of the
+// graph.  For comparison,
 // scafes_batch_step_looped runs the reference's schedule on the GPU: one
 // plain launch per instance per step.
 #include <algorithm>
@@ -33,6 +37,7 @@ void set_last_error(const char* msg);
 namespace {
 
 constexpr int kZChunk = 32;  // planes per work item
+constexpr int kSideStreams = 16;  // parallel launch chains of a depth-2 step
 
 struct BatchInst {
     Layout L;
@@ -153,6 +158,13 @@ struct scafes_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int tile = 1;
     int ctas_per_sm = 0;  // 0 = occupancy limit
+    int depth = 1;        // temporal-blocking depth of scafes_batch_step (1 or 2)
+    float depth_ms[2] = {-1.f, -1.f};  // the autotuner's best time per depth
+    // Depth 2: per instance the TMA maps of both iterates for the depth-2
+    // box, the side streams of the capture and their fork/join events.
+    std::vector<CUtensorMap> htb;
+    cudaStream_t side[kSideStreams] = {};
+    cudaEvent_t fork = nullptr, join[kSideStreams] = {};
     int cur = 0;
     int t = 0;
     int launches = 0;
@@ -278,6 +290,74 @@ int check_status(scafes_batch* b) {
     return SCAFES_OK;
 }
 
+// Depth-2 resources, made on first use: the TMA maps of both iterates of
+// every instance for the depth-2 box, the side streams and their events.
+int ensure_tb(scafes_batch* b) {
+    if (!b->htb.empty()) return SCAFES_OK;
+    int bw = 0, bh = 0;
+    star7_tb_box(b->precision, &bw, &bh);
+    std::vector<CUtensorMap> maps(b->hinst.size() * 2);
+    for (size_t i = 0; i < b->hinst.size(); ++i) {
+        const BatchInst& I = b->hinst[i];
+        for (int buf = 0; buf < 2; ++buf) {
+            const CUresult r = make_tensor_map_3d(&maps[i * 2 + buf], (char*)b->pool + (size_t)I.off_u[buf] * b->esz,
+                                                  (int)b->esz, I.L.nx, I.L.ny, I.L.nz, (size_t)I.L.pitch * b->esz,
+                                                  (size_t)I.L.plane * b->esz, bw, bh);
+            if (r != CUDA_SUCCESS)
+                return bfail(b, SCAFES_ERR_CUDA, "scafes_batch: cuTensorMapEncodeTiled failed (%d)", (int)r);
+        }
+    }
+    for (int k = 0; k < kSideStreams; ++k) {
+        if (!b->side[k]) BTRY(b, cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
+        if (!b->join[k]) BTRY(b, cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+    }
+    if (!b->fork) BTRY(b, cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->htb.swap(maps);
+    return SCAFES_OK;
+}
+
+// Enqueues n_pairs depth-2 passes of every instance starting from iterate
+// `cur`: instance i on side stream i % kSideStreams, forked from and joined
+// back into the batch's stream (inside a capture this makes kSideStreams
+// independent chains of the graph).
+int enqueue_tb(scafes_batch* b, int cur, int n_pairs) {
+    BTRY(b, cudaEventRecord(b->fork, b->stream));
+    const int ns = std::min<int>(kSideStreams, (int)b->hinst.size());
+    for (int k = 0; k < ns; ++k) BTRY(b, cudaStreamWaitEvent(b->side[k], b->fork, 0));
+    for (int pass = 0; pass < n_pairs; ++pass) {
+        for (int i = 0; i < (int)b->hinst.size(); ++i) {
+            const BatchInst& I = b->hinst[i];
+            Star7Launch a;
+            a.precision = b->precision;
+            a.border = SCAFES_BORDER_DIRICHLET;
+            a.tile = 0;
+            a.L = I.L;
+            a.tm_uo = nullptr;
+            a.tm_f = nullptr;
+            a.tm_tb = &b->htb[(size_t)i * 2 + cur];
+            a.table = nullptr;
+            a.status = b->status;
+            a.uo = (char*)b->pool + (size_t)I.off_u[cur] * b->esz;
+            a.un = (char*)b->pool + (size_t)I.off_u[cur ^ 1] * b->esz;
+            a.fa = (char*)b->pool + (size_t)I.off_f * b->esz;
+            a.fb = nullptr;
+            a.ga = nullptr;
+            a.gb = nullptr;
+            a.gconst = I.gconst;
+            a.c = I.c;
+            a.time_old = a.time_new = a.time_new2 = a.mirror_corr = 0.0;
+            const cudaError_t e = launch_star7_tb(a, b->side[i % ns]);
+            if (e != cudaSuccess) return bfail(b, SCAFES_ERR_CUDA, "scafes_batch depth-2 pass: %s", cudaGetErrorString(e));
+        }
+        cur ^= 1;
+    }
+    for (int k = 0; k < ns; ++k) {
+        BTRY(b, cudaEventRecord(b->join[k], b->side[k]));
+        BTRY(b, cudaStreamWaitEvent(b->stream, b->join[k], 0));
+    }
+    return SCAFES_OK;
+}
+
 void build_items(scafes_batch* b) {
     for (int tile = 0; tile < STAR7_NUM_TILES; ++tile) {
         auto& v = b->hitems[tile];
@@ -326,6 +406,11 @@ extern "C" void scafes_batch_destroy(scafes_batch* b) {
     cudaFree(b->status);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
+    for (int k = 0; k < kSideStreams; ++k) {
+        if (b->side[k]) cudaStreamDestroy(b->side[k]);
+        if (b->join[k]) cudaEventDestroy(b->join[k]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }
@@ -528,7 +613,16 @@ extern "C" int scafes_batch_step(scafes_batch* b, int n_steps) {
     if (rc) return rc;
     const KernelInfo k = kinfo(b->precision, b->tile);
     grid_size(b, k);  // sets the smem attribute outside any capture
-    const long long key = ((long long)n_steps * 2 + b->cur) * 64 + b->tile * 16 + b->ctas_per_sm;
+    // Depth 2: n_steps / 2 passes, an odd last step by the persistent kernel.
+    const int pairs = b->depth == 2 ? n_steps / 2 : 0;
+    const int singles = n_steps - 2 * pairs;
+    if (pairs > 0) {
+        if ((rc = ensure_tb(b))) return rc;
+        if (launch_star7_tb_prepare(b->precision) != cudaSuccess)
+            return bfail(b, SCAFES_ERR_CUDA, "scafes_batch_step: depth-2 kernel attributes");
+    }
+    const long long key = ((((long long)n_steps * 2 + b->cur) * 2 + (b->depth - 1)) * 8 + b->tile) * 32 +
+                          b->ctas_per_sm;
     auto it = b->graphs.find(key);
     if (it == b->graphs.end()) {
         cudaGraph_t g = nullptr;
@@ -536,8 +630,9 @@ extern "C" int scafes_batch_step(scafes_batch* b, int n_steps) {
         BTRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
         int rc2 = SCAFES_OK;
         cudaError_t e = cudaMemsetAsync(b->counters, 0, sizeof(int) * (size_t)n_steps, b->stream);
-        for (int s = 0; s < n_steps && e == cudaSuccess && rc2 == SCAFES_OK; ++s)
-            rc2 = enqueue_step(b, b->cur ^ (s & 1), b->counters + s);
+        if (e == cudaSuccess && pairs > 0) rc2 = enqueue_tb(b, b->cur, pairs);
+        for (int s = 0; s < singles && e == cudaSuccess && rc2 == SCAFES_OK; ++s)
+            rc2 = enqueue_step(b, b->cur ^ ((2 * pairs + s) & 1), b->counters + s);
         cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
         if (e != cudaSuccess || rc2 != SCAFES_OK || e2 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -554,7 +649,7 @@ extern "C" int scafes_batch_step(scafes_batch* b, int n_steps) {
     BTRY(b, cudaEventRecord(b->ev1, b->stream));
     b->cur ^= (n_steps & 1);
     b->t += n_steps;
-    b->launches = n_steps;
+    b->launches = pairs * (int)b->hinst.size() + singles;
     b->timed = true;
     return SCAFES_OK;
 }
@@ -632,21 +727,43 @@ extern "C" int scafes_batch_autotune(scafes_batch* b, int n_steps, int* tile_out
     BTRY(b, cudaMalloc(&save, bytes));
     cudaError_t e = cudaMemcpyAsync(save, b->pool, bytes, cudaMemcpyDeviceToDevice, b->stream);
     const int cur0 = b->cur, t0 = b->t;
-    int best_tile = b->tile, best_ctas = b->ctas_per_sm, rc = SCAFES_OK;
+    int best_tile = b->tile, best_ctas = b->ctas_per_sm, best_depth = 1, rc = SCAFES_OK;
     float best = -1.f;
     const int ctas_opts[] = {0, 1, 2, 4};
+    // Depth 1: every tile x CTAs per SM; then depth 2 (its own kernel, no
+    // tile or CTA choice), over an even number of steps for both.
+    const int trial = n_steps + (n_steps & 1);
+    b->depth = 1;
     for (int tile = 0; tile < STAR7_NUM_TILES && rc == SCAFES_OK && e == cudaSuccess; ++tile) {
         for (int ci = 0; ci < 4 && rc == SCAFES_OK && e == cudaSuccess; ++ci) {
             b->tile = tile;
             b->ctas_per_sm = ctas_opts[ci];
-            rc = scafes_batch_step(b, n_steps);  // first call captures the graph
-            if (rc == SCAFES_OK) rc = scafes_batch_step(b, n_steps);
+            rc = scafes_batch_step(b, trial);  // first call captures the graph
+            if (rc == SCAFES_OK) rc = scafes_batch_step(b, trial);
             float ms = 0.f;
             if (rc == SCAFES_OK) rc = scafes_batch_last_ms(b, &ms);
             if (rc == SCAFES_OK && (best < 0.f || ms < best)) {
                 best = ms;
                 best_tile = tile;
                 best_ctas = ctas_opts[ci];
+            }
+        }
+    }
+    b->depth_ms[0] = best;
+    b->depth_ms[1] = -1.f;
+    if (rc == SCAFES_OK && e == cudaSuccess) {
+        b->depth = 2;
+        b->tile = best_tile;
+        b->ctas_per_sm = best_ctas;
+        rc = scafes_batch_step(b, trial);
+        if (rc == SCAFES_OK) rc = scafes_batch_step(b, trial);
+        float ms = 0.f;
+        if (rc == SCAFES_OK) rc = scafes_batch_last_ms(b, &ms);
+        if (rc == SCAFES_OK) {
+            b->depth_ms[1] = ms;
+            if (ms < best) {
+                best = ms;
+                best_depth = 2;
             }
         }
     }
@@ -657,6 +774,7 @@ extern "C" int scafes_batch_autotune(scafes_batch* b, int n_steps, int* tile_out
     b->t = t0;
     b->tile = best_tile;
     b->ctas_per_sm = best_ctas;
+    b->depth = best_depth;
     b->timed = false;
     if (rc != SCAFES_OK) return rc;
     if (e != cudaSuccess) return bfail(b, SCAFES_ERR_CUDA, "scafes_batch_autotune: %s", cudaGetErrorString(e));
@@ -673,5 +791,21 @@ extern "C" int scafes_batch_set_schedule(scafes_batch* b, int tile, int ctas_per
         return bfail(b, SCAFES_ERR_ARG, "scafes_batch_set_schedule: tile %d / ctas %d out of range", tile, ctas_per_sm);
     b->tile = tile - 1;
     b->ctas_per_sm = ctas_per_sm;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_batch_set_temporal_depth(scafes_batch* b, int depth) {
+    if (!b) return bfail(nullptr, SCAFES_ERR_ARG, "scafes_batch_set_temporal_depth: batch is NULL");
+    if (depth != 1 && depth != 2)
+        return bfail(b, SCAFES_ERR_ARG, "scafes_batch_set_temporal_depth: depth %d (1 or 2)", depth);
+    b->depth = depth;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_batch_temporal_depth(const scafes_batch* b, int* depth, float* ms_depth1, float* ms_depth2) {
+    if (!b || !depth) return bfail(nullptr, SCAFES_ERR_ARG, "scafes_batch_temporal_depth: NULL argument");
+    *depth = b->depth;
+    if (ms_depth1) *ms_depth1 = b->depth_ms[0];
+    if (ms_depth2) *ms_depth2 = b->depth_ms[1];
     return SCAFES_OK;
 }

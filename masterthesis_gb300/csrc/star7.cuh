@@ -132,6 +132,9 @@ cudaError_t launch_star7(const Star7Launch& a, cudaStream_t stream);
 // encoded by star7_tb_box.  Returns cudaErrorInvalidValue for any other
 // problem.
 cudaError_t launch_star7_tb(const Star7Launch& a, cudaStream_t stream);
+// Sets the depth-2 kernels' attributes of a precision (before a stream
+// capture that launches them).
+cudaError_t launch_star7_tb_prepare(int precision);
 // TMA box (width, rows) of the depth-2 pass for a precision.
 void star7_tb_box(int precision, int* width, int* rows);
 // Whether a problem can take depth-2 passes.

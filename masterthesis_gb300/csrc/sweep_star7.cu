@@ -51,6 +51,9 @@ cudaError_t launch_star7_f32x2(const Star7Launch& a, cudaStream_t stream);
 cudaError_t launch_star7_tb_f64(const Star7Launch& a, cudaStream_t stream);
 cudaError_t launch_star7_tb_f32(const Star7Launch& a, cudaStream_t stream);
 cudaError_t launch_star7_tb_f32x2(const Star7Launch& a, cudaStream_t stream);
+cudaError_t prepare_star7_tb_f64();
+cudaError_t prepare_star7_tb_f32();
+cudaError_t prepare_star7_tb_f32x2();
 
 bool star7_tb_eligible(const Star7Launch& a) {
     return a.border == SCAFES_BORDER_DIRICHLET && a.L.nl == 1 && a.fb == nullptr && !a.vc;
@@ -67,6 +70,15 @@ cudaError_t launch_star7_tb(const Star7Launch& a, cudaStream_t stream) {
         case SCAFES_PREC_F64: return launch_star7_tb_f64(a, stream);
         case SCAFES_PREC_F32: return launch_star7_tb_f32(a, stream);
         case SCAFES_PREC_F32X2: return launch_star7_tb_f32x2(a, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_star7_tb_prepare(int precision) {
+    switch (precision) {
+        case SCAFES_PREC_F64: return prepare_star7_tb_f64();
+        case SCAFES_PREC_F32: return prepare_star7_tb_f32();
+        case SCAFES_PREC_F32X2: return prepare_star7_tb_f32x2();
         default: return cudaErrorInvalidValue;
     }
 }

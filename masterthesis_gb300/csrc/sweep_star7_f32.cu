@@ -11,4 +11,6 @@ cudaError_t launch_star7_tb_f32(const Star7Launch& a, cudaStream_t stream) {
     return launch_tb_prec<PolF32>(a, stream);
 }
 
+cudaError_t prepare_star7_tb_f32() { return prepare_tb_prec<PolF32>(); }
+
 }  // namespace scafes

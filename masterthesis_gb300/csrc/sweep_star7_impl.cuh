@@ -231,17 +231,35 @@ static int tb_zchunk(const Layout& L) {
     return zc;
 }
 
+// Shared-memory attributes of the depth-2 kernel (once; also callable
+// before a stream capture that launches it).
+template <class P, bool HAS_F>
+static cudaError_t tb_attributes() {
+    static cudaError_t done = cudaErrorNotReady;
+    if (done == cudaErrorNotReady) {
+        auto kern = star7_tb2<P, HAS_F>;
+        constexpr size_t SMEM = tb_smem(sizeof(typename P::T));
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared);
+        done = e;
+    }
+    return done;
+}
+
+template <class P>
+cudaError_t prepare_tb_prec() {
+    const cudaError_t e = tb_attributes<P, false>();
+    return e != cudaSuccess ? e : tb_attributes<P, true>();
+}
+
 template <class P, bool HAS_F>
 static cudaError_t launch_tb_typed(const Star7Launch& a, cudaStream_t stream) {
     using T = typename P::T;
     auto kern = star7_tb2<P, HAS_F>;
     constexpr size_t SMEM = tb_smem(sizeof(T));
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM);
-        cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-        attr = true;
-    }
+    if (const cudaError_t e = tb_attributes<P, HAS_F>()) return e;
     T gval;
     to_elem(a.gconst, gval);
     const Layout& L = a.L;

@@ -118,12 +118,36 @@ def test_batch_equals_looped_and_all_schedules(gpu):
                     assert np.array_equal(b.download(i), want[i]), (tile, ctas, i)
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+def test_batch_depth2_equals_looped(gpu, prec):
+    """Temporal depth 2 (two steps per pass over each instance, the plain
+    sweep's depth-2 kernel on parallel graph chains; an odd last step at
+    depth 1) gives the looped single-step results bit for bit."""
+    M = gpu
+    specs = small_ensemble(n_inst=9, seed=4)
+    T = 13
+    with make_batch(M, specs, prec) as ref:
+        ref.step_looped(T)
+        want = [ref.download(i) for i in range(len(specs))]
+    with make_batch(M, specs, prec) as b:
+        b.set_temporal_depth(2)
+        b.step(T)
+        assert b.info()["launches"] == 6 * len(specs) + 1
+        for i in range(len(specs)):
+            assert np.array_equal(b.download(i), want[i]), i
+        with pytest.raises(M.ScafesError):
+            b.set_temporal_depth(3)
+
+
 def test_batch_graph_replay_and_autotune(gpu):
     M = gpu
     specs = small_ensemble(n_inst=5, seed=5)
     with make_batch(M, specs, "f64") as b:
         tile, ctas = b.autotune(3)
         assert 1 <= tile <= 4 and ctas in (0, 1, 2, 4)
+        d = b.temporal_depth()
+        assert d["ms_depth1"] > 0.0 and d["ms_depth2"] > 0.0  # both depths measured
+        assert d["depth"] == (2 if d["ms_depth2"] < d["ms_depth1"] else 1)
         b.step(10)   # captures the graph for 10 steps
         b.step(10)   # replays it (other buffer parity: second graph)
         b.step(10)   # replays the first graph
