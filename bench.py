@@ -528,48 +528,52 @@ def adjoint_oracle_error(M, m: int = 64, T: int = 200, snaps: int = 12):
 # ---- multi-field leapfrog workloads ------------------------------------------
 
 def run_multifield(M, args, dist: Dist, hbm_peak: float):
-    """Lame-Navier 384^3 FP64 (lambda=1, mu=0.5, rho=1, seeded Gaussian bump,
-    seed 3) and Yee 512^3 FP32 and FP64 (eps=mu=1, Courant 0.5, seeded point
-    dipole, seed 4): GLUP/s over a timed run of leapfrog steps.  Algorithmic
-    bytes per node update: Lame 72 (u^n and u^{n-1} read, u^{n+1} written,
-    3 components), Yee 6 fields read + written (96 B FP64, 48 B FP32)."""
+    """Lame-Navier 384^3 in FP64 and FP32 pairs (lambda=1, mu=0.5, rho=1,
+    seeded Gaussian bump, seed 3) and Yee 512^3 in FP32, FP32 pairs and FP64
+    (eps=mu=1, Courant 0.5, seeded point dipole, seed 4): GLUP/s over a timed
+    run of leapfrog steps.  Algorithmic bytes per node update: Lame 72 (u^n
+    and u^{n-1} read, u^{n+1} written, 3 components), Yee 6 fields read +
+    written (96 B FP64 and pairs, 48 B FP32)."""
     from masterthesis_gb300 import workloads as W
     T = args.mf_time_steps
     out = {}
     n = (args.lame_n,) * 3
-    u0 = W.gaussian_bump_displacement(n, seed=3)
-    with M.MultiField(M.MF_LAME, n, W.lame_tau(n), (1.0, 0.5, 1.0)) as mf:
-        for c in range(3):
-            mf.upload(c, u0[c])
-            mf.upload(3 + c, u0[c])
-        del u0
-        mf.step(5)
-        dist.barrier()
-        mf.step(T)
-        ms = dist.max(mf.last_ms())
-    lup = float(np.prod(n)) * T
-    g = dist.world * lup / (ms * 1e-3) / 1e9
-    out["lame_f64"] = {"workload": f"Lame-Navier {n[0]}^3 FP64, leapfrog, {T} steps", "value": g, "unit": UNIT,
-                       "hbm_frac": 72 * g / hbm_peak, "bytes_per_lup": 72, "ms": ms}
     check = not args.no_oracle_error and dist.rank == 0
     E = 10  # steps of the full-size comparison with the oracle
+    for prec in ("f64", "f32x2"):
+        u0 = W.gaussian_bump_displacement(n, seed=3)
+        with M.MultiField(M.MF_LAME, n, W.lame_tau(n), (1.0, 0.5, 1.0), precision=prec) as mf:
+            for c in range(3):
+                mf.upload(c, u0[c])
+                mf.upload(3 + c, u0[c])
+            del u0
+            mf.step(5)
+            dist.barrier()
+            mf.step(T)
+            ms = dist.max(mf.last_ms())
+        lup = float(np.prod(n)) * T
+        g = dist.world * lup / (ms * 1e-3) / 1e9
+        out[f"lame_{prec}"] = {"workload": f"Lame-Navier {n[0]}^3 {prec.upper()}, leapfrog, {T} steps", "value": g,
+                               "unit": UNIT, "hbm_frac": 72 * g / hbm_peak, "bytes_per_lup": 72, "ms": ms}
     if check:
         import oracle as O
         threads = os.cpu_count() or 1
         u0 = W.gaussian_bump_displacement(n, seed=3)
-        with M.MultiField(M.MF_LAME, n, W.lame_tau(n), (1.0, 0.5, 1.0)) as mf:
-            for c in range(3):
-                mf.upload(c, u0[c])
-                mf.upload(3 + c, u0[c])
-            mf.step(E)
-            u = np.stack([mf.download(c) for c in range(3)])
         ref, _ = O.lame(O.make_grid(n, tau=W.lame_tau(n)), u0, u0, E, 1.0, 0.5, 1.0, nthreads=threads)
-        out["lame_f64"]["error_vs_oracle"] = {"max_rel": rel_err(u, ref),
-                                              "sample": f"{n[0]}^3, first {E} steps (full grid)"}
-        del u0, u, ref
+        for prec in ("f64", "f32x2"):
+            with M.MultiField(M.MF_LAME, n, W.lame_tau(n), (1.0, 0.5, 1.0), precision=prec) as mf:
+                for c in range(3):
+                    mf.upload(c, u0[c])
+                    mf.upload(3 + c, u0[c])
+                mf.step(E)
+                u = np.stack([mf.download(c) for c in range(3)])
+            out[f"lame_{prec}"]["error_vs_oracle"] = {"max_rel": rel_err(u, ref),
+                                                      "sample": f"{n[0]}^3, first {E} steps (full grid)"}
+            del u
+        del u0, ref
     n = (args.yee_n,) * 3
     tau, src, par = W.yee_setup(n)
-    for prec, bpl in (("f32", 48), ("f64", 96)):
+    for prec, bpl in (("f32", 48), ("f32x2", 96), ("f64", 96)):
         with M.MultiField(M.MF_YEE, n, tau, par, precision=prec, src=src) as mf:
             mf.step(5)
             dist.barrier()
@@ -584,7 +588,7 @@ def run_multifield(M, args, dist: Dist, hbm_peak: float):
         # Both precisions against the oracle after 2E steps from the
         # workload's initial state (zero fields, the dipole switched on).
         ref = O.yee(O.make_grid(n, tau=tau), np.zeros((6, n[2], n[1], n[0])), 2 * E, src, *par, nthreads=threads)
-        for prec in ("f32", "f64"):
+        for prec in ("f32", "f32x2", "f64"):
             with M.MultiField(M.MF_YEE, n, tau, par, precision=prec, src=src) as mf:
                 mf.step(2 * E)
                 f = np.stack([mf.download(i) for i in range(6)])

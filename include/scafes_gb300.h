@@ -450,11 +450,15 @@ void scafes_gpu_batch_destroy(scafes_gpu_batch* q);
  *     central differences incl. the 4-point mixed difference, border 0
  *     (examples/LameNavierEqnFDM/LameNavierEqnFDM.hpp:269-378 is the
  *     reference's form; it cannot advance, :23-25).  p = {lambda, mu, rho}.
- *     Fields 0..2: u^n (x, y, z), 3..5: u^{n-1}.  FP64.
+ *     Fields 0..2: u^n (x, y, z), 3..5: u^{n-1}.  FP64 or FP32 pairs.
  *  SCAFES_MF_YEE   Yee FDTD in a PEC box (eps = mu = 1), H half step then
  *     E step (examples/EMFDTD/EMFDTD.hpp:295-385 without CPML), soft
  *     current source Ez[src] -= tau*amp*exp(-((t-t0)/w)^2) sin(2 pi f t).
- *     p = {amp, t0, w, f}.  Fields 0..5: Ex, Ey, Ez, Hx, Hy, Hz.  FP64/FP32. */
+ *     p = {amp, t0, w, f}.  Fields 0..5: Ex, Ey, Ez, Hx, Hy, Hz.  FP64, FP32
+ *     or FP32 pairs.
+ * FP32 pairs (SCAFES_PREC_F32X2): each value hi + lo, 8 bytes as FP64, the
+ * update in compensated FP32 arithmetic (errors of relative size ~2^-48 per
+ * step) with no FP64 instruction. */
 enum scafes_mf_kind { SCAFES_MF_LAME = 0, SCAFES_MF_YEE = 1 };
 
 typedef struct scafes_mf_cfg {
@@ -464,7 +468,7 @@ typedef struct scafes_mf_cfg {
     double coord_last[3];
     double tau;
     double t_start;
-    int precision;           /* SCAFES_PREC_F64 (both) or SCAFES_PREC_F32 (Yee) */
+    int precision;           /* SCAFES_PREC_F64 or _F32X2 (both), SCAFES_PREC_F32 (Yee) */
     double p[8];             /* problem parameters, see above */
     int src[3];              /* Yee source node */
     void* stream;

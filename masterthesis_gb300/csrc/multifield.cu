@@ -15,13 +15,16 @@
 // Both are FP64-issue-bound on GB300 (Lame: ~57 FP64 operations per node,
 // Yee: ~24 per cell and step), so the kernels read neighbours straight from
 // global memory through L1 instead of staging tiles: one thread per (x, y)
-// column marches a chunk of 16 z-planes.
+// column marches a chunk of 16 z-planes.  The FP32-pair kernels (k_lame_x2,
+// k_yee_h_x2, k_yee_e_x2) keep the same layout and bytes per node and move
+// the arithmetic to the FP32 pipe.
 #include <cstdarg>
 #include <cmath>
 #include <cstdio>
 #include <string>
 
 #include "scafes_common.cuh"
+#include "star7.cuh"
 #include "tma.cuh"
 #include "../../include/scafes_gb300.h"
 
@@ -114,6 +117,181 @@ k_yee_e(T* __restrict__ ex, T* __restrict__ ey, T* __restrict__ ez, const T* __r
         if (z + 1 < L.nz && xin && yin) {
             T v = ez[m] + ch * ((hy[m] - hy[m - 1]) - (hx[m] - hx[m - L.pitch]));
             if (m == src) v -= src_val;
+            ez[m] = v;
+        }
+    }
+}
+
+// ---- compensated FP32 pairs (SCAFES_PREC_F32X2) -----------------------------
+//
+// Each value is a pair hi + lo of floats (8 bytes, as FP64).  A node update
+// is a sum of products c * S of host-split coefficients (c = h + l + ll,
+// ~72 bits) and operands S formed from neighbour differences or sums whose
+// hi parts are combined exactly (TwoSum) and whose lo parts and rounding
+// errors ride along in an FP32 tail.  The products' hi parts are exact
+// (FMA TwoProd) and summed with TwoSum; everything of relative size 2^-24
+// goes into one FP32 error term, so a step carries errors of relative size
+// about 2^-48, and the pair is renormalised once per node (FastTwoSum).
+// No FP64 instruction is issued.
+
+struct C3 { float h, l, ll; };
+
+C3 split3(double d) {
+    C3 c;
+    c.h = (float)d;
+    const double r = d - (double)c.h;
+    c.l = (float)r;
+    c.ll = (float)(r - (double)c.l);
+    return c;
+}
+
+struct LameCoefX2 {
+    C3 d[3];      // centre weight of component c: 2 - 2 sum_p a[c][p]
+    C3 a[3][3];   // as LameCoef
+    C3 b[3][3];
+};
+
+// An operand S + t: hi part exact, t its FP32 tail.
+struct Op { float s, t; };
+
+__device__ __forceinline__ Op op_sum(float2 a, float2 b) {
+    const f2 r = two_sum(a.x, b.x);
+    return {r.hi, r.lo + (a.y + b.y)};
+}
+
+__device__ __forceinline__ Op op_diff(float2 a, float2 b) {
+    const f2 r = two_sum(a.x, -b.x);
+    return {r.hi, r.lo + (a.y - b.y)};
+}
+
+// (a - b) - (c - d)
+__device__ __forceinline__ Op op_diff2(float2 a, float2 b, float2 c, float2 d) {
+    const Op p = op_diff(a, b), q = op_diff(c, d);
+    const f2 r = two_sum(p.s, -q.s);
+    return {r.hi, r.lo + (p.t - q.t)};
+}
+
+// Running sum: H exact-ish hi, E the FP32 error term.
+struct PAcc { float H, E; };
+
+// acc += c * (S + t)
+__device__ __forceinline__ void pa_prod(PAcc& acc, const C3& c, Op o) {
+    const float p = c.h * o.s;
+    float e = fmaf(c.h, o.s, -p);
+    e = fmaf(c.l, o.s, e);
+    e = fmaf(c.h, o.t, e);
+    e = fmaf(c.ll, o.s, e);
+    const f2 r = two_sum(acc.H, p);
+    acc.H = r.hi;
+    acc.E += r.lo + e;
+}
+
+// acc += sign * v (a pair)
+__device__ __forceinline__ void pa_add(PAcc& acc, float2 v, float sign) {
+    const f2 r = two_sum(acc.H, sign * v.x);
+    acc.H = r.hi;
+    acc.E += r.lo + sign * v.y;
+}
+
+__device__ __forceinline__ float2 pa_result(PAcc acc) {
+    const f2 r = fast_two_sum(acc.H, acc.E);
+    return make_float2(r.hi, r.lo);
+}
+
+// Lame-Navier step on pairs: u^{n+1} = d_c u + sum_p a_cp (u(+p) + u(-p))
+// + sum_q b_cq ((u_q(+c+q) - u_q(+c-q)) - (u_q(-c+q) - u_q(-c-q))) - u^{n-1},
+// the FP64 form rearranged with the centre weight d_c = 2 - 2 sum_p a_cp.
+__global__ void __launch_bounds__(MX * MY)
+k_lame_x2(const float2* __restrict__ u, float2* __restrict__ up, LameCoefX2 K, Layout L, long long comp) {
+    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
+    const long long st[3] = {1, L.pitch, L.plane};
+    const int z0 = blockIdx.z * MZ, z1 = min(z0 + MZ, L.nz);
+    const float2 zero = make_float2(0.f, 0.f);
+    for (int z = z0; z < z1; ++z) {
+        const long long m = L.idx(x, y, z);
+        if (colb || z == 0 || z == L.nz - 1) {
+            up[m] = zero;
+            up[m + comp] = zero;
+            up[m + 2 * comp] = zero;
+            continue;
+        }
+        float2 out[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float2* uc = u + c * comp;
+            const float2 uv = uc[m];
+            PAcc acc{0.f, 0.f};
+            pa_prod(acc, K.d[c], Op{uv.x, uv.y});
+            pa_add(acc, up[m + c * comp], -1.f);
+#pragma unroll
+            for (int p = 0; p < 3; ++p) pa_prod(acc, K.a[c][p], op_sum(uc[m + st[p]], uc[m - st[p]]));
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                if (q == c) continue;
+                const float2* uq = u + q * comp;
+                const long long sp = st[c], sq = st[q];
+                pa_prod(acc, K.b[c][q],
+                        op_diff2(uq[m + sp + sq], uq[m + sp - sq], uq[m - sp + sq], uq[m - sp - sq]));
+            }
+            out[c] = pa_result(acc);
+        }
+        up[m] = out[0];
+        up[m + comp] = out[1];
+        up[m + 2 * comp] = out[2];
+    }
+}
+
+// v + sign * ch * ((a - b) - (c - d)) on pairs.
+__device__ __forceinline__ float2 yee_upd(float2 v, const C3& ch, float sign, float2 a, float2 b, float2 c,
+                                          float2 d) {
+    PAcc acc{v.x, v.y};
+    const C3 cs{sign * ch.h, sign * ch.l, sign * ch.ll};
+    pa_prod(acc, cs, op_diff2(a, b, c, d));
+    return pa_result(acc);
+}
+
+// Yee H half step on pairs (the staggering of k_yee_h).
+__global__ void __launch_bounds__(MX * MY)
+k_yee_h_x2(const float2* __restrict__ ex, const float2* __restrict__ ey, const float2* __restrict__ ez,
+           float2* __restrict__ hx, float2* __restrict__ hy, float2* __restrict__ hz, Layout L, C3 ch) {
+    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const int z0 = blockIdx.z * MZ, z1 = min(z0 + MZ, L.nz);
+    for (int z = z0; z < z1; ++z) {
+        const long long m = L.idx(x, y, z);
+        const bool xi = x + 1 < L.nx, yi = y + 1 < L.ny, zi = z + 1 < L.nz;
+        if (yi && zi) hx[m] = yee_upd(hx[m], ch, -1.f, ez[m + L.pitch], ez[m], ey[m + L.plane], ey[m]);
+        if (xi && zi) hy[m] = yee_upd(hy[m], ch, -1.f, ex[m + L.plane], ex[m], ez[m + 1], ez[m]);
+        if (xi && yi) hz[m] = yee_upd(hz[m], ch, -1.f, ey[m + 1], ey[m], ex[m + L.pitch], ex[m]);
+    }
+}
+
+// Yee E step on pairs with PEC walls and the soft source (src_val: the
+// host-split tau*J(t)).
+__global__ void __launch_bounds__(MX * MY)
+k_yee_e_x2(float2* __restrict__ ex, float2* __restrict__ ey, float2* __restrict__ ez, const float2* __restrict__ hx,
+           const float2* __restrict__ hy, const float2* __restrict__ hz, Layout L, C3 ch, long long src,
+           float2 src_val) {
+    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
+    if (x >= L.nx || y >= L.ny) return;
+    const int z0 = blockIdx.z * MZ, z1 = min(z0 + MZ, L.nz);
+    const bool xin = x > 0 && x + 1 < L.nx, yin = y > 0 && y + 1 < L.ny;
+    for (int z = z0; z < z1; ++z) {
+        const long long m = L.idx(x, y, z);
+        const bool zin = z > 0 && z + 1 < L.nz;
+        if (x + 1 < L.nx && yin && zin)
+            ex[m] = yee_upd(ex[m], ch, 1.f, hz[m], hz[m - L.pitch], hy[m], hy[m - L.plane]);
+        if (y + 1 < L.ny && xin && zin)
+            ey[m] = yee_upd(ey[m], ch, 1.f, hx[m], hx[m - L.plane], hz[m], hz[m - 1]);
+        if (z + 1 < L.nz && xin && yin) {
+            float2 v = yee_upd(ez[m], ch, 1.f, hy[m], hy[m - 1], hx[m], hx[m - L.pitch]);
+            if (m == src) {
+                PAcc acc{v.x, v.y};
+                pa_add(acc, src_val, -1.f);
+                v = pa_result(acc);
+            }
             ez[m] = v;
         }
     }
@@ -409,10 +587,11 @@ extern "C" int scafes_mf_create(const scafes_mf_cfg* cfg, scafes_mf** out) {
     for (int p = 0; p < 3; ++p)
         if (cfg->n_nodes[p] < 3 || cfg->n_nodes[p] > (1 << 16))
             return mfail(nullptr, SCAFES_ERR_ARG, "scafes_mf_create: n_nodes[%d]=%d out of [3, 65536]", p, cfg->n_nodes[p]);
-    if (cfg->kind == SCAFES_MF_LAME && cfg->precision != SCAFES_PREC_F64)
-        return mfail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_mf_create: Lame-Navier runs in FP64 only");
-    if (cfg->kind == SCAFES_MF_YEE && cfg->precision != SCAFES_PREC_F64 && cfg->precision != SCAFES_PREC_F32)
-        return mfail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_mf_create: Yee runs in FP64 or FP32");
+    if (cfg->kind == SCAFES_MF_LAME && cfg->precision != SCAFES_PREC_F64 && cfg->precision != SCAFES_PREC_F32X2)
+        return mfail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_mf_create: Lame-Navier runs in FP64 or FP32 pairs");
+    if (cfg->kind == SCAFES_MF_YEE && cfg->precision != SCAFES_PREC_F64 && cfg->precision != SCAFES_PREC_F32 &&
+        cfg->precision != SCAFES_PREC_F32X2)
+        return mfail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_mf_create: Yee runs in FP64, FP32 or FP32 pairs");
     if (cfg->kind == SCAFES_MF_YEE)
         for (int p = 0; p < 3; ++p)
             if (cfg->src[p] < 0 || cfg->src[p] >= cfg->n_nodes[p])
@@ -494,7 +673,8 @@ extern "C" int scafes_mf_upload(scafes_mf* h, int field, const double* host, siz
     if (n != (size_t)h->L.nx * h->L.ny * h->L.nz) return mfail(h, SCAFES_ERR_ARG, "scafes_mf_upload: wrong size");
     MTRY(h, cudaMemcpyAsync(h->stage, host, n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     char* f = field_ptr(h, phys_field(h, field));
-    if (h->esz == 8) k_dense_to_field<double><<<256, 256, 0, h->stream>>>(h->stage, (double*)f, h->L);
+    if (h->cfg.precision == SCAFES_PREC_F32X2) MTRY(h, convert_to_device(SCAFES_PREC_F32X2, h->stage, f, h->L, h->stream));
+    else if (h->esz == 8) k_dense_to_field<double><<<256, 256, 0, h->stream>>>(h->stage, (double*)f, h->L);
     else k_dense_to_field<float><<<256, 256, 0, h->stream>>>(h->stage, (float*)f, h->L);
     MTRY(h, cudaGetLastError());
     MTRY(h, cudaStreamSynchronize(h->stream));
@@ -509,7 +689,9 @@ extern "C" int scafes_mf_download(scafes_mf* h, int field, double* host, size_t 
     const int st = mf_status(h);
     if (st) return st;
     const char* f = field_ptr(h, phys_field(h, field));
-    if (h->esz == 8) k_field_to_dense<double><<<256, 256, 0, h->stream>>>((const double*)f, h->stage, h->L);
+    if (h->cfg.precision == SCAFES_PREC_F32X2)
+        MTRY(h, convert_from_device(SCAFES_PREC_F32X2, f, h->stage, h->L, h->stream));
+    else if (h->esz == 8) k_field_to_dense<double><<<256, 256, 0, h->stream>>>((const double*)f, h->stage, h->L);
     else k_field_to_dense<float><<<256, 256, 0, h->stream>>>((const float*)f, h->stage, h->L);
     MTRY(h, cudaGetLastError());
     MTRY(h, cudaMemcpyAsync(host, h->stage, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -535,10 +717,24 @@ extern "C" int scafes_mf_step(scafes_mf* h, int n_steps) {
                 K.b[cc][p] = (p == cc) ? 0.0 : s * (lam + mu) / (4.0 * hh[cc] * hh[p]);
             }
         const long long comp = L.size();
+        LameCoefX2 K2;
+        for (int cc = 0; cc < 3; ++cc) {
+            double sa = 0.0;
+            for (int p = 0; p < 3; ++p) {
+                K2.a[cc][p] = split3(K.a[cc][p]);
+                K2.b[cc][p] = split3(K.b[cc][p]);
+                sa += K.a[cc][p];
+            }
+            K2.d[cc] = split3(2.0 - 2.0 * sa);
+        }
+        const bool x2 = c.precision == SCAFES_PREC_F32X2;
         for (int st = 0; st < n_steps; ++st) {
-            const double* u = (const double*)field_ptr(h, 3 * h->cur);
-            double* up = (double*)field_ptr(h, 3 * (h->cur ^ 1));
-            k_lame<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(u, up, K, L, comp);
+            void* u = field_ptr(h, 3 * h->cur);
+            void* up = field_ptr(h, 3 * (h->cur ^ 1));
+            if (x2)
+                k_lame_x2<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>((const float2*)u, (float2*)up, K2, L, comp);
+            else
+                k_lame<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>((const double*)u, (double*)up, K, L, comp);
             MTRY(h, cudaGetLastError());
             h->cur ^= 1;
             h->t += 1;
@@ -552,7 +748,15 @@ extern "C" int scafes_mf_step(scafes_mf* h, int n_steps) {
             const double time = c.t_start + (h->t + 1) * c.tau;
             const double a = (time - t0) / w;
             const double sv = c.tau * amp * std::exp(-a * a) * std::sin(2.0 * 3.14159265358979323846 * freq * time);
-            if (h->esz == 8) {
+            if (c.precision == SCAFES_PREC_F32X2) {
+                float2* f[6];
+                for (int i = 0; i < 6; ++i) f[i] = (float2*)field_ptr(h, i);
+                const C3 chs = split3(ch);
+                const f2 sp = split_double(sv);
+                k_yee_h_x2<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L, chs);
+                k_yee_e_x2<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L, chs,
+                                                                     src, make_float2(sp.hi, sp.lo));
+            } else if (h->esz == 8) {
                 double* f[6];
                 for (int i = 0; i < 6; ++i) f[i] = (double*)field_ptr(h, i);
                 k_yee_h<double><<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L, ch);

@@ -1,6 +1,7 @@
 """Multi-field leapfrog workloads (C ABI, CUDA) against their oracle
 restatements (orc_lame, orc_yee), plus size-independent properties.
-Tolerances: 1e-12 relative max-norm for FP64, 1e-4 for FP32 (Yee)."""
+Tolerances: 1e-12 relative max-norm for FP64 and FP32 pairs, 1e-4 for
+FP32 (Yee)."""
 from __future__ import annotations
 
 import numpy as np
@@ -15,8 +16,8 @@ pytestmark = pytest.mark.gpu
 LAME = (1.0, 0.5, 1.0)  # lambda, mu, rho
 
 
-def run_lame(M, n, T, u0, tau):
-    with M.MultiField(M.MF_LAME, n, tau, LAME) as mf:
+def run_lame(M, n, T, u0, tau, prec="f64"):
+    with M.MultiField(M.MF_LAME, n, tau, LAME, precision=prec) as mf:
         for c in range(3):
             mf.upload(c, u0[c])
             mf.upload(3 + c, u0[c])
@@ -24,13 +25,14 @@ def run_lame(M, n, T, u0, tau):
         return np.stack([mf.download(c) for c in range(3)]), np.stack([mf.download(3 + c) for c in range(3)])
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
 @pytest.mark.parametrize("n", [(13, 11, 9), (40, 33, 35)])
-def test_lame_matches_oracle(gpu, n):
+def test_lame_matches_oracle(gpu, n, prec):
     M = gpu
     T = 30
     u0 = W.gaussian_bump_displacement(n, seed=3)
     tau = W.lame_tau(n)
-    u, up = run_lame(M, n, T, u0, tau)
+    u, up = run_lame(M, n, T, u0, tau, prec)
     g = O.make_grid(n, tau=tau)
     ru, rup = O.lame(g, u0, u0, T, *LAME)
     assert cases.rel_err(u, ru) <= 1e-12
@@ -54,7 +56,8 @@ def yee_fields_zero(n):
 
 
 @pytest.mark.parametrize("prec,tol,n", [("f64", 1e-12, (20, 18, 16)), ("f32", 1e-4, (20, 18, 16)),
-                                        ("f32", 1e-4, (37, 29, 41)), ("f64", 1e-12, (37, 29, 41))])
+                                        ("f32", 1e-4, (37, 29, 41)), ("f64", 1e-12, (37, 29, 41)),
+                                        ("f32x2", 1e-12, (20, 18, 16)), ("f32x2", 1e-12, (37, 29, 41))])
 def test_yee_matches_oracle(gpu, prec, tol, n):
     """FP32 runs the fused one-pass step (tiles, halos and z-chunks cut
     across these odd sizes), FP64 the two-kernel step."""
@@ -103,6 +106,28 @@ def test_yee_energy_bounded_after_source(gpu):
     assert e1 > 0.0
     assert e2 <= e1 * 1.05
     assert e2 >= e1 * 0.95
+
+
+def test_pairs_at_full_size_track_f64(gpu):
+    """Lame 384^3 x 10 steps and Yee 256^3 x 60 steps: the FP32-pair runs
+    against the FP64 runs (relative max-norm 1e-12)."""
+    M = gpu
+    n = (384, 384, 384)
+    u0 = W.gaussian_bump_displacement(n, seed=3)
+    a, _ = run_lame(M, n, 10, u0, W.lame_tau(n), "f64")
+    b, _ = run_lame(M, n, 10, u0, W.lame_tau(n), "f32x2")
+    del u0
+    assert cases.rel_err(b, a) <= 1e-12
+    del a, b
+    n, T = (256, 256, 256), 60
+    tau, src, par = W.yee_setup(n)
+    out = {}
+    for prec in ("f64", "f32x2"):
+        with M.MultiField(M.MF_YEE, n, tau, par, precision=prec, src=src) as mf:
+            mf.step(T)
+            out[prec] = np.stack([mf.download(i) for i in range(6)])
+    assert np.max(np.abs(out["f64"])) > 0.0
+    assert cases.rel_err(out["f32x2"], out["f64"]) <= 1e-12
 
 
 def test_multifield_errors(gpu):
