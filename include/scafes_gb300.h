@@ -618,10 +618,9 @@ int scafes_gpu_adjoint(scafes_handle* h, const double* dJ_du_T, double* dJ_dk,
 
 /* No counterpart in the reference.  The same max-norm check as
  * scafes_gpu_err_linf, for callers that must not allocate device memory at
- * the point of the call -- a time loop being recorded into a CUDA graph, a
- * serving loop that forbids cudaMalloc after start-up (it can synchronise
- * the device and fail under memory pressure), or a host whose device memory
- * all comes from its own pool.  It allocates nothing: u and exact are
+ * the point of the call -- a serving loop that forbids cudaMalloc after
+ * start-up (it can synchronise the device and fail under memory pressure),
+ * or a host whose device memory all comes from its own pool.  It allocates nothing: u and exact are
  * caller-owned device arrays of n doubles, out is a caller-owned device
  * array of 2 doubles that receives max|u - exact| and max|exact|, and the
  * partial maxima live in a fixed 256 KiB array in the library's device

@@ -2,12 +2,11 @@
 //
 // Who needs this: some callers of the stencil engine are not allowed to
 // call cudaMalloc at the point where they want an error check.  Examples
-// are a time loop that is being recorded into a CUDA graph (allocation is
-// not a capturable operation), a serving or real-time loop whose owner
-// forbids allocation after start-up because cudaMalloc can synchronise the
-// device and fail under memory pressure at any moment, and a host program
-// that hands us device memory from its own pool allocator and must not have
-// us grab memory behind its back.  scafes_gpu_err_linf keeps its partial
+// are a serving or real-time loop whose owner forbids allocation after
+// start-up because cudaMalloc can synchronise the device and fail under
+// memory pressure at any moment, and a host program that hands us device
+// memory from its own pool allocator and must not have us grab memory
+// behind its back.  scafes_gpu_err_linf keeps its partial
 // maxima in a buffer that scafes_gpu_create allocates, so it is not usable
 // without a handle; this entry point works on caller-owned device arrays and
 // keeps its partial maxima in a fixed array in the library's device image.

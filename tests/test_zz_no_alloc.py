@@ -1,9 +1,8 @@
 """The allocation-free max-norm check (scafes_err_linf_noalloc).
 
 This entry point exists for callers that must not allocate device memory
-where they check the error -- a time loop being recorded into a CUDA graph,
-a serving loop that forbids cudaMalloc after start-up, a host whose device
-memory all comes from its own pool.  It keeps its partial maxima in a fixed
+where they check the error -- a serving loop that forbids cudaMalloc after
+start-up, a host whose device memory all comes from its own pool.  It keeps its partial maxima in a fixed
 array inside the library instead of a buffer made by scafes_gpu_create.
 
 The test checks it through the C ABI against the handle-based
