@@ -292,6 +292,19 @@ int scafes_gpu_step(scafes_handle* h, int n_steps);
  * upload.  Synchronises the handle's stream. */
 int scafes_gpu_download(scafes_handle* h, int field, double* host, size_t n);
 
+/* No counterpart in the reference (its fields live in host memory).  The
+ * unknown field's upload and download enqueued on the handle's stream
+ * without waiting: the host array must stay valid and unchanged (upload) or
+ * unread (download) until scafes_gpu_synchronize returns, and should be
+ * page-locked (scafes_host_alloc, cudaHostAlloc) for the copy to overlap
+ * other work.  With two handles on two streams a caller overlaps one
+ * problem's copies with the other's sweeps. */
+int scafes_gpu_upload_async(scafes_handle* h, const double* host, size_t n);
+int scafes_gpu_download_async(scafes_handle* h, double* host, size_t n);
+/* Waits for the handle's stream and reports a sweep that gave up waiting
+ * for its loads (SCAFES_ERR_TIMEOUT), as scafes_gpu_download does. */
+int scafes_gpu_synchronize(scafes_handle* h);
+
 /* No counterpart in the reference (its node loop has no tunables): times
  * n_steps sweeps with each tile variant of the sweep kernel (32 x BY CTA
  * tile, R rows per thread) on the uploaded problem, keeps the fastest for

@@ -107,6 +107,9 @@ def lib() -> C.CDLL:
                                            C.POINTER(C.c_double)]
         L.scafes_gpu_upload.argtypes = [vp, C.c_int, dp, C.c_size_t]
         L.scafes_gpu_download.argtypes = [vp, C.c_int, dp, C.c_size_t]
+        L.scafes_gpu_upload_async.argtypes = [vp, dp, C.c_size_t]
+        L.scafes_gpu_download_async.argtypes = [vp, dp, C.c_size_t]
+        L.scafes_gpu_synchronize.argtypes = [vp]
         L.scafes_gpu_step.argtypes = [vp, C.c_int]
         L.scafes_gpu_keep_initial.argtypes = [vp, C.c_int]
         L.scafes_gpu_adjoint.argtypes = [vp, dp, dp, dp, C.c_int]
@@ -297,6 +300,24 @@ class Plain:
 
     def step(self, n_steps: int):
         _check(lib().scafes_gpu_step(self.h, n_steps), self.h)
+
+    def upload_async(self, arr: np.ndarray):
+        """Enqueues the upload of the unknown field (scafes_gpu_upload_async):
+        `arr` (C-contiguous float64, ideally page-locked, e.g. a HostArray)
+        must stay unchanged until synchronize() returns."""
+        if arr.dtype != np.float64 or not arr.flags.c_contiguous or arr.size != int(np.prod(self.n)):
+            raise ValueError("upload_async needs a C-contiguous float64 array of the grid's size")
+        _check(lib().scafes_gpu_upload_async(self.h, _dp(arr), arr.size), self.h)
+
+    def download_async(self, out: np.ndarray):
+        """Enqueues the download of the current iterate into `out`, valid once
+        synchronize() returns."""
+        if out.dtype != np.float64 or not out.flags.c_contiguous or out.size != int(np.prod(self.n)):
+            raise ValueError("download_async needs a C-contiguous float64 array of the grid's size")
+        _check(lib().scafes_gpu_download_async(self.h, _dp(out), out.size), self.h)
+
+    def synchronize(self):
+        _check(lib().scafes_gpu_synchronize(self.h), self.h)
 
     def keep_initial(self, on: bool = True):
         """Keeps an FP64 device copy of every later upload of the unknown

@@ -374,6 +374,9 @@ constexpr int RO_Y = RO_X + pad16(FXW * FXH), RO_Z = RO_Y + pad16(FYW * FYH), RO
 constexpr int RSLOT = RO_D + pad16(FKW * FKH);
 constexpr uint32_t RTX_BYTES = (uint32_t)(2 * RLW * RLH + FXW * FXH + FYW * FYH + 2 * FKW * FKH) * 8u;
 constexpr size_t RSMEM = (size_t)RNS * RSLOT * 8 + RNS * 8;
+// FP64 fields: the lambda and u boxes of two planes also as FP32 pairs.
+constexpr int RPAIR = pad16(RLW * RLH);
+constexpr size_t RSMEM_F64 = (size_t)RNS * RSLOT * 8 + (size_t)4 * RPAIR * 8 + RNS * 8;
 static_assert(RSLOT * 8 % 128 == 0 && RO_U * 8 % 128 == 0 && RO_X * 8 % 128 == 0, "TMA destinations 128-byte aligned");
 
 // (u_b - u_a)(l_b - l_a) as an unnormalised pair.
@@ -407,7 +410,11 @@ __device__ __forceinline__ float2 pview(double v) { return pbits(v); }
 // arithmetic.  E = double: lambda, u, the faces and the diagonal FP64 and
 // the lambda update in FP64 in the order of k_forward (diagonal, +x, -x,
 // +y, -y, +z, -z; 7 FP64 operations per node), the gradient in FP32 pairs
-// from integer splits of u and lambda (no FP64 instruction).
+// from integer splits of u and lambda (no FP64 instruction).  With FP64
+// fields the lambda and u boxes of each plane are split once, cooperatively,
+// into a two-plane ring of pairs in shared memory when the plane arrives
+// (each node's neighbours then read pairs instead of splitting them again);
+// the centre values' pairs travel in registers from the plane above.
 template <class E>
 __global__ void __launch_bounds__(RTX * RTY)
 k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__ CUtensorMap tu,
@@ -418,7 +425,8 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
     constexpr bool F64 = std::is_same<E, double>::value;
     extern __shared__ __align__(128) unsigned char rsm_raw[];
     E* rsm = reinterpret_cast<E*>(rsm_raw);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(rsm + RNS * RSLOT);
+    float2* pring = reinterpret_cast<float2*>(rsm + RNS * RSLOT);  // F64: [2 planes][lambda, u][RPAIR]
+    uint64_t* bar = reinterpret_cast<uint64_t*>(rsm + RNS * RSLOT + (F64 ? 4 * RPAIR : 0));
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * RTX + tx;
     const int x0 = blockIdx.x * RTX, y0 = blockIdx.y * RTY;
     const int z0 = blockIdx.z * RZ_, z1 = min(z0 + RZ_, L.nz);
@@ -459,6 +467,18 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
     const int bk = ty * FKW + tx;
     const float2 zero = make_float2(0.f, 0.f);
     const E ezero = E{};
+    constexpr int NT = RTX * RTY;
+    // F64: input plane j's lambda and u boxes as pairs into ring slot j & 1.
+    auto to_pairs = [&](int j) {
+        if constexpr (F64) {
+            const E* sj = rsm + (j & (RNS - 1)) * RSLOT;
+            float2* pj = pring + (j & 1) * 2 * RPAIR;
+            for (int i = tid; i < RLW * RLH; i += NT) {
+                pj[i] = pview(sj[RO_L + i]);
+                pj[RPAIR + i] = pview(sj[RO_U + i]);
+            }
+        }
+    };
     long long o = live ? L.idx(x, y, z0) : 0;
     float2 gn = live ? g[o] : zero;
     bool ok = wait(0);
@@ -466,9 +486,11 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
     E ub = z0 > 0 ? rsm[RO_U + bl] : ezero;
     E kzb = z0 > 0 ? rsm[RO_Z + bk] : ezero;
     ok = wait(1) && ok;
+    to_pairs(1);
+    // Pairs of the centre values of plane z0, then of each plane in turn.
+    float2 plc = pview(rsm[RSLOT + RO_L + bl]), puc = pview(rsm[RSLOT + RO_U + bl]);
     // The z-face product of the plane below (face z-1 | z).
-    f2 pzb = z0 > 0 ? pface(pview(ub), pview(rsm[RSLOT + RO_U + bl]), pview(lb), pview(rsm[RSLOT + RO_L + bl]))
-                    : f2{0.f, 0.f};
+    f2 pzb = z0 > 0 ? pface(pview(ub), puc, pview(lb), plc) : f2{0.f, 0.f};
     int issued = RNS - 1;
     for (int z = z0; z < z1; ++z, o += L.plane) {
         const int jc = z - z0 + 1;  // input plane of z
@@ -484,24 +506,34 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
         const float2 gc = gn;
         if (live && z + 1 < z1) gn = g[o + L.plane];
         ok = wait(jc + 1) && ok;  // plane z+1
+        to_pairs(jc + 1);         // read from the next iteration on (after its barrier)
         const E* sc = rsm + (jc & (RNS - 1)) * RSLOT;
         const E* sa = rsm + ((jc + 1) & (RNS - 1)) * RSLOT;
+        const float2* ppl = pring + (jc & 1) * 2 * RPAIR;  // F64: plane z's pairs
+        const float2* ppu = ppl + RPAIR;
+        auto PL = [&](int i) -> float2 {
+            if constexpr (F64) return ppl[i];
+            else return pview(sc[RO_L + i]);
+        };
+        auto PU = [&](int i) -> float2 {
+            if constexpr (F64) return ppu[i];
+            else return pview(sc[RO_U + i]);
+        };
         const bool top = z + 1 < L.nz;
         const E la = top ? sa[RO_L + bl] : ezero;
         const E ua = top ? sa[RO_U + bl] : ezero;
-        const E lc = sc[RO_L + bl], uc = sc[RO_U + bl];
+        const E lc = sc[RO_L + bl];
         const E kzc = sc[RO_Z + bk];
-        const float2 plc = pview(lc), puc = pview(uc);
-        const f2 pza = pface(puc, pview(ua), plc, pview(la));  // face z | z+1
+        const float2 pla = pview(la), pua = pview(ua);
+        const f2 pza = pface(puc, pua, plc, pla);  // face z | z+1
         if (live) {
             const bool border = colb || z == 0 || z == L.nz - 1;
             const E lxp = sc[RO_L + bl + 1], lxm = sc[RO_L + bl - 1];
             const E lyp = sc[RO_L + bl + RLW], lym = sc[RO_L + bl - RLW];
             // dJ/dk_i: the two faces along each axis.
-            f2 gk = pscale2(hx2, pface(puc, pview(sc[RO_U + bl + 1]), plc, pview(lxp)),
-                            pface(pview(sc[RO_U + bl - 1]), puc, pview(lxm), plc));
-            pacc(gk, pscale2(hy2, pface(puc, pview(sc[RO_U + bl + RLW]), plc, pview(lyp)),
-                             pface(pview(sc[RO_U + bl - RLW]), puc, pview(lym), plc)));
+            f2 gk = pscale2(hx2, pface(puc, PU(bl + 1), plc, PL(bl + 1)), pface(PU(bl - 1), puc, PL(bl - 1), plc));
+            pacc(gk, pscale2(hy2, pface(puc, PU(bl + RLW), plc, PL(bl + RLW)),
+                             pface(PU(bl - RLW), puc, PL(bl - RLW), plc)));
             pacc(gk, pscale2(hz2, pza, pzb));
             f2 gsum{gc.x, gc.y};
             pacc(gsum, {-gk.hi, -gk.lo});
@@ -542,9 +574,10 @@ k_adjoint_x2_tma(const __grid_constant__ CUtensorMap tl, const __grid_constant__
             }
         }
         lb = lc;
-        ub = uc;
         kzb = kzc;
         pzb = pza;
+        plc = pla;
+        puc = pua;
     }
     if (!__syncthreads_and(ok)) fail(issued);
 }
@@ -696,7 +729,8 @@ int coefficient_maps(scafes_adj* a) {
     ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RSMEM));
     ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma<float2>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared));
-    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RSMEM));
+    ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)RSMEM_F64));
     ATRY(a, cudaFuncSetAttribute(k_adjoint_x2_tma<double>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared));
     a->cmaps_ok = true;
@@ -843,7 +877,7 @@ int adj_step(Rev& R, const double* u_t) {
             ml, mu, a->cmaps[0], a->cmaps[1], a->cmaps[2], a->cmaps[3], P2(a->lam[R.cur ^ 1]), P2(a->gx),
             P2(a->bnd), half(a->w[0]), half(a->w[1]), half(a->w[2]), a->L, a->status);
     else
-        k_adjoint_x2_tma<double><<<grid, dim3(RTX, RTY), RSMEM, a->stream>>>(
+        k_adjoint_x2_tma<double><<<grid, dim3(RTX, RTY), RSMEM_F64, a->stream>>>(
             ml, mu, a->cmaps[0], a->cmaps[1], a->cmaps[2], a->cmaps[3], a->lam[R.cur ^ 1], P2(a->gx), a->bnd,
             half(a->w[0]), half(a->w[1]), half(a->w[2]), a->L, a->status);
     ATRY(a, cudaGetLastError());

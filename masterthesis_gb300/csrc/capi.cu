@@ -411,6 +411,41 @@ extern "C" int scafes_gpu_download(scafes_handle* h, int field, double* host, si
     return SCAFES_OK;
 }
 
+extern "C" int scafes_gpu_upload_async(scafes_handle* h, const double* host, size_t n) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_upload_async: handle is NULL");
+    if (!host || n != n_nodes(h))
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_upload_async: expected %zu values, got %zu%s",
+                    n_nodes(h), n, host ? "" : " (NULL pointer)");
+    if (h->keep_initial && !h->u0keep)
+        CUDA_TRY(h, cudaMalloc(&h->u0keep, (size_t)h->L.size() * sizeof(double)));
+    int rc = h2d(h, h->u[0], h->cfg.precision, host);
+    if (rc) return rc;
+    h->u0keep_valid = false;
+    if (h->keep_initial) {
+        if ((rc = h2d(h, h->u0keep, SCAFES_PREC_F64, host))) return rc;
+        h->u0keep_valid = true;
+    }
+    h->cur = 0;
+    h->t = 0;
+    h->uploaded = true;
+    return SCAFES_OK;
+}
+
+extern "C" int scafes_gpu_download_async(scafes_handle* h, double* host, size_t n) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_download_async: handle is NULL");
+    if (!host || n != n_nodes(h))
+        return fail(&h->err, SCAFES_ERR_ARG, "scafes_gpu_download_async: expected %zu values, got %zu",
+                    n_nodes(h), n);
+    if (!h->uploaded)
+        return fail(&h->err, SCAFES_ERR_STATE, "scafes_gpu_download_async: the unknown field was never uploaded");
+    return d2h(h, h->u[h->cur], h->cfg.precision, host);
+}
+
+extern "C" int scafes_gpu_synchronize(scafes_handle* h) {
+    if (!h) return fail(nullptr, SCAFES_ERR_ARG, "scafes_gpu_synchronize: handle is NULL");
+    return check_status(h);
+}
+
 // TMA descriptor of buffer `buf` for tile variant `tile` (encoded on first use).
 static const CUtensorMap* tensor_map(scafes_handle* h, int buf, int tile) {
     if (!h->tm_ok[buf][tile]) {

@@ -214,3 +214,53 @@ def test_host_alloc_buffers_roundtrip(gpu):
             p.download(M.FIELD_U, hout.a)
             ref = p.download()
         assert np.array_equal(hout.a, ref)
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32x2", "f32"])
+def test_async_copies_on_two_handles(gpu, prec):
+    """scafes_gpu_upload_async / _download_async / _synchronize, pipelined
+    over two handles on two streams as the bench's end-to-end loop runs
+    them: every step's result equals the synchronous path's bit for bit."""
+    import torch
+    M = gpu
+    n = (48, 40, 36)
+    shape = (n[2], n[1], n[0])
+    rng = np.random.default_rng(9)
+    inputs = [rng.uniform(-1.0, 1.0, shape) for _ in range(5)]
+    cfg = dict(tau=1e-4, heat=(1.0, 1.0, 0.0), precision=prec)
+    want = []
+    with M.Plain(M.make_cfg(n, **cfg)) as p:
+        for u in inputs:
+            p.upload(M.FIELD_U, u)
+            p.step(6)
+            want.append(p.download())
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    hin = [M.HostArray(shape) for _ in range(2)]
+    hout = [M.HostArray(shape) for _ in range(2)]
+    got = [None] * len(inputs)
+    handles = [M.Plain(M.make_cfg(n, stream=s.cuda_stream, **cfg)) for s in streams]
+    try:
+        for k, u in enumerate(inputs):
+            h = handles[k % 2]
+            if k >= 2:
+                h.synchronize()
+                got[k - 2] = hout[k % 2].a.copy()
+            hin[k % 2].a[...] = u
+            h.upload_async(hin[k % 2].a)
+            h.step(6)
+            h.download_async(hout[k % 2].a)
+        for k in range(len(inputs) - 2, len(inputs)):
+            handles[k % 2].synchronize()
+            got[k] = hout[k % 2].a.copy()
+    finally:
+        for h in handles:
+            h.close()
+        for a in hin + hout:
+            a.close()
+    for k in range(len(inputs)):
+        assert np.array_equal(got[k], want[k]), k
+    with M.Plain(M.make_cfg(n, **cfg)) as p:
+        with pytest.raises(M.ScafesError):
+            p.download_async(np.empty(shape))  # nothing uploaded yet
+        with pytest.raises(ValueError):
+            p.upload_async(np.empty((3, 3)))
