@@ -11,12 +11,16 @@
 //     (:3434-3485);
 //  2. run initInner/initBorder on the host for the initial iterate
 //     (evalInitPbPhase, :2755-2826);
-//  3. extract the update: updateInner<gpu::Sym> at probe nodes and
+//  3. extract the update: updateInner<gpu::Sym> at every inner node and
 //     updateBorder<gpu::Sym> at every global-border node, at two time
 //     steps, give linear forms that must match one of the device kernels --
-//     the 7-point star with a source, and the Dirichlet or StencilWidthOne
-//     mirror border -- otherwise the constructor-time contract is broken and
-//     iterateOverTime throws (there is no CPU fallback);
+//     the 7-point star with a source, with constant coefficients or with a
+//     centre weight and axis scale per node (the tissue examples), and the
+//     Dirichlet, StencilWidthOne mirror, per-class table or per-node border
+//     -- or, for a problem with several unknown fields or a leapfrog second
+//     phase (updateInner2/updateBorder2), a linear multi-field rule per
+//     phase, field and node class (scafes_lin_*); otherwise iterateOverTime
+//     throws with the reason (there is no CPU fallback);
 //  4. upload, run all nTimesteps sweeps on the device through the C ABI
 //     (include/scafes_gb300.h), download the final iterate into the
 //     unknown data fields, and compute the max-norm error against the exact
