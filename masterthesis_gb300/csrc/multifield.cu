@@ -15,9 +15,9 @@
 // Both are FP64-issue-bound on GB300 (Lame: ~57 FP64 operations per node,
 // Yee: ~24 per cell and step), so the kernels read neighbours straight from
 // global memory through L1 instead of staging tiles: one thread per (x, y)
-// column marches a chunk of 16 z-planes.  The FP32-pair kernels (k_lame_x2,
-// k_yee_h_x2, k_yee_e_x2) keep the same layout and bytes per node and move
-// the arithmetic to the FP32 pipe.
+// column marches a chunk of 16 z-planes.  The FP32-pair Lame kernel
+// (k_lame_x2) keeps that form with the arithmetic on the FP32 pipe; FP32
+// and FP32-pair Yee run the fused one-pass step (k_yee_tma) below.
 #include <cstdarg>
 #include <cmath>
 #include <cstdio>
@@ -252,55 +252,11 @@ __device__ __forceinline__ float2 yee_upd(float2 v, const C3& ch, float sign, fl
     return pa_result(acc);
 }
 
-// Yee H half step on pairs (the staggering of k_yee_h).
-__global__ void __launch_bounds__(MX * MY)
-k_yee_h_x2(const float2* __restrict__ ex, const float2* __restrict__ ey, const float2* __restrict__ ez,
-           float2* __restrict__ hx, float2* __restrict__ hy, float2* __restrict__ hz, Layout L, C3 ch) {
-    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
-    if (x >= L.nx || y >= L.ny) return;
-    const int z0 = blockIdx.z * MZ, z1 = min(z0 + MZ, L.nz);
-    for (int z = z0; z < z1; ++z) {
-        const long long m = L.idx(x, y, z);
-        const bool xi = x + 1 < L.nx, yi = y + 1 < L.ny, zi = z + 1 < L.nz;
-        if (yi && zi) hx[m] = yee_upd(hx[m], ch, -1.f, ez[m + L.pitch], ez[m], ey[m + L.plane], ey[m]);
-        if (xi && zi) hy[m] = yee_upd(hy[m], ch, -1.f, ex[m + L.plane], ex[m], ez[m + 1], ez[m]);
-        if (xi && yi) hz[m] = yee_upd(hz[m], ch, -1.f, ey[m + 1], ey[m], ex[m + L.pitch], ex[m]);
-    }
-}
-
-// Yee E step on pairs with PEC walls and the soft source (src_val: the
-// host-split tau*J(t)).
-__global__ void __launch_bounds__(MX * MY)
-k_yee_e_x2(float2* __restrict__ ex, float2* __restrict__ ey, float2* __restrict__ ez, const float2* __restrict__ hx,
-           const float2* __restrict__ hy, const float2* __restrict__ hz, Layout L, C3 ch, long long src,
-           float2 src_val) {
-    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
-    if (x >= L.nx || y >= L.ny) return;
-    const int z0 = blockIdx.z * MZ, z1 = min(z0 + MZ, L.nz);
-    const bool xin = x > 0 && x + 1 < L.nx, yin = y > 0 && y + 1 < L.ny;
-    for (int z = z0; z < z1; ++z) {
-        const long long m = L.idx(x, y, z);
-        const bool zin = z > 0 && z + 1 < L.nz;
-        if (x + 1 < L.nx && yin && zin)
-            ex[m] = yee_upd(ex[m], ch, 1.f, hz[m], hz[m - L.pitch], hy[m], hy[m - L.plane]);
-        if (y + 1 < L.ny && xin && zin)
-            ey[m] = yee_upd(ey[m], ch, 1.f, hx[m], hx[m - L.plane], hz[m], hz[m - 1]);
-        if (z + 1 < L.nz && xin && yin) {
-            float2 v = yee_upd(ez[m], ch, 1.f, hy[m], hy[m - 1], hx[m], hx[m - L.pitch]);
-            if (m == src) {
-                PAcc acc{v.x, v.y};
-                pa_add(acc, src_val, -1.f);
-                v = pa_result(acc);
-            }
-            ez[m] = v;
-        }
-    }
-}
-
-// One FP32 Yee step (H half step, then E with the new H) in one pass over
-// the fields, where the two-kernel form is bandwidth- and latency-bound (it
-// moves 72 bytes per cell and step; this moves the 48 of reading E, H and
-// writing E, H once).  It reads the old set of six fields and writes the
+// One FP32 or FP32-pair Yee step (H half step, then E with the new H) in
+// one pass over the fields, where the two-kernel form is bandwidth- and
+// latency-bound (it moves 72 bytes per cell and step in FP32, 144 in pairs;
+// this moves the 48 / 96 of reading E, H and writing E, H once).  The
+// element policy (YeeF32, YeeF32x2) gives the arithmetic.  It reads the old set of six fields and writes the
 // other (ping-pong: a CTA recomputes the new H of its x-1 / y-1 halo from
 // old values that its neighbours must not have overwritten yet).
 //
@@ -318,24 +274,60 @@ constexpr int YX = 32, YY = 8;
 constexpr int YBW = YX + 8;                            // box width (x0-4 .. x0+YX+3)
 constexpr int YE_BOX = YBW * (YY + 2);                 // E box: rows y0-1 .. y0+YY
 constexpr int YH_BOX = YBW * (YY + 1);                 // H box: rows y0-1 .. y0+YY-1
-constexpr int YE_PAD = (YE_BOX * 4 + 127) / 128 * 32;  // floats per E box, 128-byte aligned
-constexpr int YH_PAD = (YH_BOX * 4 + 127) / 128 * 32;
+// Elements per E / H box of ESZ-byte elements, 128-byte aligned.
+__host__ __device__ constexpr int ye_pad(int esz) { return (YE_BOX * esz + 127) / 128 * 128 / esz; }
+__host__ __device__ constexpr int yh_pad(int esz) { return (YH_BOX * esz + 127) / 128 * 128 / esz; }
 constexpr int YHS = YX + 1, YHN = YHS * (YY + 1);     // new-H cells: x0-1 .. x0+YX-1, y0-1 ..
-constexpr size_t YEE_SMEM = (size_t)(9 * YE_PAD + 6 * YH_PAD + 6 * YH_BOX) * 4 + 5 * 8;
+constexpr size_t yee_smem(int esz) {
+    return (size_t)(9 * ye_pad(esz) + 6 * yh_pad(esz) + 6 * YH_BOX) * esz + 5 * 8;
+}
 
-__global__ void __launch_bounds__(YX * YY, 4)
+// Element policies of the fused step: v + sign * ch * ((a - b) - (c - d))
+// and v - s, in FP32 (one FMA: the arithmetic of k_yee_h / k_yee_e) or in
+// FP32 pairs (the arithmetic of k_yee_h_x2 / k_yee_e_x2).
+struct YeeF32 {
+    using T = float;
+    using C = float;
+    static constexpr int MINB = 4;  // CTAs per SM
+    static __device__ __forceinline__ T zero() { return 0.f; }
+    static __device__ __forceinline__ T upd(T v, C ch, float sign, T a, T b, T c, T d) {
+        return v + (sign * ch) * ((a - b) - (c - d));
+    }
+    static __device__ __forceinline__ T sub(T v, T s) { return v - s; }
+};
+
+struct YeeF32x2 {
+    using T = float2;
+    using C = C3;
+    static constexpr int MINB = 3;
+    static __device__ __forceinline__ T zero() { return make_float2(0.f, 0.f); }
+    static __device__ __forceinline__ T upd(T v, const C& ch, float sign, T a, T b, T c, T d) {
+        return yee_upd(v, ch, sign, a, b, c, d);
+    }
+    static __device__ __forceinline__ T sub(T v, T s) {
+        PAcc acc{v.x, v.y};
+        pa_add(acc, s, -1.f);
+        return pa_result(acc);
+    }
+};
+
+template <class P>
+__global__ void __launch_bounds__(YX * YY, P::MINB)
 k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUtensorMap tey,
           const __grid_constant__ CUtensorMap tez, const __grid_constant__ CUtensorMap thx,
           const __grid_constant__ CUtensorMap thy, const __grid_constant__ CUtensorMap thz,
-          float* __restrict__ exn, float* __restrict__ eyn, float* __restrict__ ezn,
-          float* __restrict__ hxn, float* __restrict__ hyn, float* __restrict__ hzn,
-          Layout L, float ch, long long src, float src_val, int zchunk, int* __restrict__ status) {
+          typename P::T* __restrict__ exn, typename P::T* __restrict__ eyn, typename P::T* __restrict__ ezn,
+          typename P::T* __restrict__ hxn, typename P::T* __restrict__ hyn, typename P::T* __restrict__ hzn,
+          Layout L, typename P::C ch, long long src, typename P::T src_val, int zchunk, int* __restrict__ status) {
+    using T = typename P::T;
+    constexpr int ESZ = sizeof(T);
+    constexpr int YE_PAD = ye_pad(ESZ), YH_PAD = yh_pad(ESZ);
     constexpr int NT = YX * YY;
     constexpr int HPT = (YHN + NT - 1) / NT;
-    extern __shared__ __align__(128) float ysm[];
-    float* se = ysm;                   // [3 slots][ex, ey, ez][YE_PAD]
-    float* sho = se + 9 * YE_PAD;      // [2 slots][hx, hy, hz][YH_PAD]   old H
-    float* shn = sho + 6 * YH_PAD;     // [2 slots][hx, hy, hz][YH_BOX]   new H
+    extern __shared__ __align__(128) unsigned char ysm_raw[];
+    T* se = reinterpret_cast<T*>(ysm_raw);  // [3 slots][ex, ey, ez][YE_PAD]
+    T* sho = se + 9 * YE_PAD;               // [2 slots][hx, hy, hz][YH_PAD]   old H
+    T* shn = sho + 6 * YH_PAD;              // [2 slots][hx, hy, hz][YH_BOX]   new H
     uint64_t* bar = reinterpret_cast<uint64_t*>(shn + 6 * YH_BOX);  // E slots 0-2, H slots 3-4
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * YX + tx;
     const int x0 = blockIdx.x * YX, y0 = blockIdx.y * YY;
@@ -352,16 +344,16 @@ k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUten
     __syncthreads();
     auto issue_e = [&](int p, int slot) {  // old E of plane zs+p into a ring slot
         uint64_t* b = &bar[slot];
-        float* d = se + slot * 3 * YE_PAD;
-        mbar_arrive_expect_tx(b, 3u * YE_BOX * 4u);
+        T* d = se + slot * 3 * YE_PAD;
+        mbar_arrive_expect_tx(b, 3u * YE_BOX * (uint32_t)ESZ);
         tma_load_3d(d, &tex, x0 - 4, y0 - 1, zs + p, b);
         tma_load_3d(d + YE_PAD, &tey, x0 - 4, y0 - 1, zs + p, b);
         tma_load_3d(d + 2 * YE_PAD, &tez, x0 - 4, y0 - 1, zs + p, b);
     };
     auto issue_h = [&](int p) {  // old H of plane zs+p into slot p % 2
         uint64_t* b = &bar[3 + (p & 1)];
-        float* d = sho + (p & 1) * 3 * YH_PAD;
-        mbar_arrive_expect_tx(b, 3u * YH_BOX * 4u);
+        T* d = sho + (p & 1) * 3 * YH_PAD;
+        mbar_arrive_expect_tx(b, 3u * YH_BOX * (uint32_t)ESZ);
         tma_load_3d(d, &thx, x0 - 4, y0 - 1, zs + p, b);
         tma_load_3d(d + YH_PAD, &thy, x0 - 4, y0 - 1, zs + p, b);
         tma_load_3d(d + 2 * YH_PAD, &thz, x0 - 4, y0 - 1, zs + p, b);
@@ -401,7 +393,7 @@ k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUten
     uint32_t eph = 0;
     bool ok = bounded_wait(&bar[0], 0);  // E plane 0
     eph ^= 1u;
-    float hx_prev = 0.f, hy_prev = 0.f;
+    T hx_prev = P::zero(), hy_prev = P::zero();
     for (int p = 0; p < np; ++p) {
         const int z = zs + p;
         __syncthreads();  // iteration p-1 is done with the slots refilled below
@@ -413,25 +405,25 @@ k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUten
         ok = bounded_wait(&bar[s1], (eph >> s1) & 1u) && ok;   // E plane p+1
         eph ^= 1u << s1;
         ok = bounded_wait(&bar[3 + (p & 1)], (p >> 1) & 1) && ok;  // old H plane p
-        const float* ea = se + s0 * 3 * YE_PAD;
-        const float* eb = se + s1 * 3 * YE_PAD;
-        const float* ho = sho + (p & 1) * 3 * YH_PAD;
-        float* hn = shn + (p & 1) * 3 * YH_BOX;
+        const T* ea = se + s0 * 3 * YE_PAD;
+        const T* eb = se + s1 * 3 * YE_PAD;
+        const T* ho = sho + (p & 1) * 3 * YH_PAD;
+        T* hn = shn + (p & 1) * 3 * YH_BOX;
         const bool zi = z + 1 < L.nz;
         if (ok) {
 #pragma unroll
             for (int k = 0; k < HPT; ++k) {
                 if (tid + k * NT >= YHN) break;
                 const int b = hb[k];
-                float vhx = 0.f, vhy = 0.f, vhz = 0.f;
+                T vhx = P::zero(), vhy = P::zero(), vhz = P::zero();
                 if (hin[k]) {
                     vhx = ho[b];
                     vhy = ho[YH_PAD + b];
                     vhz = ho[2 * YH_PAD + b];
-                    const float ex0 = ea[b], ey0 = ea[YE_PAD + b], ez0 = ea[2 * YE_PAD + b];
-                    if (hyi[k] && zi) vhx -= ch * ((ea[2 * YE_PAD + b + YBW] - ez0) - (eb[YE_PAD + b] - ey0));
-                    if (hxi[k] && zi) vhy -= ch * ((eb[b] - ex0) - (ea[2 * YE_PAD + b + 1] - ez0));
-                    if (hxi[k] && hyi[k]) vhz -= ch * ((ea[YE_PAD + b + 1] - ey0) - (ea[b + YBW] - ex0));
+                    const T ex0 = ea[b], ey0 = ea[YE_PAD + b], ez0 = ea[2 * YE_PAD + b];
+                    if (hyi[k] && zi) vhx = P::upd(vhx, ch, -1.f, ea[2 * YE_PAD + b + YBW], ez0, eb[YE_PAD + b], ey0);
+                    if (hxi[k] && zi) vhy = P::upd(vhy, ch, -1.f, eb[b], ex0, ea[2 * YE_PAD + b + 1], ez0);
+                    if (hxi[k] && hyi[k]) vhz = P::upd(vhz, ch, -1.f, ea[YE_PAD + b + 1], ey0, ea[b + YBW], ex0);
                 }
                 hn[b] = vhx;
                 hn[YH_BOX + b] = vhy;
@@ -451,19 +443,19 @@ k_yee_tma(const __grid_constant__ CUtensorMap tex, const __grid_constant__ CUten
             }
             return;
         }
-        const float hx = hn[ob], hy = hn[YH_BOX + ob], hz = hn[2 * YH_BOX + ob];
+        const T hx = hn[ob], hy = hn[YH_BOX + ob], hz = hn[2 * YH_BOX + ob];
         if (live && z >= z0) {
             const long long m = (long long)z * L.plane + oo;
             hxn[m] = hx;
             hyn[m] = hy;
             hzn[m] = hz;
-            float ex = ea[ob], ey = ea[YE_PAD + ob], ez = ea[2 * YE_PAD + ob];
+            T ex = ea[ob], ey = ea[YE_PAD + ob], ez = ea[2 * YE_PAD + ob];
             const bool zin = z > 0 && zi;
-            if (ex_upd && zin) ex += ch * ((hz - hn[2 * YH_BOX + ob - YBW]) - (hy - hy_prev));
-            if (ey_upd && zin) ey += ch * ((hx - hx_prev) - (hz - hn[2 * YH_BOX + ob - 1]));
+            if (ex_upd && zin) ex = P::upd(ex, ch, 1.f, hz, hn[2 * YH_BOX + ob - YBW], hy, hy_prev);
+            if (ey_upd && zin) ey = P::upd(ey, ch, 1.f, hx, hx_prev, hz, hn[2 * YH_BOX + ob - 1]);
             if (ez_upd && zi) {
-                float v = ez + ch * ((hy - hn[YH_BOX + ob - 1]) - (hx - hn[ob - YBW]));
-                if (m == src) v -= src_val;
+                T v = P::upd(ez, ch, 1.f, hy, hn[YH_BOX + ob - 1], hx, hn[ob - YBW]);
+                if (m == src) v = P::sub(v, src_val);
                 ez = v;
             }
             exn[m] = ex;
@@ -596,7 +588,7 @@ extern "C" int scafes_mf_create(const scafes_mf_cfg* cfg, scafes_mf** out) {
         for (int p = 0; p < 3; ++p)
             if (cfg->src[p] < 0 || cfg->src[p] >= cfg->n_nodes[p])
                 return mfail(nullptr, SCAFES_ERR_ARG, "scafes_mf_create: source index out of the grid");
-    if (cfg->kind == SCAFES_MF_YEE && cfg->precision == SCAFES_PREC_F32) {
+    if (cfg->kind == SCAFES_MF_YEE && cfg->precision != SCAFES_PREC_F64) {
         const Layout Lp = make_layout(cfg->n_nodes[0], cfg->n_nodes[1], cfg->n_nodes[2]);
         if (Lp.plane > 0x7fffffffLL)  // the fused step keeps in-plane offsets in 32 bits
             return mfail(nullptr, SCAFES_ERR_UNSUPPORTED, "scafes_mf_create: a z-plane of %lld cells is too large",
@@ -608,8 +600,10 @@ extern "C" int scafes_mf_create(const scafes_mf_cfg* cfg, scafes_mf** out) {
     h->L = make_layout(cfg->n_nodes[0], cfg->n_nodes[1], cfg->n_nodes[2]);
     h->esz = cfg->precision == SCAFES_PREC_F32 ? 4 : 8;
     h->nfields = 6;  // Lame: u^n (3) + u^{n-1} (3); Yee: Ex..Hz
-    // The fused FP32 Yee step reads one set of six fields and writes another.
-    const int sets = (cfg->kind == SCAFES_MF_YEE && h->esz == 4) ? 2 : 1;
+    // The fused Yee step (FP32, FP32 pairs) reads one set of six fields and
+    // writes another.
+    const bool fused = cfg->kind == SCAFES_MF_YEE && cfg->precision != SCAFES_PREC_F64;
+    const int sets = fused ? 2 : 1;
     cudaError_t e = cudaSuccess;
     if (cfg->stream) h->stream = (cudaStream_t)cfg->stream;
     else { e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking); h->own_stream = true; }
@@ -658,11 +652,16 @@ static int yee_maps(scafes_mf* h) {
     const Layout& L = h->L;
     for (int set = 0; set < 2; ++set)
         for (int f = 0; f < 6; ++f) {
-            const CUresult r = make_tensor_map_3d(&h->ytm[set][f], field_ptr(h, set * 6 + f), 4, L.nx, L.ny, L.nz,
-                                                  (size_t)L.pitch * 4, (size_t)L.plane * 4, YBW,
-                                                  f < 3 ? YY + 2 : YY + 1);
+            const CUresult r = make_tensor_map_3d(&h->ytm[set][f], field_ptr(h, set * 6 + f), (int)h->esz, L.nx,
+                                                  L.ny, L.nz, (size_t)L.pitch * h->esz, (size_t)L.plane * h->esz,
+                                                  YBW, f < 3 ? YY + 2 : YY + 1);
             if (r != CUDA_SUCCESS) return mfail(h, SCAFES_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
         }
+    if (h->esz == 8) {
+        const cudaError_t e = cudaFuncSetAttribute(k_yee_tma<YeeF32x2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)yee_smem(8));
+        if (e != cudaSuccess) return mfail(h, SCAFES_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    }
     h->ytm_ok = true;
     return SCAFES_OK;
 }
@@ -749,13 +748,18 @@ extern "C" int scafes_mf_step(scafes_mf* h, int n_steps) {
             const double a = (time - t0) / w;
             const double sv = c.tau * amp * std::exp(-a * a) * std::sin(2.0 * 3.14159265358979323846 * freq * time);
             if (c.precision == SCAFES_PREC_F32X2) {
-                float2* f[6];
-                for (int i = 0; i < 6; ++i) f[i] = (float2*)field_ptr(h, i);
-                const C3 chs = split3(ch);
+                const int rc = yee_maps(h);
+                if (rc) return rc;
+                float2* g[6];
+                for (int i = 0; i < 6; ++i) g[i] = (float2*)field_ptr(h, (h->cur ^ 1) * 6 + i);
+                const CUtensorMap* t = h->ytm[h->cur];
+                const int zc = yee_zchunk(L);
+                const dim3 grid((L.nx + YX - 1) / YX, (L.ny + YY - 1) / YY, (L.nz + zc - 1) / zc);
                 const f2 sp = split_double(sv);
-                k_yee_h_x2<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L, chs);
-                k_yee_e_x2<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>(f[0], f[1], f[2], f[3], f[4], f[5], L, chs,
-                                                                     src, make_float2(sp.hi, sp.lo));
+                k_yee_tma<YeeF32x2><<<grid, dim3(YX, YY), yee_smem(8), h->stream>>>(
+                    t[0], t[1], t[2], t[3], t[4], t[5], g[0], g[1], g[2], g[3], g[4], g[5], L, split3(ch), src,
+                    make_float2(sp.hi, sp.lo), zc, h->status);
+                h->cur ^= 1;
             } else if (h->esz == 8) {
                 double* f[6];
                 for (int i = 0; i < 6; ++i) f[i] = (double*)field_ptr(h, i);
@@ -770,9 +774,9 @@ extern "C" int scafes_mf_step(scafes_mf* h, int n_steps) {
                 const CUtensorMap* t = h->ytm[h->cur];
                 const int zc = yee_zchunk(L);
                 const dim3 grid((L.nx + YX - 1) / YX, (L.ny + YY - 1) / YY, (L.nz + zc - 1) / zc);
-                k_yee_tma<<<grid, dim3(YX, YY), YEE_SMEM, h->stream>>>(t[0], t[1], t[2], t[3], t[4], t[5], g[0], g[1],
-                                                                       g[2], g[3], g[4], g[5], L, (float)ch, src,
-                                                                       (float)sv, zc, h->status);
+                k_yee_tma<YeeF32><<<grid, dim3(YX, YY), yee_smem(4), h->stream>>>(
+                    t[0], t[1], t[2], t[3], t[4], t[5], g[0], g[1], g[2], g[3], g[4], g[5], L, (float)ch, src,
+                    (float)sv, zc, h->status);
                 h->cur ^= 1;
             }
             MTRY(h, cudaGetLastError());
