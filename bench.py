@@ -489,7 +489,9 @@ def run_adjoint(M, args, dist: Dist):
         for seed in range(args.adj_fd_directions):
             rng = np.random.default_rng(7000 + seed)
             dk = rng.standard_normal(k.shape) * k
-            eps = 1e-6
+            # eps 1e-4: the difference's truncation error (~eps^2) and its
+            # rounding noise (~1e-16 J / eps) both stay near 1e-8 here.
+            eps = 1e-4
             fd = (J_of(k + eps * dk, u0) - J_of(k - eps * dk, u0)) / (2 * eps)
             for p, (_, g, _) in grads.items():
                 errs[p].append(abs(fd - float(np.sum(g * dk))) / abs(fd))

@@ -68,20 +68,24 @@ __host__ __device__ inline double join_pair(float hi, float lo) {
 }
 
 // Split a double into hi + lo with integer instructions only (no FP64
-// operation, which GB300 issues at a small fraction of its FP32 rate): hi
-// is the value with its significand truncated to 24 bits, lo the remaining
-// 29 bits rounded to a float (one I2F).  |v - (hi + lo)| <= 2^-48 |v| for
-// 2^-74 <= |v| < 2^127; smaller nonzero |v| keep only hi (truncated),
-// zero gives (0, 0).  Larger magnitudes, infinities and NaN do not occur
-// in the fields this serves (they go through the FP32 conversion).
+// operation, which GB300 issues at a small fraction of its FP32 rate, not
+// even a predicated one on a rare path): hi is the value with its
+// significand truncated to 24 bits, lo the remaining 29 bits rounded to a
+// float (one I2F).  |v - (hi + lo)| <= 2^-48 |v| for 2^-74 <= |v| < 2^128;
+// smaller |v| down to 2^-126 keep only hi (truncated); below that (FP32
+// subnormals, double subnormals, zero) the result is a signed zero;
+// |v| >= 2^128 gives a signed infinity, infinities and NaN keep their kind.
 __device__ __forceinline__ f2 split_bits(double v) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
     const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
     const int e = (int)((b >> 52) & 0x7FF);
     const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
     const int ef = e - 1023 + 127;
-    if (e == 0) return {__int_as_float((int)sign), 0.f};  // (signed) zero, or a double subnormal
-    if (ef <= 0 || ef >= 255) return {(float)v, 0.f};    // below or above the FP32 range
+    if (ef <= 0) return {__int_as_float((int)sign), 0.f};  // below the FP32 normal range
+    if (ef >= 255) {                                         // above it: infinity, or NaN for a NaN
+        const unsigned nan = (e == 0x7FF && m != 0) ? 0x400000u : 0u;
+        return {__int_as_float((int)(sign | 0x7F800000u | nan)), 0.f};
+    }
     const float hi = __int_as_float((int)(sign | ((unsigned)ef << 23) | (unsigned)(m >> 29)));
     const int es = e - 1075 + 127;
     if (es <= 0) return {hi, 0.f};
