@@ -101,14 +101,16 @@ def test_config5_ensemble_matches_oracle(gpu, ensemble, prec):
     assert worst <= 1e-12, worst
 
 
-def test_config3_lame_384_matches_oracle(gpu):
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+def test_config3_lame_384_matches_oracle(gpu, prec):
     """Lame-Navier at its workload size, 384^3, 10 leapfrog steps from the
-    seeded bump: both time levels against the oracle, 1e-12."""
+    seeded bump: both time levels against the oracle, 1e-12 (FP64 and FP32
+    pairs)."""
     M = gpu
     n, T = (384, 384, 384), 10
     u0 = W.gaussian_bump_displacement(n, seed=3)
     tau = W.lame_tau(n)
-    with M.MultiField(M.MF_LAME, n, tau, (1.0, 0.5, 1.0)) as mf:
+    with M.MultiField(M.MF_LAME, n, tau, (1.0, 0.5, 1.0), precision=prec) as mf:
         for c in range(3):
             mf.upload(c, u0[c])
             mf.upload(3 + c, u0[c])
@@ -120,7 +122,7 @@ def test_config3_lame_384_matches_oracle(gpu):
     assert cases.rel_err(up, rup) <= 1e-12
 
 
-@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f32", 1e-4)])
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-12), ("f32x2", 1e-12), ("f32", 1e-4)])
 def test_config3_yee_512_matches_oracle(gpu, prec, tol):
     """Yee FDTD at its workload size, 512^3, 20 steps of the seeded dipole
     from zero fields: all six fields against the oracle."""
