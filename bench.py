@@ -52,6 +52,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--kernel-case", choices=sorted(KERNEL_CASES), default=None,
+                    help="run one small case of one kernel (for an ncu capture) and exit")
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--time-steps", type=int, default=1000)
     ap.add_argument("--no-variants", action="store_true")
@@ -973,8 +975,76 @@ def run_reference(args, dist: Dist):
     }
 
 
+# ---- single-kernel cases for profiler captures ----------------------------------
+
+def case_adjoint(prec: str, m: int = 160, T: int = 6):
+    """The adjoint workload's problem at m^3: a forward solve and a gradient
+    of T steps (16 snapshots: every state kept)."""
+    import masterthesis_gb300 as M
+    from masterthesis_gb300 import workloads as W
+    n = (m,) * 3
+    k = np.exp(0.3 * smooth_gauss(n, 5))
+    tau = 0.9 / (2.0 * k.max() * sum((v - 1) ** 2 for v in n))
+    u0 = W.heat_sine_noise(n, amp=0.0)
+    with M.Adjoint(n, tau, 16, precision=prec) as a:
+        a.set_conductivity(k)
+        uT = a.forward(u0, T)
+        J, gk, _ = a.gradient(u0, 0.5 * uT, T)
+    return f"J {J:.6e}, max|dJ/dk| {float(np.abs(gk).max()):.6e}"
+
+
+def case_lame(prec: str, m: int = 192, T: int = 4):
+    import masterthesis_gb300 as M
+    from masterthesis_gb300 import workloads as W
+    n = (m,) * 3
+    u0 = W.gaussian_bump_displacement(n, seed=3)
+    with M.MultiField(M.MF_LAME, n, W.lame_tau(n), (1.0, 0.5, 1.0), precision=prec) as mf:
+        for c in range(3):
+            mf.upload(c, u0[c])
+            mf.upload(3 + c, u0[c])
+        mf.step(T)
+        return f"max|u_x| {float(np.abs(mf.download(0)).max()):.6e}"
+
+
+def case_yee(prec: str, m: int = 256, T: int = 4):
+    import masterthesis_gb300 as M
+    from masterthesis_gb300 import workloads as W
+    n = (m,) * 3
+    tau, src, par = W.yee_setup(n)
+    with M.MultiField(M.MF_YEE, n, tau, par, precision=prec, src=src) as mf:
+        mf.step(T)
+        return f"max|Ez| {float(np.abs(mf.download(2)).max()):.6e}"
+
+
+def case_tissue(prec: str, m: int = 256, T: int = 4):
+    import masterthesis_gb300 as M
+    p = tissue_problem(M, tissue_arrays(m), prec)
+    try:
+        p.step(T)
+        return f"max T {float(p.download().max()):.6e}"
+    finally:
+        p.close()
+
+
+KERNEL_CASES = {
+    "adjoint_f64_160": lambda: case_adjoint("f64"),
+    "adjoint_x2_160": lambda: case_adjoint("f32x2"),
+    "lame_x2_192": lambda: case_lame("f32x2"),
+    "lame_f64_192": lambda: case_lame("f64"),
+    "yee_x2_256": lambda: case_yee("f32x2"),
+    "yee_f32_256": lambda: case_yee("f32"),
+    "tissue_f32_256": lambda: case_tissue("f32"),
+    "tissue_f64_256": lambda: case_tissue("f64"),
+}
+
+
 def main():
     args = parse_args()
+    if args.kernel_case:
+        from masterthesis_gb300 import build as B
+        B.build_library()
+        print(f"{args.kernel_case}: {KERNEL_CASES[args.kernel_case]()}", flush=True)
+        return
     if args.impl == "reference":
         dist = Dist("gloo")
         res = run_reference(args, dist)
