@@ -591,6 +591,25 @@ def run_multifield(M, args, dist: Dist, hbm_peak: float):
         out[f"yee_{prec}"] = {"workload": f"Yee FDTD {n[0]}^3 {prec.upper()}, PEC, point dipole, {T} steps",
                               "value": g, "unit": UNIT, "hbm_frac": bpl * g / hbm_peak, "bytes_per_lup": bpl,
                               "ms": ms}
+    # The same cavity (no source) as recorded linear rules on the generic
+    # multi-field kernel (scafes_lin_*: what the drop-in runs for a Yee
+    # class written against the callbacks): FP64, plain loads.
+    with M.Linear(n, 6, 2) as lin:
+        for (ph, f, c), terms in W.yee_linear_rules(tau * (n[0] - 1)).items():
+            lin.set_rule(ph, f, c, terms)
+        rng = np.random.default_rng(4)
+        for f in range(6):
+            lin.upload(f, rng.uniform(-1.0, 1.0, (n[2], n[1], n[0])))
+        lin.step(2)
+        dist.barrier()
+        lin.step(T)
+        ms = dist.max(lin.last_ms())
+    lup = float(np.prod(n)) * T
+    g = dist.world * lup / (ms * 1e-3) / 1e9
+    out["yee_linear_f64"] = {"workload": f"Yee cavity {n[0]}^3 as recorded linear rules (scafes_lin), FP64, "
+                                         f"seeded fields (seed 4), no source, {T} steps",
+                             "value": g, "unit": UNIT, "hbm_frac": 96 * g / hbm_peak, "bytes_per_lup": 96, "ms": ms,
+                             "launches_per_step": 2}
     if check:
         # Both precisions against the oracle after 2E steps from the
         # workload's initial state (zero fields, the dipole switched on).
@@ -602,6 +621,20 @@ def run_multifield(M, args, dist: Dist, hbm_peak: float):
             out[f"yee_{prec}"]["error_vs_oracle"] = {"max_rel": rel_err(f, ref),
                                                      "sample": f"{n[0]}^3, first {2 * E} steps (full grid)"}
             del f
+        # The linear-rule path against the oracle's Yee without a source.
+        m = (128, 128, 128)
+        tau_m, _, _ = W.yee_setup(m)
+        f0 = np.random.default_rng(4).uniform(-1.0, 1.0, (6, m[2], m[1], m[0]))
+        with M.Linear(m, 6, 2) as lin:
+            for (ph, f, c), terms in W.yee_linear_rules(tau_m * (m[0] - 1)).items():
+                lin.set_rule(ph, f, c, terms)
+            for f in range(6):
+                lin.upload(f, f0[f])
+            lin.step(2 * E)
+            got = np.stack([lin.download(f) for f in range(6)])
+        ref = O.yee(O.make_grid(m, tau=tau_m), f0, 2 * E, (0, 0, 0), 0.0, 1.0, 1.0, 1.0, nthreads=threads)
+        out["yee_linear_f64"]["error_vs_oracle"] = {"max_rel": rel_err(got, ref),
+                                                    "sample": f"{m[0]}^3, {2 * E} steps, same construction"}
     return out
 
 

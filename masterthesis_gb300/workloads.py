@@ -129,6 +129,34 @@ def yee_setup(n, seed: int = 4, courant: float = 0.5):
     return tau, src, (1.0, 2.0 * w, w, freq)
 
 
+def yee_linear_rules(ch: float) -> dict:
+    """The Yee cavity without a source (the staggering of the fused Yee
+    kernels, ch = tau / h) as rules of the linear multi-field kernel
+    (scafes_lin_*): phase 1 the H half step, phase 2 the E step on its
+    result; fields Ex Ey Ez Hx Hy Hz; {(phase, field, class): terms} with
+    terms (src, dx, dy, dz, w).  A node of class c has no +p neighbour when
+    bit 2p+1 is set and is inner along p when neither bit 2p nor 2p+1 is."""
+    unit = ((1, 0, 0), (0, 1, 0), (0, 0, 1))
+    rules = {}
+    for cls in range(64):
+        has_up = [not (cls >> (2 * p + 1)) & 1 for p in range(3)]
+        inner = [has_up[p] and not (cls >> (2 * p)) & 1 for p in range(3)]
+        for c in range(3):
+            a, b = (c + 1) % 3, (c + 2) % 3
+            ident_e, ident_h = [(c, 0, 0, 0, 1.0)], [(3 + c, 0, 0, 0, 1.0)]
+            # H_c -= ch ((E_b(+a) - E_b) - (E_a(+b) - E_a))
+            rules[(1, 3 + c, cls)] = (ident_h + [(b, *unit[a], -ch), (b, 0, 0, 0, ch), (a, *unit[b], ch),
+                                                 (a, 0, 0, 0, -ch)]) if has_up[a] and has_up[b] else ident_h
+            rules[(1, c, cls)] = ident_e
+            # E_c += ch ((H_b - H_b(-a)) - (H_a - H_a(-b)))
+            down_a = tuple(-v for v in unit[a])
+            down_b = tuple(-v for v in unit[b])
+            rules[(2, c, cls)] = (ident_e + [(3 + b, 0, 0, 0, ch), (3 + b, *down_a, -ch), (3 + a, 0, 0, 0, -ch),
+                                             (3 + a, *down_b, ch)]) if has_up[c] and inner[a] and inner[b] else ident_e
+            rules[(2, 3 + c, cls)] = ident_h
+    return rules
+
+
 # ---- tissue workloads (coefficients per node) ----------------------------------
 
 TISSUE_FIELDS = ("rho", "c", "k", "rho_b", "c_b", "omega", "t_blood", "q")

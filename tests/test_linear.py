@@ -56,6 +56,16 @@ def test_yee_rules_on_cpu_match_oracle():
     assert cases.rel_err(got, ref) <= 1e-13
 
 
+def test_workload_rules_equal_test_restatement():
+    """The bench's Yee rules (workloads.yee_linear_rules) are the test's."""
+    from masterthesis_gb300 import workloads as W
+    for ch in (0.25, 0.5 / np.sqrt(3.0)):
+        a, b = W.yee_linear_rules(ch), cases.yee_lin_rules(ch)
+        assert a.keys() == b.keys()
+        for k in a:
+            assert sorted(a[k]) == sorted(b[k]), k
+
+
 def read_lin_rules(path):
     d = read_device_form(path)
     nu, nph = int(d["lin_cfg"][3]), int(d["lin_cfg"][4])
