@@ -106,8 +106,9 @@ enum scafes_border {
 };
 
 /* The rule of one border node of a SCAFES_BORDER_NODES problem, evaluated
- * in FP64:  u_new = cu*u + sum_d cn[d]*u_d + cst,  neighbours d = x-, x+,
- * y-, y+, z-, z+ (a neighbour outside the grid must have weight 0). */
+ * in FP64 (in FP32 for an SCAFES_PREC_F32 problem):
+ *   u_new = cu*u + sum_d cn[d]*u_d + cst,  neighbours d = x-, x+, y-, y+,
+ * z-, z+ (a neighbour outside the grid must have weight 0). */
 typedef struct scafes_border_node_rule {
     double cu;
     double cn[6];

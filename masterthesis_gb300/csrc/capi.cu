@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "adjoint.cuh"
 #include "star7.cuh"
@@ -710,6 +711,20 @@ extern "C" int scafes_gpu_set_border_node_rules(scafes_handle* h, const scafes_b
                 ++r;
             }
     if (!h->nodes) CUDA_TRY(h, cudaMalloc(&h->nodes, (size_t)count * sizeof(scafes_border_node_rule)));
+    if (h->cfg.precision == SCAFES_PREC_F32) {
+        // The FP32 sweep evaluates the rules in FP32: 8 floats per node
+        // (cu, cn[0..5], cst) in the same allocation.
+        std::vector<float> f((size_t)count * 8);
+        for (long long i = 0; i < count; ++i) {
+            f[i * 8] = (float)rules[i].cu;
+            for (int d = 0; d < 6; ++d) f[i * 8 + 1 + d] = (float)rules[i].cn[d];
+            f[i * 8 + 7] = (float)rules[i].cst;
+        }
+        CUDA_TRY(h, cudaMemcpyAsync(h->nodes, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice,
+                                    h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        return SCAFES_OK;
+    }
     CUDA_TRY(h, cudaMemcpyAsync(h->nodes, rules, (size_t)count * sizeof(scafes_border_node_rule),
                                 cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));

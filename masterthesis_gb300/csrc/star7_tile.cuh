@@ -72,13 +72,28 @@ struct TileJob {
     const scafes_border_node_rule* nodes = nullptr;  // per-node rules (SCAFES_BORDER_NODES)
 };
 
-// The rule of one border node of a SCAFES_BORDER_NODES problem, in FP64
-// whatever the element type: u_new = cu*u + sum_d cn[d]*u_d + cst.
+// The rule of one border node of a SCAFES_BORDER_NODES problem:
+// u_new = cu*u + sum_d cn[d]*u_d + cst, in FP64, except for the FP32 sweep,
+// whose rules the host stores as 8 floats per node (cu, cn[0..5], cst) and
+// which evaluates them in FP32: on an x-face tile every warp calls this for
+// one or two lanes, and a warp's FP64 instructions (and FP32<->FP64
+// conversions) hold GB300's narrow FP64 pipe whatever the active lanes.
 template <class P>
 __device__ __noinline__ typename P::T node_rule(const TileJob<typename P::T>& J, int x, int y, int z,
                                                  typename P::T u, typename P::T w, typename P::T e,
                                                  typename P::T s, typename P::T n, typename P::T b,
                                                  typename P::T t) {
+    if constexpr (std::is_same<P, PolF32>::value) {
+        const float* Rf = reinterpret_cast<const float*>(J.nodes) + 8 * border_node_index(J.L, x, y, z);
+        float v = fmaf(Rf[0], u, Rf[7]);
+        v = fmaf(Rf[1], w, v);
+        v = fmaf(Rf[2], e, v);
+        v = fmaf(Rf[3], s, v);
+        v = fmaf(Rf[4], n, v);
+        v = fmaf(Rf[5], b, v);
+        v = fmaf(Rf[6], t, v);
+        return v;
+    }
     const scafes_border_node_rule& R = J.nodes[border_node_index(J.L, x, y, z)];
     double v = fma(R.cu, P::to_double(u), R.cst);
     v = fma(R.cn[0], P::to_double(w), v);
