@@ -16,8 +16,9 @@
 // Yee: ~24 per cell and step), so the kernels read neighbours straight from
 // global memory through L1 instead of staging tiles: one thread per (x, y)
 // column marches a chunk of 16 z-planes.  The FP32-pair Lame kernel
-// (k_lame_x2) keeps that form with the arithmetic on the FP32 pipe; FP32
-// and FP32-pair Yee run the fused one-pass step (k_yee_tma) below.
+// (k_lame_x2_tma) stages the three components through TMA instead (its
+// pair arithmetic needs the loads' latency hidden); FP32 and FP32-pair Yee
+// run the fused one-pass step (k_yee_tma) below.
 #include <cstdarg>
 #include <cmath>
 #include <cstdio>
@@ -201,46 +202,121 @@ __device__ __forceinline__ float2 pa_result(PAcc acc) {
 // Lame-Navier step on pairs: u^{n+1} = d_c u + sum_p a_cp (u(+p) + u(-p))
 // + sum_q b_cq ((u_q(+c+q) - u_q(+c-q)) - (u_q(-c+q) - u_q(-c-q))) - u^{n-1},
 // the FP64 form rearranged with the centre weight d_c = 2 - 2 sum_p a_cp.
-__global__ void __launch_bounds__(MX * MY)
-k_lame_x2(const float2* __restrict__ u, float2* __restrict__ up, LameCoefX2 K, Layout L, long long comp) {
-    const int x = blockIdx.x * MX + threadIdx.x, y = blockIdx.y * MY + threadIdx.y;
-    if (x >= L.nx || y >= L.ny) return;
+// The three components of u^n are staged by TMA: a CTA
+// owns an LX x LY column tile and marches LZ planes; per input plane one
+// mbarrier covers the three components' boxes with a one-node halo in x and
+// y (x from x0-2 for 16-byte alignment), in a ring of LNS planes: planes
+// z-1, z, z+1 are read from shared memory while the next LNS-3 are in
+// flight.  u^{n-1} is read and u^{n+1} written with plain coalesced
+// accesses of the node itself.  The terms come in the order of the FP64
+// kernel's.  Every wait is bounded (status word, drain,
+// return).
+constexpr int LX = 32, LY = 8, LZ = 32, LNS = 6;
+constexpr int LBW = LX + 4, LBH = LY + 2;                     // box: x0-2 .. x0+33, y0-1 .. y0+8
+constexpr int LBOX = (LBW * LBH + 15) / 16 * 16;              // float2 per box, 128-byte multiple
+constexpr int LSLOT = 3 * LBOX;                               // float2 per ring slot
+constexpr uint32_t LTX_BYTES = (uint32_t)(3 * LBW * LBH * 8);
+constexpr size_t LAME_SMEM = (size_t)LNS * LSLOT * 8 + LNS * 8;
+
+__global__ void __launch_bounds__(LX * LY)
+k_lame_x2_tma(const __grid_constant__ CUtensorMap t0, const __grid_constant__ CUtensorMap t1,
+              const __grid_constant__ CUtensorMap t2, float2* __restrict__ up, LameCoefX2 K, Layout L,
+              long long comp, int* __restrict__ status) {
+    extern __shared__ __align__(128) float2 lsm[];
+    uint64_t* bar = reinterpret_cast<uint64_t*>(lsm + LNS * LSLOT);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * LX + tx;
+    const int x0 = blockIdx.x * LX, y0 = blockIdx.y * LY;
+    const int z0 = blockIdx.z * LZ, z1 = min(z0 + LZ, L.nz);
+    if (__syncthreads_or(tid == 0 && *(volatile int*)status != 0)) return;
+    if (tid == 0) {
+        for (int b = 0; b < LNS; ++b) mbar_init(&bar[b], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    // Input plane j is z0-1+j (j = 0 .. n_in-1), in ring slot j % LNS.
+    const int n_in = z1 - z0 + 2;
+    auto issue = [&](int j) {
+        const int sl = j % LNS, z = z0 - 1 + j;
+        float2* d = lsm + sl * LSLOT;
+        mbar_arrive_expect_tx(&bar[sl], LTX_BYTES);
+        tma_load_3d(d, &t0, x0 - 2, y0 - 1, z, &bar[sl]);
+        tma_load_3d(d + LBOX, &t1, x0 - 2, y0 - 1, z, &bar[sl]);
+        tma_load_3d(d + 2 * LBOX, &t2, x0 - 2, y0 - 1, z, &bar[sl]);
+    };
+    if (tid == 0)
+        for (int j = 0; j < LNS && j < n_in; ++j) issue(j);
+    auto wait = [&](int j) { return bounded_wait(&bar[j % LNS], (uint32_t)(j / LNS) & 1u); };
+    auto fail = [&](int last_issued) {
+        if (tid == 0) {
+            atomicExch(status, SCAFES_ERR_TIMEOUT);
+            for (int j = last_issued - (LNS - 1); j <= last_issued; ++j)
+                if (j >= 0 && j < n_in) bounded_wait(&bar[j % LNS], (uint32_t)(j / LNS) & 1u, kWaitLimitNs / 16);
+        }
+    };
+    const int x = x0 + tx, y = y0 + ty;
+    const bool live = x < L.nx && y < L.ny;
     const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
-    const long long st[3] = {1, L.pitch, L.plane};
-    const int z0 = blockIdx.z * MZ, z1 = min(z0 + MZ, L.nz);
+    const int bc = (ty + 1) * LBW + tx + 2;                 // own node in a box
     const float2 zero = make_float2(0.f, 0.f);
-    for (int z = z0; z < z1; ++z) {
-        const long long m = L.idx(x, y, z);
+    bool ok = wait(0);
+    ok = wait(1) && ok;
+    int issued = min(LNS, n_in) - 1;
+    long long o = live ? L.idx(x, y, z0) : 0;
+    for (int z = z0; z < z1; ++z, o += L.plane) {
+        const int jc = z - z0 + 1;  // input plane of z
+        if (!__syncthreads_and(ok)) {  // plane z-2's slot is free; all waits so far succeeded
+            fail(issued);
+            return;
+        }
+        if (tid == 0 && jc + LNS - 2 < n_in && jc + LNS - 2 > issued) {
+            fence_proxy_async_smem();
+            issue(jc + LNS - 2);
+            issued = jc + LNS - 2;
+        }
+        ok = wait(jc + 1) && ok;  // plane z+1
+        if (!live) continue;
         if (colb || z == 0 || z == L.nz - 1) {
-            up[m] = zero;
-            up[m + comp] = zero;
-            up[m + 2 * comp] = zero;
+            up[o] = zero;
+            up[o + comp] = zero;
+            up[o + 2 * comp] = zero;
             continue;
         }
+        const float2* pb = lsm + ((jc - 1) % LNS) * LSLOT;  // plane z-1
+        const float2* pc = lsm + (jc % LNS) * LSLOT;        // plane z
+        const float2* pa = lsm + ((jc + 1) % LNS) * LSLOT;  // plane z+1
+        // Component q of u^n at offset (dx, dy, dz), dz in {-1, 0, 1}.
+        auto U = [&](int q, int dx, int dy, int dz) -> float2 {
+            const float2* pl = dz < 0 ? pb : (dz > 0 ? pa : pc);
+            return pl[q * LBOX + bc + dx + dy * LBW];
+        };
         float2 out[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float2* uc = u + c * comp;
-            const float2 uv = uc[m];
+            const float2 uv = U(c, 0, 0, 0);
             PAcc acc{0.f, 0.f};
             pa_prod(acc, K.d[c], Op{uv.x, uv.y});
-            pa_add(acc, up[m + c * comp], -1.f);
+            pa_add(acc, up[o + c * comp], -1.f);
 #pragma unroll
-            for (int p = 0; p < 3; ++p) pa_prod(acc, K.a[c][p], op_sum(uc[m + st[p]], uc[m - st[p]]));
+            for (int p = 0; p < 3; ++p) {
+                const int dx = p == 0, dy = p == 1, dz = p == 2;
+                pa_prod(acc, K.a[c][p], op_sum(U(c, dx, dy, dz), U(c, -dx, -dy, -dz)));
+            }
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 if (q == c) continue;
-                const float2* uq = u + q * comp;
-                const long long sp = st[c], sq = st[q];
+                // (u_q(+c+q) - u_q(+c-q)) - (u_q(-c+q) - u_q(-c-q))
+                const int cx = c == 0, cy = c == 1, cz = c == 2, qx = q == 0, qy = q == 1, qz = q == 2;
                 pa_prod(acc, K.b[c][q],
-                        op_diff2(uq[m + sp + sq], uq[m + sp - sq], uq[m - sp + sq], uq[m - sp - sq]));
+                        op_diff2(U(q, cx + qx, cy + qy, cz + qz), U(q, cx - qx, cy - qy, cz - qz),
+                                 U(q, -cx + qx, -cy + qy, -cz + qz), U(q, -cx - qx, -cy - qy, -cz - qz)));
             }
             out[c] = pa_result(acc);
         }
-        up[m] = out[0];
-        up[m + comp] = out[1];
-        up[m + 2 * comp] = out[2];
+        up[o] = out[0];
+        up[o + comp] = out[1];
+        up[o + 2 * comp] = out[2];
     }
+    if (!__syncthreads_and(ok)) fail(issued);
 }
 
 // v + sign * ch * ((a - b) - (c - d)) on pairs.
@@ -510,6 +586,8 @@ struct scafes_mf {
     int* status = nullptr;    // device status word of the TMA sweeps (0 = ok)
     CUtensorMap ytm[2][6];    // FP32 Yee: per field set, the TMA maps of Ex..Hz
     bool ytm_ok = false;
+    CUtensorMap ltm[2][3];    // pair Lame: per half of mem, the TMA maps of its three components
+    bool ltm_ok = false;
     std::string err;
 };
 
@@ -640,8 +718,25 @@ static int mf_status(scafes_mf* h) {
     MTRY(h, cudaStreamSynchronize(h->stream));
     if (st != 0) {
         cudaMemsetAsync(h->status, 0, sizeof(int), h->stream);
-        return mfail(h, SCAFES_ERR_TIMEOUT, "a Yee sweep gave up waiting for its TMA loads; results are invalid");
+        return mfail(h, SCAFES_ERR_TIMEOUT, "a multi-field sweep gave up waiting for its TMA loads; results are invalid");
     }
+    return SCAFES_OK;
+}
+
+// TMA maps of both halves (pair Lame): 36 x 10 boxes of each component.
+static int lame_maps(scafes_mf* h) {
+    if (h->ltm_ok) return SCAFES_OK;
+    const Layout& L = h->L;
+    for (int half = 0; half < 2; ++half)
+        for (int c = 0; c < 3; ++c) {
+            const CUresult r = make_tensor_map_3d(&h->ltm[half][c], field_ptr(h, 3 * half + c), 8, L.nx, L.ny, L.nz,
+                                                  (size_t)L.pitch * 8, (size_t)L.plane * 8, LBW, LBH);
+            if (r != CUDA_SUCCESS) return mfail(h, SCAFES_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+        }
+    const cudaError_t e = cudaFuncSetAttribute(k_lame_x2_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)LAME_SMEM);
+    if (e != cudaSuccess) return mfail(h, SCAFES_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(e));
+    h->ltm_ok = true;
     return SCAFES_OK;
 }
 
@@ -727,13 +822,21 @@ extern "C" int scafes_mf_step(scafes_mf* h, int n_steps) {
             K2.d[cc] = split3(2.0 - 2.0 * sa);
         }
         const bool x2 = c.precision == SCAFES_PREC_F32X2;
+        if (x2) {
+            const int rc = lame_maps(h);
+            if (rc) return rc;
+        }
+        const dim3 lgrid((L.nx + LX - 1) / LX, (L.ny + LY - 1) / LY, (L.nz + LZ - 1) / LZ);
         for (int st = 0; st < n_steps; ++st) {
             void* u = field_ptr(h, 3 * h->cur);
             void* up = field_ptr(h, 3 * (h->cur ^ 1));
-            if (x2)
-                k_lame_x2<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>((const float2*)u, (float2*)up, K2, L, comp);
-            else
+            if (x2) {
+                const CUtensorMap* t = h->ltm[h->cur];
+                k_lame_x2_tma<<<lgrid, dim3(LX, LY), LAME_SMEM, h->stream>>>(t[0], t[1], t[2], (float2*)up, K2, L,
+                                                                            comp, h->status);
+            } else {
                 k_lame<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>((const double*)u, (double*)up, K, L, comp);
+            }
             MTRY(h, cudaGetLastError());
             h->cur ^= 1;
             h->t += 1;
