@@ -262,6 +262,12 @@ k_lame_x2_tma(const __grid_constant__ CUtensorMap t0, const __grid_constant__ CU
     ok = wait(1) && ok;
     int issued = min(LNS, n_in) - 1;
     long long o = live ? L.idx(x, y, z0) : 0;
+    // u^{n-1} of the node one plane ahead, in registers (its loads overlap
+    // the plane before).
+    float2 pn[3] = {zero, zero, zero};
+    if (live)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) pn[c] = up[o + c * comp];
     for (int z = z0; z < z1; ++z, o += L.plane) {
         const int jc = z - z0 + 1;  // input plane of z
         if (!__syncthreads_and(ok)) {  // plane z-2's slot is free; all waits so far succeeded
@@ -273,6 +279,10 @@ k_lame_x2_tma(const __grid_constant__ CUtensorMap t0, const __grid_constant__ CU
             issue(jc + LNS - 2);
             issued = jc + LNS - 2;
         }
+        const float2 pc0 = pn[0], pc1 = pn[1], pc2 = pn[2];
+        if (live && z + 1 < z1)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) pn[c] = up[o + L.plane + c * comp];
         ok = wait(jc + 1) && ok;  // plane z+1
         if (!live) continue;
         if (colb || z == 0 || z == L.nz - 1) {
@@ -295,7 +305,7 @@ k_lame_x2_tma(const __grid_constant__ CUtensorMap t0, const __grid_constant__ CU
             const float2 uv = U(c, 0, 0, 0);
             PAcc acc{0.f, 0.f};
             pa_prod(acc, K.d[c], Op{uv.x, uv.y});
-            pa_add(acc, up[o + c * comp], -1.f);
+            pa_add(acc, c == 0 ? pc0 : (c == 1 ? pc1 : pc2), -1.f);
 #pragma unroll
             for (int p = 0; p < 3; ++p) {
                 const int dx = p == 0, dy = p == 1, dz = p == 2;
