@@ -8,6 +8,7 @@
 //   5 PropagationFromLeftLowerCorner              6 HeatEqnFDM/Cauchy/TimeLinSpaceLin
 //   7 PennesBioheatEqnFDM/Neumann/TimeLinSpaceLin 8 PennesBioheatEqnFDM/Radiation/TimeLinSpaceLin
 //   9 examples/TumorHeatEqnFDM                   10 examples/MRIDataPBHEqnFDM
+//  11 examples/LameNavierEqnFDMFirstOrder (six unknown fields)
 // (the examples need Boost.PropertyTree for their constants: the stand-in
 // of oracle/ref_harness/stub goes on the include path).  Options:
 //   --dump=PATH       also write the device form to PATH (dumpDeviceForm)
@@ -15,6 +16,8 @@
 //                     Parameters.ini in TumorHeatEqnFDM order; MRI: H T_INF
 //                     Q_BC Q_SKULL EPSILON T_INIT)
 //   --fields=PATH     MRI: its nine known fields, raw FP64
+//   --run=PATH        run iterateOverTime() on the GPU and write every
+//                     unknown field of the final iterate to PATH
 #include <cstdio>
 #include <iostream>
 #include <sstream>
@@ -43,6 +46,15 @@ struct MriFilled : public MRIDataPBHEqnFDM<double, 3> {
     }
 };
 #endif
+#if PROBLEM == 11
+#include "LameNavierEqnFDMFirstOrder.hpp"
+#endif
+// The final iterate (the "old" set after the last swap) of a problem class.
+template <class P>
+struct Latest : public P {
+    using P::P;
+    const std::vector<ScaFES::DataField<double, 3>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};
 #if PROBLEM == 1 || PROBLEM == 2 || PROBLEM == 4 || PROBLEM == 6 || PROBLEM == 7 || PROBLEM == 8
 #include "TimeLinSpaceLin.hpp"
 #define CLASS TimeLinSpaceLin
@@ -64,7 +76,7 @@ static std::vector<double> read_doubles(const std::string& path) {
 }
 
 int main(int argc, char** argv) {
-    std::string dump;
+    std::string dump, run;
     std::vector<double> pv, fields;
     for (int i = 1; i < argc; ++i) {
         const std::string a = argv[i];
@@ -75,6 +87,7 @@ int main(int argc, char** argv) {
             while (std::getline(ss, item, ',')) pv.push_back(std::atof(item.c_str()));
         }
         if (a.compare(0, 9, "--fields=") == 0) fields = read_doubles(a.substr(9));
+        if (a.compare(0, 6, "--run=") == 0) run = a.substr(6);
     }
     (void)fields;
     try {
@@ -88,6 +101,15 @@ int main(int argc, char** argv) {
         TumorHeatEqnFDM<double, 3> ppp(params, gg, false, {"T"}, {1}, {false}, pt, {0}, {0.0},
                                        std::vector<ScaFES::WriteHowOften>(1, ScaFES::WriteHowOften::NEVER), {true},
                                        std::vector<double>(), {false});
+#elif PROBLEM == 11
+        const std::vector<std::string> names{"F1", "F2", "F3", "G1", "G2", "G3", "U1", "U2", "U3", "V1", "V2", "V3"};
+        std::vector<bool> known(12, false);
+        for (int i = 0; i < 6; ++i) known[i] = true;
+        Latest<LameNavierEqnFDMFirstOrder<double, 3>> ppp(
+            params, gg, false, names, std::vector<int>{0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1}, known,
+            std::vector<int>(12, 0), std::vector<double>(12, 0.0),
+            std::vector<ScaFES::WriteHowOften>(12, ScaFES::WriteHowOften::NEVER), std::vector<bool>(12, false),
+            std::vector<double>());
 #elif PROBLEM == 10
         static const char* NAMES[] = {"H", "T_INF", "Q_BC", "Q_SKULL", "EPSILON"};
         boost::property_tree::ptree pt;
@@ -122,6 +144,19 @@ int main(int argc, char** argv) {
 #endif
         if (!dump.empty()) ppp.dumpDeviceForm(dump);
         std::cout << "FORM " << ppp.deviceForm() << std::endl;
+#if PROBLEM == 11
+        if (!run.empty()) {
+            ppp.iterateOverTime();
+            const auto& g = ppp.globalGrid().discreteDomain();
+            std::vector<double> v;
+            for (const auto& df : ppp.latest())
+                for (long long m = 0; m < g.nNodesTotal(); ++m) v.push_back(df(g.idxNodeScalar2TupleStyleFortran(m)));
+            FILE* f = std::fopen(run.c_str(), "wb");
+            if (!f || std::fwrite(v.data(), sizeof(double), v.size(), f) != v.size()) return 4;
+            std::fclose(f);
+            std::cout << "RAN " << ppp.gpuMilliseconds() << " ms" << std::endl;
+        }
+#endif
     } catch (const std::exception& e) {
         std::cout << "REFUSED " << e.what() << std::endl;
     }

@@ -627,3 +627,96 @@ public:
     }
     const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
 };
+
+// LameFirstOrder -- the update of the reference's first-order Lame-Navier
+// example (examples/LameNavierEqnFDMFirstOrder/LameNavierEqnFDMFirstOrder.hpp:
+// 393-520), restated statement by statement in the example's operation
+// order so that the recorded rules are the same doubles: unknown fields
+// U1 U2 U3 V1 V2 V3 (indices 0..5), known fields F1..F3, G1..G3 (zero in
+// the example), material constants of the example.  Its statements are
+// kept as the example has them, including the ones that look unintended
+// (the third component's Laplacian accumulates into the first
+// displacement; the first velocity starts from twice its old value): the
+// point is to run what the reference runs.
+template <typename CT, std::size_t DIM>
+class LameFirstOrder : public ScaFES::Problem<LameFirstOrder<CT, DIM>, CT, DIM> {
+    using Base = ScaFES::Problem<LameFirstOrder<CT, DIM>, CT, DIM>;
+    using Tup = ScaFES::Ntuple<int, DIM>;
+public:
+    using Base::Base;
+    const double E = 1.0e6, NU = 0.4999;
+    const double LAMBDA = NU * E / ((1.0 + NU) * (1.0 - 2.0 * NU));
+    const double MU = E / (2.0 * (1.0 + NU));
+    const double RHO = 1.0, FREQ = 1.0;
+    const double OMEGA = 2.0 * M_PI * FREQ;
+    void evalInner(std::vector<ScaFES::DataField<CT, DIM>>& v, const Tup& n, const int& t) {
+        for (int i = 0; i < 8; ++i) v[i](n) = 0.0;
+        v[8](n) = OMEGA * std::cos(OMEGA * this->time(t));
+    }
+    void evalBorder(std::vector<ScaFES::DataField<CT, DIM>>& v, const Tup& n, const int& t) { evalInner(v, n, t); }
+    template <typename TT>
+    void initInner(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>&, const Tup& n, const int& t) {
+        const double w = OMEGA * this->time(t);
+        for (int i = 0; i < 6; ++i) v[i](n) = 0.0;
+        v[2](n) = std::sin(w);
+        v[5](n) = OMEGA * std::cos(w);
+    }
+    template <typename TT>
+    void initBorder(std::vector<ScaFES::DataField<TT, DIM>>& v, const std::vector<TT>& o, const Tup& n, const int& t) {
+        initInner<TT>(v, o, n, t);
+    }
+    // t -= MU tau (2 s(n) - s(n-p) - s(n+p)) / hh, summed over the axes p.
+    template <typename TT>
+    void lap(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+             const Tup& n, int t, int s, bool with_rho) {
+        for (std::size_t p = 0; p < DIM; ++p) {
+            const double hh = with_rho ? this->gridsize(p) * this->gridsize(p) * RHO
+                                       : this->gridsize(p) * this->gridsize(p);
+            vNew[t](n) -= MU * this->tau() *
+                          (2.0 * vOld[s](n) - vOld[s](this->connect(n, 2 * p)) - vOld[s](this->connect(n, 2 * p + 1))) /
+                          hh;
+        }
+    }
+    // t -= (MU + LAMBDA) tau (s(a) - s(b) - s(n) + s(d)) / hh
+    template <typename TT>
+    void mix(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+             const Tup& n, int t, int s, const Tup& a, const Tup& b, const Tup& d, double hh) {
+        vNew[t](n) -= (MU + LAMBDA) * this->tau() * (vOld[s](a) - vOld[s](b) - vOld[s](n) + vOld[s](d)) / hh;
+    }
+    template <typename TT>
+    void updateInner(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                     const Tup& n, const int&) {
+        auto c = [&](const Tup& m, int dir) { return this->connect(m, dir); };
+        const double h0 = this->gridsize(0), h1 = this->gridsize(1), h2 = this->gridsize(2);
+        for (int a = 0; a < 3; ++a) vNew[a](n) = vOld[a](n) + this->tau() * vOld[3 + a](n);
+        vNew[3](n) += vOld[3](n);
+        lap<TT>(vNew, vOld, n, 0, 0, true);
+        mix<TT>(vNew, vOld, n, 3, 0, c(n, 1), n, c(n, 0), h0 * h0);
+        mix<TT>(vNew, vOld, n, 3, 0, c(n, 3), c(c(n, 3), 0), c(n, 0), h0 * h1);
+        mix<TT>(vNew, vOld, n, 3, 0, c(n, 5), c(c(n, 5), 0), c(n, 0), h0 * h2);
+        vNew[3](n) -= this->tau() * this->knownDf(0, n);
+        vNew[4](n) = vOld[4](n);
+        lap<TT>(vNew, vOld, n, 1, 1, false);
+        mix<TT>(vNew, vOld, n, 4, 1, c(n, 3), n, c(n, 2), h1 * h1);
+        mix<TT>(vNew, vOld, n, 4, 1, c(n, 1), c(c(n, 1), 2), c(n, 2), h1 * h0);
+        mix<TT>(vNew, vOld, n, 4, 1, c(n, 5), c(c(n, 5), 2), c(n, 2), h1 * h2);
+        vNew[4](n) -= this->tau() * this->knownDf(1, n);
+        vNew[5](n) = vOld[5](n);
+        lap<TT>(vNew, vOld, n, 0, 2, false);
+        mix<TT>(vNew, vOld, n, 5, 2, c(n, 1), n, c(n, 4), h2 * h2);
+        mix<TT>(vNew, vOld, n, 5, 2, c(n, 1), c(c(n, 1), 4), c(n, 4), h2 * h1);
+        mix<TT>(vNew, vOld, n, 5, 2, c(n, 3), c(c(n, 3), 4), c(n, 4), h2 * h2);
+        vNew[5](n) -= this->tau() * this->knownDf(2, n);
+    }
+    template <typename TT>
+    void updateBorder(std::vector<ScaFES::DataField<TT, DIM>>& vNew, const std::vector<ScaFES::DataField<TT, DIM>>& vOld,
+                      const Tup& n, const int&) {
+        for (int a = 0; a < 3; ++a) vNew[a](n) = vOld[a](n) + this->tau() * vOld[3 + a](n);
+        for (int a = 0; a < 3; ++a) vNew[3 + a](n) = this->knownDf(3 + a, n);
+    }
+    template <typename TT>
+    void updateInner2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const Tup&, const int&) {}
+    template <typename TT>
+    void updateBorder2(std::vector<ScaFES::DataField<TT, DIM>>&, const std::vector<ScaFES::DataField<TT, DIM>>&, const Tup&, const int&) {}
+    const std::vector<ScaFES::DataField<CT, DIM>>& latest() const { return this->mVectUnknownDfsDomOld; }
+};

@@ -1,7 +1,7 @@
 // Runs one problem of problems.hpp through the drop-in ScaFES::Problem
 // (test infrastructure).  Usage:
 //   run_problem <heat_lin|pennes_lin|mirror_pow2|heat_sine|heat_neumann|heat_cauchy|
-//                pennes_radiation|tumour|mri|yee> out.bin
+//                pennes_radiation|tumour|mri|yee|lame_first_order> out.bin
 //               [--extract-only] [--dump=PATH] [--params=a,b,...] [--fields=PATH]
 //               [ScaFES options...]
 // Writes the final iterate as raw doubles (x fastest); with --extract-only
@@ -107,6 +107,17 @@ int main(int argc, char** argv) {
                                    std::vector<ScaFES::WriteHowOften>(6, ScaFES::WriteHowOften::NEVER),
                                    std::vector<bool>(6, false));
             p.setFields(g_fields);
+            return run(p, out, extract);
+        }
+        if (which == "lame_first_order") {
+            std::vector<bool> known(12, false);
+            for (int i = 0; i < 6; ++i) known[i] = true;
+            LameFirstOrder<double, 3> p(params, gg, false,
+                                        {"F1", "F2", "F3", "G1", "G2", "G3", "U1", "U2", "U3", "V1", "V2", "V3"},
+                                        std::vector<int>{0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1}, known,
+                                        std::vector<int>(12, 0), std::vector<double>(12, 0.0),
+                                        std::vector<ScaFES::WriteHowOften>(12, ScaFES::WriteHowOften::NEVER),
+                                        std::vector<bool>(12, false));
             return run(p, out, extract);
         }
         if (which == "mirror_pow2") {

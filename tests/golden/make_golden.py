@@ -7,7 +7,7 @@ headers by ``make -C oracle ref`` -- and stores its inputs and final iterate.
 
 Run from the repository root (needs the reference checkout for the build):
 
-    make -C oracle ref && python tests/golden/make_golden.py [--tissue | --tangent]
+    make -C oracle ref && python tests/golden/make_golden.py [--tissue | --tangent | --lame-first-order]
 
 The .npz files are committed; the GPU machine never runs this script.
 """
@@ -122,6 +122,7 @@ def main():
 
     cases.update(tissue_cases(tmp))
     cases.update(tangent_cases(tmp))
+    cases.update(lame_first_order_cases(tmp))
     save(cases)
 
 
@@ -195,6 +196,20 @@ def tissue_cases(tmp):
     return cases
 
 
+def lame_first_order_cases(tmp):
+    """The reference's first-order Lame-Navier example (examples/
+    LameNavierEqnFDMFirstOrder), compiled unmodified: six unknown fields
+    coupled through its updateInner/updateBorder, known fields zero, its own
+    initial state (V3 = omega); a time step small enough for the example's
+    stiff constants (lambda ~ 1.7e9)."""
+    cases = {}
+    for name, n, T, tau in (("lame_first_order", (12, 10, 9), 40, 1e-10),
+                            ("lame_first_order_b", (17, 9, 13), 25, 5e-11)):
+        r = O.run_ref("ref_lame_first_order", n, T, tmp, tau=tau, t_end=tau * T, inputs=None, nfields=6)
+        cases[name] = dict(n=n, nsteps=T, tau=tau, t_end=tau * T, final=r)
+    return cases
+
+
 def save(cases):
     for name, c in cases.items():
         arrays = {k: np.asarray(v) for k, v in c.items()}
@@ -207,5 +222,7 @@ if __name__ == "__main__":
         save(tissue_cases(tempfile.mkdtemp()))
     elif sys.argv[1:] == ["--tangent"]:  # only the dual-number gradient case
         save(tangent_cases(tempfile.mkdtemp()))
+    elif sys.argv[1:] == ["--lame-first-order"]:  # only the multi-unknown example
+        save(lame_first_order_cases(tempfile.mkdtemp()))
     else:
         main()

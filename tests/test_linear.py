@@ -191,3 +191,86 @@ def test_dropin_yee_matches_oracle(gpu, run_problem, tmp_path):
     got = np.fromfile(out, dtype=np.float64).reshape(6, n[2], n[1], n[0])
     ref = O.yee(O.make_grid(n, last=last, tau=tau), f0, T, (0, 0, 0), 0.0, 1.0, 1.0, 1.0)
     assert cases.rel_err(got, ref) <= 1e-12
+
+
+# The reference's own multi-unknown class: examples/LameNavierEqnFDMFirstOrder
+# (six unknown fields, displacements and velocities, coupled through its
+# updateInner/updateBorder), compiled unchanged against the drop-in where the
+# reference checkout exists; its restatement LameFirstOrder
+# (tests/dropin/problems.hpp) must give the same device form byte for byte,
+# and runs on the GPU against the reference's own run of the example
+# (tests/golden/lame_first_order*.npz, made by
+# oracle/ref_harness/ref_lame_first_order.cpp from the untouched headers).
+from dropin.build import REFERENCE  # noqa: E402
+
+LAME_FO = REFERENCE / "examples" / "LameNavierEqnFDMFirstOrder"
+LAME_FO_GOLDEN = ["lame_first_order", "lame_first_order_b"]
+
+
+def lame_fo_args(d):
+    n = [int(v) for v in d["n"]]
+    return [f"--nNodes={n[0]}x{n[1]}x{n[2]}", f"--tau={float(d['tau'])!r}", f"--nTimesteps={int(d['nsteps'])}",
+            f"--endtime={float(d['t_end'])!r}"]
+
+
+@pytest.mark.skipif(not (LAME_FO / "LameNavierEqnFDMFirstOrder.hpp").exists(), reason="reference checkout not present")
+@pytest.mark.parametrize("golden", LAME_FO_GOLDEN)
+def test_reference_multi_unknown_class_equals_restatement(run_problem, tmp_path, golden):
+    from conftest import load_golden
+    d = load_golden(golden)
+    exe = compile_cpp(HERE / "extract_reference.cpp", tmp_path / "xref11", ["-DPROBLEM=11", "-I", str(LAME_FO)])
+    r = subprocess.run([str(exe), f"--dump={tmp_path}/ref.bin", *lame_fo_args(d)], capture_output=True, text=True,
+                       timeout=300)
+    assert "FORM linear multi-field fields=6 phases=1" in r.stdout, r.stdout + r.stderr
+    o = subprocess.run([str(run_problem), "lame_first_order", "/dev/null", f"--dump={tmp_path}/ours.bin",
+                        *lame_fo_args(d)], capture_output=True, text=True, timeout=300)
+    assert o.returncode == 0, o.stderr
+    assert (tmp_path / "ref.bin").read_bytes() == (tmp_path / "ours.bin").read_bytes()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("golden", LAME_FO_GOLDEN)
+def test_reference_multi_unknown_class_matches_reference_run(gpu, run_problem, tmp_path, golden):
+    """Every unknown field against the reference's run of the example,
+    relative max-norm 1e-12 per field (fields that stay zero must stay
+    exactly zero)."""
+    from conftest import load_golden
+    d = load_golden(golden)
+    n = [int(v) for v in d["n"]]
+    out = tmp_path / "out.bin"
+    res = subprocess.run([str(run_problem), "lame_first_order", str(out), *lame_fo_args(d)], capture_output=True,
+                         text=True, timeout=300)
+    assert res.returncode == 0, res.stdout + res.stderr
+    got = np.fromfile(out, dtype=np.float64).reshape(6, n[2], n[1], n[0])
+    ref = d["final"]
+    for f in range(6):
+        if np.max(np.abs(ref[f])) == 0.0:
+            assert np.all(got[f] == 0.0), f
+        else:
+            assert cases.rel_err(got[f], ref[f]) <= 1e-12, f
+
+
+@pytest.mark.parametrize("golden", LAME_FO_GOLDEN)
+def test_recorded_rules_reproduce_reference_run_on_cpu(run_problem, tmp_path, golden):
+    """The rules the drop-in records from the restated example, applied on
+    the CPU (numpy) from the example's initial state (V3 = omega, the rest
+    zero), reproduce the reference's own run: relative max-norm 1e-12 per
+    field."""
+    from conftest import load_golden
+    d = load_golden(golden)
+    n = [int(v) for v in d["n"]]
+    o = subprocess.run([str(run_problem), "lame_first_order", "/dev/null", f"--dump={tmp_path}/d.bin",
+                        *lame_fo_args(d)], capture_output=True, text=True, timeout=300)
+    assert o.returncode == 0, o.stderr
+    nu, nph, rules = read_lin_rules(tmp_path / "d.bin")
+    assert (nu, nph) == (6, 1)
+    terms = {k: [(s, dx, dy, dz, w) for (s, dx, dy, dz), w in v.items()] for k, v in rules.items()}
+    f0 = np.zeros((6, n[2], n[1], n[0]))
+    f0[5] = 2.0 * np.pi
+    got = apply_rules(terms, f0, 1, int(d["nsteps"]))
+    ref = d["final"]
+    for f in range(6):
+        if np.max(np.abs(ref[f])) == 0.0:
+            assert np.all(got[f] == 0.0), f
+        else:
+            assert cases.rel_err(got[f], ref[f]) <= 1e-12, f
