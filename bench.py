@@ -270,7 +270,7 @@ def cpu_section_baselines(args) -> dict:
     host threads), each timed on a bounded sample of its workload:
     batched -- the first 16 ensemble instances x 50 steps; adjoint -- the
     forward solve and the adjoint at 64^3 x 200 steps (every state stored);
-    Lame 192^3 x 40 steps; Yee 256^3 x 80 steps."""
+    Lame 192^3 x 40 steps; Yee 256^3 x 80 steps; tissue 192^3 x 20 steps."""
     import oracle as O
     from masterthesis_gb300 import workloads as W
     threads = os.cpu_count() or 1
@@ -322,6 +322,18 @@ def cpu_section_baselines(args) -> dict:
     dt = time.perf_counter() - t0
     out["yee_f64"] = {"value": 256 ** 3 * T / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
                       "sample": f"256^3 x {T} steps ({dt:.1f} s)"}
+    # Tissue (the MRI-data example's update with per-node coefficients).
+    m, T = 192, 20
+    nn = (m, m, m)
+    f = W.tissue_fields_slab(nn, 0, m, 31)
+    g = O.make_grid(nn, last=TISSUE_LAST, tau=W.tissue_tau(nn, TISSUE_LAST))
+    u0 = np.full((m, m, m), 37.0)
+    t0 = time.perf_counter()
+    O.pennes_tissue(g, u0, T, f, zmax_kind=0, q_bc=TISSUE_FLUX["q_bc"], q_skull=TISSUE_FLUX["q_skull"],
+                    nthreads=threads)
+    dt = time.perf_counter() - t0
+    out["tissue"] = {"value": m ** 3 * T / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                     "sample": f"{m}^3 x {T} steps ({dt:.1f} s)"}
     return out
 
 
@@ -963,6 +975,8 @@ def run_ours(args, dist: Dist):
             adjoint["cpu_baseline"] = sec["adjoint"]
         if multifield:
             multifield["cpu_baseline"] = {"lame_f64": sec["lame_f64"], "yee_f64": sec["yee_f64"]}
+        if tissue:
+            tissue["cpu_baseline"] = sec["tissue"]
     return res
 
 
