@@ -11,7 +11,9 @@
 // 2596-2619, 2829-2918; every node of the new iterate starts as a copy of
 // the old one, :5078-5082, which a recorded rule already contains).
 // FP64, plain loads: a correctness path for the problems the fused kernels
-// (Lame-Navier, Yee) do not cover as recorded callbacks.
+// (Lame-Navier, Yee) do not cover as recorded callbacks.  Each field has its
+// own pair of buffers; a field that a phase leaves alone on every node (its
+// rule the identity) is neither copied nor swapped in that phase.
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -44,21 +46,30 @@ struct Term {
 
 constexpr int kClasses = SCAFES_BORDER_CLASSES;
 
-__global__ void k_linear(const double* __restrict__ in, double* __restrict__ out, const Rule* __restrict__ rules,
-                         const Term* __restrict__ terms, int n_fields, long long field_stride, Layout L) {
+// Where each field of one phase is read from and written to.  A field whose
+// rule is the identity on every node class in this phase is neither
+// written nor swapped (out = nullptr): its current buffer stays current.
+struct FieldPtrs {
+    const double* in[SCAFES_LIN_MAX_FIELDS];
+    double* out[SCAFES_LIN_MAX_FIELDS];
+};
+
+__global__ void k_linear(FieldPtrs P, const Rule* __restrict__ rules, const Term* __restrict__ terms, int n_fields,
+                         Layout L) {
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y, z = blockIdx.z;
     if (x >= L.nx || y >= L.ny) return;
     const int cls = (x == 0) | ((x == L.nx - 1) << 1) | ((y == 0) << 2) | ((y == L.ny - 1) << 3) | ((z == 0) << 4) |
                     ((z == L.nz - 1) << 5);
     const long long o = L.idx(x, y, z);
     for (int f = 0; f < n_fields; ++f) {
+        if (P.out[f] == nullptr) continue;
         const Rule r = rules[f * kClasses + cls];
         double v = r.cst;
         for (int k = r.off; k < r.off + r.n; ++k) {
             const Term t = terms[k];
-            v = fma(t.w, in[t.src * field_stride + o + t.d], v);
+            v = fma(t.w, P.in[t.src][o + t.d], v);
         }
-        out[f * field_stride + o] = v;
+        P.out[f][o] = v;
     }
 }
 
@@ -70,7 +81,8 @@ struct scafes_lin {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     double* buf[2] = {nullptr, nullptr};  // all fields, padded layout, field after field
-    int cur = 0;
+    int cur[SCAFES_LIN_MAX_FIELDS] = {};  // per field, the buffer holding its current values
+    std::vector<bool> ident;              // [phase][field]: the identity on every class
     // Host rules: [phase][field][class] -> terms; the device copies are
     // rebuilt when a rule changes.
     std::vector<std::vector<scafes_lin_term>> host_terms;
@@ -124,6 +136,14 @@ int sync_rules(scafes_lin* h) {
         r[s].n = (int)h->host_terms[s].size();
         r[s].cst = h->host_cst[s];
         for (const auto& q : h->host_terms[s]) t.push_back(Term{h->L.idx(q.dx, q.dy, q.dz), q.src, q.w});
+    }
+    h->ident.assign((size_t)h->n_phases * h->n_fields, true);
+    for (size_t s = 0; s < r.size(); ++s) {
+        const int ph = (int)(s / ((size_t)h->n_fields * kClasses)), f = (int)(s / kClasses % h->n_fields);
+        const auto& tl = h->host_terms[s];
+        const bool id = h->host_cst[s] == 0.0 && tl.size() == 1 && tl[0].src == f && tl[0].dx == 0 &&
+                        tl[0].dy == 0 && tl[0].dz == 0 && tl[0].w == 1.0;
+        if (!id) h->ident[(size_t)ph * h->n_fields + f] = false;
     }
     cudaFree(h->rules);
     cudaFree(h->terms);
@@ -230,7 +250,7 @@ extern "C" int scafes_lin_upload(scafes_lin* h, int field, const double* host, s
     const Layout& L = h->L;
     if (field < 0 || field >= h->n_fields || n != (size_t)L.nx * L.ny * L.nz)
         return lfail(h, SCAFES_ERR_ARG, "scafes_lin_upload: field %d / %zu values", field, n);
-    double* d = h->buf[h->cur] + (size_t)field * field_stride(h);
+    double* d = h->buf[h->cur[field]] + (size_t)field * field_stride(h);
     LTRY(h, cudaMemcpy2DAsync(d, (size_t)L.pitch * 8, host, (size_t)L.nx * 8, (size_t)L.nx * 8, (size_t)L.ny * L.nz,
                               cudaMemcpyHostToDevice, h->stream));
     LTRY(h, cudaStreamSynchronize(h->stream));
@@ -242,7 +262,7 @@ extern "C" int scafes_lin_download(scafes_lin* h, int field, double* host, size_
     const Layout& L = h->L;
     if (field < 0 || field >= h->n_fields || n != (size_t)L.nx * L.ny * L.nz)
         return lfail(h, SCAFES_ERR_ARG, "scafes_lin_download: field %d / %zu values", field, n);
-    const double* d = h->buf[h->cur] + (size_t)field * field_stride(h);
+    const double* d = h->buf[h->cur[field]] + (size_t)field * field_stride(h);
     LTRY(h, cudaMemcpy2DAsync(host, (size_t)L.nx * 8, d, (size_t)L.pitch * 8, (size_t)L.nx * 8, (size_t)L.ny * L.nz,
                               cudaMemcpyDeviceToHost, h->stream));
     LTRY(h, cudaStreamSynchronize(h->stream));
@@ -259,10 +279,20 @@ extern "C" int scafes_lin_step(scafes_lin* h, int n_steps) {
     LTRY(h, cudaEventRecord(h->e0, h->stream));
     for (int s = 0; s < n_steps; ++s)
         for (int ph = 0; ph < h->n_phases; ++ph) {
-            k_linear<<<grid, block, 0, h->stream>>>(h->buf[h->cur], h->buf[h->cur ^ 1], h->rules + ph * per_phase,
-                                                    h->terms, h->n_fields, field_stride(h), L);
+            FieldPtrs P;
+            for (int f = 0; f < SCAFES_LIN_MAX_FIELDS; ++f) {
+                P.in[f] = nullptr;
+                P.out[f] = nullptr;
+            }
+            for (int f = 0; f < h->n_fields; ++f) {
+                const size_t fo = (size_t)f * field_stride(h);
+                P.in[f] = h->buf[h->cur[f]] + fo;
+                if (!h->ident[(size_t)ph * h->n_fields + f]) P.out[f] = h->buf[h->cur[f] ^ 1] + fo;
+            }
+            k_linear<<<grid, block, 0, h->stream>>>(P, h->rules + ph * per_phase, h->terms, h->n_fields, L);
             LTRY(h, cudaGetLastError());
-            h->cur ^= 1;
+            for (int f = 0; f < h->n_fields; ++f)
+                if (P.out[f]) h->cur[f] ^= 1;
         }
     LTRY(h, cudaEventRecord(h->e1, h->stream));
     LTRY(h, cudaEventSynchronize(h->e1));
