@@ -316,6 +316,44 @@ def test_plain_handle_backward_entry_matches_oracle(gpu, prec, tol):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-11), ("f32x2", 1e-10)])
+def test_plain_handle_backward_entry_nonzero_border(gpu, prec, tol):
+    """A non-zero constant Dirichlet value: G_A uploaded as 0.35 everywhere
+    and u0 equal to it on the border (the border check compares the two in
+    the handle's arithmetic, FP32 pairs included); the forward iterate and
+    both gradients against the oracle; then an initial iterate whose border
+    differs from G_A is refused (UNSUPPORTED) and the handle still works."""
+    M = gpu
+    n, T, a, gval = (18, 16, 14), 20, 0.6, 0.35
+    g, tau, u0, target = plain_heat_case(n, T, a, 41)
+    u0[O.border_mask(g)] = gval
+    k = np.full(u0.shape, a)
+    uT_ref, traj = O.kheat_forward(g, k, u0, T, keep_traj=True)
+    _, gk_ref, gu_ref = O.kheat_adjoint(g, k, traj, target, reset_border=True)
+    with M.Plain(M.make_cfg(n, tau=tau, precision=prec, heat=(a, 1.0, 0.0))) as p:
+        p.upload(M.FIELD_G_A, np.full(u0.shape, gval))
+        p.keep_initial()
+        p.upload(M.FIELD_U, u0)
+        p.step(T)
+        uT = p.download()
+        gk, gu = p.adjoint(uT - target, 5)
+        assert cases.rel_err(uT, uT_ref) <= (1e-12 if prec == "f64" else 1e-11)
+        assert cases.rel_err(gk, gk_ref) <= tol
+        assert cases.rel_err(gu, gu_ref) <= tol
+        bad = u0.copy()
+        bad[0, 3, 4] = gval + 0.25           # one border node off the Dirichlet value
+        p.upload(M.FIELD_U, bad)
+        p.step(T)
+        with pytest.raises(M.ScafesError) as e:
+            p.adjoint(p.download() - target, 5)
+        assert e.value.code == -4
+        p.upload(M.FIELD_U, u0)               # a valid run afterwards gives the same gradients
+        p.step(T)
+        gk2, gu2 = p.adjoint(p.download() - target, 5)
+        assert np.array_equal(gk2, gk) and np.array_equal(gu2, gu)
+
+
+@pytest.mark.gpu
 def test_plain_handle_backward_entry_refuses_what_it_does_not_cover(gpu):
     """Status codes, no fault: no kept initial iterate or no step (STATE),
     a border that differs from the Dirichlet value, a source, the Pennes
