@@ -70,6 +70,10 @@ struct TileJob {
     const CUtensorMap* tmc0 = nullptr;  // TMA descriptors of C0, CA (box 32 x BY), VC tiles only
     const CUtensorMap* tmca = nullptr;
     const scafes_border_node_rule* nodes = nullptr;  // per-node rules (SCAFES_BORDER_NODES)
+    // Per-node rules in FP64: the nodes on an x face outside the y and z
+    // border rows are left to a separate pass (k_xface_node_rules), so that
+    // no warp of an x-face tile spends the narrow FP64 pipe on one lane.
+    bool xface_pass = false;
 };
 
 // The rule of one border node of a SCAFES_BORDER_NODES problem:
@@ -284,8 +288,11 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
             for (int k = 0; k < R; ++k) {
                 const long long off = o0 + (long long)k * L.pitch;
                 const int y = yb + k;
-                const bool live = INNER || (xin && y < L.ny);
-                if (!INNER && live && (xb || y < nl || y > L.ny - 1 - nl)) {
+                bool live = INNER || (xin && y < L.ny);
+                const bool ybord = y < nl || y > L.ny - 1 - nl;
+                if (BORDER == SCAFES_BORDER_NODES && !INNER && J.xface_pass && xb && !ybord)
+                    live = false;  // written by the x-face pass
+                if (!INNER && live && (xb || ybord)) {
                     const T s = (k == 0) ? ym : cur[k - 1];
                     const T n = (k == R - 1) ? yp : cur[k + 1];
                     if (BORDER == SCAFES_BORDER_NODES) {

@@ -34,6 +34,38 @@ star7_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtens
     star7_tile<P, SRC, BORDER, BY, R, NS, FS, ML>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
 }
 
+// FP64 per-node border rules leave the x-face nodes outside the y and z
+// border rows to k_xface_node_rules.
+template <class P, int BORDER>
+constexpr bool XFACE_PASS = std::is_same<P, PolF64>::value && BORDER == SCAFES_BORDER_NODES;
+
+// The per-node rules of the nodes on the two x faces outside the y and z
+// border rows (one border layer), from the old iterate: what node_rule
+// computes for them, in the same FP64 order (a neighbour outside the grid
+// reads 0, as from the TMA halo).  One thread per (face, y, z).
+static __global__ void k_xface_node_rules(const double* __restrict__ uo, double* __restrict__ un,
+                                   const scafes_border_node_rule* __restrict__ nodes, Layout L) {
+    const long long rows = (long long)(L.ny - 2) * (L.nz - 2);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 2 * rows;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int side = (int)(i / rows);
+        const long long r = i % rows;
+        const int y = 1 + (int)(r % (L.ny - 2)), z = 1 + (int)(r / (L.ny - 2));
+        const int x = side ? L.nx - 1 : 0;
+        const long long o = L.idx(x, y, z);
+        const scafes_border_node_rule& R = nodes[border_node_index(L, x, y, z)];
+        const double w = x > 0 ? uo[o - 1] : 0.0, e = x < L.nx - 1 ? uo[o + 1] : 0.0;
+        double v = fma(R.cu, uo[o], R.cst);
+        v = fma(R.cn[0], w, v);
+        v = fma(R.cn[1], e, v);
+        v = fma(R.cn[2], uo[o - L.pitch], v);
+        v = fma(R.cn[3], uo[o + L.pitch], v);
+        v = fma(R.cn[4], uo[o - L.plane], v);
+        v = fma(R.cn[5], uo[o + L.plane], v);
+        un[o] = v;
+    }
+}
+
 // The variable-coefficient sweep: as star7_tma, with the coefficient fields
 // C0 and CA staged by TMA with every plane (and F_A with them when the
 // source is present), and the Dirichlet, table or per-node border.
@@ -55,7 +87,7 @@ star7_vc_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUt
     if (__syncthreads_or(threadIdx.x == 0 && threadIdx.y == 0 && *(volatile int*)status != 0)) return;
     ring_init<NS>(bar);
     TileJob<T> J{&tm, &tmf, un, fa, nullptr, ga, nullptr, gval, L, time_old, time_new, Split{0.0, 0.f, 0.f}, table,
-                 &tmc0, &tmca, nodes};
+                 &tmc0, &tmca, nodes, XFACE_PASS<P, BORDER>};
     const int z0 = blockIdx.z * zchunk;
     const int z1 = min(z0 + zchunk, L.nz);
     uint32_t base = 0;
@@ -172,6 +204,13 @@ static cudaError_t launch_vc_typed(const Star7Launch& a, cudaStream_t stream) {
     kern<<<grid, block, G::SMEM, stream>>>(*a.tm_uo, FS ? *a.tm_f : *a.tm_uo, *a.tm_c0, *a.tm_ca, (T*)a.un,
                                            (const T*)a.fa, (const T*)a.ga, gval, L, a.c, make_split(a.time_old),
                                            make_split(a.time_new), a.table, a.nodes, zchunk, a.status);
+    if constexpr (XFACE_PASS<P, BORDER>) {
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        const long long work = 2LL * (L.ny - 2) * (L.nz - 2);
+        const int blocks = (int)std::min<long long>((work + 255) / 256, (long long)num_sms() * 8);
+        k_xface_node_rules<<<blocks, 256, 0, stream>>>((const double*)a.uo, (double*)a.un, a.nodes, L);
+    }
     return cudaGetLastError();
 }
 
