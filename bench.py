@@ -1073,7 +1073,24 @@ def case_tissue(prec: str, m: int = 256, T: int = 4):
         p.close()
 
 
+def case_heat(prec: str, n: int = 512, T: int = 4):
+    """The large heat workload's field at n^3 in one arithmetic, T sweeps
+    with the autotuned tile (depth 1)."""
+    import masterthesis_gb300 as M
+    _, tau = workload(n)
+    u0 = np.empty((n, n, n))
+    make_u0(n, u0)
+    with M.Plain(M.make_cfg((n, n, n), tau=tau, precision=prec, heat=(1.0, 1.0, 0.0))) as p:
+        p.upload(M.FIELD_U, u0)
+        p.autotune(4)
+        p.set_temporal_depth(1)
+        p.step(T)
+        return f"max|u| {float(np.abs(p.download()).max()):.6e}"
+
+
 KERNEL_CASES = {
+    "heat_f32x2_512": lambda: case_heat("f32x2"),
+    "heat_f64_512": lambda: case_heat("f64"),
     "adjoint_f64_160": lambda: case_adjoint("f64"),
     "adjoint_x2_160": lambda: case_adjoint("f32x2"),
     "lame_x2_192": lambda: case_lame("f32x2"),
