@@ -1073,16 +1073,16 @@ def case_tissue(prec: str, m: int = 256, T: int = 4):
         p.close()
 
 
-def case_heat(prec: str, n: int = 512, T: int = 4):
+def case_heat(prec: str, n: int = 512, T: int = 4, tile: int = 4):
     """The large heat workload's field at n^3 in one arithmetic, T sweeps
-    with the autotuned tile (depth 1)."""
+    with a fixed tile (default {BY 16, R 4, 4 stages}, the autotuner's choice
+    at 512^3) and depth 1: every launch is the same kernel."""
     import masterthesis_gb300 as M
     _, tau = workload(n)
     u0 = np.empty((n, n, n))
     make_u0(n, u0)
-    with M.Plain(M.make_cfg((n, n, n), tau=tau, precision=prec, heat=(1.0, 1.0, 0.0))) as p:
+    with M.Plain(M.make_cfg((n, n, n), tau=tau, precision=prec, heat=(1.0, 1.0, 0.0), tile=tile)) as p:
         p.upload(M.FIELD_U, u0)
-        p.autotune(4)
         p.set_temporal_depth(1)
         p.step(T)
         return f"max|u| {float(np.abs(p.download()).max()):.6e}"
