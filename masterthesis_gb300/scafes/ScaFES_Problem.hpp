@@ -1070,6 +1070,69 @@ void Problem<OWNPRBLM, CT, DIM>::prepareLinear() {
             }
         }
     }
+    // Every other inner node at step 1 must give the inner rule too (a
+    // coefficient read from a known field or a coordinate would not):
+    // recorded in parallel and compared with the rules found above.
+    auto equal_rule = [&](std::size_t s, const std::vector<scafes_lin_term>& terms, double cst) {
+        if (cst != mLinCst[s] || terms.size() != mLinTerms[s].size()) return false;
+        for (const auto& a : terms) {
+            bool found = false;
+            for (const auto& b : mLinTerms[s])
+                if (a.src == b.src && a.dx == b.dx && a.dy == b.dy && a.dz == b.dz) { found = a.w == b.w; break; }
+            if (!found) return false;
+        }
+        return true;
+    };
+    for (int ph = 0; ph < mLinPhases; ++ph) {
+        long long bad = -1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4096)
+#endif
+        for (long long m = 0; m < mN; ++m) {
+            long long seen_bad;
+#ifdef _OPENMP
+#pragma omp atomic read
+#endif
+            seen_bad = bad;
+            if (seen_bad >= 0) continue;
+            const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(m);
+            if (isBorder(n)) continue;
+            std::string e2;
+            const std::vector<gpu::Sym> out = ph == 0 ? record<false, 1>(n, 1, e2) : record<false, 2>(n, 1, e2);
+            bool ok = e2.empty();
+            for (std::size_t f = 0; ok && f < nu; ++f) {
+                std::vector<scafes_lin_term> terms;
+                double cst = 0.0;
+                ok = linearRule(out[f], aff, terms, cst).empty() && equal_rule(slot(ph, f, 0), terms, cst);
+            }
+            if (!ok) {
+#ifdef _OPENMP
+#pragma omp critical(scafes_lin_bad)
+#endif
+                {
+                    long long cur;
+#ifdef _OPENMP
+#pragma omp atomic read
+#endif
+                    cur = bad;
+                    if (cur < 0 || m < cur) {
+#ifdef _OPENMP
+#pragma omp atomic write
+#endif
+                        bad = m;
+                    }
+                }
+            }
+        }
+        if (bad >= 0) {
+            const ScaFES_IntNtuple n = g.idxNodeScalar2TupleStyleFortran(bad);
+            std::ostringstream e;
+            e << "ScaFES::Problem: " << (ph == 0 ? "updateInner" : "updateInner2") << " at node (" << n[0] << ","
+              << n[1] << "," << n[2] << ") differs from the other inner nodes' (coefficients that vary over the "
+              << "nodes have no multi-field device form)";
+            throw std::runtime_error(e.str());
+        }
+    }
     std::ostringstream os;
     os << "linear multi-field fields=" << nu << " phases=" << mLinPhases;
     mSummary = os.str();

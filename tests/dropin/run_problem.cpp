@@ -1,7 +1,7 @@
 // Runs one problem of problems.hpp through the drop-in ScaFES::Problem
 // (test infrastructure).  Usage:
 //   run_problem <heat_lin|pennes_lin|mirror_pow2|heat_sine|heat_neumann|heat_cauchy|
-//                pennes_radiation|tumour|mri|yee|lame_first_order> out.bin
+//                pennes_radiation|tumour|mri|yee|yee_varying|lame_first_order> out.bin
 //               [--extract-only] [--dump=PATH] [--params=a,b,...] [--fields=PATH]
 //               [ScaFES options...]
 // Writes the final iterate as raw doubles (x fastest); with --extract-only
@@ -100,13 +100,14 @@ int main(int argc, char** argv) {
             p.setFields(g_fields);
             return run(p, out, extract);
         }
-        if (which == "yee") {
+        if (which == "yee" || which == "yee_varying") {
             YeeCavity<double, 3> p(params, gg, true, {"Ex", "Ey", "Ez", "Hx", "Hy", "Hz"},
                                    std::vector<int>(6, 1), std::vector<bool>(6, false), std::vector<int>(6, 0),
                                    std::vector<double>(6, 0.0),
                                    std::vector<ScaFES::WriteHowOften>(6, ScaFES::WriteHowOften::NEVER),
                                    std::vector<bool>(6, false));
             p.setFields(g_fields);
+            p.setVarying(which == "yee_varying");
             return run(p, out, extract);
         }
         if (which == "lame_first_order") {

@@ -116,6 +116,19 @@ def test_dropin_yee_records_the_yee_rules(run_problem, tmp_path):
             assert got[(ph, f, c)][k] == pytest.approx(w[k], rel=1e-15), (ph, f, c, k)
 
 
+def test_dropin_refuses_node_varying_multi_field_update(run_problem, tmp_path):
+    """A Yee class whose H coefficient differs at one inner node off the
+    probed lines: every inner node is checked, and the drop-in refuses the
+    problem naming that node (no CPU fallback)."""
+    n, T = (10, 9, 8), 5
+    last, tau, ch, f0 = yee_case(n)
+    f0.tofile(tmp_path / "f.bin")
+    res = subprocess.run([str(run_problem), "yee_varying", "/dev/null", "--extract-only",
+                          *yee_args(n, last, tau, T, tmp_path / "f.bin")], capture_output=True, text=True,
+                         timeout=120)
+    assert res.returncode != 0 and "(3,3,3) differs" in res.stderr, res.stdout + res.stderr
+
+
 def test_lin_create_checks_arguments(native):
     L = native.lib()
     native._lin_bind(L)
