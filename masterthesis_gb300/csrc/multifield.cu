@@ -155,11 +155,6 @@ struct LameCoefX2 {
 // An operand S + t: hi part exact, t its FP32 tail.
 struct Op { float s, t; };
 
-__device__ __forceinline__ Op op_sum(float2 a, float2 b) {
-    const f2 r = two_sum(a.x, b.x);
-    return {r.hi, r.lo + (a.y + b.y)};
-}
-
 __device__ __forceinline__ Op op_diff(float2 a, float2 b) {
     const f2 r = two_sum(a.x, -b.x);
     return {r.hi, r.lo + (a.y - b.y)};
@@ -202,15 +197,15 @@ __device__ __forceinline__ float2 pa_result(PAcc acc) {
 // Lame-Navier step on pairs: u^{n+1} = d_c u + sum_p a_cp (u(+p) + u(-p))
 // + sum_q b_cq ((u_q(+c+q) - u_q(+c-q)) - (u_q(-c+q) - u_q(-c-q))) - u^{n-1},
 // the FP64 form rearranged with the centre weight d_c = 2 - 2 sum_p a_cp.
-// The three components of u^n are staged by TMA: a CTA
-// owns an LX x LY column tile and marches LZ planes; per input plane one
-// mbarrier covers the three components' boxes with a one-node halo in x and
-// y (x from x0-2 for 16-byte alignment), in a ring of LNS planes: planes
-// z-1, z, z+1 are read from shared memory while the next LNS-3 are in
-// flight.  u^{n-1} is read and u^{n+1} written with plain coalesced
-// accesses of the node itself.  The terms come in the order of the FP64
-// kernel's.  Every wait is bounded (status word, drain,
-// return).
+// The three components of u^n are staged by TMA: a CTA owns an LX x LY
+// column tile (LX x LY/2 threads, two rows each) and marches LZ planes; per
+// input plane one mbarrier covers the three components' boxes with a
+// one-node halo in x and y (x from x0-2 for 16-byte alignment), in a ring
+// of LNS planes: planes z-1, z, z+1 are read from shared memory while the
+// next LNS-3 are in flight.  u^{n-1} is read a plane ahead and u^{n+1}
+// written with plain coalesced accesses of the nodes themselves.  The terms
+// come in the order of the FP64 kernel's.  Every wait is bounded (status
+// word, drain, return).
 constexpr int LX = 32, LY = 8, LZ = 32, LNS = 6;
 constexpr int LBW = LX + 4, LBH = LY + 2;                     // box: x0-2 .. x0+33, y0-1 .. y0+8
 constexpr int LBOX = (LBW * LBH + 15) / 16 * 16;              // float2 per box, 128-byte multiple
@@ -218,7 +213,74 @@ constexpr int LSLOT = 3 * LBOX;                               // float2 per ring
 constexpr uint32_t LTX_BYTES = (uint32_t)(3 * LBW * LBH * 8);
 constexpr size_t LAME_SMEM = (size_t)LNS * LSLOT * 8 + LNS * 8;
 
-__global__ void __launch_bounds__(LX * LY)
+// Two nodes per thread (rows y and y+1) on the paired FP32 instructions of
+// sm_100+ (FFMA2, FADD2, FMUL2): lane .x carries the first node, .y the
+// second, with exactly the operations of pa_prod / pa_add / op_sum /
+// op_diff2 / pa_result per lane (bit-identical to the one-node form) and
+// half the arithmetic instructions issued.
+struct PAcc2 { float2 H, E; };
+
+__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {  // a - b, one rounding
+    return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ float2 tsum2(float2 a, float2 b, float2& err) {
+    const float2 sm = __fadd2_rn(a, b);
+    const float2 bb = sub2(sm, a);
+    err = __fadd2_rn(sub2(a, sub2(sm, bb)), sub2(b, bb));
+    return sm;
+}
+__device__ __forceinline__ float2 hi2(float2 a, float2 b) { return make_float2(a.x, b.x); }
+__device__ __forceinline__ float2 lo2(float2 a, float2 b) { return make_float2(a.y, b.y); }
+
+// (S, t) of a + b for the two nodes' pairs (a0, a1), (b0, b1).
+__device__ __forceinline__ void op_sum2(float2 a0, float2 a1, float2 b0, float2 b1, float2& S, float2& t) {
+    float2 e;
+    S = tsum2(hi2(a0, a1), hi2(b0, b1), e);
+    t = __fadd2_rn(e, __fadd2_rn(lo2(a0, a1), lo2(b0, b1)));
+}
+// (S, t) of a - b.
+__device__ __forceinline__ void op_diff_2(float2 ah, float2 al, float2 bh, float2 bl, float2& S, float2& t) {
+    float2 e;
+    S = tsum2(ah, make_float2(-bh.x, -bh.y), e);
+    t = __fadd2_rn(e, sub2(al, bl));
+}
+// (S, t) of (a - b) - (c - d).
+__device__ __forceinline__ void op_diff2_2(float2 a0, float2 a1, float2 b0, float2 b1, float2 c0, float2 c1,
+                                           float2 d0, float2 d1, float2& S, float2& t) {
+    float2 ps, pt, qs, qt, e;
+    op_diff_2(hi2(a0, a1), lo2(a0, a1), hi2(b0, b1), lo2(b0, b1), ps, pt);
+    op_diff_2(hi2(c0, c1), lo2(c0, c1), hi2(d0, d1), lo2(d0, d1), qs, qt);
+    S = tsum2(ps, make_float2(-qs.x, -qs.y), e);
+    t = __fadd2_rn(e, sub2(pt, qt));
+}
+// acc += c * (S + t): the negated tail chain -e (exact negation of pa_prod's
+// e, its roundings being symmetric), added back as E + (r - (-e)).
+__device__ __forceinline__ void pa_prod2(PAcc2& acc, const C3& c, float2 S, float2 t) {
+    const float2 P = __fmul2_rn(bc2(c.h), S);
+    float2 ne = __ffma2_rn(bc2(-c.h), S, P);
+    ne = __ffma2_rn(bc2(-c.l), S, ne);
+    ne = __ffma2_rn(bc2(-c.h), t, ne);
+    ne = __ffma2_rn(bc2(-c.ll), S, ne);
+    float2 r;
+    acc.H = tsum2(acc.H, P, r);
+    acc.E = __fadd2_rn(acc.E, sub2(r, ne));
+}
+// acc -= v for the two nodes' pairs v0, v1.
+__device__ __forceinline__ void pa_sub2(PAcc2& acc, float2 v0, float2 v1) {
+    const float2 vh = hi2(v0, v1), vl = lo2(v0, v1);
+    float2 r;
+    acc.H = tsum2(acc.H, make_float2(-vh.x, -vh.y), r);
+    acc.E = __fadd2_rn(acc.E, sub2(r, vl));
+}
+__device__ __forceinline__ void pa_result2(const PAcc2& acc, float2& o0, float2& o1) {
+    const float2 S = __fadd2_rn(acc.H, acc.E);
+    const float2 E = sub2(acc.E, sub2(S, acc.H));
+    o0 = make_float2(S.x, E.x);
+    o1 = make_float2(S.y, E.y);
+}
+
+__global__ void __launch_bounds__(LX * LY / 2)
 k_lame_x2_tma(const __grid_constant__ CUtensorMap t0, const __grid_constant__ CUtensorMap t1,
               const __grid_constant__ CUtensorMap t2, float2* __restrict__ up, LameCoefX2 K, Layout L,
               long long comp, int* __restrict__ status) {
@@ -253,21 +315,24 @@ k_lame_x2_tma(const __grid_constant__ CUtensorMap t0, const __grid_constant__ CU
                 if (j >= 0 && j < n_in) bounded_wait(&bar[j % LNS], (uint32_t)(j / LNS) & 1u, kWaitLimitNs / 16);
         }
     };
-    const int x = x0 + tx, y = y0 + ty;
-    const bool live = x < L.nx && y < L.ny;
-    const bool colb = x == 0 || y == 0 || x == L.nx - 1 || y == L.ny - 1;
-    const int bc = (ty + 1) * LBW + tx + 2;                 // own node in a box
+    // This thread's two nodes: rows y and y+1 of column x.
+    const int x = x0 + tx, y = y0 + 2 * ty;
+    const bool live0 = x < L.nx && y < L.ny, live1 = x < L.nx && y + 1 < L.ny;
+    const bool xb = x == 0 || x == L.nx - 1;
+    const bool colb0 = xb || y == 0 || y == L.ny - 1, colb1 = xb || y + 1 == 0 || y + 1 == L.ny - 1;
+    const int bc = (2 * ty + 1) * LBW + tx + 2;             // first node in a box
     const float2 zero = make_float2(0.f, 0.f);
     bool ok = wait(0);
     ok = wait(1) && ok;
     int issued = min(LNS, n_in) - 1;
-    long long o = live ? L.idx(x, y, z0) : 0;
-    // u^{n-1} of the node one plane ahead, in registers (its loads overlap
-    // the plane before).
-    float2 pn[3] = {zero, zero, zero};
-    if (live)
+    long long o = live0 ? L.idx(x, y, z0) : 0;
+    // u^{n-1} of both nodes one plane ahead, in registers.
+    float2 pn0[3] = {zero, zero, zero}, pn1[3] = {zero, zero, zero};
 #pragma unroll
-        for (int c = 0; c < 3; ++c) pn[c] = up[o + c * comp];
+    for (int c = 0; c < 3; ++c) {
+        if (live0) pn0[c] = up[o + c * comp];
+        if (live1) pn1[c] = up[o + L.pitch + c * comp];
+    }
     for (int z = z0; z < z1; ++z, o += L.plane) {
         const int jc = z - z0 + 1;  // input plane of z
         if (!__syncthreads_and(ok)) {  // plane z-2's slot is free; all waits so far succeeded
@@ -279,52 +344,64 @@ k_lame_x2_tma(const __grid_constant__ CUtensorMap t0, const __grid_constant__ CU
             issue(jc + LNS - 2);
             issued = jc + LNS - 2;
         }
-        const float2 pc0 = pn[0], pc1 = pn[1], pc2 = pn[2];
-        if (live && z + 1 < z1)
+        float2 pc0[3], pc1[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) pn[c] = up[o + L.plane + c * comp];
-        ok = wait(jc + 1) && ok;  // plane z+1
-        if (!live) continue;
-        if (colb || z == 0 || z == L.nz - 1) {
-            up[o] = zero;
-            up[o + comp] = zero;
-            up[o + 2 * comp] = zero;
-            continue;
+        for (int c = 0; c < 3; ++c) {
+            pc0[c] = pn0[c];
+            pc1[c] = pn1[c];
         }
+        if (z + 1 < z1)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if (live0) pn0[c] = up[o + L.plane + c * comp];
+                if (live1) pn1[c] = up[o + L.plane + L.pitch + c * comp];
+            }
+        ok = wait(jc + 1) && ok;  // plane z+1
+        if (!live0) continue;
+        const bool zb = z == 0 || z == L.nz - 1;
         const float2* pb = lsm + ((jc - 1) % LNS) * LSLOT;  // plane z-1
         const float2* pc = lsm + (jc % LNS) * LSLOT;        // plane z
         const float2* pa = lsm + ((jc + 1) % LNS) * LSLOT;  // plane z+1
-        // Component q of u^n at offset (dx, dy, dz), dz in {-1, 0, 1}.
-        auto U = [&](int q, int dx, int dy, int dz) -> float2 {
+        // Component q of u^n at offset (dx, dy, dz) from node r (0, 1).
+        auto U = [&](int r, int q, int dx, int dy, int dz) -> float2 {
             const float2* pl = dz < 0 ? pb : (dz > 0 ? pa : pc);
-            return pl[q * LBOX + bc + dx + dy * LBW];
+            return pl[q * LBOX + bc + r * LBW + dx + dy * LBW];
         };
-        float2 out[3];
+        float2 out0[3], out1[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float2 uv = U(c, 0, 0, 0);
-            PAcc acc{0.f, 0.f};
-            pa_prod(acc, K.d[c], Op{uv.x, uv.y});
-            pa_add(acc, c == 0 ? pc0 : (c == 1 ? pc1 : pc2), -1.f);
+            const float2 u0 = U(0, c, 0, 0, 0), u1 = U(1, c, 0, 0, 0);
+            PAcc2 acc{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+            pa_prod2(acc, K.d[c], hi2(u0, u1), lo2(u0, u1));
+            pa_sub2(acc, pc0[c], pc1[c]);
 #pragma unroll
             for (int p = 0; p < 3; ++p) {
                 const int dx = p == 0, dy = p == 1, dz = p == 2;
-                pa_prod(acc, K.a[c][p], op_sum(U(c, dx, dy, dz), U(c, -dx, -dy, -dz)));
+                float2 S, t;
+                op_sum2(U(0, c, dx, dy, dz), U(1, c, dx, dy, dz), U(0, c, -dx, -dy, -dz), U(1, c, -dx, -dy, -dz),
+                        S, t);
+                pa_prod2(acc, K.a[c][p], S, t);
             }
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
                 if (q == c) continue;
                 // (u_q(+c+q) - u_q(+c-q)) - (u_q(-c+q) - u_q(-c-q))
                 const int cx = c == 0, cy = c == 1, cz = c == 2, qx = q == 0, qy = q == 1, qz = q == 2;
-                pa_prod(acc, K.b[c][q],
-                        op_diff2(U(q, cx + qx, cy + qy, cz + qz), U(q, cx - qx, cy - qy, cz - qz),
-                                 U(q, -cx + qx, -cy + qy, -cz + qz), U(q, -cx - qx, -cy - qy, -cz - qz)));
+                float2 S, t;
+                op_diff2_2(U(0, q, cx + qx, cy + qy, cz + qz), U(1, q, cx + qx, cy + qy, cz + qz),
+                           U(0, q, cx - qx, cy - qy, cz - qz), U(1, q, cx - qx, cy - qy, cz - qz),
+                           U(0, q, -cx + qx, -cy + qy, -cz + qz), U(1, q, -cx + qx, -cy + qy, -cz + qz),
+                           U(0, q, -cx - qx, -cy - qy, -cz - qz), U(1, q, -cx - qx, -cy - qy, -cz - qz), S, t);
+                pa_prod2(acc, K.b[c][q], S, t);
             }
-            out[c] = pa_result(acc);
+            pa_result2(acc, out0[c], out1[c]);
         }
-        up[o] = out[0];
-        up[o + comp] = out[1];
-        up[o + 2 * comp] = out[2];
+        // Border nodes (any face) are held at zero.
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            up[o + c * comp] = (colb0 || zb) ? zero : out0[c];
+            if (live1) up[o + L.pitch + c * comp] = (colb1 || zb) ? zero : out1[c];
+        }
     }
     if (!__syncthreads_and(ok)) fail(issued);
 }
@@ -842,8 +919,8 @@ extern "C" int scafes_mf_step(scafes_mf* h, int n_steps) {
             void* up = field_ptr(h, 3 * (h->cur ^ 1));
             if (x2) {
                 const CUtensorMap* t = h->ltm[h->cur];
-                k_lame_x2_tma<<<lgrid, dim3(LX, LY), LAME_SMEM, h->stream>>>(t[0], t[1], t[2], (float2*)up, K2, L,
-                                                                            comp, h->status);
+                k_lame_x2_tma<<<lgrid, dim3(LX, LY / 2), LAME_SMEM, h->stream>>>(t[0], t[1], t[2], (float2*)up, K2,
+                                                                                L, comp, h->status);
             } else {
                 k_lame<<<mgrid(L), dim3(MX, MY), 0, h->stream>>>((const double*)u, (double*)up, K, L, comp);
             }
