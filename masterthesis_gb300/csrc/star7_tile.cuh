@@ -70,9 +70,9 @@ struct TileJob {
     const CUtensorMap* tmc0 = nullptr;  // TMA descriptors of C0, CA (box 32 x BY), VC tiles only
     const CUtensorMap* tmca = nullptr;
     const scafes_border_node_rule* nodes = nullptr;  // per-node rules (SCAFES_BORDER_NODES)
-    // Per-node rules in FP64: the nodes on an x face outside the y and z
-    // border rows are left to a separate pass (k_xface_node_rules), so that
-    // no warp of an x-face tile spends the narrow FP64 pipe on one lane.
+    // Per-node rules: the nodes on an x face outside the y and z border
+    // rows are left to a separate pass (k_xface_node_rules), so that no
+    // warp of an x-face tile evaluates a rule for one lane.
     bool xface_pass = false;
 };
 

@@ -34,17 +34,23 @@ star7_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtens
     star7_tile<P, SRC, BORDER, BY, R, NS, FS, ML>(J, c, blockIdx.x * BX, blockIdx.y * BY, z0, z1, st, bar, base, status);
 }
 
-// FP64 per-node border rules leave the x-face nodes outside the y and z
-// border rows to k_xface_node_rules.
+// Per-node border rules (FP64 and FP32 sweeps) leave the x-face nodes
+// outside the y and z border rows to k_xface_node_rules: otherwise every
+// warp of an x-face tile evaluates a rule for one or two lanes (FP64
+// instructions that hold the narrow FP64 pipe; rule loads it waits for).
 template <class P, int BORDER>
-constexpr bool XFACE_PASS = std::is_same<P, PolF64>::value && BORDER == SCAFES_BORDER_NODES;
+constexpr bool XFACE_PASS =
+    (std::is_same<P, PolF64>::value || std::is_same<P, PolF32>::value) && BORDER == SCAFES_BORDER_NODES;
 
 // The per-node rules of the nodes on the two x faces outside the y and z
 // border rows (one border layer), from the old iterate: what node_rule
-// computes for them, in the same FP64 order (a neighbour outside the grid
-// reads 0, as from the TMA halo).  One thread per (face, y, z).
-static __global__ void k_xface_node_rules(const double* __restrict__ uo, double* __restrict__ un,
-                                   const scafes_border_node_rule* __restrict__ nodes, Layout L) {
+// computes for them, in the same order and arithmetic (FP64 rules for
+// double fields, the FP32 copy of the rules for float fields; a neighbour
+// outside the grid reads 0, as from the TMA halo).  One thread per
+// (face, y, z).
+template <typename T>
+static __global__ void k_xface_node_rules(const T* __restrict__ uo, T* __restrict__ un,
+                                          const scafes_border_node_rule* __restrict__ nodes, Layout L) {
     const long long rows = (long long)(L.ny - 2) * (L.nz - 2);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 2 * rows;
          i += (long long)gridDim.x * blockDim.x) {
@@ -53,16 +59,28 @@ static __global__ void k_xface_node_rules(const double* __restrict__ uo, double*
         const int y = 1 + (int)(r % (L.ny - 2)), z = 1 + (int)(r / (L.ny - 2));
         const int x = side ? L.nx - 1 : 0;
         const long long o = L.idx(x, y, z);
-        const scafes_border_node_rule& R = nodes[border_node_index(L, x, y, z)];
-        const double w = x > 0 ? uo[o - 1] : 0.0, e = x < L.nx - 1 ? uo[o + 1] : 0.0;
-        double v = fma(R.cu, uo[o], R.cst);
-        v = fma(R.cn[0], w, v);
-        v = fma(R.cn[1], e, v);
-        v = fma(R.cn[2], uo[o - L.pitch], v);
-        v = fma(R.cn[3], uo[o + L.pitch], v);
-        v = fma(R.cn[4], uo[o - L.plane], v);
-        v = fma(R.cn[5], uo[o + L.plane], v);
-        un[o] = v;
+        const T w = x > 0 ? uo[o - 1] : T(0), e = x < L.nx - 1 ? uo[o + 1] : T(0);
+        if constexpr (std::is_same<T, float>::value) {
+            const float* R = reinterpret_cast<const float*>(nodes) + 8 * border_node_index(L, x, y, z);
+            float v = fmaf(R[0], uo[o], R[7]);
+            v = fmaf(R[1], w, v);
+            v = fmaf(R[2], e, v);
+            v = fmaf(R[3], uo[o - L.pitch], v);
+            v = fmaf(R[4], uo[o + L.pitch], v);
+            v = fmaf(R[5], uo[o - L.plane], v);
+            v = fmaf(R[6], uo[o + L.plane], v);
+            un[o] = v;
+        } else {
+            const scafes_border_node_rule& R = nodes[border_node_index(L, x, y, z)];
+            double v = fma(R.cu, uo[o], R.cst);
+            v = fma(R.cn[0], w, v);
+            v = fma(R.cn[1], e, v);
+            v = fma(R.cn[2], uo[o - L.pitch], v);
+            v = fma(R.cn[3], uo[o + L.pitch], v);
+            v = fma(R.cn[4], uo[o - L.plane], v);
+            v = fma(R.cn[5], uo[o + L.plane], v);
+            un[o] = v;
+        }
     }
 }
 
@@ -209,7 +227,7 @@ static cudaError_t launch_vc_typed(const Star7Launch& a, cudaStream_t stream) {
         if (e != cudaSuccess) return e;
         const long long work = 2LL * (L.ny - 2) * (L.nz - 2);
         const int blocks = (int)std::min<long long>((work + 255) / 256, (long long)num_sms() * 8);
-        k_xface_node_rules<<<blocks, 256, 0, stream>>>((const double*)a.uo, (double*)a.un, a.nodes, L);
+        k_xface_node_rules<T><<<blocks, 256, 0, stream>>>((const T*)a.uo, (T*)a.un, a.nodes, L);
     }
     return cudaGetLastError();
 }
