@@ -287,3 +287,27 @@ def test_recorded_rules_reproduce_reference_run_on_cpu(run_problem, tmp_path, go
             assert np.all(got[f] == 0.0), f
         else:
             assert cases.rel_err(got[f], ref[f]) <= 1e-12, f
+
+
+@pytest.mark.gpu
+def test_linear_smallest_grid_and_most_fields(gpu):
+    """A 3 x 3 x 3 grid (one inner node; corner, edge and face classes) with
+    SCAFES_LIN_MAX_FIELDS fields: each field takes the rule
+    u' = 2u + 0.5 * (next field at the same node) on every class, checked
+    against numpy after 3 steps, bit for bit."""
+    M = gpu
+    n, nf = (3, 3, 3), M.LIN_MAX_FIELDS
+    rng = np.random.default_rng(12)
+    f0 = rng.uniform(-1.0, 1.0, (nf, 3, 3, 3))
+    with M.Linear(n, nf, 1) as lin:
+        for f in range(nf):
+            for c in range(64):
+                lin.set_rule(1, f, c, [(f, 0, 0, 0, 2.0), ((f + 1) % nf, 0, 0, 0, 0.5)])
+            lin.upload(f, f0[f])
+        lin.step(3)
+        got = np.stack([lin.download(f) for f in range(nf)])
+    # 2u and 0.5v are exact, so the kernel's FMA and numpy's sum round alike.
+    want = f0.copy()
+    for _ in range(3):
+        want = np.stack([2.0 * want[f] + 0.5 * want[(f + 1) % nf] for f in range(nf)])
+    assert np.array_equal(got, want)
