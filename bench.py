@@ -270,7 +270,7 @@ def cpu_section_baselines(args) -> dict:
     host threads), each timed on a bounded sample of its workload:
     batched -- the first 16 ensemble instances x 50 steps; adjoint -- the
     forward solve and the adjoint at 64^3 x 200 steps (every state stored);
-    Lame 192^3 x 40 steps; Yee 256^3 x 80 steps; tissue 192^3 x 20 steps."""
+    Lame 192^3 x 40 steps; Yee 256^3 x 80 steps; tissue 256^3 x 40 steps."""
     import oracle as O
     from masterthesis_gb300 import workloads as W
     threads = os.cpu_count() or 1
@@ -323,7 +323,7 @@ def cpu_section_baselines(args) -> dict:
     out["yee_f64"] = {"value": 256 ** 3 * T / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
                       "sample": f"256^3 x {T} steps ({dt:.1f} s)"}
     # Tissue (the MRI-data example's update with per-node coefficients).
-    m, T = 192, 20
+    m, T = 256, 40
     nn = (m, m, m)
     f = W.tissue_fields_slab(nn, 0, m, 31)
     g = O.make_grid(nn, last=TISSUE_LAST, tau=W.tissue_tau(nn, TISSUE_LAST))
