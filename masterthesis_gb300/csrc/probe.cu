@@ -4,6 +4,7 @@
 // benchmark reports that bound beside the HBM one.
 #include <cuda_runtime.h>
 
+#include "dadd_int.cuh"
 #include "tma.cuh"
 #include "../../include/scafes_gb300.h"
 
@@ -52,7 +53,41 @@ __global__ void k_wait_probe(unsigned long long limit_ns, int* status, unsigned 
     }
 }
 
+// The integer-pipe addition of the FP64 sweep, element by element.
+__global__ void k_dadd_int(const uint64_t* a, const uint64_t* b, uint64_t* sum, unsigned char* ok, long long n) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
+        bool o;
+        sum[i] = scafes::dadd_same_sign_bits(a[i], b[i], o);
+        ok[i] = o ? 1 : 0;
+    }
+}
+
 }  // namespace
+
+// No counterpart in the reference: runs the integer-pipe binary64 addition
+// of the FP64 sweep on the device for n pairs of bit patterns (host arrays,
+// 1 <= n <= 2^26), for a check against the FP64 adder.  sum[i] is defined
+// where ok[i] is 1.
+extern "C" int scafes_probe_dadd_int(const unsigned long long* a, const unsigned long long* b,
+                                     unsigned long long* sum, unsigned char* ok, long long n) {
+    if (!a || !b || !sum || !ok || n < 1 || n > (1ll << 26)) return SCAFES_ERR_ARG;
+    const size_t bytes = sizeof(uint64_t) * (size_t)n;
+    uint64_t* d = nullptr;
+    if (cudaMalloc(&d, 3 * bytes + (size_t)n) != cudaSuccess) return SCAFES_ERR_NOMEM;
+    unsigned char* d_ok = reinterpret_cast<unsigned char*>(d + 3 * n);
+    cudaError_t e = cudaMemcpy(d, a, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, b, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        const long long blocks = (n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096;
+        k_dadd_int<<<(unsigned)blocks, 256>>>(d, d + n, d + 2 * n, d_ok, n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(sum, d + 2 * n, bytes, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(ok, d_ok, (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? SCAFES_OK : SCAFES_ERR_CUDA;
+}
 
 // No counterpart in the reference: exercises the timeout path of the
 // bounded device waits without any fault (no load is ever issued; the

@@ -4,6 +4,7 @@
 // and the batched ensemble kernels.
 #pragma once
 
+#include "dadd_int.cuh"
 #include "star7.cuh"
 
 namespace scafes {
@@ -12,18 +13,58 @@ namespace scafes {
 
 struct PolF64 {
     using T = double;
+    // How many of the three neighbour sums (w+e, s+n, b+t) of the star are
+    // added on the integer pipe (dadd_int.cuh, the FP64 adder's exact bits)
+    // instead of the FP64 pipe, which bounds the FP64 sweep.  A warp with a
+    // lane outside the integer adder's range adds all its sums in FP64.
+    static constexpr int kIntSums = 3;
     static __device__ __forceinline__ T zero() { return 0.0; }
     static __device__ __forceinline__ T from_double(double d) { return d; }
     static __device__ __forceinline__ double to_double(T v) { return v; }
+    static __device__ __forceinline__ double int_sum(double a, double b, bool& ok) {
+        bool o;
+        const uint64_t r = dadd_same_sign_bits((uint64_t)__double_as_longlong(a),
+                                               (uint64_t)__double_as_longlong(b), o);
+        ok = ok && o;
+        return __longlong_as_double((long long)r);
+    }
+    // The three sums of R nodes; sx/sy/sz[k] = w+e, s+n, b+t of node k.
+    template <int R>
+    static __device__ __forceinline__ void sums(const T (&w)[R], const T (&e)[R], const T (&s)[R], const T (&n)[R],
+                                                const T (&b)[R], const T (&t)[R], T (&sx)[R], T (&sy)[R],
+                                                T (&sz)[R]) {
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            sx[k] = kIntSums >= 3 ? int_sum(w[k], e[k], ok) : w[k] + e[k];
+            sy[k] = kIntSums >= 2 ? int_sum(s[k], n[k], ok) : s[k] + n[k];
+            sz[k] = kIntSums >= 1 ? int_sum(b[k], t[k], ok) : b[k] + t[k];
+        }
+        if (kIntSums > 0 && __any_sync(__activemask(), !ok)) {
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                sx[k] = w[k] + e[k];
+                sy[k] = s[k] + n[k];
+                sz[k] = b[k] + t[k];
+            }
+        }
+    }
+    template <bool HAS_F>
+    static __device__ __forceinline__ T star_of_sums(const Star7Coeffs& c, T u, T sx, T sy, T sz, T f) {
+        double v = c.c0 * u;
+        v = fma(c.cx, sx, v);
+        v = fma(c.cy, sy, v);
+        v = fma(c.cz, sz, v);
+        if (HAS_F) v = fma(c.cf, f, v);
+        return v;
+    }
     template <bool HAS_F>
     static __device__ __forceinline__ T star(const Star7Coeffs& c, T u, T w, T e,
                                              T s, T n, T b, T t, T f) {
-        double v = c.c0 * u;
-        v = fma(c.cx, w + e, v);
-        v = fma(c.cy, s + n, v);
-        v = fma(c.cz, b + t, v);
-        if (HAS_F) v = fma(c.cf, f, v);
-        return v;
+        T sx[1], sy[1], sz[1];
+        const T w1[1] = {w}, e1[1] = {e}, s1[1] = {s}, n1[1] = {n}, b1[1] = {b}, t1[1] = {t};
+        sums<1>(w1, e1, s1, n1, b1, t1, sx, sy, sz);
+        return star_of_sums<HAS_F>(c, u, sx[0], sy[0], sz[0], f);
     }
     static __device__ __forceinline__ T mirror(T u, T uo, const Split& corr) {
         return (u + uo) - corr.d;
@@ -50,10 +91,15 @@ struct PolF64 {
     static __device__ __forceinline__ void star_rows(const Star7Coeffs& c, const T (&below)[R], const T (&cur)[R],
                                                      const T (&above)[R], T ym, T yp, const T (&w)[R],
                                                      const T (&e)[R], const T (&f)[R], T (&v)[R]) {
+        T s[R], n[R], sx[R], sy[R], sz[R];
 #pragma unroll
-        for (int k = 0; k < R; ++k)
-            v[k] = star<HAS_F>(c, cur[k], w[k], e[k], k == 0 ? ym : cur[k - 1], k == R - 1 ? yp : cur[k + 1],
-                               below[k], above[k], f[k]);
+        for (int k = 0; k < R; ++k) {
+            s[k] = k == 0 ? ym : cur[k - 1];
+            n[k] = k == R - 1 ? yp : cur[k + 1];
+        }
+        sums<R>(w, e, s, n, below, above, sx, sy, sz);
+#pragma unroll
+        for (int k = 0; k < R; ++k) v[k] = star_of_sums<HAS_F>(c, cur[k], sx[k], sy[k], sz[k], f[k]);
     }
 };
 
