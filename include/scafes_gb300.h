@@ -670,10 +670,10 @@ void scafes_host_free(void* p);
 int scafes_probe_pipe_rates(double* fp64_gops, double* fp32_gops);
 
 /* No counterpart in the reference: runs the FP64 sweep's integer-pipe
- * binary64 addition (both operands normal and of one sign, exponents at
- * most 10 apart, the larger exponent field at most 2045; round to nearest
- * even) on the device for n
- * pairs of bit patterns a[i], b[i] (host arrays, 1 <= n <= 2^26).  ok[i] = 1
+ * binary64 addition (both operands of one sign, exponents at most 10
+ * apart, the smaller exponent field in [1, 2035]; round to nearest even)
+ * on the device for n pairs of bit patterns a[i], b[i] (host arrays,
+ * 1 <= n <= 2^26).  ok[i] = 1
  * where the pair lies in that range, and then sum[i] holds the bits of
  * a[i] + b[i]; elsewhere the sweep adds in FP64 and sum[i] is undefined. */
 int scafes_probe_dadd_int(const unsigned long long* a, const unsigned long long* b, unsigned long long* sum,

@@ -5,11 +5,12 @@
 // integer pipe idles.  dadd_same_sign_bits computes a + b, rounded to
 // nearest even exactly as the FP64 adder does (the same bits), from the
 // operands' bit patterns with integer instructions only.  It covers the case
-// that dominates the neighbour sums of a smooth field -- both operands
-// normal, of one sign, exponents at most 10 apart, the larger exponent field
-// at most 2045 -- and reports every other case (zeros, subnormals,
-// infinities, NaNs, opposite signs, distant exponents, results near the
-// overflow threshold) through `ok`, for the caller to add in FP64 instead.
+// that dominates the neighbour sums of a smooth field -- both operands of
+// one sign, exponents at most 10 apart, the smaller exponent field in
+// [1, 2035] (magnitudes from 2^-1022 to about 2^1013) -- and reports every
+// other case (zeros, subnormals, infinities, NaNs, opposite signs, distant
+// exponents, huge magnitudes) through `ok`, for the caller to add in FP64
+// instead.
 //
 // Method (textbook IEEE addition with guard bits): order the operands by
 // magnitude, place the larger significand (hidden bit included) at bits
@@ -38,11 +39,22 @@ SCAFES_HD uint64_t dadd_same_sign_bits(uint64_t a, uint64_t b, bool& ok) {
     const bool a_big = ah >= bh;
     const uint32_t hh = a_big ? ah : bh, hl = a_big ? al : bl;
     const uint32_t lh = a_big ? bh : ah, ll = a_big ? bl : al;
-    const uint32_t d = (hh >> 20) - (lh >> 20);  // the sign bits cancel
-    ok = (int32_t)(ah ^ bh) >= 0 && (lh & 0x7ff00000u) != 0 && (hh & 0x7fffffffu) < 0x7fe00000u && d <= 10u;
-    const uint64_t ma = ((uint64_t)((hh & 0x000fffffu) | 0x00100000u) << 32 | hl) << 10;
-    const uint64_t mb = ((uint64_t)((lh & 0x000fffffu) | 0x00100000u) << 32 | ll) << ((10u - d) & 31u);
-    uint64_t s = ma + mb;  // exact, below 2^64
+    const uint32_t d = (hh >> 20) - (lh >> 20);  // the exponent difference when the signs agree
+    // The smaller exponent in [1, 2035] and d <= 10.  With opposite signs d
+    // is 2048 + ea - eb, which is above 10 for any eb <= 2035, so the range
+    // test covers the sign test; the larger exponent is at most 2045.
+    ok = d <= 10u && (lh & 0x7fffffffu) - 0x00100000u < 0x7f300000u;
+    const uint32_t mah = (hh & 0x000fffffu) | 0x00100000u;
+    const uint32_t mbh = (lh & 0x000fffffu) | 0x00100000u;
+    uint32_t pb = 1u << ((10u - d) & 31u);
+#if defined(__CUDA_ARCH__)
+    // Keeps the alignment a multiply by 2^(10-d) (the FMA pipe) rather than
+    // a shift (the integer ALU, which the adder keeps busier).
+    asm("" : "+r"(pb));
+#endif
+    // ma * 2^10 + mb * 2^(10-d): exact, below 2^64.
+    uint64_t s = (uint64_t)hl * 1024u + (uint64_t)ll * pb;
+    s += (uint64_t)(mah * 1024u + mbh * pb) << 32;
     const uint32_t c = (uint32_t)(s >> 63);
     const uint32_t sh = 10u + c;
     // + (half - 1) + the last kept bit: rounds half to even.

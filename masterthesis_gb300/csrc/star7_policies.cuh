@@ -13,41 +13,63 @@ namespace scafes {
 
 struct PolF64 {
     using T = double;
-    // How many of the three neighbour sums (w+e, s+n, b+t) of the star are
-    // added on the integer pipe (dadd_int.cuh, the FP64 adder's exact bits)
-    // instead of the FP64 pipe, which bounds the FP64 sweep.  A warp with a
-    // lane outside the integer adder's range adds all its sums in FP64.
-    static constexpr int kIntSums = 3;
     static __device__ __forceinline__ T zero() { return 0.0; }
     static __device__ __forceinline__ T from_double(double d) { return d; }
     static __device__ __forceinline__ double to_double(T v) { return v; }
-    static __device__ __forceinline__ double int_sum(double a, double b, bool& ok) {
+    static __device__ __forceinline__ double int_sum(double a, double b, bool& ok, bool skip) {
         bool o;
         const uint64_t r = dadd_same_sign_bits((uint64_t)__double_as_longlong(a),
                                                (uint64_t)__double_as_longlong(b), o);
-        ok = ok && o;
+        ok = ok && (o || skip);
         return __longlong_as_double((long long)r);
     }
-    // The three sums of R nodes; sx/sy/sz[k] = w+e, s+n, b+t of node k.
+    // The three neighbour sums of R nodes, sx/sy/sz[k] = w+e, s+n, b+t of
+    // node k, added on the integer pipe (dadd_int.cuh: the FP64 adder's
+    // exact bits) instead of the FP64 pipe, which bounds the FP64 sweep.  A
+    // warp with a lane outside the integer adder's range (a zero border
+    // value, opposite signs) adds that axis's sums in FP64, in a call: a
+    // predicated FP64 add inline would hold the FP64 pipe in every warp.
+    // Bit k of `skip` marks row k's result as replaced (a border rule, or
+    // not stored): its sums do not call for the FP64 adds.
     template <int R>
     static __device__ __forceinline__ void sums(const T (&w)[R], const T (&e)[R], const T (&s)[R], const T (&n)[R],
                                                 const T (&b)[R], const T (&t)[R], T (&sx)[R], T (&sy)[R],
-                                                T (&sz)[R]) {
-        bool ok = true;
+                                                T (&sz)[R], unsigned skip) {
+        bool okx = true, oky = true, okz = true;
 #pragma unroll
         for (int k = 0; k < R; ++k) {
-            sx[k] = kIntSums >= 3 ? int_sum(w[k], e[k], ok) : w[k] + e[k];
-            sy[k] = kIntSums >= 2 ? int_sum(s[k], n[k], ok) : s[k] + n[k];
-            sz[k] = kIntSums >= 1 ? int_sum(b[k], t[k], ok) : b[k] + t[k];
+            const bool sk = (skip >> k) & 1u;
+            sx[k] = int_sum(w[k], e[k], okx, sk);
+            sy[k] = int_sum(s[k], n[k], oky, sk);
+            sz[k] = int_sum(b[k], t[k], okz, sk);
         }
-        if (kIntSums > 0 && __any_sync(__activemask(), !ok)) {
+        const unsigned lanes = __activemask();
+        if (__any_sync(lanes, !okx)) fp64_sums<R>(w, e, sx);
+        if (__any_sync(lanes, !oky)) fp64_sums<R>(s, n, sy);
+        if (__any_sync(lanes, !okz)) fp64_sums<R>(b, t, sz);
+    }
+    template <int R>
+    struct Nodes {
+        double v[R];
+    };
+    template <int R>
+    static __device__ __noinline__ Nodes<R> fp64_add(Nodes<R> a, Nodes<R> b) {
+        Nodes<R> r;
 #pragma unroll
-            for (int k = 0; k < R; ++k) {
-                sx[k] = w[k] + e[k];
-                sy[k] = s[k] + n[k];
-                sz[k] = b[k] + t[k];
-            }
+        for (int k = 0; k < R; ++k) r.v[k] = a.v[k] + b.v[k];
+        return r;
+    }
+    template <int R>
+    static __device__ __forceinline__ void fp64_sums(const T (&a)[R], const T (&b)[R], T (&out)[R]) {
+        Nodes<R> x, y;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            x.v[k] = a[k];
+            y.v[k] = b[k];
         }
+        const Nodes<R> r = fp64_add<R>(x, y);
+#pragma unroll
+        for (int k = 0; k < R; ++k) out[k] = r.v[k];
     }
     template <bool HAS_F>
     static __device__ __forceinline__ T star_of_sums(const Star7Coeffs& c, T u, T sx, T sy, T sz, T f) {
@@ -63,7 +85,7 @@ struct PolF64 {
                                              T s, T n, T b, T t, T f) {
         T sx[1], sy[1], sz[1];
         const T w1[1] = {w}, e1[1] = {e}, s1[1] = {s}, n1[1] = {n}, b1[1] = {b}, t1[1] = {t};
-        sums<1>(w1, e1, s1, n1, b1, t1, sx, sy, sz);
+        sums<1>(w1, e1, s1, n1, b1, t1, sx, sy, sz, 0u);
         return star_of_sums<HAS_F>(c, u, sx[0], sy[0], sz[0], f);
     }
     static __device__ __forceinline__ T mirror(T u, T uo, const Split& corr) {
@@ -86,18 +108,20 @@ struct PolF64 {
         return fma(cax, l, v);
     }
     // All R rows of one thread (row k's s/n neighbours are rows k-1/k+1,
-    // ym/yp beyond the ends).
+    // ym/yp beyond the ends).  Bit k of `skip`: row k's result is replaced
+    // by the caller.
     template <bool HAS_F, int R>
     static __device__ __forceinline__ void star_rows(const Star7Coeffs& c, const T (&below)[R], const T (&cur)[R],
                                                      const T (&above)[R], T ym, T yp, const T (&w)[R],
-                                                     const T (&e)[R], const T (&f)[R], T (&v)[R]) {
+                                                     const T (&e)[R], const T (&f)[R], T (&v)[R],
+                                                     unsigned skip = 0u) {
         T s[R], n[R], sx[R], sy[R], sz[R];
 #pragma unroll
         for (int k = 0; k < R; ++k) {
             s[k] = k == 0 ? ym : cur[k - 1];
             n[k] = k == R - 1 ? yp : cur[k + 1];
         }
-        sums<R>(w, e, s, n, below, above, sx, sy, sz);
+        sums<R>(w, e, s, n, below, above, sx, sy, sz, skip);
 #pragma unroll
         for (int k = 0; k < R; ++k) v[k] = star_of_sums<HAS_F>(c, cur[k], sx[k], sy[k], sz[k], f[k]);
     }
@@ -138,7 +162,8 @@ struct PolF32 {
     template <bool HAS_F, int R>
     static __device__ __forceinline__ void star_rows(const Star7Coeffs& c, const T (&below)[R], const T (&cur)[R],
                                                      const T (&above)[R], T ym, T yp, const T (&w)[R],
-                                                     const T (&e)[R], const T (&f)[R], T (&v)[R]) {
+                                                     const T (&e)[R], const T (&f)[R], T (&v)[R],
+                                                     unsigned skip = 0u) {
 #pragma unroll
         for (int k = 0; k < R; ++k)
             v[k] = star<HAS_F>(c, cur[k], w[k], e[k], k == 0 ? ym : cur[k - 1], k == R - 1 ? yp : cur[k + 1],
@@ -296,7 +321,8 @@ struct PolF32x2 {
     template <bool HAS_F, int R>
     static __device__ __forceinline__ void star_rows(const Star7Coeffs& c, const T (&below)[R], const T (&cur)[R],
                                                      const T (&above)[R], T ym, T yp, const T (&w)[R],
-                                                     const T (&e)[R], const T (&f)[R], T (&v)[R]) {
+                                                     const T (&e)[R], const T (&f)[R], T (&v)[R],
+                                                     unsigned skip = 0u) {
 #pragma unroll
         for (int k = 0; k + 1 < R; k += 2) {
             const T s0 = k == 0 ? ym : cur[k - 1];

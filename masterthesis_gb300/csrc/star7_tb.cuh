@@ -195,7 +195,13 @@ star7_tb2(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
                 if (HAS_F && l1_in && x < L.nx && yb + k < L.ny) f[k] = fa[(long long)l1 * L.plane + oo + (long long)k * L.pitch];
             }
             const T ym = pc[ob - BW], yp = pc[ob + R * BW];
-            P::template star_rows<HAS_F, R>(c, qb, qc, qa, ym, yp, w, e, f, v);
+            unsigned skip = 0u;  // rows the border rule replaces
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const int y = yb + k;
+                if (!l1_in || l1_zb || x <= 0 || x >= L.nx - 1 || y <= 0 || y >= L.ny - 1) skip |= 1u << k;
+            }
+            P::template star_rows<HAS_F, R>(c, qb, qc, qa, ym, yp, w, e, f, v, skip);
             if (!inner_xy || l1_zb || !l1_in) {
 #pragma unroll
                 for (int k = 0; k < R; ++k) {
@@ -250,7 +256,13 @@ star7_tb2(const __grid_constant__ CUtensorMap tm, typename P::T* __restrict__ un
                 if (HAS_F && x < L.nx && yb + k < L.ny) f[k] = fa[(long long)l2 * L.plane + oo + (long long)k * L.pitch];
             }
             const T ym = r1[ou - TB_U1W], yp = r1[ou + R * TB_U1W];
-            P::template star_rows<HAS_F, R>(c, ub, uc, ua, ym, yp, w, e, f, v);
+            unsigned skip = 0u;  // rows the border rule replaces
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                const int y = yb + k;
+                if (l2_zb || x <= 0 || x >= L.nx - 1 || y <= 0 || y >= L.ny - 1) skip |= 1u << k;
+            }
+            P::template star_rows<HAS_F, R>(c, ub, uc, ua, ym, yp, w, e, f, v, skip);
 #pragma unroll
             for (int k = 0; k < R; ++k) {
                 const int y = yb + k;

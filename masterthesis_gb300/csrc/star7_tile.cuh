@@ -282,7 +282,17 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                                                       k == R - 1 ? yp : cur[k + 1], below[k], above[k], f[k],
                                                       c0b[k * BX], cab[k * BX]);
             } else {
-                P::template star_rows<HAS_F, R>(c, below, cur, above, ym, yp, w, e, f, v);
+                // Rows whose result the border rule replaces (or that are
+                // not stored) set their bit in `skip`.
+                unsigned skip = 0u;
+                if constexpr (!INNER) {
+#pragma unroll
+                    for (int k = 0; k < R; ++k) {
+                        const int y = yb + k;
+                        if (!xin || y >= L.ny || xb || y < nl || y > L.ny - 1 - nl) skip |= 1u << k;
+                    }
+                }
+                P::template star_rows<HAS_F, R>(c, below, cur, above, ym, yp, w, e, f, v, skip);
             }
 #pragma unroll
             for (int k = 0; k < R; ++k) {

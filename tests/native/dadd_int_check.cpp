@@ -81,6 +81,17 @@ int main(int argc, char** argv) {
         make((int)(i % 5), a, b);
         bool ok;
         const uint64_t r = scafes::dadd_same_sign_bits(a, b, ok);
+        // The documented range: one sign, exponents at most 10 apart, the
+        // smaller one in [1, 2035].
+        const uint64_t ea = (a >> 52) & 0x7ff, eb = (b >> 52) & 0x7ff;
+        const uint64_t lo = ea < eb ? ea : eb, hi = ea < eb ? eb : ea;
+        const bool in_range = (a >> 63) == (b >> 63) && lo >= 1 && lo <= 2035 && hi - lo <= 10;
+        if (ok != in_range) {
+            if (bad < 8)
+                printf("range a=%016llx b=%016llx ok=%d\n", (unsigned long long)a, (unsigned long long)b, (int)ok);
+            ++bad;
+            continue;
+        }
         if (!ok) continue;
         ++fast;
         double x, y;

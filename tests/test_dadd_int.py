@@ -105,7 +105,7 @@ def test_integer_adder_matches_fp64_adder_on_device(gpu, seed):
     eb = (b >> np.uint64(52)) & np.uint64(0x7FF)
     big, small = np.maximum(ea, eb), np.minimum(ea, eb)
     same = (a >> np.uint64(63)) == (b >> np.uint64(63))
-    expect_ok = same & (small != 0) & (big <= 2045) & (big - small <= 10)
+    expect_ok = same & (small >= 1) & (small <= 2035) & (big - small <= 10)
     assert np.array_equal(ok.astype(bool), expect_ok)
     with np.errstate(over="ignore", invalid="ignore"):
         want = (a.view(np.float64) + b.view(np.float64)).view(np.uint64)
