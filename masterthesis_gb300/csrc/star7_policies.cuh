@@ -97,15 +97,42 @@ struct PolF64 {
 
     // Variable coefficients: c0x * u + cax * (cx (w+e) + cy (s+n) + cz (b+t))
     // + f, with the node's own C0 and CA and the source with weight 1
-    // (8 FP64 operations).
+    // (8 FP64 operations, the three sums on the integer pipe as in sums()).
+    template <bool HAS_F>
+    static __device__ __forceinline__ T star_vc_of_sums(const Star7Coeffs& c, T u, T sx, T sy, T sz, T f, T c0x,
+                                                        T cax) {
+        double l = c.cx * sx;
+        l = fma(c.cy, sy, l);
+        l = fma(c.cz, sz, l);
+        const double v = HAS_F ? fma(c0x, u, f) : c0x * u;
+        return fma(cax, l, v);
+    }
     template <bool HAS_F>
     static __device__ __forceinline__ T star_vc(const Star7Coeffs& c, T u, T w, T e, T s, T n, T b, T t, T f,
                                                 T c0x, T cax) {
-        double l = c.cx * (w + e);
-        l = fma(c.cy, s + n, l);
-        l = fma(c.cz, b + t, l);
-        const double v = HAS_F ? fma(c0x, u, f) : c0x * u;
-        return fma(cax, l, v);
+        T sx[1], sy[1], sz[1];
+        const T w1[1] = {w}, e1[1] = {e}, s1[1] = {s}, n1[1] = {n}, b1[1] = {b}, t1[1] = {t};
+        sums<1>(w1, e1, s1, n1, b1, t1, sx, sy, sz, 0u);
+        return star_vc_of_sums<HAS_F>(c, u, sx[0], sy[0], sz[0], f, c0x, cax);
+    }
+    // All R rows of one thread with the coefficients c0[k * stride],
+    // ca[k * stride] of row k; `skip` as for star_rows.
+    template <bool HAS_F, int R>
+    static __device__ __forceinline__ void star_vc_rows(const Star7Coeffs& c, const T (&below)[R],
+                                                        const T (&cur)[R], const T (&above)[R], T ym, T yp,
+                                                        const T (&w)[R], const T (&e)[R], const T (&f)[R],
+                                                        const T* c0, const T* ca, int stride, T (&v)[R],
+                                                        unsigned skip) {
+        T s[R], n[R], sx[R], sy[R], sz[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            s[k] = k == 0 ? ym : cur[k - 1];
+            n[k] = k == R - 1 ? yp : cur[k + 1];
+        }
+        sums<R>(w, e, s, n, below, above, sx, sy, sz, skip);
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+            v[k] = star_vc_of_sums<HAS_F>(c, cur[k], sx[k], sy[k], sz[k], f[k], c0[k * stride], ca[k * stride]);
     }
     // All R rows of one thread (row k's s/n neighbours are rows k-1/k+1,
     // ym/yp beyond the ends).  Bit k of `skip`: row k's result is replaced
@@ -156,6 +183,17 @@ struct PolF32 {
         l = fmaf(c.czh, b + t, l);
         const float v = HAS_F ? fmaf(c0x, u, f) : c0x * u;
         return fmaf(cax, l, v);
+    }
+    template <bool HAS_F, int R>
+    static __device__ __forceinline__ void star_vc_rows(const Star7Coeffs& c, const T (&below)[R],
+                                                        const T (&cur)[R], const T (&above)[R], T ym, T yp,
+                                                        const T (&w)[R], const T (&e)[R], const T (&f)[R],
+                                                        const T* c0, const T* ca, int stride, T (&v)[R],
+                                                        unsigned) {
+#pragma unroll
+        for (int k = 0; k < R; ++k)
+            v[k] = star_vc<HAS_F>(c, cur[k], w[k], e[k], k == 0 ? ym : cur[k - 1], k == R - 1 ? yp : cur[k + 1],
+                                  below[k], above[k], f[k], c0[k * stride], ca[k * stride]);
     }
     // All R rows of one thread (row k's s/n neighbours are rows k-1/k+1,
     // ym/yp beyond the ends).

@@ -273,25 +273,21 @@ __device__ __forceinline__ bool star7_tile(const TileJob<typename P::T>& J, cons
                 else if (HAS_F && live)
                     f[k] = P::src(J.fa[off], has_fb ? J.fb[off] : P::zero(), J.time_old, has_fb);
             }
+            // Rows whose result the border rule replaces (or that are not
+            // stored) set their bit in `skip`.
+            unsigned skip = 0u;
+            if constexpr (!INNER) {
+#pragma unroll
+                for (int k = 0; k < R; ++k) {
+                    const int y = yb + k;
+                    if (!xin || y >= L.ny || xb || y < nl || y > L.ny - 1 - nl) skip |= 1u << k;
+                }
+            }
             if constexpr (VC) {
                 const T* c0b = st + slot(p) * G::STRIDE + G::C0OFF + ty * R * BX + tx;
                 const T* cab = st + slot(p) * G::STRIDE + G::CAOFF + ty * R * BX + tx;
-#pragma unroll
-                for (int k = 0; k < R; ++k)
-                    v[k] = P::template star_vc<HAS_F>(c, cur[k], w[k], e[k], k == 0 ? ym : cur[k - 1],
-                                                      k == R - 1 ? yp : cur[k + 1], below[k], above[k], f[k],
-                                                      c0b[k * BX], cab[k * BX]);
+                P::template star_vc_rows<HAS_F, R>(c, below, cur, above, ym, yp, w, e, f, c0b, cab, BX, v, skip);
             } else {
-                // Rows whose result the border rule replaces (or that are
-                // not stored) set their bit in `skip`.
-                unsigned skip = 0u;
-                if constexpr (!INNER) {
-#pragma unroll
-                    for (int k = 0; k < R; ++k) {
-                        const int y = yb + k;
-                        if (!xin || y >= L.ny || xb || y < nl || y > L.ny - 1 - nl) skip |= 1u << k;
-                    }
-                }
                 P::template star_rows<HAS_F, R>(c, below, cur, above, ym, yp, w, e, f, v, skip);
             }
 #pragma unroll

@@ -24,3 +24,23 @@ void star7_sweep_f64(const double* u, double* out, int nx, int ny, int nz, doubl
                 out[o] = v;
             }
 }
+
+/* The variable-coefficient sweep's order (per-node C0 and CA, no source):
+ *   l = cx*(w+e);  l = fma(cy, s+n, l);  l = fma(cz, b+t, l);  v = fma(ca, l, c0*u) */
+void star7_vc_sweep_f64(const double* u, const double* c0f, const double* caf, double* out, int nx, int ny,
+                        int nz, double cx, double cy, double cz, double border) {
+    const long long px = 1, py = nx, pz = (long long)nx * ny;
+    for (int z = 0; z < nz; ++z)
+        for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x) {
+                const long long o = x * px + y * py + z * pz;
+                if (x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1) {
+                    out[o] = border;
+                    continue;
+                }
+                double l = cx * (u[o - px] + u[o + px]);
+                l = fma(cy, u[o - py] + u[o + py], l);
+                l = fma(cz, u[o - pz] + u[o + pz], l);
+                out[o] = fma(caf[o], l, c0f[o] * u[o]);
+            }
+}

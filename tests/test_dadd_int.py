@@ -121,6 +121,7 @@ def star_model(tmp_path_factory):
     lib = C.CDLL(str(so))
     dp = C.POINTER(C.c_double)
     lib.star7_sweep_f64.argtypes = [dp, dp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 5
+    lib.star7_vc_sweep_f64.argtypes = [dp, dp, dp, dp, C.c_int, C.c_int, C.c_int] + [C.c_double] * 4
     return lib
 
 
@@ -130,6 +131,16 @@ def _model_step(lib, u, coeffs, border=0.0):
     out = np.empty_like(u)
     dp = C.POINTER(C.c_double)
     lib.star7_sweep_f64(u.ctypes.data_as(dp), out.ctypes.data_as(dp), nx, ny, nz, *coeffs, border)
+    return out
+
+
+def _model_vc_step(lib, u, c0f, caf, cp, border=0.0):
+    nz, ny, nx = u.shape
+    u = np.ascontiguousarray(u)
+    out = np.empty_like(u)
+    dp = C.POINTER(C.c_double)
+    lib.star7_vc_sweep_f64(u.ctypes.data_as(dp), c0f.ctypes.data_as(dp), caf.ctypes.data_as(dp),
+                           out.ctypes.data_as(dp), nx, ny, nz, *cp, border)
     return out
 
 
@@ -194,3 +205,30 @@ def test_f64_depth2_sweep_bitwise_equals_operation_order_model(gpu, star_model, 
     for _ in range(4):
         u = _model_step(star_model, u, coeffs)
     assert np.array_equal(got.view(np.uint64), u.view(np.uint64)), kind
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["smooth", "signed", "wide"])
+@pytest.mark.parametrize("tile", [1, 2, 3, 4])
+def test_f64_variable_coefficient_sweep_bitwise_equals_model(gpu, star_model, kind, tile):
+    """The variable-coefficient sweep (per-node C0 and CA) adds its sums on
+    the integer pipe too: bit for bit against the C model of its order."""
+    M = gpu
+    n = (45, 33, 21)
+    shape = (n[2], n[1], n[0])
+    rng = np.random.default_rng(100 + 10 * KINDS.index(kind) + tile)
+    cp = (0.11, 0.09, 0.145)
+    u = _fields(kind, shape, rng)
+    c0f = rng.uniform(0.3, 0.5, shape)
+    caf = rng.uniform(0.6, 1.2, shape)
+    cfg = M.make_cfg(n, tau=1e-3, precision="f64", c0=1.0, cp=cp, cf=1.0, tile=tile)
+    with M.Plain(cfg) as p:
+        p.upload(M.FIELD_C0, c0f)
+        p.upload(M.FIELD_CA, caf)
+        p.upload(M.FIELD_U, u)
+        for _ in range(3):
+            p.step(1)
+            got = p.download()
+            want = _model_vc_step(star_model, u, c0f, caf, cp)
+            assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), kind
+            u = got
