@@ -665,7 +665,7 @@ extern "C" int scafes_batch_step_looped(scafes_batch* b, int n_steps) {
             Star7Launch a;
             a.precision = b->precision;
             a.border = SCAFES_BORDER_DIRICHLET;
-            a.tile = star7_default_tile(I.L);
+            a.tile = star7_default_tile(I.L, b->precision);
             a.L = I.L;
             a.tm_uo = &b->hmaps[((size_t)i * 3 + b->cur) * STAR7_NUM_TILES + a.tile];
             a.tm_f = &b->hmaps[((size_t)i * 3 + 2) * STAR7_NUM_TILES + a.tile];

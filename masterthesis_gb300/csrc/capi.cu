@@ -222,7 +222,7 @@ extern "C" int scafes_gpu_create(const scafes_cfg* cfg, scafes_handle** out) {
         if ((e = cudaMemsetAsync(h->u[i], 0, bytes, h->stream)) != cudaSuccess)
             return bail(SCAFES_ERR_CUDA, "cudaMemset(u)", e);
     }
-    h->tile = cfg->tile > 0 ? cfg->tile - 1 : star7_default_tile(h->L);
+    h->tile = cfg->tile > 0 ? cfg->tile - 1 : star7_default_tile(h->L, cfg->precision);
     if ((e = cudaMalloc(&h->status, sizeof(int))) != cudaSuccess)
         return bail(SCAFES_ERR_NOMEM, "cudaMalloc(status)", e);
     if ((e = cudaMemsetAsync(h->status, 0, sizeof(int), h->stream)) != cudaSuccess)

@@ -58,8 +58,9 @@ __host__ __device__ inline Split negated(const Split& s) {
 int star7_box_width(int precision);
 // Height (rows) of the TMA box of tile variant `tile`.
 int star7_box_height(int tile);
-// Tile variant used when none is chosen: {32,4} on large grids, {8,1} else.
-int star7_default_tile(const Layout& L);
+// Tile variant used when none is chosen: {8,1} for FP64; otherwise {32,4}
+// on large grids and {8,1} else.
+int star7_default_tile(const Layout& L, int precision);
 
 // Device block of a SCAFES_BORDER_TABLE problem: the rule of each border
 // class and the border field's higher time orders and time variable

@@ -39,8 +39,11 @@ int star7_box_height(int tile) {
     return kTiles[tile].by + 2;
 }
 
-int star7_default_tile(const Layout& L) {
-    // Four rows per thread once the grid has enough tiles to fill the GPU.
+int star7_default_tile(const Layout& L, int precision) {
+    // FP64: one row per thread (the integer-pipe sums want resident warps,
+    // not registers; the autotuner's choice at every size measured).  Else
+    // four rows per thread once the grid has enough tiles to fill the GPU.
+    if (precision == SCAFES_PREC_F64) return 0;
     const long long cols = (long long)L.nx * L.ny;
     return cols >= 256LL * 256LL ? 2 : 0;
 }

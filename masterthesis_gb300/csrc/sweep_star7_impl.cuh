@@ -8,8 +8,23 @@
 
 namespace scafes {
 
+// Minimum resident CTAs per SM asked of the compiler: 8 for the one-row
+// FP64 tile without a source and with a Dirichlet or mirror border, whose
+// integer-pipe neighbour sums are latency-bound and gain more from 64
+// resident warps (32 registers, 32-44 bytes spilled to L1: 113.9 against
+// 110.6 GLUP/s at 512^3) than they lose to the spills.  The source and
+// table-border variants would spill 92-228 bytes: no constraint for them
+// or for any other tile.
+template <class P, int R, int SRC, int BORDER>
+constexpr int star7_min_ctas() {
+    return (R == 1 && std::is_same<P, PolF64>::value && SRC == SRC_NONE &&
+            (BORDER == SCAFES_BORDER_DIRICHLET || BORDER == SCAFES_BORDER_MIRROR_POW2))
+               ? 8
+               : 0;
+}
+
 template <class P, int SRC, int BORDER, int BY, int R, int NS, bool FS, bool ML>
-__global__ void __launch_bounds__(BX * (BY / R))
+__global__ void __launch_bounds__(BX * (BY / R), star7_min_ctas<P, R, SRC, BORDER>())
 star7_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmf,
           typename P::T* __restrict__ un,
           const typename P::T* __restrict__ fa, const typename P::T* __restrict__ fb,
