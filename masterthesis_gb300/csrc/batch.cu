@@ -117,12 +117,19 @@ batch_star7(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ 
     batch_loop<P, BY, R, NS>(inst, maps, map_stride, items, n_items, pool, cur, counter, status);
 }
 
-// FP64 variant with a register cap of 64 (1024 threads' worth of CTAs per
-// SM): the FP64 pipe needs every resident warp it can get, and the cap
-// costs these kernels no spills.  The FP32 policies keep the compiler's
-// choice (a cap spills the pair kernels' row pairs and measured slower).
+// FP64 variant with a register cap: resident warps hide the latency of
+// the FP64 pipe and of the integer-pipe neighbour sums.  One row per
+// thread: 6 CTAs (40 registers); two rows: 1024 threads' worth of CTAs (64
+// registers, 72 bytes spilled); four rows: no cap (a 64-register cap would
+// spill the four rows' integer sums, 1.8 KB).  The FP32 policies keep the
+// compiler's choice (a cap spills the pair kernels' row pairs and measured
+// slower).
+template <int R>
+constexpr int batch_f64_min_ctas(int threads) {
+    return R == 1 ? 1536 / threads : (R >= 4 ? 0 : 1024 / threads);
+}
 template <int BY, int R, int NS>
-__global__ void __launch_bounds__(BX * (BY / R), 1024 / (BX * (BY / R)))
+__global__ void __launch_bounds__(BX * (BY / R), batch_f64_min_ctas<R>(BX * (BY / R)))
 batch_star7_f64(const BatchInst* __restrict__ inst, const CUtensorMap* __restrict__ maps, int map_stride,
                 const BatchItem* __restrict__ items, int n_items, double* __restrict__ pool, int cur,
                 int* __restrict__ counter, int* __restrict__ status) {
