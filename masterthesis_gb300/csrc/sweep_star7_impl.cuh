@@ -102,8 +102,16 @@ static __global__ void k_xface_node_rules(const T* __restrict__ uo, T* __restric
 // The variable-coefficient sweep: as star7_tma, with the coefficient fields
 // C0 and CA staged by TMA with every plane (and F_A with them when the
 // source is present), and the Dirichlet, table or per-node border.
+// The variable-coefficient one-row FP64 tile asks for 6 CTAs per SM (40
+// registers, up to 12 bytes spilled): 89.5 against 85.8 GLUP/s on the
+// 512^3 tissue workload (5 CTAs: 85.8).
+template <class P, int R>
+constexpr int star7_vc_min_ctas() {
+    return (R == 1 && std::is_same<P, PolF64>::value) ? 6 : 0;
+}
+
 template <class P, int SRC, int BORDER, int BY, int R, int NS>
-__global__ void __launch_bounds__(BX * (BY / R))
+__global__ void __launch_bounds__(BX * (BY / R), star7_vc_min_ctas<P, R>())
 star7_vc_tma(const __grid_constant__ CUtensorMap tm, const __grid_constant__ CUtensorMap tmf,
              const __grid_constant__ CUtensorMap tmc0, const __grid_constant__ CUtensorMap tmca,
              typename P::T* __restrict__ un, const typename P::T* __restrict__ fa,
