@@ -232,3 +232,24 @@ def test_f64_variable_coefficient_sweep_bitwise_equals_model(gpu, star_model, ki
             want = _model_vc_step(star_model, u, c0f, caf, cp)
             assert np.array_equal(got.view(np.uint64), want.view(np.uint64)), kind
             u = got
+
+
+@pytest.mark.gpu
+def test_f64_sweep_bitwise_at_full_size(gpu, star_model):
+    """The benchmark's 512^3 field (sine mode plus noise, Dirichlet 0), two
+    sweeps with the default tile, each bit for bit against the C model."""
+    from masterthesis_gb300.workloads import heat_sine_noise, heat_tau
+    M = gpu
+    n = (512, 512, 512)
+    tau = heat_tau(n)
+    cp = tuple(tau * (m - 1) ** 2 for m in n)  # tau / h^2 per axis on the unit cube
+    c0 = 1.0 - 2.0 * sum(cp)
+    u = heat_sine_noise(n)
+    with M.Plain(M.make_cfg(n, tau=tau, precision="f64", c0=c0, cp=cp)) as p:
+        p.upload(M.FIELD_U, u)
+        for _ in range(2):
+            p.step(1)
+            got = p.download()
+            want = _model_step(star_model, u, (c0,) + cp)
+            assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+            u = got
