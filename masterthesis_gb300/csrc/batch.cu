@@ -638,8 +638,11 @@ extern "C" int scafes_batch_step(scafes_batch* b, int n_steps) {
         int rc2 = SCAFES_OK;
         cudaError_t e = cudaMemsetAsync(b->counters, 0, sizeof(int) * (size_t)n_steps, b->stream);
         if (e == cudaSuccess && pairs > 0) rc2 = enqueue_tb(b, b->cur, pairs);
+        // Each depth-2 pass writes the other iterate: after `pairs` passes
+        // the field is in cur ^ (pairs & 1).
+        const int after_pairs = b->cur ^ (pairs & 1);
         for (int s = 0; s < singles && e == cudaSuccess && rc2 == SCAFES_OK; ++s)
-            rc2 = enqueue_step(b, b->cur ^ ((2 * pairs + s) & 1), b->counters + s);
+            rc2 = enqueue_step(b, after_pairs ^ (s & 1), b->counters + s);
         cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
         if (e != cudaSuccess || rc2 != SCAFES_OK || e2 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -654,7 +657,7 @@ extern "C" int scafes_batch_step(scafes_batch* b, int n_steps) {
     BTRY(b, cudaEventRecord(b->ev0, b->stream));
     BTRY(b, cudaGraphLaunch(it->second, b->stream));
     BTRY(b, cudaEventRecord(b->ev1, b->stream));
-    b->cur ^= (n_steps & 1);
+    b->cur ^= (pairs + singles) & 1;  // one iterate swap per pass and per single step
     b->t += n_steps;
     b->launches = pairs * (int)b->hinst.size() + singles;
     b->timed = true;

@@ -139,6 +139,27 @@ def test_batch_depth2_equals_looped(gpu, prec):
             b.set_temporal_depth(3)
 
 
+@pytest.mark.parametrize("prec", ["f64", "f32x2"])
+def test_batch_depth2_odd_pass_counts(gpu, prec):
+    """Depth 2 over calls with an odd number of passes (step(10) = 5 passes,
+    then step(2) = 1, then step(3) = 1 pass and a single step), each graph
+    captured and replayed with both iterate parities: bit for bit the
+    looped single-step results, on the small instances (3 and 4 nodes on
+    an axis) of the graph-replay test."""
+    M = gpu
+    specs = small_ensemble(n_inst=5, seed=5)
+    seq = [10, 2, 3, 10, 10]
+    with make_batch(M, specs, prec) as ref:
+        ref.step_looped(sum(seq))
+        want = [ref.download(i) for i in range(len(specs))]
+    with make_batch(M, specs, prec) as b:
+        b.set_temporal_depth(2)
+        for t in seq:
+            b.step(t)
+        for i in range(len(specs)):
+            assert np.array_equal(b.download(i), want[i]), i
+
+
 def test_batch_graph_replay_and_autotune(gpu):
     M = gpu
     specs = small_ensemble(n_inst=5, seed=5)
