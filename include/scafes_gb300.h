@@ -180,8 +180,10 @@ typedef struct scafes_cfg {
                                 the mirror border takes 1 only */
     int precision;           /* enum scafes_precision */
     int border;              /* enum scafes_border */
-    int tile;                /* sweep tile variant 1..4, 0 = default
-                                (see scafes_gpu_autotune) */
+    int tile;                /* sweep tile variant 1..4 (see
+                                scafes_gpu_autotune), 0 = default: 1 for
+                                FP64, else 3 on grids of at least 256 x 256
+                                columns and 1 below */
     double c0;               /* centre coefficient */
     double cp[3];            /* pair coefficient per axis */
     double cf;               /* source coefficient (0 disables F) */
